@@ -1,0 +1,436 @@
+"""CPU oracle for the symmetric-BEM forward path -- TEST INFRASTRUCTURE ONLY.
+
+This module is the parity checker and the CPU baseline ("port").  Only
+``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs use it; the
+product (``openmeeg_gb300``) never imports it.
+
+It restates, in Python, OpenMEEG's geometry bookkeeping for meshes given as
+interfaces (``.geom`` v1.1 with one mesh per interface):
+
+* interface orientation from the solid angle at the bounding-box centre
+  (``OpenMEEG/src/interface.cpp:55-95``),
+* domain/mesh orientation (``OpenMEEG/include/domain.h:43-45,95-101``),
+* current barriers, outermost meshes and isolated parts
+  (``OpenMEEG/src/geometry.cpp:424-536``, ``include/geometry.h:228-249``),
+* unknown numbering (``OpenMEEG/src/geometry.cpp:256-295``),
+* mesh pairs and S/N/D coefficients (``OpenMEEG/src/geometry.cpp:405-420``,
+  ``OpenMEEG/src/assembleHeadMat.cpp:92-95``),
+* dipole domain lookup (``OpenMEEG/src/geometry.cpp:146-154``,
+  ``OpenMEEG/src/domain.cpp:12-17``, ``OpenMEEG/src/interface.cpp:18-35``),
+
+and drives the C restatement of the numerical kernels in ``om_oracle.c``.
+The dense solve uses LAPACK's symmetric-indefinite (Bunch-Kaufman) solver via
+scipy, the same family as the reference's DSPTRF/DSPTRS
+(``OpenMEEGMaths/src/symmatrix.cpp:133-152``).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libomoracle.so")
+K = 1.0 / (4.0 * math.pi)
+
+
+def build(force: bool = False) -> str:
+    """Compile om_oracle.c (gcc, OpenMP) into oracle/_build/."""
+    src = os.path.join(HERE, "om_oracle.c")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB_PATH + f".{os.getpid()}.tmp"
+    subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        _lib.oo_num_threads.restype = ctypes.c_int
+    return _lib
+
+
+class _Geom(ctypes.Structure):
+    _fields_ = [
+        ("nv", ctypes.c_int64), ("V", ctypes.c_void_p), ("nt", ctypes.c_int64), ("T", ctypes.c_void_p),
+        ("nmesh", ctypes.c_int), ("mesh_vbeg", ctypes.c_void_p), ("mesh_tbeg", ctypes.c_void_p),
+        ("vidx", ctypes.c_void_p), ("tidx", ctypes.c_void_p), ("barrier", ctypes.c_void_p),
+        ("npairs", ctypes.c_int), ("pairs", ctypes.c_void_p), ("coefs", ctypes.c_void_p),
+        ("nparts", ctypes.c_int), ("part_beg", ctypes.c_void_p), ("part_meshes", ctypes.c_void_p),
+        ("N", ctypes.c_int64),
+    ]
+
+
+class _Integ(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("levels", ctypes.c_int), ("tol", ctypes.c_double)]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _tri_solid_angles(V, T, p):
+    """Triangle::solid_angle summed over a mesh (triangle.h:123-136)."""
+    r0, r1, r2 = V[T[:, 0]] - p, V[T[:, 1]] - p, V[T[:, 2]] - p
+    d0, d1, d2 = (np.linalg.norm(r, axis=1) for r in (r0, r1, r2))
+    nn = np.cross(V[T[:, 1]] - V[T[:, 0]], V[T[:, 2]] - V[T[:, 0]])
+    nrm = np.linalg.norm(nn, axis=1)
+    area = 0.5 * nrm
+    n = nn / nrm[:, None]
+    d = 2 * area * np.einsum("ij,ij->i", r0, n)
+    den = d0 * d1 * d2 + d0 * np.einsum("ij,ij->i", r1, r2) + d1 * np.einsum("ij,ij->i", r2, r0) + \
+        d2 * np.einsum("ij,ij->i", r0, r1)
+    s = np.where(np.abs(d) < 1e-10, 0.0, 2 * np.arctan2(d, den))
+    return float(np.sum(s))
+
+
+def _almost_equal(x, y, eps=1e3):
+    # om_common.h:24-26
+    return abs(x - y) < np.finfo(float).eps * abs(x + y) * eps or abs(x - y) < np.finfo(float).tiny
+
+
+@dataclass
+class OracleGeometry:
+    """Digested geometry: flat arrays plus the domain bookkeeping."""
+    V: np.ndarray
+    T: np.ndarray
+    mesh_vbeg: np.ndarray
+    mesh_tbeg: np.ndarray
+    vidx: np.ndarray
+    tidx: np.ndarray
+    barrier: np.ndarray
+    pairs: np.ndarray
+    coefs: np.ndarray
+    part_beg: np.ndarray
+    part_meshes: np.ndarray
+    N: int
+    orient: np.ndarray          # per mesh (interface) orientation +-1
+    domains: list               # (name, [(mesh, inside)], sigma)
+    outermost: np.ndarray
+
+    @property
+    def nmesh(self):
+        return len(self.mesh_tbeg) - 1
+
+    def c_struct(self):
+        g = _Geom()
+        self._keep = [self.V, self.T, self.mesh_vbeg, self.mesh_tbeg, self.vidx, self.tidx, self.barrier,
+                      self.pairs, self.coefs, self.part_beg, self.part_meshes]
+        g.nv = self.V.shape[0]; g.V = _ptr(self.V); g.nt = self.T.shape[0]; g.T = _ptr(self.T)
+        g.nmesh = self.nmesh; g.mesh_vbeg = _ptr(self.mesh_vbeg); g.mesh_tbeg = _ptr(self.mesh_tbeg)
+        g.vidx = _ptr(self.vidx); g.tidx = _ptr(self.tidx); g.barrier = _ptr(self.barrier)
+        g.npairs = self.pairs.shape[0]; g.pairs = _ptr(self.pairs); g.coefs = _ptr(self.coefs)
+        g.nparts = len(self.part_beg) - 1; g.part_beg = _ptr(self.part_beg); g.part_meshes = _ptr(self.part_meshes)
+        g.N = self.N
+        return g
+
+    # --- domain helpers -------------------------------------------------
+    def mesh_orientation(self, d, m):
+        for (mm, inside) in self.domains[d][1]:
+            if mm == m:
+                return int(self.orient[m]) if inside else -int(self.orient[m])
+        return 0
+
+    def domains_of(self, m):
+        return [d for d in range(len(self.domains)) if self.mesh_orientation(d, m) != 0]
+
+    def conductivity_jump(self, m):
+        # geometry.h:188-194
+        return sum(self.domains[d][2] * self.mesh_orientation(d, m) for d in self.domains_of(m))
+
+    def interface_contains(self, m, p, sa=None):
+        s = self.orient[m] * (sa if sa is not None else _tri_solid_angles(
+            self.V, self.T[self.mesh_tbeg[m]:self.mesh_tbeg[m + 1]], p))
+        if _almost_equal(s, -4 * math.pi):
+            return True
+        if _almost_equal(s, 0.0):
+            return False
+        if _almost_equal(s, 4 * math.pi):
+            return True
+        return abs(s) > 2 * math.pi
+
+    def domain_of_point(self, p, sas=None):
+        for d, (_, bounds, _) in enumerate(self.domains):
+            if all(self.interface_contains(m, p, None if sas is None else sas[m]) == inside
+                   for (m, inside) in bounds):
+                return d
+        raise ValueError("point in no domain")
+
+    def eeg_meshes(self):
+        out = []
+        for (_, bounds, sigma) in self.domains:
+            if sigma == 0.0:
+                out += [m for (m, _) in bounds]
+        return out
+
+
+def digest(head) -> OracleGeometry:
+    """Restate Geometry::finalize for a NestedHead-like object (vertices,
+    triangles lists and .geom-style domains)."""
+    nmesh = len(head.vertices)
+    V = np.ascontiguousarray(np.vstack(head.vertices), dtype=np.float64)
+    vbeg = np.zeros(nmesh + 1, np.int64)
+    tbeg = np.zeros(nmesh + 1, np.int64)
+    Ts = []
+    for m in range(nmesh):
+        vbeg[m + 1] = vbeg[m] + head.vertices[m].shape[0]
+        tbeg[m + 1] = tbeg[m] + head.triangles[m].shape[0]
+        Ts.append(np.asarray(head.triangles[m], np.int64) + vbeg[m])
+    T = np.ascontiguousarray(np.vstack(Ts), dtype=np.int64)
+
+    # interface orientation (interface.cpp:55-95): one mesh per interface
+    orient = np.ones(nmesh, np.int64)
+    for m in range(nmesh):
+        vv = head.vertices[m]
+        center = 0.5 * (vv.min(axis=0) + vv.max(axis=0))
+        s = _tri_solid_angles(V, T[tbeg[m]:tbeg[m + 1]], center)
+        if _almost_equal(s, 4 * math.pi):
+            orient[m] = -1
+            s = -s
+        if not (_almost_equal(s, 0.0) or _almost_equal(s, -4 * math.pi)):
+            raise ValueError(f"interface {m} is not closed (solid angle {s / math.pi} pi)")
+
+    domains = []
+    for (name, bounds, sigma) in head.domains:
+        # GeomFile.h:289-291: a leading '-' means "inside"
+        domains.append((name, [(abs(b) - 1, b < 0) for b in bounds], float(sigma)))
+    g = OracleGeometry(V, T, vbeg, tbeg, None, None, None, None, None, None, None, 0, orient, domains, None)
+
+    # mark_current_barriers (geometry.cpp:424-536)
+    barrier = np.zeros(nmesh, np.int32)
+    isolated = np.zeros(nmesh, bool)
+    outermost = np.zeros(nmesh, bool)
+    for (_, bounds, sigma) in domains:
+        if _almost_equal(sigma, 0.0):
+            for (m, _) in bounds:
+                if barrier[m]:
+                    isolated[m] = True
+                    outermost[m] = False
+                barrier[m] = 1
+    for (_, bounds, sigma) in domains:
+        if _almost_equal(sigma, 0.0):
+            for (m, inside) in bounds:
+                if not inside and barrier[m] and not isolated[m]:
+                    outermost[m] = True
+    # connectivity of meshes through common domains -> independent parts
+    cand = list(range(nmesh))
+    parts = []
+    while cand:
+        c = cand.pop(0)
+        conn, pend = [c], [c]
+        while pend:
+            cur = pend.pop(0)
+            keep = []
+            for it in cand:
+                if set(g.domains_of(cur)) & set(g.domains_of(it)):
+                    conn.append(it)
+                    pend.append(it)
+                else:
+                    keep.append(it)
+            cand = keep
+        if len(conn) > 1 or not isolated[conn[0]]:
+            parts.append(conn)
+    # outermost domain = the one with no inside boundary (geometry.cpp:23-41)
+    for (_, bounds, _) in domains:
+        if all(not inside for (_, inside) in bounds):
+            for (m, _) in bounds:
+                outermost[m] = True
+            break
+    if isolated.any():
+        raise NotImplementedError("isolated meshes are outside this oracle's scope")
+
+    # generate_indices (geometry.cpp:256-295)
+    nv = V.shape[0]
+    vidx = np.arange(nv, dtype=np.int64)
+    idx = nv
+    tidx = np.full(T.shape[0], -1, np.int64)
+    for m in range(nmesh):
+        if not barrier[m]:
+            tidx[tbeg[m]:tbeg[m + 1]] = np.arange(idx, idx + tbeg[m + 1] - tbeg[m])
+            idx += tbeg[m + 1] - tbeg[m]
+    nbarrier_tri = 0
+    for m in range(nmesh):
+        if barrier[m]:
+            nbarrier_tri += tbeg[m + 1] - tbeg[m]
+            tidx[tbeg[m]:tbeg[m + 1]] = np.arange(idx, idx + tbeg[m + 1] - tbeg[m])
+            idx += tbeg[m + 1] - tbeg[m]
+    N = int(idx - nbarrier_tri)
+
+    # make_mesh_pairs (geometry.cpp:405-420) + coefficients (assembleHeadMat.cpp:92-95)
+    pairs, coefs = [], []
+    for m1 in range(nmesh):
+        for m2 in range(m1 + 1):
+            common = sorted(set(g.domains_of(m1)) & set(g.domains_of(m2)))
+            if m1 == m2:
+                orientation = 1
+            else:
+                orientation = 0 if not common else (
+                    1 if g.mesh_orientation(common[0], m1) == g.mesh_orientation(common[0], m2) else -1)
+            sig = sum(domains[d][2] for d in common)
+            if sig != 0.0 and orientation != 0:
+                with np.errstate(divide="ignore"):
+                    sinv = sum((1.0 / domains[d][2]) if domains[d][2] != 0 else np.inf for d in common)
+                factor = orientation * K
+                pairs.append((m1, m2))
+                coefs.append((factor * sinv, factor * sig, -factor * len(common)))
+    part_meshes, part_beg = [], [0]
+    for part in parts:
+        part_meshes += [m for m in part if outermost[m]]
+        part_beg.append(len(part_meshes))
+
+    g.vidx, g.tidx, g.barrier = vidx, tidx, barrier.astype(np.int32)
+    g.pairs = np.ascontiguousarray(np.array(pairs, np.int32).reshape(-1, 2))
+    g.coefs = np.ascontiguousarray(np.array(coefs, np.float64).reshape(-1, 3))
+    g.part_beg = np.array(part_beg, np.int32)
+    g.part_meshes = np.array(part_meshes, np.int32)
+    g.N = N
+    g.outermost = outermost
+    return g
+
+
+# ---------------------------------------------------------------------------
+# Numerical entry points
+# ---------------------------------------------------------------------------
+
+def _integ(order=3, levels=0, tol=0.005):
+    return _Integ(order, levels, tol)
+
+
+def packed_to_dense(p: np.ndarray, n: int) -> np.ndarray:
+    """Packed upper (i + j(j+1)/2) -> dense symmetric."""
+    M = np.zeros((n, n))
+    iu = np.triu_indices(n)
+    # index of (i,j), i<=j, in packed storage
+    M[iu] = p[iu[0] + iu[1] * (iu[1] + 1) // 2]
+    return M + np.triu(M, 1).T
+
+
+def headmat_packed(g: OracleGeometry, order=3, levels=0, tol=0.005) -> np.ndarray:
+    out = np.zeros(g.N * (g.N + 1) // 2)
+    gs = g.c_struct()
+    it = _integ(order, levels, tol)
+    lib().oo_headmat(ctypes.byref(gs), ctypes.byref(it), _ptr(out))
+    return out
+
+
+def headmat(g: OracleGeometry, **kw) -> np.ndarray:
+    return packed_to_dense(headmat_packed(g, **kw), g.N)
+
+
+def mesh_solid_angles(g: OracleGeometry, pts: np.ndarray) -> np.ndarray:
+    pts = np.ascontiguousarray(pts, np.float64)
+    out = np.zeros((pts.shape[0], g.nmesh))
+    gs = g.c_struct()
+    lib().oo_mesh_solid_angles(ctypes.byref(gs), _ptr(pts), ctypes.c_int64(pts.shape[0]), _ptr(out))
+    return out
+
+
+def dipole_domains(g: OracleGeometry, dipoles: np.ndarray):
+    """Per dipole: the boundary meshes of its domain, their coeffD and the
+    domain conductivity (assembleSourceMat.cpp:79-98)."""
+    sas = mesh_solid_angles(g, dipoles[:, :3])
+    n = dipoles.shape[0]
+    maxb = max(len(b) for (_, b, _) in g.domains)
+    nb = np.zeros(n, np.int32)
+    mesh = np.zeros((n, maxb), np.int32)
+    coeff = np.zeros((n, maxb))
+    cond = np.zeros(n)
+    for i in range(n):
+        d = g.domain_of_point(dipoles[i, :3], sas[i])
+        name, bounds, sigma = g.domains[d]
+        cond[i] = sigma
+        k = 0
+        for (m, inside) in bounds:
+            factorD = -K if inside else K
+            mesh[i, k] = m
+            coeff[i, k] = factorD * g.orient[m]
+            k += 1
+        nb[i] = k
+    return nb, mesh, coeff, cond, maxb
+
+
+def dsm(g: OracleGeometry, dipoles: np.ndarray, order=3, levels=10, tol=0.001) -> np.ndarray:
+    dipoles = np.ascontiguousarray(dipoles, np.float64)
+    nb, mesh, coeff, cond, maxb = dipole_domains(g, dipoles)
+    n = dipoles.shape[0]
+    out = np.zeros((n, g.N))  # column-major N x n
+    gs = g.c_struct()
+    it = _integ(order, levels, tol)
+    lib().oo_dsm(ctypes.byref(gs), _ptr(dipoles), ctypes.c_int64(n), _ptr(nb), _ptr(np.ascontiguousarray(mesh)),
+                 _ptr(np.ascontiguousarray(coeff)), _ptr(cond), ctypes.c_int(maxb), ctypes.byref(it), _ptr(out))
+    return out.T.copy()
+
+
+def h2em(g: OracleGeometry, electrodes: np.ndarray) -> np.ndarray:
+    """Dense n_e x N Head2EEGMat (the reference stores it sparse)."""
+    pos = np.ascontiguousarray(electrodes[:, :3], np.float64)
+    meshes = np.array(g.eeg_meshes(), np.int32)
+    ne = pos.shape[0]
+    tri = np.zeros(ne, np.int64)
+    w = np.zeros((ne, 3))
+    gs = g.c_struct()
+    lib().oo_h2em(ctypes.byref(gs), _ptr(pos), ctypes.c_int64(ne), ctypes.c_int(len(meshes)), _ptr(meshes),
+                  _ptr(tri), _ptr(w))
+    M = np.zeros((ne, g.N))
+    for i in range(ne):
+        for j in range(3):
+            M[i, g.vidx[g.T[tri[i], j]]] = w[i, j]
+    return M
+
+
+def h2mm(g: OracleGeometry, squids: np.ndarray) -> np.ndarray:
+    """n_s x N Head2MEGMat for point sensors with unit weights."""
+    pos = np.ascontiguousarray(squids[:, :3], np.float64)
+    ori = np.ascontiguousarray(squids[:, 3:6], np.float64)
+    jump = np.array([g.conductivity_jump(m) for m in range(g.nmesh)], np.float64)
+    n = pos.shape[0]
+    out = np.zeros((g.N, n))
+    gs = g.c_struct()
+    lib().oo_h2mm(ctypes.byref(gs), _ptr(pos), _ptr(ori), ctypes.c_int64(n), _ptr(jump), _ptr(out))
+    return out.T.copy()
+
+
+def ds2mm(dipoles: np.ndarray, squids: np.ndarray) -> np.ndarray:
+    dip = np.ascontiguousarray(dipoles, np.float64)
+    pos = np.ascontiguousarray(squids[:, :3], np.float64)
+    ori = np.ascontiguousarray(squids[:, 3:6], np.float64)
+    out = np.zeros((dip.shape[0], pos.shape[0]))
+    lib().oo_ds2mm(_ptr(dip), ctypes.c_int64(dip.shape[0]), _ptr(pos), _ptr(ori), ctypes.c_int64(pos.shape[0]),
+                   _ptr(out))
+    return out.T.copy()
+
+
+def solve_adjoint(HM: np.ndarray, rhs_rows: np.ndarray) -> np.ndarray:
+    """HM^-1 applied to the rows of `rhs_rows` (linsolve, gain.h:52-57),
+    symmetric-indefinite LAPACK solve.  Returns (k x N)."""
+    import scipy.linalg as sla
+    return sla.solve(HM, rhs_rows.T, assume_a="sym").T
+
+
+def gain_eeg(HM, DSM, H2EM):
+    """GainEEGadjoint semantics (gain.h:78-89): (HM^-1 H2EM^T)^T DSM."""
+    return solve_adjoint(HM, H2EM) @ DSM
+
+
+def gain_meg(HM, DSM, H2MM, DS2MM):
+    return solve_adjoint(HM, H2MM) @ DSM + DS2MM
+
+
+def set_threads(n: int):
+    lib().oo_set_num_threads(ctypes.c_int(n))
+
+
+def num_threads() -> int:
+    return int(lib().oo_num_threads())
