@@ -1,0 +1,176 @@
+/*
+ * openmeeg_gb300.h -- C ABI of the GB300 symmetric-BEM forward path.
+ *
+ * Drop-in for OpenMEEG's forward path (HeadMat, DipSourceMat, Head2EEGMat,
+ * Head2MEGMat, DipSource2MEGMat and the Gain* products).  Every entry point is
+ * plain C: opaque handles, plain pointers, 64-bit sizes, an int status.
+ *
+ * Conventions
+ *  - Return value: OMG_OK (0) or a negative OMG_ERR_* code; omg_last_error()
+ *    gives a message for the calling thread.
+ *  - Matrices are column-major float64, leading dimension = row count unless
+ *    an `ld` argument says otherwise.
+ *  - Unknowns follow the reference numbering (OpenMEEG/src/geometry.cpp:256-295):
+ *    all vertices first, then the triangles of each mesh that is not a
+ *    current barrier.
+ *  - Functions named *_dev take device pointers (memory of the context's
+ *    device); functions named *_host take host pointers and perform the
+ *    host<->device copies themselves.
+ *  - All work is queued on the context's stream; *_host functions and
+ *    omg_context_synchronize() wait for it.
+ */
+#ifndef OPENMEEG_GB300_H
+#define OPENMEEG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OMG_OK                    0
+#define OMG_ERR_INVALID          -1  /* bad argument or geometry (OMExceptions.H BadData/BadDomain...) */
+#define OMG_ERR_CUDA             -2  /* CUDA runtime error */
+#define OMG_ERR_NOT_DEFINITE     -3  /* HeadMat is not quasi-definite: factorization pivot of wrong sign */
+#define OMG_ERR_NOT_CONVERGED    -4  /* iterative refinement did not reach its tolerance */
+#define OMG_ERR_NOMEM            -5  /* device allocation failed */
+#define OMG_ERR_IO               -6  /* file could not be read or parsed */
+#define OMG_ERR_UNSUPPORTED      -7  /* valid request outside this build's scope */
+#define OMG_ERR_TIMEOUT          -8  /* a bounded device-side wait gave up */
+
+#define OMG_PREC_FP64             0  /* all-FP64 drop-in */
+#define OMG_PREC_MIXED            1  /* FP32 far field + FP32 factorization + FP64-residual refinement */
+
+typedef struct omg_context_s*  omg_context;
+typedef struct omg_geometry_s* omg_geometry;
+typedef struct omg_solver_s*   omg_solver;
+
+/* Integrator(order, levels, tol) (OpenMEEG/include/integrator.h:192-196):
+ * order 0..3 selects the 3/6/7/16-point Gauss rule, levels > 0 enables the
+ * adaptive 4-way subdivision with relative tolerance tol. */
+typedef struct {
+    int32_t order;
+    int32_t levels;
+    double  tol;
+} omg_integrator;
+
+typedef struct {
+    int64_t n_vertices;          /* all meshes */
+    int64_t n_triangles;         /* all meshes */
+    int64_t n_unknowns;          /* HeadMat dimension (nb_parameters - nb_current_barrier_triangles) */
+    int64_t n_triangle_unknowns; /* unknowns carried by triangles */
+    int32_t n_meshes;
+    int32_t n_domains;
+    int32_t n_mesh_pairs;        /* communicating mesh pairs (geometry.cpp:405-420) */
+    int32_t nested;              /* 1 when every mesh bounds at most two domains */
+} omg_geometry_info;
+
+/* Per-call statistics of omg_gain_* (times in milliseconds, device clocks). */
+typedef struct {
+    double t_total_ms;
+    double t_headmat_ms;
+    double t_sources_ms;         /* DSM + H2EM + H2MM + DS2MM */
+    double t_factor_ms;
+    double t_solve_ms;           /* solves + refinement + gain GEMM */
+    int32_t refinement_steps;    /* mixed precision only */
+    int32_t gmres_iterations;    /* mixed precision only */
+    double  final_residual;      /* max over RHS of ||b - HM x|| / ||b|| (mixed precision) */
+    int64_t device_bytes;        /* peak device workspace of the call */
+} omg_gain_stats;
+
+/* ---- errors / context ---------------------------------------------------- */
+const char* omg_last_error(void);
+const char* omg_version(void);
+int omg_context_create(int device, omg_context* out);
+int omg_context_destroy(omg_context ctx);
+/* Use an external CUDA stream (cudaStream_t passed as void*); NULL restores
+ * the context's own stream. */
+int omg_context_set_stream(omg_context ctx, void* stream);
+int omg_context_synchronize(omg_context ctx);
+/* Number of kernels this context has launched so far. */
+int64_t omg_context_kernel_launches(omg_context ctx);
+
+/* ---- geometry ------------------------------------------------------------ *
+ * Replaces Geometry(geom, cond) + Geometry::finalize
+ * (OpenMEEG/include/geometry.h:67,211-249).  Meshes are given as interfaces
+ * (.geom v1.1, one mesh per interface); `verts` concatenates the meshes'
+ * vertices (n x 3, row-major), `tris` their triangles (local 0-based vertex
+ * indices, m x 3).  Domain d has dom_nbounds[d] boundaries listed in
+ * dom_bounds as signed 1-based mesh ids (-i: inside mesh i, +i: outside),
+ * as in the .geom "Domain" lines (GeomFile.h:265-300). */
+int omg_geometry_create(omg_context ctx, int32_t n_meshes, const int64_t* mesh_nverts, const double* verts,
+                        const int64_t* mesh_ntris, const int64_t* tris, int32_t n_domains,
+                        const int32_t* dom_nbounds, const int32_t* dom_bounds, const double* dom_sigma,
+                        omg_geometry* out);
+/* Geometry::load(geom, cond) for .geom v1.1 files whose interfaces are .tri
+ * meshes (GeomFile.h:165-300, geometry.cpp:231-252, MeshIOs/tri.h). */
+int omg_geometry_load(omg_context ctx, const char* geom_file, const char* cond_file, omg_geometry* out);
+int omg_geometry_destroy(omg_geometry geo);
+int omg_geometry_get_info(omg_geometry geo, omg_geometry_info* info);
+/* Replace the domain conductivities (same domain order); coefficients and
+ * barrier-dependent numbering must stay valid (no conductivity may change
+ * to or from zero). */
+int omg_geometry_set_conductivities(omg_geometry geo, const double* dom_sigma);
+
+/* ---- assembly (device pointers) ------------------------------------------ */
+/* HeadMat (OpenMEEG/src/assembleHeadMat.cpp:133-135): N x N symmetric, both
+ * triangles written, column-major with leading dimension ld >= N. */
+int omg_headmat_dev(omg_context ctx, omg_geometry geo, const omg_integrator* integ, int32_t precision,
+                    double* hm, int64_t ld);
+/* Same, in SymMatrix packed-upper storage (N(N+1)/2 doubles, i + j(j+1)/2). */
+int omg_headmat_packed_dev(omg_context ctx, omg_geometry geo, const omg_integrator* integ, double* packed);
+/* SourceMatrix<Dipole> (OpenMEEG/src/assembleSourceMat.cpp:66-104):
+ * dipoles n x 6 row-major (x y z qx qy qz); out N x n.  domain = -1 looks up
+ * each dipole's domain from its position; domain >= 0 forces that domain. */
+int omg_dipsourcemat_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                         const omg_integrator* integ, int32_t domain, double* dsm);
+/* Head2EEGMat (OpenMEEG/src/assembleSensors.cpp:25-39): electrodes n x 3
+ * row-major; out n x N dense (3 nonzeros per row), plus optionally the sparse
+ * form: vertex unknown indices (n x 3) and weights (n x 3). */
+int omg_head2eegmat_dev(omg_context ctx, omg_geometry geo, const double* electrodes, int64_t n_electrodes,
+                        double* h2em, int64_t* sparse_cols, double* sparse_vals);
+/* Head2MEGMat (OpenMEEG/src/assembleSensors.cpp:69-96) for point sensors:
+ * squids n x 6 row-major (position, orientation); out n x N. */
+int omg_head2megmat_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids, double* h2mm);
+/* DipSource2MEGMat (OpenMEEG/src/assembleSensors.cpp:133-159): out n_squids x n_dipoles. */
+int omg_dipsource2megmat_dev(omg_context ctx, const double* dipoles, int64_t n_dipoles, const double* squids,
+                             int64_t n_squids, double* ds2mm);
+
+/* ---- dense solve ---------------------------------------------------------- *
+ * Replaces SymMatrix::solveLin / linsolve (OpenMEEGMaths/src/symmatrix.cpp:133-152,
+ * OpenMEEG/include/gain.h:52-57): the solver owns a factorization of HeadMat.
+ * FP64: quasi-definite L D L^T with D = diag(+1 on triangle unknowns, -1 on
+ * vertex unknowns).  Mixed: the same factorization in FP32 plus FP64-residual
+ * iterative refinement against the FP64 HeadMat. */
+int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* integ, int32_t precision,
+                      omg_solver* out);
+/* Factor a caller-provided HeadMat (dense, column-major, reference
+ * numbering, lower triangle read) -- SymMatrix::solveLin on an existing HM. */
+int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double* hm, int64_t ld,
+                                int32_t precision, omg_solver* out);
+/* In place: B (N x nrhs, leading dimension ldb) <- HeadMat^-1 B. */
+int omg_solver_solve_dev(omg_solver s, double* b, int64_t ldb, int64_t nrhs);
+int omg_solver_destroy(omg_solver s);
+
+/* ---- gain ------------------------------------------------------------------ *
+ * GainEEGadjoint / GainMEGadjoint / GainEEGMEGadjoint (OpenMEEG/include/gain.h:78-136):
+ * assemble HeadMat, factor it, solve for the sensor rows, contract with the
+ * DipSourceMat and add DipSource2MEGMat.  Any of electrodes/squids may be
+ * NULL (count 0).  gain_eeg: n_electrodes x n_dipoles; gain_meg: n_squids x
+ * n_dipoles.  `hm_integ` / `dsm_integ` may be NULL for the reference
+ * defaults (3,0,0.005) and (3,10,0.001). */
+int omg_gain_dev(omg_context ctx, omg_geometry geo, int32_t precision, const omg_integrator* hm_integ,
+                 const omg_integrator* dsm_integ, const double* dipoles, int64_t n_dipoles,
+                 const double* electrodes, int64_t n_electrodes, const double* squids, int64_t n_squids,
+                 double* gain_eeg, double* gain_meg, omg_gain_stats* stats);
+/* Same with host buffers (inputs copied in, gains copied out). */
+int omg_gain_host(omg_context ctx, omg_geometry geo, int32_t precision, const omg_integrator* hm_integ,
+                  const omg_integrator* dsm_integ, const double* dipoles, int64_t n_dipoles,
+                  const double* electrodes, int64_t n_electrodes, const double* squids, int64_t n_squids,
+                  double* gain_eeg, double* gain_meg, omg_gain_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENMEEG_GB300_H */

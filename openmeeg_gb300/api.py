@@ -1,0 +1,346 @@
+"""Python mirror of OpenMEEG's forward-path API on the GB300 library.
+
+Names and argument meanings follow the reference's Python module
+(``wrapping/python/openmeeg/__init__.py:15-39``, SWIG over
+``OpenMEEG/include/assemble.h``, ``assembleSourceMat.h``, ``gain.h``):
+``Geometry``, ``Integrator``, ``HeadMat``, ``DipSourceMat``, ``Head2EEGMat``,
+``Head2MEGMat``, ``DipSource2MEGMat``, ``GainEEG``, ``GainMEG``,
+``GainEEGadjoint``, ``GainMEGadjoint``, ``GainEEGMEGadjoint``.  Matrices are
+returned as float64 torch tensors on the CUDA device (``.cpu().numpy()`` gives
+the reference's numpy view); inputs may be numpy arrays or tensors.  Errors
+raise ``OMGError`` carrying the C status, where the reference raises its
+``OpenMEEG::Exception`` hierarchy.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import GainStats, GeometryInfo, Integrator, OMGError, check
+
+__all__ = ["Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
+           "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
+           "GainEEGMEGadjoint", "forward_gain", "OMGError", "kernel_launches"]
+
+FP64 = "fp64"
+MIXED = "mixed"
+
+
+def _prec(p) -> int:
+    if p in (FP64, _lib.PREC_FP64, None):
+        return _lib.PREC_FP64
+    if p in (MIXED, _lib.PREC_MIXED):
+        return _lib.PREC_MIXED
+    raise ValueError(f"unknown precision {p!r}")
+
+
+class Context:
+    """A CUDA device + stream for the library (one per device and thread)."""
+
+    _default = {}
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self.lib.omg_context_create(device, ctypes.byref(h)))
+        self.handle = h
+
+    @classmethod
+    def default(cls, device: Optional[int] = None) -> "Context":
+        if device is None:
+            device = torch.cuda.current_device() if torch.cuda.is_available() else 0
+        if device not in cls._default:
+            cls._default[device] = cls(device)
+        return cls._default[device]
+
+    def bind_current_stream(self):
+        """Queue library work on torch's current stream of this device."""
+        s = torch.cuda.current_stream(self.device)
+        check(self.lib.omg_context_set_stream(self.handle, ctypes.c_void_p(s.cuda_stream)))
+
+    def synchronize(self):
+        check(self.lib.omg_context_synchronize(self.handle))
+
+    def launches(self) -> int:
+        return int(self.lib.omg_context_kernel_launches(self.handle))
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.omg_context_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def kernel_launches(ctx: Optional[Context] = None) -> int:
+    return (ctx or Context.default()).launches()
+
+
+def _dev(ctx: Context):
+    return torch.device("cuda", ctx.device)
+
+
+def _as_dev(x, ctx: Context, cols: Optional[int] = None) -> torch.Tensor:
+    t = torch.as_tensor(np.asarray(x) if not isinstance(x, torch.Tensor) else x, dtype=torch.float64)
+    t = t.to(_dev(ctx)).contiguous()
+    if cols is not None:
+        if t.ndim != 2 or t.shape[1] < cols:
+            raise ValueError(f"expected an (n, {cols}) array")
+        if t.shape[1] != cols:
+            t = t[:, :cols].contiguous()
+    return t
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else ctypes.c_void_p(0)
+
+
+class Geometry:
+    """Geometry(geom_file, cond_file) or Geometry.from_meshes(...)
+    (OpenMEEG/include/geometry.h:67).  Meshes are interfaces of a
+    ``.geom`` v1.1 description; domains carry conductivities."""
+
+    def __init__(self, geom_file: Optional[str] = None, cond_file: Optional[str] = None, ctx: Optional[Context] = None,
+                 _handle=None):
+        self.ctx = ctx or Context.default()
+        self.lib = self.ctx.lib
+        if _handle is not None:
+            self.handle = _handle
+        else:
+            if geom_file is None or cond_file is None:
+                raise ValueError("Geometry needs a .geom and a .cond file (or use Geometry.from_meshes)")
+            h = ctypes.c_void_p()
+            check(self.lib.omg_geometry_load(self.ctx.handle, geom_file.encode(), cond_file.encode(), ctypes.byref(h)))
+            self.handle = h
+        self.domain_names = None
+
+    @classmethod
+    def from_meshes(cls, vertices: Sequence[np.ndarray], triangles: Sequence[np.ndarray], domains,
+                    ctx: Optional[Context] = None) -> "Geometry":
+        """domains: list of (name, [signed 1-based interface ids], sigma)."""
+        ctx = ctx or Context.default()
+        nv = np.array([np.asarray(v).shape[0] for v in vertices], np.int64)
+        nt = np.array([np.asarray(t).shape[0] for t in triangles], np.int64)
+        V = np.ascontiguousarray(np.vstack([np.asarray(v, np.float64) for v in vertices]))
+        T = np.ascontiguousarray(np.vstack([np.asarray(t, np.int64) for t in triangles]))
+        nb = np.array([len(d[1]) for d in domains], np.int32)
+        bounds = np.array([b for d in domains for b in d[1]], np.int32)
+        sig = np.array([float(d[2]) for d in domains], np.float64)
+        h = ctypes.c_void_p()
+        P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+        check(ctx.lib.omg_geometry_create(ctx.handle, len(vertices), P(nv, ctypes.c_int64), P(V, ctypes.c_double),
+                                          P(nt, ctypes.c_int64), P(T, ctypes.c_int64), len(domains),
+                                          P(nb, ctypes.c_int32), P(bounds, ctypes.c_int32), P(sig, ctypes.c_double),
+                                          ctypes.byref(h)))
+        g = cls(ctx=ctx, _handle=h)
+        g.domain_names = [d[0] for d in domains]
+        g._sigmas = sig
+        return g
+
+    @classmethod
+    def from_head(cls, head, ctx: Optional[Context] = None) -> "Geometry":
+        return cls.from_meshes(head.vertices, head.triangles, head.domains, ctx)
+
+    def info(self) -> GeometryInfo:
+        i = GeometryInfo()
+        check(self.lib.omg_geometry_get_info(self.handle, ctypes.byref(i)))
+        return i
+
+    def nb_parameters(self) -> int:
+        return int(self.info().n_unknowns)
+
+    @property
+    def size(self) -> int:
+        return self.nb_parameters()
+
+    def set_conductivities(self, sigmas):
+        s = np.ascontiguousarray(np.asarray(sigmas, np.float64))
+        check(self.lib.omg_geometry_set_conductivities(self.handle, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        self._sigmas = s
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.omg_geometry_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def _default(integ, order, levels, tol):
+    return integ if integ is not None else Integrator(order, levels, tol)
+
+
+def HeadMat(geom: Geometry, integrator: Optional[Integrator] = None, precision=FP64) -> torch.Tensor:
+    """HeadMat(geo, Integrator(3,0,0.005)) (assembleHeadMat.cpp:133-135): dense N x N (both halves)."""
+    ctx = geom.ctx
+    N = geom.size
+    out = torch.empty((N, N), dtype=torch.float64, device=_dev(ctx))
+    it = _default(integrator, 3, 0, 0.005)
+    check(ctx.lib.omg_headmat_dev(ctx.handle, geom.handle, ctypes.byref(it), _prec(precision), _ptr(out), N))
+    return out   # symmetric: column-major == row-major
+
+
+def HeadMatPacked(geom: Geometry, integrator: Optional[Integrator] = None) -> torch.Tensor:
+    """HeadMat in SymMatrix packed-upper storage (what a .bin SymMatrix holds)."""
+    ctx = geom.ctx
+    N = geom.size
+    out = torch.empty(N * (N + 1) // 2, dtype=torch.float64, device=_dev(ctx))
+    it = _default(integrator, 3, 0, 0.005)
+    check(ctx.lib.omg_headmat_packed_dev(ctx.handle, geom.handle, ctypes.byref(it), _ptr(out)))
+    return out
+
+
+def DipSourceMat(geom: Geometry, dipoles, integrator: Optional[Integrator] = None, domain_name: str = "",
+                 adaptive: bool = True) -> torch.Tensor:
+    """SourceMatrix<Dipole>(geo, dipoles, Integrator(3,10,0.001), domain) (assembleSourceMat.cpp:66-104).
+    Returns N x n_dipoles.  ``adaptive=False`` is om_assemble's -DSMNA (levels 0)."""
+    ctx = geom.ctx
+    d = _as_dev(dipoles, ctx, 6)
+    n = d.shape[0]
+    N = geom.size
+    out = torch.empty((n, N), dtype=torch.float64, device=_dev(ctx))   # column-major N x n
+    it = _default(integrator, 3, 10 if adaptive else 0, 0.001)
+    dom = -1
+    if domain_name:
+        if geom.domain_names is None or domain_name not in geom.domain_names:
+            raise OMGError(-1, f"unknown domain {domain_name!r}")
+        dom = geom.domain_names.index(domain_name)
+    check(ctx.lib.omg_dipsourcemat_dev(ctx.handle, geom.handle, _ptr(d), n, ctypes.byref(it), dom, _ptr(out)))
+    return out.T
+
+
+def Head2EEGMat(geom: Geometry, electrodes, sparse: bool = False):
+    """Head2EEGMat (assembleSensors.cpp:25-39): n_e x N (3 nonzeros per row).
+    With sparse=True also returns (columns (n_e x 3), values (n_e x 3))."""
+    ctx = geom.ctx
+    e = _as_dev(electrodes, ctx, 3)
+    n = e.shape[0]
+    N = geom.size
+    out = torch.empty((N, n), dtype=torch.float64, device=_dev(ctx))   # column-major n x N
+    cols = torch.empty((n, 3), dtype=torch.int64, device=_dev(ctx))
+    vals = torch.empty((n, 3), dtype=torch.float64, device=_dev(ctx))
+    check(ctx.lib.omg_head2eegmat_dev(ctx.handle, geom.handle, _ptr(e), n, _ptr(out), _ptr(cols), _ptr(vals)))
+    return (out.T, cols, vals) if sparse else out.T
+
+
+def Head2MEGMat(geom: Geometry, squids) -> torch.Tensor:
+    """Head2MEGMat (assembleSensors.cpp:69-96) for point sensors (n x 6: position, orientation)."""
+    ctx = geom.ctx
+    s = _as_dev(squids, ctx, 6)
+    n = s.shape[0]
+    N = geom.size
+    out = torch.empty((N, n), dtype=torch.float64, device=_dev(ctx))
+    check(ctx.lib.omg_head2megmat_dev(ctx.handle, geom.handle, _ptr(s), n, _ptr(out)))
+    return out.T
+
+
+def DipSource2MEGMat(dipoles, squids, ctx: Optional[Context] = None) -> torch.Tensor:
+    """DipSource2MEGMat (assembleSensors.cpp:133-159): n_squids x n_dipoles."""
+    ctx = ctx or Context.default()
+    d = _as_dev(dipoles, ctx, 6)
+    s = _as_dev(squids, ctx, 6)
+    out = torch.empty((d.shape[0], s.shape[0]), dtype=torch.float64, device=_dev(ctx))
+    check(ctx.lib.omg_dipsource2megmat_dev(ctx.handle, _ptr(d), d.shape[0], _ptr(s), s.shape[0], _ptr(out)))
+    return out.T
+
+
+class Solver:
+    """Factorization of the HeadMat (replaces SymMatrix::solveLin / linsolve,
+    symmatrix.cpp:133-152, gain.h:52-57)."""
+
+    def __init__(self, geom: Geometry, precision=FP64, integrator: Optional[Integrator] = None, hm=None):
+        self.geom = geom
+        self.ctx = geom.ctx
+        h = ctypes.c_void_p()
+        if hm is None:
+            it = _default(integrator, 3, 0, 0.005)
+            check(self.ctx.lib.omg_solver_create(self.ctx.handle, geom.handle, ctypes.byref(it), _prec(precision),
+                                                 ctypes.byref(h)))
+        else:
+            A = _as_dev(hm, self.ctx)
+            check(self.ctx.lib.omg_solver_from_headmat_dev(self.ctx.handle, geom.handle, _ptr(A), A.shape[0],
+                                                           _prec(precision), ctypes.byref(h)))
+        self.handle = h
+
+    def solve(self, B) -> torch.Tensor:
+        """HM^-1 B for B of shape (N,) or (N, k)."""
+        b = _as_dev(B, self.ctx)
+        vec = b.ndim == 1
+        if vec:
+            b = b[:, None]
+        X = b.T.contiguous()   # column-major N x k
+        check(self.ctx.lib.omg_solver_solve_dev(self.handle, _ptr(X), b.shape[0], b.shape[1]))
+        X = X.T
+        return X[:, 0] if vec else X
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.ctx.lib.omg_solver_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def forward_gain(geom: Geometry, dipoles, electrodes=None, squids=None, precision=FP64,
+                 hm_integrator: Optional[Integrator] = None, dsm_integrator: Optional[Integrator] = None,
+                 host: bool = False):
+    """Adjoint gain pipeline (gain.h:78-136) in one call.  Returns
+    (G_eeg or None, G_meg or None, stats dict).  host=True goes through the
+    host-buffer entry point (copies included)."""
+    ctx = geom.ctx
+    dip = np.ascontiguousarray(np.asarray(dipoles, np.float64)[:, :6]) if host else _as_dev(dipoles, ctx, 6)
+    nd = dip.shape[0]
+    ne = 0 if electrodes is None else len(electrodes)
+    nm = 0 if squids is None else len(squids)
+    st = GainStats()
+    hi = _default(hm_integrator, 3, 0, 0.005)
+    di = _default(dsm_integrator, 3, 10, 0.001)
+    if host:
+        el = np.ascontiguousarray(np.asarray(electrodes, np.float64)[:, :3]) if ne else np.zeros((0, 3))
+        sq = np.ascontiguousarray(np.asarray(squids, np.float64)[:, :6]) if nm else np.zeros((0, 6))
+        ge = np.zeros((nd, ne))   # column-major ne x nd
+        gm = np.zeros((nd, nm))
+        P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        check(ctx.lib.omg_gain_host(ctx.handle, geom.handle, _prec(precision), ctypes.byref(hi), ctypes.byref(di),
+                                    P(dip), nd, P(el), ne, P(sq), nm, P(ge), P(gm), ctypes.byref(st)))
+        return (ge.T if ne else None), (gm.T if nm else None), st.as_dict()
+    el = _as_dev(electrodes, ctx, 3) if ne else None
+    sq = _as_dev(squids, ctx, 6) if nm else None
+    ge = torch.empty((nd, ne), dtype=torch.float64, device=_dev(ctx)) if ne else None
+    gm = torch.empty((nd, nm), dtype=torch.float64, device=_dev(ctx)) if nm else None
+    check(ctx.lib.omg_gain_dev(ctx.handle, geom.handle, _prec(precision), ctypes.byref(hi), ctypes.byref(di),
+                               _ptr(dip), nd, _ptr(el), ne, _ptr(sq), nm, _ptr(ge), _ptr(gm), ctypes.byref(st)))
+    return (ge.T if ne else None), (gm.T if nm else None), st.as_dict()
+
+
+# ---- reference class names (gain.h:60-136) --------------------------------
+
+def GainEEG(HMinv, DSM, H2EM):
+    """GainEEG(HeadMatInv, SourceMat, Head2EEGMat) = H2EM HMinv DSM (gain.h:69-76)."""
+    return torch.as_tensor(H2EM) @ torch.as_tensor(HMinv) @ torch.as_tensor(DSM)
+
+
+def GainMEG(HMinv, DSM, H2MM, DS2MM):
+    """GainMEG = DS2MM + H2MM HMinv DSM (gain.h:60-67)."""
+    return torch.as_tensor(DS2MM) + torch.as_tensor(H2MM) @ torch.as_tensor(HMinv) @ torch.as_tensor(DSM)
+
+
+def GainEEGadjoint(geom: Geometry, dipoles, electrodes, precision=FP64):
+    """GainEEGadjoint(geo, dipoles, HM, H2EM) (gain.h:78-89), HM/H2EM assembled here."""
+    return forward_gain(geom, dipoles, electrodes=electrodes, precision=precision)[0]
+
+
+def GainMEGadjoint(geom: Geometry, dipoles, squids, precision=FP64):
+    """GainMEGadjoint(geo, dipoles, HM, H2MM, DS2MM) (gain.h:91-104)."""
+    return forward_gain(geom, dipoles, squids=squids, precision=precision)[1]
+
+
+def GainEEGMEGadjoint(geom: Geometry, dipoles, electrodes, squids, precision=FP64):
+    """GainEEGMEGadjoint (gain.h:106-136): (EEG leadfield, MEG leadfield)."""
+    ge, gm, _ = forward_gain(geom, dipoles, electrodes=electrodes, squids=squids, precision=precision)
+    return ge, gm

@@ -1,0 +1,883 @@
+// C ABI of the GB300 forward path: contexts, geometry handles, assembly,
+// the quasi-definite solver and the adjoint gain pipeline.  Host code only
+// orchestrates; every numerical step runs in the kernels of bem_kernels.cu and
+// dense_kernels.cu on the context's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "omg_internal.h"
+
+namespace omg {
+// kernel launchers (bem_kernels.cu)
+void launch_prepare_triangles_order(const DevGeom& g, int order, cudaStream_t s);
+void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
+                                 cudaStream_t s);
+void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
+                              const double* srec, double* out, cudaStream_t s);
+void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int maxb, const int* dnb,
+                          const int* bmesh, const int* binside, const int* orient, int forced, int* dom, int* err,
+                          cudaStream_t s);
+void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
+                const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
+                const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
+                double tol, int perm, double* out, int64_t ldo, double* p1tmp, cudaStream_t s);
+void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
+                 double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
+void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s);
+void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
+                  cudaStream_t s);
+// dense_kernels.cu
+template <typename T>
+void gemm(int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, bool ta, const T* B, int64_t ldb, bool tb,
+          T beta, T* C, int64_t ldc, cudaStream_t s, bool lower = false, int64_t row0 = 0, int64_t col0 = 0);
+template <typename T>
+void potrf_trinv(T* A, int64_t lda, int n, T* Linv, int ldi, int* err, int64_t* err_col, int64_t col_offset,
+                 cudaStream_t s);
+template <typename T>
+void negate_lower(T* A, int64_t lda, int64_t n, cudaStream_t s);
+template <typename T>
+void negate_rows(T* B, int64_t ldb, int64_t r0, int64_t r1, int64_t n, cudaStream_t s);
+template <typename Tin, typename Tout>
+void copy_convert(int64_t m, int64_t n, const Tin* a, int64_t lda, Tout* b, int64_t ldb, bool lower, Tout scale,
+                  cudaStream_t s);
+void symmetrize(double* A, int64_t lda, int64_t n, cudaStream_t s);
+void col_norms(int64_t m, int64_t n, const double* A, int64_t lda, double* out, cudaStream_t s);
+void axpy_f32(int64_t m, int64_t n, const float* d, int64_t ldd, double* x, int64_t ldx, const double* colscale,
+              cudaStream_t s);
+void scale_to_f32(int64_t m, int64_t n, const double* r, int64_t ldr, float* b, int64_t ldb, const double* colnorm,
+                  double* colscale, cudaStream_t s);
+}  // namespace omg
+
+using namespace omg;
+
+static thread_local std::string g_last_error;
+
+// ---------------------------------------------------------------------------
+// Handles
+// ---------------------------------------------------------------------------
+struct omg_context_s {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    int* d_err = nullptr;          // [0] status, [1..2] pad
+    int64_t* d_errcol = nullptr;
+    double* d_scalar = nullptr;
+    int64_t launches_at_create = 0;
+};
+
+struct DevBuf {
+    void* p = nullptr;
+    cudaStream_t s = nullptr;
+    DevBuf() = default;
+    DevBuf(size_t bytes, cudaStream_t st) : s(st) {
+        if (bytes) OMG_CUDA(cudaMallocAsync(&p, bytes, st));
+    }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        release();
+        p = o.p;
+        s = o.s;
+        o.p = nullptr;
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+template <typename T>
+static T* upload(std::vector<DevBuf>& keep, const std::vector<T>& v, cudaStream_t s) {
+    keep.emplace_back(std::max<size_t>(1, v.size()) * sizeof(T), s);
+    if (!v.empty()) OMG_CUDA(cudaMemcpyAsync(keep.back().p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return keep.back().as<T>();
+}
+
+struct omg_geometry_s {
+    omg_context ctx = nullptr;
+    HostGeometry h;
+    DevGeom d;
+    std::vector<DevBuf> bufs;
+    // mesh-level device tables
+    int32_t* tmesh = nullptr;
+    int64_t* tidx_ref = nullptr;
+    int* barrier = nullptr;
+    int* orient = nullptr;
+    int64_t* tbeg = nullptr;
+    double* jump = nullptr;
+    int32_t* eeg_cand = nullptr;
+    int64_t n_eeg_cand = 0;
+    // domain tables
+    int ndom = 0, maxb = 1;
+    int* dnb = nullptr;
+    int* bmesh = nullptr;
+    int* binside = nullptr;
+    double* dsigma = nullptr;
+    int prepared_order = -1;
+};
+
+struct omg_solver_s {
+    omg_context ctx = nullptr;
+    omg_geometry geo = nullptr;
+    int precision = OMG_PREC_FP64;
+    int64_t N = 0, nP = 0;
+    std::vector<int64_t> bounds;            // block boundaries (include nP)
+    std::vector<int64_t> linv_off;          // offsets of each block's inverse
+    DevBuf A64;                             // FP64: factor (lower). Mixed: symmetrized FP64 HeadMat
+    DevBuf A32;                             // mixed: FP32 factor
+    DevBuf Linv;                            // per-block inverses (T)
+    double refine_tol = 1e-11;
+    int max_refine = 12;
+    int last_steps = 0;
+    double last_residual = 0.0;
+};
+
+// ---------------------------------------------------------------------------
+// Error plumbing
+// ---------------------------------------------------------------------------
+template <typename F>
+static int guarded(F&& f) {
+    try {
+        f();
+        return OMG_OK;
+    } catch (const Error& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return OMG_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return OMG_ERR_INVALID;
+    }
+}
+
+static void set_device(omg_context ctx) { OMG_CUDA(cudaSetDevice(ctx->device)); }
+
+static void reset_err(omg_context ctx) {
+    OMG_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int) * 4, ctx->stream));
+    OMG_CUDA(cudaMemsetAsync(ctx->d_errcol, 0, sizeof(int64_t), ctx->stream));
+}
+
+// Synchronizes the stream and turns a device-side status into an exception.
+static void check_err(omg_context ctx, const char* what) {
+    int h[4] = {0, 0, 0, 0};
+    int64_t col = 0;
+    OMG_CUDA(cudaMemcpyAsync(h, ctx->d_err, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    OMG_CUDA(cudaMemcpyAsync(&col, ctx->d_errcol, sizeof(col), cudaMemcpyDeviceToHost, ctx->stream));
+    OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h[0] == OMG_ERR_NOT_DEFINITE)
+        throw Error(OMG_ERR_NOT_DEFINITE, std::string(what) + ": pivot of the wrong sign at internal column " +
+                                              std::to_string(col) + " (head matrix not quasi-definite)");
+    if (h[0] == OMG_ERR_TIMEOUT) throw Error(OMG_ERR_TIMEOUT, std::string(what) + ": a bounded device wait gave up");
+    if (h[0] == OMG_ERR_INVALID)
+        throw Error(OMG_ERR_INVALID, std::string(what) + ": a dipole lies in no domain of the geometry");
+    if (h[0] != 0) throw Error(h[0], std::string(what) + ": device error");
+}
+
+static omg_integrator default_hm_integrator() { return {3, 0, 0.005}; }      // assemble.h:32
+static omg_integrator default_dsm_integrator() { return {3, 10, 0.001}; }    // assembleSourceMat.h:28
+
+static void check_integrator(const omg_integrator& it, bool allow_adaptive) {
+    OMG_REQUIRE(it.order >= 0 && it.order <= 3, "integrator order must be 0..3");
+    OMG_REQUIRE(it.levels >= 0, "integrator levels must be >= 0");
+    if (!allow_adaptive && it.levels > 0)
+        throw Error(OMG_ERR_UNSUPPORTED, "adaptive integration of the head matrix is not supported");
+    OMG_REQUIRE(it.levels <= 12, "adaptive integration depth is limited to 12 levels");
+}
+
+// ---------------------------------------------------------------------------
+// Geometry upload
+// ---------------------------------------------------------------------------
+static void upload_geometry(omg_geometry g) {
+    cudaStream_t s = g->ctx->stream;
+    HostGeometry& h = g->h;
+    DevGeom& d = g->d;
+    d.nv = h.nv;
+    d.nt = h.nt;
+    d.N = h.N;
+    d.nP = h.nP;
+    d.nmesh = h.nmesh;
+    d.V = upload(g->bufs, h.V, s);
+    d.T = upload(g->bufs, h.T, s);
+    std::vector<int32_t> tpos(h.nt, -1), tmesh(h.nt, 0);
+    for (int m = 0; m < h.nmesh; ++m)
+        for (int64_t t = h.tbeg[m]; t < h.tbeg[m + 1]; ++t) {
+            tmesh[t] = m;
+            if (!h.barrier[m]) tpos[t] = (int32_t)(h.tidx[t] - h.nv);
+        }
+    d.tpos = upload(g->bufs, tpos, s);
+    g->bufs.emplace_back((size_t)h.nt * SREC * 8, s);
+    d.srec = g->bufs.back().as<double>();
+    g->bufs.emplace_back((size_t)h.nt * PREC * 8, s);
+    d.prec = g->bufs.back().as<double>();
+    g->bufs.emplace_back((size_t)h.nt * QREC * 8, s);
+    d.qrec = g->bufs.back().as<double>();
+    d.v2t_beg = upload(g->bufs, h.v2t_beg, s);
+    d.v2t_tri = upload(g->bufs, h.v2t_tri, s);
+    d.v2t_loc = upload(g->bufs, h.v2t_loc, s);
+    g->tmesh = upload(g->bufs, tmesh, s);
+    g->tidx_ref = upload(g->bufs, h.tidx, s);
+    g->barrier = upload(g->bufs, h.barrier, s);
+    g->orient = upload(g->bufs, h.orient, s);
+    g->tbeg = upload(g->bufs, h.tbeg, s);
+    std::vector<double> jump(h.nmesh);
+    for (int m = 0; m < h.nmesh; ++m) jump[m] = h.conductivity_jump(m);
+    g->jump = upload(g->bufs, jump, s);
+    std::vector<int32_t> cand;
+    for (int m : h.eeg_meshes)
+        for (int64_t t = h.tbeg[m]; t < h.tbeg[m + 1]; ++t) cand.push_back((int32_t)t);
+    g->n_eeg_cand = (int64_t)cand.size();
+    g->eeg_cand = upload(g->bufs, cand, s);
+    g->ndom = (int)h.domains.size();
+    g->maxb = 1;
+    for (const auto& dm : h.domains) g->maxb = std::max(g->maxb, (int)dm.bounds.size());
+    std::vector<int> dnb(g->ndom), bm(g->ndom * g->maxb, -1), bi(g->ndom * g->maxb, 0);
+    std::vector<double> sig(g->ndom);
+    for (int k = 0; k < g->ndom; ++k) {
+        dnb[k] = (int)h.domains[k].bounds.size();
+        sig[k] = h.domains[k].sigma;
+        for (int j = 0; j < dnb[k]; ++j) {
+            bm[k * g->maxb + j] = h.domains[k].bounds[j].mesh;
+            bi[k * g->maxb + j] = h.domains[k].bounds[j].inside ? 1 : 0;
+        }
+    }
+    g->dnb = upload(g->bufs, dnb, s);
+    g->bmesh = upload(g->bufs, bm, s);
+    g->binside = upload(g->bufs, bi, s);
+    g->dsigma = upload(g->bufs, sig, s);
+    launch_prepare_triangles_order(d, 3, s);
+    g->prepared_order = 3;
+}
+
+static void ensure_order(omg_geometry g, int order) {
+    if (g->prepared_order != order) {
+        launch_prepare_triangles_order(g->d, order, g->ctx->stream);
+        g->prepared_order = order;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// HeadMat assembly into the internal lower triangle (assembleHeadMat.cpp:73-115)
+// ---------------------------------------------------------------------------
+static void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld) {
+    omg_context ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    const HostGeometry& h = g->h;
+    const DevGeom& d = g->d;
+    check_integrator(integ, false);
+    ensure_order(g, integ.order);
+    const int order = integ.order;
+    OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)h.N, s));
+    for (const auto& p : h.pairs) {
+        const int m1 = p.m1, m2 = p.m2;
+        const bool same = (m1 == m2);
+        const int64_t t1b = h.tbeg[m1], t1e = h.tbeg[m1 + 1], t2b = h.tbeg[m2], t2e = h.tbeg[m2 + 1];
+        const int64_t v1b = h.vbeg[m1], v1e = h.vbeg[m1 + 1], v2b = h.vbeg[m2], v2e = h.vbeg[m2 + 1];
+        double Scoeff = 0.0;
+        if (same ? !h.barrier[m1] : (!h.barrier[m1] && !h.barrier[m2])) {   // set_S_block
+            launch_S_block(d, t1b, t1e, t2b, t2e, same, p.cS, order, hm, ld, nullptr, ctx->d_err, s);
+            Scoeff = p.cS;
+        }
+        if (Scoeff != 0.0) {   // set_N_block from the S already in the matrix
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / Scoeff, hm, ld, nullptr, hm, s);
+        } else {               // ... or from a temporary unit S block (current barriers)
+            DevBuf tmp((size_t)(t1e - t1b) * (t2e - t2b) * 8, s);
+            launch_S_block(d, t1b, t1e, t2b, t2e, same, 1.0, order, nullptr, 0, tmp.as<double>(), ctx->d_err, s);
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN, nullptr, ld, tmp.as<double>(), hm, s);
+        }
+        auto dblock = [&](int ma, int mb) {
+            const int64_t tab = h.tbeg[ma], tae = h.tbeg[ma + 1], tbb = h.tbeg[mb], tbe = h.tbeg[mb + 1];
+            DevBuf tmp((size_t)(tae - tab) * (tbe - tbb) * 3 * 8, s);
+            launch_D_block(d, tab, tae, tbb, tbe, order, tmp.as<double>(), ctx->d_err, s);
+            launch_D_gather(d, tab, tae, tbb, tbe, h.vbeg[mb], h.vbeg[mb + 1], p.cD, tmp.as<double>(), hm, ld, s);
+        };
+        if (!h.barrier[m1]) dblock(m1, m2);                 // set_D_block
+        if (!same && !h.barrier[m2]) dblock(m2, m1);        // set_Dstar_block
+    }
+    // deflate (assembleHeadMat.cpp:27-60)
+    for (const auto& part : h.part_outermost) {
+        int64_t nb = 0, i_first = 0;
+        std::vector<std::pair<int64_t, int64_t>> ranges;
+        for (int m : part) {
+            nb += h.vbeg[m + 1] - h.vbeg[m];
+            if (i_first == 0) i_first = h.vbeg[m];
+            ranges.push_back({h.vbeg[m], h.vbeg[m + 1]});
+        }
+        if (nb > 0) launch_deflate(d, ranges, i_first, nb, hm, ld, ctx->d_scalar, s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Factorization: HM = L diag(+I_P, -I_V) L^T, blocked right-looking.
+// ---------------------------------------------------------------------------
+template <typename T>
+static void factor_ldlt(omg_solver sv, T* A, int64_t ld, int nb) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N, nP = sv->nP;
+    sv->bounds.clear();
+    for (int64_t k = 0; k < N;) {
+        sv->bounds.push_back(k);
+        int64_t e = std::min(N, k + nb);
+        if (k < nP && e > nP) e = nP;
+        k = e;
+    }
+    sv->bounds.push_back(N);
+    const size_t nblocks = sv->bounds.size() - 1;
+    sv->linv_off.assign(nblocks + 1, 0);
+    for (size_t b = 0; b < nblocks; ++b) {
+        const int64_t nk = sv->bounds[b + 1] - sv->bounds[b];
+        sv->linv_off[b + 1] = sv->linv_off[b] + nk * nk;
+    }
+    sv->Linv = DevBuf((size_t)sv->linv_off[nblocks] * sizeof(T), s);
+    DevBuf W((size_t)N * nb * sizeof(T), s);
+    T* Li = sv->Linv.as<T>();
+    for (size_t b = 0; b < nblocks; ++b) {
+        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
+        if (k0 == nP) negate_lower<T>(A + k0 + k0 * ld, ld, N - k0, s);
+        potrf_trinv<T>(A + k0 + k0 * ld, ld, (int)nk, Li + sv->linv_off[b], (int)nk, sv->ctx->d_err,
+                       sv->ctx->d_errcol, k0, s);
+        if (m > 0) {
+            T* w = W.as<T>();
+            gemm<T>(m, nk, nk, T(1), A + k1 + k0 * ld, ld, false, Li + sv->linv_off[b], nk, true, T(0), w, m, s);
+            gemm<T>(m, m, nk, T(-1), w, m, false, w, m, true, T(1), A + k1 + k1 * ld, ld, s, true, 0, 0);
+            copy_convert<T, T>(m, nk, w, m, A + k1 + k0 * ld, ld, false, T(1), s);
+        }
+    }
+}
+
+// In place: B <- HM^-1 B (internal numbering).
+template <typename T>
+static void solve_ldlt(omg_solver sv, const T* A, int64_t ld, T* B, int64_t ldb, int64_t nrhs) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N;
+    const size_t nblocks = sv->bounds.size() - 1;
+    int64_t nbmax = 0;
+    for (size_t b = 0; b < nblocks; ++b) nbmax = std::max(nbmax, sv->bounds[b + 1] - sv->bounds[b]);
+    DevBuf W((size_t)nbmax * nrhs * sizeof(T), s);
+    T* w = W.as<T>();
+    const T* Li = sv->Linv.as<T>();
+    for (size_t b = 0; b < nblocks; ++b) {
+        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0;
+        gemm<T>(nk, nrhs, nk, T(1), Li + sv->linv_off[b], nk, false, B + k0, ldb, false, T(0), w, nk, s);
+        copy_convert<T, T>(nk, nrhs, w, nk, B + k0, ldb, false, T(1), s);
+        if (k1 < N) gemm<T>(N - k1, nrhs, nk, T(-1), A + k1 + k0 * ld, ld, false, w, nk, false, T(1), B + k1, ldb, s);
+    }
+    negate_rows<T>(B, ldb, sv->nP, N, nrhs, s);
+    for (size_t bb = nblocks; bb-- > 0;) {
+        const int64_t k0 = sv->bounds[bb], k1 = sv->bounds[bb + 1], nk = k1 - k0;
+        if (k1 < N) gemm<T>(nk, nrhs, N - k1, T(-1), A + k1 + k0 * ld, ld, true, B + k1, ldb, false, T(1), B + k0, ldb, s);
+        gemm<T>(nk, nrhs, nk, T(1), Li + sv->linv_off[bb], nk, true, B + k0, ldb, false, T(0), w, nk, s);
+        copy_convert<T, T>(nk, nrhs, w, nk, B + k0, ldb, false, T(1), s);
+    }
+}
+
+constexpr int NB64 = 96;    // FP64 diagonal block (2 x 96^2 x 8 B of shared memory)
+constexpr int NB32 = 128;   // FP32 diagonal block
+
+// Factor the internal-order HeadMat held in `hm` (FP64, lower), taking ownership.
+static void solver_factor(omg_solver sv, DevBuf&& hm) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N;
+    reset_err(sv->ctx);
+    if (sv->precision == OMG_PREC_FP64) {
+        sv->A64 = std::move(hm);
+        factor_ldlt<double>(sv, sv->A64.as<double>(), N, NB64);
+    } else {
+        sv->A64 = std::move(hm);
+        sv->A32 = DevBuf((size_t)N * N * sizeof(float), s);
+        copy_convert<double, float>(N, N, sv->A64.as<double>(), N, sv->A32.as<float>(), N, true, 1.0f, s);
+        symmetrize(sv->A64.as<double>(), N, N, s);
+        factor_ldlt<float>(sv, sv->A32.as<float>(), N, NB32);
+    }
+    check_err(sv->ctx, "factorization");
+}
+
+// Mixed precision: x = HM^-1 b by FP32 solves refined against the FP64 HM.
+static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N;
+    DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s);
+    DevBuf bn((size_t)nrhs * 8, s), rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s);
+    double* x = X.as<double>();
+    double* r = R.as<double>();
+    OMG_CUDA(cudaMemsetAsync(x, 0, (size_t)N * nrhs * 8, s));
+    copy_convert<double, double>(N, nrhs, B, ldb, r, N, false, 1.0, s);
+    col_norms(N, nrhs, r, N, bn.as<double>(), s);
+    std::vector<double> hb(nrhs), hr(nrhs);
+    OMG_CUDA(cudaMemcpyAsync(hb.data(), bn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
+    int steps = 0;
+    double rel = 1.0;
+    for (; steps < sv->max_refine; ++steps) {
+        scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, steps == 0 ? bn.as<double>() : rn.as<double>(),
+                     sc.as<double>(), s);
+        solve_ldlt<float>(sv, sv->A32.as<float>(), N, B32.as<float>(), N, nrhs);
+        axpy_f32(N, nrhs, B32.as<float>(), N, x, N, sc.as<double>(), s);
+        // r = b - HM x in FP64
+        copy_convert<double, double>(N, nrhs, B, ldb, r, N, false, 1.0, s);
+        gemm<double>(N, nrhs, N, -1.0, sv->A64.as<double>(), N, false, x, N, false, 1.0, r, N, s);
+        col_norms(N, nrhs, r, N, rn.as<double>(), s);
+        OMG_CUDA(cudaMemcpyAsync(hr.data(), rn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+        rel = 0.0;
+        for (int64_t j = 0; j < nrhs; ++j) rel = std::max(rel, hb[j] > 0 ? hr[j] / hb[j] : 0.0);
+        if (!(rel > sv->refine_tol)) {
+            ++steps;
+            break;
+        }
+    }
+    sv->last_steps = steps;
+    sv->last_residual = rel;
+    copy_convert<double, double>(N, nrhs, x, N, B, ldb, false, 1.0, s);
+    if (rel > sv->refine_tol)
+        throw Error(OMG_ERR_NOT_CONVERGED,
+                    "iterative refinement stopped at relative residual " + std::to_string(rel));
+}
+
+static void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
+    if (nrhs <= 0) return;
+    if (sv->precision == OMG_PREC_FP64)
+        solve_ldlt<double>(sv, sv->A64.as<double>(), sv->N, B, ldb, nrhs);
+    else
+        solve_mixed(sv, B, ldb, nrhs);
+}
+
+// ---------------------------------------------------------------------------
+// Sources / sensors
+// ---------------------------------------------------------------------------
+static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain,
+                         int perm, double* out, int64_t ldo) {
+    omg_context ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    check_integrator(integ, true);
+    OMG_REQUIRE(domain >= -1 && domain < g->ndom, "domain index out of range");
+    if (ldo == g->h.N)
+        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)g->h.N * nd * 8, s));
+    else
+        for (int64_t j = 0; j < nd; ++j) OMG_CUDA(cudaMemsetAsync(out + j * ldo, 0, (size_t)g->h.N * 8, s));
+    if (nd == 0) return;
+    DevBuf sa((size_t)nd * g->h.nmesh * 8, s), dom((size_t)nd * sizeof(int), s);
+    launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s);
+    launch_domain_lookup(nd, g->h.nmesh, sa.as<double>(), g->ndom, g->maxb, g->dnb, g->bmesh, g->binside, g->orient,
+                         domain, dom.as<int>(), ctx->d_err, s);
+    // chunk the dipoles so the P1 scratch stays near 512 MB
+    const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (g->h.nt * 24)));
+    DevBuf p1((size_t)std::min(per, nd) * g->h.nt * 24, s);
+    for (int64_t d0 = 0; d0 < nd; d0 += per) {
+        const int64_t n = std::min(per, nd - d0);
+        launch_dsm(g->d, d0, n, dip, g->tmesh, g->tidx_ref, g->barrier, g->orient, dom.as<int>(), g->maxb, g->dnb,
+                   g->bmesh, g->binside, g->dsigma, integ.order, integ.levels, integ.tol, perm, out, ldo,
+                   p1.as<double>(), s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* omg_last_error(void) { return g_last_error.c_str(); }
+const char* omg_version(void) { return "openmeeg_gb300 0.1 (sm_103a)"; }
+
+int omg_context_create(int device, omg_context* out) {
+    return guarded([&] {
+        OMG_REQUIRE(out != nullptr, "null output handle");
+        int n = 0;
+        OMG_CUDA(cudaGetDeviceCount(&n));
+        OMG_REQUIRE(device >= 0 && device < n, "no such CUDA device");
+        auto ctx = std::make_unique<omg_context_s>();
+        ctx->device = device;
+        OMG_CUDA(cudaSetDevice(device));
+        OMG_CUDA(cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking));
+        ctx->stream = ctx->own;
+        OMG_CUDA(cudaMalloc(&ctx->d_err, sizeof(int) * 4));
+        OMG_CUDA(cudaMalloc(&ctx->d_errcol, sizeof(int64_t)));
+        OMG_CUDA(cudaMalloc(&ctx->d_scalar, sizeof(double) * 4));
+        OMG_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int) * 4));
+        ctx->launches_at_create = kernel_launch_count();
+        *out = ctx.release();
+    });
+}
+
+int omg_context_destroy(omg_context ctx) {
+    return guarded([&] {
+        if (!ctx) return;
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->d_err);
+        cudaFree(ctx->d_errcol);
+        cudaFree(ctx->d_scalar);
+        if (ctx->own) cudaStreamDestroy(ctx->own);
+        delete ctx;
+    });
+}
+
+int omg_context_set_stream(omg_context ctx, void* stream) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx, "null context");
+        ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    });
+}
+
+int omg_context_synchronize(omg_context ctx) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx, "null context");
+        set_device(ctx);
+        OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int64_t omg_context_kernel_launches(omg_context ctx) {
+    return ctx ? kernel_launch_count() - ctx->launches_at_create : 0;
+}
+
+static void finish_geometry(omg_context ctx, std::unique_ptr<omg_geometry_s>& g, omg_geometry* out) {
+    g->ctx = ctx;
+    upload_geometry(g.get());
+    OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = g.release();
+}
+
+int omg_geometry_create(omg_context ctx, int32_t n_meshes, const int64_t* mesh_nverts, const double* verts,
+                        const int64_t* mesh_ntris, const int64_t* tris, int32_t n_domains, const int32_t* dom_nbounds,
+                        const int32_t* dom_bounds, const double* dom_sigma, omg_geometry* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && out && mesh_nverts && verts && mesh_ntris && tris && dom_nbounds && dom_bounds && dom_sigma,
+                    "null argument");
+        set_device(ctx);
+        auto g = std::make_unique<omg_geometry_s>();
+        g->h = build_geometry(n_meshes, mesh_nverts, verts, mesh_ntris, tris, n_domains, dom_nbounds, dom_bounds,
+                              dom_sigma, {});
+        finish_geometry(ctx, g, out);
+    });
+}
+
+int omg_geometry_load(omg_context ctx, const char* geom_file, const char* cond_file, omg_geometry* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geom_file && cond_file && out, "null argument");
+        set_device(ctx);
+        auto g = std::make_unique<omg_geometry_s>();
+        g->h = load_geometry_files(geom_file, cond_file);
+        finish_geometry(ctx, g, out);
+    });
+}
+
+int omg_geometry_destroy(omg_geometry geo) {
+    return guarded([&] {
+        if (!geo) return;
+        cudaSetDevice(geo->ctx->device);
+        cudaStreamSynchronize(geo->ctx->stream);
+        geo->bufs.clear();
+        cudaStreamSynchronize(geo->ctx->stream);
+        delete geo;
+    });
+}
+
+int omg_geometry_get_info(omg_geometry geo, omg_geometry_info* info) {
+    return guarded([&] {
+        OMG_REQUIRE(geo && info, "null argument");
+        info->n_vertices = geo->h.nv;
+        info->n_triangles = geo->h.nt;
+        info->n_unknowns = geo->h.N;
+        info->n_triangle_unknowns = geo->h.nP;
+        info->n_meshes = geo->h.nmesh;
+        info->n_domains = (int32_t)geo->h.domains.size();
+        info->n_mesh_pairs = (int32_t)geo->h.pairs.size();
+        info->nested = geo->h.nested ? 1 : 0;
+    });
+}
+
+int omg_geometry_set_conductivities(omg_geometry geo, const double* dom_sigma) {
+    return guarded([&] {
+        OMG_REQUIRE(geo && dom_sigma, "null argument");
+        HostGeometry& h = geo->h;
+        for (size_t d = 0; d < h.domains.size(); ++d) {
+            OMG_REQUIRE(std::isfinite(dom_sigma[d]) && dom_sigma[d] >= 0.0, "conductivity must be finite and >= 0");
+            OMG_REQUIRE((dom_sigma[d] == 0.0) == (h.domains[d].sigma == 0.0),
+                        "a conductivity may not change to or from zero");
+        }
+        for (size_t d = 0; d < h.domains.size(); ++d) h.domains[d].sigma = dom_sigma[d];
+        h.recompute_coefficients();
+        std::vector<double> jump(h.nmesh);
+        for (int m = 0; m < h.nmesh; ++m) jump[m] = h.conductivity_jump(m);
+        cudaStream_t s = geo->ctx->stream;
+        OMG_CUDA(cudaMemcpyAsync(geo->jump, jump.data(), jump.size() * 8, cudaMemcpyHostToDevice, s));
+        std::vector<double> sig(h.domains.size());
+        for (size_t d = 0; d < sig.size(); ++d) sig[d] = h.domains[d].sigma;
+        OMG_CUDA(cudaMemcpyAsync(geo->dsigma, sig.data(), sig.size() * 8, cudaMemcpyHostToDevice, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int omg_headmat_dev(omg_context ctx, omg_geometry geo, const omg_integrator* integ, int32_t precision, double* hm,
+                    int64_t ld) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && hm, "null argument");
+        OMG_REQUIRE(ld >= geo->h.N, "ld must be >= N");
+        OMG_REQUIRE(precision == OMG_PREC_FP64 || precision == OMG_PREC_MIXED, "unknown precision");
+        set_device(ctx);
+        reset_err(ctx);
+        const omg_integrator it = integ ? *integ : default_hm_integrator();
+        const int64_t N = geo->h.N;
+        DevBuf tmp((size_t)N * N * 8, ctx->stream);
+        assemble_headmat_internal(geo, it, tmp.as<double>(), N);
+        launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, hm, ld, false, ctx->stream);
+        check_err(ctx, "HeadMat");
+    });
+}
+
+int omg_headmat_packed_dev(omg_context ctx, omg_geometry geo, const omg_integrator* integ, double* packed) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && packed, "null argument");
+        set_device(ctx);
+        reset_err(ctx);
+        const omg_integrator it = integ ? *integ : default_hm_integrator();
+        const int64_t N = geo->h.N;
+        DevBuf tmp((size_t)N * N * 8, ctx->stream);
+        assemble_headmat_internal(geo, it, tmp.as<double>(), N);
+        launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, packed, 0, true, ctx->stream);
+        check_err(ctx, "HeadMat");
+    });
+}
+
+int omg_dipsourcemat_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                         const omg_integrator* integ, int32_t domain, double* dsm) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_dipoles == 0 || (dipoles && dsm)), "null argument");
+        OMG_REQUIRE(n_dipoles >= 0, "negative dipole count");
+        set_device(ctx);
+        reset_err(ctx);
+        const omg_integrator it = integ ? *integ : default_dsm_integrator();
+        dsm_internal(geo, dipoles, n_dipoles, it, domain, 0, dsm, geo->h.N);
+        check_err(ctx, "DipSourceMat");
+    });
+}
+
+int omg_head2eegmat_dev(omg_context ctx, omg_geometry geo, const double* electrodes, int64_t n_electrodes,
+                        double* h2em, int64_t* sparse_cols, double* sparse_vals) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_electrodes == 0 || electrodes), "null argument");
+        OMG_REQUIRE(geo->n_eeg_cand > 0, "no interface touches a zero-conductivity domain");
+        set_device(ctx);
+        reset_err(ctx);
+        if (h2em) OMG_CUDA(cudaMemsetAsync(h2em, 0, (size_t)n_electrodes * geo->h.N * 8, ctx->stream));
+        launch_h2em(geo->d, electrodes, n_electrodes, geo->n_eeg_cand, geo->eeg_cand, 0, h2em, n_electrodes, 1, 0,
+                    sparse_cols, sparse_vals, ctx->stream);
+        check_err(ctx, "Head2EEGMat");
+    });
+}
+
+int omg_head2megmat_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids, double* h2mm) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_squids == 0 || (squids && h2mm)), "null argument");
+        set_device(ctx);
+        reset_err(ctx);
+        if (n_squids == 0) return;
+        OMG_CUDA(cudaMemsetAsync(h2mm, 0, (size_t)n_squids * geo->h.N * 8, ctx->stream));
+        DevBuf F((size_t)n_squids * geo->h.nt * 8, ctx->stream);
+        launch_h2mm(geo->d, squids, n_squids, geo->tmesh, geo->jump, 0, h2mm, n_squids, 1, 0, F.as<double>(),
+                    ctx->stream);
+        check_err(ctx, "Head2MEGMat");
+    });
+}
+
+int omg_dipsource2megmat_dev(omg_context ctx, const double* dipoles, int64_t n_dipoles, const double* squids,
+                             int64_t n_squids, double* ds2mm) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && (n_dipoles == 0 || n_squids == 0 || (dipoles && squids && ds2mm)), "null argument");
+        set_device(ctx);
+        launch_ds2mm(dipoles, n_dipoles, squids, n_squids, ds2mm, n_squids, ctx->stream);
+        OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* integ, int32_t precision,
+                      omg_solver* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && out, "null argument");
+        OMG_REQUIRE(precision == OMG_PREC_FP64 || precision == OMG_PREC_MIXED, "unknown precision");
+        set_device(ctx);
+        reset_err(ctx);
+        auto sv = std::make_unique<omg_solver_s>();
+        sv->ctx = ctx;
+        sv->geo = geo;
+        sv->precision = precision;
+        sv->N = geo->h.N;
+        sv->nP = geo->h.nP;
+        DevBuf hm((size_t)sv->N * sv->N * 8, ctx->stream);
+        const omg_integrator it = integ ? *integ : default_hm_integrator();
+        assemble_headmat_internal(geo, it, hm.as<double>(), sv->N);
+        check_err(ctx, "HeadMat");
+        solver_factor(sv.get(), std::move(hm));
+        *out = sv.release();
+    });
+}
+
+int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double* hm, int64_t ld, int32_t precision,
+                                omg_solver* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && hm && out, "null argument");
+        OMG_REQUIRE(ld >= geo->h.N, "ld must be >= N");
+        set_device(ctx);
+        auto sv = std::make_unique<omg_solver_s>();
+        sv->ctx = ctx;
+        sv->geo = geo;
+        sv->precision = precision;
+        sv->N = geo->h.N;
+        sv->nP = geo->h.nP;
+        DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream);
+        launch_from_reference_dense(geo->d, hm, ld, A.as<double>(), sv->N, ctx->stream);
+        solver_factor(sv.get(), std::move(A));
+        *out = sv.release();
+    });
+}
+
+int omg_solver_solve_dev(omg_solver sv, double* b, int64_t ldb, int64_t nrhs) {
+    return guarded([&] {
+        OMG_REQUIRE(sv && b, "null argument");
+        OMG_REQUIRE(ldb >= sv->N && nrhs >= 0, "bad right-hand side shape");
+        set_device(sv->ctx);
+        cudaStream_t s = sv->ctx->stream;
+        const int64_t N = sv->N, nv = sv->geo->h.nv, nP = sv->nP;
+        // reference -> internal numbering: rows [nv, N) first, then [0, nv)
+        DevBuf X((size_t)N * nrhs * 8, s);
+        double* x = X.as<double>();
+        for (int64_t j = 0; j < nrhs; ++j) {
+            OMG_CUDA(cudaMemcpyAsync(x + j * N, b + j * ldb + nv, (size_t)nP * 8, cudaMemcpyDeviceToDevice, s));
+            OMG_CUDA(cudaMemcpyAsync(x + j * N + nP, b + j * ldb, (size_t)nv * 8, cudaMemcpyDeviceToDevice, s));
+        }
+        solver_solve_internal(sv, x, N, nrhs);
+        for (int64_t j = 0; j < nrhs; ++j) {
+            OMG_CUDA(cudaMemcpyAsync(b + j * ldb + nv, x + j * N, (size_t)nP * 8, cudaMemcpyDeviceToDevice, s));
+            OMG_CUDA(cudaMemcpyAsync(b + j * ldb, x + j * N + nP, (size_t)nv * 8, cudaMemcpyDeviceToDevice, s));
+        }
+        OMG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int omg_solver_destroy(omg_solver sv) {
+    return guarded([&] {
+        if (!sv) return;
+        cudaSetDevice(sv->ctx->device);
+        cudaStreamSynchronize(sv->ctx->stream);
+        delete sv;
+    });
+}
+
+// Adjoint gain (gain.h:78-136): factor once, solve the sensor rows, contract
+// with the DipSourceMat.
+static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, const omg_integrator& hm_it,
+                          const omg_integrator& dsm_it, const double* dip, int64_t nd, const double* el, int64_t ne,
+                          const double* sq, int64_t nm, double* geeg, double* gmeg, omg_gain_stats* st) {
+    cudaStream_t s = ctx->stream;
+    const int64_t N = geo->h.N, k = ne + nm;
+    cudaEvent_t ev[6];
+    for (auto& e : ev) OMG_CUDA(cudaEventCreate(&e));
+    OMG_CUDA(cudaEventRecord(ev[0], s));
+    reset_err(ctx);
+    auto sv = std::make_unique<omg_solver_s>();
+    sv->ctx = ctx;
+    sv->geo = geo;
+    sv->precision = precision;
+    sv->N = N;
+    sv->nP = geo->h.nP;
+    DevBuf hm((size_t)N * N * 8, s);
+    assemble_headmat_internal(geo, hm_it, hm.as<double>(), N);
+    OMG_CUDA(cudaEventRecord(ev[1], s));
+    // right-hand sides (internal numbering) and DSM
+    DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
+    OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
+    if (ne > 0) {
+        OMG_REQUIRE(geo->n_eeg_cand > 0, "no interface touches a zero-conductivity domain");
+        launch_h2em(geo->d, el, ne, geo->n_eeg_cand, geo->eeg_cand, 1, B.as<double>(), 1, N, 0, nullptr, nullptr, s);
+    }
+    DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
+    if (nm > 0) launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
+    dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N);
+    if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s);
+    OMG_CUDA(cudaEventRecord(ev[2], s));
+    solver_factor(sv.get(), std::move(hm));
+    OMG_CUDA(cudaEventRecord(ev[3], s));
+    solver_solve_internal(sv.get(), B.as<double>(), N, k);
+    if (ne > 0) gemm<double>(ne, nd, N, 1.0, B.as<double>(), N, true, DSM.as<double>(), N, false, 0.0, geeg, ne, s);
+    if (nm > 0)
+        gemm<double>(nm, nd, N, 1.0, B.as<double>() + ne * N, N, true, DSM.as<double>(), N, false, 1.0, gmeg, nm, s);
+    OMG_CUDA(cudaEventRecord(ev[4], s));
+    check_err(ctx, "gain");
+    if (st) {
+        float a = 0, b = 0, c = 0, d = 0;
+        OMG_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]));
+        OMG_CUDA(cudaEventElapsedTime(&b, ev[1], ev[2]));
+        OMG_CUDA(cudaEventElapsedTime(&c, ev[2], ev[3]));
+        OMG_CUDA(cudaEventElapsedTime(&d, ev[3], ev[4]));
+        st->t_headmat_ms = a;
+        st->t_sources_ms = b;
+        st->t_factor_ms = c;
+        st->t_solve_ms = d;
+        st->t_total_ms = a + b + c + d;
+        st->refinement_steps = sv->last_steps;
+        st->gmres_iterations = 0;
+        st->final_residual = sv->last_residual;
+        st->device_bytes = (int64_t)(N * N * 8) * (precision == OMG_PREC_MIXED ? 3 : 2) / 2 + N * (k + nd) * 8;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+}
+
+int omg_gain_dev(omg_context ctx, omg_geometry geo, int32_t precision, const omg_integrator* hm_integ,
+                 const omg_integrator* dsm_integ, const double* dipoles, int64_t n_dipoles, const double* electrodes,
+                 int64_t n_electrodes, const double* squids, int64_t n_squids, double* gain_eeg, double* gain_meg,
+                 omg_gain_stats* stats) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo, "null argument");
+        OMG_REQUIRE(precision == OMG_PREC_FP64 || precision == OMG_PREC_MIXED, "unknown precision");
+        OMG_REQUIRE(n_dipoles >= 0 && n_electrodes >= 0 && n_squids >= 0, "negative count");
+        OMG_REQUIRE(n_dipoles == 0 || dipoles, "null dipoles");
+        OMG_REQUIRE(n_electrodes == 0 || (electrodes && (gain_eeg || n_dipoles == 0)), "null electrodes or EEG output");
+        OMG_REQUIRE(n_squids == 0 || (squids && (gain_meg || n_dipoles == 0)), "null squids or MEG output");
+        set_device(ctx);
+        const omg_integrator hi = hm_integ ? *hm_integ : default_hm_integrator();
+        const omg_integrator di = dsm_integ ? *dsm_integ : default_dsm_integrator();
+        gain_pipeline(ctx, geo, precision, hi, di, dipoles, n_dipoles, electrodes, n_electrodes, squids, n_squids,
+                      gain_eeg, gain_meg, stats);
+    });
+}
+
+int omg_gain_host(omg_context ctx, omg_geometry geo, int32_t precision, const omg_integrator* hm_integ,
+                  const omg_integrator* dsm_integ, const double* dipoles, int64_t n_dipoles, const double* electrodes,
+                  int64_t n_electrodes, const double* squids, int64_t n_squids, double* gain_eeg, double* gain_meg,
+                  omg_gain_stats* stats) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo, "null argument");
+        set_device(ctx);
+        cudaStream_t s = ctx->stream;
+        DevBuf d_dip((size_t)n_dipoles * 6 * 8, s), d_el((size_t)n_electrodes * 3 * 8, s),
+            d_sq((size_t)n_squids * 6 * 8, s), d_ge((size_t)n_electrodes * n_dipoles * 8, s),
+            d_gm((size_t)n_squids * n_dipoles * 8, s);
+        if (n_dipoles) OMG_CUDA(cudaMemcpyAsync(d_dip.p, dipoles, n_dipoles * 48, cudaMemcpyHostToDevice, s));
+        if (n_electrodes) OMG_CUDA(cudaMemcpyAsync(d_el.p, electrodes, n_electrodes * 24, cudaMemcpyHostToDevice, s));
+        if (n_squids) OMG_CUDA(cudaMemcpyAsync(d_sq.p, squids, n_squids * 48, cudaMemcpyHostToDevice, s));
+        int rc = omg_gain_dev(ctx, geo, precision, hm_integ, dsm_integ, d_dip.as<double>(), n_dipoles,
+                              d_el.as<double>(), n_electrodes, d_sq.as<double>(), n_squids, d_ge.as<double>(),
+                              d_gm.as<double>(), stats);
+        if (rc != OMG_OK) throw Error(rc, g_last_error);
+        if (n_electrodes && n_dipoles)
+            OMG_CUDA(cudaMemcpyAsync(gain_eeg, d_ge.p, n_electrodes * n_dipoles * 8, cudaMemcpyDeviceToHost, s));
+        if (n_squids && n_dipoles)
+            OMG_CUDA(cudaMemcpyAsync(gain_meg, d_gm.p, n_squids * n_dipoles * 8, cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+}  // extern "C"

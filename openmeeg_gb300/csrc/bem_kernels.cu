@@ -1,0 +1,891 @@
+// BEM assembly kernels for sm_103a: HeadMat blocks (S, D, N, deflation),
+// DipSourceMat, the sensor matrices and the triangle preprocessing they share.
+//
+// Layout in HBM.  The head matrix lives as a dense N x N column-major FP64
+// array in the solver's internal numbering -- triangle unknowns first, then
+// vertex unknowns (the reference's [V | P] order rotated by n_vertices) --
+// and only its lower triangle is written.  Per-triangle records (OperatorS
+// data, P1 single-layer data, quadrature points) are precomputed once and
+// staged tile by tile into shared memory with bulk (TMA) copies.
+//
+// Each kernel restates the reference loop it replaces; the per-pair work is
+// the reference's analytic inner integral times its Gauss outer rule, so the
+// FP64 results agree with the reference to rounding.
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "device_common.cuh"
+#include "omg_internal.h"
+
+namespace omg {
+
+using dev::d3;
+
+// Gauss rules of 3/6/7/16 points (OpenMEEG/include/integrator.h:260-318;
+// Bonnet's tables).  The digits are those of the reference: parity at 1e-10
+// requires the same truncated nodes.  [order][point] = {b0, b1, b2, weight}.
+__constant__ double c_rules[4][16][4] = {
+    {{0.166666666666667, 0.166666666666667, 0.666666666666667, 0.333333333333334},
+     {0.166666666666667, 0.666666666666667, 0.166666666666667, 0.333333333333334},
+     {0.666666666666667, 0.166666666666667, 0.166666666666667, 0.333333333333334}},
+    {{0.445948490915965, 0.445948490915965, 0.108103018168070, 0.223381589678010},
+     {0.445948490915965, 0.108103018168070, 0.445948490915965, 0.223381589678010},
+     {0.108103018168070, 0.445948490915965, 0.445948490915965, 0.223381589678010},
+     {0.091576213509771, 0.091576213509771, 0.816847572980458, 0.109951743655322},
+     {0.091576213509771, 0.816847572980458, 0.091576213509771, 0.109951743655322},
+     {0.816847572980458, 0.091576213509771, 0.091576213509771, 0.109951743655322}},
+    {{0.333333333333333, 0.333333333333333, 0.333333333333333, 0.2250},
+     {0.470142064105115, 0.470142064105115, 0.059715871789770, 0.132394152788506},
+     {0.470142064105115, 0.059715871789770, 0.470142064105115, 0.132394152788506},
+     {0.059715871789770, 0.470142064105115, 0.470142064105115, 0.132394152788506},
+     {0.101286507323456, 0.101286507323456, 0.797426985353088, 0.125939180544828},
+     {0.101286507323456, 0.797426985353088, 0.101286507323456, 0.125939180544828},
+     {0.797426985353088, 0.101286507323456, 0.101286507323456, 0.125939180544828}},
+    {{0.333333333333333, 0.333333333333333, 0.333333333333333, 0.144315607677786},
+     {0.081414823414554, 0.459292588292722, 0.459292588292722, 0.095091634267284},
+     {0.459292588292722, 0.081414823414554, 0.459292588292722, 0.095091634267284},
+     {0.459292588292722, 0.459292588292722, 0.081414823414554, 0.095091634267284},
+     {0.898905543365937, 0.050547228317031, 0.050547228317031, 0.032458497623198},
+     {0.050547228317031, 0.898905543365937, 0.050547228317031, 0.032458497623198},
+     {0.050547228317031, 0.050547228317031, 0.898905543365937, 0.032458497623198},
+     {0.658861384496479, 0.170569307751760, 0.170569307751761, 0.103217370534718},
+     {0.170569307751760, 0.658861384496479, 0.170569307751761, 0.103217370534718},
+     {0.170569307751760, 0.170569307751761, 0.658861384496479, 0.103217370534718},
+     {0.008394777409957, 0.728492392955404, 0.263112829634639, 0.027230314174434},
+     {0.728492392955404, 0.008394777409957, 0.263112829634639, 0.027230314174434},
+     {0.728492392955404, 0.263112829634639, 0.008394777409957, 0.027230314174434},
+     {0.008394777409957, 0.263112829634639, 0.728492392955404, 0.027230314174434},
+     {0.263112829634639, 0.008394777409957, 0.728492392955404, 0.027230314174434},
+     {0.263112829634639, 0.728492392955404, 0.008394777409957, 0.027230314174434}}};
+__constant__ int c_nbpts[4] = {3, 6, 7, 16};
+
+static int64_t g_launches = 0;
+int64_t kernel_launch_count() { return g_launches; }
+void count_launch(int n) { g_launches += n; }
+
+static inline void check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(OMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    count_launch();
+}
+
+static inline unsigned nblocks(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// Quadrature point: sum_j b_j p_j accumulated from zero without contraction,
+// as Vect3::multadd does (integrator.h:214-225).
+__device__ __forceinline__ d3 bary_point(const double* r, d3 p0, d3 p1, d3 p2) {
+    d3 v;
+    v.x = __dadd_rn(__dadd_rn(__dmul_rn(r[0], p0.x), __dmul_rn(r[1], p1.x)), __dmul_rn(r[2], p2.x));
+    v.y = __dadd_rn(__dadd_rn(__dmul_rn(r[0], p0.y), __dmul_rn(r[1], p1.y)), __dmul_rn(r[2], p2.y));
+    v.z = __dadd_rn(__dadd_rn(__dmul_rn(r[0], p0.z), __dmul_rn(r[1], p1.z)), __dmul_rn(r[2], p2.z));
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// Triangle preprocessing: normal/area (triangle.h:57-62), OperatorS edge data
+// (analytics.h:22-30), P1SingleLayerPotential edge data (analytics.h:81-85),
+// and the points of the `order` rule.
+// ---------------------------------------------------------------------------
+__global__ void prepare_triangles_kernel(int64_t nt, const double* __restrict__ V, const int32_t* __restrict__ T,
+                                         int order, double* srec, double* prec, double* qrec) {
+    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const d3 p0 = dev::ld3(V + 3 * (int64_t)T[3 * t]);
+    const d3 p1 = dev::ld3(V + 3 * (int64_t)T[3 * t + 1]);
+    const d3 p2 = dev::ld3(V + 3 * (int64_t)T[3 * t + 2]);
+    d3 nn = dev::cross(p1 - p0, p2 - p0);
+    const double nrm = dev::norm(nn);
+    const double area = 0.5 * nrm;
+    const d3 n = nn * (1.0 / nrm);
+    double* s = srec + t * SREC;
+    const d3 P[3] = {p0, p1, p2};
+    for (int i = 0; i < 3; ++i) {
+        s[3 * i] = P[i].x;
+        s[3 * i + 1] = P[i].y;
+        s[3 * i + 2] = P[i].z;
+    }
+    s[9] = n.x; s[10] = n.y; s[11] = n.z;
+    s[12] = area;
+    for (int i = 0; i < 3; ++i) {
+        const d3 vref = P[i] - P[(i + 1) % 3];
+        const double len = dev::norm(vref);
+        const d3 unit = dev::mk(vref.x / len, vref.y / len, vref.z / len);
+        const d3 en = dev::cross(n, unit);
+        s[13 + i] = len;
+        s[16 + 3 * i] = en.x; s[17 + 3 * i] = en.y; s[18 + 3 * i] = en.z;
+    }
+    for (int i = 25; i < SREC; ++i) s[i] = 0.0;
+    double* p = prec + t * PREC;
+    for (int i = 0; i < 13; ++i) p[i] = s[i];
+    const d3 D[3] = {p1 - p0, p2 - p1, p0 - p2};
+    for (int i = 0; i < 3; ++i) {
+        const double dn = dev::norm(D[i]);
+        p[13 + 3 * i] = D[i].x; p[14 + 3 * i] = D[i].y; p[15 + 3 * i] = D[i].z;
+        p[22 + 3 * i] = D[i].x / dn; p[23 + 3 * i] = D[i].y / dn; p[24 + 3 * i] = D[i].z / dn;
+    }
+    p[31] = 0.0;
+    double* q = qrec + t * QREC;
+    const int np = c_nbpts[order];
+    for (int k = 0; k < MAXQ; ++k) {
+        d3 v = dev::mk(0, 0, 0);
+        if (k < np) v = bary_point(c_rules[order][k], p0, p1, p2);
+        q[3 * k] = v.x; q[3 * k + 1] = v.y; q[3 * k + 2] = v.z;
+    }
+    q[48] = area;
+    for (int i = 49; i < QREC; ++i) q[i] = 0.0;
+}
+
+void launch_prepare_triangles_order(const DevGeom& g, int order, cudaStream_t s) {
+    prepare_triangles_kernel<<<nblocks(g.nt, 128), 128, 0, s>>>(g.nt, g.V, g.T, order, g.srec, g.prec, g.qrec);
+    check_launch("prepare_triangles");
+}
+void launch_prepare_triangles(const DevGeom& g, cudaStream_t s) { launch_prepare_triangles_order(g, 3, s); }
+
+// Lower-triangle address of (a, b) in the internal column-major matrix.
+__device__ __forceinline__ int64_t lower_at(int64_t a, int64_t b, int64_t ld) {
+    return a >= b ? a + b * ld : b + a * ld;
+}
+
+// ---------------------------------------------------------------------------
+// S block (DiagonalBlock::S operators.h:209-237, NonDiagonalBlock::S :391-425):
+// S(t1,t2) = coeff * integral over t2 (Gauss rule) of OperatorS(t1).
+// One CTA per TI x TJ tile; t1 OperatorS records and t2 quadrature records
+// are bulk-copied into shared memory.  One thread per (t1,t2) pair.
+// ---------------------------------------------------------------------------
+constexpr int S_TI = 16, S_TJ = 64, S_THREADS = 256;
+
+__global__ void __launch_bounds__(S_THREADS) s_block_kernel(const double* __restrict__ srec,
+                                                            const double* __restrict__ qrec, int64_t t1b, int64_t n1,
+                                                            int64_t t2b, int64_t n2, int same, double coeff,
+                                                            int order, const int32_t* __restrict__ tpos, double* hm,
+                                                            int64_t ld, double* tmp, int* err) {
+    extern __shared__ __align__(16) double smem[];
+    __shared__ __align__(8) uint64_t bar;
+    const int64_t i0 = (int64_t)blockIdx.y * S_TI, j0 = (int64_t)blockIdx.x * S_TJ;
+    if (same && j0 + S_TJ <= i0) return;   // tile strictly below the diagonal
+    const int ni = (int)(n1 - i0 < (int64_t)S_TI ? n1 - i0 : (int64_t)S_TI), nj = (int)(n2 - j0 < (int64_t)S_TJ ? n2 - j0 : (int64_t)S_TJ);
+    double* sS = smem;                 // ni x SREC
+    double* sQ = smem + S_TI * SREC;   // nj x QREC
+    if (!dev::stage_two(sS, srec + (t1b + i0) * SREC, (uint32_t)(ni * SREC * 8), sQ, qrec + (t2b + j0) * QREC,
+                        (uint32_t)(nj * QREC * 8), &bar, err))
+        return;
+    const int np = c_nbpts[order];
+    for (int p = threadIdx.x; p < ni * nj; p += S_THREADS) {
+        const int i = p / nj, j = p % nj;
+        if (same && j0 + j < i0 + i) continue;
+        const double* s = sS + i * SREC;
+        const double* q = sQ + j * QREC;
+        double acc = 0.0;
+        for (int k = 0; k < np; ++k) acc += c_rules[order][k][3] * dev::operator_S(s, dev::ld3(q + 3 * k));
+        const double val = q[48] * acc;
+        const int64_t a = t1b + i0 + i, b = t2b + j0 + j;
+        if (hm) {
+            hm[lower_at(tpos[a], tpos[b], ld)] = val * coeff;
+        } else {
+            tmp[(i0 + i) * n2 + (j0 + j)] = val;
+            if (same) tmp[(j0 + j) * n2 + (i0 + i)] = val;
+        }
+    }
+}
+
+void launch_S_block(const DevGeom& g, int64_t t1b, int64_t t1e, int64_t t2b, int64_t t2e, bool same, double coeff,
+                    int order, double* hm, int64_t ld, double* tmp, int* err, cudaStream_t s) {
+    const int64_t n1 = t1e - t1b, n2 = t2e - t2b;
+    dim3 grid(nblocks(n2, S_TJ), nblocks(n1, S_TI));
+    const size_t sm = (size_t)(S_TI * SREC + S_TJ * QREC) * 8;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(s_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        attr = true;
+    }
+    s_block_kernel<<<grid, S_THREADS, sm, s>>>(g.srec, g.qrec, t1b, n1, t2b, n2, same ? 1 : 0, coeff, order, g.tpos,
+                                               hm, ld, tmp, err);
+    check_launch("S block");
+}
+
+// ---------------------------------------------------------------------------
+// D block (BlocksBase::D operators.h:83-115): for t1 in A, t2 in B the three
+// integrals over t1 of P1SingleLayerPotential(t2), stored per pair in a
+// scratch array; the gather kernel below adds them into (t1, vertex) entries
+// in a fixed order, so the result does not depend on thread timing.
+// ---------------------------------------------------------------------------
+constexpr int D_TI = 16, D_TJ = 32, D_THREADS = 256;
+
+__global__ void __launch_bounds__(D_THREADS) d_block_kernel(const double* __restrict__ qrec,
+                                                            const double* __restrict__ prec, int64_t tab, int64_t na,
+                                                            int64_t tbb, int64_t nb, int order, double* tmp,
+                                                            int* err) {
+    extern __shared__ __align__(16) double smem[];
+    __shared__ __align__(8) uint64_t bar;
+    const int64_t i0 = (int64_t)blockIdx.y * D_TI, j0 = (int64_t)blockIdx.x * D_TJ;
+    const int ni = (int)(na - i0 < (int64_t)D_TI ? na - i0 : (int64_t)D_TI), nj = (int)(nb - j0 < (int64_t)D_TJ ? nb - j0 : (int64_t)D_TJ);
+    double* sQ = smem;                 // ni x QREC (integration triangles t1)
+    double* sP = smem + D_TI * QREC;   // nj x PREC (analytic triangles t2)
+    if (!dev::stage_two(sQ, qrec + (tab + i0) * QREC, (uint32_t)(ni * QREC * 8), sP, prec + (tbb + j0) * PREC,
+                        (uint32_t)(nj * PREC * 8), &bar, err))
+        return;
+    const int np = c_nbpts[order];
+    for (int p = threadIdx.x; p < ni * nj; p += D_THREADS) {
+        const int i = p / nj, j = p % nj;
+        const double* q = sQ + i * QREC;
+        const double* P = sP + j * PREC;
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < np; ++k) {
+            double v[3];
+            dev::p1_single_layer(P, dev::ld3(q + 3 * k), v);
+            const double w = c_rules[order][k][3];
+            acc[0] += w * v[0];
+            acc[1] += w * v[1];
+            acc[2] += w * v[2];
+        }
+        double* o = tmp + ((i0 + i) * nb + (j0 + j)) * 3;
+        o[0] = q[48] * acc[0];
+        o[1] = q[48] * acc[1];
+        o[2] = q[48] * acc[2];
+    }
+}
+
+void launch_D_block(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int64_t tbe, int order, double* tmp,
+                    int* err, cudaStream_t s) {
+    const int64_t na = tae - tab, nb = tbe - tbb;
+    dim3 grid(nblocks(nb, D_TJ), nblocks(na, D_TI));
+    const size_t sm = (size_t)(D_TI * QREC + D_TJ * PREC) * 8;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(d_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        attr = true;
+    }
+    d_block_kernel<<<grid, D_THREADS, sm, s>>>(g.qrec, g.prec, tab, na, tbb, nb, order, tmp, err);
+    check_launch("D block");
+}
+
+// HM(t1, v) += coeff * sum over triangles t2 of B containing v of tmp[t1][t2][local(v)]
+// (the += of operators.h:108-109, in increasing t2 order).
+__global__ void d_gather_kernel(int64_t tab, int64_t na, int64_t tbb, int64_t nb, int64_t vbb, int64_t nvb,
+                                double coeff, const double* __restrict__ tmp, const int32_t* __restrict__ v2t_beg,
+                                const int32_t* __restrict__ v2t_tri, const int8_t* __restrict__ v2t_loc,
+                                const int32_t* __restrict__ tpos, int64_t nP, double* hm, int64_t ld) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= na * nvb) return;
+    const int64_t iv = idx % nvb, ia = idx / nvb;
+    const int64_t v = vbb + iv;
+    double sum = 0.0;
+    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
+        const int64_t t2 = v2t_tri[k];
+        if (t2 < tbb || t2 >= tbb + nb) continue;
+        sum += tmp[(ia * nb + (t2 - tbb)) * 3 + v2t_loc[k]];
+    }
+    hm[lower_at(tpos[tab + ia], nP + v, ld)] += coeff * sum;
+}
+
+void launch_D_gather(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int64_t tbe, int64_t vbb, int64_t vbe,
+                     double coeff, const double* tmp, double* hm, int64_t ld, cudaStream_t s) {
+    const int64_t n = (tae - tab) * (vbe - vbb);
+    d_gather_kernel<<<nblocks(n, 256), 256, 0, s>>>(tab, tae - tab, tbb, tbe - tbb, vbb, vbe - vbb, coeff, tmp,
+                                                    g.v2t_beg, g.v2t_tri, g.v2t_loc, g.tpos, g.nP, hm, ld);
+    check_launch("D gather");
+}
+
+// ---------------------------------------------------------------------------
+// N block (BlocksBase::N operators.h:119-148 through DiagonalBlock::N :271-296
+// and NonDiagonalBlock::N :454-480):
+//   N(v1,v2) = - sum_{t1 ∋ v1, t2 ∋ v2} f (CB1.CB2) S(t1,t2) / (A1 A2)
+// with f = 1/4 (1/2 for the same vertex across meshes).  S comes from the head
+// matrix (scaled by coeff/Scoeff) or from a temporary unit-coefficient block.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ d3 edge_cb(const double* V, const int32_t* T, int64_t t, int loc) {
+    // Edge(V) opposite the vertex: vertices {1,2},{2,0},{0,1} (triangle.h:87-94,154)
+    const int a = (loc + 1) % 3, b = (loc + 2) % 3;
+    return dev::ld3(V + 3 * (int64_t)T[3 * t + a]) - dev::ld3(V + 3 * (int64_t)T[3 * t + b]);
+}
+
+__global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e, int64_t v2b, int64_t n2,
+                               int64_t t2b, int64_t t2e, int same, double coeff, const double* __restrict__ hm_src,
+                               int64_t ld, const double* __restrict__ tmp, const double* __restrict__ V,
+                               const int32_t* __restrict__ T, const double* __restrict__ srec,
+                               const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
+                               const int8_t* __restrict__ v2t_loc, const int32_t* __restrict__ tpos, int64_t nP,
+                               double* hm) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= n1 * n2) return;
+    const int64_t i1 = idx % n1, i2 = idx / n1;   // v1 fastest: coalesced writes down a column
+    if (same && i2 > i1) return;
+    const int64_t v1 = v1b + i1, v2 = v2b + i2;
+    const double factor = same ? 0.25 : (v1 == v2 ? 0.5 : 0.25);
+    const int64_t nt2 = t2e - t2b;
+    double result = 0.0;
+    for (int k1 = v2t_beg[v1]; k1 < v2t_beg[v1 + 1]; ++k1) {
+        const int64_t a = v2t_tri[k1];
+        if (a < t1b || a >= t1e) continue;
+        const d3 cb1 = edge_cb(V, T, a, v2t_loc[k1]);
+        const double A1 = srec[a * SREC + 12];
+        for (int k2 = v2t_beg[v2]; k2 < v2t_beg[v2 + 1]; ++k2) {
+            const int64_t b = v2t_tri[k2];
+            if (b < t2b || b >= t2e) continue;
+            const d3 cb2 = edge_cb(V, T, b, v2t_loc[k2]);
+            const double A2 = srec[b * SREC + 12];
+            const double sv = hm_src ? hm_src[lower_at(tpos[a], tpos[b], ld)] : tmp[(a - t1b) * nt2 + (b - t2b)];
+            result -= factor * dev::dot(cb1, cb2) * sv / (A1 * A2);
+        }
+    }
+    hm[lower_at(nP + v1, nP + v2, ld)] += result * coeff;
+}
+
+void launch_N_block(const DevGeom& g, int64_t v1b, int64_t v1e, int64_t t1b, int64_t t1e, int64_t v2b, int64_t v2e,
+                    int64_t t2b, int64_t t2e, bool same, double coeff, const double* hm_src, int64_t ld,
+                    const double* tmp, double* hm, cudaStream_t s) {
+    const int64_t n = (v1e - v1b) * (v2e - v2b);
+    n_block_kernel<<<nblocks(n, 256), 256, 0, s>>>(v1b, v1e - v1b, t1b, t1e, v2b, v2e - v2b, t2b, t2e, same ? 1 : 0,
+                                                   coeff, hm_src, ld, tmp, g.V, g.T, g.srec, g.v2t_beg, g.v2t_tri,
+                                                   g.v2t_loc, g.tpos, g.nP, hm);
+    check_launch("N block");
+}
+
+// ---------------------------------------------------------------------------
+// Deflation (Details::deflate, assembleHeadMat.cpp:27-60): add M(i0,i0)/n to
+// every vertex pair of each outermost mesh.  The coefficient is read by a
+// separate launch so no thread can observe a partially deflated diagonal.
+// ---------------------------------------------------------------------------
+__global__ void deflate_coef_kernel(const double* hm, int64_t pos, int64_t ld, double inv_nb, double* coef) {
+    coef[0] = hm[pos + pos * ld] * inv_nb;
+}
+__global__ void deflate_add_kernel(int64_t vb, int64_t n, int64_t nP, const double* coef, double* hm, int64_t ld) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= n * n) return;
+    const int64_t i1 = idx % n, i2 = idx / n;
+    if (i2 > i1) return;
+    hm[(nP + vb + i1) + (nP + vb + i2) * ld] += coef[0];
+}
+
+void launch_deflate(const DevGeom& g, const std::vector<std::pair<int64_t, int64_t>>& vranges, int64_t i_first,
+                    int64_t nb, double* hm, int64_t ld, double* scratch, cudaStream_t s) {
+    const int64_t pos = g.nP + i_first;
+    deflate_coef_kernel<<<1, 1, 0, s>>>(hm, pos, ld, 1.0 / (double)nb, scratch);
+    check_launch("deflate coef");
+    for (const auto& r : vranges) {
+        const int64_t n = r.second - r.first;
+        deflate_add_kernel<<<nblocks(n * n, 256), 256, 0, s>>>(r.first, n, g.nP, scratch, hm, ld);
+        check_launch("deflate add");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Internal lower-triangle matrix -> reference numbering, dense (both halves)
+// or SymMatrix packed upper.  ipos(r) = r >= nv ? r - nv : r + nP.
+// ---------------------------------------------------------------------------
+__global__ void to_reference_dense_kernel(int64_t N, int64_t nv, int64_t nP, const double* __restrict__ hm,
+                                          int64_t ld, double* out, int64_t ldo) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    for (int64_t j = blockIdx.y; j < N; j += gridDim.y) {
+        const int64_t a = i >= nv ? i - nv : i + nP, b = j >= nv ? j - nv : j + nP;
+        out[i + j * ldo] = hm[lower_at(a, b, ld)];
+    }
+}
+__global__ void to_reference_packed_kernel(int64_t N, int64_t nv, int64_t nP, const double* __restrict__ hm,
+                                           int64_t ld, double* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    for (int64_t j = blockIdx.y; j < N; j += gridDim.y) {
+        if (i > j) continue;
+        const int64_t a = i >= nv ? i - nv : i + nP, b = j >= nv ? j - nv : j + nP;
+        out[i + j * (j + 1) / 2] = hm[lower_at(a, b, ld)];
+    }
+}
+
+void launch_symmetrize_to_reference(const DevGeom& g, const double* hm_int, int64_t ld_int, double* out,
+                                    int64_t ld_out, bool packed, cudaStream_t s) {
+    dim3 grid(nblocks(g.N, 256), (unsigned)std::min<int64_t>(g.N, 32768));
+    if (packed)
+        to_reference_packed_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, hm_int, ld_int, out);
+    else
+        to_reference_dense_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, hm_int, ld_int, out, ld_out);
+    check_launch("to reference");
+}
+
+// Reference-numbered dense (lower triangle read) -> internal lower triangle.
+__global__ void from_reference_dense_kernel(int64_t N, int64_t nv, int64_t nP, const double* __restrict__ in,
+                                            int64_t ldi, double* hm, int64_t ld) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;   // internal row
+    if (a >= N) return;
+    for (int64_t b = blockIdx.y; b <= a; b += gridDim.y) {             // internal column
+        const int64_t i = a < nP ? a + nv : a - nP, j = b < nP ? b + nv : b - nP;
+        hm[a + b * ld] = i >= j ? in[i + j * ldi] : in[j + i * ldi];
+    }
+}
+
+void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
+                                 cudaStream_t s) {
+    dim3 grid(nblocks(g.N, 256), (unsigned)std::min<int64_t>(g.N, 32768));
+    from_reference_dense_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, in, ldi, hm, ld);
+    check_launch("from reference");
+}
+
+// ===========================================================================
+// Sources and sensors
+// ===========================================================================
+
+// Interface::contains (OpenMEEG/src/interface.cpp:18-35) on an oriented solid angle.
+__device__ __forceinline__ bool almost_eq(double x, double y) {
+    return fabs(x - y) < 2.220446049250313e-16 * fabs(x + y) * 1e3 || fabs(x - y) < 2.2250738585072014e-308;
+}
+__device__ __forceinline__ bool interface_contains(double s) {
+    const double fourpi = 12.566370614359172;
+    if (almost_eq(s, -fourpi)) return true;
+    if (almost_eq(s, 0.0)) return false;
+    if (almost_eq(s, fourpi)) return true;
+    return fabs(s) > 0.5 * fourpi;
+}
+
+// Mesh::solid_angle (mesh.cpp:239-244) of every mesh seen from every point:
+// one CTA per point, a fixed-order tree reduction per mesh.
+__global__ void mesh_solid_angles_kernel(const double* __restrict__ pts, int64_t pstride, int nmesh,
+                                         const int64_t* __restrict__ tbeg, const double* __restrict__ srec,
+                                         double* out) {
+    __shared__ double red[256];
+    const int64_t i = blockIdx.x;
+    const d3 p = dev::ld3(pts + i * pstride);
+    for (int m = 0; m < nmesh; ++m) {
+        double acc = 0.0;
+        for (int64_t t = tbeg[m] + threadIdx.x; t < tbeg[m + 1]; t += blockDim.x) {
+            const double* s = srec + t * SREC;
+            const d3 r0 = dev::ld3(s) - p, r1 = dev::ld3(s + 3) - p, r2 = dev::ld3(s + 6) - p;
+            acc += dev::solid_angle(r0, r1, r2, dev::norm(r0), dev::norm(r1), dev::norm(r2), dev::ld3(s + 9), s[12]);
+        }
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[i * nmesh + m] = red[0];
+        __syncthreads();
+    }
+}
+
+// Geometry::domain(point) (geometry.cpp:146-154, domain.cpp:12-17): the first
+// domain all of whose boundaries agree with the point's inside/outside state.
+__global__ void domain_lookup_kernel(int64_t n, int nmesh, const double* __restrict__ sa, int ndom, int maxb,
+                                     const int* __restrict__ dnb, const int* __restrict__ bmesh,
+                                     const int* __restrict__ binside, const int* __restrict__ orient, int forced,
+                                     int* dom, int* err) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (forced >= 0) {
+        dom[i] = forced;
+        return;
+    }
+    int found = -1;
+    for (int d = 0; d < ndom && found < 0; ++d) {
+        bool ok = true;
+        for (int k = 0; k < dnb[d]; ++k) {
+            const int m = bmesh[d * maxb + k];
+            const bool c = interface_contains(orient[m] * sa[i * nmesh + m]);
+            if (c != (binside[d * maxb + k] != 0)) ok = false;
+        }
+        if (ok) found = d;
+    }
+    dom[i] = found;
+    if (found < 0) atomicExch(err, -1 /* OMG_ERR_INVALID: point in no domain */);
+}
+
+// Integrands of the DipSourceMat: Dipole::potential / Dipole::gradient
+// (dipole.h:29-46) and the barycentric weights of PotentialDerivative
+// (analytics.h:140-150, BarycentricCoordinates.h:33-69).
+struct DsmTri {
+    d3 p0, e10, e20, n;
+    double d11, d12, d22;
+};
+__device__ __forceinline__ void dsm_eval(int kind, const DsmTri& T, d3 r0, d3 q, d3 r, double out[3]) {
+    const d3 x = r - r0;
+    if (kind == 1) {
+        const double nrm2 = dev::dot(x, x);
+        out[0] = dev::dot(q, x) / (nrm2 * sqrt(nrm2));
+        return;
+    }
+    const double inv = 1.0 / dev::dot(x, x);
+    const d3 grad = q - x * (3 * dev::dot(q, x) * inv);
+    const double g = dev::dot(grad, T.n) * (inv * sqrt(inv));
+    const d3 v = r - T.p0;
+    const double a1 = dev::dot(v, T.e10), a2 = dev::dot(v, T.e20);
+    const double l1 = T.d11 * a1 + T.d12 * a2;
+    const double l2 = T.d12 * a1 + T.d22 * a2;
+    const double l0 = 1.0 - l1 - l2;
+    out[0] = g * l0;
+    out[1] = g * l1;
+    out[2] = g * l2;
+}
+
+__device__ __forceinline__ void dsm_rule(int kind, int order, const DsmTri& T, d3 r0, d3 q, d3 P0, d3 P1, d3 P2,
+                                         double area, double res[3]) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    const int np = c_nbpts[order];
+    for (int k = 0; k < np; ++k) {
+        const d3 x = bary_point(c_rules[order][k], P0, P1, P2);
+        double v[3];
+        dsm_eval(kind, T, r0, q, x, v);
+        const double w = c_rules[order][k][3];
+        acc[0] += w * v[0];
+        if (kind == 0) {
+            acc[1] += w * v[1];
+            acc[2] += w * v[2];
+        }
+    }
+    res[0] = area * acc[0];
+    res[1] = area * acc[1];
+    res[2] = area * acc[2];
+}
+
+__device__ __forceinline__ void subtriangle(d3& P0, d3& P1, d3& P2, int c) {
+    const d3 m0 = (P1 + P2) * 0.5, m1 = (P2 + P0) * 0.5, m2 = (P0 + P1) * 0.5;
+    if (c == 0) { P1 = m1; P2 = m2; }
+    else if (c == 1) { P0 = m0; P2 = m2; }
+    else if (c == 2) { P0 = m0; P1 = m1; }
+    else { P0 = m0; P1 = m1; P2 = m2; }
+}
+
+constexpr int DSM_MAX_LEVELS = 12;
+constexpr int DSM_STACK = 3 * (DSM_MAX_LEVELS + 1) + 4;
+
+// Integrator::integrate with adaptive_integration (integrator.h:44-48,228-252)
+// as an explicit depth-first stack.  A node is its path of child indices from
+// the root (2 bits per level), so the stack holds no vertex coordinates.
+__device__ void dsm_adaptive(int kind, int order, int levels, double tol, const DsmTri& T, d3 r0, d3 q, d3 R0, d3 R1,
+                             d3 R2, double area, double result[3]) {
+    double coarse[3];
+    dsm_rule(kind, order, T, r0, q, R0, R1, R2, area, coarse);
+    if (levels == 0) {
+        result[0] = coarse[0]; result[1] = coarse[1]; result[2] = coarse[2];
+        return;
+    }
+    uint32_t st_path[DSM_STACK];
+    int8_t st_depth[DSM_STACK], st_level[DSM_STACK];
+    double st_c[DSM_STACK][3];
+    int sp = 0;
+    st_path[0] = 0; st_depth[0] = 0; st_level[0] = (int8_t)levels;
+    st_c[0][0] = coarse[0]; st_c[0][1] = coarse[1]; st_c[0][2] = coarse[2];
+    sp = 1;
+    double total[3] = {0.0, 0.0, 0.0};
+    const int dim = kind == 0 ? 3 : 1;
+    while (sp > 0) {
+        --sp;
+        const uint32_t path = st_path[sp];
+        const int depth = st_depth[sp], level = st_level[sp];
+        const double c0 = st_c[sp][0], c1 = st_c[sp][1], c2 = st_c[sp][2];
+        d3 P0 = R0, P1 = R1, P2 = R2;
+        double a = area;
+        for (int d = 0; d < depth; ++d) {
+            subtriangle(P0, P1, P2, (path >> (2 * d)) & 3);
+            a *= 0.25;
+        }
+        const double sub = 0.25 * a;
+        double integ[4][3];
+        double ref[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < 4; ++c) {
+            d3 Q0 = P0, Q1 = P1, Q2 = P2;
+            subtriangle(Q0, Q1, Q2, c);
+            dsm_rule(kind, order, T, r0, q, Q0, Q1, Q2, sub, integ[c]);
+            for (int k = 0; k < dim; ++k) ref[k] += integ[c][k];
+        }
+        double dn, cn;
+        if (dim == 1) {
+            dn = fabs(c0 - ref[0]);
+            cn = fabs(c0);
+        } else {
+            const double e0 = c0 - ref[0], e1 = c1 - ref[1], e2 = c2 - ref[2];
+            dn = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+            cn = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+        }
+        if (dn <= tol * cn || level == 0) {
+            for (int k = 0; k < dim; ++k) total[k] += ref[k];
+            continue;
+        }
+        for (int c = 3; c >= 0; --c) {
+            st_path[sp] = path | ((uint32_t)c << (2 * depth));
+            st_depth[sp] = (int8_t)(depth + 1);
+            st_level[sp] = (int8_t)(level - 1);
+            st_c[sp][0] = integ[c][0]; st_c[sp][1] = integ[c][1]; st_c[sp][2] = integ[c][2];
+            ++sp;
+        }
+    }
+    result[0] = total[0]; result[1] = total[1]; result[2] = total[2];
+}
+
+// SourceMatrix<Dipole> (assembleSourceMat.cpp:66-104) with
+// operatorPotentialDerivative / operatorPotential (operators.cpp:40-88):
+// one thread per (dipole, triangle).  P0 rows are written directly (one
+// triangle per row); the three P1 contributions go to `p1tmp` for a
+// fixed-order vertex gather (the reference accumulates them atomically).
+__global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__ dip, int64_t nt,
+                           const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
+                           const int64_t* __restrict__ tidx_ref, const int* __restrict__ barrier,
+                           const int* __restrict__ orient, const int* __restrict__ dom, int maxb,
+                           const int* __restrict__ dnb, const int* __restrict__ bmesh,
+                           const int* __restrict__ binside, const double* __restrict__ dsigma, int order, int levels,
+                           double tol, int64_t nv, int64_t nP, int perm, double* out, int64_t ldo, double* p1tmp) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t il = blockIdx.y;
+    if (t >= nt || il >= ndc) return;
+    const int64_t i = dip0 + il;
+    double* o3 = p1tmp + (il * nt + t) * 3;
+    o3[0] = o3[1] = o3[2] = 0.0;
+    const int d = dom[i];
+    if (d < 0) return;
+    const double sigma = dsigma[d];
+    if (sigma == 0.0) return;
+    const int m = tmesh[t];
+    double coeffD = 0.0;
+    bool on = false;
+    for (int k = 0; k < dnb[d]; ++k)
+        if (bmesh[d * maxb + k] == m) {
+            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[m];
+            on = true;
+        }
+    if (!on) return;
+    const double* s = srec + t * SREC;
+    const d3 R0 = dev::ld3(s), R1 = dev::ld3(s + 3), R2 = dev::ld3(s + 6);
+    DsmTri T;
+    T.p0 = R0;
+    T.n = dev::ld3(s + 9);
+    T.e10 = R1 - R0;
+    T.e20 = R2 - R0;
+    const double c11 = dev::dot(T.e10, T.e10), c12 = dev::dot(T.e10, T.e20), c22 = dev::dot(T.e20, T.e20);
+    const double inv_det = 1.0 / (c11 * c22 - c12 * c12);
+    T.d11 = c22 * inv_det;
+    T.d12 = -c12 * inv_det;
+    T.d22 = c11 * inv_det;
+    const d3 r0 = dev::ld3(dip + 6 * i), q = dev::ld3(dip + 6 * i + 3);
+    const double area = s[12];
+    double v[3];
+    dsm_adaptive(0, order, levels, tol, T, r0, q, R0, R1, R2, area, v);
+    o3[0] = v[0] * coeffD;
+    o3[1] = v[1] * coeffD;
+    o3[2] = v[2] * coeffD;
+    if (!barrier[m]) {
+        double p[3];
+        dsm_adaptive(1, order, levels, tol, T, r0, q, R0, R1, R2, area, p);
+        const int64_t ref = tidx_ref[t];
+        const int64_t row = perm ? ref - nv : ref;
+        out[row + i * ldo] = p[0] * (coeffD / sigma);
+    }
+}
+
+__global__ void dsm_gather_kernel(int64_t dip0, int64_t ndc, int64_t nv, int64_t nt, const double* __restrict__ p1tmp,
+                                  const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
+                                  const int8_t* __restrict__ v2t_loc, int64_t nP, int perm, double* out,
+                                  int64_t ldo) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t il = blockIdx.y;
+    if (v >= nv || il >= ndc) return;
+    double sum = 0.0;
+    bool any = false;
+    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
+        const double x = p1tmp[(il * nt + v2t_tri[k]) * 3 + v2t_loc[k]];
+        if (x != 0.0) any = true;
+        sum += x;
+    }
+    if (any) out[(perm ? nP + v : v) + (dip0 + il) * ldo] = sum;
+}
+
+// ---- Head2EEGMat: nearest triangle by Danielsson's point-triangle distance
+// (danielsson.cpp:26-128); one CTA per electrode, fixed-order min reduction.
+__device__ double danielsson(d3 p, const d3 P[3], double al[3]) {
+    int idx[3] = {0, 1, 2};
+    int nb = 3;
+    al[0] = al[1] = al[2] = 0.0;
+    for (;;) {
+        if (nb == 1) {
+            al[idx[0]] = 1.0;
+            return dev::norm(p - P[idx[0]]);
+        }
+        d3 A0Ai[3];
+        for (int i = 1; i < nb; ++i) A0Ai[i] = P[idx[i]] - P[idx[0]];
+        const d3 A0M = p - P[idx[0]];
+        if (nb == 2) {
+            al[idx[1]] = dev::dot(A0M, A0Ai[1]) / dev::dot(A0Ai[1], A0Ai[1]);
+            al[idx[0]] = 1.0 - al[idx[1]];
+        } else {
+            const double a00 = dev::dot(A0Ai[1], A0Ai[1]), a10 = dev::dot(A0Ai[1], A0Ai[2]),
+                         a11 = dev::dot(A0Ai[2], A0Ai[2]);
+            const double b0 = dev::dot(A0M, A0Ai[1]), b1 = dev::dot(A0M, A0Ai[2]);
+            const double dd = a00 * a11 - a10 * a10;
+            al[idx[1]] = (b0 * a11 - b1 * a10) / dd;
+            al[idx[2]] = (a00 * b1 - a10 * b0) / dd;
+            al[idx[0]] = 1.0 - al[idx[1]] - al[idx[2]];
+        }
+        int neg = -1;
+        for (int i = 0; i < nb; ++i)
+            if (al[idx[i]] < 0) {
+                neg = i;
+                break;
+            }
+        if (neg >= 0) {
+            al[idx[neg]] = 0;
+            const int tmp = idx[neg];
+            idx[neg] = idx[nb - 1];
+            idx[nb - 1] = tmp;
+            --nb;
+            continue;
+        }
+        d3 MH = A0M * -1.0;
+        for (int i = 1; i < nb; ++i) MH = MH + A0Ai[i] * al[idx[i]];
+        return dev::norm(MH);
+    }
+}
+
+__global__ void h2em_kernel(const double* __restrict__ pos, int64_t ncand, const int32_t* __restrict__ cand,
+                            const double* __restrict__ srec, const int32_t* __restrict__ T, int64_t nP, int perm,
+                            double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals) {
+    __shared__ double sd[256];
+    __shared__ int64_t so[256];
+    __shared__ double sa[256][3];
+    const int64_t e = blockIdx.x;
+    const d3 p = dev::ld3(pos + 3 * e);
+    double best = 1.79769313486231570e+308, bal[3] = {0, 0, 0};
+    int64_t bo = INT64_MAX;
+    for (int64_t k = threadIdx.x; k < ncand; k += blockDim.x) {
+        const double* s = srec + (int64_t)cand[k] * SREC;
+        const d3 P[3] = {dev::ld3(s), dev::ld3(s + 3), dev::ld3(s + 6)};
+        double al[3];
+        const double dist = danielsson(p, P, al);
+        if (dist < best) {
+            best = dist;
+            bo = k;
+            bal[0] = al[0]; bal[1] = al[1]; bal[2] = al[2];
+        }
+    }
+    sd[threadIdx.x] = best;
+    so[threadIdx.x] = bo;
+    sa[threadIdx.x][0] = bal[0]; sa[threadIdx.x][1] = bal[1]; sa[threadIdx.x][2] = bal[2];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const int o = threadIdx.x + w;
+            if (sd[o] < sd[threadIdx.x] || (sd[o] == sd[threadIdx.x] && so[o] < so[threadIdx.x])) {
+                sd[threadIdx.x] = sd[o];
+                so[threadIdx.x] = so[o];
+                sa[threadIdx.x][0] = sa[o][0]; sa[threadIdx.x][1] = sa[o][1]; sa[threadIdx.x][2] = sa[o][2];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int64_t t = cand[so[0]];
+        for (int j = 0; j < 3; ++j) {
+            const int64_t v = T[3 * t + j];
+            if (dense) dense[(perm ? nP + v : v) * rs + (col0 + e) * cs] = sa[0][j];
+            if (scols) scols[3 * e + j] = v;
+            if (svals) svals[3 * e + j] = sa[0][j];
+        }
+    }
+}
+
+// ---- Head2MEGMat (assembleSensors.cpp:69-96, assembleFerguson.cpp:18-31,
+// operators.h:40-61): OperatorS of every triangle at every sensor, then a
+// fixed-order gather per (sensor, vertex) of (B-A) S / (2 A).
+__global__ void ferguson_s_kernel(const double* __restrict__ sq, int64_t np, int64_t nt,
+                                  const double* __restrict__ srec, double* F) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t i = blockIdx.y;
+    if (t >= nt || i >= np) return;
+    F[i * nt + t] = dev::operator_S(srec + t * SREC, dev::ld3(sq + 6 * i));
+}
+
+__global__ void ferguson_gather_kernel(const double* __restrict__ sq, int64_t np, int64_t nv, int64_t nt,
+                                       const double* __restrict__ F, const double* __restrict__ srec,
+                                       const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
+                                       const int8_t* __restrict__ v2t_loc, const int32_t* __restrict__ tmesh,
+                                       const double* __restrict__ jump, int64_t nP, int perm, double* out,
+                                       int64_t rs, int64_t cs, int64_t col0) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t i = blockIdx.y;
+    if (v >= nv || i >= np) return;
+    d3 res = dev::mk(0, 0, 0);
+    double coeff = 0.0;
+    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
+        const int64_t t = v2t_tri[k];
+        const int loc = v2t_loc[k];
+        const double* s = srec + t * SREC;
+        const d3 A = dev::ld3(s + 3 * ((loc + 1) % 3)), B = dev::ld3(s + 3 * ((loc + 2) % 3));
+        res = res + (B - A) * (F[i * nt + t] / (2 * s[12]));
+        coeff = kMagFactor * jump[tmesh[t]];
+    }
+    const d3 o = dev::ld3(sq + 6 * i + 3);
+    out[(perm ? nP + v : v) * rs + (col0 + i) * cs] = dev::dot(res * coeff, o) / dev::norm(o);
+}
+
+// ---- DipSource2MEGMat (assembleSensors.cpp:133-159): Biot-Savart primary field.
+__global__ void ds2mm_kernel(const double* __restrict__ dip, int64_t nd, const double* __restrict__ sq, int64_t np,
+                             double* out, int64_t ldo) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t j = blockIdx.y;
+    if (i >= np || j >= nd) return;
+    const d3 r = dev::ld3(dip + 6 * j), q = dev::ld3(dip + 6 * j + 3);
+    const d3 diff = dev::ld3(sq + 6 * i) - r;
+    const double nd3 = dev::norm(diff);
+    const d3 f = dev::cross(q, diff) * (1.0 / (nd3 * nd3 * nd3));
+    const d3 o = dev::ld3(sq + 6 * i + 3);
+    out[i + j * ldo] = dev::dot(f, o) * kMagFactor / dev::norm(o);
+}
+
+void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
+                              const double* srec, double* out, cudaStream_t s) {
+    if (n == 0) return;
+    mesh_solid_angles_kernel<<<(unsigned)n, 256, 0, s>>>(pts, pstride, nmesh, tbeg_dev, srec, out);
+    check_launch("mesh solid angles");
+}
+
+void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int maxb, const int* dnb,
+                          const int* bmesh, const int* binside, const int* orient, int forced, int* dom, int* err,
+                          cudaStream_t s) {
+    if (n == 0) return;
+    domain_lookup_kernel<<<nblocks(n, 128), 128, 0, s>>>(n, nmesh, sa, ndom, maxb, dnb, bmesh, binside, orient,
+                                                         forced, dom, err);
+    check_launch("domain lookup");
+}
+
+void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
+                const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
+                const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
+                double tol, int perm, double* out, int64_t ldo, double* p1tmp, cudaStream_t s) {
+    if (ndc == 0) return;
+    dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
+    dsm_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, tmesh, tidx_ref, barrier, orient, dom, maxb, dnb,
+                                    bmesh, binside, dsigma, order, levels, tol, g.nv, g.nP, perm, out, ldo, p1tmp);
+    check_launch("DSM");
+    dim3 grid2(nblocks(g.nv, 128), (unsigned)ndc);
+    dsm_gather_kernel<<<grid2, 128, 0, s>>>(dip0, ndc, g.nv, g.nt, p1tmp, g.v2t_beg, g.v2t_tri, g.v2t_loc, g.nP,
+                                            perm, out, ldo);
+    check_launch("DSM gather");
+}
+
+void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
+                 double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s) {
+    if (ne == 0) return;
+    h2em_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, ncand, cand, g.srec, g.T, g.nP, perm, dense, rs, cs, col0, scols,
+                                             svals);
+    check_launch("H2EM");
+}
+
+void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s) {
+    if (np == 0) return;
+    dim3 grid(nblocks(g.nt, 128), (unsigned)np);
+    ferguson_s_kernel<<<grid, 128, 0, s>>>(sq, np, g.nt, g.srec, F);
+    check_launch("Ferguson S");
+    dim3 grid2(nblocks(g.nv, 128), (unsigned)np);
+    ferguson_gather_kernel<<<grid2, 128, 0, s>>>(sq, np, g.nv, g.nt, F, g.srec, g.v2t_beg, g.v2t_tri, g.v2t_loc,
+                                                 tmesh, jump, g.nP, perm, out, rs, cs, col0);
+    check_launch("Ferguson gather");
+}
+
+void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
+                  cudaStream_t s) {
+    if (nd == 0 || np == 0) return;
+    dim3 grid(nblocks(np, 128), (unsigned)nd);
+    ds2mm_kernel<<<grid, 128, 0, s>>>(dip, nd, sq, np, out, ldo);
+    check_launch("DS2MM");
+}
+
+}  // namespace omg

@@ -1,0 +1,77 @@
+"""Generates the golden fixtures of tests/golden/ by running the reference
+OpenMEEG command-line tools (built from the reference sources by
+oracle/ref/Makefile into oracle/_ref/).  Run where the reference sources are
+available:
+
+    python tests/golden/make_golden.py [--big]
+
+Each fixture is an .npz of the reference's own outputs (read from its .bin
+files) for a seeded workload of openmeeg_gb300.workloads:
+  small_ico1_3l      HM (packed), DSM, H2EM, H2MM, DS2MM, EEG/MEG adjoint gains
+  small_ico1_4l_out  same, 4 layers, outward-oriented meshes (interfaces flipped)
+  small_ico2_3l_pert gains + DSM, SH-perturbed ico2 head
+  config0            EEG/MEG adjoint gains of config0 (ico3, N=4486), 200 dipoles
+  config1_200        (--big) EEG/MEG adjoint gains of config1 (ico4, N=17926) for
+                     its first 200 dipoles
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_runner  # noqa: E402
+from openmeeg_gb300 import io, workloads  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, w, R, keep_hm=False):
+    d = {"dipoles": w.dipoles, "electrodes": w.electrodes, "squids": w.squids}
+    for k in ("dsm", "h2em", "h2mm", "ds2mm", "eeg", "meg"):
+        if k in R:
+            d[k] = R[k]
+    if keep_hm:
+        d["hm_packed"] = io.packed_upper(R["hm"])
+    d["times"] = np.array([R["times"].get(k, np.nan) for k in ("hm", "dsm", "h2em", "h2mm", "ds2mm", "eeg", "meg")])
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **d)
+    print(name, {k: (v.shape if hasattr(v, "shape") else v) for k, v in d.items()}, R["times"])
+
+
+def main():
+    if not ref_runner.available():
+        ref_runner.build()
+    big = "--big" in sys.argv
+    w = workloads.small(1, layers=3)
+    save("small_ico1_3l", w, ref_runner.run_pipeline(w.head, w.dipoles, w.electrodes, w.squids), keep_hm=True)
+    w = workloads.small(1, layers=4, inward=False)
+    save("small_ico1_4l_out", w, ref_runner.run_pipeline(w.head, w.dipoles, w.electrodes, w.squids), keep_hm=True)
+    w = workloads.small(2, layers=3, perturb=True)
+    R = ref_runner.run_pipeline(w.head, w.dipoles, w.electrodes, w.squids)
+    R.pop("hm")
+    R.pop("h2mm")
+    save("small_ico2_3l_pert", w, R)
+    w = workloads.config0()
+    R = ref_runner.run_pipeline(w.head, w.dipoles, w.electrodes, w.squids, want=("hm", "h2em", "h2mm", "ds2mm",
+                                                                                  "eeg", "meg"))
+    for k in ("hm", "h2mm", "h2em"):
+        R.pop(k)
+    save("config0", w, R)
+    if big:
+        w = workloads.config1(200)
+        t0 = time.time()
+        R = ref_runner.run_pipeline(w.head, w.dipoles, w.electrodes, w.squids,
+                                    want=("hm", "h2em", "h2mm", "ds2mm", "eeg", "meg"))
+        for k in ("hm", "h2mm", "h2em", "ds2mm"):
+            R.pop(k)
+        save("config1_200", w, R)
+        print("config1 reference run", time.time() - t0, "s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,132 @@
+"""CPU tests: the oracle restatement against the reference's own outputs
+(golden fixtures), file formats, and the C ABI library's exported symbols."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, rel
+
+
+def _w(name):
+    from openmeeg_gb300 import workloads
+    return {
+        "small_ico1_3l": lambda: workloads.small(1, layers=3),
+        "small_ico1_4l_out": lambda: workloads.small(1, layers=4, inward=False),
+        "small_ico2_3l_pert": lambda: workloads.small(2, layers=3, perturb=True),
+    }[name]()
+
+
+@pytest.mark.parametrize("name", ["small_ico1_3l", "small_ico1_4l_out"])
+def test_oracle_headmat_pinned_to_reference(name):
+    from oracle import oracle
+    from openmeeg_gb300 import io
+    G = golden(name)
+    w = _w(name)
+    g = oracle.digest(w.head)
+    HM = oracle.headmat(g)
+    ref = io.unpack_upper(G["hm_packed"], g.N)
+    assert rel(HM, ref) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["small_ico1_3l", "small_ico1_4l_out", "small_ico2_3l_pert"])
+def test_oracle_sources_sensors_gains_pinned_to_reference(name):
+    from oracle import oracle
+    G = golden(name)
+    w = _w(name)
+    g = oracle.digest(w.head)
+    D = oracle.dsm(g, w.dipoles)
+    assert rel(D, G["dsm"]) < 1e-14
+    E = oracle.h2em(g, w.electrodes)
+    assert rel(E, G["h2em"]) < 1e-14
+    M = oracle.h2mm(g, w.squids)
+    if "h2mm" in G:
+        assert rel(M, G["h2mm"]) < 1e-11
+    S = oracle.ds2mm(w.dipoles, w.squids)
+    assert rel(S, G["ds2mm"]) < 1e-14
+    HM = oracle.headmat(g)
+    assert rel(oracle.gain_eeg(HM, D, E), G["eeg"]) < 1e-12
+    assert rel(oracle.gain_meg(HM, D, M, S), G["meg"]) < 1e-12
+
+
+def test_oracle_numbering_and_pairs():
+    """Unknown count and mesh pairs of nested heads (geometry.cpp:256-295, 405-420)."""
+    from oracle import oracle
+    from openmeeg_gb300 import synthetic as syn
+    h3 = syn.nested_head(3, [0.87, 0.92, 1.0], [1.0, 0.0125, 1.0])
+    g = oracle.digest(h3)
+    assert g.N == 3 * 642 + 2 * 1280 == 4486
+    assert g.pairs.tolist() == [[0, 0], [1, 0], [1, 1], [2, 1], [2, 2]]
+    assert list(g.barrier) == [0, 0, 1]
+    h4 = syn.nested_head(1, [0.85, 0.88, 0.92, 1.0], [0.33, 1.79, 0.0042, 0.33], inward=False)
+    g4 = oracle.digest(h4)
+    assert g4.N == 4 * 42 + 3 * 80
+    assert list(g4.orient) == [-1, -1, -1, -1]
+
+
+def test_bin_roundtrip(tmp_path):
+    from openmeeg_gb300 import io
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((7, 5))
+    io.write_bin(str(tmp_path / "a.bin"), A)
+    k, B = io.read_bin(str(tmp_path / "a.bin"))
+    assert k == "full" and np.array_equal(A, B)
+    S = rng.standard_normal((6, 6))
+    S = S + S.T
+    io.write_bin(str(tmp_path / "s.bin"), S, kind="sym")
+    raw = open(tmp_path / "s.bin", "rb").read()
+    assert len(raw) == 4 + 8 * 21   # uint32 n + packed upper
+    k, B = io.read_bin(str(tmp_path / "s.bin"))
+    assert k == "sym" and np.array_equal(S, B)
+    # packed-upper order is i + j(j+1)/2 (symmatrix.h:52-62)
+    p = io.packed_upper(S)
+    assert p[1 + 2 * 3 // 2] == S[1, 2]
+    io.write_bin(str(tmp_path / "v.bin"), np.arange(4.0), kind="vector")
+    assert io.read_bin(str(tmp_path / "v.bin"))[0] == "vector"
+    io.write_bin(str(tmp_path / "sp.bin"), ([0, 2], [1, 3], [1.5, -2.0], 3, 4), kind="sparse")
+    k, M = io.read_bin(str(tmp_path / "sp.bin"))
+    assert k == "sparse" and M[0, 1] == 1.5 and M[2, 3] == -2.0
+
+
+def test_geom_files_roundtrip(tmp_path):
+    from openmeeg_gb300 import io, workloads
+    from oracle import ref_runner
+    w = workloads.small(1)
+    ref_runner.write_head(str(tmp_path), w.head)
+    meshes, doms = io.read_geom(str(tmp_path / "head.geom"))
+    assert [os.path.basename(m) for m in meshes] == ["cortex.tri", "skull.tri", "scalp.tri"]
+    assert doms == [(d[0], d[1]) for d in w.head.domains]
+    V, T = io.read_tri(meshes[0])
+    assert np.array_equal(V, w.head.vertices[0]) and np.array_equal(T, w.head.triangles[0])
+    cond = io.read_cond(str(tmp_path / "head.cond"))
+    assert cond["Skull"] == 0.0125
+
+
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "openmeeg_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(omg_\w+)\(", txt, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from openmeeg_gb300 import build, _lib
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    syms = _header_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) <= set(_lib.EXPORTED) | set(syms)
+
+
+def test_library_fails_loudly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from openmeeg_gb300 import _lib
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    rc = lib.omg_context_create(0, ctypes.byref(h))
+    assert rc != 0
+    assert lib.omg_last_error()
