@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark: time-to-gain of the symmetric-BEM forward path on one GB300.
+
+Workload (config1, all data seeded and synthetic): 3 nested ico4 surfaces
+(2562 vertices / 5120 triangles each, radii .87/.92/1 perturbed by a 2%
+degree<=4 spherical-harmonic field), conductivities 1/.0125/1, HeadMat size
+17926, 2000 dipoles, 64 EEG electrodes, 151 radial magnetometers at r=1.2.
+
+One step = one full forward gain (HeadMat assembly, DipSourceMat, Head2EEG /
+Head2MEG / DipSource2MEG, factorization, adjoint solves, gain products) in the
+mixed-precision mode, geometry and sensor arrays already resident on the
+device.  `value` is seconds per step (lower is better).  The FP64 drop-in is
+timed on the same box in the same run, and the mixed result's relative error
+against it is reported (target <= 1e-6).
+
+`--impl reference` times the reference CPU path's restatement (the oracle
+port, all host threads) on a bounded sample of the same workload and scales
+it to the full workload.
+
+Inputs exceed the 129 MB L2 (the 2.6 GB head matrix is rebuilt every step),
+so no explicit L2 flush is done between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "time-to-gain (s) ico4-ico5, mixed-prec vs FP64 on same GB300 at rel err <=1e-6"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), \
+            "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in out.splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle port on a bounded sample, scaled to config1
+# ---------------------------------------------------------------------------
+def cpu_sample_time(threads: int | None = None):
+    """Times the oracle (C restatement + LAPACK) on a sample of config1 and
+    scales each stage to the full workload by its operation count."""
+    from oracle import oracle
+    from openmeeg_gb300 import workloads
+    if threads:
+        oracle.set_threads(threads)
+    nthr = oracle.num_threads()
+    w1 = workloads.config1()
+    w0 = workloads.config0()
+    g1 = oracle.digest(w1.head)
+    g0 = oracle.digest(w0.head)
+    T0 = w0.head.triangles[0].shape[0]
+    T1 = w1.head.triangles[0].shape[0]
+    t = {}
+    s = time.perf_counter()
+    HM0 = oracle.headmat(g0)
+    t["headmat"] = (time.perf_counter() - s) * (T1 / T0) ** 2           # S and D pair counts scale as T^2
+    s = time.perf_counter()
+    oracle.solve_adjoint(HM0, np.ones((64 + 151, g0.N)))
+    t["solve"] = (time.perf_counter() - s) * (g1.N / g0.N) ** 3          # symmetric-indefinite solve ~ N^3
+    nd = 100
+    s = time.perf_counter()
+    D = oracle.dsm(g1, w1.dipoles[:nd])
+    t["dsm"] = (time.perf_counter() - s) * (w1.dipoles.shape[0] / nd)   # per-dipole columns
+    s = time.perf_counter()
+    oracle.h2em(g1, w1.electrodes)
+    oracle.h2mm(g1, w1.squids)
+    oracle.ds2mm(w1.dipoles, w1.squids)
+    t["sensors"] = time.perf_counter() - s
+    t["gain_gemm"] = 2.0 * 215 * g1.N * w1.dipoles.shape[0] / 20e9       # GEMM at ~20 GFLOP/s
+    total = sum(t.values())
+    sample = (f"config0 HeadMat (N={g0.N}) x{(T1 / T0) ** 2:.0f} pair-count scale; LAPACK solve N={g0.N}, 215 rhs "
+              f"x(N ratio)^3; DSM of {nd} config1 dipoles x{w1.dipoles.shape[0] // nd}; config1 sensor matrices; "
+              f"gain GEMM modelled")
+    return total, t, sample, nthr
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    times = []
+    for i in range(args.warmup + args.steps):
+        total, parts, sample, nthr = cpu_sample_time()
+        if i >= args.warmup:
+            times.append(total)
+    v = float(np.mean(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded nested icosphere heads)",
+        "config": {"workload": "config1: 3-layer ico4 SH-perturbed head, N=17926, 2000 dipoles, 64 EEG, 151 MEG",
+                   "parallelism": "cpu"},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": nthr, "kind": "port", "sample": sample,
+                         "stages_s": {k: round(x, 3) for k, x in parts.items()}},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+# Algorithmic work per launch for the roofline of the dominant kernel.
+def algorithmic_work(name, w, N, k, nd):
+    """(amount per step, unit, bound) for the kernels that can dominate."""
+    L = 3
+    T = w.head.triangles[0].shape[0]
+    if name in ("gemm_f64", "gemm_f32"):
+        # factorization N^3/3 + forward/backward solves 2 N^2 k per refinement step + gain GEMM 2 k N nd
+        return None
+    return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    __import__("__graft_entry__").build()
+    from openmeeg_gb300 import _lib, api, workloads
+
+    w = getattr(workloads, args.config)()
+    ctx = api.Context(local)
+    ctx.bind_current_stream()
+    geo = api.Geometry.from_head(w.head, ctx)
+    dev = torch.device("cuda", local)
+    dip = torch.as_tensor(w.dipoles, dtype=torch.float64, device=dev)
+    el = torch.as_tensor(w.electrodes, dtype=torch.float64, device=dev)
+    sq = torch.as_tensor(w.squids, dtype=torch.float64, device=dev) if len(w.squids) else None
+    N = geo.size
+    nd, ne, nm = dip.shape[0], el.shape[0], (0 if sq is None else sq.shape[0])
+
+    def step(prec):
+        return api.forward_gain(geo, dip, el, sq, precision=prec)
+
+    # FP64 drop-in on the same box (its result is the accuracy reference)
+    step("fp64")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f64_times = []
+    for _ in range(max(1, args.fp64_steps)):
+        e0.record()
+        ge64, gm64, st64 = step("fp64")
+        e1.record()
+        torch.cuda.synchronize()
+        f64_times.append(e0.elapsed_time(e1) / 1e3)
+    t_fp64 = float(np.median(f64_times))
+
+    for _ in range(args.warmup):
+        step("mixed")
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = ctx.launches()
+    _lib.profile_enable(True)
+    _lib.profile_read()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        gex, gmx, stx = step("mixed")
+    e1.record()
+    torch.cuda.synchronize()
+    _lib.profile_enable(False)
+    prof = _lib.profile_read()
+    launches = ctx.launches() - launches0
+    ck = clocks.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    t_max = t_step
+    if world > 1:
+        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+        dist.barrier()
+
+    def relerr(a, b):
+        return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+    err_eeg = relerr(gex, ge64)
+    err_meg = relerr(gmx, gm64) if gm64 is not None else None
+
+    # end to end through the C ABI with host buffers: geometry from host arrays + gain_host
+    e2e_times = []
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        s = time.perf_counter()
+        g2 = api.Geometry.from_head(w.head, ctx)
+        api.forward_gain(g2, w.dipoles, w.electrodes, w.squids if nm else None, precision="mixed", host=True)
+        e2e_times.append(time.perf_counter() - s)
+        del g2
+    t_e2e = float(np.median(e2e_times))
+    h2d = sum(a.nbytes for a in w.head.vertices) + sum(a.nbytes for a in w.head.triangles) + \
+        w.dipoles.nbytes + w.electrodes.nbytes + (w.squids.nbytes if nm else 0)
+    d2h = 8 * nd * (ne + nm)
+
+    # roofline of the dominant kernel over the timed region
+    hbm, bf16, bf16_sus, peak_kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
+    dname, (dl, dms) = dom
+    total_prof_ms = sum(v[1] for v in prof.values())
+    roof = roofline_entry(dname, dl, dms, args.steps, N, geo, w, nd, ne + nm, stx, hbm, bf16, bf16_sus, peak_kind)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        total, parts, sample, nthr = cpu_sample_time()
+        cpu = {"value": total, "unit": "s", "cores": nthr, "kind": "port", "sample": sample,
+               "stages_s": {k: round(x, 3) for k, x in parts.items()}}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": t_max / world, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 (mixed); f64 drop-in timed beside it",
+            "data": "synthetic (seeded nested icosphere heads, dipoles, Fibonacci sensors)",
+            "config": {"workload": f"{args.config}: 3-layer ico4 SH-perturbed head, N={N}, {nd} dipoles, {ne} EEG, "
+                                   f"{nm} MEG", "N": N, "dipoles": nd, "eeg": ne, "meg": nm,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs > L2 (2.6 GB head matrix rebuilt each step); no flush"},
+            "fp64_s": t_fp64, "speedup_vs_fp64": t_fp64 / t_step,
+            "rel_err_vs_fp64": {"eeg": err_eeg, "meg": err_meg},
+            "mixed_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stx.items()},
+            "fp64_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st64.items()},
+            "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "path": "omg_geometry_create + omg_gain_host (host buffers, mixed)"},
+            "gpu_launches": int(launches),
+            "kernels_ms_per_step": {k: round(v[1] / args.steps, 3) for k, v in
+                                    sorted(prof.items(), key=lambda kv: -kv[1][1])},
+            "profiled_ms_per_step": round(total_prof_ms / args.steps, 3),
+            "roofline": roof,
+            "clocks": ck,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def roofline_entry(name, launches, ms, steps, N, geo, w, nd, k, st, hbm, bf16, bf16_sus, peak_kind):
+    """achieved = algorithmic work per launch / mean launch time of the dominant kernel."""
+    if launches == 0:
+        return None
+    per_launch_s = ms / 1e3 / launches
+    info = {"kernel": name, "launches_per_step": launches / steps, "mean_launch_ms": ms / launches}
+    if name.startswith("gemm"):
+        # Work of all GEMM launches in a step: FP32 factorization N^3/3, solves
+        # 2*N^2*k per refinement step, FP64 residual 2*N^2*k per step, gain 2*k*N*nd.
+        steps_ref = max(1, int(st.get("refinement_steps", 1)))
+        flops = N ** 3 / 3 + 2 * 2 * N * N * k * steps_ref + 2 * N * N * k * steps_ref + 2 * k * N * nd
+        achieved = flops / steps / (ms / 1e3) * steps / 1e12 if False else flops / (ms / 1e3 / steps) / 1e12
+        info.update({"bound": "tensor", "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s",
+                     "frac": achieved / bf16_sus, "traffic": None,
+                     "note": f"CUDA-core GEMM vs {peak_kind} bf16 sustained peak"})
+    else:
+        T = sum(t.shape[0] for t in w.head.triangles)
+        bytes_per = None
+        if name == "s_block" or name == "d_block":
+            # assembly is FP64-pipe bound; traffic is the per-pair record loads + outputs
+            evals = None
+        info.update({"bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+                     "traffic": None, "note": f"{peak_kind} peaks"})
+    return info
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="config1")
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

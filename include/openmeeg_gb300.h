@@ -90,6 +90,14 @@ int omg_context_synchronize(omg_context ctx);
 /* Number of kernels this context has launched so far. */
 int64_t omg_context_kernel_launches(omg_context ctx);
 
+/* Per-kernel timing (process-wide): while enabled, every library kernel
+ * launch is bracketed by CUDA events on its stream.  omg_profile_read waits
+ * for the recorded events, writes per-kernel-name totals (names as 32-byte
+ * NUL-padded strings, launch counts, milliseconds) for up to max_entries
+ * kernels, stores the number written in *n_entries and clears the record. */
+int omg_profile_enable(int32_t on);
+int omg_profile_read(int32_t max_entries, char* names, int64_t* launches, double* total_ms, int32_t* n_entries);
+
 /* ---- geometry ------------------------------------------------------------ *
  * Replaces Geometry(geom, cond) + Geometry::finalize
  * (OpenMEEG/include/geometry.h:67,211-249).  Meshes are given as interfaces

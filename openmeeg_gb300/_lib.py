@@ -69,6 +69,8 @@ _PROTOS = [
     ("omg_context_set_stream", c_i32, [c_vp, c_vp]),
     ("omg_context_synchronize", c_i32, [c_vp]),
     ("omg_context_kernel_launches", c_i64, [c_vp]),
+    ("omg_profile_enable", c_i32, [c_i32]),
+    ("omg_profile_read", c_i32, [c_i32, ctypes.c_char_p, P_i64, P_dbl, P_i32]),
     ("omg_geometry_create", c_i32, [c_vp, c_i32, P_i64, P_dbl, P_i64, P_i64, c_i32, P_i32, P_i32, P_dbl,
                                     ctypes.POINTER(c_vp)]),
     ("omg_geometry_load", c_i32, [c_vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(c_vp)]),
@@ -111,6 +113,24 @@ def load(path: str = LIB_PATH):
                 f.argtypes = args
             _lib = lib
     return _lib
+
+
+def profile_enable(on: bool = True):
+    check(load().omg_profile_enable(1 if on else 0))
+
+
+def profile_read(max_entries: int = 64):
+    """{kernel name: (launches, total ms)} recorded since the last read."""
+    names = ctypes.create_string_buffer(32 * max_entries)
+    launches = (ctypes.c_int64 * max_entries)()
+    ms = (ctypes.c_double * max_entries)()
+    n = ctypes.c_int32()
+    check(load().omg_profile_read(max_entries, names, launches, ms, ctypes.byref(n)))
+    out = {}
+    for i in range(n.value):
+        nm = names.raw[32 * i:32 * (i + 1)].split(b"\0", 1)[0].decode()
+        out[nm] = (int(launches[i]), float(ms[i]))
+    return out
 
 
 def check(rc: int):

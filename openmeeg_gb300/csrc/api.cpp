@@ -9,11 +9,14 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "omg_internal.h"
 
 namespace omg {
+void profile_enable(bool on);
+std::vector<std::tuple<std::string, int64_t, double>> profile_collect();
 // kernel launchers (bem_kernels.cu)
 void launch_prepare_triangles_order(const DevGeom& g, int order, cudaStream_t s);
 void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
@@ -536,6 +539,29 @@ int omg_context_synchronize(omg_context ctx) {
         OMG_REQUIRE(ctx, "null context");
         set_device(ctx);
         OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int omg_profile_enable(int32_t on) {
+    return guarded([&] { profile_enable(on != 0); });
+}
+
+int omg_profile_read(int32_t max_entries, char* names, int64_t* launches, double* total_ms, int32_t* n_entries) {
+    return guarded([&] {
+        OMG_REQUIRE(max_entries >= 0 && n_entries, "bad arguments");
+        auto v = profile_collect();
+        int32_t n = 0;
+        for (const auto& e : v) {
+            if (n >= max_entries) break;
+            if (names) {
+                std::memset(names + 32 * n, 0, 32);
+                std::strncpy(names + 32 * n, std::get<0>(e).c_str(), 31);
+            }
+            if (launches) launches[n] = std::get<1>(e);
+            if (total_ms) total_ms[n] = std::get<2>(e);
+            ++n;
+        }
+        *n_entries = n;
     });
 }
 

@@ -13,6 +13,8 @@
 // FP64 results agree with the reference to rounding.
 #include <algorithm>
 #include <cstdio>
+#include <string>
+#include <tuple>
 #include <vector>
 
 #include "device_common.cuh"
@@ -63,6 +65,49 @@ __constant__ int c_nbpts[4] = {3, 6, 7, 16};
 static int64_t g_launches = 0;
 int64_t kernel_launch_count() { return g_launches; }
 void count_launch(int n) { g_launches += n; }
+
+// ---- launch profiler (events pooled; aggregated on read) ----
+struct ProfEntry {
+    const char* name;
+    cudaEvent_t a, b;
+};
+static bool g_prof = false;
+static std::vector<ProfEntry> g_prof_entries;
+static std::vector<cudaEvent_t> g_prof_pool;
+bool profiling_enabled() { return g_prof; }
+cudaEvent_t profile_event() {
+    if (!g_prof_pool.empty()) {
+        cudaEvent_t e = g_prof_pool.back();
+        g_prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+void profile_record(const char* name, cudaEvent_t a, cudaEvent_t b) { g_prof_entries.push_back({name, a, b}); }
+void profile_enable(bool on) { g_prof = on; }
+// Aggregates recorded launches per name (synchronizes on each event).
+std::vector<std::tuple<std::string, int64_t, double>> profile_collect() {
+    std::vector<std::tuple<std::string, int64_t, double>> out;
+    for (auto& e : g_prof_entries) {
+        cudaEventSynchronize(e.b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e.a, e.b);
+        bool found = false;
+        for (auto& o : out)
+            if (std::get<0>(o) == e.name) {
+                std::get<1>(o) += 1;
+                std::get<2>(o) += ms;
+                found = true;
+            }
+        if (!found) out.emplace_back(e.name, 1, (double)ms);
+        g_prof_pool.push_back(e.a);
+        g_prof_pool.push_back(e.b);
+    }
+    g_prof_entries.clear();
+    return out;
+}
 
 static inline void check_launch(const char* what) {
     cudaError_t e = cudaGetLastError();
@@ -137,6 +182,7 @@ __global__ void prepare_triangles_kernel(int64_t nt, const double* __restrict__ 
 }
 
 void launch_prepare_triangles_order(const DevGeom& g, int order, cudaStream_t s) {
+    ProfScope prof_("prepare_triangles", s);
     prepare_triangles_kernel<<<nblocks(g.nt, 128), 128, 0, s>>>(g.nt, g.V, g.T, order, g.srec, g.prec, g.qrec);
     check_launch("prepare_triangles");
 }
@@ -192,6 +238,7 @@ __global__ void __launch_bounds__(S_THREADS) s_block_kernel(const double* __rest
 void launch_S_block(const DevGeom& g, int64_t t1b, int64_t t1e, int64_t t2b, int64_t t2e, bool same, double coeff,
                     int order, double* hm, int64_t ld, double* tmp, int* err, cudaStream_t s) {
     const int64_t n1 = t1e - t1b, n2 = t2e - t2b;
+    ProfScope prof_("s_block", s);
     dim3 grid(nblocks(n2, S_TJ), nblocks(n1, S_TI));
     const size_t sm = (size_t)(S_TI * SREC + S_TJ * QREC) * 8;
     static bool attr = false;
@@ -249,6 +296,7 @@ __global__ void __launch_bounds__(D_THREADS) d_block_kernel(const double* __rest
 void launch_D_block(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int64_t tbe, int order, double* tmp,
                     int* err, cudaStream_t s) {
     const int64_t na = tae - tab, nb = tbe - tbb;
+    ProfScope prof_("d_block", s);
     dim3 grid(nblocks(nb, D_TJ), nblocks(na, D_TI));
     const size_t sm = (size_t)(D_TI * QREC + D_TJ * PREC) * 8;
     static bool attr = false;
@@ -281,6 +329,7 @@ __global__ void d_gather_kernel(int64_t tab, int64_t na, int64_t tbb, int64_t nb
 
 void launch_D_gather(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int64_t tbe, int64_t vbb, int64_t vbe,
                      double coeff, const double* tmp, double* hm, int64_t ld, cudaStream_t s) {
+    ProfScope prof_("d_gather", s);
     const int64_t n = (tae - tab) * (vbe - vbb);
     d_gather_kernel<<<nblocks(n, 256), 256, 0, s>>>(tab, tae - tab, tbb, tbe - tbb, vbb, vbe - vbb, coeff, tmp,
                                                     g.v2t_beg, g.v2t_tri, g.v2t_loc, g.tpos, g.nP, hm, ld);
@@ -336,6 +385,7 @@ void launch_N_block(const DevGeom& g, int64_t v1b, int64_t v1e, int64_t t1b, int
                     int64_t t2b, int64_t t2e, bool same, double coeff, const double* hm_src, int64_t ld,
                     const double* tmp, double* hm, cudaStream_t s) {
     const int64_t n = (v1e - v1b) * (v2e - v2b);
+    ProfScope prof_("n_block", s);
     n_block_kernel<<<nblocks(n, 256), 256, 0, s>>>(v1b, v1e - v1b, t1b, t1e, v2b, v2e - v2b, t2b, t2e, same ? 1 : 0,
                                                    coeff, hm_src, ld, tmp, g.V, g.T, g.srec, g.v2t_beg, g.v2t_tri,
                                                    g.v2t_loc, g.tpos, g.nP, hm);
@@ -360,6 +410,7 @@ __global__ void deflate_add_kernel(int64_t vb, int64_t n, int64_t nP, const doub
 
 void launch_deflate(const DevGeom& g, const std::vector<std::pair<int64_t, int64_t>>& vranges, int64_t i_first,
                     int64_t nb, double* hm, int64_t ld, double* scratch, cudaStream_t s) {
+    ProfScope prof_("deflate", s);
     const int64_t pos = g.nP + i_first;
     deflate_coef_kernel<<<1, 1, 0, s>>>(hm, pos, ld, 1.0 / (double)nb, scratch);
     check_launch("deflate coef");
@@ -396,6 +447,7 @@ __global__ void to_reference_packed_kernel(int64_t N, int64_t nv, int64_t nP, co
 
 void launch_symmetrize_to_reference(const DevGeom& g, const double* hm_int, int64_t ld_int, double* out,
                                     int64_t ld_out, bool packed, cudaStream_t s) {
+    ProfScope prof_("to_reference", s);
     dim3 grid(nblocks(g.N, 256), (unsigned)std::min<int64_t>(g.N, 32768));
     if (packed)
         to_reference_packed_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, hm_int, ld_int, out);
@@ -417,6 +469,7 @@ __global__ void from_reference_dense_kernel(int64_t N, int64_t nv, int64_t nP, c
 
 void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
                                  cudaStream_t s) {
+    ProfScope prof_("from_reference", s);
     dim3 grid(nblocks(g.N, 256), (unsigned)std::min<int64_t>(g.N, 32768));
     from_reference_dense_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, in, ldi, hm, ld);
     check_launch("from reference");
@@ -832,6 +885,7 @@ __global__ void ds2mm_kernel(const double* __restrict__ dip, int64_t nd, const d
 void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
                               const double* srec, double* out, cudaStream_t s) {
     if (n == 0) return;
+    ProfScope prof_("solid_angles", s);
     mesh_solid_angles_kernel<<<(unsigned)n, 256, 0, s>>>(pts, pstride, nmesh, tbeg_dev, srec, out);
     check_launch("mesh solid angles");
 }
@@ -839,6 +893,7 @@ void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int
 void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int maxb, const int* dnb,
                           const int* bmesh, const int* binside, const int* orient, int forced, int* dom, int* err,
                           cudaStream_t s) {
+    ProfScope prof_("domain_lookup", s);
     if (n == 0) return;
     domain_lookup_kernel<<<nblocks(n, 128), 128, 0, s>>>(n, nmesh, sa, ndom, maxb, dnb, bmesh, binside, orient,
                                                          forced, dom, err);
@@ -849,6 +904,7 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
                 const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
                 const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
                 double tol, int perm, double* out, int64_t ldo, double* p1tmp, cudaStream_t s) {
+    ProfScope prof_("dsm", s);
     if (ndc == 0) return;
     dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
     dsm_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, tmesh, tidx_ref, barrier, orient, dom, maxb, dnb,
@@ -863,6 +919,7 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
 void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
                  double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s) {
     if (ne == 0) return;
+    ProfScope prof_("h2em", s);
     h2em_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, ncand, cand, g.srec, g.T, g.nP, perm, dense, rs, cs, col0, scols,
                                              svals);
     check_launch("H2EM");
@@ -870,6 +927,7 @@ void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand,
 
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
                  double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s) {
+    ProfScope prof_("h2mm", s);
     if (np == 0) return;
     dim3 grid(nblocks(g.nt, 128), (unsigned)np);
     ferguson_s_kernel<<<grid, 128, 0, s>>>(sq, np, g.nt, g.srec, F);
@@ -882,6 +940,7 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
 
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s) {
+    ProfScope prof_("ds2mm", s);
     if (nd == 0 || np == 0) return;
     dim3 grid(nblocks(np, 128), (unsigned)nd);
     ds2mm_kernel<<<grid, 128, 0, s>>>(dip, nd, sq, np, out, ldo);

@@ -97,6 +97,7 @@ template <typename T>
 void gemm(int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, bool ta, const T* B, int64_t ldb, bool tb,
           T beta, T* C, int64_t ldc, cudaStream_t s, bool lower = false, int64_t row0 = 0, int64_t col0 = 0) {
     if (M <= 0 || N <= 0) return;
+    ProfScope prof_(sizeof(T) == 8 ? "gemm_f64" : "gemm_f32", s);
     constexpr bool dbl = sizeof(T) == 8;
     constexpr int BM = dbl ? 64 : 128, BN = dbl ? 64 : 128, BK = 8, TM = dbl ? 4 : 8, TN = dbl ? 4 : 8;
     dim3 grid(nblk(N, BN), nblk(M, BM));
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(512) potrf_trinv_kernel(T* A, int64_t lda, int
 template <typename T>
 void potrf_trinv(T* A, int64_t lda, int n, T* Linv, int ldi, int* err, int64_t* err_col, int64_t col_offset,
                  cudaStream_t s) {
+    ProfScope prof_("potrf_trinv", s);
     const size_t sm = 2 * (size_t)n * n * sizeof(T);
     if (sm > 227 * 1024) throw Error(OMG_ERR_INVALID, "diagonal block too large for shared memory");
     static bool attr = false;
@@ -193,6 +195,7 @@ __global__ void negate_lower_kernel(T* A, int64_t lda, int64_t n) {
 }
 template <typename T>
 void negate_lower(T* A, int64_t lda, int64_t n, cudaStream_t s) {
+    ProfScope prof_("negate_lower", s);
     if (n <= 0) return;
     dim3 grid(nblk(n, 256), (unsigned)std::min<int64_t>(n, 32768));
     negate_lower_kernel<T><<<grid, 256, 0, s>>>(A, lda, n);
@@ -214,6 +217,7 @@ __global__ void copy_convert_kernel(int64_t m, int64_t n, const Tin* __restrict_
 template <typename Tin, typename Tout>
 void copy_convert(int64_t m, int64_t n, const Tin* a, int64_t lda, Tout* b, int64_t ldb, bool lower, Tout scale,
                   cudaStream_t s) {
+    ProfScope prof_("copy_convert", s);
     if (m <= 0 || n <= 0) return;
     dim3 grid(nblk(m, 256), (unsigned)std::min<int64_t>(n, 32768));
     copy_convert_kernel<Tin, Tout><<<grid, 256, 0, s>>>(m, n, a, lda, b, ldb, lower ? 1 : 0, scale);
@@ -245,6 +249,7 @@ __global__ void symmetrize_kernel(double* A, int64_t lda, int64_t n) {
     }
 }
 void symmetrize(double* A, int64_t lda, int64_t n, cudaStream_t s) {
+    ProfScope prof_("symmetrize", s);
     const int64_t nt = (n + 31) / 32;
     if (nt > 65535) throw Error(OMG_ERR_UNSUPPORTED, "matrix too large to symmetrize");
     dim3 grid((unsigned)nt, (unsigned)nt);
@@ -261,6 +266,7 @@ __global__ void negate_rows_kernel(T* B, int64_t ldb, int64_t r0, int64_t r1, in
 }
 template <typename T>
 void negate_rows(T* B, int64_t ldb, int64_t r0, int64_t r1, int64_t n, cudaStream_t s) {
+    ProfScope prof_("negate_rows", s);
     if (r1 <= r0 || n <= 0) return;
     dim3 grid(nblk(r1 - r0, 256), (unsigned)std::min<int64_t>(n, 32768));
     negate_rows_kernel<T><<<grid, 256, 0, s>>>(B, ldb, r0, r1, n);
@@ -287,6 +293,7 @@ __global__ void col_norms_kernel(int64_t m, const double* __restrict__ A, int64_
     if (threadIdx.x == 0) out[j] = sqrt(red[0]);
 }
 void col_norms(int64_t m, int64_t n, const double* A, int64_t lda, double* out, cudaStream_t s) {
+    ProfScope prof_("col_norms", s);
     if (n <= 0) return;
     col_norms_kernel<<<(unsigned)n, 256, 0, s>>>(m, A, lda, out);
     check("col_norms");
@@ -302,6 +309,7 @@ __global__ void axpy_f32_kernel(int64_t m, int64_t n, const float* __restrict__ 
 }
 void axpy_f32(int64_t m, int64_t n, const float* d, int64_t ldd, double* x, int64_t ldx, const double* colscale,
               cudaStream_t s) {
+    ProfScope prof_("axpy_f32", s);
     dim3 grid(nblk(m, 256), (unsigned)std::min<int64_t>(n, 32768));
     axpy_f32_kernel<<<grid, 256, 0, s>>>(m, n, d, ldd, x, ldx, colscale);
     check("axpy_f32");
@@ -320,6 +328,7 @@ __global__ void scale_to_f32_kernel(int64_t m, int64_t n, const double* __restri
 }
 void scale_to_f32(int64_t m, int64_t n, const double* r, int64_t ldr, float* b, int64_t ldb, const double* colnorm,
                   double* colscale, cudaStream_t s) {
+    ProfScope prof_("scale_to_f32", s);
     dim3 grid(nblk(m, 256), (unsigned)std::min<int64_t>(n, 32768));
     scale_to_f32_kernel<<<grid, 256, 0, s>>>(m, n, r, ldr, b, ldb, colnorm, colscale);
     check("scale_to_f32");

@@ -132,4 +132,29 @@ void launch_symmetrize_to_reference(const DevGeom& g, const double* hm_int, int6
 int64_t kernel_launch_count();
 void count_launch(int n = 1);
 
+// Optional per-launch timing: when enabled, every launcher brackets its
+// kernel with CUDA events on the launch stream; omg_profile_read() aggregates
+// them per kernel name.
+bool profiling_enabled();
+void profile_record(const char* name, cudaEvent_t start, cudaEvent_t stop);
+cudaEvent_t profile_event();
+struct ProfScope {
+    const char* name;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    ProfScope(const char* n, cudaStream_t st) : name(n), s(st) {
+        if (profiling_enabled()) {
+            a = profile_event();
+            cudaEventRecord(a, s);
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEvent_t b = profile_event();
+            cudaEventRecord(b, s);
+            profile_record(name, a, b);
+        }
+    }
+};
+
 }  // namespace omg
