@@ -36,6 +36,14 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
                  double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s);
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
+void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s);
+void launch_ff_block(const DevGeom& g, const float* grec, int64_t t1b, int64_t t1e, int64_t t2b, int64_t t2e,
+                     bool same, bool wantS, bool wantD12, bool wantD21, double cS, double* hm, int64_t ld,
+                     double* stmp, double* d12, double* d21, int2* near, int* near_count, int near_cap, float rho,
+                     int* err, cudaStream_t s);
+void launch_near_pairs(const DevGeom& g, const int2* near, int count, int64_t t1b, int64_t t1e, int64_t t2b,
+                       int64_t t2e, bool same, bool wantS, bool wantD12, bool wantD21, double cS, int order,
+                       double* hm, int64_t ld, double* stmp, double* d12, double* d21, cudaStream_t s);
 // dense_kernels.cu
 template <typename T>
 void gemm(int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, bool ta, const T* B, int64_t ldb, bool tb,
@@ -129,6 +137,7 @@ struct omg_geometry_s {
     int* binside = nullptr;
     double* dsigma = nullptr;
     int prepared_order = -1;
+    float* grec = nullptr;      // FP32 far-field records (mixed precision), built on first use
 };
 
 struct omg_solver_s {
@@ -323,6 +332,82 @@ static void assemble_headmat_internal(omg_geometry g, const omg_integrator& inte
     }
 }
 
+// Mixed precision: far pairs by the FP32 product rule, near pairs (centroid
+// distance < kRhoFar x larger max edge) by the FP64 analytic kernels.
+constexpr float kRhoFar = 2.0f;
+
+static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld) {
+    omg_context ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    const HostGeometry& h = g->h;
+    const DevGeom& d = g->d;
+    check_integrator(integ, false);
+    OMG_REQUIRE(integ.order == 3, "mixed-precision assembly uses the 16-point rule (integrator order 3)");
+    ensure_order(g, 3);
+    if (!g->grec) {
+        g->bufs.emplace_back((size_t)h.nt * 64 * sizeof(float), s);
+        g->grec = g->bufs.back().as<float>();
+        launch_prepare_gg(d, g->grec, s);
+    }
+    OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)h.N, s));
+    DevBuf counter(sizeof(int), s);
+    for (const auto& p : h.pairs) {
+        const int m1 = p.m1, m2 = p.m2;
+        const bool same = (m1 == m2);
+        const int64_t t1b = h.tbeg[m1], t1e = h.tbeg[m1 + 1], t2b = h.tbeg[m2], t2e = h.tbeg[m2 + 1];
+        const int64_t v1b = h.vbeg[m1], v1e = h.vbeg[m1 + 1], v2b = h.vbeg[m2], v2e = h.vbeg[m2 + 1];
+        const int64_t n1 = t1e - t1b, n2 = t2e - t2b;
+        const bool sInHM = same ? !h.barrier[m1] : (!h.barrier[m1] && !h.barrier[m2]);
+        const bool wantD12 = !h.barrier[m1];
+        const bool wantD21 = !same && !h.barrier[m2];
+        DevBuf stmp(sInHM ? 0 : (size_t)n1 * n2 * 8, s);
+        DevBuf d12(wantD12 ? (size_t)n1 * n2 * 24 : 0, s), d21(wantD21 ? (size_t)n1 * n2 * 24 : 0, s);
+        const int64_t npairs = same ? n1 * (n1 + 1) / 2 : n1 * n2;
+        int cap = (int)std::min<int64_t>(npairs, std::max<int64_t>(1 << 22, npairs / 8));
+        int count = 0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            DevBuf nearb((size_t)cap * sizeof(int2), s);
+            OMG_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(int), s));
+            launch_ff_block(d, g->grec, t1b, t1e, t2b, t2e, same, true, wantD12, wantD21, p.cS,
+                            sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(), d21.as<double>(),
+                            nearb.as<int2>(), counter.as<int>(), cap, kRhoFar, ctx->d_err, s);
+            OMG_CUDA(cudaMemcpyAsync(&count, counter.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            OMG_CUDA(cudaStreamSynchronize(s));
+            if (count <= cap) {
+                launch_near_pairs(d, nearb.as<int2>(), count, t1b, t1e, t2b, t2e, same, true, wantD12, wantD21, p.cS,
+                                  3, sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(), d21.as<double>(),
+                                  s);
+                break;
+            }
+            cap = count;   // rerun with room for every near pair (far writes are idempotent)
+        }
+        if (sInHM)
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / p.cS, hm, ld, nullptr, hm, s);
+        else
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN, nullptr, ld, stmp.as<double>(), hm,
+                           s);
+        if (wantD12) launch_D_gather(d, t1b, t1e, t2b, t2e, v2b, v2e, p.cD, d12.as<double>(), hm, ld, s);
+        if (wantD21) launch_D_gather(d, t2b, t2e, t1b, t1e, v1b, v1e, p.cD, d21.as<double>(), hm, ld, s);
+    }
+    for (const auto& part : h.part_outermost) {
+        int64_t nb = 0, i_first = 0;
+        std::vector<std::pair<int64_t, int64_t>> ranges;
+        for (int m : part) {
+            nb += h.vbeg[m + 1] - h.vbeg[m];
+            if (i_first == 0) i_first = h.vbeg[m];
+            ranges.push_back({h.vbeg[m], h.vbeg[m + 1]});
+        }
+        if (nb > 0) launch_deflate(d, ranges, i_first, nb, hm, ld, ctx->d_scalar, s);
+    }
+}
+
+static void assemble(omg_geometry g, const omg_integrator& integ, int precision, double* hm, int64_t ld) {
+    if (precision == OMG_PREC_MIXED)
+        assemble_headmat_mixed(g, integ, hm, ld);
+    else
+        assemble_headmat_internal(g, integ, hm, ld);
+}
+
 // ---------------------------------------------------------------------------
 // Factorization: HM = L diag(+I_P, -I_V) L^T, blocked right-looking.
 // ---------------------------------------------------------------------------
@@ -379,11 +464,13 @@ static void solve_ldlt(omg_solver sv, const T* A, int64_t ld, T* B, int64_t ldb,
         if (k1 < N) gemm<T>(N - k1, nrhs, nk, T(-1), A + k1 + k0 * ld, ld, false, w, nk, false, T(1), B + k1, ldb, s);
     }
     negate_rows<T>(B, ldb, sv->nP, N, nrhs, s);
+    // L^T x = y, right-looking: once block k is solved, remove its
+    // contribution from all earlier blocks (K = block size, M = k0).
     for (size_t bb = nblocks; bb-- > 0;) {
         const int64_t k0 = sv->bounds[bb], k1 = sv->bounds[bb + 1], nk = k1 - k0;
-        if (k1 < N) gemm<T>(nk, nrhs, N - k1, T(-1), A + k1 + k0 * ld, ld, true, B + k1, ldb, false, T(1), B + k0, ldb, s);
         gemm<T>(nk, nrhs, nk, T(1), Li + sv->linv_off[bb], nk, true, B + k0, ldb, false, T(0), w, nk, s);
         copy_convert<T, T>(nk, nrhs, w, nk, B + k0, ldb, false, T(1), s);
+        if (k0 > 0) gemm<T>(k0, nrhs, nk, T(-1), A + k0, ld, true, w, nk, false, T(1), B, ldb, s);
     }
 }
 
@@ -658,7 +745,7 @@ int omg_headmat_dev(omg_context ctx, omg_geometry geo, const omg_integrator* int
         const omg_integrator it = integ ? *integ : default_hm_integrator();
         const int64_t N = geo->h.N;
         DevBuf tmp((size_t)N * N * 8, ctx->stream);
-        assemble_headmat_internal(geo, it, tmp.as<double>(), N);
+        assemble(geo, it, precision, tmp.as<double>(), N);
         launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, hm, ld, false, ctx->stream);
         check_err(ctx, "HeadMat");
     });
@@ -744,7 +831,7 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
         sv->nP = geo->h.nP;
         DevBuf hm((size_t)sv->N * sv->N * 8, ctx->stream);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
-        assemble_headmat_internal(geo, it, hm.as<double>(), sv->N);
+        assemble(geo, it, precision, hm.as<double>(), sv->N);
         check_err(ctx, "HeadMat");
         solver_factor(sv.get(), std::move(hm));
         *out = sv.release();
@@ -820,7 +907,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     sv->N = N;
     sv->nP = geo->h.nP;
     DevBuf hm((size_t)N * N * 8, s);
-    assemble_headmat_internal(geo, hm_it, hm.as<double>(), N);
+    assemble(geo, hm_it, precision, hm.as<double>(), N);
     OMG_CUDA(cudaEventRecord(ev[1], s));
     // right-hand sides (internal numbering) and DSM
     DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);

@@ -476,6 +476,251 @@ void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi
 }
 
 // ===========================================================================
+// Mixed-precision HeadMat assembly
+//
+// Far pairs (centroid distance >= rho_far x the larger max edge) are computed
+// by a 16 x 16 Gauss product rule in FP32 -- the same outer rule as the
+// reference, with the analytic inner integral replaced by the rule on the
+// other triangle.  Coordinates are taken relative to each triangle's centroid
+// and the centroid difference is formed in FP64 before rounding, so the FP32
+// distances carry no cancellation.  One pass over a triangle pair yields S,
+// D(t1 -> vertices of t2) and D(t2 -> vertices of t1): the 256 point-point
+// distances are shared.  Near pairs are appended to a list and recomputed
+// with the FP64 analytic kernels.
+// ===========================================================================
+constexpr int GREC = 64;   // floats per triangle: centroid (3 doubles), 16 offsets, normal, h, area (double)
+__constant__ float c_w16[16];
+__constant__ float c_b16[16][3];
+
+__global__ void prepare_gg_kernel(int64_t nt, const double* __restrict__ V, const int32_t* __restrict__ T,
+                                  float* grec) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const d3 p0 = dev::ld3(V + 3 * (int64_t)T[3 * t]);
+    const d3 p1 = dev::ld3(V + 3 * (int64_t)T[3 * t + 1]);
+    const d3 p2 = dev::ld3(V + 3 * (int64_t)T[3 * t + 2]);
+    const d3 c = (p0 + p1 + p2) * (1.0 / 3.0);
+    float* g = grec + t * GREC;
+    double* gc = reinterpret_cast<double*>(g);
+    gc[0] = c.x; gc[1] = c.y; gc[2] = c.z;
+    for (int k = 0; k < 16; ++k) {
+        const d3 v = bary_point(c_rules[3][k], p0, p1, p2) - c;
+        g[6 + 3 * k] = (float)v.x; g[7 + 3 * k] = (float)v.y; g[8 + 3 * k] = (float)v.z;
+    }
+    const d3 nn = dev::cross(p1 - p0, p2 - p0);
+    const double nrm = dev::norm(nn);
+    g[54] = (float)(nn.x / nrm); g[55] = (float)(nn.y / nrm); g[56] = (float)(nn.z / nrm);
+    g[57] = (float)fmax(dev::norm(p1 - p0), fmax(dev::norm(p2 - p1), dev::norm(p0 - p2)));
+    reinterpret_cast<double*>(g + 58)[0] = 0.5 * nrm;
+    g[60] = g[61] = g[62] = g[63] = 0.f;
+}
+
+void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s) {
+    ProfScope prof_("prepare_gg", s);
+    static bool init = false;
+    if (!init) {
+        float w[16], b[16][3];
+        for (int k = 0; k < 16; ++k) {
+            static const double R[16][4] = {
+                {0.333333333333333, 0.333333333333333, 0.333333333333333, 0.144315607677786},
+                {0.081414823414554, 0.459292588292722, 0.459292588292722, 0.095091634267284},
+                {0.459292588292722, 0.081414823414554, 0.459292588292722, 0.095091634267284},
+                {0.459292588292722, 0.459292588292722, 0.081414823414554, 0.095091634267284},
+                {0.898905543365937, 0.050547228317031, 0.050547228317031, 0.032458497623198},
+                {0.050547228317031, 0.898905543365937, 0.050547228317031, 0.032458497623198},
+                {0.050547228317031, 0.050547228317031, 0.898905543365937, 0.032458497623198},
+                {0.658861384496479, 0.170569307751760, 0.170569307751761, 0.103217370534718},
+                {0.170569307751760, 0.658861384496479, 0.170569307751761, 0.103217370534718},
+                {0.170569307751760, 0.170569307751761, 0.658861384496479, 0.103217370534718},
+                {0.008394777409957, 0.728492392955404, 0.263112829634639, 0.027230314174434},
+                {0.728492392955404, 0.008394777409957, 0.263112829634639, 0.027230314174434},
+                {0.728492392955404, 0.263112829634639, 0.008394777409957, 0.027230314174434},
+                {0.008394777409957, 0.263112829634639, 0.728492392955404, 0.027230314174434},
+                {0.263112829634639, 0.008394777409957, 0.728492392955404, 0.027230314174434},
+                {0.263112829634639, 0.728492392955404, 0.008394777409957, 0.027230314174434}};
+            w[k] = (float)R[k][3];
+            for (int i = 0; i < 3; ++i) b[k][i] = (float)R[k][i];
+        }
+        cudaMemcpyToSymbol(c_w16, w, sizeof(w));
+        cudaMemcpyToSymbol(c_b16, b, sizeof(b));
+        init = true;
+    }
+    prepare_gg_kernel<<<nblocks(g.nt, 128), 128, 0, s>>>(g.nt, g.V, g.T, grec);
+    check_launch("prepare_gg");
+}
+
+constexpr int FF_TI = 128, FF_TJ = 32;
+
+// One thread per t1 row, looping over the CTA's FF_TJ staged t2 records.
+__global__ void __launch_bounds__(FF_TI) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
+                                                         int64_t t2b, int64_t n2, int same, int wantS, int wantD12,
+                                                         int wantD21, double cS, const int32_t* __restrict__ tpos,
+                                                         double* hm, int64_t ld, double* stmp, double* d12,
+                                                         double* d21, int2* near, int* near_count, int near_cap,
+                                                         float rho, int* err) {
+    __shared__ __align__(16) float sJ[FF_TJ * GREC];
+    __shared__ __align__(8) uint64_t bar;
+    const int64_t i0 = (int64_t)blockIdx.y * FF_TI, j0 = (int64_t)blockIdx.x * FF_TJ;
+    if (same && j0 + FF_TJ <= i0) return;
+    const int nj = (int)(n2 - j0 < (int64_t)FF_TJ ? n2 - j0 : (int64_t)FF_TJ);
+    if (!dev::stage_two(sJ, grec + (t2b + j0) * GREC, (uint32_t)(nj * GREC * 4), nullptr, nullptr, 0, &bar, err))
+        return;
+    const int64_t i = i0 + threadIdx.x;
+    if (i >= n1) return;
+    const float* g1 = grec + (t1b + i) * GREC;
+    const double* c1p = reinterpret_cast<const double*>(g1);
+    const double c1x = c1p[0], c1y = c1p[1], c1z = c1p[2];
+    float p1[16][3];
+#pragma unroll
+    for (int p = 0; p < 16; ++p) {
+        p1[p][0] = g1[6 + 3 * p]; p1[p][1] = g1[7 + 3 * p]; p1[p][2] = g1[8 + 3 * p];
+    }
+    const float n1x = g1[54], n1y = g1[55], n1z = g1[56], h1 = g1[57];
+    const double A1 = reinterpret_cast<const double*>(g1 + 58)[0];
+    for (int jj = 0; jj < nj; ++jj) {
+        const int64_t j = j0 + jj;
+        if (same && j < i) continue;
+        const float* g2 = sJ + jj * GREC;
+        const double* c2p = reinterpret_cast<const double*>(g2);
+        const double dx = c2p[0] - c1x, dy = c2p[1] - c1y, dz = c2p[2] - c1z;
+        const float hmax = fmaxf(h1, g2[57]);
+        const float dist2 = (float)(dx * dx + dy * dy + dz * dz);
+        if (dist2 < rho * rho * hmax * hmax) {
+            const int slot = atomicAdd(near_count, 1);
+            if (slot < near_cap) near[slot] = make_int2((int)i, (int)j);
+            continue;
+        }
+        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+        const float n2x = g2[54], n2y = g2[55], n2z = g2[56];
+        float acc21[16];
+#pragma unroll
+        for (int p = 0; p < 16; ++p) acc21[p] = 0.f;
+        float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
+        for (int q = 0; q < 16; ++q) {
+            const float yx = fx + g2[6 + 3 * q], yy = fy + g2[7 + 3 * q], yz = fz + g2[8 + 3 * q];
+            const float wq = c_w16[q];
+            float sq = 0.f, k12 = 0.f;
+#pragma unroll
+            for (int p = 0; p < 16; ++p) {
+                const float rx = yx - p1[p][0], ry = yy - p1[p][1], rz = yz - p1[p][2];
+                const float ir = rsqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
+                const float ir3 = ir * ir * ir;
+                const float wp = c_w16[p];
+                sq = fmaf(wp, ir, sq);
+                k12 = fmaf(wp * ir3, fmaf(rx, n2x, fmaf(ry, n2y, rz * n2z)), k12);
+                acc21[p] = fmaf(-wq * ir3, fmaf(rx, n1x, fmaf(ry, n1y, rz * n1z)), acc21[p]);
+            }
+            s = fmaf(wq, sq, s);
+            const float kq = wq * k12;
+            e0 = fmaf(kq, c_b16[q][0], e0);
+            e1 = fmaf(kq, c_b16[q][1], e1);
+            e2 = fmaf(kq, c_b16[q][2], e2);
+        }
+        const double AA = A1 * reinterpret_cast<const double*>(g2 + 58)[0];
+        if (wantS) {
+            if (hm)
+                hm[lower_at(tpos[t1b + i], tpos[t2b + j], ld)] = (double)s * AA * cS;
+            else {
+                stmp[i * n2 + j] = (double)s * AA;
+                if (same) stmp[j * n2 + i] = (double)s * AA;
+            }
+        }
+        if (wantD12) {
+            double* o = d12 + (i * n2 + j) * 3;
+            o[0] = (double)e0 * AA; o[1] = (double)e1 * AA; o[2] = (double)e2 * AA;
+        }
+        if (wantD21 || (same && wantD12)) {
+            float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+#pragma unroll
+            for (int p = 0; p < 16; ++p) {
+                const float a = c_w16[p] * acc21[p];
+                f0 = fmaf(a, c_b16[p][0], f0);
+                f1 = fmaf(a, c_b16[p][1], f1);
+                f2 = fmaf(a, c_b16[p][2], f2);
+            }
+            double* o = same ? d12 + (j * n2 + i) * 3 : d21 + (j * n1 + i) * 3;
+            o[0] = (double)f0 * AA; o[1] = (double)f1 * AA; o[2] = (double)f2 * AA;
+        }
+    }
+}
+
+// Near pairs: the FP64 analytic kernels of the reference (same outer rule).
+__global__ void near_pairs_kernel(const int2* __restrict__ near, int count, const double* __restrict__ srec,
+                                  const double* __restrict__ prec, const double* __restrict__ qrec, int64_t t1b,
+                                  int64_t n1, int64_t t2b, int64_t n2, int same, int wantS, int wantD12, int wantD21,
+                                  double cS, int order, const int32_t* __restrict__ tpos, double* hm, int64_t ld,
+                                  double* stmp, double* d12, double* d21) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t i = near[k].x, j = near[k].y;
+    const int64_t a = t1b + i, b = t2b + j;
+    const int np = c_nbpts[order];
+    if (wantS) {
+        const double* S1 = srec + a * SREC;
+        const double* q2 = qrec + b * QREC;
+        double acc = 0.0;
+        for (int m = 0; m < np; ++m) acc += c_rules[order][m][3] * dev::operator_S(S1, dev::ld3(q2 + 3 * m));
+        const double val = q2[48] * acc;
+        if (hm)
+            hm[lower_at(tpos[a], tpos[b], ld)] = val * cS;
+        else {
+            stmp[i * n2 + j] = val;
+            if (same) stmp[j * n2 + i] = val;
+        }
+    }
+    if (wantD12) {   // integral over t1 of P1SLP(t2)
+        const double* q1 = qrec + a * QREC;
+        const double* P2 = prec + b * PREC;
+        double acc[3] = {0, 0, 0};
+        for (int m = 0; m < np; ++m) {
+            double v[3];
+            dev::p1_single_layer(P2, dev::ld3(q1 + 3 * m), v);
+            const double w = c_rules[order][m][3];
+            acc[0] += w * v[0]; acc[1] += w * v[1]; acc[2] += w * v[2];
+        }
+        double* o = d12 + (i * n2 + j) * 3;
+        o[0] = q1[48] * acc[0]; o[1] = q1[48] * acc[1]; o[2] = q1[48] * acc[2];
+    }
+    if ((wantD21 || (same && wantD12)) && !(same && i == j)) {   // integral over t2 of P1SLP(t1)
+        const double* q2 = qrec + b * QREC;
+        const double* P1 = prec + a * PREC;
+        double acc[3] = {0, 0, 0};
+        for (int m = 0; m < np; ++m) {
+            double v[3];
+            dev::p1_single_layer(P1, dev::ld3(q2 + 3 * m), v);
+            const double w = c_rules[order][m][3];
+            acc[0] += w * v[0]; acc[1] += w * v[1]; acc[2] += w * v[2];
+        }
+        double* o = same ? d12 + (j * n2 + i) * 3 : d21 + (j * n1 + i) * 3;
+        o[0] = q2[48] * acc[0]; o[1] = q2[48] * acc[1]; o[2] = q2[48] * acc[2];
+    }
+}
+
+void launch_ff_block(const DevGeom& g, const float* grec, int64_t t1b, int64_t t1e, int64_t t2b, int64_t t2e,
+                     bool same, bool wantS, bool wantD12, bool wantD21, double cS, double* hm, int64_t ld,
+                     double* stmp, double* d12, double* d21, int2* near, int* near_count, int near_cap, float rho,
+                     int* err, cudaStream_t s) {
+    ProfScope prof_("ff_block", s);
+    const int64_t n1 = t1e - t1b, n2 = t2e - t2b;
+    dim3 grid(nblocks(n2, FF_TJ), nblocks(n1, FF_TI));
+    ff_block_kernel<<<grid, FF_TI, 0, s>>>(grec, t1b, n1, t2b, n2, same ? 1 : 0, wantS ? 1 : 0, wantD12 ? 1 : 0,
+                                           wantD21 ? 1 : 0, cS, g.tpos, hm, ld, stmp, d12, d21, near, near_count,
+                                           near_cap, rho, err);
+    check_launch("ff block");
+}
+
+void launch_near_pairs(const DevGeom& g, const int2* near, int count, int64_t t1b, int64_t t1e, int64_t t2b,
+                       int64_t t2e, bool same, bool wantS, bool wantD12, bool wantD21, double cS, int order,
+                       double* hm, int64_t ld, double* stmp, double* d12, double* d21, cudaStream_t s) {
+    if (count <= 0) return;
+    ProfScope prof_("near_pairs", s);
+    near_pairs_kernel<<<nblocks(count, 128), 128, 0, s>>>(near, count, g.srec, g.prec, g.qrec, t1b, t1e - t1b, t2b,
+                                                          t2e - t2b, same ? 1 : 0, wantS ? 1 : 0, wantD12 ? 1 : 0,
+                                                          wantD21 ? 1 : 0, cS, order, g.tpos, hm, ld, stmp, d12, d21);
+    check_launch("near pairs");
+}
+
+// ===========================================================================
 // Sources and sensors
 // ===========================================================================
 

@@ -99,7 +99,18 @@ void gemm(int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, boo
     if (M <= 0 || N <= 0) return;
     ProfScope prof_(sizeof(T) == 8 ? "gemm_f64" : "gemm_f32", s);
     constexpr bool dbl = sizeof(T) == 8;
+    // Large tiles for big products; 32x32 tiles when the big-tile grid would
+    // leave most of the 152 SMs idle (block-sized solve steps).
     constexpr int BM = dbl ? 64 : 128, BN = dbl ? 64 : 128, BK = 8, TM = dbl ? 4 : 8, TN = dbl ? 4 : 8;
+    const int64_t big_ctas = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+    if (big_ctas < 152 && (M > 32 || N > 32)) {
+        dim3 grid(nblk(N, 32), nblk(M, 32));
+        if (grid.y > 65535) throw Error(OMG_ERR_UNSUPPORTED, "GEMM too tall");
+        gemm_kernel<T, 32, 32, 8, 2, 2><<<grid, 256, 0, s>>>(M, N, K, alpha, A, lda, ta ? 1 : 0, B, ldb, tb ? 1 : 0,
+                                                          beta, C, ldc, lower ? 1 : 0, row0, col0);
+        check("gemm");
+        return;
+    }
     dim3 grid(nblk(N, BN), nblk(M, BM));
     if (grid.y > 65535) throw Error(OMG_ERR_UNSUPPORTED, "GEMM too tall");
     gemm_kernel<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, s>>>(

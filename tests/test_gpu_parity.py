@@ -172,3 +172,16 @@ def test_empty_and_invalid_inputs(cuda):
     T[1] = T[1][1:]
     with pytest.raises(api.OMGError):
         api.Geometry.from_meshes(V, T, w.head.domains)
+
+
+@pytest.mark.parametrize("name", ["small_ico2_3l_pert", "config0"])
+def test_mixed_headmat_close_to_fp64(cuda, name):
+    """Far pairs by the FP32 product rule, near pairs in FP64: the assembled
+    matrix stays within 1e-6 (relative Frobenius) of the FP64 drop-in."""
+    api = _api()
+    w = _w(name)
+    geo = api.Geometry.from_head(w.head)
+    H64 = api.HeadMat(geo, precision="fp64").cpu().numpy()
+    H32 = api.HeadMat(geo, precision="mixed").cpu().numpy()
+    assert np.array_equal(H32, H32.T)
+    assert rel(H32, H64) < 1e-6
