@@ -14,6 +14,7 @@ raise ``OMGError`` carrying the C status, where the reference raises its
 from __future__ import annotations
 
 import ctypes
+import sys
 from typing import Optional, Sequence
 
 import numpy as np
@@ -70,6 +71,10 @@ class Context:
         return int(self.lib.omg_context_kernel_launches(self.handle))
 
     def __del__(self):
+        # At interpreter shutdown the process is going away; leave the
+        # handles to the OS rather than racing the CUDA runtime's teardown.
+        if sys.is_finalizing():
+            return
         try:
             if getattr(self, "handle", None):
                 self.lib.omg_context_destroy(self.handle)
@@ -164,6 +169,8 @@ class Geometry:
         self._sigmas = s
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             if getattr(self, "handle", None):
                 self.lib.omg_geometry_destroy(self.handle)
@@ -279,6 +286,8 @@ class Solver:
         return X[:, 0] if vec else X
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             if getattr(self, "handle", None):
                 self.ctx.lib.omg_solver_destroy(self.handle)

@@ -81,28 +81,46 @@ struct omg_context_s {
     int64_t* d_errcol = nullptr;
     double* d_scalar = nullptr;
     int64_t launches_at_create = 0;
+    int refs = 1;              // the caller's handle + one per live geometry / solver
 };
 
+// Device buffer.  Temporaries of one call are stream-ordered
+// (cudaMallocAsync/cudaFreeAsync on the call's stream); buffers that outlive
+// the call (geometry, solver) are plain allocations, so freeing them never
+// depends on a stream that may be gone by then.
 struct DevBuf {
     void* p = nullptr;
     cudaStream_t s = nullptr;
+    bool persistent = false;
     DevBuf() = default;
-    DevBuf(size_t bytes, cudaStream_t st) : s(st) {
-        if (bytes) OMG_CUDA(cudaMallocAsync(&p, bytes, st));
+    DevBuf(size_t bytes, cudaStream_t st, bool keep = false) : s(st), persistent(keep) {
+        if (!bytes) return;
+        if (persistent)
+            OMG_CUDA(cudaMalloc(&p, bytes));
+        else
+            OMG_CUDA(cudaMallocAsync(&p, bytes, st));
     }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
-    DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
+    DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s), persistent(o.persistent) { o.p = nullptr; }
     DevBuf& operator=(DevBuf&& o) noexcept {
         release();
         p = o.p;
         s = o.s;
+        persistent = o.persistent;
         o.p = nullptr;
         return *this;
     }
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFreeAsync(p, s);
+        if (p) {
+            if (persistent) {
+                cudaStreamSynchronize(s);
+                cudaFree(p);
+            } else {
+                cudaFreeAsync(p, s);
+            }
+        }
         p = nullptr;
     }
     template <typename T>
@@ -111,13 +129,14 @@ struct DevBuf {
 
 template <typename T>
 static T* upload(std::vector<DevBuf>& keep, const std::vector<T>& v, cudaStream_t s) {
-    keep.emplace_back(std::max<size_t>(1, v.size()) * sizeof(T), s);
+    keep.emplace_back(std::max<size_t>(1, v.size()) * sizeof(T), s, true);
     if (!v.empty()) OMG_CUDA(cudaMemcpyAsync(keep.back().p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     return keep.back().as<T>();
 }
 
 struct omg_geometry_s {
     omg_context ctx = nullptr;
+    int refs = 1;              // the caller's handle + one per live solver
     HostGeometry h;
     DevGeom d;
     std::vector<DevBuf> bufs;
@@ -150,6 +169,7 @@ struct omg_solver_s {
     DevBuf A64;                             // FP64: factor (lower). Mixed: symmetrized FP64 HeadMat
     DevBuf A32;                             // mixed: FP32 factor
     DevBuf Linv;                            // per-block inverses (T)
+    bool persistent = false;                // outlives the call that made it (public solver handle)
     double refine_tol = 1e-11;
     int max_refine = 12;
     int last_steps = 0;
@@ -177,6 +197,29 @@ static int guarded(F&& f) {
 }
 
 static void set_device(omg_context ctx) { OMG_CUDA(cudaSetDevice(ctx->device)); }
+
+// Handles are reference counted so that destroying them in any order is safe:
+// a context stays alive while a geometry or solver made from it lives, and a
+// geometry while a solver built on it lives.
+static void release_context(omg_context ctx) {
+    if (!ctx || --ctx->refs > 0) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->own);
+    cudaFree(ctx->d_err);
+    cudaFree(ctx->d_errcol);
+    cudaFree(ctx->d_scalar);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+}
+
+static void release_geometry(omg_geometry geo) {
+    if (!geo || --geo->refs > 0) return;
+    omg_context ctx = geo->ctx;
+    cudaSetDevice(ctx->device);
+    geo->bufs.clear();
+    delete geo;
+    release_context(ctx);
+}
 
 static void reset_err(omg_context ctx) {
     OMG_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int) * 4, ctx->stream));
@@ -231,11 +274,11 @@ static void upload_geometry(omg_geometry g) {
             if (!h.barrier[m]) tpos[t] = (int32_t)(h.tidx[t] - h.nv);
         }
     d.tpos = upload(g->bufs, tpos, s);
-    g->bufs.emplace_back((size_t)h.nt * SREC * 8, s);
+    g->bufs.emplace_back((size_t)h.nt * SREC * 8, s, true);
     d.srec = g->bufs.back().as<double>();
-    g->bufs.emplace_back((size_t)h.nt * PREC * 8, s);
+    g->bufs.emplace_back((size_t)h.nt * PREC * 8, s, true);
     d.prec = g->bufs.back().as<double>();
-    g->bufs.emplace_back((size_t)h.nt * QREC * 8, s);
+    g->bufs.emplace_back((size_t)h.nt * QREC * 8, s, true);
     d.qrec = g->bufs.back().as<double>();
     d.v2t_beg = upload(g->bufs, h.v2t_beg, s);
     d.v2t_tri = upload(g->bufs, h.v2t_tri, s);
@@ -345,7 +388,7 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
     OMG_REQUIRE(integ.order == 3, "mixed-precision assembly uses the 16-point rule (integrator order 3)");
     ensure_order(g, 3);
     if (!g->grec) {
-        g->bufs.emplace_back((size_t)h.nt * 64 * sizeof(float), s);
+        g->bufs.emplace_back((size_t)h.nt * 64 * sizeof(float), s, true);
         g->grec = g->bufs.back().as<float>();
         launch_prepare_gg(d, g->grec, s);
     }
@@ -429,7 +472,7 @@ static void factor_ldlt(omg_solver sv, T* A, int64_t ld, int nb) {
         const int64_t nk = sv->bounds[b + 1] - sv->bounds[b];
         sv->linv_off[b + 1] = sv->linv_off[b] + nk * nk;
     }
-    sv->Linv = DevBuf((size_t)sv->linv_off[nblocks] * sizeof(T), s);
+    sv->Linv = DevBuf((size_t)sv->linv_off[nblocks] * sizeof(T), s, sv->persistent);
     DevBuf W((size_t)N * nb * sizeof(T), s);
     T* Li = sv->Linv.as<T>();
     for (size_t b = 0; b < nblocks; ++b) {
@@ -487,7 +530,7 @@ static void solver_factor(omg_solver sv, DevBuf&& hm) {
         factor_ldlt<double>(sv, sv->A64.as<double>(), N, NB64);
     } else {
         sv->A64 = std::move(hm);
-        sv->A32 = DevBuf((size_t)N * N * sizeof(float), s);
+        sv->A32 = DevBuf((size_t)N * N * sizeof(float), s, sv->persistent);
         copy_convert<double, float>(N, N, sv->A64.as<double>(), N, sv->A32.as<float>(), N, true, 1.0f, s);
         symmetrize(sv->A64.as<double>(), N, N, s);
         factor_ldlt<float>(sv, sv->A32.as<float>(), N, NB32);
@@ -606,11 +649,8 @@ int omg_context_destroy(omg_context ctx) {
         if (!ctx) return;
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
-        cudaFree(ctx->d_err);
-        cudaFree(ctx->d_errcol);
-        cudaFree(ctx->d_scalar);
-        if (ctx->own) cudaStreamDestroy(ctx->own);
-        delete ctx;
+        ctx->stream = ctx->own;   // an external stream must not be used after its owner lets go
+        release_context(ctx);
     });
 }
 
@@ -660,6 +700,7 @@ static void finish_geometry(omg_context ctx, std::unique_ptr<omg_geometry_s>& g,
     g->ctx = ctx;
     upload_geometry(g.get());
     OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->refs++;
     *out = g.release();
 }
 
@@ -692,9 +733,7 @@ int omg_geometry_destroy(omg_geometry geo) {
         if (!geo) return;
         cudaSetDevice(geo->ctx->device);
         cudaStreamSynchronize(geo->ctx->stream);
-        geo->bufs.clear();
-        cudaStreamSynchronize(geo->ctx->stream);
-        delete geo;
+        release_geometry(geo);
     });
 }
 
@@ -829,11 +868,14 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
         sv->precision = precision;
         sv->N = geo->h.N;
         sv->nP = geo->h.nP;
-        DevBuf hm((size_t)sv->N * sv->N * 8, ctx->stream);
+        sv->persistent = true;
+        DevBuf hm((size_t)sv->N * sv->N * 8, ctx->stream, true);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
         assemble(geo, it, precision, hm.as<double>(), sv->N);
         check_err(ctx, "HeadMat");
         solver_factor(sv.get(), std::move(hm));
+        ctx->refs++;
+        geo->refs++;
         *out = sv.release();
     });
 }
@@ -850,9 +892,12 @@ int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double*
         sv->precision = precision;
         sv->N = geo->h.N;
         sv->nP = geo->h.nP;
-        DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream);
+        sv->persistent = true;
+        DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream, true);
         launch_from_reference_dense(geo->d, hm, ld, A.as<double>(), sv->N, ctx->stream);
         solver_factor(sv.get(), std::move(A));
+        ctx->refs++;
+        geo->refs++;
         *out = sv.release();
     });
 }
@@ -885,7 +930,11 @@ int omg_solver_destroy(omg_solver sv) {
         if (!sv) return;
         cudaSetDevice(sv->ctx->device);
         cudaStreamSynchronize(sv->ctx->stream);
+        omg_context ctx = sv->ctx;
+        omg_geometry geo = sv->geo;
         delete sv;
+        release_geometry(geo);
+        release_context(ctx);
     });
 }
 
