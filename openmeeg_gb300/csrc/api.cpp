@@ -29,7 +29,7 @@ void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int 
 void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
                 const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
                 const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
-                double tol, int perm, double* out, int64_t ldo, double* p1tmp, cudaStream_t s);
+                double tol, int perm, double* out, int64_t ldo, double* p1tmp, int mixed, cudaStream_t s);
 void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
                  double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
@@ -49,9 +49,6 @@ template <typename T>
 void gemm(int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, bool ta, const T* B, int64_t ldb, bool tb,
           T beta, T* C, int64_t ldc, cudaStream_t s, bool lower = false, int64_t row0 = 0, int64_t col0 = 0);
 template <typename T>
-void potrf_trinv(T* A, int64_t lda, int n, T* Linv, int ldi, int* err, int64_t* err_col, int64_t col_offset,
-                 cudaStream_t s);
-template <typename T>
 void negate_lower(T* A, int64_t lda, int64_t n, cudaStream_t s);
 template <typename T>
 void negate_rows(T* B, int64_t ldb, int64_t r0, int64_t r1, int64_t n, cudaStream_t s);
@@ -64,6 +61,16 @@ void axpy_f32(int64_t m, int64_t n, const float* d, int64_t ldd, double* x, int6
               cudaStream_t s);
 void scale_to_f32(int64_t m, int64_t n, const double* r, int64_t ldr, float* b, int64_t ldb, const double* colnorm,
                   double* colscale, cudaStream_t s);
+void residual_df64(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* X, int64_t ldx,
+                   const double* B, int64_t ldb, double* R, int64_t ldr, cudaStream_t s);
+template <typename T>
+void potrf(T* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, cudaStream_t s);
+template <typename T>
+void trsm_rows(int64_t m, int n, const T* L, int64_t ldl, T* P, int64_t ldp, cudaStream_t s);
+template <typename T>
+void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, int64_t ldb, cudaStream_t s);
+void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
+                   cudaStream_t s);
 }  // namespace omg
 
 using namespace omg;
@@ -165,15 +172,14 @@ struct omg_solver_s {
     int precision = OMG_PREC_FP64;
     int64_t N = 0, nP = 0;
     std::vector<int64_t> bounds;            // block boundaries (include nP)
-    std::vector<int64_t> linv_off;          // offsets of each block's inverse
     DevBuf A64;                             // FP64: factor (lower). Mixed: symmetrized FP64 HeadMat
     DevBuf A32;                             // mixed: FP32 factor
-    DevBuf Linv;                            // per-block inverses (T)
     bool persistent = false;                // outlives the call that made it (public solver handle)
-    double refine_tol = 1e-11;
-    int max_refine = 12;
+    double refine_tol = 1e-6;               // stop when corrections are this small relative to x
+    int max_refine = 10;
     int last_steps = 0;
     double last_residual = 0.0;
+    double last_correction = 0.0;
 };
 
 // ---------------------------------------------------------------------------
@@ -375,6 +381,8 @@ static void assemble_headmat_internal(omg_geometry g, const omg_integrator& inte
     }
 }
 
+static void ensure_gg_tables(omg_geometry g);
+
 // Mixed precision: far pairs by the FP32 product rule, near pairs (centroid
 // distance < kRhoFar x larger max edge) by the FP64 analytic kernels.
 constexpr float kRhoFar = 2.0f;
@@ -387,11 +395,7 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
     check_integrator(integ, false);
     OMG_REQUIRE(integ.order == 3, "mixed-precision assembly uses the 16-point rule (integrator order 3)");
     ensure_order(g, 3);
-    if (!g->grec) {
-        g->bufs.emplace_back((size_t)h.nt * 64 * sizeof(float), s, true);
-        g->grec = g->bufs.back().as<float>();
-        launch_prepare_gg(d, g->grec, s);
-    }
+    ensure_gg_tables(g);
     OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)h.N, s));
     DevBuf counter(sizeof(int), s);
     for (const auto& p : h.pairs) {
@@ -444,6 +448,14 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
     }
 }
 
+static void ensure_gg_tables(omg_geometry g) {
+    if (!g->grec) {
+        g->bufs.emplace_back((size_t)g->h.nt * 64 * sizeof(float), g->ctx->stream, true);
+        g->grec = g->bufs.back().as<float>();
+        launch_prepare_gg(g->d, g->grec, g->ctx->stream);
+    }
+}
+
 static void assemble(omg_geometry g, const omg_integrator& integ, int precision, double* hm, int64_t ld) {
     if (precision == OMG_PREC_MIXED)
         assemble_headmat_mixed(g, integ, hm, ld);
@@ -467,57 +479,40 @@ static void factor_ldlt(omg_solver sv, T* A, int64_t ld, int nb) {
     }
     sv->bounds.push_back(N);
     const size_t nblocks = sv->bounds.size() - 1;
-    sv->linv_off.assign(nblocks + 1, 0);
-    for (size_t b = 0; b < nblocks; ++b) {
-        const int64_t nk = sv->bounds[b + 1] - sv->bounds[b];
-        sv->linv_off[b + 1] = sv->linv_off[b] + nk * nk;
-    }
-    sv->Linv = DevBuf((size_t)sv->linv_off[nblocks] * sizeof(T), s, sv->persistent);
-    DevBuf W((size_t)N * nb * sizeof(T), s);
-    T* Li = sv->Linv.as<T>();
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
-        if (k0 == nP) negate_lower<T>(A + k0 + k0 * ld, ld, N - k0, s);
-        potrf_trinv<T>(A + k0 + k0 * ld, ld, (int)nk, Li + sv->linv_off[b], (int)nk, sv->ctx->d_err,
-                       sv->ctx->d_errcol, k0, s);
+        if (k0 == nP) negate_lower<T>(A + k0 + k0 * ld, ld, N - k0, s);   // continue on -(vertex Schur complement)
+        potrf<T>(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0, s);
         if (m > 0) {
-            T* w = W.as<T>();
-            gemm<T>(m, nk, nk, T(1), A + k1 + k0 * ld, ld, false, Li + sv->linv_off[b], nk, true, T(0), w, m, s);
-            gemm<T>(m, m, nk, T(-1), w, m, false, w, m, true, T(1), A + k1 + k1 * ld, ld, s, true, 0, 0);
-            copy_convert<T, T>(m, nk, w, m, A + k1 + k0 * ld, ld, false, T(1), s);
+            trsm_rows<T>(m, (int)nk, A + k0 + k0 * ld, ld, A + k1 + k0 * ld, ld, s);          // L21 = A21 L11^-T
+            gemm<T>(m, m, nk, T(-1), A + k1 + k0 * ld, ld, false, A + k1 + k0 * ld, ld, true, T(1), A + k1 + k1 * ld,
+                    ld, s, true, 0, 0);                                                          // A22 -= L21 L21^T
         }
     }
 }
 
-// In place: B <- HM^-1 B (internal numbering).
+// In place: B <- HM^-1 B (internal numbering), HM = L diag(+I_P, -I_V) L^T.
 template <typename T>
 static void solve_ldlt(omg_solver sv, const T* A, int64_t ld, T* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
     const size_t nblocks = sv->bounds.size() - 1;
-    int64_t nbmax = 0;
-    for (size_t b = 0; b < nblocks; ++b) nbmax = std::max(nbmax, sv->bounds[b + 1] - sv->bounds[b]);
-    DevBuf W((size_t)nbmax * nrhs * sizeof(T), s);
-    T* w = W.as<T>();
-    const T* Li = sv->Linv.as<T>();
-    for (size_t b = 0; b < nblocks; ++b) {
+    for (size_t b = 0; b < nblocks; ++b) {   // L y = b
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0;
-        gemm<T>(nk, nrhs, nk, T(1), Li + sv->linv_off[b], nk, false, B + k0, ldb, false, T(0), w, nk, s);
-        copy_convert<T, T>(nk, nrhs, w, nk, B + k0, ldb, false, T(1), s);
-        if (k1 < N) gemm<T>(N - k1, nrhs, nk, T(-1), A + k1 + k0 * ld, ld, false, w, nk, false, T(1), B + k1, ldb, s);
+        trsm_cols<T>(nrhs, (int)nk, A + k0 + k0 * ld, ld, false, B + k0, ldb, s);
+        if (k1 < N) gemm<T>(N - k1, nrhs, nk, T(-1), A + k1 + k0 * ld, ld, false, B + k0, ldb, false, T(1), B + k1, ldb, s);
     }
     negate_rows<T>(B, ldb, sv->nP, N, nrhs, s);
     // L^T x = y, right-looking: once block k is solved, remove its
     // contribution from all earlier blocks (K = block size, M = k0).
     for (size_t bb = nblocks; bb-- > 0;) {
         const int64_t k0 = sv->bounds[bb], k1 = sv->bounds[bb + 1], nk = k1 - k0;
-        gemm<T>(nk, nrhs, nk, T(1), Li + sv->linv_off[bb], nk, true, B + k0, ldb, false, T(0), w, nk, s);
-        copy_convert<T, T>(nk, nrhs, w, nk, B + k0, ldb, false, T(1), s);
-        if (k0 > 0) gemm<T>(k0, nrhs, nk, T(-1), A + k0, ld, true, w, nk, false, T(1), B, ldb, s);
+        trsm_cols<T>(nrhs, (int)nk, A + k0 + k0 * ld, ld, true, B + k0, ldb, s);
+        if (k0 > 0) gemm<T>(k0, nrhs, nk, T(-1), A + k0, ld, true, B + k0, ldb, false, T(1), B, ldb, s);
     }
 }
 
-constexpr int NB64 = 96;    // FP64 diagonal block (2 x 96^2 x 8 B of shared memory)
+constexpr int NB64 = 128;   // FP64 diagonal block (128 x 129 x 8 B of shared memory)
 constexpr int NB32 = 128;   // FP32 diagonal block
 
 // Factor the internal-order HeadMat held in `hm` (FP64, lower), taking ownership.
@@ -539,44 +534,58 @@ static void solver_factor(omg_solver sv, DevBuf&& hm) {
 }
 
 // Mixed precision: x = HM^-1 b by FP32 solves refined against the FP64 HM.
+// x0 = A32^-1 b; then r = b - A x (FP64-accurate, double-float residual),
+// d = A32^-1 r, x += d, until every column's correction is below refine_tol
+// relative to the column (the error of the final x is then about the
+// contraction factor times that, far below it).
 static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
     DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s);
-    DevBuf bn((size_t)nrhs * 8, s), rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s);
+    DevBuf rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s), dn((size_t)nrhs * 8, s), xn((size_t)nrhs * 8, s),
+        bn((size_t)nrhs * 8, s);
     double* x = X.as<double>();
     double* r = R.as<double>();
     OMG_CUDA(cudaMemsetAsync(x, 0, (size_t)N * nrhs * 8, s));
     copy_convert<double, double>(N, nrhs, B, ldb, r, N, false, 1.0, s);
     col_norms(N, nrhs, r, N, bn.as<double>(), s);
-    std::vector<double> hb(nrhs), hr(nrhs);
+    std::vector<double> hb(nrhs), hr(nrhs, 0.0), hd(nrhs), hx(nrhs);
     OMG_CUDA(cudaMemcpyAsync(hb.data(), bn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
+    const double* cn = bn.as<double>();
     int steps = 0;
-    double rel = 1.0;
-    for (; steps < sv->max_refine; ++steps) {
-        scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, steps == 0 ? bn.as<double>() : rn.as<double>(),
-                     sc.as<double>(), s);
+    double last_res = 1.0, est = 1.0, prev_est = 1e300;
+    for (int it = 0; it <= sv->max_refine; ++it) {
+        if (it > 0) {   // r = b - HM x
+            residual_df64(N, nrhs, N, sv->A64.as<double>(), N, x, N, B, ldb, r, N, s);
+            col_norms(N, nrhs, r, N, rn.as<double>(), s);
+            cn = rn.as<double>();
+            ++steps;
+        }
+        scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, cn, sc.as<double>(), s);
         solve_ldlt<float>(sv, sv->A32.as<float>(), N, B32.as<float>(), N, nrhs);
         axpy_f32(N, nrhs, B32.as<float>(), N, x, N, sc.as<double>(), s);
-        // r = b - HM x in FP64
-        copy_convert<double, double>(N, nrhs, B, ldb, r, N, false, 1.0, s);
-        gemm<double>(N, nrhs, N, -1.0, sv->A64.as<double>(), N, false, x, N, false, 1.0, r, N, s);
-        col_norms(N, nrhs, r, N, rn.as<double>(), s);
-        OMG_CUDA(cudaMemcpyAsync(hr.data(), rn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
+        col_norms_f32(N, nrhs, B32.as<float>(), N, sc.as<double>(), dn.as<double>(), s);
+        col_norms(N, nrhs, x, N, xn.as<double>(), s);
+        OMG_CUDA(cudaMemcpyAsync(hd.data(), dn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaMemcpyAsync(hx.data(), xn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
+        if (it > 0) OMG_CUDA(cudaMemcpyAsync(hr.data(), rn.p, nrhs * 8, cudaMemcpyDeviceToHost, s));
         OMG_CUDA(cudaStreamSynchronize(s));
-        rel = 0.0;
-        for (int64_t j = 0; j < nrhs; ++j) rel = std::max(rel, hb[j] > 0 ? hr[j] / hb[j] : 0.0);
-        if (!(rel > sv->refine_tol)) {
-            ++steps;
-            break;
+        est = 0.0;
+        last_res = 0.0;
+        for (int64_t j = 0; j < nrhs; ++j) {
+            if (hx[j] > 0) est = std::max(est, hd[j] / hx[j]);
+            if (it > 0 && hb[j] > 0) last_res = std::max(last_res, hr[j] / hb[j]);
         }
+        if (it > 0 && !(est > sv->refine_tol)) break;
+        if (it > 1 && !(est < prev_est)) break;   // stagnation: report below
+        prev_est = est;
     }
     sv->last_steps = steps;
-    sv->last_residual = rel;
+    sv->last_residual = last_res;
+    sv->last_correction = est;
     copy_convert<double, double>(N, nrhs, x, N, B, ldb, false, 1.0, s);
-    if (rel > sv->refine_tol)
-        throw Error(OMG_ERR_NOT_CONVERGED,
-                    "iterative refinement stopped at relative residual " + std::to_string(rel));
+    if (est > sv->refine_tol)
+        throw Error(OMG_ERR_NOT_CONVERGED, "iterative refinement stalled at relative correction " + std::to_string(est));
 }
 
 static void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
@@ -591,7 +600,7 @@ static void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t
 // Sources / sensors
 // ---------------------------------------------------------------------------
 static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain,
-                         int perm, double* out, int64_t ldo) {
+                         int perm, double* out, int64_t ldo, int precision = OMG_PREC_FP64) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     check_integrator(integ, true);
@@ -612,7 +621,7 @@ static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const om
         const int64_t n = std::min(per, nd - d0);
         launch_dsm(g->d, d0, n, dip, g->tmesh, g->tidx_ref, g->barrier, g->orient, dom.as<int>(), g->maxb, g->dnb,
                    g->bmesh, g->binside, g->dsigma, integ.order, integ.levels, integ.tol, perm, out, ldo,
-                   p1.as<double>(), s);
+                   p1.as<double>(), precision == OMG_PREC_MIXED ? 1 : 0, s);
     }
 }
 
@@ -967,7 +976,8 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     }
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
     if (nm > 0) launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
-    dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N);
+    if (precision == OMG_PREC_MIXED) ensure_gg_tables(geo);
+    dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision);
     if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s);
     OMG_CUDA(cudaEventRecord(ev[2], s));
     solver_factor(sv.get(), std::move(hm));

@@ -489,8 +489,25 @@ void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi
 // with the FP64 analytic kernels.
 // ===========================================================================
 constexpr int GREC = 64;   // floats per triangle: centroid (3 doubles), 16 offsets, normal, h, area (double)
-__constant__ float c_w16[16];
-__constant__ float c_b16[16][3];
+// The 16-point rule of c_rules[3] rounded to FP32 (weights, barycentric nodes).
+__constant__ float c_w16[16] = {0.144315607677786f, 0.095091634267284f, 0.095091634267284f, 0.095091634267284f, 0.032458497623198f, 0.032458497623198f, 0.032458497623198f, 0.103217370534718f, 0.103217370534718f, 0.103217370534718f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f};
+__constant__ float c_b16[16][3] = {
+    {0.333333333333333f, 0.333333333333333f, 0.333333333333333f},
+    {0.081414823414554f, 0.459292588292722f, 0.459292588292722f},
+    {0.459292588292722f, 0.081414823414554f, 0.459292588292722f},
+    {0.459292588292722f, 0.459292588292722f, 0.081414823414554f},
+    {0.898905543365937f, 0.050547228317031f, 0.050547228317031f},
+    {0.050547228317031f, 0.898905543365937f, 0.050547228317031f},
+    {0.050547228317031f, 0.050547228317031f, 0.898905543365937f},
+    {0.658861384496479f, 0.170569307751760f, 0.170569307751761f},
+    {0.170569307751760f, 0.658861384496479f, 0.170569307751761f},
+    {0.170569307751760f, 0.170569307751761f, 0.658861384496479f},
+    {0.008394777409957f, 0.728492392955404f, 0.263112829634639f},
+    {0.728492392955404f, 0.008394777409957f, 0.263112829634639f},
+    {0.728492392955404f, 0.263112829634639f, 0.008394777409957f},
+    {0.008394777409957f, 0.263112829634639f, 0.728492392955404f},
+    {0.263112829634639f, 0.008394777409957f, 0.728492392955404f},
+    {0.263112829634639f, 0.728492392955404f, 0.008394777409957f}};
 
 __global__ void prepare_gg_kernel(int64_t nt, const double* __restrict__ V, const int32_t* __restrict__ T,
                                   float* grec) {
@@ -517,34 +534,6 @@ __global__ void prepare_gg_kernel(int64_t nt, const double* __restrict__ V, cons
 
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s) {
     ProfScope prof_("prepare_gg", s);
-    static bool init = false;
-    if (!init) {
-        float w[16], b[16][3];
-        for (int k = 0; k < 16; ++k) {
-            static const double R[16][4] = {
-                {0.333333333333333, 0.333333333333333, 0.333333333333333, 0.144315607677786},
-                {0.081414823414554, 0.459292588292722, 0.459292588292722, 0.095091634267284},
-                {0.459292588292722, 0.081414823414554, 0.459292588292722, 0.095091634267284},
-                {0.459292588292722, 0.459292588292722, 0.081414823414554, 0.095091634267284},
-                {0.898905543365937, 0.050547228317031, 0.050547228317031, 0.032458497623198},
-                {0.050547228317031, 0.898905543365937, 0.050547228317031, 0.032458497623198},
-                {0.050547228317031, 0.050547228317031, 0.898905543365937, 0.032458497623198},
-                {0.658861384496479, 0.170569307751760, 0.170569307751761, 0.103217370534718},
-                {0.170569307751760, 0.658861384496479, 0.170569307751761, 0.103217370534718},
-                {0.170569307751760, 0.170569307751761, 0.658861384496479, 0.103217370534718},
-                {0.008394777409957, 0.728492392955404, 0.263112829634639, 0.027230314174434},
-                {0.728492392955404, 0.008394777409957, 0.263112829634639, 0.027230314174434},
-                {0.728492392955404, 0.263112829634639, 0.008394777409957, 0.027230314174434},
-                {0.008394777409957, 0.263112829634639, 0.728492392955404, 0.027230314174434},
-                {0.263112829634639, 0.008394777409957, 0.728492392955404, 0.027230314174434},
-                {0.263112829634639, 0.728492392955404, 0.008394777409957, 0.027230314174434}};
-            w[k] = (float)R[k][3];
-            for (int i = 0; i < 3; ++i) b[k][i] = (float)R[k][i];
-        }
-        cudaMemcpyToSymbol(c_w16, w, sizeof(w));
-        cudaMemcpyToSymbol(c_b16, b, sizeof(b));
-        init = true;
-    }
     prepare_gg_kernel<<<nblocks(g.nt, 128), 128, 0, s>>>(g.nt, g.V, g.T, grec);
     check_launch("prepare_gg");
 }
@@ -910,6 +899,81 @@ __device__ void dsm_adaptive(int kind, int order, int levels, double tol, const 
     result[0] = total[0]; result[1] = total[1]; result[2] = total[2];
 }
 
+
+// Mixed precision: the first adaptive level in FP32 with coordinates relative
+// to the triangle centroid.  The FP32 value is kept only when the acceptance
+// test |coarse - refined| <= tol |coarse| (integrator.h:245) holds with a
+// factor-2 margin -- a decision FP32 rounding cannot flip; otherwise the
+// caller recomputes in FP64.
+struct DsmTriF {
+    float3 p0, e10, e20, n;   // p0 relative to the centroid
+    float d11, d12, d22;
+};
+__device__ __forceinline__ void dsm_eval_f(int kind, const DsmTriF& T, float3 xc, float3 q, float3 v, float out[3]) {
+    const float3 x = make_float3(xc.x + v.x, xc.y + v.y, xc.z + v.z);   // r - r0
+    const float n2 = x.x * x.x + x.y * x.y + x.z * x.z;
+    const float qx = q.x * x.x + q.y * x.y + q.z * x.z;
+    if (kind == 1) {
+        out[0] = qx / (n2 * sqrtf(n2));
+        return;
+    }
+    const float inv = 1.f / n2;
+    const float3 g = make_float3(q.x - 3.f * qx * x.x * inv, q.y - 3.f * qx * x.y * inv, q.z - 3.f * qx * x.z * inv);
+    const float gn = (g.x * T.n.x + g.y * T.n.y + g.z * T.n.z) * (inv * sqrtf(inv));
+    const float3 w = make_float3(v.x - T.p0.x, v.y - T.p0.y, v.z - T.p0.z);   // r - p0
+    const float a1 = w.x * T.e10.x + w.y * T.e10.y + w.z * T.e10.z;
+    const float a2 = w.x * T.e20.x + w.y * T.e20.y + w.z * T.e20.z;
+    const float l1 = T.d11 * a1 + T.d12 * a2, l2 = T.d12 * a1 + T.d22 * a2;
+    out[0] = gn * (1.f - l1 - l2);
+    out[1] = gn * l1;
+    out[2] = gn * l2;
+}
+__device__ __forceinline__ void dsm_rule_f(int kind, const DsmTriF& T, float3 xc, float3 q, float3 P0, float3 P1,
+                                           float3 P2, float area, float res[3]) {
+    float acc[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < 16; ++k) {
+        const float b0 = c_b16[k][0], b1 = c_b16[k][1], b2 = c_b16[k][2];
+        const float3 v = make_float3(b0 * P0.x + b1 * P1.x + b2 * P2.x, b0 * P0.y + b1 * P1.y + b2 * P2.y,
+                                     b0 * P0.z + b1 * P1.z + b2 * P2.z);
+        float e[3];
+        dsm_eval_f(kind, T, xc, q, v, e);
+        const float w = c_w16[k];
+        acc[0] = fmaf(w, e[0], acc[0]);
+        if (kind == 0) {
+            acc[1] = fmaf(w, e[1], acc[1]);
+            acc[2] = fmaf(w, e[2], acc[2]);
+        }
+    }
+    res[0] = area * acc[0]; res[1] = area * acc[1]; res[2] = area * acc[2];
+}
+__device__ __forceinline__ float3 fmid(float3 a, float3 b) {
+    return make_float3(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z));
+}
+// Returns true (and the refined value) when FP32 settles the first level.
+__device__ bool dsm_first_level_f32(int kind, double tol, const DsmTriF& T, float3 xc, float3 q, float3 R0,
+                                    float3 R1, float3 R2, float area, double result[3]) {
+    float coarse[3];
+    dsm_rule_f(kind, T, xc, q, R0, R1, R2, area, coarse);
+    const float3 m0 = fmid(R1, R2), m1 = fmid(R2, R0), m2 = fmid(R0, R1);
+    float a[3], b[3], c[3], d[3];
+    const float sub = 0.25f * area;
+    dsm_rule_f(kind, T, xc, q, R0, m1, m2, sub, a);
+    dsm_rule_f(kind, T, xc, q, m0, R1, m2, sub, b);
+    dsm_rule_f(kind, T, xc, q, m0, m1, R2, sub, c);
+    dsm_rule_f(kind, T, xc, q, m0, m1, m2, sub, d);
+    const int dim = kind == 0 ? 3 : 1;
+    double ref[3], dn = 0.0, cn = 0.0;
+    for (int k = 0; k < dim; ++k) {
+        ref[k] = (double)a[k] + (double)b[k] + (double)c[k] + (double)d[k];
+        const double e = (double)coarse[k] - ref[k];
+        dn += e * e;
+        cn += (double)coarse[k] * (double)coarse[k];
+    }
+    if (!(sqrt(dn) <= 0.5 * tol * sqrt(cn))) return false;
+    for (int k = 0; k < dim; ++k) result[k] = ref[k];
+    return true;
+}
+
 // SourceMatrix<Dipole> (assembleSourceMat.cpp:66-104) with
 // operatorPotentialDerivative / operatorPotential (operators.cpp:40-88):
 // one thread per (dipole, triangle).  P0 rows are written directly (one
@@ -921,7 +985,8 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
                            const int* __restrict__ orient, const int* __restrict__ dom, int maxb,
                            const int* __restrict__ dnb, const int* __restrict__ bmesh,
                            const int* __restrict__ binside, const double* __restrict__ dsigma, int order, int levels,
-                           double tol, int64_t nv, int64_t nP, int perm, double* out, int64_t ldo, double* p1tmp) {
+                           double tol, int64_t nv, int64_t nP, int perm, double* out, int64_t ldo, double* p1tmp,
+                           int mixed) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t il = blockIdx.y;
     if (t >= nt || il >= ndc) return;
@@ -956,13 +1021,36 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
     const d3 r0 = dev::ld3(dip + 6 * i), q = dev::ld3(dip + 6 * i + 3);
     const double area = s[12];
     double v[3];
-    dsm_adaptive(0, order, levels, tol, T, r0, q, R0, R1, R2, area, v);
+    bool f32v = false, f32p = false;
+    double pf[3];
+    if (mixed && order == 3 && levels > 0) {
+        const d3 c = (R0 + R1 + R2) * (1.0 / 3.0);
+        const d3 xcd = c - r0;
+        const float3 xc = make_float3((float)xcd.x, (float)xcd.y, (float)xcd.z);
+        const float3 qf = make_float3((float)q.x, (float)q.y, (float)q.z);
+        const d3 a0 = R0 - c, a1 = R1 - c, a2 = R2 - c;
+        const float3 F0 = make_float3((float)a0.x, (float)a0.y, (float)a0.z);
+        const float3 F1 = make_float3((float)a1.x, (float)a1.y, (float)a1.z);
+        const float3 F2 = make_float3((float)a2.x, (float)a2.y, (float)a2.z);
+        DsmTriF TF;
+        TF.p0 = F0;
+        TF.n = make_float3((float)T.n.x, (float)T.n.y, (float)T.n.z);
+        TF.e10 = make_float3((float)T.e10.x, (float)T.e10.y, (float)T.e10.z);
+        TF.e20 = make_float3((float)T.e20.x, (float)T.e20.y, (float)T.e20.z);
+        TF.d11 = (float)T.d11; TF.d12 = (float)T.d12; TF.d22 = (float)T.d22;
+        f32v = dsm_first_level_f32(0, tol, TF, xc, qf, F0, F1, F2, (float)area, v);
+        if (!barrier[m]) f32p = dsm_first_level_f32(1, tol, TF, xc, qf, F0, F1, F2, (float)area, pf);
+    }
+    if (!f32v) dsm_adaptive(0, order, levels, tol, T, r0, q, R0, R1, R2, area, v);
     o3[0] = v[0] * coeffD;
     o3[1] = v[1] * coeffD;
     o3[2] = v[2] * coeffD;
     if (!barrier[m]) {
         double p[3];
-        dsm_adaptive(1, order, levels, tol, T, r0, q, R0, R1, R2, area, p);
+        if (f32p)
+            p[0] = pf[0];
+        else
+            dsm_adaptive(1, order, levels, tol, T, r0, q, R0, R1, R2, area, p);
         const int64_t ref = tidx_ref[t];
         const int64_t row = perm ? ref - nv : ref;
         out[row + i * ldo] = p[0] * (coeffD / sigma);
@@ -1148,12 +1236,12 @@ void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int 
 void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
                 const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
                 const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
-                double tol, int perm, double* out, int64_t ldo, double* p1tmp, cudaStream_t s) {
+                double tol, int perm, double* out, int64_t ldo, double* p1tmp, int mixed, cudaStream_t s) {
     ProfScope prof_("dsm", s);
     if (ndc == 0) return;
     dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
     dsm_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, tmesh, tidx_ref, barrier, orient, dom, maxb, dnb,
-                                    bmesh, binside, dsigma, order, levels, tol, g.nv, g.nP, perm, out, ldo, p1tmp);
+                                    bmesh, binside, dsigma, order, levels, tol, g.nv, g.nP, perm, out, ldo, p1tmp, mixed);
     check_launch("DSM");
     dim3 grid2(nblocks(g.nv, 128), (unsigned)ndc);
     dsm_gather_kernel<<<grid2, 128, 0, s>>>(dip0, ndc, g.nv, g.nt, p1tmp, g.v2t_beg, g.v2t_tri, g.v2t_loc, g.nP,

@@ -123,79 +123,6 @@ template void gemm<float>(int64_t, int64_t, int64_t, float, const float*, int64_
                           float, float*, int64_t, cudaStream_t, bool, int64_t, int64_t);
 
 // ---------------------------------------------------------------------------
-// Diagonal block: lower Cholesky in shared memory, then L^-1 (row by row).
-// A (n x n, lower read) is overwritten by L; Linv (n x n) receives L^-1 with
-// zeros above the diagonal.  A non-positive pivot sets *err (with the global
-// column in *err_col) and is replaced by 1 so the launch completes.
-// ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(512) potrf_trinv_kernel(T* A, int64_t lda, int n, T* Linv, int ldi, int* err,
-                                                          int64_t* err_col, int64_t col_offset) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    T* L = reinterpret_cast<T*>(smraw);   // n x n, column-major, ld = n
-    T* X = L + n * n;                     // n x n inverse
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int e = tid; e < n * n; e += nt) {
-        const int i = e % n, j = e / n;
-        L[e] = (i >= j) ? A[i + j * lda] : T(0);
-        X[e] = T(0);
-    }
-    __syncthreads();
-    for (int j = 0; j < n; ++j) {
-        if (tid == 0) {
-            T d = L[j + j * n];
-            if (!(d > T(0))) {
-                if (atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0) *err_col = col_offset + j;
-                d = T(1);
-            }
-            L[j + j * n] = sqrt(d);
-        }
-        __syncthreads();
-        const T djj = L[j + j * n];
-        for (int i = j + 1 + tid; i < n; i += nt) L[i + j * n] /= djj;
-        __syncthreads();
-        const int m = n - j - 1;
-        for (int e = tid; e < m * m; e += nt) {
-            const int r = j + 1 + e % m, c = j + 1 + e / m;
-            if (r >= c) L[r + c * n] -= L[r + j * n] * L[c + j * n];
-        }
-        __syncthreads();
-    }
-    // X = L^-1: row i depends on rows < i.
-    for (int i = 0; i < n; ++i) {
-        const T inv = T(1) / L[i + i * n];
-        for (int c = tid; c <= i; c += nt) {
-            T s = (c == i) ? T(1) : T(0);
-            for (int k = c; k < i; ++k) s -= L[i + k * n] * X[k + c * n];
-            X[i + c * n] = s * inv;
-        }
-        __syncthreads();
-    }
-    for (int e = tid; e < n * n; e += nt) {
-        const int i = e % n, j = e / n;
-        if (i >= j) A[i + j * lda] = L[e];
-        Linv[i + j * ldi] = X[e];
-    }
-}
-
-template <typename T>
-void potrf_trinv(T* A, int64_t lda, int n, T* Linv, int ldi, int* err, int64_t* err_col, int64_t col_offset,
-                 cudaStream_t s) {
-    ProfScope prof_("potrf_trinv", s);
-    const size_t sm = 2 * (size_t)n * n * sizeof(T);
-    if (sm > 227 * 1024) throw Error(OMG_ERR_INVALID, "diagonal block too large for shared memory");
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(potrf_trinv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr = true;
-    }
-    potrf_trinv_kernel<T><<<1, 512, sm, s>>>(A, lda, n, Linv, ldi, err, err_col, col_offset);
-    check("potrf_trinv");
-}
-template void potrf_trinv<double>(double*, int64_t, int, double*, int, int*, int64_t*, int64_t, cudaStream_t);
-template void potrf_trinv<float>(float*, int64_t, int, float*, int, int*, int64_t*, int64_t, cudaStream_t);
-
-// ---------------------------------------------------------------------------
 // Utilities
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -343,6 +270,319 @@ void scale_to_f32(int64_t m, int64_t n, const double* r, int64_t ldr, float* b, 
     dim3 grid(nblk(m, 256), (unsigned)std::min<int64_t>(n, 32768));
     scale_to_f32_kernel<<<grid, 256, 0, s>>>(m, n, r, ldr, b, ldb, colnorm, colscale);
     check("scale_to_f32");
+}
+
+// ---------------------------------------------------------------------------
+// Refinement residual R = B - A X with FP64 accuracy on the FP32 pipes.
+// A (FP64) and X (FP64) are split into float pairs hi + lo when staged into
+// shared memory; each product is formed exactly (TwoProd by FMA, plus the
+// cross terms) and accumulated in a compensated pair (TwoSum), the "Dot2"
+// scheme of Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26(6), 2005), which
+// returns the dot product as if computed in twice the working precision.
+// ---------------------------------------------------------------------------
+constexpr int RB_M = 64, RB_N = 32, RB_K = 16, RB_TM = 4, RB_TN = 2;   // 256 threads
+
+__global__ void __launch_bounds__(256) residual_df64_kernel(int64_t M, int64_t N, int64_t K,
+                                                           const double* __restrict__ A, int64_t lda,
+                                                           const double* __restrict__ X, int64_t ldx,
+                                                           const double* __restrict__ B, int64_t ldb, double* R,
+                                                           int64_t ldr) {
+    __shared__ float Ah[RB_K][RB_M + 1], Al[RB_K][RB_M + 1];
+    __shared__ float Xh[RB_K][RB_N + 1], Xl[RB_K][RB_N + 1];
+    const int64_t m0 = (int64_t)blockIdx.y * RB_M, n0 = (int64_t)blockIdx.x * RB_N;
+    const int tid = threadIdx.x;
+    const int tx = tid % (RB_N / RB_TN), ty = tid / (RB_N / RB_TN);
+    float sh[RB_TM][RB_TN], sl[RB_TM][RB_TN];
+#pragma unroll
+    for (int i = 0; i < RB_TM; ++i)
+#pragma unroll
+        for (int j = 0; j < RB_TN; ++j) sh[i][j] = sl[i][j] = 0.f;
+    for (int64_t k0 = 0; k0 < K; k0 += RB_K) {
+        for (int e = tid; e < RB_M * RB_K; e += 256) {
+            const int i = e % RB_M, k = e / RB_M;
+            const int64_t gi = m0 + i, gk = k0 + k;
+            const double v = (gi < M && gk < K) ? A[gi + gk * lda] : 0.0;
+            const float h = (float)v;
+            Ah[k][i] = h;
+            Al[k][i] = (float)(v - (double)h);
+        }
+        for (int e = tid; e < RB_N * RB_K; e += 256) {
+            const int k = e % RB_K, j = e / RB_K;
+            const int64_t gj = n0 + j, gk = k0 + k;
+            const double v = (gj < N && gk < K) ? X[gk + gj * ldx] : 0.0;
+            const float h = (float)v;
+            Xh[k][j] = h;
+            Xl[k][j] = (float)(v - (double)h);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < RB_K; ++k) {
+            float ah[RB_TM], al[RB_TM], xh[RB_TN], xl[RB_TN];
+#pragma unroll
+            for (int i = 0; i < RB_TM; ++i) { ah[i] = Ah[k][ty * RB_TM + i]; al[i] = Al[k][ty * RB_TM + i]; }
+#pragma unroll
+            for (int j = 0; j < RB_TN; ++j) { xh[j] = Xh[k][tx * RB_TN + j]; xl[j] = Xl[k][tx * RB_TN + j]; }
+#pragma unroll
+            for (int i = 0; i < RB_TM; ++i)
+#pragma unroll
+                for (int j = 0; j < RB_TN; ++j) {
+                    const float p = ah[i] * xh[j];
+                    float e = fmaf(ah[i], xh[j], -p);           // exact product error
+                    e = fmaf(ah[i], xl[j], e);
+                    e = fmaf(al[i], xh[j], e);
+                    const float s = sh[i][j] + p;               // TwoSum(sh, p)
+                    const float bp = s - sh[i][j];
+                    const float t = (sh[i][j] - (s - bp)) + (p - bp);
+                    sh[i][j] = s;
+                    sl[i][j] += t + e;
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < RB_TN; ++j) {
+        const int64_t gj = n0 + tx * RB_TN + j;
+        if (gj >= N) continue;
+#pragma unroll
+        for (int i = 0; i < RB_TM; ++i) {
+            const int64_t gi = m0 + ty * RB_TM + i;
+            if (gi >= M) continue;
+            R[gi + gj * ldr] = B[gi + gj * ldb] - ((double)sh[i][j] + (double)sl[i][j]);
+        }
+    }
+}
+
+void residual_df64(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* X, int64_t ldx,
+                   const double* B, int64_t ldb, double* R, int64_t ldr, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return;
+    ProfScope prof_("residual_df64", s);
+    dim3 grid(nblk(N, RB_N), nblk(M, RB_M));
+    residual_df64_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, X, ldx, B, ldb, R, ldr);
+    check("residual_df64");
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal block Cholesky (lower, right-looking) with the block resident in
+// shared memory; thread (r, c-chunk) mapping avoids integer division in the
+// update loop.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) potrf_kernel(T* A, int64_t lda, int n, int* err, int64_t* err_col,
+                                                   int64_t col_offset) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* L = reinterpret_cast<T*>(smraw);   // n x (n+1) column-major (padded)
+    const int ldl = n + 1;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < n * n; e += 512) {
+        const int i = e % n, j = e / n;
+        L[i + j * ldl] = (i >= j) ? A[i + j * lda] : T(0);
+    }
+    __syncthreads();
+    const int lane_r = tid % 32, grp = tid / 32;   // 16 groups of 32 rows-threads
+    for (int j = 0; j < n; ++j) {
+        if (tid == 0) {
+            T d = L[j + j * ldl];
+            if (!(d > T(0))) {
+                if (atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0) *err_col = col_offset + j;
+                d = T(1);
+            }
+            L[j + j * ldl] = sqrt(d);
+        }
+        __syncthreads();
+        const T inv = T(1) / L[j + j * ldl];
+        for (int i = j + 1 + tid; i < n; i += 512) L[i + j * ldl] *= inv;
+        __syncthreads();
+        // trailing update of columns c in (j, n): group g handles columns c = j+1+g, j+1+g+16, ...
+        for (int c = j + 1 + grp; c < n; c += 16) {
+            const T lc = L[c + j * ldl];
+            for (int r = c + lane_r; r < n; r += 32) L[r + c * ldl] -= L[r + j * ldl] * lc;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < n * n; e += 512) {
+        const int i = e % n, j = e / n;
+        if (i >= j) A[i + j * lda] = L[i + j * ldl];
+    }
+}
+
+template <typename T>
+void potrf(T* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, cudaStream_t s) {
+    ProfScope prof_("potrf", s);
+    const size_t sm = (size_t)n * (n + 1) * sizeof(T);
+    if (sm > 227 * 1024) throw Error(OMG_ERR_INVALID, "diagonal block too large for shared memory");
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(potrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    potrf_kernel<T><<<1, 512, sm, s>>>(A, lda, n, err, err_col, col_offset);
+    check("potrf");
+}
+template void potrf<double>(double*, int64_t, int, int*, int64_t*, int64_t, cudaStream_t);
+template void potrf<float>(float*, int64_t, int, int*, int64_t*, int64_t, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Triangular solves with a diagonal block L (n x n lower, staged in shared
+// memory).  Panel form (rows independent):  W = P L^-T  for P (m x n).
+// Column form (columns independent):       B <- L^-1 B  or  L^-T B.
+// Each row / column is one warp: the substitution runs serially over the
+// block, the inner products across the 32 lanes.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_rows_kernel(int64_t m, int n, const T* __restrict__ L, int64_t ldl,
+                                                        T* P, int64_t ldp) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* sL = reinterpret_cast<T*>(smraw);          // n x n (row-major copy: sL[j*n + l] = L[j][l])
+    T* sx = sL + n * n;                           // 8 warps x n
+    for (int e = threadIdx.x; e < n * n; e += 256) {
+        const int j = e / n, l = e % n;
+        sL[e] = (l <= j) ? L[j + l * ldl] : T(0);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    T* x = sx + warp * n;
+    for (int64_t row = (int64_t)blockIdx.x * 8 + warp; row < m; row += (int64_t)gridDim.x * 8) {
+        for (int l = lane; l < n; l += 32) x[l] = P[row + (int64_t)l * ldp];
+        __syncwarp();
+        // x L^T = p  <=>  L x^T = p^T : forward substitution over j
+        for (int j = 0; j < n; ++j) {
+            T acc = T(0);
+            for (int l = lane; l < j; l += 32) acc += x[l] * sL[j * n + l];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) x[j] = (x[j] - acc) / sL[j * n + j];
+            __syncwarp();
+        }
+        for (int l = lane; l < n; l += 32) P[row + (int64_t)l * ldp] = x[l];
+        __syncwarp();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_cols_kernel(int64_t nrhs, int n, const T* __restrict__ L, int64_t ldl,
+                                                        int trans, T* B, int64_t ldb) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* sL = reinterpret_cast<T*>(smraw);   // n x n, sL[j*n + l] = (trans ? L[l][j] : L[j][l]) for the used part
+    T* sx = sL + n * n;
+    for (int e = threadIdx.x; e < n * n; e += 256) {
+        const int j = e / n, l = e % n;
+        sL[e] = trans ? ((j <= l) ? L[l + j * ldl] : T(0)) : ((l <= j) ? L[j + l * ldl] : T(0));
+    }
+    __syncthreads();
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    T* x = sx + warp * n;
+    for (int64_t col = (int64_t)blockIdx.x * 8 + warp; col < nrhs; col += (int64_t)gridDim.x * 8) {
+        T* b = B + col * ldb;
+        for (int l = lane; l < n; l += 32) x[l] = b[l];
+        __syncwarp();
+        if (!trans) {   // L x = b, forward
+            for (int j = 0; j < n; ++j) {
+                T acc = T(0);
+                for (int l = lane; l < j; l += 32) acc += sL[j * n + l] * x[l];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) x[j] = (x[j] - acc) / sL[j * n + j];
+                __syncwarp();
+            }
+        } else {        // L^T x = b, backward: row j of L^T is column j of L
+            for (int j = n - 1; j >= 0; --j) {
+                T acc = T(0);
+                for (int l = j + 1 + lane; l < n; l += 32) acc += sL[j * n + l] * x[l];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) x[j] = (x[j] - acc) / sL[j * n + j];
+                __syncwarp();
+            }
+        }
+        for (int l = lane; l < n; l += 32) b[l] = x[l];
+        __syncwarp();
+    }
+}
+
+template <typename T>
+static void set_max_smem(const void* f) {
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+template <typename T>
+void trsm_rows(int64_t m, int n, const T* L, int64_t ldl, T* P, int64_t ldp, cudaStream_t s) {
+    if (m <= 0) return;
+    ProfScope prof_("trsm_rows", s);
+    static bool attr = false;
+    if (!attr) {
+        set_max_smem<T>((const void*)trsm_rows_kernel<T>);
+        attr = true;
+    }
+    const size_t sm = ((size_t)n * n + 8 * (size_t)n) * sizeof(T);
+    const unsigned grid = (unsigned)std::min<int64_t>((m + 7) / 8, 152 * 8);
+    trsm_rows_kernel<T><<<grid, 256, sm, s>>>(m, n, L, ldl, P, ldp);
+    check("trsm_rows");
+}
+template <typename T>
+void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, int64_t ldb, cudaStream_t s) {
+    if (nrhs <= 0) return;
+    ProfScope prof_("trsm_cols", s);
+    static bool attr = false;
+    if (!attr) {
+        set_max_smem<T>((const void*)trsm_cols_kernel<T>);
+        attr = true;
+    }
+    const size_t sm = ((size_t)n * n + 8 * (size_t)n) * sizeof(T);
+    const unsigned grid = (unsigned)std::min<int64_t>((nrhs + 7) / 8, 152 * 8);
+    trsm_cols_kernel<T><<<grid, 256, sm, s>>>(nrhs, n, L, ldl, trans ? 1 : 0, B, ldb);
+    check("trsm_cols");
+}
+template void trsm_rows<double>(int64_t, int, const double*, int64_t, double*, int64_t, cudaStream_t);
+template void trsm_rows<float>(int64_t, int, const float*, int64_t, float*, int64_t, cudaStream_t);
+template void trsm_cols<double>(int64_t, int, const double*, int64_t, bool, double*, int64_t, cudaStream_t);
+template void trsm_cols<float>(int64_t, int, const float*, int64_t, bool, float*, int64_t, cudaStream_t);
+
+// Max-norm of each column of an m x n FP32 matrix scaled by colscale, and of
+// an FP64 matrix: one CTA per column (for the refinement stopping test).
+__global__ void col_amax_kernel(int64_t m, const double* __restrict__ A, int64_t lda, double* out) {
+    __shared__ double red[256];
+    const int64_t j = blockIdx.x;
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) s = fmax(s, fabs(A[i + j * lda]));
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[j] = red[0];
+}
+// 2-norms of the columns of an FP32 matrix times a per-column scale.
+__global__ void col_norms_f32_kernel(int64_t m, const float* __restrict__ A, int64_t lda,
+                                     const double* __restrict__ scale, double* out) {
+    __shared__ double red[256];
+    const int64_t j = blockIdx.x;
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const double v = A[i + j * lda];
+        s += v * v;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[j] = sqrt(red[0]) * (scale ? scale[j] : 1.0);
+}
+void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
+                   cudaStream_t s) {
+    if (n <= 0) return;
+    ProfScope prof_("col_norms", s);
+    col_norms_f32_kernel<<<(unsigned)n, 256, 0, s>>>(m, A, lda, scale, out);
+    check("col_norms_f32");
+}
+
+void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, cudaStream_t s) {
+    if (n <= 0) return;
+    ProfScope prof_("col_amax", s);
+    col_amax_kernel<<<(unsigned)n, 256, 0, s>>>(m, A, lda, out);
+    check("col_amax");
 }
 
 }  // namespace omg
