@@ -12,7 +12,7 @@
 #include <tuple>
 #include <vector>
 
-#include "omg_internal.h"
+#include "handles.h"
 
 namespace omg {
 void profile_enable(bool on);
@@ -76,96 +76,11 @@ void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const doub
 using namespace omg;
 
 static thread_local std::string g_last_error;
+void set_last_error(const char* msg) { g_last_error = msg; }
 
 // ---------------------------------------------------------------------------
 // Handles
 // ---------------------------------------------------------------------------
-struct omg_context_s {
-    int device = 0;
-    cudaStream_t own = nullptr;
-    cudaStream_t stream = nullptr;
-    int* d_err = nullptr;          // [0] status, [1..2] pad
-    int64_t* d_errcol = nullptr;
-    double* d_scalar = nullptr;
-    int64_t launches_at_create = 0;
-    int refs = 1;              // the caller's handle + one per live geometry / solver
-};
-
-// Device buffer.  Temporaries of one call are stream-ordered
-// (cudaMallocAsync/cudaFreeAsync on the call's stream); buffers that outlive
-// the call (geometry, solver) are plain allocations, so freeing them never
-// depends on a stream that may be gone by then.
-struct DevBuf {
-    void* p = nullptr;
-    cudaStream_t s = nullptr;
-    bool persistent = false;
-    DevBuf() = default;
-    DevBuf(size_t bytes, cudaStream_t st, bool keep = false) : s(st), persistent(keep) {
-        if (!bytes) return;
-        if (persistent)
-            OMG_CUDA(cudaMalloc(&p, bytes));
-        else
-            OMG_CUDA(cudaMallocAsync(&p, bytes, st));
-    }
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s), persistent(o.persistent) { o.p = nullptr; }
-    DevBuf& operator=(DevBuf&& o) noexcept {
-        release();
-        p = o.p;
-        s = o.s;
-        persistent = o.persistent;
-        o.p = nullptr;
-        return *this;
-    }
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) {
-            if (persistent) {
-                cudaStreamSynchronize(s);
-                cudaFree(p);
-            } else {
-                cudaFreeAsync(p, s);
-            }
-        }
-        p = nullptr;
-    }
-    template <typename T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-template <typename T>
-static T* upload(std::vector<DevBuf>& keep, const std::vector<T>& v, cudaStream_t s) {
-    keep.emplace_back(std::max<size_t>(1, v.size()) * sizeof(T), s, true);
-    if (!v.empty()) OMG_CUDA(cudaMemcpyAsync(keep.back().p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-    return keep.back().as<T>();
-}
-
-struct omg_geometry_s {
-    omg_context ctx = nullptr;
-    int refs = 1;              // the caller's handle + one per live solver
-    HostGeometry h;
-    DevGeom d;
-    std::vector<DevBuf> bufs;
-    // mesh-level device tables
-    int32_t* tmesh = nullptr;
-    int64_t* tidx_ref = nullptr;
-    int* barrier = nullptr;
-    int* orient = nullptr;
-    int64_t* tbeg = nullptr;
-    double* jump = nullptr;
-    int32_t* eeg_cand = nullptr;
-    int64_t n_eeg_cand = 0;
-    // domain tables
-    int ndom = 0, maxb = 1;
-    int* dnb = nullptr;
-    int* bmesh = nullptr;
-    int* binside = nullptr;
-    double* dsigma = nullptr;
-    int prepared_order = -1;
-    float* grec = nullptr;      // FP32 far-field records (mixed precision), built on first use
-};
-
 struct omg_solver_s {
     omg_context ctx = nullptr;
     omg_geometry geo = nullptr;

@@ -434,9 +434,9 @@ __global__ void __launch_bounds__(256) trsm_rows_kernel(int64_t m, int n, const 
     extern __shared__ __align__(16) unsigned char smraw[];
     T* sL = reinterpret_cast<T*>(smraw);          // n x n (row-major copy: sL[j*n + l] = L[j][l])
     T* sx = sL + n * n;                           // 8 warps x n
-    for (int e = threadIdx.x; e < n * n; e += 256) {
-        const int j = e / n, l = e % n;
-        sL[e] = (l <= j) ? L[j + l * ldl] : T(0);
+    for (int e = threadIdx.x; e < n * n; e += 256) {   // coalesced read down the columns of L
+        const int j = e % n, l = e / n;
+        sL[j * n + l] = (l <= j) ? L[j + l * ldl] : T(0);
     }
     __syncthreads();
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -464,9 +464,13 @@ __global__ void __launch_bounds__(256) trsm_cols_kernel(int64_t nrhs, int n, con
     extern __shared__ __align__(16) unsigned char smraw[];
     T* sL = reinterpret_cast<T*>(smraw);   // n x n, sL[j*n + l] = (trans ? L[l][j] : L[j][l]) for the used part
     T* sx = sL + n * n;
-    for (int e = threadIdx.x; e < n * n; e += 256) {
-        const int j = e / n, l = e % n;
-        sL[e] = trans ? ((j <= l) ? L[l + j * ldl] : T(0)) : ((l <= j) ? L[j + l * ldl] : T(0));
+    for (int e = threadIdx.x; e < n * n; e += 256) {   // coalesced: r runs down column c of L
+        const int r = e % n, c = e / n;
+        const T v = (r >= c) ? L[r + c * ldl] : T(0);
+        if (trans)
+            sL[c * n + r] = v;   // (L^T)[c][r]
+        else
+            sL[r * n + c] = v;   // L[r][c]
     }
     __syncthreads();
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
