@@ -140,6 +140,18 @@ int omg_head2eegmat_dev(omg_context ctx, omg_geometry geo, const double* electro
 /* Head2MEGMat (OpenMEEG/src/assembleSensors.cpp:69-96) for point sensors:
  * squids n x 6 row-major (position, orientation); out n x N. */
 int omg_head2megmat_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids, double* h2mm);
+/* Head2MEGMat that allocates no device memory.  No counterpart in the
+ * reference.  For callers that may not allocate once running (real-time
+ * loops that cannot wait on the allocator, hosts that reserve the GPU's memory
+ * up front, plugin hosts that forbid device allocations): the Ferguson pass
+ * uses a fixed scratch array built into the library instead of a per-call
+ * allocation.  Limit: n_squids x n_triangles <= OMG_NOALLOC_SCRATCH_DOUBLES.
+ * The first call on a device sets up the scratch address (make it before any
+ * stream capture); calls that overlap on the GPU share the array and race.
+ * Output and arguments as omg_head2megmat_dev. */
+#define OMG_NOALLOC_SCRATCH_DOUBLES (4 * 1024 * 1024)
+int omg_head2megmat_noalloc_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids,
+                                double* h2mm);
 /* DipSource2MEGMat (OpenMEEG/src/assembleSensors.cpp:133-159): out n_squids x n_dipoles. */
 int omg_dipsource2megmat_dev(omg_context ctx, const double* dipoles, int64_t n_dipoles, const double* squids,
                              int64_t n_squids, double* ds2mm);

@@ -82,6 +82,7 @@ _PROTOS = [
     ("omg_dipsourcemat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, ctypes.POINTER(Integrator), c_i32, c_vp]),
     ("omg_head2eegmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     ("omg_head2megmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
+    ("omg_head2megmat_noalloc_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
     ("omg_dipsource2megmat_dev", c_i32, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp]),
     ("omg_solver_create", c_i32, [c_vp, c_vp, ctypes.POINTER(Integrator), c_i32, ctypes.POINTER(c_vp)]),
     ("omg_solver_from_headmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_i32, ctypes.POINTER(c_vp)]),
