@@ -37,6 +37,7 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s);
+void launch_pad_identity(const DevGeom& g, double* hm, int64_t ld, cudaStream_t s);
 void launch_ff_block(const DevGeom& g, const float* grec, int64_t t1b, int64_t t1e, int64_t t2b, int64_t t2e,
                      bool same, bool wantS, bool wantD12, bool wantD21, double cS, double* hm, int64_t ld,
                      double* stmp, double* d12, double* d21, int2* near, int* near_count, int near_cap, float rho,
@@ -183,8 +184,10 @@ static void upload_geometry(omg_geometry g) {
     DevGeom& d = g->d;
     d.nv = h.nv;
     d.nt = h.nt;
-    d.N = h.N;
-    d.nP = h.nP;
+    d.nPt = h.nP;
+    d.nP = (h.nP + kPad - 1) / kPad * kPad;
+    d.N = d.nP + h.nv;
+    d.Nref = h.N;
     d.nmesh = h.nmesh;
     d.V = upload(g->bufs, h.V, s);
     d.T = upload(g->bufs, h.T, s);
@@ -256,7 +259,8 @@ static void assemble_headmat_internal(omg_geometry g, const omg_integrator& inte
     check_integrator(integ, false);
     ensure_order(g, integ.order);
     const int order = integ.order;
-    OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)h.N, s));
+    OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)d.N, s));
+    launch_pad_identity(d, hm, ld, s);
     for (const auto& p : h.pairs) {
         const int m1 = p.m1, m2 = p.m2;
         const bool same = (m1 == m2);
@@ -311,7 +315,8 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
     OMG_REQUIRE(integ.order == 3, "mixed-precision assembly uses the 16-point rule (integrator order 3)");
     ensure_order(g, 3);
     ensure_gg_tables(g);
-    OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)h.N, s));
+    OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)d.N, s));
+    launch_pad_identity(d, hm, ld, s);
     DevBuf counter(sizeof(int), s);
     for (const auto& p : h.pairs) {
         const int m1 = p.m1, m2 = p.m2;
@@ -520,10 +525,11 @@ static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const om
     cudaStream_t s = ctx->stream;
     check_integrator(integ, true);
     OMG_REQUIRE(domain >= -1 && domain < g->ndom, "domain index out of range");
-    if (ldo == g->h.N)
-        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)g->h.N * nd * 8, s));
+    const int64_t rows = perm ? g->d.N : g->h.N;
+    if (ldo == rows)
+        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)rows * nd * 8, s));
     else
-        for (int64_t j = 0; j < nd; ++j) OMG_CUDA(cudaMemsetAsync(out + j * ldo, 0, (size_t)g->h.N * 8, s));
+        for (int64_t j = 0; j < nd; ++j) OMG_CUDA(cudaMemsetAsync(out + j * ldo, 0, (size_t)rows * 8, s));
     if (nd == 0) return;
     DevBuf sa((size_t)nd * g->h.nmesh * 8, s), dom((size_t)nd * sizeof(int), s);
     launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s);
@@ -706,7 +712,7 @@ int omg_headmat_dev(omg_context ctx, omg_geometry geo, const omg_integrator* int
         set_device(ctx);
         reset_err(ctx);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
-        const int64_t N = geo->h.N;
+        const int64_t N = geo->d.N;
         DevBuf tmp((size_t)N * N * 8, ctx->stream);
         assemble(geo, it, precision, tmp.as<double>(), N);
         launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, hm, ld, false, ctx->stream);
@@ -720,7 +726,7 @@ int omg_headmat_packed_dev(omg_context ctx, omg_geometry geo, const omg_integrat
         set_device(ctx);
         reset_err(ctx);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
-        const int64_t N = geo->h.N;
+        const int64_t N = geo->d.N;
         DevBuf tmp((size_t)N * N * 8, ctx->stream);
         assemble_headmat_internal(geo, it, tmp.as<double>(), N);
         launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, packed, 0, true, ctx->stream);
@@ -790,8 +796,8 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
         sv->ctx = ctx;
         sv->geo = geo;
         sv->precision = precision;
-        sv->N = geo->h.N;
-        sv->nP = geo->h.nP;
+        sv->N = geo->d.N;
+        sv->nP = geo->d.nP;
         sv->persistent = true;
         DevBuf hm((size_t)sv->N * sv->N * 8, ctx->stream, true);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
@@ -810,12 +816,13 @@ int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double*
         OMG_REQUIRE(ctx && geo && hm && out, "null argument");
         OMG_REQUIRE(ld >= geo->h.N, "ld must be >= N");
         set_device(ctx);
+        reset_err(ctx);
         auto sv = std::make_unique<omg_solver_s>();
         sv->ctx = ctx;
         sv->geo = geo;
         sv->precision = precision;
-        sv->N = geo->h.N;
-        sv->nP = geo->h.nP;
+        sv->N = geo->d.N;
+        sv->nP = geo->d.nP;
         sv->persistent = true;
         DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream, true);
         launch_from_reference_dense(geo->d, hm, ld, A.as<double>(), sv->N, ctx->stream);
@@ -829,20 +836,21 @@ int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double*
 int omg_solver_solve_dev(omg_solver sv, double* b, int64_t ldb, int64_t nrhs) {
     return guarded([&] {
         OMG_REQUIRE(sv && b, "null argument");
-        OMG_REQUIRE(ldb >= sv->N && nrhs >= 0, "bad right-hand side shape");
+        OMG_REQUIRE(ldb >= sv->geo->h.N && nrhs >= 0, "bad right-hand side shape");
         set_device(sv->ctx);
         cudaStream_t s = sv->ctx->stream;
-        const int64_t N = sv->N, nv = sv->geo->h.nv, nP = sv->nP;
-        // reference -> internal numbering: rows [nv, N) first, then [0, nv)
+        const int64_t N = sv->N, nv = sv->geo->h.nv, nP = sv->nP, nPt = sv->geo->d.nPt;
+        // reference -> internal numbering: triangle rows [nv, nv+nPt) first, zero padding, then vertices [0, nv)
         DevBuf X((size_t)N * nrhs * 8, s);
         double* x = X.as<double>();
+        OMG_CUDA(cudaMemsetAsync(x, 0, (size_t)N * nrhs * 8, s));
         for (int64_t j = 0; j < nrhs; ++j) {
-            OMG_CUDA(cudaMemcpyAsync(x + j * N, b + j * ldb + nv, (size_t)nP * 8, cudaMemcpyDeviceToDevice, s));
+            OMG_CUDA(cudaMemcpyAsync(x + j * N, b + j * ldb + nv, (size_t)nPt * 8, cudaMemcpyDeviceToDevice, s));
             OMG_CUDA(cudaMemcpyAsync(x + j * N + nP, b + j * ldb, (size_t)nv * 8, cudaMemcpyDeviceToDevice, s));
         }
         solver_solve_internal(sv, x, N, nrhs);
         for (int64_t j = 0; j < nrhs; ++j) {
-            OMG_CUDA(cudaMemcpyAsync(b + j * ldb + nv, x + j * N, (size_t)nP * 8, cudaMemcpyDeviceToDevice, s));
+            OMG_CUDA(cudaMemcpyAsync(b + j * ldb + nv, x + j * N, (size_t)nPt * 8, cudaMemcpyDeviceToDevice, s));
             OMG_CUDA(cudaMemcpyAsync(b + j * ldb, x + j * N + nP, (size_t)nv * 8, cudaMemcpyDeviceToDevice, s));
         }
         OMG_CUDA(cudaStreamSynchronize(s));
@@ -868,7 +876,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
                           const omg_integrator& dsm_it, const double* dip, int64_t nd, const double* el, int64_t ne,
                           const double* sq, int64_t nm, double* geeg, double* gmeg, omg_gain_stats* st) {
     cudaStream_t s = ctx->stream;
-    const int64_t N = geo->h.N, k = ne + nm;
+    const int64_t N = geo->d.N, k = ne + nm;
     cudaEvent_t ev[6];
     for (auto& e : ev) OMG_CUDA(cudaEventCreate(&e));
     OMG_CUDA(cudaEventRecord(ev[0], s));
@@ -878,7 +886,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     sv->geo = geo;
     sv->precision = precision;
     sv->N = N;
-    sv->nP = geo->h.nP;
+    sv->nP = geo->d.nP;
     DevBuf hm((size_t)N * N * 8, s);
     assemble(geo, hm_it, precision, hm.as<double>(), N);
     OMG_CUDA(cudaEventRecord(ev[1], s));

@@ -448,30 +448,48 @@ __global__ void to_reference_packed_kernel(int64_t N, int64_t nv, int64_t nP, co
 void launch_symmetrize_to_reference(const DevGeom& g, const double* hm_int, int64_t ld_int, double* out,
                                     int64_t ld_out, bool packed, cudaStream_t s) {
     ProfScope prof_("to_reference", s);
-    dim3 grid(nblocks(g.N, 256), (unsigned)std::min<int64_t>(g.N, 32768));
+    dim3 grid(nblocks(g.Nref, 256), (unsigned)std::min<int64_t>(g.Nref, 32768));
     if (packed)
-        to_reference_packed_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, hm_int, ld_int, out);
+        to_reference_packed_kernel<<<grid, 256, 0, s>>>(g.Nref, g.nv, g.nP, hm_int, ld_int, out);
     else
-        to_reference_dense_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, hm_int, ld_int, out, ld_out);
+        to_reference_dense_kernel<<<grid, 256, 0, s>>>(g.Nref, g.nv, g.nP, hm_int, ld_int, out, ld_out);
     check_launch("to reference");
 }
 
-// Reference-numbered dense (lower triangle read) -> internal lower triangle.
-__global__ void from_reference_dense_kernel(int64_t N, int64_t nv, int64_t nP, const double* __restrict__ in,
-                                            int64_t ldi, double* hm, int64_t ld) {
+// Reference-numbered dense (lower triangle read) -> internal lower triangle,
+// identity on the padding.
+__global__ void from_reference_dense_kernel(int64_t N, int64_t nv, int64_t nP, int64_t nPt,
+                                            const double* __restrict__ in, int64_t ldi, double* hm, int64_t ld) {
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;   // internal row
     if (a >= N) return;
     for (int64_t b = blockIdx.y; b <= a; b += gridDim.y) {             // internal column
-        const int64_t i = a < nP ? a + nv : a - nP, j = b < nP ? b + nv : b - nP;
+        const bool pa = (a >= nPt && a < nP), pb = (b >= nPt && b < nP);
+        if (pa || pb) {
+            hm[a + b * ld] = (a == b) ? 1.0 : 0.0;
+            continue;
+        }
+        const int64_t i = a < nPt ? a + nv : a - nP, j = b < nPt ? b + nv : b - nP;
         hm[a + b * ld] = i >= j ? in[i + j * ldi] : in[j + i * ldi];
     }
+}
+
+__global__ void pad_identity_kernel(int64_t nPt, int64_t nP, double* hm, int64_t ld) {
+    const int64_t a = nPt + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a < nP) hm[a + a * ld] = 1.0;
+}
+
+void launch_pad_identity(const DevGeom& g, double* hm, int64_t ld, cudaStream_t s) {
+    if (g.nP == g.nPt) return;
+    ProfScope prof_("pad_identity", s);
+    pad_identity_kernel<<<1, 128, 0, s>>>(g.nPt, g.nP, hm, ld);
+    check_launch("pad identity");
 }
 
 void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
                                  cudaStream_t s) {
     ProfScope prof_("from_reference", s);
     dim3 grid(nblocks(g.N, 256), (unsigned)std::min<int64_t>(g.N, 32768));
-    from_reference_dense_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, in, ldi, hm, ld);
+    from_reference_dense_kernel<<<grid, 256, 0, s>>>(g.N, g.nv, g.nP, g.nPt, in, ldi, hm, ld);
     check_launch("from reference");
 }
 

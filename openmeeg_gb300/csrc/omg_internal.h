@@ -91,11 +91,20 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
 
 // --------------------------------------------------------------------------
 // Device geometry (flat arrays, internal numbering).
-// Internal position of an unknown: triangle unknowns first, then vertices:
-//   pos(triangle t) = tidx[t] - nv,  pos(vertex v) = nP + v.
+// Internal position of an unknown: triangle unknowns first, then identity
+// padding up to a multiple of kPad, then vertices:
+//   pos(triangle t) = tidx[t] - nv,  pos(vertex v) = nP + v,
+// with nPt <= nP the true triangle-unknown count.  The padding keeps every
+// block boundary of the factorization a multiple of 128 (aligned tensor-core
+// tiles); padded rows/columns hold the identity and never touch the solution.
 // --------------------------------------------------------------------------
+constexpr int64_t kPad = 128;
 struct DevGeom {
-    int64_t nv = 0, nt = 0, N = 0, nP = 0;
+    int64_t nv = 0, nt = 0;
+    int64_t N = 0;      // internal size nP + nv
+    int64_t nP = 0;     // padded offset of the vertex unknowns
+    int64_t nPt = 0;    // triangle unknowns
+    int64_t Nref = 0;   // reference size nPt + nv
     int nmesh = 0;
     double* V = nullptr;          // nv x 3
     int32_t* T = nullptr;         // nt x 3

@@ -1,0 +1,378 @@
+// Tensor-core GEMM for the mixed-precision solver (sm_103a, tcgen05).
+//
+//   C = beta * C + alpha * A * B^T          A: M x K, B: N x K (both K-major)
+//
+// FP32 accuracy on the TF32 tensor pipe by operand splitting: each FP32
+// operand is X = Xh + Xl with Xh the TF32-representable head (low 13
+// mantissa bits cleared) and Xl = X - Xh; the product is accumulated as
+// Ah*Bh + Ah*Bl + Al*Bh (the "3xTF32" scheme), with FP32 accumulation in TMEM.
+//
+// One CTA computes a 128 x 128 tile.  Warp 0 allocates 128 TMEM columns; one
+// thread streams the K dimension in 32-element (128-byte) chunks through a
+// two-stage shared-memory ring filled by TMA (cp.async.bulk.tensor, 128-byte
+// swizzle) and issues tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=128, K=8)
+// per 8-element step; tcgen05.commit signals each stage free and the final
+// accumulation done.  All four warps then read their 32 TMEM lanes with
+// tcgen05.ld and update C.  Every mbarrier wait is bounded: on timeout the
+// kernel records OMG_ERR_TIMEOUT, waits (bounded) for copies in flight,
+// releases TMEM and returns without touching C.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "device_common.cuh"
+#include "omg_internal.h"
+
+namespace omg {
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int STAGES = 2;
+constexpr int TILE_BYTES = BM * BK * 4;           // 16 KiB (BM == BN)
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;       // Ah, Al, Bh, Bl
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+constexpr uint32_t TMEM_COLS = 128;
+
+// Instruction descriptor: D=F32, A=B=TF32, both K-major, N=128, M=128.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);         // start address
+    d |= (uint64_t)1 << 16;                            // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                  // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                            // descriptor version
+    d |= (uint64_t)2 << 61;                            // 128-byte swizzle
+    return d;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(dev::smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     dev::smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%"
+        "20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(128, 1)
+    gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+                       const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
+                       int K, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod, int* err) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[STAGES];
+    __shared__ __align__(8) uint64_t mma_bar[STAGES];
+    __shared__ __align__(8) uint64_t done_bar;
+    __shared__ uint32_t tmem_holder;
+    __shared__ int s_abort;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    if (lower && n0 > m0 + BM - 1) return;   // tile strictly above the diagonal (uniform for the CTA)
+    const uint32_t sbase = (dev::smem_u32(smem_raw) + 1023u) & ~1023u;   // 1024-byte aligned ring
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            dev::mbar_init(&full_bar[s], 1);
+            dev::mbar_init(&mma_bar[s], 1);
+        }
+        dev::mbar_init(&done_bar, 1);
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         dev::smem_u32(&tmem_holder)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_holder;
+    const int nk = (K + BK - 1) / BK;
+    const uint32_t bytes_per_stage = (nprod == 3 ? 4u : 2u) * TILE_BYTES;
+
+    if (threadIdx.x == 0) {
+        int issued = 0, consumed = 0;
+        auto issue = [&](int c) {
+            const int slot = c % STAGES;
+            const uint32_t st = sbase + slot * STAGE_BYTES;
+            dev::mbar_expect_tx(&full_bar[slot], bytes_per_stage);
+            tma_load_2d(st, &tAh, c * BK, m0, &full_bar[slot]);
+            tma_load_2d(st + 2 * TILE_BYTES, &tBh, c * BK, n0, &full_bar[slot]);
+            if (nprod == 3) {
+                tma_load_2d(st + TILE_BYTES, &tAl, c * BK, m0, &full_bar[slot]);
+                tma_load_2d(st + 3 * TILE_BYTES, &tBl, c * BK, n0, &full_bar[slot]);
+            }
+            ++issued;
+        };
+        for (int c = 0; c < STAGES && c < nk; ++c) issue(c);
+        bool ok = true;
+        for (int c = 0; c < nk; ++c) {
+            const int slot = c % STAGES;
+            const uint32_t ph = (uint32_t)((c / STAGES) & 1);
+            if (!dev::mbar_wait_bounded(&full_bar[slot], ph)) {
+                ok = false;
+                break;
+            }
+            ++consumed;
+            fence_after();
+            const uint32_t st = sbase + slot * STAGE_BYTES;
+            const uint64_t dAh = sdesc_sw128(st), dAl = sdesc_sw128(st + TILE_BYTES);
+            const uint64_t dBh = sdesc_sw128(st + 2 * TILE_BYTES), dBl = sdesc_sw128(st + 3 * TILE_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk) {
+                const uint64_t off = (uint64_t)(kk * 32) >> 4;   // 8 TF32 = 32 bytes along the swizzled row
+                mma_tf32(tmem, dAh + off, dBh + off, (c | kk) != 0 ? 1u : 0u);
+                if (nprod == 3) {
+                    mma_tf32(tmem, dAh + off, dBl + off, 1u);
+                    mma_tf32(tmem, dAl + off, dBh + off, 1u);
+                }
+            }
+            mma_commit(&mma_bar[slot]);
+            if (c + STAGES < nk) {
+                if (!dev::mbar_wait_bounded(&mma_bar[slot], ph)) {
+                    ok = false;
+                    break;
+                }
+                issue(c + STAGES);
+            }
+        }
+        if (!ok) {
+            s_abort = 1;
+            atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
+            for (int c = consumed; c < issued; ++c)   // let copies in flight land before the CTA exits
+                dev::mbar_wait_bounded(&full_bar[c % STAGES], (uint32_t)((c / STAGES) & 1));
+        }
+        mma_commit(&done_bar);   // arrives once every MMA issued above has completed
+    }
+    __syncthreads();
+    const bool done = dev::mbar_wait_bounded(&done_bar, 0);
+    fence_after();
+    const bool all_done = __syncthreads_and(done ? 1 : 0) != 0;   // CTA-uniform: tcgen05.ld is warp-collective
+    if (all_done && !s_abort) {
+        const int row = m0 + warp * 32 + lane;
+        for (int chunk = 0; chunk < BN / 32; ++chunk) {
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(chunk * 32), r);
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int col = n0 + chunk * 32 + j;
+                    if (col < N && (!lower || row >= col)) {
+                        float* c = C + (int64_t)row + (int64_t)col * ldc;
+                        const float acc = __uint_as_float(r[j]);
+                        *c = (beta == 0.f) ? alpha * acc : fmaf(alpha, acc, beta * *c);
+                    }
+                }
+            }
+        }
+    } else if (!all_done && threadIdx.x == 0) {
+        atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Host side: tensor maps (driver entry point fetched through the runtime)
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    if (!fn) throw Error(OMG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    return fn;
+}
+
+// K-major FP32 matrix: `rows` rows of `k_extent` elements, row stride `ld` elements.
+static CUtensorMap make_map(const float* base, int64_t rows, int64_t k_extent, int64_t ld) {
+    if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 4) % 16 != 0)
+        throw Error(OMG_ERR_INVALID, "tensor-core operand not 16-byte aligned");
+    CUtensorMap m;
+    const cuuint64_t dims[2] = {(cuuint64_t)k_extent, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+    const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)BM};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(OMG_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
+}
+
+}  // namespace tc
+
+static inline void check_tc(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(OMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    count_launch();
+}
+
+// C(M x N, ldc) = beta*C + alpha * A B^T.  A: M x K (K-major, row stride lda),
+// B: N x K (K-major, row stride ldb); *h are TF32 heads, *l the remainders
+// (may be null when nprod == 1).  `k0` offsets the K coordinate of A and B.
+void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
+                 int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
+                 int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return;
+    if (K <= 0) throw Error(OMG_ERR_INVALID, "empty K");
+    ProfScope prof_("gemm_tf32x3", s);
+    const int nprod = (Al && Bl) ? 3 : 1;
+    // Operands are offset along K by moving the base pointer (k0 multiple of 4 keeps 16-byte alignment).
+    if ((a_k0 % 4) || (b_k0 % 4)) throw Error(OMG_ERR_INVALID, "tensor-core K offset not 16-byte aligned");
+    const CUtensorMap mAh = tc::make_map(Ah + a_k0, M, a_kext - a_k0, lda);
+    const CUtensorMap mAl = nprod == 3 ? tc::make_map(Al + a_k0, M, a_kext - a_k0, lda) : mAh;
+    const CUtensorMap mBh = tc::make_map(Bh + b_k0, N, b_kext - b_k0, ldb);
+    const CUtensorMap mBl = nprod == 3 ? tc::make_map(Bl + b_k0, N, b_kext - b_k0, ldb) : mBh;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        attr = true;
+    }
+    dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
+    if (grid.y > 65535) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM too tall");
+    tc::gemm_tf32x3_kernel<<<grid, 128, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, alpha, beta,
+                                                             C, ldc, lower ? 1 : 0, nprod, err);
+    check_tc("gemm_tf32x3");
+}
+
+// ---------------------------------------------------------------------------
+// Operand splitting: X = Xh + Xl with Xh = X with its low 13 mantissa bits
+// cleared (exactly representable in TF32) and Xl = X - Xh (exact in FP32).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void split_tf32(float x, float& h, float& l) {
+    h = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    l = x - h;
+}
+
+// Column-major panel P (m x nk, ld) -> K-major (row-major) heads/remainders
+// (m x kpad, row stride kpad), zero beyond nk.  32 x 32 tiles through shared
+// memory so both reads and writes are coalesced.
+__global__ void split_panel_kmajor_kernel(int64_t m, int nk, int kpad, const float* __restrict__ P, int64_t ld,
+                                          float* H, float* L) {
+    __shared__ float t[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32;
+    const int k0 = blockIdx.y * 32;
+    for (int kk = threadIdx.y; kk < 32; kk += blockDim.y) {
+        const int64_t i = i0 + threadIdx.x;
+        const int k = k0 + kk;
+        t[kk][threadIdx.x] = (i < m && k < nk) ? P[i + (int64_t)k * ld] : 0.f;
+    }
+    __syncthreads();
+    for (int ii = threadIdx.y; ii < 32; ii += blockDim.y) {
+        const int64_t i = i0 + ii;
+        const int k = k0 + threadIdx.x;
+        if (i < m && k < kpad) {
+            float h, l;
+            split_tf32(t[threadIdx.x][ii], h, l);
+            H[i * kpad + k] = h;
+            L[i * kpad + k] = l;
+        }
+    }
+}
+
+void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
+                        cudaStream_t s) {
+    if (m <= 0) return;
+    ProfScope prof_("split_panel", s);
+    dim3 grid((unsigned)((m + 31) / 32), (unsigned)((kpad + 31) / 32));
+    split_panel_kmajor_kernel<<<grid, dim3(32, 8), 0, s>>>(m, nk, kpad, P, ld, H, L);
+    check_tc("split_panel");
+}
+
+// Column-major block X (nk x ncol, ldx): column j becomes K-major row j of
+// (ncol x kpad) heads/remainders.
+__global__ void split_cols_kernel(int nk, int64_t ncol, int kpad, const float* __restrict__ X, int64_t ldx, float* H,
+                                  float* L) {
+    const int64_t j = blockIdx.y;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kpad; k += gridDim.x * blockDim.x) {
+        const float v = k < nk ? X[k + j * ldx] : 0.f;
+        float h, l;
+        split_tf32(v, h, l);
+        H[j * kpad + k] = h;
+        L[j * kpad + k] = l;
+    }
+}
+
+void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s) {
+    if (ncol <= 0) return;
+    ProfScope prof_("split_cols", s);
+    dim3 grid((unsigned)((kpad + 127) / 128), (unsigned)ncol);
+    split_cols_kernel<<<grid, 128, 0, s>>>(nk, ncol, kpad, X, ldx, H, L);
+    check_tc("split_cols");
+}
+
+// In place on the lower triangle of a column-major n x n matrix A: A <- head,
+// R <- remainder.
+__global__ void split_lower_inplace_kernel(int64_t n, float* A, int64_t lda, float* R) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int64_t j = blockIdx.y; j <= i; j += gridDim.y) {
+        float h, l;
+        split_tf32(A[i + j * lda], h, l);
+        A[i + j * lda] = h;
+        R[i + j * lda] = l;
+    }
+}
+
+void split_lower_inplace(int64_t n, float* A, int64_t lda, float* R, cudaStream_t s) {
+    if (n <= 0) return;
+    ProfScope prof_("split_lower", s);
+    dim3 grid((unsigned)((n + 255) / 256), (unsigned)std::min<int64_t>(n, 32768));
+    split_lower_inplace_kernel<<<grid, 256, 0, s>>>(n, A, lda, R);
+    check_tc("split_lower");
+}
+
+}  // namespace omg
+
+// Test hook (not part of the public header): the tensor-core GEMM on caller
+// operands, for the unit tests of the kernel itself.
+extern "C" int omg_internal_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
+                                        const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb,
+                                        float beta, float* C, int64_t ldc, int lower, int* err) {
+    try {
+        omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, lower != 0, err, 0);
+        cudaError_t e = cudaDeviceSynchronize();
+        return e == cudaSuccess ? 0 : -2;
+    } catch (const omg::Error& e) {
+        return e.code;
+    }
+}
