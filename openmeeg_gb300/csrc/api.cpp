@@ -69,7 +69,16 @@ void potrf(T* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_off
 template <typename T>
 void trsm_rows(int64_t m, int n, const T* L, int64_t ldl, T* P, int64_t ldp, cudaStream_t s);
 template <typename T>
-void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, int64_t ldb, cudaStream_t s);
+void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, int64_t ldb, cudaStream_t s,
+               const T* Lr = nullptr);
+// tc_gemm.cu
+void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
+                 int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
+                 int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s);
+void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
+                        cudaStream_t s);
+void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
+void split_lower_inplace(int64_t n, float* A, int64_t lda, float* R, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
                    cudaStream_t s);
 }  // namespace omg
@@ -89,7 +98,11 @@ struct omg_solver_s {
     int64_t N = 0, nP = 0;
     std::vector<int64_t> bounds;            // block boundaries (include nP)
     DevBuf A64;                             // FP64: factor (lower). Mixed: symmetrized FP64 HeadMat
-    DevBuf A32;                             // mixed: FP32 factor
+    DevBuf A32;                             // mixed: FP32 factor (TF32 heads after the split), ld = ld32
+    DevBuf A32r;                            // mixed: FP32 remainders of the factor
+    DevBuf W;                               // mixed: K-major head/remainder copies of every panel
+    std::vector<int64_t> w_off;             // offset (floats) of panel b's heads; remainders follow
+    int64_t ld32 = 0;
     bool persistent = false;                // outlives the call that made it (public solver handle)
     double refine_tol = 1e-6;               // stop when corrections are this small relative to x
     int max_refine = 10;
@@ -411,6 +424,78 @@ static void factor_ldlt(omg_solver sv, T* A, int64_t ld, int nb) {
     }
 }
 
+constexpr int NB32_TC = 128;   // tensor-core path: panel width = GEMM K = 4 x 32-element TMA chunks
+
+// FP32 factorization with the trailing updates on the tensor cores (3xTF32):
+// each panel L21 is split into K-major TF32 heads/remainders (kept for the
+// forward solves), the trailing block is updated by the tcgen05 GEMM, and at
+// the end the whole factor is split in place (heads) + remainders (A32r) for
+// the backward solves.
+static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N, nP = sv->nP;
+    sv->bounds.clear();
+    for (int64_t k = 0; k < N;) {
+        sv->bounds.push_back(k);
+        int64_t e = std::min(N, k + nb);
+        if (k < nP && e > nP) e = nP;
+        k = e;
+    }
+    sv->bounds.push_back(N);
+    const size_t nblocks = sv->bounds.size() - 1;
+    sv->w_off.assign(nblocks + 1, 0);
+    for (size_t b = 0; b < nblocks; ++b) sv->w_off[b + 1] = sv->w_off[b] + 2 * (N - sv->bounds[b + 1]) * nb;
+    sv->W = DevBuf((size_t)std::max<int64_t>(1, sv->w_off[nblocks]) * sizeof(float), s, sv->persistent);
+    for (size_t b = 0; b < nblocks; ++b) {
+        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
+        if (k0 == nP) negate_lower<float>(A + k0 + k0 * ld, ld, N - k0, s);
+        potrf<float>(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0, s);
+        if (m > 0) {
+            trsm_rows<float>(m, (int)nk, A + k0 + k0 * ld, ld, A + k1 + k0 * ld, ld, s);
+            float* Wh = sv->W.as<float>() + sv->w_off[b];
+            float* Wl = Wh + m * nb;
+            split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Wh, Wl, s);
+            gemm_tf32x3(m, m, nk, -1.f, Wh, Wl, nb, nb, 0, Wh, Wl, nb, nb, 0, 1.f, A + k1 + k1 * ld, ld, true,
+                        sv->ctx->d_err, s);
+        }
+    }
+    sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
+    split_lower_inplace(N, A, ld, sv->A32r.as<float>(), s);
+}
+
+// FP32 solve on the tensor cores: B <- HM^-1 B (internal numbering).
+static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N, ld = sv->ld32;
+    const float* A = sv->A32.as<float>();
+    const float* Ar = sv->A32r.as<float>();
+    const int nb = NB32_TC;
+    const size_t nblocks = sv->bounds.size() - 1;
+    DevBuf X((size_t)2 * nb * nrhs * sizeof(float), s);
+    float* Xh = X.as<float>();
+    float* Xl = Xh + (size_t)nb * nrhs;
+    for (size_t b = 0; b < nblocks; ++b) {   // L y = b
+        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
+        trsm_cols<float>(nrhs, (int)nk, A + k0 + k0 * ld, ld, false, B + k0, ldb, s, Ar + k0 + k0 * ld);
+        if (m > 0) {
+            split_cols((int)nk, nrhs, nb, B + k0, ldb, Xh, Xl, s);
+            const float* Wh = sv->W.as<float>() + sv->w_off[b];
+            gemm_tf32x3(m, nrhs, nk, -1.f, Wh, Wh + m * nb, nb, nb, 0, Xh, Xl, nb, nb, 0, 1.f, B + k1, ldb, false,
+                        sv->ctx->d_err, s);
+        }
+    }
+    negate_rows<float>(B, ldb, sv->nP, N, nrhs, s);
+    for (size_t bb = nblocks; bb-- > 0;) {   // L^T x = y, right-looking
+        const int64_t k0 = sv->bounds[bb], k1 = sv->bounds[bb + 1], nk = k1 - k0;
+        trsm_cols<float>(nrhs, (int)nk, A + k0 + k0 * ld, ld, true, B + k0, ldb, s, Ar + k0 + k0 * ld);
+        if (k0 > 0) {
+            split_cols((int)nk, nrhs, nb, B + k0, ldb, Xh, Xl, s);
+            gemm_tf32x3(k0, nrhs, nk, -1.f, A, Ar, ld, N, k0, Xh, Xl, nb, nb, 0, 1.f, B, ldb, false, sv->ctx->d_err,
+                        s);
+        }
+    }
+}
+
 // In place: B <- HM^-1 B (internal numbering), HM = L diag(+I_P, -I_V) L^T.
 template <typename T>
 static void solve_ldlt(omg_solver sv, const T* A, int64_t ld, T* B, int64_t ldb, int64_t nrhs) {
@@ -445,10 +530,11 @@ static void solver_factor(omg_solver sv, DevBuf&& hm) {
         factor_ldlt<double>(sv, sv->A64.as<double>(), N, NB64);
     } else {
         sv->A64 = std::move(hm);
-        sv->A32 = DevBuf((size_t)N * N * sizeof(float), s, sv->persistent);
-        copy_convert<double, float>(N, N, sv->A64.as<double>(), N, sv->A32.as<float>(), N, true, 1.0f, s);
+        sv->ld32 = (N + 31) / 32 * 32;
+        sv->A32 = DevBuf((size_t)sv->ld32 * N * sizeof(float), s, sv->persistent);
+        copy_convert<double, float>(N, N, sv->A64.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
         symmetrize(sv->A64.as<double>(), N, N, s);
-        factor_ldlt<float>(sv, sv->A32.as<float>(), N, NB32);
+        factor_ldlt_tc(sv, sv->A32.as<float>(), sv->ld32, NB32_TC);
     }
     check_err(sv->ctx, "factorization");
 }
@@ -482,7 +568,7 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
             ++steps;
         }
         scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, cn, sc.as<double>(), s);
-        solve_ldlt<float>(sv, sv->A32.as<float>(), N, B32.as<float>(), N, nrhs);
+        solve_ldlt_tc(sv, B32.as<float>(), N, nrhs);
         axpy_f32(N, nrhs, B32.as<float>(), N, x, N, sc.as<double>(), s);
         col_norms_f32(N, nrhs, B32.as<float>(), N, sc.as<double>(), dn.as<double>(), s);
         col_norms(N, nrhs, x, N, xn.as<double>(), s);

@@ -460,13 +460,13 @@ __global__ void __launch_bounds__(256) trsm_rows_kernel(int64_t m, int n, const 
 
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_cols_kernel(int64_t nrhs, int n, const T* __restrict__ L, int64_t ldl,
-                                                        int trans, T* B, int64_t ldb) {
+                                                        const T* __restrict__ Lr, int trans, T* B, int64_t ldb) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* sL = reinterpret_cast<T*>(smraw);   // n x n, sL[j*n + l] = (trans ? L[l][j] : L[j][l]) for the used part
     T* sx = sL + n * n;
     for (int e = threadIdx.x; e < n * n; e += 256) {   // coalesced: r runs down column c of L
         const int r = e % n, c = e / n;
-        const T v = (r >= c) ? L[r + c * ldl] : T(0);
+        const T v = (r >= c) ? (Lr ? L[r + c * ldl] + Lr[r + c * ldl] : L[r + c * ldl]) : T(0);
         if (trans)
             sL[c * n + r] = v;   // (L^T)[c][r]
         else
@@ -523,7 +523,8 @@ void trsm_rows(int64_t m, int n, const T* L, int64_t ldl, T* P, int64_t ldp, cud
     check("trsm_rows");
 }
 template <typename T>
-void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, int64_t ldb, cudaStream_t s) {
+void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, int64_t ldb, cudaStream_t s,
+               const T* Lr) {
     if (nrhs <= 0) return;
     ProfScope prof_("trsm_cols", s);
     static bool attr = false;
@@ -533,13 +534,14 @@ void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, i
     }
     const size_t sm = ((size_t)n * n + 8 * (size_t)n) * sizeof(T);
     const unsigned grid = (unsigned)std::min<int64_t>((nrhs + 7) / 8, 152 * 8);
-    trsm_cols_kernel<T><<<grid, 256, sm, s>>>(nrhs, n, L, ldl, trans ? 1 : 0, B, ldb);
+    trsm_cols_kernel<T><<<grid, 256, sm, s>>>(nrhs, n, L, ldl, Lr, trans ? 1 : 0, B, ldb);
     check("trsm_cols");
 }
 template void trsm_rows<double>(int64_t, int, const double*, int64_t, double*, int64_t, cudaStream_t);
 template void trsm_rows<float>(int64_t, int, const float*, int64_t, float*, int64_t, cudaStream_t);
-template void trsm_cols<double>(int64_t, int, const double*, int64_t, bool, double*, int64_t, cudaStream_t);
-template void trsm_cols<float>(int64_t, int, const float*, int64_t, bool, float*, int64_t, cudaStream_t);
+template void trsm_cols<double>(int64_t, int, const double*, int64_t, bool, double*, int64_t, cudaStream_t,
+                                const double*);
+template void trsm_cols<float>(int64_t, int, const float*, int64_t, bool, float*, int64_t, cudaStream_t, const float*);
 
 // Max-norm of each column of an m x n FP32 matrix scaled by colscale, and of
 // an FP64 matrix: one CTA per column (for the refinement stopping test).
