@@ -201,6 +201,12 @@ def run_gpu(args):
     def step(prec):
         return api.forward_gain(geo, dip, el, sq, precision=prec)
 
+    if args.only_mixed:
+        for _ in range(args.warmup + args.steps):
+            step("mixed")
+        torch.cuda.synchronize()
+        print(json.dumps({"only_mixed": True, "config": args.config, "steps": args.steps}))
+        return 0
     # FP64 drop-in on the same box (its result is the accuracy reference)
     step("fp64")
     torch.cuda.synchronize()
@@ -341,6 +347,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-mixed", action="store_true",
+                    help="profiling aid: run the mixed-precision steps only (no FP64 reference, e2e or CPU leg)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
