@@ -79,6 +79,9 @@ void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
 void split_lower_inplace(int64_t n, float* A, int64_t lda, float* R, cudaStream_t s);
+void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_t lda, float* Linv, cudaStream_t s);
+void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, float* B, int64_t ldb, float* H,
+                     float* L, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
                    cudaStream_t s);
 }  // namespace omg
@@ -101,6 +104,7 @@ struct omg_solver_s {
     DevBuf A32;                             // mixed: FP32 factor (TF32 heads after the split), ld = ld32
     DevBuf A32r;                            // mixed: FP32 remainders of the factor
     DevBuf W;                               // mixed: K-major head/remainder copies of every panel
+    DevBuf Linv32;                          // mixed: inverses of the 128 x 128 diagonal blocks
     std::vector<int64_t> w_off;             // offset (floats) of panel b's heads; remainders follow
     int64_t ld32 = 0;
     bool persistent = false;                // outlives the call that made it (public solver handle)
@@ -461,6 +465,8 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     }
     sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
     split_lower_inplace(N, A, ld, sv->A32r.as<float>(), s);
+    sv->Linv32 = DevBuf((size_t)nblocks * nb * nb * sizeof(float), s, sv->persistent);
+    inv_lower_blocks(N, nb, A, sv->A32r.as<float>(), ld, sv->Linv32.as<float>(), s);
 }
 
 // FP32 solve on the tensor cores: B <- HM^-1 B (internal numbering).
@@ -476,9 +482,8 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
     float* Xl = Xh + (size_t)nb * nrhs;
     for (size_t b = 0; b < nblocks; ++b) {   // L y = b
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
-        trsm_cols<float>(nrhs, (int)nk, A + k0 + k0 * ld, ld, false, B + k0, ldb, s, Ar + k0 + k0 * ld);
+        apply_inv_split((int)nk, nb, nrhs, sv->Linv32.as<float>() + b * nb * nb, false, B + k0, ldb, Xh, Xl, s);
         if (m > 0) {
-            split_cols((int)nk, nrhs, nb, B + k0, ldb, Xh, Xl, s);
             const float* Wh = sv->W.as<float>() + sv->w_off[b];
             gemm_tf32x3(m, nrhs, nk, -1.f, Wh, Wh + m * nb, nb, nb, 0, Xh, Xl, nb, nb, 0, 1.f, B + k1, ldb, false,
                         sv->ctx->d_err, s);
@@ -487,9 +492,8 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
     negate_rows<float>(B, ldb, sv->nP, N, nrhs, s);
     for (size_t bb = nblocks; bb-- > 0;) {   // L^T x = y, right-looking
         const int64_t k0 = sv->bounds[bb], k1 = sv->bounds[bb + 1], nk = k1 - k0;
-        trsm_cols<float>(nrhs, (int)nk, A + k0 + k0 * ld, ld, true, B + k0, ldb, s, Ar + k0 + k0 * ld);
+        apply_inv_split((int)nk, nb, nrhs, sv->Linv32.as<float>() + bb * nb * nb, true, B + k0, ldb, Xh, Xl, s);
         if (k0 > 0) {
-            split_cols((int)nk, nrhs, nb, B + k0, ldb, Xh, Xl, s);
             gemm_tf32x3(k0, nrhs, nk, -1.f, A, Ar, ld, N, k0, Xh, Xl, nb, nb, 0, 1.f, B, ldb, false, sv->ctx->d_err,
                         s);
         }
@@ -606,7 +610,8 @@ static void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t
 // Sources / sensors
 // ---------------------------------------------------------------------------
 static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain,
-                         int perm, double* out, int64_t ldo, int precision = OMG_PREC_FP64) {
+                         int perm, double* out, int64_t ldo, int precision = OMG_PREC_FP64,
+                         std::vector<int>* meshes_used = nullptr) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     check_integrator(integ, true);
@@ -621,6 +626,18 @@ static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const om
     launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s);
     launch_domain_lookup(nd, g->h.nmesh, sa.as<double>(), g->ndom, g->maxb, g->dnb, g->bmesh, g->binside, g->orient,
                          domain, dom.as<int>(), ctx->d_err, s);
+    if (meshes_used) {   // which meshes carry nonzero DSM rows: boundaries of the dipoles' domains
+        std::vector<int> hdom(nd);
+        OMG_CUDA(cudaMemcpyAsync(hdom.data(), dom.p, nd * sizeof(int), cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+        std::vector<char> used(g->h.nmesh, 0);
+        for (int d : hdom)
+            if (d >= 0 && g->h.domains[d].sigma != 0.0)
+                for (const auto& b : g->h.domains[d].bounds) used[b.mesh] = 1;
+        meshes_used->clear();
+        for (int m = 0; m < g->h.nmesh; ++m)
+            if (used[m]) meshes_used->push_back(m);
+    }
     // chunk the dipoles so the P1 scratch stays near 512 MB
     const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (g->h.nt * 24)));
     DevBuf p1((size_t)std::min(per, nd) * g->h.nt * 24, s);
@@ -986,15 +1003,41 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
     if (nm > 0) launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
     if (precision == OMG_PREC_MIXED) ensure_gg_tables(geo);
-    dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision);
+    std::vector<int> src_meshes;
+    dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, &src_meshes);
     if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s);
     OMG_CUDA(cudaEventRecord(ev[2], s));
     solver_factor(sv.get(), std::move(hm));
     OMG_CUDA(cudaEventRecord(ev[3], s));
     solver_solve_internal(sv.get(), B.as<double>(), N, k);
-    if (ne > 0) gemm<double>(ne, nd, N, 1.0, B.as<double>(), N, true, DSM.as<double>(), N, false, 0.0, geeg, ne, s);
-    if (nm > 0)
-        gemm<double>(nm, nd, N, 1.0, B.as<double>() + ne * N, N, true, DSM.as<double>(), N, false, 1.0, gmeg, nm, s);
+    // G = Y^T DSM over the rows where DSM can be nonzero (the source meshes' triangles and vertices)
+    std::vector<std::pair<int64_t, int64_t>> kr;
+    for (int m : src_meshes) {
+        if (!geo->h.barrier[m])
+            kr.push_back({geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv, geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv +
+                                                                       (geo->h.tbeg[m + 1] - geo->h.tbeg[m])});
+        kr.push_back({geo->d.nP + geo->h.vbeg[m], geo->d.nP + geo->h.vbeg[m + 1]});
+    }
+    std::sort(kr.begin(), kr.end());
+    std::vector<std::pair<int64_t, int64_t>> merged;
+    for (const auto& r : kr) {
+        if (!merged.empty() && r.first <= merged.back().second)
+            merged.back().second = std::max(merged.back().second, r.second);
+        else
+            merged.push_back(r);
+    }
+    if (ne > 0 && nd > 0) {
+        if (merged.empty()) OMG_CUDA(cudaMemsetAsync(geeg, 0, (size_t)ne * nd * 8, s));
+        for (size_t q = 0; q < merged.size(); ++q) {
+            const int64_t r0 = merged[q].first, kk = merged[q].second - merged[q].first;
+            gemm<double>(ne, nd, kk, 1.0, B.as<double>() + r0, N, true, DSM.as<double>() + r0, N, false,
+                         q == 0 ? 0.0 : 1.0, geeg, ne, s);
+        }
+    }
+    if (nm > 0 && nd > 0)
+        for (const auto& r : merged)
+            gemm<double>(nm, nd, r.second - r.first, 1.0, B.as<double>() + ne * N + r.first, N, true,
+                         DSM.as<double>() + r.first, N, false, 1.0, gmeg, nm, s);
     OMG_CUDA(cudaEventRecord(ev[4], s));
     check_err(ctx, "gain");
     if (st) {

@@ -591,4 +591,115 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
     check("col_amax");
 }
 
+// ---------------------------------------------------------------------------
+// Explicit inverses of the diagonal blocks of a lower-triangular factor
+// (block b starts at b*128; the factor may be split as head + remainder).
+// One CTA per block; each warp solves L x = e_c for its columns c with the
+// block staged in shared memory.  Output: Linv (nblk x 128 x 128, column-
+// major, zero above the diagonal).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) inv_lower_blocks_kernel(int64_t N, int nb, const float* __restrict__ A,
+                                                               const float* __restrict__ Ar, int64_t lda,
+                                                               float* Linv) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float* sL = reinterpret_cast<float*>(smraw);   // n x n row-major: sL[j*n + l] = L[j][l]
+    float* sx = sL + nb * nb;                      // 8 warps x n
+    const int64_t k0 = (int64_t)blockIdx.x * nb;
+    const int n = (int)((N - k0) < nb ? (N - k0) : nb);
+    const float* Ab = A + k0 + k0 * lda;
+    const float* Rb = Ar ? Ar + k0 + k0 * lda : nullptr;
+    for (int e = threadIdx.x; e < n * n; e += 256) {
+        const int r = e % n, c = e / n;
+        sL[r * n + c] = (r >= c) ? (Rb ? Ab[r + c * lda] + Rb[r + c * lda] : Ab[r + c * lda]) : 0.f;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    float* x = sx + warp * n;
+    float* out = Linv + (int64_t)blockIdx.x * nb * nb;
+    for (int c = warp; c < nb; c += 8) {
+        if (c >= n) {   // identity on the unused part of a short last block
+            for (int i = lane; i < nb; i += 32) out[i + c * nb] = (i == c) ? 1.f : 0.f;
+            continue;
+        }
+        for (int l = lane; l < n; l += 32) x[l] = 0.f;
+        __syncwarp();
+        for (int j = c; j < n; ++j) {
+            float acc = 0.f;
+            for (int l = c + lane; l < j; l += 32) acc += sL[j * n + l] * x[l];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) x[j] = ((j == c ? 1.f : 0.f) - acc) / sL[j * n + j];
+            __syncwarp();
+        }
+        for (int i = lane; i < nb; i += 32) out[i + c * nb] = (i < n) ? x[i] : 0.f;
+        __syncwarp();
+    }
+}
+
+void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_t lda, float* Linv, cudaStream_t s) {
+    ProfScope prof_("inv_blocks", s);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(inv_lower_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    const unsigned nblk_ = (unsigned)((N + nb - 1) / nb);
+    const size_t sm = ((size_t)nb * nb + 8 * (size_t)nb) * sizeof(float);
+    inv_lower_blocks_kernel<<<nblk_, 256, sm, s>>>(N, nb, A, Ar, lda, Linv);
+    check("inv_lower_blocks");
+}
+
+// B_k <- op(Linv_k) B_k for the n x ncol block at B (ldb), op = transpose if
+// `trans`; also writes the TF32 head/remainder split of the result as K-major
+// rows (column j -> row j of H/L, kpad = nb) for the following tensor-core
+// update.  One warp per column, Linv_k staged in shared memory.
+__global__ void __launch_bounds__(256) apply_inv_split_kernel(int n, int nb, int64_t ncol, const float* __restrict__ Li,
+                                                              int trans, float* B, int64_t ldb, float* H, float* L) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int ldm = nb + 1;                        // padded rows: lanes read different rows at the same l
+    float* sM = reinterpret_cast<float*>(smraw);   // nb x nb, sM[i*ldm + l] = op(Linv)[i][l]
+    float* sb = sM + nb * ldm;                     // 8 warps x nb
+    for (int e = threadIdx.x; e < nb * nb; e += 256) {
+        const int r = e % nb, c = e / nb;          // coalesced read of column-major Linv
+        const float v = Li[r + c * nb];
+        if (trans)
+            sM[c * ldm + r] = v;
+        else
+            sM[r * ldm + c] = v;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    float* b = sb + warp * nb;
+    for (int64_t j = (int64_t)blockIdx.x * 8 + warp; j < ncol; j += (int64_t)gridDim.x * 8) {
+        float* bj = B + j * ldb;
+        for (int l = lane; l < nb; l += 32) b[l] = l < n ? bj[l] : 0.f;
+        __syncwarp();
+        for (int i = lane; i < nb; i += 32) {
+            float acc = 0.f;
+            const float* row = sM + i * ldm;
+            for (int l = 0; l < nb; ++l) acc = fmaf(row[l], b[l], acc);
+            const float h = __uint_as_float(__float_as_uint(acc) & 0xFFFFE000u);
+            H[j * nb + i] = (i < n) ? h : 0.f;
+            L[j * nb + i] = (i < n) ? acc - h : 0.f;
+            if (i < n) bj[i] = acc;
+        }
+        __syncwarp();
+    }
+}
+
+void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, float* B, int64_t ldb, float* H,
+                     float* L, cudaStream_t s) {
+    if (ncol <= 0) return;
+    ProfScope prof_("apply_inv", s);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(apply_inv_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr = true;
+    }
+    const size_t sm = ((size_t)nb * (nb + 1) + 8 * (size_t)nb) * sizeof(float);
+    const unsigned grid = (unsigned)std::min<int64_t>((ncol + 7) / 8, 1024);
+    apply_inv_split_kernel<<<grid, 256, sm, s>>>(n, nb, ncol, Li, trans ? 1 : 0, B, ldb, H, L);
+    check("apply_inv_split");
+}
+
 }  // namespace omg

@@ -184,14 +184,20 @@ __global__ void __launch_bounds__(128, 1)
             uint32_t r[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(chunk * 32), r);
             if (row < M) {
+                // All loads of the chunk first (independent, in flight together), then the stores.
+                float cv[32];
+                const int64_t cbase = (int64_t)row + (int64_t)(n0 + chunk * 32) * ldc;
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int col = n0 + chunk * 32 + j;
-                    if (col < N && (!lower || row >= col)) {
-                        float* c = C + (int64_t)row + (int64_t)col * ldc;
-                        const float acc = __uint_as_float(r[j]);
-                        *c = (beta == 0.f) ? alpha * acc : fmaf(alpha, acc, beta * *c);
-                    }
+                    const bool ok = col < N && (!lower || row >= col);
+                    cv[j] = (ok && beta != 0.f) ? __ldcg(C + cbase + (int64_t)j * ldc) : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int col = n0 + chunk * 32 + j;
+                    if (col < N && (!lower || row >= col))
+                        __stcg(C + cbase + (int64_t)j * ldc, fmaf(alpha, __uint_as_float(r[j]), beta * cv[j]));
                 }
             }
         }
