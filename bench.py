@@ -201,11 +201,11 @@ def run_gpu(args):
     def step(prec):
         return api.forward_gain(geo, dip, el, sq, precision=prec)
 
-    if args.only_mixed:
+    if args.only_mixed or args.only_fp64:
         for _ in range(args.warmup + args.steps):
-            step("mixed")
+            step("mixed" if args.only_mixed else "fp64")
         torch.cuda.synchronize()
-        print(json.dumps({"only_mixed": True, "config": args.config, "steps": args.steps}))
+        print(json.dumps({"only": "mixed" if args.only_mixed else "fp64", "config": args.config, "steps": args.steps}))
         return 0
     # FP64 drop-in on the same box (its result is the accuracy reference)
     step("fp64")
@@ -349,6 +349,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-mixed", action="store_true",
                     help="profiling aid: run the mixed-precision steps only (no FP64 reference, e2e or CPU leg)")
+    ap.add_argument("--only-fp64", action="store_true", help="profiling aid: run FP64 drop-in steps only")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
