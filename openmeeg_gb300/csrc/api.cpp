@@ -62,8 +62,10 @@ void axpy_f32(int64_t m, int64_t n, const float* d, int64_t ldd, double* x, int6
               cudaStream_t s);
 void scale_to_f32(int64_t m, int64_t n, const double* r, int64_t ldr, float* b, int64_t ldb, const double* colnorm,
                   double* colscale, cudaStream_t s);
-void residual_df64(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* X, int64_t ldx,
-                   const double* B, int64_t ldb, double* R, int64_t ldr, cudaStream_t s);
+void residual_df64(int64_t M, int64_t N, int64_t K, const float* Ahi, const float* Alo, int64_t lda,
+                   const float* Xhi, const float* Xlo, int64_t ldx, const double* B, int64_t ldb, double* R,
+                   int64_t ldr, cudaStream_t s);
+void split_f64(int64_t m, int64_t n, const double* A, int64_t lda, float* H, float* L, int64_t ldo, cudaStream_t s);
 template <typename T>
 void potrf(T* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, cudaStream_t s);
 template <typename T>
@@ -100,7 +102,8 @@ struct omg_solver_s {
     int precision = OMG_PREC_FP64;
     int64_t N = 0, nP = 0;
     std::vector<int64_t> bounds;            // block boundaries (include nP)
-    DevBuf A64;                             // FP64: factor (lower). Mixed: symmetrized FP64 HeadMat
+    DevBuf A64;                             // FP64: factor (lower).  Mixed: the head matrix as float pairs
+                                            // (hi, lo; 2 x N x N floats) for the refinement residual
     DevBuf A32;                             // mixed: FP32 factor (TF32 heads after the split), ld = ld32
     DevBuf A32r;                            // mixed: FP32 remainders of the factor
     DevBuf W;                               // mixed: K-major head/remainder copies of every panel
@@ -533,11 +536,14 @@ static void solver_factor(omg_solver sv, DevBuf&& hm) {
         sv->A64 = std::move(hm);
         factor_ldlt<double>(sv, sv->A64.as<double>(), N, NB64);
     } else {
-        sv->A64 = std::move(hm);
         sv->ld32 = (N + 31) / 32 * 32;
         sv->A32 = DevBuf((size_t)sv->ld32 * N * sizeof(float), s, sv->persistent);
-        copy_convert<double, float>(N, N, sv->A64.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
-        symmetrize(sv->A64.as<double>(), N, N, s);
+        copy_convert<double, float>(N, N, hm.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
+        symmetrize(hm.as<double>(), N, N, s);
+        // the FP64 matrix is kept only as an exact float pair (hi + lo) for the residual
+        sv->A64 = DevBuf((size_t)2 * N * N * sizeof(float), s, sv->persistent);
+        split_f64(N, N, hm.as<double>(), N, sv->A64.as<float>(), sv->A64.as<float>() + (size_t)N * N, N, s);
+        hm.release();
         factor_ldlt_tc(sv, sv->A32.as<float>(), sv->ld32, NB32_TC);
     }
     check_err(sv->ctx, "factorization");
@@ -551,7 +557,8 @@ static void solver_factor(omg_solver sv, DevBuf&& hm) {
 static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
-    DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s);
+    DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s),
+        XS((size_t)2 * N * nrhs * 4, s);
     DevBuf rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s), dn((size_t)nrhs * 8, s), xn((size_t)nrhs * 8, s),
         bn((size_t)nrhs * 8, s);
     double* x = X.as<double>();
@@ -566,7 +573,10 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     double last_res = 1.0, est = 1.0, prev_est = 1e300;
     for (int it = 0; it <= sv->max_refine; ++it) {
         if (it > 0) {   // r = b - HM x
-            residual_df64(N, nrhs, N, sv->A64.as<double>(), N, x, N, B, ldb, r, N, s);
+            float* xh = XS.as<float>();
+            split_f64(N, nrhs, x, N, xh, xh + (size_t)N * nrhs, N, s);
+            const float* ah = sv->A64.as<float>();
+            residual_df64(N, nrhs, N, ah, ah + (size_t)N * N, N, xh, xh + (size_t)N * nrhs, N, B, ldb, r, N, s);
             col_norms(N, nrhs, r, N, rn.as<double>(), s);
             cn = rn.as<double>();
             ++steps;

@@ -282,9 +282,13 @@ void scale_to_f32(int64_t m, int64_t n, const double* r, int64_t ldr, float* b, 
 // ---------------------------------------------------------------------------
 constexpr int RB_M = 64, RB_N = 32, RB_K = 16, RB_TM = 4, RB_TN = 2;   // 256 threads
 
+// Operands arrive pre-split (A = Ah + Al, X = Xh + Xl, float pairs, see
+// split_f64), so the inner loop runs on the FP32 pipe only.
 __global__ void __launch_bounds__(256) residual_df64_kernel(int64_t M, int64_t N, int64_t K,
-                                                           const double* __restrict__ A, int64_t lda,
-                                                           const double* __restrict__ X, int64_t ldx,
+                                                           const float* __restrict__ Ahi,
+                                                           const float* __restrict__ Alo, int64_t lda,
+                                                           const float* __restrict__ Xhi,
+                                                           const float* __restrict__ Xlo, int64_t ldx,
                                                            const double* __restrict__ B, int64_t ldb, double* R,
                                                            int64_t ldr) {
     __shared__ float Ah[RB_K][RB_M + 1], Al[RB_K][RB_M + 1];
@@ -301,18 +305,16 @@ __global__ void __launch_bounds__(256) residual_df64_kernel(int64_t M, int64_t N
         for (int e = tid; e < RB_M * RB_K; e += 256) {
             const int i = e % RB_M, k = e / RB_M;
             const int64_t gi = m0 + i, gk = k0 + k;
-            const double v = (gi < M && gk < K) ? A[gi + gk * lda] : 0.0;
-            const float h = (float)v;
-            Ah[k][i] = h;
-            Al[k][i] = (float)(v - (double)h);
+            const bool ok = gi < M && gk < K;
+            Ah[k][i] = ok ? Ahi[gi + gk * lda] : 0.f;
+            Al[k][i] = ok ? Alo[gi + gk * lda] : 0.f;
         }
         for (int e = tid; e < RB_N * RB_K; e += 256) {
             const int k = e % RB_K, j = e / RB_K;
             const int64_t gj = n0 + j, gk = k0 + k;
-            const double v = (gj < N && gk < K) ? X[gk + gj * ldx] : 0.0;
-            const float h = (float)v;
-            Xh[k][j] = h;
-            Xl[k][j] = (float)(v - (double)h);
+            const bool ok = gj < N && gk < K;
+            Xh[k][j] = ok ? Xhi[gk + gj * ldx] : 0.f;
+            Xl[k][j] = ok ? Xlo[gk + gj * ldx] : 0.f;
         }
         __syncthreads();
 #pragma unroll 4
@@ -352,13 +354,34 @@ __global__ void __launch_bounds__(256) residual_df64_kernel(int64_t M, int64_t N
     }
 }
 
-void residual_df64(int64_t M, int64_t N, int64_t K, const double* A, int64_t lda, const double* X, int64_t ldx,
-                   const double* B, int64_t ldb, double* R, int64_t ldr, cudaStream_t s) {
+void residual_df64(int64_t M, int64_t N, int64_t K, const float* Ahi, const float* Alo, int64_t lda,
+                   const float* Xhi, const float* Xlo, int64_t ldx, const double* B, int64_t ldb, double* R,
+                   int64_t ldr, cudaStream_t s) {
     if (M <= 0 || N <= 0) return;
     ProfScope prof_("residual_df64", s);
     dim3 grid(nblk(N, RB_N), nblk(M, RB_M));
-    residual_df64_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, X, ldx, B, ldb, R, ldr);
+    residual_df64_kernel<<<grid, 256, 0, s>>>(M, N, K, Ahi, Alo, lda, Xhi, Xlo, ldx, B, ldb, R, ldr);
     check("residual_df64");
+}
+
+// FP64 m x n (lda) -> float pair hi = fl(a), lo = fl(a - hi), column-major (ldo).
+__global__ void split_f64_kernel(int64_t m, int64_t n, const double* __restrict__ A, int64_t lda, float* H, float* L,
+                                 int64_t ldo) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+        const double v = A[i + j * lda];
+        const float h = (float)v;
+        H[i + j * ldo] = h;
+        L[i + j * ldo] = (float)(v - (double)h);
+    }
+}
+void split_f64(int64_t m, int64_t n, const double* A, int64_t lda, float* H, float* L, int64_t ldo, cudaStream_t s) {
+    if (m <= 0 || n <= 0) return;
+    ProfScope prof_("split_f64", s);
+    dim3 grid(nblk(m, 256), (unsigned)std::min<int64_t>(n, 32768));
+    split_f64_kernel<<<grid, 256, 0, s>>>(m, n, A, lda, H, L, ldo);
+    check("split_f64");
 }
 
 // ---------------------------------------------------------------------------
