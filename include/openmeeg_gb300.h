@@ -156,6 +156,43 @@ int omg_head2megmat_noalloc_dev(omg_context ctx, omg_geometry geo, const double*
 int omg_dipsource2megmat_dev(omg_context ctx, const double* dipoles, int64_t n_dipoles, const double* squids,
                              int64_t n_squids, double* ds2mm);
 
+/* ---- adjoint (gradients) -------------------------------------------------- *
+ * Building blocks of the vector-Jacobian products of the gain with respect to
+ * the conductivities and the dipoles (no counterpart in the reference, which
+ * has no derivatives). */
+typedef struct {
+    int64_t vbeg, vend;        /* vertex unknowns of the mesh (reference numbering) */
+    int64_t tri_unknown;       /* first triangle unknown, -1 for a current barrier */
+    int64_t n_triangles;
+    int32_t barrier;           /* touches a zero-conductivity domain */
+    int32_t orientation;       /* interface orientation (+1/-1) */
+    int32_t outermost;
+    int32_t reserved;
+} omg_mesh_layout;
+typedef struct {
+    int32_t m1, m2, orientation, reserved;
+    double cS, cN, cD;         /* S, N, D block coefficients (assembleHeadMat.cpp:92-95) */
+} omg_mesh_pair;
+int omg_geometry_get_layout(omg_geometry geo, int32_t max_meshes, omg_mesh_layout* out);
+int omg_geometry_get_pairs(omg_geometry geo, int32_t max_pairs, omg_mesh_pair* out, int32_t* n_pairs);
+/* Domain index of each dipole position (Geometry::domain(point)); -1 if none. */
+int omg_dipole_domains_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                           int32_t* domains);
+/* Head2MEGMat contribution of one mesh with a unit conductivity jump
+ * (assembleFerguson.cpp:18-31 without the jump factor): out n_squids x N. */
+int omg_head2megmat_mesh_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids,
+                             int32_t mesh, double* out);
+/* d/d(position, moment) of sum_rows U[row, j] DSM[row, j] for every dipole j:
+ * U is N x n_dipoles (reference numbering, leading dimension ldu); out is
+ * n_dipoles x 6 row-major (dx dy dz dqx dqy dqz).  Same integrator and
+ * adaptive trees as omg_dipsourcemat_dev. */
+int omg_dipsourcemat_vjp_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                             const omg_integrator* integ, int32_t domain, const double* U, int64_t ldu,
+                             double* out);
+/* C = alpha op(A) op(B) + beta C in FP64 (column-major; trans = 1 transposes). */
+int omg_gemm_f64_dev(omg_context ctx, int32_t trans_a, int32_t trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                     const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
+
 /* ---- dense solve ---------------------------------------------------------- *
  * Replaces SymMatrix::solveLin / linsolve (OpenMEEGMaths/src/symmatrix.cpp:133-152,
  * OpenMEEG/include/gain.h:52-57): the solver owns a factorization of HeadMat.

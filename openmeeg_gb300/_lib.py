@@ -51,6 +51,16 @@ class GeometryInfo(ctypes.Structure):
                 ("n_mesh_pairs", c_i32), ("nested", c_i32)]
 
 
+class MeshLayout(ctypes.Structure):
+    _fields_ = [("vbeg", c_i64), ("vend", c_i64), ("tri_unknown", c_i64), ("n_triangles", c_i64), ("barrier", c_i32),
+                ("orientation", c_i32), ("outermost", c_i32), ("reserved", c_i32)]
+
+
+class MeshPair(ctypes.Structure):
+    _fields_ = [("m1", c_i32), ("m2", c_i32), ("orientation", c_i32), ("reserved", c_i32), ("cS", c_dbl),
+                ("cN", c_dbl), ("cD", c_dbl)]
+
+
 class GainStats(ctypes.Structure):
     _fields_ = [("t_total_ms", c_dbl), ("t_headmat_ms", c_dbl), ("t_sources_ms", c_dbl), ("t_factor_ms", c_dbl),
                 ("t_solve_ms", c_dbl), ("refinement_steps", c_i32), ("gmres_iterations", c_i32),
@@ -84,6 +94,14 @@ _PROTOS = [
     ("omg_head2megmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
     ("omg_head2megmat_noalloc_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
     ("omg_dipsource2megmat_dev", c_i32, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp]),
+    ("omg_geometry_get_layout", c_i32, [c_vp, c_i32, ctypes.POINTER(MeshLayout)]),
+    ("omg_geometry_get_pairs", c_i32, [c_vp, c_i32, ctypes.POINTER(MeshPair), P_i32]),
+    ("omg_dipole_domains_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
+    ("omg_head2megmat_mesh_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_i32, c_vp]),
+    ("omg_dipsourcemat_vjp_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, ctypes.POINTER(Integrator), c_i32, c_vp, c_i64,
+                                         c_vp]),
+    ("omg_gemm_f64_dev", c_i32, [c_vp, c_i32, c_i32, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp, c_i64, c_dbl,
+                                 c_vp, c_i64]),
     ("omg_solver_create", c_i32, [c_vp, c_vp, ctypes.POINTER(Integrator), c_i32, ctypes.POINTER(c_vp)]),
     ("omg_solver_from_headmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_i32, ctypes.POINTER(c_vp)]),
     ("omg_solver_solve_dev", c_i32, [c_vp, c_vp, c_i64, c_i64]),

@@ -37,6 +37,10 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s);
+void launch_dsm_vjp(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
+                    const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
+                    const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
+                    double tol, const double* U, int64_t ldu, double* part, double* out, cudaStream_t s);
 void launch_pad_identity(const DevGeom& g, double* hm, int64_t ld, cudaStream_t s);
 void launch_ff_block(const DevGeom& g, const float* grec, int64_t t1b, int64_t t1e, int64_t t2b, int64_t t2e,
                      bool same, bool wantS, bool wantD12, bool wantD21, double cS, double* hm, int64_t ld,
@@ -894,6 +898,115 @@ int omg_dipsource2megmat_dev(omg_context ctx, const double* dipoles, int64_t n_d
         OMG_REQUIRE(ctx && (n_dipoles == 0 || n_squids == 0 || (dipoles && squids && ds2mm)), "null argument");
         set_device(ctx);
         launch_ds2mm(dipoles, n_dipoles, squids, n_squids, ds2mm, n_squids, ctx->stream);
+        OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int omg_geometry_get_layout(omg_geometry geo, int32_t max_meshes, omg_mesh_layout* out) {
+    return guarded([&] {
+        OMG_REQUIRE(geo && out, "null argument");
+        const HostGeometry& h = geo->h;
+        OMG_REQUIRE(max_meshes >= h.nmesh, "output too small");
+        for (int m = 0; m < h.nmesh; ++m) {
+            omg_mesh_layout& L = out[m];
+            L.vbeg = h.vbeg[m];
+            L.vend = h.vbeg[m + 1];
+            L.tri_unknown = h.barrier[m] ? -1 : h.tidx[h.tbeg[m]];
+            L.n_triangles = h.tbeg[m + 1] - h.tbeg[m];
+            L.barrier = h.barrier[m];
+            L.orientation = h.orient[m];
+            L.outermost = h.outermost[m];
+            L.reserved = 0;
+        }
+    });
+}
+
+int omg_geometry_get_pairs(omg_geometry geo, int32_t max_pairs, omg_mesh_pair* out, int32_t* n_pairs) {
+    return guarded([&] {
+        OMG_REQUIRE(geo && n_pairs, "null argument");
+        const auto& P = geo->h.pairs;
+        *n_pairs = (int32_t)P.size();
+        if (!out) return;
+        OMG_REQUIRE(max_pairs >= (int32_t)P.size(), "output too small");
+        for (size_t k = 0; k < P.size(); ++k) out[k] = {P[k].m1, P[k].m2, P[k].orientation, 0, P[k].cS, P[k].cN, P[k].cD};
+    });
+}
+
+int omg_dipole_domains_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                           int32_t* domains) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_dipoles == 0 || (dipoles && domains)), "null argument");
+        set_device(ctx);
+        reset_err(ctx);
+        if (n_dipoles == 0) return;
+        cudaStream_t s = ctx->stream;
+        DevBuf sa((size_t)n_dipoles * geo->h.nmesh * 8, s);
+        launch_mesh_solid_angles(dipoles, 6, n_dipoles, geo->h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+        launch_domain_lookup(n_dipoles, geo->h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
+                             geo->binside, geo->orient, -1, domains, ctx->d_err, s);
+        OMG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int omg_head2megmat_mesh_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids, int32_t mesh,
+                             double* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_squids == 0 || (squids && out)), "null argument");
+        OMG_REQUIRE(mesh >= 0 && mesh < geo->h.nmesh, "mesh index out of range");
+        set_device(ctx);
+        reset_err(ctx);
+        if (n_squids == 0) return;
+        cudaStream_t s = ctx->stream;
+        std::vector<double> unit(geo->h.nmesh, 0.0);
+        unit[mesh] = 1.0;
+        DevBuf jump(unit.size() * 8, s), F((size_t)n_squids * geo->h.nt * 8, s);
+        OMG_CUDA(cudaMemcpyAsync(jump.p, unit.data(), unit.size() * 8, cudaMemcpyHostToDevice, s));
+        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)n_squids * geo->h.N * 8, s));
+        launch_h2mm(geo->d, squids, n_squids, geo->tmesh, jump.as<double>(), 0, out, n_squids, 1, 0, F.as<double>(), s);
+        check_err(ctx, "Head2MEGMat (one mesh)");
+    });
+}
+
+int omg_dipsourcemat_vjp_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                             const omg_integrator* integ, int32_t domain, const double* U, int64_t ldu, double* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_dipoles == 0 || (dipoles && U && out)), "null argument");
+        OMG_REQUIRE(ldu >= geo->h.N, "ldu must be >= N");
+        OMG_REQUIRE(domain >= -1 && domain < geo->ndom, "domain index out of range");
+        set_device(ctx);
+        reset_err(ctx);
+        if (n_dipoles == 0) return;
+        const omg_integrator it = integ ? *integ : default_dsm_integrator();
+        check_integrator(it, true);
+        cudaStream_t s = ctx->stream;
+        DevBuf sa((size_t)n_dipoles * geo->h.nmesh * 8, s), dom((size_t)n_dipoles * sizeof(int), s);
+        launch_mesh_solid_angles(dipoles, 6, n_dipoles, geo->h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+        launch_domain_lookup(n_dipoles, geo->h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
+                             geo->binside, geo->orient, domain, dom.as<int>(), ctx->d_err, s);
+        const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (geo->h.nt * 48)));
+        DevBuf part((size_t)std::min(per, n_dipoles) * geo->h.nt * 48, s);
+        for (int64_t d0 = 0; d0 < n_dipoles; d0 += per) {
+            const int64_t n = std::min(per, n_dipoles - d0);
+            launch_dsm_vjp(geo->d, d0, n, dipoles, geo->tmesh, geo->tidx_ref, geo->barrier, geo->orient, dom.as<int>(),
+                           geo->maxb, geo->dnb, geo->bmesh, geo->binside, geo->dsigma, it.order, it.levels, it.tol, U,
+                           ldu, part.as<double>(), out, s);
+        }
+        check_err(ctx, "DipSourceMat vjp");
+    });
+}
+
+int omg_gemm_f64_dev(omg_context ctx, int32_t trans_a, int32_t trans_b, int64_t m, int64_t n, int64_t k, double alpha,
+                     const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && (m == 0 || n == 0 || (A && B && C)), "null argument");
+        set_device(ctx);
+        if (k == 0) {
+            OMG_REQUIRE(beta == 0.0 || beta == 1.0, "k = 0 with a general beta is not supported");
+            if (beta == 0.0)
+                for (int64_t j = 0; j < n; ++j) OMG_CUDA(cudaMemsetAsync(C + j * ldc, 0, (size_t)m * 8, ctx->stream));
+        } else {
+            gemm<double>(m, n, k, alpha, A, lda, trans_a != 0, B, ldb, trans_b != 0, beta, C, ldc, ctx->stream);
+        }
         OMG_CUDA(cudaStreamSynchronize(ctx->stream));
     });
 }

@@ -1298,4 +1298,206 @@ void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, d
     check_launch("DS2MM");
 }
 
+// ===========================================================================
+// DipSourceMat vector-Jacobian product: for each dipole j,
+//   d/d(r0_j, q_j) of  sum_rows U[row, j] * DSM[row, j]
+// from the analytic derivatives of the integrands (Dipole::potential and
+// Dipole::gradient, dipole.h:29-46) integrated over the same adaptive trees as
+// the forward assembly (integrator.h:228-252): refinement decisions come from
+// the forward integrand, so this is the exact derivative of the assembled
+// (piecewise) DSM.
+// ===========================================================================
+struct VjpW {
+    double W[3];   // U at the triangle's vertices x coeffD (P1 rows)
+    double w0;     // U at the triangle's row x coeffD / sigma (P0 row; 0 on current barriers)
+};
+
+// Derivative integrand: kind 0 -> w1(r) * d g / d(r0, q); kind 1 -> w0 * d p / d(r0, q).
+__device__ __forceinline__ void dsm_vjp_point(int kind, const DsmTri& T, d3 r0, d3 q, d3 r, const VjpW& w,
+                                              double out[6]) {
+    const d3 x = r - r0;
+    const double inv = 1.0 / dev::dot(x, x);
+    const double inv3 = inv * sqrt(inv), inv5 = inv3 * inv, inv7 = inv5 * inv;
+    const double qx = dev::dot(q, x);
+    if (kind == 1) {
+        // p = (q.x)/|x|^3 ; dp/dq = x/|x|^3 ; dp/dr0 = -(q/|x|^3 - 3 (q.x) x/|x|^5)
+        const d3 dq = x * inv3;
+        const d3 dx = q * inv3 - x * (3.0 * qx * inv5);
+        out[0] = -w.w0 * dx.x; out[1] = -w.w0 * dx.y; out[2] = -w.w0 * dx.z;
+        out[3] = w.w0 * dq.x; out[4] = w.w0 * dq.y; out[5] = w.w0 * dq.z;
+        return;
+    }
+    const d3 n = T.n;
+    const double xn = dev::dot(x, n), qn = dev::dot(q, n);
+    // g = (q.n)/|x|^3 - 3 (q.x)(x.n)/|x|^5
+    const d3 dq = n * inv3 - x * (3.0 * xn * inv5);
+    const d3 dx = x * (-3.0 * qn * inv5 + 15.0 * qx * xn * inv7) - q * (3.0 * xn * inv5) - n * (3.0 * qx * inv5);
+    const d3 v = r - T.p0;
+    const double a1 = dev::dot(v, T.e10), a2 = dev::dot(v, T.e20);
+    const double l1 = T.d11 * a1 + T.d12 * a2, l2 = T.d12 * a1 + T.d22 * a2, l0 = 1.0 - l1 - l2;
+    const double w1 = w.W[0] * l0 + w.W[1] * l1 + w.W[2] * l2;
+    out[0] = -w1 * dx.x; out[1] = -w1 * dx.y; out[2] = -w1 * dx.z;
+    out[3] = w1 * dq.x; out[4] = w1 * dq.y; out[5] = w1 * dq.z;
+}
+
+__device__ __forceinline__ void dsm_vjp_rule(int kind, int order, const DsmTri& T, d3 r0, d3 q, const VjpW& w,
+                                             d3 P0, d3 P1, d3 P2, double area, double acc[6]) {
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    const int np = c_nbpts[order];
+    for (int k = 0; k < np; ++k) {
+        const d3 xk = bary_point(c_rules[order][k], P0, P1, P2);
+        double e[6];
+        dsm_vjp_point(kind, T, r0, q, xk, w, e);
+        const double wk = c_rules[order][k][3];
+        for (int c = 0; c < 6; ++c) s[c] += wk * e[c];
+    }
+    for (int c = 0; c < 6; ++c) acc[c] += area * s[c];
+}
+
+// Same traversal as dsm_adaptive; accepted nodes contribute the derivative
+// rule over their four children (the values the forward sums).
+__device__ void dsm_vjp_adaptive(int kind, int order, int levels, double tol, const DsmTri& T, d3 r0, d3 q,
+                                 const VjpW& w, d3 R0, d3 R1, d3 R2, double area, double grad[6]) {
+    if (levels == 0) {
+        dsm_vjp_rule(kind, order, T, r0, q, w, R0, R1, R2, area, grad);
+        return;
+    }
+    double coarse[3];
+    dsm_rule(kind, order, T, r0, q, R0, R1, R2, area, coarse);
+    uint32_t st_path[DSM_STACK];
+    int8_t st_depth[DSM_STACK], st_level[DSM_STACK];
+    double st_c[DSM_STACK][3];
+    int sp = 1;
+    st_path[0] = 0; st_depth[0] = 0; st_level[0] = (int8_t)levels;
+    st_c[0][0] = coarse[0]; st_c[0][1] = coarse[1]; st_c[0][2] = coarse[2];
+    const int dim = kind == 0 ? 3 : 1;
+    while (sp > 0) {
+        --sp;
+        const uint32_t path = st_path[sp];
+        const int depth = st_depth[sp], level = st_level[sp];
+        const double c0 = st_c[sp][0], c1 = st_c[sp][1], c2 = st_c[sp][2];
+        d3 P0 = R0, P1 = R1, P2 = R2;
+        double a = area;
+        for (int d = 0; d < depth; ++d) {
+            subtriangle(P0, P1, P2, (path >> (2 * d)) & 3);
+            a *= 0.25;
+        }
+        const double sub = 0.25 * a;
+        double integ[4][3];
+        double ref[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < 4; ++c) {
+            d3 Q0 = P0, Q1 = P1, Q2 = P2;
+            subtriangle(Q0, Q1, Q2, c);
+            dsm_rule(kind, order, T, r0, q, Q0, Q1, Q2, sub, integ[c]);
+            for (int k = 0; k < dim; ++k) ref[k] += integ[c][k];
+        }
+        double dn, cn;
+        if (dim == 1) {
+            dn = fabs(c0 - ref[0]);
+            cn = fabs(c0);
+        } else {
+            const double e0 = c0 - ref[0], e1 = c1 - ref[1], e2 = c2 - ref[2];
+            dn = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+            cn = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+        }
+        if (dn <= tol * cn || level == 0) {
+            for (int c = 0; c < 4; ++c) {
+                d3 Q0 = P0, Q1 = P1, Q2 = P2;
+                subtriangle(Q0, Q1, Q2, c);
+                dsm_vjp_rule(kind, order, T, r0, q, w, Q0, Q1, Q2, sub, grad);
+            }
+            continue;
+        }
+        for (int c = 3; c >= 0; --c) {
+            st_path[sp] = path | ((uint32_t)c << (2 * depth));
+            st_depth[sp] = (int8_t)(depth + 1);
+            st_level[sp] = (int8_t)(level - 1);
+            st_c[sp][0] = integ[c][0]; st_c[sp][1] = integ[c][1]; st_c[sp][2] = integ[c][2];
+            ++sp;
+        }
+    }
+}
+
+__global__ void dsm_vjp_kernel(int64_t dip0, int64_t ndc, const double* __restrict__ dip, int64_t nt,
+                               const double* __restrict__ srec, const int32_t* __restrict__ T32,
+                               const int32_t* __restrict__ tmesh, const int64_t* __restrict__ tidx_ref,
+                               const int* __restrict__ barrier, const int* __restrict__ orient,
+                               const int* __restrict__ dom, int maxb, const int* __restrict__ dnb,
+                               const int* __restrict__ bmesh, const int* __restrict__ binside,
+                               const double* __restrict__ dsigma, int order, int levels, double tol,
+                               const double* __restrict__ U, int64_t ldu, double* part) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t il = blockIdx.y;
+    if (t >= nt || il >= ndc) return;
+    const int64_t i = dip0 + il;
+    double* o = part + (il * nt + t) * 6;
+    for (int c = 0; c < 6; ++c) o[c] = 0.0;
+    const int d = dom[i];
+    if (d < 0) return;
+    const double sigma = dsigma[d];
+    if (sigma == 0.0) return;
+    const int m = tmesh[t];
+    double coeffD = 0.0;
+    bool on = false;
+    for (int k = 0; k < dnb[d]; ++k)
+        if (bmesh[d * maxb + k] == m) {
+            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[m];
+            on = true;
+        }
+    if (!on) return;
+    const double* s = srec + t * SREC;
+    const d3 R0 = dev::ld3(s), R1 = dev::ld3(s + 3), R2 = dev::ld3(s + 6);
+    DsmTri T;
+    T.p0 = R0;
+    T.n = dev::ld3(s + 9);
+    T.e10 = R1 - R0;
+    T.e20 = R2 - R0;
+    const double c11 = dev::dot(T.e10, T.e10), c12 = dev::dot(T.e10, T.e20), c22 = dev::dot(T.e20, T.e20);
+    const double inv_det = 1.0 / (c11 * c22 - c12 * c12);
+    T.d11 = c22 * inv_det;
+    T.d12 = -c12 * inv_det;
+    T.d22 = c11 * inv_det;
+    const d3 r0 = dev::ld3(dip + 6 * i), q = dev::ld3(dip + 6 * i + 3);
+    const double* Uj = U + i * ldu;
+    VjpW w;
+    for (int k = 0; k < 3; ++k) w.W[k] = Uj[T32[3 * t + k]] * coeffD;
+    w.w0 = barrier[m] ? 0.0 : Uj[tidx_ref[t]] * (coeffD / sigma);
+    double g[6] = {0, 0, 0, 0, 0, 0};
+    dsm_vjp_adaptive(0, order, levels, tol, T, r0, q, w, R0, R1, R2, s[12], g);
+    if (!barrier[m]) dsm_vjp_adaptive(1, order, levels, tol, T, r0, q, w, R0, R1, R2, s[12], g);
+    for (int c = 0; c < 6; ++c) o[c] = g[c];
+}
+
+// Fixed-order sum over triangles: one CTA per dipole.
+__global__ void dsm_vjp_reduce_kernel(int64_t dip0, int64_t ndc, int64_t nt, const double* __restrict__ part,
+                                      double* out) {
+    __shared__ double red[6][128];
+    const int64_t il = blockIdx.x;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t t = threadIdx.x; t < nt; t += 128)
+        for (int c = 0; c < 6; ++c) acc[c] += part[(il * nt + t) * 6 + c];
+    for (int c = 0; c < 6; ++c) red[c][threadIdx.x] = acc[c];
+    __syncthreads();
+    for (int w = 64; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int c = 0; c < 6; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) out[(dip0 + il) * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+void launch_dsm_vjp(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
+                    const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
+                    const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
+                    double tol, const double* U, int64_t ldu, double* part, double* out, cudaStream_t s) {
+    if (ndc == 0) return;
+    ProfScope prof_("dsm_vjp", s);
+    dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
+    dsm_vjp_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, g.T, tmesh, tidx_ref, barrier, orient, dom, maxb,
+                                        dnb, bmesh, binside, dsigma, order, levels, tol, U, ldu, part);
+    check_launch("DSM vjp");
+    dsm_vjp_reduce_kernel<<<(unsigned)ndc, 128, 0, s>>>(dip0, ndc, g.nt, part, out);
+    check_launch("DSM vjp reduce");
+}
+
 }  // namespace omg
