@@ -222,6 +222,9 @@ class _Gain(torch.autograd.Function):
                     o = _mesh_orientation(domains, orient, dk, m)
                     if o:
                         grad_sigma[dk] += o * t
+        # a zero conductivity (air) fixes the structure of the system (no
+        # potential-jump unknowns outside); it is not a parameter
+        grad_sigma[np.asarray(sig) == 0.0] = 0.0
         sdev, sdt, ddev, ddt = ctx.in_devices
         gs = torch.as_tensor(grad_sigma, dtype=sdt, device=sdev)
         return gs, ddip.to(ddev, ddt), None

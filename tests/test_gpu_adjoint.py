@@ -12,10 +12,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _setup(cuda, layers=3):
+def _setup(cuda, layers=3, inward=True):
     import torch
     from openmeeg_gb300 import api, workloads
-    w = workloads.small(2, n_dipoles=6, layers=layers, perturb=True)
+    w = workloads.small(2, n_dipoles=6, layers=layers, inward=inward, perturb=True)
     geo = api.Geometry.from_head(w.head)
     sig0 = torch.tensor([d[2] for d in w.head.domains], dtype=torch.float64)
     dip0 = torch.as_tensor(w.dipoles, dtype=torch.float64, device=cuda)
@@ -31,9 +31,10 @@ def _loss(w, geo, sig, dip, Gbar, precision="fp64"):
     return (G * Gbar).sum()
 
 
-def test_conductivity_gradient_matches_central_differences(cuda):
+@pytest.mark.parametrize("layers,inward", [(3, True), (4, False)])
+def test_conductivity_gradient_matches_central_differences(cuda, layers, inward):
     import torch
-    w, geo, sig0, dip0, Gbar = _setup(cuda)
+    w, geo, sig0, dip0, Gbar = _setup(cuda, layers, inward)
     sig = sig0.clone().requires_grad_(True)
     L = _loss(w, geo, sig, dip0, Gbar)
     (gs,) = torch.autograd.grad(L, [sig])
