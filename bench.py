@@ -163,15 +163,60 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-# Algorithmic work per launch for the roofline of the dominant kernel.
-def algorithmic_work(name, w, N, k, nd):
-    """(amount per step, unit, bound) for the kernels that can dominate."""
-    L = 3
-    T = w.head.triangles[0].shape[0]
-    if name in ("gemm_f64", "gemm_f32"):
-        # factorization N^3/3 + forward/backward solves 2 N^2 k per refinement step + gain GEMM 2 k N nd
+# Nominal FP32 CUDA-core issue rate of a GB300 (152 SMs x 128 lanes x 2.07 GHz),
+# used only to state how busy an FP32-pipe kernel keeps the cores.
+FP32_ISSUE_NOMINAL = 152 * 128 * 2.07e9
+
+# DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+# on a smaller head, per unit of the kernel's size (the summaries in profiles/ give
+# the command and the raw figures); scaled to the bench workload by that unit.
+NCU_TRAFFIC_PER_UNIT = {
+    # residual B - A X: bytes per N^2 element of the float-pair head matrix
+    "residual_df64": None,
+}
+
+
+def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
+    """Roofline of one kernel over the timed region: achieved = algorithmic work
+    per launch / mean launch duration (CUDA events around each launch on the
+    library's stream).
+
+    Algorithmic work:
+      residual_df64 -- R = B - A X in double-float arithmetic: reads the float-pair
+        head matrix (8 N^2 bytes), X pairs (8 N k), B (8 N k), writes R (8 N k);
+        N^2 k multiply-adds at 12 FP32 operations each (exact product + TwoSum).
+      gemm_tf32x3 -- tcgen05 3xTF32 updates of the factorization and the solves:
+        N^3/3 flops (LDL^T trailing updates) + 2 N^2 k per solve, solves =
+        refinement steps + 1; executed tensor flops are 3x (hi*hi, hi*lo, lo*hi).
+    """
+    if launches == 0:
         return None
-    return None
+    hbm, bf16, bf16_sus, kind = peaks_
+    t_launch = ms / 1e3 / launches
+    per_step = launches / steps
+    info = {"kernel": name, "launches_per_step": per_step, "mean_launch_ms": ms / launches}
+    if name == "residual_df64":
+        nbytes = 8.0 * N * N + 24.0 * N * k
+        achieved = nbytes / t_launch / 1e9
+        tr = NCU_TRAFFIC_PER_UNIT.get(name)
+        fp32_ops = 12.0 * N * N * k
+        info.update({"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": (tr * N * N) if tr else None,
+                     "algorithmic_bytes_per_launch": nbytes,
+                     "fp32_issue_frac_of_nominal": fp32_ops / t_launch / FP32_ISSUE_NOMINAL,
+                     "note": f"HBM fraction of {kind} copy bandwidth; the kernel is FP32-issue bound "
+                             f"(12 FP32 ops per multiply-add), see fp32_issue_frac_of_nominal"})
+    elif name == "gemm_tf32x3":
+        solves = int(stats.get("refinement_steps", 1)) + 1
+        flops = (N ** 3 / 3.0 + solves * 2.0 * N * N * k) / per_step
+        achieved = flops / t_launch / 1e12
+        info.update({"bound": "tensor", "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s",
+                     "frac": achieved / bf16_sus, "traffic": None, "executed_tf32_tflops": 3 * achieved,
+                     "note": f"algorithmic FP32-equivalent flops vs {kind} bf16 sustained peak (TF32 runs at half "
+                             f"the bf16 rate; 3 TF32 products per FP32-accurate product)"})
+    else:
+        info.update({"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None})
+    return info
 
 
 def run_gpu(args):
@@ -269,11 +314,13 @@ def run_gpu(args):
     d2h = 8 * nd * (ne + nm)
 
     # roofline of the dominant kernel over the timed region
-    hbm, bf16, bf16_sus, peak_kind = peaks()
+    pk = peaks()
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
     dname, (dl, dms) = dom
     total_prof_ms = sum(v[1] for v in prof.values())
-    roof = roofline_entry(dname, dl, dms, args.steps, N, geo, w, nd, ne + nm, stx, hbm, bf16, bf16_sus, peak_kind)
+    roof = roofline_entry(dname, dl, dms, args.steps, N, ne + nm, nd, stx, pk)
+    others = {n: roofline_entry(n, v[0], v[1], args.steps, N, ne + nm, nd, stx, pk)
+              for n, v in prof.items() if n in ("residual_df64", "gemm_tf32x3") and n != dname}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -302,6 +349,7 @@ def run_gpu(args):
                                     sorted(prof.items(), key=lambda kv: -kv[1][1])},
             "profiled_ms_per_step": round(total_prof_ms / args.steps, 3),
             "roofline": roof,
+            "roofline_other": others,
             "clocks": ck,
             "cpu_baseline": cpu,
         }
@@ -311,30 +359,106 @@ def run_gpu(args):
     return 0
 
 
-def roofline_entry(name, launches, ms, steps, N, geo, w, nd, k, st, hbm, bf16, bf16_sus, peak_kind):
-    """achieved = algorithmic work per launch / mean launch time of the dominant kernel."""
-    if launches == 0:
-        return None
-    per_launch_s = ms / 1e3 / launches
-    info = {"kernel": name, "launches_per_step": launches / steps, "mean_launch_ms": ms / launches}
-    if name.startswith("gemm"):
-        # Work of all GEMM launches in a step: FP32 factorization N^3/3, solves
-        # 2*N^2*k per refinement step, FP64 residual 2*N^2*k per step, gain 2*k*N*nd.
-        steps_ref = max(1, int(st.get("refinement_steps", 1)))
-        flops = N ** 3 / 3 + 2 * 2 * N * N * k * steps_ref + 2 * N * N * k * steps_ref + 2 * k * N * nd
-        achieved = flops / steps / (ms / 1e3) * steps / 1e12 if False else flops / (ms / 1e3 / steps) / 1e12
-        info.update({"bound": "tensor", "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s",
-                     "frac": achieved / bf16_sus, "traffic": None,
-                     "note": f"CUDA-core GEMM vs {peak_kind} bf16 sustained peak"})
-    else:
-        T = sum(t.shape[0] for t in w.head.triangles)
-        bytes_per = None
-        if name == "s_block" or name == "d_block":
-            # assembly is FP64-pipe bound; traffic is the per-pair record loads + outputs
-            evals = None
-        info.update({"bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
-                     "traffic": None, "note": f"{peak_kind} peaks"})
-    return info
+def run_batch(args):
+    """config3: 32 uneven heads as one captured graph (mixed precision), models/s,
+    next to the sequential per-model FP64 loop on the same GPU."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    __import__("__graft_entry__").build()
+    from openmeeg_gb300 import api, workloads
+    os.environ.setdefault("OMG_TUNE_CACHE", os.path.join(ROOT, "gpurun_out", "tune_cache.txt")
+                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "")
+    if not os.environ["OMG_TUNE_CACHE"]:
+        del os.environ["OMG_TUNE_CACHE"]
+    ws = workloads.config3_models()
+    ctx = api.Context(local)
+    geos = [api.Geometry.from_head(w.head, ctx) for w in ws]
+    sizes = [g.size for g in geos]
+    nd_tot = sum(w.dipoles.shape[0] for w in ws)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    # sequential per-model FP64 loop (the reference shape of the computation)
+    ref = []
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    t0 = time.perf_counter()
+    e0.record(torch.cuda.current_stream())
+    for g, w in zip(geos, ws):
+        ge, _, _ = api.forward_gain(g, w.dipoles, w.electrodes, None, precision="fp64")
+        ref.append(ge)
+    e1.record(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    t_seq64 = time.perf_counter() - t0
+
+    # sequential per-model mixed loop (the same precision as the batch, no graph)
+    t0 = time.perf_counter()
+    for g, w in zip(geos, ws):
+        api.forward_gain(g, w.dipoles, w.electrodes, None, precision="mixed")
+    torch.cuda.synchronize()
+    t_seqmx = time.perf_counter() - t0
+
+    # batched: plan + tune + capture, then replays
+    t0 = time.perf_counter()
+    b = api.BatchForward([(g, w.dipoles, w.electrodes, None) for g, w in zip(geos, ws)], precision="mixed",
+                         n_branches=args.branches)
+    t_create = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        b.run()
+    clocks = Clocks(local)
+    clocks.start()
+    s = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.run()          # blocking: replays on the context stream and checks every model
+    t_wall = (time.perf_counter() - t0) / args.steps
+    ck = clocks.stop()
+    info = b.info()
+    errs = []
+    for i in range(len(ws)):
+        ge, _ = b.gains(i)
+        errs.append(float(torch.linalg.norm(ge - ref[i]) / torch.linalg.norm(ref[i])))
+
+    # end to end through the public API with host buffers: geometries from host
+    # arrays, batch creation (plan, cached branch count, capture), one run, gains to host
+    t0 = time.perf_counter()
+    geos2 = [api.Geometry.from_head(w.head, ctx) for w in ws]
+    b2 = api.BatchForward([(g, w.dipoles, w.electrodes, None) for g, w in zip(geos2, ws)], precision="mixed",
+                          n_branches=info["n_branches"])
+    b2.run()
+    host = [b2.gains(i)[0].cpu() for i in range(len(ws))]
+    t_e2e = time.perf_counter() - t0
+    del b2, geos2, host
+    h2d = sum(sum(a.nbytes for a in w.head.vertices) + sum(a.nbytes for a in w.head.triangles) + w.dipoles.nbytes +
+              w.electrodes.nbytes for w in ws)
+    d2h = sum(8 * w.dipoles.shape[0] * w.electrodes.shape[0] for w in ws)
+    if rank == 0:
+        line = {
+            "metric": "batched forward throughput (models/s), 32 uneven heads, mixed precision, graph replay",
+            "value": len(ws) / t_wall * world, "unit": "models/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_wall * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded nested icosphere heads)",
+            "config": {"workload": "config3: 32 heads, ico3/ico4 surfaces, 3-4 layers, inner radii +-3%, "
+                                   "100-1000 dipoles, 64 EEG", "N_min": min(sizes), "N_max": max(sizes),
+                       "N_sum": sum(sizes), "dipoles": nd_tot, "parallelism": "single GPU, graph branches",
+                       "l2": "inputs > L2 (every head matrix rebuilt each step); no flush"},
+            "sequential_fp64_s": t_seq64, "sequential_fp64_models_per_s": len(ws) / t_seq64,
+            "speedup_vs_sequential_fp64": t_seq64 / t_wall,
+            "sequential_mixed_s": t_seqmx, "speedup_vs_sequential_mixed": t_seqmx / t_wall,
+            "batch_create_s": t_create, "batch_info": info,
+            "rel_err_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
+            "e2e": {"value": len(ws) / t_e2e, "unit": "models/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "path": "Geometry.from_head x32 + BatchForward (plan, cached tune, capture) + run + gains to host"},
+            "gpu_launches": int(info["launches_per_run"]) * args.steps,
+            "clocks": ck,
+        }
+        print(json.dumps(line))
+    return 0
 
 
 def main():
@@ -344,6 +468,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config1")
+    ap.add_argument("--branches", type=int, default=0, help="config3: graph branches (0 = autotune)")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
@@ -353,6 +478,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "config3":
+        return run_batch(args)
     return run_gpu(args)
 
 

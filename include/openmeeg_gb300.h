@@ -226,6 +226,50 @@ int omg_gain_host(omg_context ctx, omg_geometry geo, int32_t precision, const om
                   const double* electrodes, int64_t n_electrodes, const double* squids, int64_t n_squids,
                   double* gain_eeg, double* gain_meg, omg_gain_stats* stats);
 
+/* ---- batched forward (no reference counterpart) -----------------------------
+ * Many head models, each with its own geometry, dipoles and sensors, computed
+ * by one captured CUDA graph: every model's forward is the adjoint gain of
+ * omg_gain_dev (GainEEGadjoint / GainMEGadjoint, OpenMEEG/include/gain.h:78-136)
+ * in the given precision with the default integrators, and the models run as
+ * parallel branches (one stream each).  omg_batch_create makes one uncaptured
+ * planning run (which fixes the mixed assembly's near-pair lists, the number of
+ * refinement steps and the DipSourceMat row ranges), picks the number of
+ * branches (n_branches = 0: timed over 1, 2, 4, 8, 16 within 70% of free
+ * device memory, cached by batch signature in the file named by the
+ * OMG_TUNE_CACHE environment variable) and captures the graph;
+ * omg_batch_run replays it on the context's stream and waits for it.
+ * Geometries stay referenced by the batch and must not be used by other calls
+ * while a batch call runs.  Changing a geometry's conductivities makes the
+ * next run plan and capture again.  New dipoles (omg_batch_set_dipoles, same
+ * count) must lie in domains whose rows the plan covers, else the run fails
+ * with OMG_ERR_INVALID. */
+typedef struct omg_batch_s* omg_batch;
+typedef struct {
+    omg_geometry geometry;
+    const double* dipoles;    int64_t n_dipoles;      /* host, n x 6 row-major */
+    const double* electrodes; int64_t n_electrodes;   /* host, n x 3 row-major */
+    const double* squids;     int64_t n_squids;       /* host, n x 6 row-major */
+} omg_batch_model;
+typedef struct {
+    int32_t n_models;
+    int32_t n_branches;
+    int32_t precision;
+    int32_t max_refine_steps;
+    int64_t launches_per_run;       /* kernel launches recorded in the graph */
+    int64_t graph_nodes;
+    int64_t graph_bytes_estimate;   /* device memory of the branches' largest models */
+    double tuned_ms;                /* replay time of the chosen branch count (0: not timed) */
+} omg_batch_info;
+int omg_batch_create(omg_context ctx, int32_t n_models, const omg_batch_model* models, int32_t precision,
+                     int32_t n_branches, omg_batch* out);
+int omg_batch_run(omg_batch batch);
+/* Device pointers owned by the batch: EEG gain n_electrodes x n_dipoles and
+ * MEG gain n_squids x n_dipoles, column-major; valid until destroy. */
+int omg_batch_gain_dev(omg_batch batch, int32_t model, const double** gain_eeg, const double** gain_meg);
+int omg_batch_set_dipoles(omg_batch batch, int32_t model, const double* dipoles);
+int omg_batch_get_info(omg_batch batch, omg_batch_info* info);
+int omg_batch_destroy(omg_batch batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,6 +70,20 @@ class GainStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchModel(ctypes.Structure):
+    _fields_ = [("geometry", c_vp), ("dipoles", P_dbl), ("n_dipoles", c_i64), ("electrodes", P_dbl),
+                ("n_electrodes", c_i64), ("squids", P_dbl), ("n_squids", c_i64)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("n_models", c_i32), ("n_branches", c_i32), ("precision", c_i32), ("max_refine_steps", c_i32),
+                ("launches_per_run", c_i64), ("graph_nodes", c_i64), ("graph_bytes_estimate", c_i64),
+                ("tuned_ms", c_dbl)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # (name, restype, argtypes)
 _PROTOS = [
     ("omg_last_error", ctypes.c_char_p, []),
@@ -110,6 +124,12 @@ _PROTOS = [
                              c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, ctypes.POINTER(GainStats)]),
     ("omg_gain_host", c_i32, [c_vp, c_vp, c_i32, ctypes.POINTER(Integrator), ctypes.POINTER(Integrator), P_dbl,
                               c_i64, P_dbl, c_i64, P_dbl, c_i64, P_dbl, P_dbl, ctypes.POINTER(GainStats)]),
+    ("omg_batch_create", c_i32, [c_vp, c_i32, ctypes.POINTER(BatchModel), c_i32, c_i32, ctypes.POINTER(c_vp)]),
+    ("omg_batch_run", c_i32, [c_vp]),
+    ("omg_batch_gain_dev", c_i32, [c_vp, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp)]),
+    ("omg_batch_set_dipoles", c_i32, [c_vp, c_i32, P_dbl]),
+    ("omg_batch_get_info", c_i32, [c_vp, ctypes.POINTER(BatchInfo)]),
+    ("omg_batch_destroy", c_i32, [c_vp]),
 ]
 
 EXPORTED = [p[0] for p in _PROTOS]

@@ -25,7 +25,7 @@ from ._lib import GainStats, GeometryInfo, Integrator, OMGError, check
 
 __all__ = ["Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
            "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
-           "GainEEGMEGadjoint", "forward_gain", "OMGError", "kernel_launches"]
+           "GainEEGMEGadjoint", "forward_gain", "BatchForward", "OMGError", "kernel_launches"]
 
 FP64 = "fp64"
 MIXED = "mixed"
@@ -325,6 +325,82 @@ def forward_gain(geom: Geometry, dipoles, electrodes=None, squids=None, precisio
     check(ctx.lib.omg_gain_dev(ctx.handle, geom.handle, _prec(precision), ctypes.byref(hi), ctypes.byref(di),
                                _ptr(dip), nd, _ptr(el), ne, _ptr(sq), nm, _ptr(ge), _ptr(gm), ctypes.byref(st)))
     return (ge.T if ne else None), (gm.T if nm else None), st.as_dict()
+
+
+class _DevView:
+    """__cuda_array_interface__ over library-owned device memory (read-only use)."""
+
+    def __init__(self, ptr: int, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f8", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+class BatchForward:
+    """Forward gains of many head models as one captured CUDA graph (no
+    reference counterpart).  Each model's gains are those of forward_gain
+    (the adjoint form of gain.h:78-136) in the same precision; the models run
+    as parallel branches of the graph, the branch count timed and chosen at
+    construction when n_branches = 0.
+
+    models: sequence of (Geometry, dipoles (n x 6), electrodes (n x 3) or None,
+    squids (n x 6) or None), all on this context's device."""
+
+    def __init__(self, models, precision=MIXED, n_branches: int = 0, ctx: Optional[Context] = None):
+        self.ctx = ctx or models[0][0].ctx
+        self.lib = self.ctx.lib
+        self._keep = []
+        arr = (_lib.BatchModel * len(models))()
+        self.shapes = []
+        for i, (geo, dip, el, sq) in enumerate(models):
+            d = np.ascontiguousarray(np.asarray(dip, np.float64)[:, :6])
+            e = np.ascontiguousarray(np.asarray(el, np.float64)[:, :3]) if el is not None and len(el) else None
+            q = np.ascontiguousarray(np.asarray(sq, np.float64)[:, :6]) if sq is not None and len(sq) else None
+            self._keep += [geo, d, e, q]
+            P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+            arr[i] = _lib.BatchModel(geo.handle, P(d), d.shape[0], P(e), 0 if e is None else e.shape[0], P(q),
+                                     0 if q is None else q.shape[0])
+            self.shapes.append((d.shape[0], 0 if e is None else e.shape[0], 0 if q is None else q.shape[0]))
+        h = ctypes.c_void_p()
+        check(self.lib.omg_batch_create(self.ctx.handle, len(models), arr, _prec(precision), int(n_branches),
+                                        ctypes.byref(h)))
+        self.handle = h
+
+    def __len__(self):
+        return len(self.shapes)
+
+    def run(self):
+        """Replay the graph: every model's gains are recomputed from its inputs."""
+        check(self.lib.omg_batch_run(self.handle))
+
+    def gains(self, i: int):
+        """(EEG gain n_electrodes x n_dipoles or None, MEG gain or None), copies."""
+        nd, ne, nm = self.shapes[i]
+        pe, pm = ctypes.c_void_p(), ctypes.c_void_p()
+        check(self.lib.omg_batch_gain_dev(self.handle, i, ctypes.byref(pe), ctypes.byref(pm)))
+        dev = _dev(self.ctx)
+        ge = torch.as_tensor(_DevView(pe.value, (nd, ne)), device=dev).T.clone() if ne and nd else None
+        gm = torch.as_tensor(_DevView(pm.value, (nd, nm)), device=dev).T.clone() if nm and nd else None
+        return ge, gm
+
+    def set_dipoles(self, i: int, dipoles):
+        d = np.ascontiguousarray(np.asarray(dipoles, np.float64)[:, :6])
+        if d.shape[0] != self.shapes[i][0]:
+            raise ValueError("a model's dipole count is fixed at construction")
+        check(self.lib.omg_batch_set_dipoles(self.handle, i, d.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+
+    def info(self) -> dict:
+        inf = _lib.BatchInfo()
+        check(self.lib.omg_batch_get_info(self.handle, ctypes.byref(inf)))
+        return inf.as_dict()
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            if getattr(self, "handle", None):
+                self.lib.omg_batch_destroy(self.handle)
+        except Exception:
+            pass
 
 
 # ---- reference class names (gain.h:60-136) --------------------------------

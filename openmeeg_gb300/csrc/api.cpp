@@ -12,7 +12,7 @@
 #include <tuple>
 #include <vector>
 
-#include "handles.h"
+#include "pipeline.h"
 
 namespace omg {
 void profile_enable(bool on);
@@ -90,6 +90,8 @@ void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, f
                      float* L, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
                    cudaStream_t s);
+void ratio_max(int64_t n, const double* num, const double* den, double* out, cudaStream_t s);
+void launch_domain_check(int64_t n, const int* dom, uint64_t allowed, int* err, cudaStream_t s);
 }  // namespace omg
 
 using namespace omg;
@@ -97,57 +99,12 @@ using namespace omg;
 static thread_local std::string g_last_error;
 void set_last_error(const char* msg) { g_last_error = msg; }
 
-// ---------------------------------------------------------------------------
-// Handles
-// ---------------------------------------------------------------------------
-struct omg_solver_s {
-    omg_context ctx = nullptr;
-    omg_geometry geo = nullptr;
-    int precision = OMG_PREC_FP64;
-    int64_t N = 0, nP = 0;
-    std::vector<int64_t> bounds;            // block boundaries (include nP)
-    DevBuf A64;                             // FP64: factor (lower).  Mixed: the head matrix as float pairs
-                                            // (hi, lo; 2 x N x N floats) for the refinement residual
-    DevBuf A32;                             // mixed: FP32 factor (TF32 heads after the split), ld = ld32
-    DevBuf A32r;                            // mixed: FP32 remainders of the factor
-    DevBuf W;                               // mixed: K-major head/remainder copies of every panel
-    DevBuf Linv32;                          // mixed: inverses of the 128 x 128 diagonal blocks
-    std::vector<int64_t> w_off;             // offset (floats) of panel b's heads; remainders follow
-    int64_t ld32 = 0;
-    bool persistent = false;                // outlives the call that made it (public solver handle)
-    double refine_tol = 1e-6;               // stop when corrections are this small relative to x
-    int max_refine = 10;
-    int last_steps = 0;
-    double last_residual = 0.0;
-    double last_correction = 0.0;
-};
-
-// ---------------------------------------------------------------------------
-// Error plumbing
-// ---------------------------------------------------------------------------
-template <typename F>
-static int guarded(F&& f) {
-    try {
-        f();
-        return OMG_OK;
-    } catch (const Error& e) {
-        g_last_error = e.what();
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        g_last_error = "host allocation failed";
-        return OMG_ERR_NOMEM;
-    } catch (const std::exception& e) {
-        g_last_error = e.what();
-        return OMG_ERR_INVALID;
-    }
-}
-
-static void set_device(omg_context ctx) { OMG_CUDA(cudaSetDevice(ctx->device)); }
+void set_device(omg_context ctx) { OMG_CUDA(cudaSetDevice(ctx->device)); }
 
 // Handles are reference counted so that destroying them in any order is safe:
 // a context stays alive while a geometry or solver made from it lives, and a
 // geometry while a solver built on it lives.
-static void release_context(omg_context ctx) {
+void release_context(omg_context ctx) {
     if (!ctx || --ctx->refs > 0) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->own);
@@ -158,7 +115,7 @@ static void release_context(omg_context ctx) {
     delete ctx;
 }
 
-static void release_geometry(omg_geometry geo) {
+void release_geometry(omg_geometry geo) {
     if (!geo || --geo->refs > 0) return;
     omg_context ctx = geo->ctx;
     cudaSetDevice(ctx->device);
@@ -167,13 +124,13 @@ static void release_geometry(omg_geometry geo) {
     release_context(ctx);
 }
 
-static void reset_err(omg_context ctx) {
+void reset_err(omg_context ctx) {
     OMG_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int) * 4, ctx->stream));
     OMG_CUDA(cudaMemsetAsync(ctx->d_errcol, 0, sizeof(int64_t), ctx->stream));
 }
 
 // Synchronizes the stream and turns a device-side status into an exception.
-static void check_err(omg_context ctx, const char* what) {
+void check_err(omg_context ctx, const char* what) {
     int h[4] = {0, 0, 0, 0};
     int64_t col = 0;
     OMG_CUDA(cudaMemcpyAsync(h, ctx->d_err, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
@@ -188,10 +145,10 @@ static void check_err(omg_context ctx, const char* what) {
     if (h[0] != 0) throw Error(h[0], std::string(what) + ": device error");
 }
 
-static omg_integrator default_hm_integrator() { return {3, 0, 0.005}; }      // assemble.h:32
-static omg_integrator default_dsm_integrator() { return {3, 10, 0.001}; }    // assembleSourceMat.h:28
+omg_integrator default_hm_integrator() { return {3, 0, 0.005}; }      // assemble.h:32
+omg_integrator default_dsm_integrator() { return {3, 10, 0.001}; }    // assembleSourceMat.h:28
 
-static void check_integrator(const omg_integrator& it, bool allow_adaptive) {
+void check_integrator(const omg_integrator& it, bool allow_adaptive) {
     OMG_REQUIRE(it.order >= 0 && it.order <= 3, "integrator order must be 0..3");
     OMG_REQUIRE(it.levels >= 0, "integrator levels must be >= 0");
     if (!allow_adaptive && it.levels > 0)
@@ -265,7 +222,7 @@ static void upload_geometry(omg_geometry g) {
     g->prepared_order = 3;
 }
 
-static void ensure_order(omg_geometry g, int order) {
+void ensure_order(omg_geometry g, int order) {
     if (g->prepared_order != order) {
         launch_prepare_triangles_order(g->d, order, g->ctx->stream);
         g->prepared_order = order;
@@ -275,7 +232,7 @@ static void ensure_order(omg_geometry g, int order) {
 // ---------------------------------------------------------------------------
 // HeadMat assembly into the internal lower triangle (assembleHeadMat.cpp:73-115)
 // ---------------------------------------------------------------------------
-static void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld) {
+void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     const HostGeometry& h = g->h;
@@ -324,13 +281,12 @@ static void assemble_headmat_internal(omg_geometry g, const omg_integrator& inte
     }
 }
 
-static void ensure_gg_tables(omg_geometry g);
 
 // Mixed precision: far pairs by the FP32 product rule, near pairs (centroid
 // distance < kRhoFar x larger max edge) by the FP64 analytic kernels.
 constexpr float kRhoFar = 2.0f;
 
-static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld) {
+void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld, NearPlan* plan) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     const HostGeometry& h = g->h;
@@ -341,8 +297,16 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
     ensure_gg_tables(g);
     OMG_CUDA(cudaMemsetAsync(hm, 0, sizeof(double) * (size_t)ld * (size_t)d.N, s));
     launch_pad_identity(d, hm, ld, s);
-    DevBuf counter(sizeof(int), s);
-    for (const auto& p : h.pairs) {
+    const bool replay = plan && plan->recorded;
+    const size_t npair = h.pairs.size();
+    if (plan && !replay) {
+        plan->count.assign(npair, 0);
+        plan->list.clear();
+        plan->counter = DevBuf(sizeof(int) * std::max<size_t>(1, npair), s, true);
+    }
+    DevBuf counter(replay ? 0 : sizeof(int), s);
+    for (size_t pi = 0; pi < npair; ++pi) {
+        const auto& p = h.pairs[pi];
         const int m1 = p.m1, m2 = p.m2;
         const bool same = (m1 == m2);
         const int64_t t1b = h.tbeg[m1], t1e = h.tbeg[m1 + 1], t2b = h.tbeg[m2], t2e = h.tbeg[m2 + 1];
@@ -353,24 +317,43 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
         const bool wantD21 = !same && !h.barrier[m2];
         DevBuf stmp(sInHM ? 0 : (size_t)n1 * n2 * 8, s);
         DevBuf d12(wantD12 ? (size_t)n1 * n2 * 24 : 0, s), d21(wantD21 ? (size_t)n1 * n2 * 24 : 0, s);
-        const int64_t npairs = same ? n1 * (n1 + 1) / 2 : n1 * n2;
-        int cap = (int)std::min<int64_t>(npairs, std::max<int64_t>(1 << 22, npairs / 8));
-        int count = 0;
-        for (int attempt = 0; attempt < 2; ++attempt) {
-            DevBuf nearb((size_t)cap * sizeof(int2), s);
-            OMG_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(int), s));
+        if (replay) {   // the near list of this pair is known: no read-back
+            int* cnt = plan->counter.as<int>() + pi;
+            const int cap = std::max(1, plan->count[pi]);
+            OMG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int), s));
             launch_ff_block(d, g->grec, t1b, t1e, t2b, t2e, same, true, wantD12, wantD21, p.cS,
                             sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(), d21.as<double>(),
-                            nearb.as<int2>(), counter.as<int>(), cap, kRhoFar, ctx->d_err, s);
-            OMG_CUDA(cudaMemcpyAsync(&count, counter.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-            OMG_CUDA(cudaStreamSynchronize(s));
-            if (count <= cap) {
-                launch_near_pairs(d, nearb.as<int2>(), count, t1b, t1e, t2b, t2e, same, true, wantD12, wantD21, p.cS,
-                                  3, sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(), d21.as<double>(),
-                                  s);
-                break;
+                            plan->list[pi].as<int2>(), cnt, cap, kRhoFar, ctx->d_err, s);
+            launch_near_pairs(d, plan->list[pi].as<int2>(), plan->count[pi], t1b, t1e, t2b, t2e, same, true, wantD12,
+                              wantD21, p.cS, 3, sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(),
+                              d21.as<double>(), s);
+        } else {
+            const int64_t npairs = same ? n1 * (n1 + 1) / 2 : n1 * n2;
+            int cap = (int)std::min<int64_t>(npairs, std::max<int64_t>(1 << 22, npairs / 8));
+            int count = 0;
+            for (int attempt = 0; attempt < 2; ++attempt) {
+                DevBuf nearb((size_t)cap * sizeof(int2), s);
+                OMG_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(int), s));
+                launch_ff_block(d, g->grec, t1b, t1e, t2b, t2e, same, true, wantD12, wantD21, p.cS,
+                                sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(), d21.as<double>(),
+                                nearb.as<int2>(), counter.as<int>(), cap, kRhoFar, ctx->d_err, s);
+                OMG_CUDA(cudaMemcpyAsync(&count, counter.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+                OMG_CUDA(cudaStreamSynchronize(s));
+                if (count <= cap) {
+                    launch_near_pairs(d, nearb.as<int2>(), count, t1b, t1e, t2b, t2e, same, true, wantD12, wantD21,
+                                      p.cS, 3, sInHM ? hm : nullptr, ld, stmp.as<double>(), d12.as<double>(),
+                                      d21.as<double>(), s);
+                    if (plan) {
+                        plan->count[pi] = count;
+                        plan->list.emplace_back(sizeof(int2) * std::max(1, count), s, true);
+                        if (count > 0)
+                            OMG_CUDA(cudaMemcpyAsync(plan->list.back().p, nearb.p, sizeof(int2) * count,
+                                                     cudaMemcpyDeviceToDevice, s));
+                    }
+                    break;
+                }
+                cap = count;   // rerun with room for every near pair (far writes are idempotent)
             }
-            cap = count;   // rerun with room for every near pair (far writes are idempotent)
         }
         if (sInHM)
             launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / p.cS, hm, ld, nullptr, hm, s);
@@ -390,9 +373,10 @@ static void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, 
         }
         if (nb > 0) launch_deflate(d, ranges, i_first, nb, hm, ld, ctx->d_scalar, s);
     }
+    if (plan) plan->recorded = true;
 }
 
-static void ensure_gg_tables(omg_geometry g) {
+void ensure_gg_tables(omg_geometry g) {
     if (!g->grec) {
         g->bufs.emplace_back((size_t)g->h.nt * 64 * sizeof(float), g->ctx->stream, true);
         g->grec = g->bufs.back().as<float>();
@@ -532,10 +516,10 @@ constexpr int NB64 = 128;   // FP64 diagonal block (128 x 129 x 8 B of shared me
 constexpr int NB32 = 128;   // FP32 diagonal block
 
 // Factor the internal-order HeadMat held in `hm` (FP64, lower), taking ownership.
-static void solver_factor(omg_solver sv, DevBuf&& hm) {
+void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
-    reset_err(sv->ctx);
+    if (check) reset_err(sv->ctx);   // unchecked (captured) factorizations keep earlier flags
     if (sv->precision == OMG_PREC_FP64) {
         sv->A64 = std::move(hm);
         factor_ldlt<double>(sv, sv->A64.as<double>(), N, NB64);
@@ -550,7 +534,7 @@ static void solver_factor(omg_solver sv, DevBuf&& hm) {
         hm.release();
         factor_ldlt_tc(sv, sv->A32.as<float>(), sv->ld32, NB32_TC);
     }
-    check_err(sv->ctx, "factorization");
+    if (check) check_err(sv->ctx, "factorization");
 }
 
 // Mixed precision: x = HM^-1 b by FP32 solves refined against the FP64 HM.
@@ -612,7 +596,39 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
         throw Error(OMG_ERR_NOT_CONVERGED, "iterative refinement stalled at relative correction " + std::to_string(est));
 }
 
-static void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
+// Mixed solve with a fixed number of residual steps and no host read-back
+// (stream-capture safe): the last correction's max relative column size is
+// left in d_est for the caller to test after the stream completes.
+void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int residual_steps, double* d_est) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N;
+    DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s),
+        XS((size_t)2 * N * nrhs * 4, s);
+    DevBuf rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s), dn((size_t)nrhs * 8, s), xn((size_t)nrhs * 8, s);
+    double* x = X.as<double>();
+    double* r = R.as<double>();
+    OMG_CUDA(cudaMemsetAsync(x, 0, (size_t)N * nrhs * 8, s));
+    copy_convert<double, double>(N, nrhs, B, ldb, r, N, false, 1.0, s);
+    col_norms(N, nrhs, r, N, rn.as<double>(), s);
+    for (int it = 0; it <= residual_steps; ++it) {
+        if (it > 0) {
+            float* xh = XS.as<float>();
+            split_f64(N, nrhs, x, N, xh, xh + (size_t)N * nrhs, N, s);
+            const float* ah = sv->A64.as<float>();
+            residual_df64(N, nrhs, N, ah, ah + (size_t)N * N, N, xh, xh + (size_t)N * nrhs, N, B, ldb, r, N, s);
+            col_norms(N, nrhs, r, N, rn.as<double>(), s);
+        }
+        scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, rn.as<double>(), sc.as<double>(), s);
+        solve_ldlt_tc(sv, B32.as<float>(), N, nrhs);
+        axpy_f32(N, nrhs, B32.as<float>(), N, x, N, sc.as<double>(), s);
+    }
+    col_norms_f32(N, nrhs, B32.as<float>(), N, sc.as<double>(), dn.as<double>(), s);
+    col_norms(N, nrhs, x, N, xn.as<double>(), s);
+    ratio_max(nrhs, dn.as<double>(), xn.as<double>(), d_est, s);
+    copy_convert<double, double>(N, nrhs, x, N, B, ldb, false, 1.0, s);
+}
+
+void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     if (nrhs <= 0) return;
     if (sv->precision == OMG_PREC_FP64)
         solve_ldlt<double>(sv, sv->A64.as<double>(), sv->N, B, ldb, nrhs);
@@ -623,9 +639,8 @@ static void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t
 // ---------------------------------------------------------------------------
 // Sources / sensors
 // ---------------------------------------------------------------------------
-static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain,
-                         int perm, double* out, int64_t ldo, int precision = OMG_PREC_FP64,
-                         std::vector<int>* meshes_used = nullptr) {
+void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain, int perm,
+                  double* out, int64_t ldo, int precision, std::vector<int>* meshes_used, uint64_t allowed_domains) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     check_integrator(integ, true);
@@ -640,6 +655,7 @@ static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const om
     launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s);
     launch_domain_lookup(nd, g->h.nmesh, sa.as<double>(), g->ndom, g->maxb, g->dnb, g->bmesh, g->binside, g->orient,
                          domain, dom.as<int>(), ctx->d_err, s);
+    if (allowed_domains) launch_domain_check(nd, dom.as<int>(), allowed_domains, ctx->d_err, s);
     if (meshes_used) {   // which meshes carry nonzero DSM rows: boundaries of the dipoles' domains
         std::vector<int> hdom(nd);
         OMG_CUDA(cudaMemcpyAsync(hdom.data(), dom.p, nd * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -661,6 +677,40 @@ static void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const om
                    g->bmesh, g->binside, g->dsigma, integ.order, integ.levels, integ.tol, perm, out, ldo,
                    p1.as<double>(), precision == OMG_PREC_MIXED ? 1 : 0, s);
     }
+}
+
+std::vector<std::pair<int64_t, int64_t>> gain_row_ranges(omg_geometry geo, const std::vector<int>& src_meshes) {
+    std::vector<std::pair<int64_t, int64_t>> kr;
+    for (int m : src_meshes) {
+        if (!geo->h.barrier[m])
+            kr.push_back({geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv, geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv +
+                                                                       (geo->h.tbeg[m + 1] - geo->h.tbeg[m])});
+        kr.push_back({geo->d.nP + geo->h.vbeg[m], geo->d.nP + geo->h.vbeg[m + 1]});
+    }
+    std::sort(kr.begin(), kr.end());
+    std::vector<std::pair<int64_t, int64_t>> merged;
+    for (const auto& r : kr) {
+        if (!merged.empty() && r.first <= merged.back().second)
+            merged.back().second = std::max(merged.back().second, r.second);
+        else
+            merged.push_back(r);
+    }
+    return merged;
+}
+
+void gain_contract(const std::vector<std::pair<int64_t, int64_t>>& merged, const double* Y, int64_t N, int64_t ne,
+                   int64_t nm, const double* DSM, int64_t nd, double* geeg, double* gmeg, cudaStream_t s) {
+    if (ne > 0 && nd > 0) {
+        if (merged.empty()) OMG_CUDA(cudaMemsetAsync(geeg, 0, (size_t)ne * nd * 8, s));
+        for (size_t q = 0; q < merged.size(); ++q) {
+            const int64_t r0 = merged[q].first, kk = merged[q].second - merged[q].first;
+            gemm<double>(ne, nd, kk, 1.0, Y + r0, N, true, DSM + r0, N, false, q == 0 ? 0.0 : 1.0, geeg, ne, s);
+        }
+    }
+    if (nm > 0 && nd > 0)
+        for (const auto& r : merged)
+            gemm<double>(nm, nd, r.second - r.first, 1.0, Y + ne * N + r.first, N, true, DSM + r.first, N, false, 1.0,
+                         gmeg, nm, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -809,6 +859,7 @@ int omg_geometry_set_conductivities(omg_geometry geo, const double* dom_sigma) {
         }
         for (size_t d = 0; d < h.domains.size(); ++d) h.domains[d].sigma = dom_sigma[d];
         h.recompute_coefficients();
+        geo->version++;
         std::vector<double> jump(h.nmesh);
         for (int m = 0; m < h.nmesh; ++m) jump[m] = h.conductivity_jump(m);
         cudaStream_t s = geo->ctx->stream;
@@ -1134,33 +1185,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaEventRecord(ev[3], s));
     solver_solve_internal(sv.get(), B.as<double>(), N, k);
     // G = Y^T DSM over the rows where DSM can be nonzero (the source meshes' triangles and vertices)
-    std::vector<std::pair<int64_t, int64_t>> kr;
-    for (int m : src_meshes) {
-        if (!geo->h.barrier[m])
-            kr.push_back({geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv, geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv +
-                                                                       (geo->h.tbeg[m + 1] - geo->h.tbeg[m])});
-        kr.push_back({geo->d.nP + geo->h.vbeg[m], geo->d.nP + geo->h.vbeg[m + 1]});
-    }
-    std::sort(kr.begin(), kr.end());
-    std::vector<std::pair<int64_t, int64_t>> merged;
-    for (const auto& r : kr) {
-        if (!merged.empty() && r.first <= merged.back().second)
-            merged.back().second = std::max(merged.back().second, r.second);
-        else
-            merged.push_back(r);
-    }
-    if (ne > 0 && nd > 0) {
-        if (merged.empty()) OMG_CUDA(cudaMemsetAsync(geeg, 0, (size_t)ne * nd * 8, s));
-        for (size_t q = 0; q < merged.size(); ++q) {
-            const int64_t r0 = merged[q].first, kk = merged[q].second - merged[q].first;
-            gemm<double>(ne, nd, kk, 1.0, B.as<double>() + r0, N, true, DSM.as<double>() + r0, N, false,
-                         q == 0 ? 0.0 : 1.0, geeg, ne, s);
-        }
-    }
-    if (nm > 0 && nd > 0)
-        for (const auto& r : merged)
-            gemm<double>(nm, nd, r.second - r.first, 1.0, B.as<double>() + ne * N + r.first, N, true,
-                         DSM.as<double>() + r.first, N, false, 1.0, gmeg, nm, s);
+    gain_contract(gain_row_ranges(geo, src_meshes), B.as<double>(), N, ne, nm, DSM.as<double>(), nd, geeg, gmeg, s);
     OMG_CUDA(cudaEventRecord(ev[4], s));
     check_err(ctx, "gain");
     if (st) {

@@ -1,0 +1,561 @@
+// Batched forward: many head models (each with its own meshes, conductivities,
+// dipoles and sensors) computed by one captured CUDA graph.
+//
+// Each model's forward is the adjoint gain of gain.h:78-136 (HeadMat,
+// Head2EEG/Head2MEG, DipSourceMat, factorization, solves, contraction), the
+// same stages as omg_gain_dev.  The models are spread over B branches (one
+// stream each, longest-first onto the least-loaded branch), so the small,
+// latency-bound launches of one model overlap the work of the others.
+//
+// Stream capture forbids host read-back, so a first, uncaptured planning run
+// records what the single-model path decides on the host: the mixed
+// assembly's near-pair lists (geometry only), the number of refinement steps
+// (geometry, conductivities and sensors only) and the DipSourceMat row ranges
+// of the contraction.  The graph then replays with these fixed; on device it
+// records the final refinement correction of every model and flags any dipole
+// that moved to a domain outside the planned ranges, and the host checks both
+// after each run.  A conductivity change invalidates the plan: the next run
+// plans and captures again.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "pipeline.h"
+
+namespace omg {
+void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
+                 double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
+void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s);
+void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
+                  cudaStream_t s);
+void profile_enable(bool on);
+bool profiling_enabled();
+}  // namespace omg
+
+using namespace omg;
+
+namespace {
+
+struct BatchModel {
+    omg_geometry geo = nullptr;
+    int64_t nd = 0, ne = 0, nm = 0;
+    DevBuf dip, el, sq;          // inputs (persistent, row-major)
+    DevBuf geeg, gmeg;           // outputs (column-major ne x nd, nm x nd)
+    DevBuf est;                  // mixed: final relative correction of the refinement
+    NearPlan near;
+    int refine_steps = 0;
+    std::vector<std::pair<int64_t, int64_t>> rows;   // contraction row ranges
+    uint64_t allowed = 0;        // domains whose dipoles the planned rows cover
+    uint64_t version = 0;        // geometry version the plan was made for
+    double cost = 0.0;           // relative work, for the branch assignment
+    size_t peak_bytes = 0;       // device memory while the model runs
+    int branch = 0;
+};
+
+// A branch: its own stream and error flags, sharing the caller's device.
+struct Branch {
+    omg_context_s c;
+    explicit Branch(int device) {
+        c.device = device;
+        OMG_CUDA(cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking));
+        c.stream = c.own;
+        OMG_CUDA(cudaMalloc(&c.d_err, sizeof(int) * 4));
+        OMG_CUDA(cudaMalloc(&c.d_errcol, sizeof(int64_t)));
+        OMG_CUDA(cudaMalloc(&c.d_scalar, sizeof(double) * 4));
+        OMG_CUDA(cudaMemset(c.d_err, 0, sizeof(int) * 4));
+        OMG_CUDA(cudaMemset(c.d_errcol, 0, sizeof(int64_t)));
+    }
+    ~Branch() {
+        cudaStreamSynchronize(c.own);
+        cudaFree(c.d_err);
+        cudaFree(c.d_errcol);
+        cudaFree(c.d_scalar);
+        cudaStreamDestroy(c.own);
+    }
+};
+
+// Points a geometry at a branch context while that branch's work is enqueued.
+struct BindGeometry {
+    omg_geometry g;
+    omg_context saved;
+    BindGeometry(omg_geometry geo, omg_context c) : g(geo), saved(geo->ctx) { g->ctx = c; }
+    ~BindGeometry() { g->ctx = saved; }
+};
+
+struct ProfileOff {
+    bool was;
+    ProfileOff() : was(profiling_enabled()) { profile_enable(false); }
+    ~ProfileOff() { profile_enable(was); }
+};
+
+}  // namespace
+
+struct omg_batch_s {
+    omg_context ctx = nullptr;
+    int precision = OMG_PREC_MIXED;
+    omg_integrator hm_it{}, dsm_it{};
+    std::vector<std::unique_ptr<BatchModel>> models;
+    std::vector<std::unique_ptr<Branch>> branches;
+    int n_branches = 1;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches_per_run = 0;
+    int64_t graph_nodes = 0;
+    double tuned_ms = 0.0;
+    bool tuned = false;
+    double refine_tol = 1e-6;
+};
+
+namespace {
+
+void drop_graph(omg_batch b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// One model's forward on the stream of `c`.  planning: uncaptured, records
+// the plan; otherwise stream-capture safe (no host read-back, no persistent
+// allocation).
+void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
+    omg_geometry g = m.geo;
+    BindGeometry bind(g, c);
+    cudaStream_t s = c->stream;
+    const int64_t N = g->d.N, ne = m.ne, nm = m.nm, nd = m.nd, k = ne + nm;
+    const bool mixed = b->precision == OMG_PREC_MIXED;
+    auto sv = std::make_unique<omg_solver_s>();
+    sv->ctx = c;
+    sv->geo = g;
+    sv->precision = b->precision;
+    sv->N = N;
+    sv->nP = g->d.nP;
+    sv->refine_tol = b->refine_tol;
+    DevBuf hm((size_t)N * N * 8, s);
+    if (mixed)
+        assemble_headmat_mixed(g, b->hm_it, hm.as<double>(), N, &m.near);
+    else
+        assemble_headmat_internal(g, b->hm_it, hm.as<double>(), N);
+    DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
+    OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
+    if (ne > 0) launch_h2em(g->d, m.el.as<double>(), ne, g->n_eeg_cand, g->eeg_cand, 1, B.as<double>(), 1, N, 0,
+                            nullptr, nullptr, s);
+    DevBuf F((size_t)std::max<int64_t>(nm, 1) * g->h.nt * 8, s);
+    if (nm > 0)
+        launch_h2mm(g->d, m.sq.as<double>(), nm, g->tmesh, g->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
+    std::vector<int> src_meshes;
+    dsm_internal(g, m.dip.as<double>(), nd, b->dsm_it, -1, 1, DSM.as<double>(), N, b->precision,
+                 planning ? &src_meshes : nullptr, planning ? 0 : m.allowed);
+    if (nm > 0) launch_ds2mm(m.dip.as<double>(), nd, m.sq.as<double>(), nm, m.gmeg.as<double>(), nm, s);
+    if (planning) {
+        m.rows = gain_row_ranges(g, src_meshes);
+        // every domain bounded only by source meshes is covered by the planned rows
+        m.allowed = 0;
+        std::vector<char> used(g->h.nmesh, 0);
+        for (int q : src_meshes) used[q] = 1;
+        for (size_t d = 0; d < g->h.domains.size() && d < 64; ++d) {
+            bool ok = g->h.domains[d].sigma != 0.0;
+            for (const auto& bd : g->h.domains[d].bounds) ok = ok && used[bd.mesh];
+            if (ok) m.allowed |= (1ull << d);
+        }
+        if (nd == 0) m.allowed = ~0ull;   // no dipoles: nothing to cover
+    }
+    solver_factor(sv.get(), std::move(hm), planning);
+    if (!mixed) {
+        solver_solve_internal(sv.get(), B.as<double>(), N, k);
+    } else if (planning) {
+        solver_solve_internal(sv.get(), B.as<double>(), N, k);
+        m.refine_steps = sv->last_steps;
+    } else {
+        solve_mixed_fixed(sv.get(), B.as<double>(), N, k, m.refine_steps, m.est.as<double>());
+    }
+    gain_contract(m.rows, B.as<double>(), N, ne, nm, DSM.as<double>(), nd, m.geeg.as<double>(), m.gmeg.as<double>(),
+                  s);
+    if (planning) {
+        check_err(c, "batched forward (planning run)");
+        m.version = g->version;
+    }
+}
+
+// Longest-first onto the least-loaded branch.
+void assign_branches(omg_batch b, int nb) {
+    std::vector<size_t> order(b->models.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t x, size_t y) { return b->models[x]->cost > b->models[y]->cost; });
+    std::vector<double> load(nb, 0.0);
+    for (size_t i : order) {
+        const int br = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        b->models[i]->branch = br;
+        load[br] += b->models[i]->cost;
+    }
+}
+
+// Device memory the graph needs with nb branches: each branch runs its models
+// one after another, so its footprint is its largest model.
+size_t graph_bytes(omg_batch b, int nb) {
+    std::vector<size_t> peak(nb, 0);
+    for (auto& m : b->models) peak[m->branch] = std::max(peak[m->branch], m->peak_bytes);
+    return std::accumulate(peak.begin(), peak.end(), (size_t)0);
+}
+
+void ensure_branches(omg_batch b, int nb) {
+    while ((int)b->branches.size() < nb) {
+        b->branches.push_back(std::make_unique<Branch>(b->ctx->device));
+        cudaEvent_t e;
+        OMG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->join.push_back(e);
+    }
+}
+
+void plan(omg_batch b) {
+    drop_graph(b);
+    ensure_branches(b, 1);
+    omg_context c = &b->branches[0]->c;
+    for (auto& m : b->models) {
+        reset_err(c);
+        enqueue_model(b, *m, c, true);
+    }
+    OMG_CUDA(cudaStreamSynchronize(c->stream));
+}
+
+void capture(omg_batch b, int nb) {
+    drop_graph(b);
+    ensure_branches(b, nb);
+    assign_branches(b, nb);
+    ProfileOff off;
+    const int64_t launches0 = kernel_launch_count();
+    OMG_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
+    try {
+        OMG_CUDA(cudaEventRecord(b->fork, b->origin));
+        for (int i = 0; i < nb; ++i) OMG_CUDA(cudaStreamWaitEvent(b->branches[i]->c.stream, b->fork, 0));
+        for (auto& m : b->models) enqueue_model(b, *m, &b->branches[m->branch]->c, false);
+        for (int i = 0; i < nb; ++i) {
+            OMG_CUDA(cudaEventRecord(b->join[i], b->branches[i]->c.stream));
+            OMG_CUDA(cudaStreamWaitEvent(b->origin, b->join[i], 0));
+        }
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(b->origin, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        throw;
+    }
+    OMG_CUDA(cudaStreamEndCapture(b->origin, &b->graph));
+    OMG_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    size_t n = 0;
+    OMG_CUDA(cudaGraphGetNodes(b->graph, nullptr, &n));
+    b->graph_nodes = (int64_t)n;
+    b->launches_per_run = kernel_launch_count() - launches0;
+    b->n_branches = nb;
+}
+
+void launch(omg_batch b) {
+    cudaStream_t s = b->ctx->stream;
+    for (int i = 0; i < b->n_branches; ++i) {
+        OMG_CUDA(cudaMemsetAsync(b->branches[i]->c.d_err, 0, sizeof(int) * 4, s));
+        OMG_CUDA(cudaMemsetAsync(b->branches[i]->c.d_errcol, 0, sizeof(int64_t), s));
+    }
+    OMG_CUDA(cudaGraphLaunch(b->exec, s));
+}
+
+void check_run(omg_batch b) {
+    cudaStream_t s = b->ctx->stream;
+    OMG_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < b->n_branches; ++i) {
+        int h[4] = {0, 0, 0, 0};
+        int64_t col = 0;
+        OMG_CUDA(cudaMemcpy(h, b->branches[i]->c.d_err, sizeof(h), cudaMemcpyDeviceToHost));
+        OMG_CUDA(cudaMemcpy(&col, b->branches[i]->c.d_errcol, sizeof(col), cudaMemcpyDeviceToHost));
+        if (h[0] == 0) continue;
+        std::string which;
+        for (size_t q = 0; q < b->models.size(); ++q)
+            if (b->models[q]->branch == i) which += (which.empty() ? "" : ",") + std::to_string(q);
+        if (h[0] == OMG_ERR_INVALID && h[1] == 1)
+            throw Error(OMG_ERR_INVALID, "batched forward: dipole " + std::to_string(h[2]) + " of a model in {" +
+                                             which + "} lies in a domain the batch was not planned for");
+        if (h[0] == OMG_ERR_NOT_DEFINITE)
+            throw Error(OMG_ERR_NOT_DEFINITE, "batched forward: pivot of the wrong sign at internal column " +
+                                                  std::to_string(col) + " in a model of {" + which + "}");
+        if (h[0] == OMG_ERR_INVALID)
+            throw Error(OMG_ERR_INVALID, "batched forward: a dipole lies in no domain (a model of {" + which + "})");
+        if (h[0] == OMG_ERR_TIMEOUT)
+            throw Error(OMG_ERR_TIMEOUT, "batched forward: a bounded device wait gave up (models {" + which + "})");
+        throw Error(h[0], "batched forward: device error in a model of {" + which + "}");
+    }
+    if (b->precision == OMG_PREC_MIXED)
+        for (size_t q = 0; q < b->models.size(); ++q) {
+            double e = 0.0;
+            OMG_CUDA(cudaMemcpy(&e, b->models[q]->est.p, sizeof(double), cudaMemcpyDeviceToHost));
+            if (!(e <= b->refine_tol))
+                throw Error(OMG_ERR_NOT_CONVERGED, "batched forward: model " + std::to_string(q) +
+                                                       " ended its refinement at relative correction " +
+                                                       std::to_string(e));
+        }
+}
+
+float time_run(omg_batch b) {
+    cudaEvent_t e0, e1;
+    OMG_CUDA(cudaEventCreate(&e0));
+    OMG_CUDA(cudaEventCreate(&e1));
+    OMG_CUDA(cudaEventRecord(e0, b->ctx->stream));
+    launch(b);
+    OMG_CUDA(cudaEventRecord(e1, b->ctx->stream));
+    check_run(b);
+    float ms = 0.f;
+    OMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms;
+}
+
+// Branch-count tuning: time one replay per candidate that fits in memory and
+// keep the fastest.  Results are cached per batch signature (model sizes and
+// device) in the file named by OMG_TUNE_CACHE, when set.
+std::string signature(omg_batch b) {
+    std::ostringstream o;
+    int dev = b->ctx->device;
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) o << p.name << "/" << p.multiProcessorCount;
+    o << "/p" << b->precision;
+    for (auto& m : b->models) o << "/" << m->geo->d.N << "x" << m->nd << "x" << (m->ne + m->nm);
+    return o.str();
+}
+
+int cached_branches(const std::string& sig) {
+    const char* path = std::getenv("OMG_TUNE_CACHE");
+    if (!path) return 0;
+    std::ifstream f(path);
+    std::string line;
+    int best = 0;
+    while (std::getline(f, line)) {
+        const size_t sp = line.rfind(' ');
+        if (sp != std::string::npos && line.compare(0, sp, "batch_branches " + sig) == 0)
+            best = std::atoi(line.c_str() + sp + 1);
+    }
+    return best;
+}
+
+void store_branches(const std::string& sig, int nb) {
+    const char* path = std::getenv("OMG_TUNE_CACHE");
+    if (!path) return;
+    std::ofstream f(path, std::ios::app);
+    f << "batch_branches " << sig << " " << nb << "\n";
+}
+
+void tune(omg_batch b, int requested) {
+    size_t free_b = 0, total_b = 0;
+    OMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = (size_t)(0.7 * (double)free_b);
+    const int nmod = (int)b->models.size();
+    if (requested > 0) {
+        capture(b, std::min(requested, std::max(1, nmod)));
+        return;
+    }
+    const std::string sig = signature(b);
+    const int cached = cached_branches(sig);
+    if (cached > 0) {
+        capture(b, std::min(cached, std::max(1, nmod)));
+        return;
+    }
+    int best = 1;
+    float best_ms = 0.f;
+    for (int nb : {1, 2, 4, 8, 16}) {
+        if (nb > nmod && nb > 1) break;
+        assign_branches(b, nb);
+        if (nb > 1 && graph_bytes(b, nb) > budget) break;
+        capture(b, nb);
+        time_run(b);                 // first replay maps the graph's memory
+        const float ms = time_run(b);
+        if (best_ms == 0.f || ms < best_ms) {
+            best_ms = ms;
+            best = nb;
+        }
+    }
+    b->tuned_ms = best_ms;
+    b->tuned = true;
+    store_branches(sig, best);
+    if (best != b->n_branches) capture(b, best);
+}
+
+size_t model_peak_bytes(const BatchModel& m, int precision) {
+    const double N = (double)m.geo->d.N, k = (double)(m.ne + m.nm), nd = (double)m.nd;
+    const double nt = (double)m.geo->h.nt;
+    double mat = precision == OMG_PREC_MIXED ? 20.0 * N * N : 8.0 * N * N;
+    double scratch = 0.0;   // largest per-pair assembly temporary (S scratch + two D scratch)
+    for (const auto& p : m.geo->h.pairs) {
+        const double n1 = (double)(m.geo->h.tbeg[p.m1 + 1] - m.geo->h.tbeg[p.m1]);
+        const double n2 = (double)(m.geo->h.tbeg[p.m2 + 1] - m.geo->h.tbeg[p.m2]);
+        scratch = std::max(scratch, 56.0 * n1 * n2);
+    }
+    const double dsm = 8.0 * N * nd + std::min(512.0 * (1 << 20), 24.0 * nt * nd);
+    return (size_t)(mat + scratch + dsm + 8.0 * N * k * 8.0);
+}
+
+double model_cost(const BatchModel& m) {
+    const double N = (double)m.geo->d.N;
+    double pairs = 0.0;
+    for (const auto& p : m.geo->h.pairs)
+        pairs += (double)(m.geo->h.tbeg[p.m1 + 1] - m.geo->h.tbeg[p.m1]) *
+                 (double)(m.geo->h.tbeg[p.m2 + 1] - m.geo->h.tbeg[p.m2]);
+    return N * N * N / 3.0 + 2000.0 * pairs + 1e5 * (double)m.nd * (double)m.geo->h.nt / 1e3;
+}
+
+}  // namespace
+
+extern "C" {
+
+int omg_batch_create(omg_context ctx, int32_t n_models, const omg_batch_model* models, int32_t precision,
+                     int32_t n_branches, omg_batch* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && out && (n_models == 0 || models), "null argument");
+        OMG_REQUIRE(n_models > 0, "a batch needs at least one model");
+        OMG_REQUIRE(precision == OMG_PREC_FP64 || precision == OMG_PREC_MIXED, "unknown precision");
+        OMG_REQUIRE(n_branches >= 0 && n_branches <= 64, "n_branches must be 0 (tune) .. 64");
+        set_device(ctx);
+        auto b = std::make_unique<omg_batch_s>();
+        b->ctx = ctx;
+        b->precision = precision;
+        b->hm_it = default_hm_integrator();
+        b->dsm_it = default_dsm_integrator();
+        OMG_CUDA(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+        OMG_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        cudaStream_t s = ctx->stream;
+        for (int32_t i = 0; i < n_models; ++i) {
+            const omg_batch_model& in = models[i];
+            OMG_REQUIRE(in.geometry, "null geometry in batch");
+            OMG_REQUIRE(in.geometry->ctx->device == ctx->device, "batch geometries must live on the context's device");
+            OMG_REQUIRE(in.n_dipoles >= 0 && in.n_electrodes >= 0 && in.n_squids >= 0, "negative count");
+            OMG_REQUIRE(in.n_dipoles == 0 || in.dipoles, "null dipoles");
+            OMG_REQUIRE(in.n_electrodes == 0 || in.electrodes, "null electrodes");
+            OMG_REQUIRE(in.n_squids == 0 || in.squids, "null squids");
+            OMG_REQUIRE(in.n_electrodes == 0 || in.geometry->n_eeg_cand > 0,
+                        "no interface touches a zero-conductivity domain");
+            auto m = std::make_unique<BatchModel>();
+            m->geo = in.geometry;
+            m->nd = in.n_dipoles;
+            m->ne = in.n_electrodes;
+            m->nm = in.n_squids;
+            m->dip = DevBuf((size_t)std::max<int64_t>(1, m->nd) * 48, s, true);
+            m->el = DevBuf((size_t)std::max<int64_t>(1, m->ne) * 24, s, true);
+            m->sq = DevBuf((size_t)std::max<int64_t>(1, m->nm) * 48, s, true);
+            m->geeg = DevBuf((size_t)std::max<int64_t>(1, m->ne * m->nd) * 8, s, true);
+            m->gmeg = DevBuf((size_t)std::max<int64_t>(1, m->nm * m->nd) * 8, s, true);
+            m->est = DevBuf(sizeof(double), s, true);
+            if (m->nd) OMG_CUDA(cudaMemcpyAsync(m->dip.p, in.dipoles, m->nd * 48, cudaMemcpyHostToDevice, s));
+            if (m->ne) OMG_CUDA(cudaMemcpyAsync(m->el.p, in.electrodes, m->ne * 24, cudaMemcpyHostToDevice, s));
+            if (m->nm) OMG_CUDA(cudaMemcpyAsync(m->sq.p, in.squids, m->nm * 48, cudaMemcpyHostToDevice, s));
+            m->cost = model_cost(*m);
+            m->peak_bytes = model_peak_bytes(*m, precision);
+            if (precision == OMG_PREC_MIXED) ensure_gg_tables(m->geo);
+            m->geo->refs++;
+            b->models.push_back(std::move(m));
+        }
+        OMG_CUDA(cudaStreamSynchronize(s));
+        ctx->refs++;
+        omg_batch raw = b.release();
+        try {
+            plan(raw);
+            tune(raw, n_branches);
+        } catch (...) {
+            omg_batch_destroy(raw);
+            throw;
+        }
+        *out = raw;
+    });
+}
+
+int omg_batch_run(omg_batch b) {
+    return guarded([&] {
+        OMG_REQUIRE(b, "null batch");
+        set_device(b->ctx);
+        bool stale = false;
+        for (auto& m : b->models) stale = stale || m->version != m->geo->version;
+        if (stale) {   // new conductivities: new coefficients and refinement plan
+            plan(b);
+            capture(b, b->n_branches);
+        }
+        launch(b);
+        check_run(b);
+    });
+}
+
+int omg_batch_gain_dev(omg_batch b, int32_t model, const double** gain_eeg, const double** gain_meg) {
+    return guarded([&] {
+        OMG_REQUIRE(b, "null batch");
+        OMG_REQUIRE(model >= 0 && model < (int32_t)b->models.size(), "model index out of range");
+        if (gain_eeg) *gain_eeg = b->models[model]->geeg.as<double>();
+        if (gain_meg) *gain_meg = b->models[model]->gmeg.as<double>();
+    });
+}
+
+int omg_batch_set_dipoles(omg_batch b, int32_t model, const double* dipoles) {
+    return guarded([&] {
+        OMG_REQUIRE(b && dipoles, "null argument");
+        OMG_REQUIRE(model >= 0 && model < (int32_t)b->models.size(), "model index out of range");
+        set_device(b->ctx);
+        BatchModel& m = *b->models[model];
+        if (m.nd)
+            OMG_CUDA(cudaMemcpyAsync(m.dip.p, dipoles, m.nd * 48, cudaMemcpyHostToDevice, b->ctx->stream));
+        OMG_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    });
+}
+
+int omg_batch_get_info(omg_batch b, omg_batch_info* info) {
+    return guarded([&] {
+        OMG_REQUIRE(b && info, "null argument");
+        info->n_models = (int32_t)b->models.size();
+        info->n_branches = b->n_branches;
+        info->precision = b->precision;
+        info->launches_per_run = b->launches_per_run;
+        info->graph_nodes = b->graph_nodes;
+        info->tuned_ms = b->tuned_ms;
+        size_t bytes = 0;
+        for (int i = 0; i < b->n_branches; ++i) {
+            size_t pk = 0;
+            for (auto& m : b->models)
+                if (m->branch == i) pk = std::max(pk, m->peak_bytes);
+            bytes += pk;
+        }
+        info->graph_bytes_estimate = (int64_t)bytes;
+        int steps = 0;
+        for (auto& m : b->models) steps = std::max(steps, m->refine_steps);
+        info->max_refine_steps = steps;
+    });
+}
+
+int omg_batch_destroy(omg_batch b) {
+    return guarded([&] {
+        if (!b) return;
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->ctx->stream);
+        drop_graph(b);
+        omg_context ctx = b->ctx;
+        std::vector<omg_geometry> geos;
+        for (auto& m : b->models) geos.push_back(m->geo);
+        b->models.clear();            // before the branches: plan buffers sync on branch streams
+        b->branches.clear();
+        for (auto e : b->join) cudaEventDestroy(e);
+        if (b->fork) cudaEventDestroy(b->fork);
+        if (b->origin) cudaStreamDestroy(b->origin);
+        for (auto g : geos) release_geometry(g);
+        delete b;
+        release_context(ctx);
+    });
+}
+
+}  // extern "C"

@@ -1251,6 +1251,26 @@ void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int 
     check_launch("domain lookup");
 }
 
+// Dipoles whose domain lies outside a planned set (bit d of `allowed`): the
+// row ranges of a planned gain contraction would miss their DipSourceMat rows.
+// Flags OMG_ERR_INVALID with err[1] = 1 and the first such dipole in err[2].
+__global__ void domain_check_kernel(int64_t n, const int* __restrict__ dom, uint64_t allowed, int* err) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int d = dom[i];
+    if (d < 0 || (d < 64 && ((allowed >> d) & 1ull))) return;   // d < 0 is flagged by the lookup itself
+    if (atomicCAS(err, 0, OMG_ERR_INVALID) == 0) {
+        err[1] = 1;
+        err[2] = (int)i;
+    }
+}
+
+void launch_domain_check(int64_t n, const int* dom, uint64_t allowed, int* err, cudaStream_t s) {
+    if (n == 0) return;
+    domain_check_kernel<<<nblocks(n, 128), 128, 0, s>>>(n, dom, allowed, err);
+    check_launch("domain check");
+}
+
 void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
                 const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
                 const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,

@@ -607,6 +607,33 @@ void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const doub
     check("col_norms_f32");
 }
 
+// out[0] = max_j num[j] / den[j] over columns with den[j] > 0 (a NaN ratio
+// gives +inf, so a broken column can never pass a tolerance test).
+__global__ void ratio_max_kernel(int64_t n, const double* __restrict__ num, const double* __restrict__ den,
+                                 double* out) {
+    __shared__ double red[256];
+    double m = 0.0;
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        if (den[j] > 0.0) {
+            const double r = num[j] / den[j];
+            m = (r != r) ? INFINITY : fmax(m, r);
+        } else if (den[j] != den[j]) {
+            m = INFINITY;
+        }
+    }
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+void ratio_max(int64_t n, const double* num, const double* den, double* out, cudaStream_t s) {
+    ratio_max_kernel<<<1, 256, 0, s>>>(n, num, den, out);
+    check("ratio_max");
+}
+
 void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, cudaStream_t s) {
     if (n <= 0) return;
     ProfScope prof_("col_amax", s);

@@ -98,6 +98,7 @@ struct omg_geometry_s {
     double* dsigma = nullptr;
     int prepared_order = -1;
     float* grec = nullptr;      // FP32 far-field records (mixed precision), built on first use
+    uint64_t version = 0;       // bumped when the conductivities change (captured graphs go stale)
 };
 
 

@@ -67,7 +67,10 @@ def config3_models(n_models: int = 32):
         L = int(rng.integers(3, 5))
         subdivs = [int(rng.integers(3, 5)) for _ in range(L)]
         base = [0.87, 0.92, 1.0] if L == 3 else [0.85, 0.88, 0.92, 1.0]
-        radii = [r * (1.0 + rng.uniform(-0.03, 0.03)) for r in base[:-1]] + [1.0]
+        while True:   # jitter the inner radii by +-3%, keeping the surfaces nested 0.02 apart
+            radii = [r * (1.0 + rng.uniform(-0.03, 0.03)) for r in base[:-1]] + [1.0]
+            if all(radii[i + 1] - radii[i] >= 0.02 for i in range(L - 1)):
+                break
         sig = []
         for i in range(L):
             skull = (i == L - 2)
@@ -78,6 +81,22 @@ def config3_models(n_models: int = 32):
         models.append(Workload(f"config3_{k}", head, syn.random_dipoles(nd, SEED + 100 + k, rmax=0.8 * radii[0] / 0.87),
                                syn.fibonacci_points(64, 1.0), np.zeros((0, 6))))
     return models
+
+
+def batch_small() -> list:
+    """Four seconds-scale heads of uneven size for batched-forward tests:
+    3 and 4 layers, ico1/ico2, one with SH-perturbed surfaces, one with MEG."""
+    out = []
+    specs = [(2, [0.87, 0.92, 1.0], [1.0, 0.0125, 1.0], None, 7, True),
+             (2, [0.85, 0.88, 0.92, 1.0], [0.33, 1.79, 0.0042, 0.33], None, 12, False),
+             (1, [0.80, 0.90, 1.0], [0.5, 0.02, 0.8], None, 5, False),
+             (2, [0.87, 0.92, 1.0], [1.2, 0.01, 0.9], SEED + 9, 9, True)]
+    for k, (sub, radii, sig, pert, nd, meg) in enumerate(specs):
+        head = syn.nested_head(sub, radii, sig, perturb_seed=pert)
+        out.append(Workload(f"batch_small_{k}", head, syn.random_dipoles(nd, SEED + 200 + k, rmax=0.7),
+                            syn.fibonacci_points(12 + 4 * k, 1.0),
+                            syn.radial_magnetometers(10, 1.2) if meg else np.zeros((0, 6))))
+    return out
 
 
 def config4(n_dipoles: int = 10000) -> Workload:
