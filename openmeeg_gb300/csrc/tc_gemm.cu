@@ -7,15 +7,19 @@
 // mantissa bits cleared) and Xl = X - Xh; the product is accumulated as
 // Ah*Bh + Ah*Bl + Al*Bh (the "3xTF32" scheme), with FP32 accumulation in TMEM.
 //
-// One CTA computes a 128 x 128 tile.  Warp 0 allocates 128 TMEM columns; one
-// thread streams the K dimension in 32-element (128-byte) chunks through a
-// two-stage shared-memory ring filled by TMA (cp.async.bulk.tensor, 128-byte
-// swizzle) and issues tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=128, K=8)
-// per 8-element step; tcgen05.commit signals each stage free and the final
-// accumulation done.  All four warps then read their 32 TMEM lanes with
-// tcgen05.ld and update C.  Every mbarrier wait is bounded: on timeout the
-// kernel records OMG_ERR_TIMEOUT, waits (bounded) for copies in flight,
-// releases TMEM and returns without touching C.
+// Persistent and warp-specialized: one CTA per SM walks a static list of
+// 128 x 128 output tiles (all tiles, or the lower triangle for a symmetric
+// update).  Warp 0 streams the K dimension in 32-element (128-byte) chunks
+// into a three-stage shared-memory ring with TMA (cp.async.bulk.tensor,
+// 128-byte swizzle); warp 1 issues tcgen05.mma.cta_group::1.kind::tf32
+// (M=128, N=128, K=8) into one of two TMEM accumulators, so the next tile's
+// products overlap the previous tile's epilogue; warps 2-9 (two per TMEM lane
+// quarter, 64 columns each) load the tile's C into registers while its
+// products run, then read their TMEM lanes with tcgen05.ld and write C.  Stages and accumulators are handed over with
+// mbarriers (TMA complete_tx, tcgen05.commit, epilogue arrivals).  Every wait
+// is bounded: on timeout the kernel records OMG_ERR_TIMEOUT, every role stops,
+// copies and products in flight are waited for (bounded), TMEM is released
+// and the CTA returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -28,11 +32,13 @@ namespace omg {
 namespace tc {
 
 constexpr int BM = 128, BN = 128, BK = 32;
-constexpr int STAGES = 2;
+constexpr int STAGES = 3;
 constexpr int TILE_BYTES = BM * BK * 4;           // 16 KiB (BM == BN)
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;       // Ah, Al, Bh, Bl
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
-constexpr uint32_t TMEM_COLS = 128;
+constexpr int THREADS = 320;                      // producer, MMA, 8 epilogue warps
+constexpr int EPI_WARPS = 8;                      // two per TMEM lane quarter, 64 columns each
+constexpr uint32_t TMEM_COLS = 256;               // two 128-column FP32 accumulators
 
 // Instruction descriptor: D=F32, A=B=TF32, both K-major, N=128, M=128.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -84,29 +90,64 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(dev::smem_u32(bar)) : "memory");
+}
+
+// Bounded wait that also gives up as soon as another role has aborted.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t phase, volatile int* abort) {
+    for (uint32_t it = 0; it < (1u << 20); ++it) {
+        if (dev::mbar_try_wait(bar, phase)) return true;
+        if (*abort) return false;
+    }
+    return false;
+}
+
+// Tile t of the walk -> (tile row, tile column).  Lower: row-major over the
+// lower triangle (diagonal included); otherwise column of tiles after column.
+__device__ __forceinline__ void tile_of(int64_t t, int tiles_m, int lower, int& tm, int& tn) {
+    if (lower) {
+        int r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((int64_t)r * (r + 1) / 2 > t) --r;
+        while ((int64_t)(r + 1) * (r + 2) / 2 <= t) ++r;
+        tm = r;
+        tn = (int)(t - (int64_t)r * (r + 1) / 2);
+    } else {
+        tm = (int)(t % tiles_m);
+        tn = (int)(t / tiles_m);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                        const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
-                       int K, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod, int* err) {
+                       int K, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod, int64_t ntiles,
+                       int* err) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t full_bar[STAGES];
-    __shared__ __align__(8) uint64_t mma_bar[STAGES];
-    __shared__ __align__(8) uint64_t done_bar;
+    __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
+    __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
     __shared__ uint32_t tmem_holder;
-    __shared__ int s_abort;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    if (lower && n0 > m0 + BM - 1) return;   // tile strictly above the diagonal (uniform for the CTA)
+    __shared__ volatile int s_abort;
+    __shared__ int64_t s_issued, s_consumed;
     const uint32_t sbase = (dev::smem_u32(smem_raw) + 1023u) & ~1023u;   // 1024-byte aligned ring
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int tiles_m = (M + BM - 1) / BM;
+    const int nk = (K + BK - 1) / BK;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             dev::mbar_init(&full_bar[s], 1);
-            dev::mbar_init(&mma_bar[s], 1);
+            dev::mbar_init(&empty_bar[s], 1);
         }
-        dev::mbar_init(&done_bar, 1);
+        for (int a = 0; a < 2; ++a) {
+            dev::mbar_init(&tfull_bar[a], 1);
+            dev::mbar_init(&tempty_bar[a], EPI_WARPS);
+        }
+        dev::mbar_init(&fin_bar, 1);
         s_abort = 0;
+        s_issued = 0;
+        s_consumed = 0;
     }
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          dev::smem_u32(&tmem_holder)),
                      "r"(TMEM_COLS)
@@ -117,96 +158,125 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_holder;
-    const int nk = (K + BK - 1) / BK;
     const uint32_t bytes_per_stage = (nprod == 3 ? 4u : 2u) * TILE_BYTES;
 
-    if (threadIdx.x == 0) {
-        int issued = 0, consumed = 0;
-        auto issue = [&](int c) {
-            const int slot = c % STAGES;
-            const uint32_t st = sbase + slot * STAGE_BYTES;
-            dev::mbar_expect_tx(&full_bar[slot], bytes_per_stage);
-            tma_load_2d(st, &tAh, c * BK, m0, &full_bar[slot]);
-            tma_load_2d(st + 2 * TILE_BYTES, &tBh, c * BK, n0, &full_bar[slot]);
-            if (nprod == 3) {
-                tma_load_2d(st + TILE_BYTES, &tAl, c * BK, m0, &full_bar[slot]);
-                tma_load_2d(st + 3 * TILE_BYTES, &tBl, c * BK, n0, &full_bar[slot]);
-            }
-            ++issued;
-        };
-        for (int c = 0; c < STAGES && c < nk; ++c) issue(c);
-        bool ok = true;
-        for (int c = 0; c < nk; ++c) {
-            const int slot = c % STAGES;
-            const uint32_t ph = (uint32_t)((c / STAGES) & 1);
-            if (!dev::mbar_wait_bounded(&full_bar[slot], ph)) {
-                ok = false;
-                break;
-            }
-            ++consumed;
-            fence_after();
-            const uint32_t st = sbase + slot * STAGE_BYTES;
-            const uint64_t dAh = sdesc_sw128(st), dAl = sdesc_sw128(st + TILE_BYTES);
-            const uint64_t dBh = sdesc_sw128(st + 2 * TILE_BYTES), dBl = sdesc_sw128(st + 3 * TILE_BYTES);
-#pragma unroll
-            for (int kk = 0; kk < BK / 8; ++kk) {
-                const uint64_t off = (uint64_t)(kk * 32) >> 4;   // 8 TF32 = 32 bytes along the swizzled row
-                mma_tf32(tmem, dAh + off, dBh + off, (c | kk) != 0 ? 1u : 0u);
-                if (nprod == 3) {
-                    mma_tf32(tmem, dAh + off, dBl + off, 1u);
-                    mma_tf32(tmem, dAl + off, dBh + off, 1u);
+    if (warp == 0) {
+        if (lane == 0) {   // ---- TMA producer
+            int64_t g = 0;
+            for (int64_t t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
+                int tm, tn;
+                tile_of(t, tiles_m, lower, tm, tn);
+                for (int c = 0; c < nk; ++c, ++g) {
+                    const int slot = (int)(g % STAGES);
+                    if (!wait_or_abort(&empty_bar[slot], (uint32_t)(((g / STAGES) & 1) ^ 1), &s_abort)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    const uint32_t st = sbase + slot * STAGE_BYTES;
+                    dev::mbar_expect_tx(&full_bar[slot], bytes_per_stage);
+                    tma_load_2d(st, &tAh, c * BK, tm * BM, &full_bar[slot]);
+                    tma_load_2d(st + 2 * TILE_BYTES, &tBh, c * BK, tn * BN, &full_bar[slot]);
+                    if (nprod == 3) {
+                        tma_load_2d(st + TILE_BYTES, &tAl, c * BK, tm * BM, &full_bar[slot]);
+                        tma_load_2d(st + 3 * TILE_BYTES, &tBl, c * BK, tn * BN, &full_bar[slot]);
+                    }
+                    s_issued = g + 1;
                 }
             }
-            mma_commit(&mma_bar[slot]);
-            if (c + STAGES < nk) {
-                if (!dev::mbar_wait_bounded(&mma_bar[slot], ph)) {
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // ---- MMA issuer
+            int64_t g = 0, lt = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
+                const uint32_t ab = (uint32_t)(lt & 1), aph = (uint32_t)((lt >> 1) & 1);
+                if (!wait_or_abort(&tempty_bar[ab], aph ^ 1u, &s_abort)) {
                     ok = false;
                     break;
                 }
-                issue(c + STAGES);
+                fence_after();
+                const uint32_t acc = tmem + ab * BN;
+                for (int c = 0; c < nk; ++c, ++g) {
+                    const int slot = (int)(g % STAGES);
+                    if (!wait_or_abort(&full_bar[slot], (uint32_t)((g / STAGES) & 1), &s_abort)) {
+                        ok = false;
+                        break;
+                    }
+                    s_consumed = g + 1;
+                    fence_after();
+                    const uint32_t st = sbase + slot * STAGE_BYTES;
+                    const uint64_t dAh = sdesc_sw128(st), dAl = sdesc_sw128(st + TILE_BYTES);
+                    const uint64_t dBh = sdesc_sw128(st + 2 * TILE_BYTES), dBl = sdesc_sw128(st + 3 * TILE_BYTES);
+#pragma unroll
+                    for (int kk = 0; kk < BK / 8; ++kk) {
+                        const uint64_t off = (uint64_t)(kk * 32) >> 4;   // 8 TF32 = 32 bytes along the swizzled row
+                        mma_tf32(acc, dAh + off, dBh + off, (c | kk) != 0 ? 1u : 0u);
+                        if (nprod == 3) {
+                            mma_tf32(acc, dAh + off, dBl + off, 1u);
+                            mma_tf32(acc, dAl + off, dBh + off, 1u);
+                        }
+                    }
+                    mma_commit(&empty_bar[slot]);   // the stage is free once these products are done
+                }
+                if (!ok) break;
+                mma_commit(&tfull_bar[ab]);         // the accumulator is complete
             }
+            if (!ok) s_abort = 1;
+            mma_commit(&fin_bar);                   // arrives once every product issued above has completed
+            if (!dev::mbar_wait_bounded(&fin_bar, 0)) s_abort = 1;
         }
-        if (!ok) {
-            s_abort = 1;
-            atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
-            for (int c = consumed; c < issued; ++c)   // let copies in flight land before the CTA exits
-                dev::mbar_wait_bounded(&full_bar[c % STAGES], (uint32_t)((c / STAGES) & 1));
+    } else {   // ---- epilogue: warp w owns TMEM lanes 32 * (w % 4) .. +31 and 64 of the 128 columns
+        const int q = warp & 3;
+        const int half = (warp - 2) / 4;
+        int64_t lt = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+            int tm, tn;
+            tile_of(t, tiles_m, lower, tm, tn);
+            const uint32_t ab = (uint32_t)(lt & 1), aph = (uint32_t)((lt >> 1) & 1);
+            const int row = tm * BM + q * 32 + lane;
+            const int n0 = tn * BN + half * 64;
+            // columns n0 + j, j < jmax, are written by this thread (inside C, lower triangle when asked)
+            int jmax = row < M ? min(64, N - n0) : 0;
+            if (lower) jmax = min(jmax, row - n0 + 1);
+            float* const cp = C + ((int64_t)row + (int64_t)n0 * ldc);
+            const int ld32 = (int)ldc;   // 64 * ldc fits in 32 bits (host-checked)
+            // C of this tile into registers while its products run (independent loads, all in flight)
+            float cv[64];
+#pragma unroll
+            for (int j = 0; j < 64; ++j) cv[j] = (j < jmax && beta != 0.f) ? __ldcg(cp + j * ld32) : 0.f;
+            bool ok = wait_or_abort(&tfull_bar[ab], aph, &s_abort);
+            ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld is warp-collective
+            if (!ok) {
+                if (lane == 0) s_abort = 1;
+                break;
+            }
+            fence_after();
+#pragma unroll
+            for (int chunk = 0; chunk < 2; ++chunk) {
+                uint32_t r[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64 + chunk * 32), r);
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (chunk * 32 + j < jmax)
+                        __stcg(cp + (chunk * 32 + j) * ld32, fmaf(alpha, __uint_as_float(r[j]), beta * cv[chunk * 32 + j]));
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty_bar[ab]);   // accumulator free for the tile after next
         }
-        mma_commit(&done_bar);   // arrives once every MMA issued above has completed
     }
     __syncthreads();
-    const bool done = dev::mbar_wait_bounded(&done_bar, 0);
-    fence_after();
-    const bool all_done = __syncthreads_and(done ? 1 : 0) != 0;   // CTA-uniform: tcgen05.ld is warp-collective
-    if (all_done && !s_abort) {
-        const int row = m0 + warp * 32 + lane;
-        for (int chunk = 0; chunk < BN / 32; ++chunk) {
-            uint32_t r[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(chunk * 32), r);
-            if (row < M) {
-                // All loads of the chunk first (independent, in flight together), then the stores.
-                float cv[32];
-                const int64_t cbase = (int64_t)row + (int64_t)(n0 + chunk * 32) * ldc;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int col = n0 + chunk * 32 + j;
-                    const bool ok = col < N && (!lower || row >= col);
-                    cv[j] = (ok && beta != 0.f) ? __ldcg(C + cbase + (int64_t)j * ldc) : 0.f;
-                }
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int col = n0 + chunk * 32 + j;
-                    if (col < N && (!lower || row >= col))
-                        __stcg(C + cbase + (int64_t)j * ldc, fmaf(alpha, __uint_as_float(r[j]), beta * cv[j]));
-                }
-            }
+    if (s_abort) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
+            for (int64_t g = s_consumed; g < s_issued; ++g)   // let copies in flight land before the CTA exits
+                dev::mbar_wait_bounded(&full_bar[g % STAGES], (uint32_t)((g / STAGES) & 1));
         }
-    } else if (!all_done && threadIdx.x == 0) {
-        atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
+        __syncthreads();
     }
     fence_before();
     __syncthreads();
-    if (warp == 0)
+    if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
@@ -269,14 +339,23 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     const CUtensorMap mBh = tc::make_map(Bh + b_k0, N, b_kext - b_k0, ldb);
     const CUtensorMap mBl = nprod == 3 ? tc::make_map(Bl + b_k0, N, b_kext - b_k0, ldb) : mBh;
     static bool attr = false;
+    static int n_sm = 0;
     if (!attr) {
         cudaFuncSetAttribute(tc::gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (n_sm <= 0) n_sm = 1;
         attr = true;
     }
-    dim3 grid((unsigned)((N + tc::BN - 1) / tc::BN), (unsigned)((M + tc::BM - 1) / tc::BM));
-    if (grid.y > 65535) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM too tall");
-    tc::gemm_tf32x3_kernel<<<grid, 128, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, alpha, beta,
-                                                             C, ldc, lower ? 1 : 0, nprod, err);
+    if (lower && M != N) throw Error(OMG_ERR_INVALID, "lower-triangle tensor-core update needs M == N");
+    if (ldc > (int64_t)(1 << 24)) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM leading dimension too large");
+    const int64_t tiles_m = (M + tc::BM - 1) / tc::BM, tiles_n = (N + tc::BN - 1) / tc::BN;
+    if (tiles_m > (1 << 30) / 2) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM too tall");
+    const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
+    tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, alpha,
+                                                                     beta, C, ldc, lower ? 1 : 0, nprod, ntiles, err);
     check_tc("gemm_tf32x3");
 }
 

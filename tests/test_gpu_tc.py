@@ -67,3 +67,9 @@ def test_tc_gemm_head_only_is_tf32_accurate(cuda):
 
 def test_tc_gemm_lower_update(cuda):
     assert _run(640, 640, 128, -1.0, 1.0, True, True) < 1e-5
+
+
+@pytest.mark.parametrize("M,N,K,lower", [(5000, 1000, 64, False), (4100, 4100, 128, True)])
+def test_tc_gemm_many_tiles_per_cta(cuda, M, N, K, lower):
+    # more tiles than SMs: every CTA walks several tiles through both TMEM accumulators
+    assert _run(M, N, K, -1.0, 1.0, lower, True) < 1e-5
