@@ -86,6 +86,8 @@ void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld,
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
 void split_lower_inplace(int64_t n, float* A, int64_t lda, float* R, cudaStream_t s);
 void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_t lda, float* Linv, cudaStream_t s);
+void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
+               float* Bl, cudaStream_t s);
 void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, float* B, int64_t ldb, float* H,
                      float* L, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
@@ -421,11 +423,12 @@ static void factor_ldlt(omg_solver sv, T* A, int64_t ld, int nb) {
 
 constexpr int NB32_TC = 128;   // tensor-core path: panel width = GEMM K = 4 x 32-element TMA chunks
 
-// FP32 factorization with the trailing updates on the tensor cores (3xTF32):
-// each panel L21 is split into K-major TF32 heads/remainders (kept for the
-// forward solves), the trailing block is updated by the tcgen05 GEMM, and at
-// the end the whole factor is split in place (heads) + remainders (A32r) for
-// the backward solves.
+// FP32 factorization with the panel solves and trailing updates on the
+// tensor cores (3xTF32): each diagonal block is factored and inverted in one
+// CTA, the panel is L21 = A21 L11^-T by the tcgen05 GEMM, L21 is split into
+// K-major TF32 heads/remainders (kept for the forward solves) and the
+// trailing block is updated by the tcgen05 GEMM; at the end the whole factor
+// is split in place (heads) + remainders (A32r) for the backward solves.
 static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N, nP = sv->nP;
@@ -441,12 +444,24 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     sv->w_off.assign(nblocks + 1, 0);
     for (size_t b = 0; b < nblocks; ++b) sv->w_off[b + 1] = sv->w_off[b] + 2 * (N - sv->bounds[b + 1]) * nb;
     sv->W = DevBuf((size_t)std::max<int64_t>(1, sv->w_off[nblocks]) * sizeof(float), s, sv->persistent);
+    sv->Linv32 = DevBuf((size_t)nblocks * nb * nb * sizeof(float), s, sv->persistent);
+    DevBuf T((size_t)2 * std::max<int64_t>(1, N) * nb * sizeof(float), s);   // A21 split, K-major
+    DevBuf Bi((size_t)2 * nb * nb * sizeof(float), s);                        // L11^-1 split, K-major
+    float* Th = T.as<float>();
+    float* Bih = Bi.as<float>();
+    float* Bil = Bih + (size_t)nb * nb;
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
         if (k0 == nP) negate_lower<float>(A + k0 + k0 * ld, ld, N - k0, s);
-        potrf<float>(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0, s);
+        // L11 and L11^-1 (the inverse also serves the solves)
+        potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
+                  sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
         if (m > 0) {
-            trsm_rows<float>(m, (int)nk, A + k0 + k0 * ld, ld, A + k1 + k0 * ld, ld, s);
+            // L21 = A21 L11^-T on the tensor cores, then its split for the trailing update
+            float* Tl = Th + m * nb;
+            split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
+            gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
+                        sv->ctx->d_err, s);
             float* Wh = sv->W.as<float>() + sv->w_off[b];
             float* Wl = Wh + m * nb;
             split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Wh, Wl, s);
@@ -456,8 +471,6 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     }
     sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
     split_lower_inplace(N, A, ld, sv->A32r.as<float>(), s);
-    sv->Linv32 = DevBuf((size_t)nblocks * nb * nb * sizeof(float), s, sv->persistent);
-    inv_lower_blocks(N, nb, A, sv->A32r.as<float>(), ld, sv->Linv32.as<float>(), s);
 }
 
 // FP32 solve on the tensor cores: B <- HM^-1 B (internal numbering).

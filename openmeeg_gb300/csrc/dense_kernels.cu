@@ -699,6 +699,189 @@ void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_
     check("inv_lower_blocks");
 }
 
+// ---------------------------------------------------------------------------
+// Diagonal block of the FP32 factorization: Cholesky of the n x n (n <= 128)
+// block A11 and the inverse of its factor, in one CTA with everything in
+// shared memory.  Both are blocked by 32:
+//   Cholesky: warp 0 factors the 32 x 32 diagonal sub-block (lane = row),
+//     one thread per row solves the sub-panel below it, all threads update
+//     the trailing lower triangle;
+//   inverse: one warp per 32 x 32 diagonal sub-block (lane = column,
+//     substitution), then the off-diagonal sub-blocks by distance from the
+//     diagonal, X_ij = -X_ii (sum_{k=j}^{i-1} L_ik X_kj).
+// Outputs: L11 over A11 (lower), Linv column-major (ldi = 128, zero above the
+// diagonal and beyond n) for the solves, and Linv as TF32 head/remainder
+// K-major rows (128 x 128 each, zero padded) for the tensor-core panel solve
+// L21 = A21 Linv^T.  A pivot that is not positive is reported as
+// OMG_ERR_NOT_DEFINITE at its column (and replaced by 1 so the kernel ends).
+// ---------------------------------------------------------------------------
+constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512;
+
+__global__ void __launch_bounds__(PI_THREADS) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
+                                                               int64_t* err_col, int64_t col_offset, float* Linv,
+                                                               float* Bh, float* Bl) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float* sL = reinterpret_cast<float*>(smraw);   // row-major: sL[r * PI_LD + c]
+    float* sX = sL + PI_NB * PI_LD;                // inverse, row-major, same layout
+    float* sT = sX + PI_NB * PI_LD;                // 4 scratch sub-blocks of 32 x 33
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
+        const int r = e % PI_NB, c = e / PI_NB;    // coalesced down the columns of A
+        sL[r * PI_LD + c] = (r < n && c < n && r >= c) ? A[r + (int64_t)c * lda] : 0.f;
+        sX[r * PI_LD + c] = 0.f;
+    }
+    __syncthreads();
+    // ---- Cholesky, blocked by 32
+    for (int kb = 0; kb < n; kb += 32) {
+        const int nb = min(32, n - kb);
+        if (warp == 0) {
+            // the 32 x 32 diagonal sub-block in registers, lane = row
+            float v[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                v[c] = (lane < nb && c < nb && c <= lane) ? sL[(kb + lane) * PI_LD + kb + c] : 0.f;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                if (j < nb) {
+                    float d = __shfl_sync(0xffffffffu, v[j], j);
+                    if (!(d > 0.f)) {
+                        if (lane == j && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
+                            *err_col = col_offset + kb + j;
+                        d = 1.f;
+                    }
+                    const float sq = sqrtf(d), inv = 1.f / sq;
+                    if (lane == j) v[j] = sq;
+                    else if (lane > j) v[j] *= inv;
+#pragma unroll
+                    for (int c = j + 1; c < 32; ++c) {
+                        const float lcj = __shfl_sync(0xffffffffu, v[j], c);
+                        if (lane >= c) v[c] = fmaf(-v[j], lcj, v[c]);
+                    }
+                }
+            }
+            if (lane < nb) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c)
+                    if (c <= lane) sL[(kb + lane) * PI_LD + kb + c] = v[c];
+            }
+            __syncwarp();
+            // its inverse, lane = column: x_j = (delta_jc - sum_{l<j} D[j][l] x_l) / D[j][j]
+            float x[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                x[j] = 0.f;
+                if (j < nb) {
+                    const float* dj = sL + (kb + j) * PI_LD + kb;
+                    float acc = (j == lane) ? 1.f : 0.f;
+#pragma unroll
+                    for (int l = 0; l < j; ++l) acc = fmaf(-dj[l], x[l], acc);
+                    x[j] = (j >= lane) ? acc / dj[j] : 0.f;
+                }
+            }
+            if (lane < nb) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (j < nb) sX[(kb + j) * PI_LD + kb + lane] = x[j];
+            }
+        }
+        __syncthreads();
+        // sub-panel below: L[r][kb + c] = sum_{l <= c} A[r][kb + l] Dinv[c][l]; four threads per row
+        const int r0 = kb + nb;
+        float out[8];
+        const int rr = r0 + tid / 4, q8 = (tid % 4) * 8;
+        const bool act = tid / 4 < 128 && rr < n;
+        if (act) {
+            const float* ar = sL + rr * PI_LD + kb;
+            float a[32];
+#pragma unroll
+            for (int l = 0; l < 32; ++l) a[l] = l < nb ? ar[l] : 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int c = q8 + k;
+                const float* di = sX + (kb + min(c, 31)) * PI_LD + kb;
+                float acc = 0.f;
+#pragma unroll
+                for (int l = 0; l < 32; ++l)
+                    if (l <= c && c < nb) acc = fmaf(a[l], di[l], acc);
+                out[k] = acc;
+            }
+        }
+        __syncthreads();
+        if (act) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (q8 + k < nb) sL[rr * PI_LD + kb + q8 + k] = out[k];
+        }
+        __syncthreads();
+        const int m2 = n - r0;
+        for (int e = tid; e < m2 * m2; e += PI_THREADS) {   // trailing lower triangle
+            const int r = r0 + e / m2, c = r0 + e % m2;
+            if (c > r) continue;
+            const float* lr = sL + r * PI_LD + kb;
+            const float* lc = sL + c * PI_LD + kb;
+            float acc = 0.f;
+            for (int l = 0; l < nb; ++l) acc = fmaf(lr[l], lc[l], acc);
+            sL[r * PI_LD + c] -= acc;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < n * n; e += PI_THREADS) {
+        const int r = e % n, c = e / n;
+        if (r >= c) A[r + (int64_t)c * lda] = sL[r * PI_LD + c];
+    }
+    const int nblk = (n + 31) / 32;
+    // ---- inverse: off-diagonal sub-blocks, X_ij = -X_ii T, T = sum_{m in [32j, 32i)} L[32i + r][m] X[m][32j + c]
+    for (int dist = 1; dist < nblk; ++dist) {
+        const int nbp = nblk - dist;   // block pairs (i, j = i - dist), i = dist .. nblk-1
+        for (int e = tid; e < nbp * 1024; e += PI_THREADS) {
+            const int p = e / 1024, r = (e % 1024) / 32, c = e % 32;
+            const int i = dist + p, j = i - dist;
+            float acc = 0.f;
+            if (32 * i + r < n && 32 * j + c < n) {
+                const float* li = sL + (32 * i + r) * PI_LD;
+                for (int m = 32 * j; m < 32 * i; ++m) acc = fmaf(li[m], sX[m * PI_LD + 32 * j + c], acc);
+            }
+            sT[p * 32 * 33 + r * 33 + c] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < nbp * 1024; e += PI_THREADS) {
+            const int p = e / 1024, r = (e % 1024) / 32, c = e % 32;
+            const int i = dist + p, j = i - dist;
+            if (32 * i + r < n && 32 * j + c < n) {
+                const float* xi = sX + (32 * i + r) * PI_LD + 32 * i;
+                float acc = 0.f;
+                for (int m = 0; m <= r; ++m) acc = fmaf(xi[m], sT[p * 32 * 33 + m * 33 + c], acc);
+                sX[(32 * i + r) * PI_LD + 32 * j + c] = -acc;
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
+        const int r = e % PI_NB, c = e / PI_NB;
+        const float v = sX[r * PI_LD + c];          // zero above the diagonal and beyond n
+        Linv[r + c * PI_NB] = v;                    // column-major
+        const int rr = e / PI_NB, cc = e % PI_NB;   // K-major rows: B[rr][cc] = Linv[rr][cc]
+        const float w = sX[rr * PI_LD + cc];
+        const float h = __uint_as_float(__float_as_uint(w) & 0xFFFFE000u);
+        Bh[rr * PI_NB + cc] = h;
+        Bl[rr * PI_NB + cc] = w - h;
+    }
+}
+
+void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
+               float* Bl, cudaStream_t s) {
+    if (n <= 0 || n > PI_NB) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
+    ProfScope prof_("potrf_inv", s);
+    const size_t sm = (2 * (size_t)PI_NB * PI_LD + 4 * 32 * 33) * sizeof(float);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(potrf_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        attr = true;
+    }
+    potrf_inv_kernel<<<1, PI_THREADS, sm, s>>>(A, lda, n, err, err_col, col_offset, Linv, Bh, Bl);
+    check("potrf_inv");
+}
+
 // B_k <- op(Linv_k) B_k for the n x ncol block at B (ldb), op = transpose if
 // `trans`; also writes the TF32 head/remainder split of the result as K-major
 // rows (column j -> row j of H/L, kpad = nb) for the following tensor-core
