@@ -182,6 +182,9 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
     library's stream).
 
     Algorithmic work:
+      residual_tc -- R = B - A X from fixed-point digits on the tensor cores: 7 x 7 bf16
+        digit planes, 28 digit pairs up to level 8, each an N x N x k_pad integer GEMM
+        (k_pad = k rounded up to 128); the FP64-equivalent work is 2 N^2 k.
       residual_df64 -- R = B - A X in double-float arithmetic: reads the float-pair
         head matrix (8 N^2 bytes), X pairs (8 N k), B (8 N k), writes R (8 N k);
         N^2 k multiply-adds at 12 FP32 operations each (exact product + TwoSum).
@@ -195,7 +198,20 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
     t_launch = ms / 1e3 / launches
     per_step = launches / steps
     info = {"kernel": name, "launches_per_step": per_step, "mean_launch_ms": ms / launches}
-    if name == "residual_df64":
+    if name == "residual_tc":
+        # R = B - A X from 7 + 7 bf16 digit planes, 28 digit pairs (levels <= 8): every pair is a full
+        # N x N x k integer GEMM on the tensor cores, padded to 128-column tiles of the k right-hand sides
+        pairs = 28
+        kpad = (k + 127) // 128 * 128
+        flops = 2.0 * N * N * kpad * pairs
+        achieved = flops / t_launch / 1e12
+        info.update({"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": achieved / bf16, "traffic": None,
+                     "algorithmic_fp64_equivalent_flops_per_launch": 2.0 * N * N * k,
+                     "executed_bf16_flops_per_launch": flops,
+                     "note": f"executed bf16 tensor flops (28 exact digit-pair GEMMs, k padded to {kpad}) vs "
+                             f"{kind} bf16 burst peak"})
+    elif name == "residual_df64":
         nbytes = 8.0 * N * N + 24.0 * N * k
         achieved = nbytes / t_launch / 1e9
         tr = NCU_TRAFFIC_PER_UNIT.get(name)
@@ -273,18 +289,22 @@ def run_gpu(args):
     clocks = Clocks(local)
     clocks.start()
     launches0 = ctx.launches()
-    _lib.profile_enable(True)
-    _lib.profile_read()
     torch.cuda.synchronize()
     e0.record()
     for _ in range(args.steps):
         gex, gmx, stx = step("mixed")
     e1.record()
     torch.cuda.synchronize()
-    _lib.profile_enable(False)
-    prof = _lib.profile_read()
     launches = ctx.launches() - launches0
     ck = clocks.stop()
+    # per-kernel breakdown from separate profiled steps (events around every launch), outside the timed region
+    _lib.profile_enable(True)
+    _lib.profile_read()
+    for _ in range(args.profile_steps):
+        step("mixed")
+    torch.cuda.synchronize()
+    _lib.profile_enable(False)
+    prof = _lib.profile_read()
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps
     t_max = t_step
     if world > 1:
@@ -318,9 +338,9 @@ def run_gpu(args):
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
     dname, (dl, dms) = dom
     total_prof_ms = sum(v[1] for v in prof.values())
-    roof = roofline_entry(dname, dl, dms, args.steps, N, ne + nm, nd, stx, pk)
-    others = {n: roofline_entry(n, v[0], v[1], args.steps, N, ne + nm, nd, stx, pk)
-              for n, v in prof.items() if n in ("residual_df64", "gemm_tf32x3") and n != dname}
+    roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx, pk)
+    others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx, pk)
+              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_tf32x3") and n != dname}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -345,9 +365,10 @@ def run_gpu(args):
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "path": "omg_geometry_create + omg_gain_host (host buffers, mixed)"},
             "gpu_launches": int(launches),
-            "kernels_ms_per_step": {k: round(v[1] / args.steps, 3) for k, v in
+            "kernels_ms_per_step": {k: round(v[1] / args.profile_steps, 3) for k, v in
                                     sorted(prof.items(), key=lambda kv: -kv[1][1])},
-            "profiled_ms_per_step": round(total_prof_ms / args.steps, 3),
+            "profiled_ms_per_step": round(total_prof_ms / args.profile_steps, 3),
+            "profile_note": "per-kernel CUDA-event times from separate profiled steps (not the timed ones)",
             "roofline": roof,
             "roofline_other": others,
             "clocks": ck,
@@ -470,6 +491,7 @@ def main():
     ap.add_argument("--config", default="config1")
     ap.add_argument("--branches", type=int, default=0, help="config3: graph branches (0 = autotune)")
     ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--profile-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-mixed", action="store_true",

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -93,6 +94,12 @@ void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, f
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
                    cudaStream_t s);
 void ratio_max(int64_t n, const double* num, const double* den, double* out, cudaStream_t s);
+int64_t digits_ld(int64_t n);
+void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta, int64_t rows_per_plane,
+                    int64_t ldo, void* out, int* ex, cudaStream_t s);
+void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
+                     int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
+                     int64_t ldr, int* err, cudaStream_t s);
 void launch_domain_check(int64_t n, const int* dom, uint64_t allowed, int* err, cudaStream_t s);
 }  // namespace omg
 
@@ -190,6 +197,8 @@ static void upload_geometry(omg_geometry g) {
     d.v2t_beg = upload(g->bufs, h.v2t_beg, s);
     d.v2t_tri = upload(g->bufs, h.v2t_tri, s);
     d.v2t_loc = upload(g->bufs, h.v2t_loc, s);
+    g->bufs.emplace_back(std::max<size_t>(1, h.v2t_tri.size()) * 3 * sizeof(double), s, true);
+    d.v2t_q = g->bufs.back().as<double>();
     g->tmesh = upload(g->bufs, tmesh, s);
     g->tidx_ref = upload(g->bufs, h.tidx, s);
     g->barrier = upload(g->bufs, h.barrier, s);
@@ -221,6 +230,7 @@ static void upload_geometry(omg_geometry g) {
     g->binside = upload(g->bufs, bi, s);
     g->dsigma = upload(g->bufs, sig, s);
     launch_prepare_triangles_order(d, 3, s);
+    launch_prepare_vertex_curls(d, s);
     g->prepared_order = 3;
 }
 
@@ -541,13 +551,51 @@ void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
         sv->A32 = DevBuf((size_t)sv->ld32 * N * sizeof(float), s, sv->persistent);
         copy_convert<double, float>(N, N, hm.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
         symmetrize(hm.as<double>(), N, N, s);
-        // the FP64 matrix is kept only as an exact float pair (hi + lo) for the residual
-        sv->A64 = DevBuf((size_t)2 * N * N * sizeof(float), s, sv->persistent);
-        split_f64(N, N, hm.as<double>(), N, sv->A64.as<float>(), sv->A64.as<float>() + (size_t)N * N, N, s);
+        const char* mode = std::getenv("OMG_RESIDUAL");
+        sv->tc_residual = !(mode && std::string(mode) == "df64");
+        if (sv->tc_residual) {
+            // the FP64 matrix is kept only as fixed-point digits for the tensor-core residual
+            const int64_t ldd = digits_ld(N);
+            sv->Adig = DevBuf((size_t)sv->nda * N * ldd * 2, s, sv->persistent);
+            sv->rexp = DevBuf((size_t)N * sizeof(int), s, sv->persistent);
+            digits_columns(hm.as<double>(), N, N, N, sv->nda, sv->beta, N, ldd, sv->Adig.p, sv->rexp.as<int>(), s);
+        } else {
+            // ... or as an exact float pair (hi + lo) for the double-float residual
+            sv->A64 = DevBuf((size_t)2 * N * N * sizeof(float), s, sv->persistent);
+            split_f64(N, N, hm.as<double>(), N, sv->A64.as<float>(), sv->A64.as<float>() + (size_t)N * N, N, s);
+        }
         hm.release();
         factor_ldlt_tc(sv, sv->A32.as<float>(), sv->ld32, NB32_TC);
     }
     if (check) check_err(sv->ctx, "factorization");
+}
+
+// Scratch of one refinement residual: X digits + column exponents, or X as a float pair.
+static size_t mixed_residual_scratch(omg_solver sv, int64_t nrhs) {
+    const int64_t N = sv->N;
+    if (!sv->tc_residual) return (size_t)2 * N * nrhs * 4;
+    const int64_t kpad = (nrhs + 127) / 128 * 128;
+    return (size_t)sv->ndx * kpad * digits_ld(N) * 2 + (size_t)kpad * sizeof(int);
+}
+
+// r = B - HM x with FP64-level accuracy (x: N x nrhs, column-major).
+static void mixed_residual(omg_solver sv, const double* x, int64_t nrhs, const double* B, int64_t ldb, double* r,
+                           DevBuf& XS) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N;
+    if (sv->tc_residual) {
+        const int64_t kpad = (nrhs + 127) / 128 * 128, ldd = digits_ld(N);
+        uint8_t* xd = XS.as<uint8_t>();
+        int* cexp = reinterpret_cast<int*>(xd + (size_t)sv->ndx * kpad * ldd * 2);
+        digits_columns(x, N, nrhs, N, sv->ndx, sv->beta, kpad, ldd, xd, cexp, s);
+        residual_slices(N, nrhs, sv->Adig.p, sv->nda, sv->rexp.as<int>(), xd, sv->ndx, kpad, cexp, sv->beta,
+                        sv->lmax, B, ldb, r, N, sv->ctx->d_err, s);
+    } else {
+        float* xh = XS.as<float>();
+        split_f64(N, nrhs, x, N, xh, xh + (size_t)N * nrhs, N, s);
+        const float* ah = sv->A64.as<float>();
+        residual_df64(N, nrhs, N, ah, ah + (size_t)N * N, N, xh, xh + (size_t)N * nrhs, N, B, ldb, r, N, s);
+    }
 }
 
 // Mixed precision: x = HM^-1 b by FP32 solves refined against the FP64 HM.
@@ -559,7 +607,7 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
     DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s),
-        XS((size_t)2 * N * nrhs * 4, s);
+        XS(mixed_residual_scratch(sv, nrhs), s);
     DevBuf rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s), dn((size_t)nrhs * 8, s), xn((size_t)nrhs * 8, s),
         bn((size_t)nrhs * 8, s);
     double* x = X.as<double>();
@@ -574,10 +622,7 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     double last_res = 1.0, est = 1.0, prev_est = 1e300;
     for (int it = 0; it <= sv->max_refine; ++it) {
         if (it > 0) {   // r = b - HM x
-            float* xh = XS.as<float>();
-            split_f64(N, nrhs, x, N, xh, xh + (size_t)N * nrhs, N, s);
-            const float* ah = sv->A64.as<float>();
-            residual_df64(N, nrhs, N, ah, ah + (size_t)N * N, N, xh, xh + (size_t)N * nrhs, N, B, ldb, r, N, s);
+            mixed_residual(sv, x, nrhs, B, ldb, r, XS);
             col_norms(N, nrhs, r, N, rn.as<double>(), s);
             cn = rn.as<double>();
             ++steps;
@@ -616,7 +661,7 @@ void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int 
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
     DevBuf X((size_t)N * nrhs * 8, s), R((size_t)N * nrhs * 8, s), B32((size_t)N * nrhs * 4, s),
-        XS((size_t)2 * N * nrhs * 4, s);
+        XS(mixed_residual_scratch(sv, nrhs), s);
     DevBuf rn((size_t)nrhs * 8, s), sc((size_t)nrhs * 8, s), dn((size_t)nrhs * 8, s), xn((size_t)nrhs * 8, s);
     double* x = X.as<double>();
     double* r = R.as<double>();
@@ -625,10 +670,7 @@ void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int 
     col_norms(N, nrhs, r, N, rn.as<double>(), s);
     for (int it = 0; it <= residual_steps; ++it) {
         if (it > 0) {
-            float* xh = XS.as<float>();
-            split_f64(N, nrhs, x, N, xh, xh + (size_t)N * nrhs, N, s);
-            const float* ah = sv->A64.as<float>();
-            residual_df64(N, nrhs, N, ah, ah + (size_t)N * N, N, xh, xh + (size_t)N * nrhs, N, B, ldb, r, N, s);
+            mixed_residual(sv, x, nrhs, B, ldb, r, XS);
             col_norms(N, nrhs, r, N, rn.as<double>(), s);
         }
         scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, rn.as<double>(), sc.as<double>(), s);

@@ -349,13 +349,41 @@ __device__ __forceinline__ d3 edge_cb(const double* V, const int32_t* T, int64_t
     return dev::ld3(V + 3 * (int64_t)T[3 * t + a]) - dev::ld3(V + 3 * (int64_t)T[3 * t + b]);
 }
 
+// Per vertex-triangle slot (CSR of v2t): q = CB / A, the edge vector opposite
+// the vertex over the triangle's area (area from the OperatorS record).
+__global__ void vertex_curls_kernel(int64_t nv, const int32_t* __restrict__ v2t_beg,
+                                    const int32_t* __restrict__ v2t_tri, const int8_t* __restrict__ v2t_loc,
+                                    const double* __restrict__ V, const int32_t* __restrict__ T,
+                                    const double* __restrict__ srec, double* q) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
+        const int64_t t = v2t_tri[k];
+        const d3 cb = edge_cb(V, T, t, v2t_loc[k]);
+        const double A = srec[t * SREC + 12];
+        q[3 * (int64_t)k + 0] = cb.x / A;
+        q[3 * (int64_t)k + 1] = cb.y / A;
+        q[3 * (int64_t)k + 2] = cb.z / A;
+    }
+}
+
+void launch_prepare_vertex_curls(const DevGeom& g, cudaStream_t s) {
+    if (g.nv == 0) return;
+    vertex_curls_kernel<<<nblocks(g.nv, 128), 128, 0, s>>>(g.nv, g.v2t_beg, g.v2t_tri, g.v2t_loc, g.V, g.T, g.srec,
+                                                            g.v2t_q);
+    check_launch("vertex curls");
+}
+
+// One thread per vertex pair; the v2 slots (triangle position + curl) are
+// kept in registers (v2 is warp-uniform for consecutive v1), every S entry is
+// read once per triangle pair.
+constexpr int NB_MAXD = 8;
+
 __global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e, int64_t v2b, int64_t n2,
                                int64_t t2b, int64_t t2e, int same, double coeff, const double* __restrict__ hm_src,
-                               int64_t ld, const double* __restrict__ tmp, const double* __restrict__ V,
-                               const int32_t* __restrict__ T, const double* __restrict__ srec,
-                               const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
-                               const int8_t* __restrict__ v2t_loc, const int32_t* __restrict__ tpos, int64_t nP,
-                               double* hm) {
+                               int64_t ld, const double* __restrict__ tmp, const int32_t* __restrict__ v2t_beg,
+                               const int32_t* __restrict__ v2t_tri, const double* __restrict__ vq,
+                               const int32_t* __restrict__ tpos, int64_t nP, double* hm) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= n1 * n2) return;
     const int64_t i1 = idx % n1, i2 = idx / n1;   // v1 fastest: coalesced writes down a column
@@ -364,18 +392,55 @@ __global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e
     const double factor = same ? 0.25 : (v1 == v2 ? 0.5 : 0.25);
     const int64_t nt2 = t2e - t2b;
     double result = 0.0;
-    for (int k1 = v2t_beg[v1]; k1 < v2t_beg[v1 + 1]; ++k1) {
-        const int64_t a = v2t_tri[k1];
-        if (a < t1b || a >= t1e) continue;
-        const d3 cb1 = edge_cb(V, T, a, v2t_loc[k1]);
-        const double A1 = srec[a * SREC + 12];
-        for (int k2 = v2t_beg[v2]; k2 < v2t_beg[v2 + 1]; ++k2) {
-            const int64_t b = v2t_tri[k2];
-            if (b < t2b || b >= t2e) continue;
-            const d3 cb2 = edge_cb(V, T, b, v2t_loc[k2]);
-            const double A2 = srec[b * SREC + 12];
-            const double sv = hm_src ? hm_src[lower_at(tpos[a], tpos[b], ld)] : tmp[(a - t1b) * nt2 + (b - t2b)];
-            result -= factor * dev::dot(cb1, cb2) * sv / (A1 * A2);
+    const int b0 = v2t_beg[v2], b1 = v2t_beg[v2 + 1];
+    if (b1 - b0 <= NB_MAXD) {
+        int64_t key[NB_MAXD];
+        double qx[NB_MAXD], qy[NB_MAXD], qz[NB_MAXD];
+        int nb = 0;
+#pragma unroll
+        for (int m = 0; m < NB_MAXD; ++m) {
+            key[m] = 0;
+            qx[m] = qy[m] = qz[m] = 0.0;
+            if (m < b1 - b0) {
+                const int64_t b = v2t_tri[b0 + m];
+                if (b >= t2b && b < t2e) {   // compact the slots of this mesh to the front
+#pragma unroll
+                    for (int w = 0; w < NB_MAXD; ++w)
+                        if (w == nb) {
+                            key[w] = hm_src ? (int64_t)tpos[b] : (b - t2b);
+                            qx[w] = vq[3 * (int64_t)(b0 + m)];
+                            qy[w] = vq[3 * (int64_t)(b0 + m) + 1];
+                            qz[w] = vq[3 * (int64_t)(b0 + m) + 2];
+                        }
+                    ++nb;
+                }
+            }
+        }
+        for (int k1 = v2t_beg[v1]; k1 < v2t_beg[v1 + 1]; ++k1) {
+            const int64_t a = v2t_tri[k1];
+            if (a < t1b || a >= t1e) continue;
+            const double px = vq[3 * (int64_t)k1], py = vq[3 * (int64_t)k1 + 1], pz = vq[3 * (int64_t)k1 + 2];
+            const int64_t ta = hm_src ? (int64_t)tpos[a] : (a - t1b) * nt2;
+#pragma unroll
+            for (int m = 0; m < NB_MAXD; ++m) {
+                if (m < nb) {
+                    const double sv = hm_src ? hm_src[lower_at(ta, key[m], ld)] : tmp[ta + key[m]];
+                    result -= factor * (px * qx[m] + py * qy[m] + pz * qz[m]) * sv;
+                }
+            }
+        }
+    } else {   // vertex of unusually high degree
+        for (int k1 = v2t_beg[v1]; k1 < v2t_beg[v1 + 1]; ++k1) {
+            const int64_t a = v2t_tri[k1];
+            if (a < t1b || a >= t1e) continue;
+            const double px = vq[3 * (int64_t)k1], py = vq[3 * (int64_t)k1 + 1], pz = vq[3 * (int64_t)k1 + 2];
+            for (int k2 = b0; k2 < b1; ++k2) {
+                const int64_t b = v2t_tri[k2];
+                if (b < t2b || b >= t2e) continue;
+                const double sv = hm_src ? hm_src[lower_at(tpos[a], tpos[b], ld)] : tmp[(a - t1b) * nt2 + (b - t2b)];
+                result -= factor * (px * vq[3 * (int64_t)k2] + py * vq[3 * (int64_t)k2 + 1] +
+                                    pz * vq[3 * (int64_t)k2 + 2]) * sv;
+            }
         }
     }
     hm[lower_at(nP + v1, nP + v2, ld)] += result * coeff;
@@ -387,8 +452,8 @@ void launch_N_block(const DevGeom& g, int64_t v1b, int64_t v1e, int64_t t1b, int
     const int64_t n = (v1e - v1b) * (v2e - v2b);
     ProfScope prof_("n_block", s);
     n_block_kernel<<<nblocks(n, 256), 256, 0, s>>>(v1b, v1e - v1b, t1b, t1e, v2b, v2e - v2b, t2b, t2e, same ? 1 : 0,
-                                                   coeff, hm_src, ld, tmp, g.V, g.T, g.srec, g.v2t_beg, g.v2t_tri,
-                                                   g.v2t_loc, g.tpos, g.nP, hm);
+                                                   coeff, hm_src, ld, tmp, g.v2t_beg, g.v2t_tri, g.v2t_q, g.tpos, g.nP,
+                                                   hm);
     check_launch("N block");
 }
 

@@ -701,165 +701,236 @@ void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_
 
 // ---------------------------------------------------------------------------
 // Diagonal block of the FP32 factorization: Cholesky of the n x n (n <= 128)
-// block A11 and the inverse of its factor, in one CTA with everything in
-// shared memory.  Both are blocked by 32:
-//   Cholesky: warp 0 factors the 32 x 32 diagonal sub-block (lane = row),
-//     one thread per row solves the sub-panel below it, all threads update
-//     the trailing lower triangle;
-//   inverse: one warp per 32 x 32 diagonal sub-block (lane = column,
-//     substitution), then the off-diagonal sub-blocks by distance from the
-//     diagonal, X_ij = -X_ii (sum_{k=j}^{i-1} L_ik X_kj).
+// block A11 and the inverse of its factor, in one CTA of 512 threads.  The
+// block lives in registers, distributed 2D-cyclically: thread (tr, tc) =
+// (tid / 32, tid % 32) holds rows tr + 16 i (i < 8) x columns tc + 32 q
+// (q < 4).  Both are right-looking in steps of 4 columns with one barrier per
+// step: the owners of the 4 columns (resp. rows of the inverse) publish them
+// to shared memory, every thread factors the 4 x 4 diagonal block itself and
+// applies the rank-4 update to the elements it holds.
 // Outputs: L11 over A11 (lower), Linv column-major (ldi = 128, zero above the
 // diagonal and beyond n) for the solves, and Linv as TF32 head/remainder
 // K-major rows (128 x 128 each, zero padded) for the tensor-core panel solve
 // L21 = A21 Linv^T.  A pivot that is not positive is reported as
 // OMG_ERR_NOT_DEFINITE at its column (and replaced by 1 so the kernel ends).
 // ---------------------------------------------------------------------------
-constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512;
+constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512, PI_W = 4;
 
 __global__ void __launch_bounds__(PI_THREADS) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
                                                                int64_t* err_col, int64_t col_offset, float* Linv,
                                                                float* Bh, float* Bl) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float* sL = reinterpret_cast<float*>(smraw);   // row-major: sL[r * PI_LD + c]
-    float* sX = sL + PI_NB * PI_LD;                // inverse, row-major, same layout
-    float* sT = sX + PI_NB * PI_LD;                // 4 scratch sub-blocks of 32 x 33
-    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    float* buf = sL + PI_NB * PI_LD;                // 2 x PI_W x 128: published columns / rows
+    const int tid = threadIdx.x, tr = tid / 32, tc = tid % 32;
     for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
         const int r = e % PI_NB, c = e / PI_NB;    // coalesced down the columns of A
         sL[r * PI_LD + c] = (r < n && c < n && r >= c) ? A[r + (int64_t)c * lda] : 0.f;
-        sX[r * PI_LD + c] = 0.f;
     }
     __syncthreads();
-    // ---- Cholesky, blocked by 32
-    for (int kb = 0; kb < n; kb += 32) {
-        const int nb = min(32, n - kb);
-        if (warp == 0) {
-            // the 32 x 32 diagonal sub-block in registers, lane = row
-            float v[32];
+    float v[8][4];
 #pragma unroll
-            for (int c = 0; c < 32; ++c)
-                v[c] = (lane < nb && c < nb && c <= lane) ? sL[(kb + lane) * PI_LD + kb + c] : 0.f;
+    for (int i = 0; i < 8; ++i)
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                if (j < nb) {
-                    float d = __shfl_sync(0xffffffffu, v[j], j);
-                    if (!(d > 0.f)) {
-                        if (lane == j && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
-                            *err_col = col_offset + kb + j;
-                        d = 1.f;
-                    }
-                    const float sq = sqrtf(d), inv = 1.f / sq;
-                    if (lane == j) v[j] = sq;
-                    else if (lane > j) v[j] *= inv;
+        for (int q = 0; q < 4; ++q) v[i][q] = sL[(tr + 16 * i) * PI_LD + tc + 32 * q];
+    // ---- Cholesky, 4 columns per step
+    for (int c0 = 0; c0 < n; c0 += PI_W) {
+        float* col = buf + ((c0 / PI_W) & 1) * PI_W * PI_NB;   // col[k * 128 + r] = a[r][c0 + k]
+        const int qj = c0 >> 5, k_own = tc - (c0 & 31);
+        if (k_own >= 0 && k_own < PI_W) {
 #pragma unroll
-                    for (int c = j + 1; c < 32; ++c) {
-                        const float lcj = __shfl_sync(0xffffffffu, v[j], c);
-                        if (lane >= c) v[c] = fmaf(-v[j], lcj, v[c]);
-                    }
+            for (int i = 0; i < 8; ++i) {
+                float x = v[i][0];
+#pragma unroll
+                for (int q = 1; q < 4; ++q) x = (q == qj) ? v[i][q] : x;
+                col[k_own * PI_NB + tr + 16 * i] = x;
+            }
+        }
+        __syncthreads();
+        // the 4 x 4 diagonal block, factored by every thread (columns past n act as identity)
+        float l[PI_W][PI_W];
+#pragma unroll
+        for (int a = 0; a < PI_W; ++a)
+#pragma unroll
+            for (int b = 0; b <= a; ++b) l[a][b] = (c0 + a < n) ? col[b * PI_NB + c0 + a] : (a == b ? 1.f : 0.f);
+        float il[PI_W];   // 1 / l[k][k]
+#pragma unroll
+        for (int k = 0; k < PI_W; ++k) {
+            float d = l[k][k];
+#pragma unroll
+            for (int m = 0; m < k; ++m) d = fmaf(-l[k][m], l[k][m], d);
+            if (!(d > 0.f)) {
+                if (tid == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0) *err_col = col_offset + c0 + k;
+                d = 1.f;
+            }
+            l[k][k] = sqrtf(d);
+            il[k] = 1.f / l[k][k];
+#pragma unroll
+            for (int a = k + 1; a < PI_W; ++a) {
+                float x = l[a][k];
+#pragma unroll
+                for (int m = 0; m < k; ++m) x = fmaf(-l[a][m], l[k][m], x);
+                l[a][k] = x * il[k];
+            }
+        }
+        // L values of the 4 columns for the rows / columns this thread holds (x D^-T = a);
+        // rows (warp-uniform) and column groups above the step are skipped
+        const int t0 = c0 + PI_W;
+        float lr[8][PI_W], lc[4][PI_W];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int r = tr + 16 * i;
+#pragma unroll
+            for (int k = 0; k < PI_W; ++k) lr[i][k] = 0.f;
+            if (r >= t0) {
+#pragma unroll
+                for (int k = 0; k < PI_W; ++k) {
+                    float x = col[k * PI_NB + r];
+#pragma unroll
+                    for (int m = 0; m < k; ++m) x = fmaf(-lr[i][m], l[k][m], x);
+                    lr[i][k] = x * il[k];
                 }
             }
-            if (lane < nb) {
+        }
 #pragma unroll
-                for (int c = 0; c < 32; ++c)
-                    if (c <= lane) sL[(kb + lane) * PI_LD + kb + c] = v[c];
-            }
-            __syncwarp();
-            // its inverse, lane = column: x_j = (delta_jc - sum_{l<j} D[j][l] x_l) / D[j][j]
-            float x[32];
+        for (int q = 0; q < 4; ++q) {
+            const int c = tc + 32 * q;
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                x[j] = 0.f;
-                if (j < nb) {
-                    const float* dj = sL + (kb + j) * PI_LD + kb;
-                    float acc = (j == lane) ? 1.f : 0.f;
+            for (int k = 0; k < PI_W; ++k) lc[q][k] = 0.f;
+            if (32 * q + 31 >= t0) {
 #pragma unroll
-                    for (int l = 0; l < j; ++l) acc = fmaf(-dj[l], x[l], acc);
-                    x[j] = (j >= lane) ? acc / dj[j] : 0.f;
+                for (int k = 0; k < PI_W; ++k) {
+                    float x = c >= t0 ? col[k * PI_NB + c] : 0.f;
+#pragma unroll
+                    for (int m = 0; m < k; ++m) x = fmaf(-lc[q][m], l[k][m], x);
+                    lc[q][k] = x * il[k];
                 }
             }
-            if (lane < nb) {
+        }
+        // rank-4 update of the trailing elements (zero L values elsewhere)
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (j < nb) sX[(kb + j) * PI_LD + kb + lane] = x[j];
+        for (int i = 0; i < 8; ++i) {
+            if (tr + 16 * i < t0) continue;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (32 * q + 31 < t0) continue;
+#pragma unroll
+                for (int k = 0; k < PI_W; ++k) v[i][q] = fmaf(-lr[i][k], lc[q][k], v[i][q]);
             }
         }
-        __syncthreads();
-        // sub-panel below: L[r][kb + c] = sum_{l <= c} A[r][kb + l] Dinv[c][l]; four threads per row
-        const int r0 = kb + nb;
-        float out[8];
-        const int rr = r0 + tid / 4, q8 = (tid % 4) * 8;
-        const bool act = tid / 4 < 128 && rr < n;
-        if (act) {
-            const float* ar = sL + rr * PI_LD + kb;
-            float a[32];
+        if (k_own >= 0 && k_own < PI_W) {   // the 4 columns are final
 #pragma unroll
-            for (int l = 0; l < 32; ++l) a[l] = l < nb ? ar[l] : 0.f;
+            for (int i = 0; i < 8; ++i) {
+                const int r = tr + 16 * i;
+                float x = 0.f;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const int c = q8 + k;
-                const float* di = sX + (kb + min(c, 31)) * PI_LD + kb;
-                float acc = 0.f;
+                for (int k = 0; k < PI_W; ++k) {
+                    if (k == k_own) x = r >= c0 + PI_W ? lr[i][k] : 0.f;
 #pragma unroll
-                for (int l = 0; l < 32; ++l)
-                    if (l <= c && c < nb) acc = fmaf(a[l], di[l], acc);
-                out[k] = acc;
+                    for (int a = k; a < PI_W; ++a)
+                        if (k == k_own && r == c0 + a) x = l[a][k];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q == qj && r >= c0) v[i][q] = x;
             }
         }
-        __syncthreads();
-        if (act) {
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (q8 + k < nb) sL[rr * PI_LD + kb + q8 + k] = out[k];
-        }
-        __syncthreads();
-        const int m2 = n - r0;
-        for (int e = tid; e < m2 * m2; e += PI_THREADS) {   // trailing lower triangle
-            const int r = r0 + e / m2, c = r0 + e % m2;
-            if (c > r) continue;
-            const float* lr = sL + r * PI_LD + kb;
-            const float* lc = sL + c * PI_LD + kb;
-            float acc = 0.f;
-            for (int l = 0; l < nb; ++l) acc = fmaf(lr[l], lc[l], acc);
-            sL[r * PI_LD + c] -= acc;
-        }
-        __syncthreads();
     }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = tr + 16 * i, c = tc + 32 * q;
+            sL[r * PI_LD + c] = (r >= c && r < n && c < n) ? v[i][q] : 0.f;
+        }
+    __syncthreads();
     for (int e = tid; e < n * n; e += PI_THREADS) {
         const int r = e % n, c = e / n;
         if (r >= c) A[r + (int64_t)c * lda] = sL[r * PI_LD + c];
     }
-    const int nblk = (n + 31) / 32;
-    // ---- inverse: off-diagonal sub-blocks, X_ij = -X_ii T, T = sum_{m in [32j, 32i)} L[32i + r][m] X[m][32j + c]
-    for (int dist = 1; dist < nblk; ++dist) {
-        const int nbp = nblk - dist;   // block pairs (i, j = i - dist), i = dist .. nblk-1
-        for (int e = tid; e < nbp * 1024; e += PI_THREADS) {
-            const int p = e / 1024, r = (e % 1024) / 32, c = e % 32;
-            const int i = dist + p, j = i - dist;
-            float acc = 0.f;
-            if (32 * i + r < n && 32 * j + c < n) {
-                const float* li = sL + (32 * i + r) * PI_LD;
-                for (int m = 32 * j; m < 32 * i; ++m) acc = fmaf(li[m], sX[m * PI_LD + 32 * j + c], acc);
-            }
-            sT[p * 32 * 33 + r * 33 + c] = acc;
-        }
-        __syncthreads();
-        for (int e = tid; e < nbp * 1024; e += PI_THREADS) {
-            const int p = e / 1024, r = (e % 1024) / 32, c = e % 32;
-            const int i = dist + p, j = i - dist;
-            if (32 * i + r < n && 32 * j + c < n) {
-                const float* xi = sX + (32 * i + r) * PI_LD + 32 * i;
-                float acc = 0.f;
-                for (int m = 0; m <= r; ++m) acc = fmaf(xi[m], sT[p * 32 * 33 + m * 33 + c], acc);
-                sX[(32 * i + r) * PI_LD + 32 * j + c] = -acc;
+    // ---- inverse: L X = I, right-looking over the rows of X, 4 rows per step
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[i][q] = (tr + 16 * i == tc + 32 * q && tc + 32 * q < n) ? 1.f : 0.f;
+    for (int r0 = 0; r0 < n; r0 += PI_W) {
+        float* row = buf + ((r0 / PI_W) & 1) * PI_W * PI_NB;   // row[k * 128 + c] = w[r0 + k][c]
+        const int ij = r0 >> 4, k_own = tr - (r0 & 15);
+        if (k_own >= 0 && k_own < PI_W) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float x = v[0][q];
+#pragma unroll
+                for (int i = 1; i < 8; ++i) x = (i == ij) ? v[i][q] : x;
+                row[k_own * PI_NB + tc + 32 * q] = x;
             }
         }
         __syncthreads();
+        // rows r0..r0+3 of X for the columns this thread holds: D x = w
+        float l[PI_W][PI_W];
+#pragma unroll
+        for (int a = 0; a < PI_W; ++a)
+#pragma unroll
+            for (int b = 0; b <= a; ++b)
+                l[a][b] = (r0 + a < n) ? sL[(r0 + a) * PI_LD + r0 + b] : (a == b ? 1.f : 0.f);
+        // X is lower triangular: column groups right of the step hold zeros (skipped)
+        float xr[4][PI_W];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int c = tc + 32 * q;
+#pragma unroll
+            for (int k = 0; k < PI_W; ++k) xr[q][k] = 0.f;
+            if (32 * q <= r0 + PI_W - 1) {
+#pragma unroll
+                for (int k = 0; k < PI_W; ++k) {
+                    float x = row[k * PI_NB + c];
+#pragma unroll
+                    for (int m = 0; m < k; ++m) x = fmaf(-l[k][m], xr[q][m], x);
+                    xr[q][k] = x / l[k][k];
+                }
+            }
+        }
+        if (k_own >= 0 && k_own < PI_W) {   // the 4 rows are final
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float x = xr[q][0];
+#pragma unroll
+                for (int k = 1; k < PI_W; ++k) x = (k == k_own) ? xr[q][k] : x;
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (i == ij) v[i][q] = x;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int r = tr + 16 * i;
+            if (r >= r0 + PI_W && r < n) {
+                float lk[PI_W];
+#pragma unroll
+                for (int k = 0; k < PI_W; ++k) lk[k] = sL[r * PI_LD + r0 + k];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (32 * q > r0 + PI_W - 1) continue;
+#pragma unroll
+                    for (int k = 0; k < PI_W; ++k) v[i][q] = fmaf(-lk[k], xr[q][k], v[i][q]);
+                }
+            }
+        }
     }
+    __syncthreads();
+    float* sX = sL;   // the factor is no longer needed: reuse its storage for X
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = tr + 16 * i, c = tc + 32 * q;
+            sX[r * PI_LD + c] = (r >= c && r < n && c < n) ? v[i][q] : 0.f;
+        }
+    __syncthreads();
     for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
         const int r = e % PI_NB, c = e / PI_NB;
-        const float v = sX[r * PI_LD + c];          // zero above the diagonal and beyond n
-        Linv[r + c * PI_NB] = v;                    // column-major
+        Linv[r + c * PI_NB] = sX[r * PI_LD + c];    // column-major
         const int rr = e / PI_NB, cc = e % PI_NB;   // K-major rows: B[rr][cc] = Linv[rr][cc]
         const float w = sX[rr * PI_LD + cc];
         const float h = __uint_as_float(__float_as_uint(w) & 0xFFFFE000u);
@@ -872,7 +943,7 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
                float* Bl, cudaStream_t s) {
     if (n <= 0 || n > PI_NB) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
     ProfScope prof_("potrf_inv", s);
-    const size_t sm = (2 * (size_t)PI_NB * PI_LD + 4 * 32 * 33) * sizeof(float);
+    const size_t sm = ((size_t)PI_NB * PI_LD + 2 * PI_W * PI_NB) * sizeof(float);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(potrf_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -936,3 +1007,49 @@ void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, f
 }
 
 }  // namespace omg
+
+// Test hook (not part of the public header): factor and invert one diagonal
+// block (device pointers).  With reps > 1 the call is then repeated on
+// scratch copies and the mean launch time (microseconds, CUDA events on the
+// default stream) is returned through *us.
+extern "C" int omg_internal_potrf_inv(int n, float* A, int64_t lda, float* Linv, float* Bh, float* Bl, int* err,
+                                      int reps, float* us) {
+    int64_t* col = nullptr;
+    float* scratch = nullptr;
+    int* err2 = nullptr;
+    int rc = 0;
+    try {
+        if (cudaMalloc(&col, sizeof(int64_t)) != cudaSuccess || cudaMalloc(&err2, sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&scratch, sizeof(float) * 4 * 128 * 128) != cudaSuccess)
+            throw omg::Error(OMG_ERR_NOMEM, "test hook allocation");
+        cudaMemset(err2, 0, sizeof(int));
+        if (reps > 1) {   // scratch copy of the input block first (the first call overwrites A)
+            cudaMemcpy2D(scratch, 128 * sizeof(float), A, lda * sizeof(float), n * sizeof(float), n,
+                         cudaMemcpyDeviceToDevice);
+        }
+        omg::potrf_inv(A, lda, n, err, col, 0, Linv, Bh, Bl, 0);
+        if (reps > 1) {
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            float* s1 = scratch + 128 * 128;
+            cudaEventRecord(e0, 0);
+            for (int r = 1; r < reps; ++r)   // same work on a scratch block (values no longer matter)
+                omg::potrf_inv(scratch, 128, n, err2, col, 0, s1, s1 + 128 * 128, s1 + 2 * 128 * 128, 0);
+            cudaEventRecord(e1, 0);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (us) *us = 1000.f * ms / (float)(reps - 1);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        rc = cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+    } catch (const omg::Error& e) {
+        rc = e.code;
+    }
+    cudaFree(col);
+    cudaFree(err2);
+    cudaFree(scratch);
+    return rc;
+}

@@ -115,12 +115,14 @@ struct DevGeom {
     int32_t* v2t_beg = nullptr;   // nv+1
     int32_t* v2t_tri = nullptr;
     int8_t* v2t_loc = nullptr;
+    double* v2t_q = nullptr;      // per vertex-triangle slot: curl of the P1 basis over the area, 3 doubles
 };
 
 // Device kernel launchers (assembly.cu / sources.cu / dense.cu).
 struct Workspace;
 
 void launch_prepare_triangles(const DevGeom& g, cudaStream_t s);
+void launch_prepare_vertex_curls(const DevGeom& g, cudaStream_t s);
 // S block: out(t1, t2) for t1 in [t1b,t1e), t2 in [t2b,t2e); `same` restricts to t2>=t1.
 //   mode 0: write coeff*S into HM lower triangle at internal positions (ld)
 //   mode 1: write S into tmp (n1 x n2 row-major, both halves when same)

@@ -23,6 +23,12 @@ struct omg_solver_s {
     DevBuf Linv32;                          // mixed: inverses of the 128 x 128 diagonal blocks
     std::vector<int64_t> w_off;             // offset (floats) of panel b's heads; remainders follow
     int64_t ld32 = 0;
+    // mixed: refinement residual on the tensor cores from fixed-point digits of
+    // the FP64 head matrix (nda planes of base-2^beta digits, row exponents);
+    // false: double-float residual on the CUDA cores from A64
+    bool tc_residual = true;
+    DevBuf Adig, rexp;
+    int nda = 7, ndx = 7, beta = 7, lmax = 8;
     bool persistent = false;                // outlives the call that made it (public solver handle)
     double refine_tol = 1e-6;               // stop when corrections are this small relative to x
     int max_refine = 10;

@@ -1,0 +1,416 @@
+// Refinement residual R = B - A X with FP64-level accuracy on the bf16 tensor
+// cores (sm_103a, tcgen05), by exact fixed-point slicing (the scheme of
+// Ozaki, Ogita, Oishi and Rump, Numer. Algorithms 59 (2012), in its
+// fixed-point form):
+//
+//   A_ij = 2^(e_i) sum_s 2^(-beta s) alpha_s,ij     (row scale e_i, integer digits |alpha| <= 2^beta)
+//   X_jc = 2^(f_c) sum_t 2^(-beta t) xi_t,jc        (column scale f_c)
+//   (A X)_ic = 2^(e_i + f_c) sum_{s,t} 2^(-beta (s+t)) (alpha_s xi_t)_ic
+//
+// Every digit is an integer of at most beta+1 bits, exact in bf16; each
+// product alpha_s xi_t is an integer GEMM.  The MMA accumulates in FP32, which
+// is exact while partial sums stay below 2^24: the K dimension is cut into
+// windows of KC = 256 (|partial sum| <= 256 * 2^(2 beta) = 2^22 for beta = 7),
+// each window is read out of TMEM, converted to int32 (exact) and summed in
+// registers; the digits of one level s+t are summed while the int32 bound
+// allows, then the level is scaled and subtracted from R in FP64.  Digit
+// pairs are kept up to level s+t <= LMAX; with beta = 7, 7 digits per operand
+// and LMAX = 8, truncated digits and dropped levels stay near 2^-48 of
+// n max|A_i.| max|X_.c| per entry, far under the refinement's needs (the head
+// matrix itself carries the mixed assembly's ~1e-8 error).
+//
+// Persistent and warp-specialized like the 3xTF32 GEMM: warp 0 streams
+// 128 x 64 bf16 tiles of the A digits and of the X digits (TMA, 128-byte
+// swizzle) through a four-stage ring, warp 1 issues
+// tcgen05.mma.cta_group::1.kind::f16 (M=128, N=128, K=16) into two TMEM
+// accumulators (one per window, alternating), warps 2-9 drain the windows.
+// Output tiles of one row block are adjacent in the walk, so the CTAs that
+// share a row block stream the same A digits at the same time (L2 reuse).
+// Every wait is bounded; on timeout the kernel records OMG_ERR_TIMEOUT, all
+// roles stop, copies and products in flight are waited for, TMEM is released.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "tcgen05.cuh"
+
+namespace omg {
+namespace tcr {
+
+using tc::fence_after;
+using tc::fence_before;
+
+constexpr int BM = 128, BN = 128, BK = 64;        // BK bf16 = 128 bytes per swizzled row
+constexpr int STAGES = 4;
+constexpr int TILE_BYTES = BM * BK * 2;           // 16 KiB
+constexpr int STAGE_BYTES = 2 * TILE_BYTES;       // A digits, X digits
+constexpr int SMEM_INT_BYTES = 64 * 256 * 4;      // per-thread spill of the level sums (64 columns x 256 threads)
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + SMEM_INT_BYTES + 1024;
+constexpr int THREADS = 320;
+constexpr int EPI_WARPS = 8;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr int KC = 256;                           // exact-accumulation window
+constexpr int CPW = KC / BK;                      // chunks per window
+constexpr int MAXPAIRS = 64;
+
+// Instruction descriptor: D=F32, A=B=BF16, both K-major, N=128, M=128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+struct PairPlan {
+    int n;                       // digit pairs, ordered by level s + t
+    int nwin;                    // windows per pair (K = nwin * KC, zero-padded)
+    uint64_t flush;              // bit p: subtract the level sum after pair p
+    uint8_t s[MAXPAIRS], t[MAXPAIRS];
+};
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    residual_slices_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tX,
+                           const __grid_constant__ PairPlan plan, int N, int k, int kpad, int beta,
+                           const int* __restrict__ rexp, const int* __restrict__ cexp, double* R, int64_t ldr,
+                           int64_t ntiles, int ncb, int* err) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
+    __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
+    __shared__ uint32_t tmem_holder;
+    __shared__ volatile int s_abort;
+    __shared__ int64_t s_issued, s_consumed;
+    const uint32_t sbase = (dev::smem_u32(smem_raw) + 1023u) & ~1023u;
+    int* const s_int = reinterpret_cast<int*>(smem_raw + (sbase - dev::smem_u32(smem_raw)) + STAGES * STAGE_BYTES);
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int units = plan.n * plan.nwin;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            dev::mbar_init(&full_bar[s], 1);
+            dev::mbar_init(&empty_bar[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            dev::mbar_init(&tfull_bar[a], 1);
+            dev::mbar_init(&tempty_bar[a], EPI_WARPS);
+        }
+        dev::mbar_init(&fin_bar, 1);
+        s_abort = 0;
+        s_issued = 0;
+        s_consumed = 0;
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         dev::smem_u32(&tmem_holder)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_holder;
+
+    if (warp == 0) {
+        if (lane == 0) {   // ---- TMA producer
+            int64_t g = 0;
+            for (int64_t t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
+                const int rb = (int)(t / ncb), cb = (int)(t % ncb);
+                for (int u = 0; u < units && !s_abort; ++u) {
+                    const int p = u / plan.nwin, w = u % plan.nwin;
+                    const int ya = (plan.s[p] - 1) * N + rb * BM, yx = (plan.t[p] - 1) * kpad + cb * BN;
+                    for (int c = 0; c < CPW; ++c, ++g) {
+                        const int slot = (int)(g % STAGES);
+                        if (!tc::wait_or_abort(&empty_bar[slot], (uint32_t)(((g / STAGES) & 1) ^ 1), &s_abort)) {
+                            s_abort = 1;
+                            break;
+                        }
+                        const uint32_t st = sbase + slot * STAGE_BYTES;
+                        const int x = (w * CPW + c) * BK;
+                        dev::mbar_expect_tx(&full_bar[slot], STAGE_BYTES);
+                        tc::tma_load_2d(st, &tA, x, ya, &full_bar[slot]);
+                        tc::tma_load_2d(st + TILE_BYTES, &tX, x, yx, &full_bar[slot]);
+                        s_issued = g + 1;
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // ---- MMA issuer
+            int64_t g = 0, lu = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                for (int u = 0; u < units && ok; ++u, ++lu) {
+                    const uint32_t ab = (uint32_t)(lu & 1), aph = (uint32_t)((lu >> 1) & 1);
+                    if (!tc::wait_or_abort(&tempty_bar[ab], aph ^ 1u, &s_abort)) {
+                        ok = false;
+                        break;
+                    }
+                    fence_after();
+                    const uint32_t acc = tmem + ab * BN;
+                    for (int c = 0; c < CPW; ++c, ++g) {
+                        const int slot = (int)(g % STAGES);
+                        if (!tc::wait_or_abort(&full_bar[slot], (uint32_t)((g / STAGES) & 1), &s_abort)) {
+                            ok = false;
+                            break;
+                        }
+                        s_consumed = g + 1;
+                        fence_after();
+                        const uint32_t st = sbase + slot * STAGE_BYTES;
+                        const uint64_t dA = tc::sdesc_sw128(st), dX = tc::sdesc_sw128(st + TILE_BYTES);
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; ++kk) {
+                            const uint64_t off = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes
+                            mma_bf16(acc, dA + off, dX + off, (c | kk) != 0 ? 1u : 0u);
+                        }
+                        tc::mma_commit(&empty_bar[slot]);
+                    }
+                    if (!ok) break;
+                    tc::mma_commit(&tfull_bar[ab]);   // the window's exact partial sums are ready
+                }
+            }
+            if (!ok) s_abort = 1;
+            tc::mma_commit(&fin_bar);
+            if (!dev::mbar_wait_bounded(&fin_bar, 0)) s_abort = 1;
+        }
+    } else {   // ---- epilogue: warp w owns TMEM lanes 32 * (w % 4) .. +31 and 64 of the 128 columns
+        const int q = warp & 3;
+        const int half = (warp - 2) / 4;
+        int64_t lu = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int rb = (int)(t / ncb), cb = (int)(t % ncb);
+            const int row = rb * BM + q * 32 + lane;
+            const int c0 = cb * BN + half * 64;
+            const int er = row < N ? rexp[row] : 0;
+            int iacc[64];
+#pragma unroll
+            for (int j = 0; j < 64; ++j) iacc[j] = 0;
+            bool stop = false;
+            for (int u = 0; u < units; ++u, ++lu) {
+                const uint32_t ab = (uint32_t)(lu & 1), aph = (uint32_t)((lu >> 1) & 1);
+                bool ok = tc::wait_or_abort(&tfull_bar[ab], aph, &s_abort);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) {
+                    if (lane == 0) s_abort = 1;
+                    stop = true;
+                    break;
+                }
+                fence_after();
+#pragma unroll
+                for (int chunk = 0; chunk < 2; ++chunk) {
+                    uint32_t r[32];
+                    tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64 + chunk * 32), r);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) iacc[chunk * 32 + j] += __float2int_rn(__uint_as_float(r[j]));
+                }
+                fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&tempty_bar[ab]);
+                const int p = u / plan.nwin, w = u % plan.nwin;
+                if (w == plan.nwin - 1 && ((plan.flush >> p) & 1ull)) {   // level sum -> R (FP64)
+                    // through shared memory so the (rare) FP64 pass does not hold 64 more registers
+                    int* si = s_int + (warp - 2) * 32 + lane;
+#pragma unroll
+                    for (int j = 0; j < 64; ++j) {
+                        si[j * (EPI_WARPS * 32)] = iacc[j];
+                        iacc[j] = 0;
+                    }
+                    const int lev = plan.s[p] + plan.t[p];
+                    if (row < N) {
+                        double* rp = R + row;
+                        for (int j = 0; j < 64; ++j) {
+                            const int col = c0 + j;
+                            const int v = si[j * (EPI_WARPS * 32)];
+                            if (col < k && v != 0)
+                                rp[(int64_t)col * ldr] -= scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
+                        }
+                    }
+                }
+            }
+            if (stop) break;
+        }
+    }
+    __syncthreads();
+    if (s_abort) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
+            for (int64_t g = s_consumed; g < s_issued; ++g)
+                dev::mbar_wait_bounded(&full_bar[g % STAGES], (uint32_t)((g / STAGES) & 1));
+        }
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// Digits of the columns of a column-major FP64 matrix: column c (rows j < n)
+// is scaled by 2^-e_c (e_c: exponent of its largest magnitude, frexp
+// convention), rounded to a multiple of 2^-(nd beta) and cut into `nd`
+// balanced base-2^beta digits (first |d| <= 2^beta, others <= 2^(beta-1)), written as bf16
+// row c of digit plane d: out[(d * rows_per_plane + c) * ldo + j], zero for
+// n <= j < ldo.  Columns c >= ncol (up to rows_per_plane) are zero.
+__global__ void digits_kernel(const double* __restrict__ M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta,
+                              int64_t rows_per_plane, int64_t ldo, __nv_bfloat16* out, int* ex) {
+    __shared__ double red[256];
+    __shared__ int s_e;
+    const int64_t c = blockIdx.x;
+    if (c >= ncol) {
+        for (int d = 0; d < nd; ++d)
+            for (int64_t j = threadIdx.x; j < ldo; j += blockDim.x)
+                out[((int64_t)d * rows_per_plane + c) * ldo + j] = __float2bfloat16_rn(0.f);
+        return;
+    }
+    const double* col = M + c * ldm;
+    double m = 0.0;
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, fabs(col[j]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int e = 0;
+        frexp(red[0], &e);   // max = f 2^e, f in [0.5, 1): every |entry| 2^-e < 1
+        s_e = e;
+        ex[c] = e;
+    }
+    __syncthreads();
+    const int e = s_e;
+    // one rounding to the digit grid 2^-(nd beta), then balanced base-2^beta digits
+    // by integer arithmetic (|Y| <= 2^(nd beta) <= 2^62)
+    const double grid = scalbn(1.0, nd * beta - e);
+    const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
+    for (int64_t j = threadIdx.x; j < ldo; j += blockDim.x) {
+        long long Y = j < n ? __double2ll_rn(col[j] * grid) : 0;
+        for (int d = nd - 1; d >= 1; --d) {
+            const long long r = ((Y + half) & mask) - half;
+            out[((int64_t)d * rows_per_plane + c) * ldo + j] = __float2bfloat16_rn((float)r);
+            Y = (Y - r) >> beta;
+        }
+        out[c * ldo + j] = __float2bfloat16_rn((float)Y);
+    }
+}
+
+}  // namespace tcr
+
+static inline void check_tcr(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw Error(OMG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    count_launch();
+}
+
+int64_t digits_ld(int64_t n) { return (n + 63) / 64 * 64; }
+
+void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta, int64_t rows_per_plane,
+                    int64_t ldo, void* out, int* ex, cudaStream_t s) {
+    if (rows_per_plane <= 0) return;
+    if (nd < 1 || nd * beta > 62 || beta < 2 || beta > 8) throw Error(OMG_ERR_INVALID, "digits: bad digit layout");
+    ProfScope prof_("digits", s);
+    tcr::digits_kernel<<<(unsigned)rows_per_plane, 256, 0, s>>>(M, n, ncol, ldm, nd, beta, rows_per_plane, ldo,
+                                                                static_cast<__nv_bfloat16*>(out), ex);
+    check_tcr("digits");
+}
+
+// R = B - A X.  A: n x n symmetric, given by its digits (nda planes of n rows,
+// row stride ld = digits_ld(n), row i = column i) and row exponents; X: n x k
+// by its digits (ndx planes of kpad rows) and column exponents.
+void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
+                     int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
+                     int64_t ldr, int* err, cudaStream_t s) {
+    if (n <= 0 || k <= 0) return;
+    if (n > (1 << 30) / 8 || kpad % tcr::BN) throw Error(OMG_ERR_INVALID, "residual digits: bad sizes");
+    ProfScope prof_("residual_tc", s);
+    const int64_t ld = digits_ld(n);
+    // plan: digit pairs by level, level sums flushed before they could leave int32
+    tcr::PairPlan plan{};
+    const double win_bound = (double)tcr::KC * std::ldexp(1.0, 2 * beta);
+    if (win_bound >= std::ldexp(1.0, 23)) throw Error(OMG_ERR_INVALID, "residual digits: window not exact");
+    auto amax = [&](int d) { return std::ldexp(1.0, d == 1 ? beta : beta - 1); };
+    std::vector<std::pair<int, int>> pairs;
+    for (int lev = 2; lev <= lmax; ++lev)
+        for (int a = std::max(1, lev - ndx); a <= std::min(nda, lev - 1); ++a) pairs.push_back({a, lev - a});
+    if ((int)pairs.size() > tcr::MAXPAIRS) throw Error(OMG_ERR_INVALID, "residual digits: too many digit pairs");
+    plan.n = (int)pairs.size();
+    const int64_t nchunk = (n + tcr::BK - 1) / tcr::BK;
+    plan.nwin = (int)((nchunk + tcr::CPW - 1) / tcr::CPW);
+    const double lim = std::ldexp(1.0, 31) * 0.9;
+    double run = 0.0;
+    for (int p = 0; p < plan.n; ++p) {
+        plan.s[p] = (uint8_t)pairs[p].first;
+        plan.t[p] = (uint8_t)pairs[p].second;
+        const double bound = (double)plan.nwin * tcr::KC * amax(pairs[p].first) * amax(pairs[p].second);
+        if (bound >= lim) throw Error(OMG_ERR_UNSUPPORTED, "residual digits: matrix too large for int32 sums");
+        run += bound;
+        const bool last = p + 1 == plan.n;
+        bool flush = last || pairs[p + 1].first + pairs[p + 1].second != pairs[p].first + pairs[p].second;
+        if (!flush) {
+            const double nb = (double)plan.nwin * tcr::KC * amax(pairs[p + 1].first) * amax(pairs[p + 1].second);
+            flush = run + nb >= lim;
+        }
+        if (flush) {
+            plan.flush |= 1ull << p;
+            run = 0.0;
+        }
+    }
+    OMG_CUDA(cudaMemcpy2DAsync(R, ldr * 8, B, ldb * 8, n * 8, k, cudaMemcpyDeviceToDevice, s));
+    const CUtensorMap mA = tc::make_map_2d(Ad, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)nda * n, ld, ld, tcr::BK,
+                                           tcr::BM);
+    const CUtensorMap mX = tc::make_map_2d(Xd, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)ndx * kpad, ld, ld,
+                                           tcr::BK, tcr::BN);
+    static bool attr = false;
+    static int n_sm = 0;
+    if (!attr) {
+        cudaFuncSetAttribute(tcr::residual_slices_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tcr::SMEM_BYTES);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (n_sm <= 0) n_sm = 1;
+        attr = true;
+    }
+    const int nrb = (int)((n + tcr::BM - 1) / tcr::BM), ncb = (int)((k + tcr::BN - 1) / tcr::BN);
+    const int64_t ntiles = (int64_t)nrb * ncb;
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
+    tcr::residual_slices_kernel<<<grid, tcr::THREADS, tcr::SMEM_BYTES, s>>>(mA, mX, plan, (int)n, (int)k, (int)kpad,
+                                                                            beta, rexp, cexp, R, ldr, ntiles, ncb,
+                                                                            err);
+    check_tcr("residual_tc");
+}
+
+}  // namespace omg
+
+// Test hook (not part of the public header): R = B - A X through the digits
+// and the tensor-core kernel, A symmetric n x n, X and B n x k (column-major,
+// device pointers), with the solver's parameters (7 digits of 7 bits, level <= 8).
+extern "C" int omg_internal_residual_tc(int64_t n, int64_t k, const double* A, const double* X, const double* B,
+                                        double* R, int* err) {
+    void* ad = nullptr;
+    void* xd = nullptr;
+    int* rexp = nullptr;
+    int* cexp = nullptr;
+    int rc = 0;
+    try {
+        const int nd = 7, beta = 7;
+        const int64_t ld = omg::digits_ld(n), kpad = (k + 127) / 128 * 128;
+        if (cudaMalloc(&ad, (size_t)nd * n * ld * 2) != cudaSuccess ||
+            cudaMalloc(&xd, (size_t)nd * kpad * ld * 2) != cudaSuccess ||
+            cudaMalloc(&rexp, (size_t)n * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&cexp, (size_t)kpad * sizeof(int)) != cudaSuccess)
+            throw omg::Error(OMG_ERR_NOMEM, "test hook allocation");
+        omg::digits_columns(A, n, n, n, nd, beta, n, ld, ad, rexp, 0);
+        omg::digits_columns(X, n, k, n, nd, beta, kpad, ld, xd, cexp, 0);
+        omg::residual_slices(n, k, ad, nd, rexp, xd, nd, kpad, cexp, beta, nd + 1, B, n, R, n, err, 0);
+        rc = cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+    } catch (const omg::Error& e) {
+        rc = e.code;
+    }
+    cudaFree(ad);
+    cudaFree(xd);
+    cudaFree(rexp);
+    cudaFree(cexp);
+    return rc;
+}

@@ -73,3 +73,79 @@ def test_tc_gemm_lower_update(cuda):
 def test_tc_gemm_many_tiles_per_cta(cuda, M, N, K, lower):
     # more tiles than SMs: every CTA walks several tiles through both TMEM accumulators
     assert _run(M, N, K, -1.0, 1.0, lower, True) < 1e-5
+
+
+def _lib_hook(name, argtypes):
+    from openmeeg_gb300 import _lib
+    f = getattr(_lib.load(), name)
+    f.restype = ctypes.c_int
+    f.argtypes = argtypes
+    return f
+
+
+def _residual_hook():
+    from openmeeg_gb300 import _lib
+    f = _lib.load().omg_internal_residual_tc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64, ctypes.c_int64] + [ctypes.c_void_p] * 5
+    return f
+
+
+@pytest.mark.parametrize("n,k", [(300, 7), (2500, 215), (4486, 130)])
+def test_tc_residual_is_fp64_accurate(cuda, n, k):
+    """R = B - A X from bf16 digits with exact windowed accumulation.  Digit
+    truncation (7 digits of 7 bits per row / column scale, levels <= 8) leaves
+    errors near 2^-48 of n times the row and column maxima: below 5e-13
+    normwise relative to |A||X| and 1e-10 elementwise even with entries spread
+    over 1e5 in a row; an inexact tensor-core sum would show up near 1e-7."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(n + k)
+    M = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+    # entries over several orders of magnitude, symmetric, strong diagonal
+    scale = torch.exp(torch.randn(n, device="cuda", dtype=torch.float64, generator=g) * 2)
+    A = (M + M.T) * scale[:, None] * scale[None, :] + torch.diag(scale ** 2 * n)
+    X = torch.randn(n, k, device="cuda", dtype=torch.float64, generator=g) * 10.0 ** torch.randint(
+        -3, 4, (1, k), device="cuda", generator=g)
+    B = A @ X + 1e-7 * torch.randn(n, k, device="cuda", dtype=torch.float64, generator=g) * (A.abs() @ X.abs())
+    Xc, Bc = X.T.contiguous(), B.T.contiguous()          # column-major n x k
+    Rc = torch.empty_like(Bc)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert _residual_hook()(n, k, p(A), p(Xc), p(Bc), p(Rc), p(err)) == 0 and int(err.item()) == 0
+    R = Rc.T
+    ref = B - A @ X
+    scale_ax = A.abs() @ X.abs()
+    elem = float(((R - ref).abs() / scale_ax).max())
+    norm = float(torch.linalg.norm(R - ref) / torch.linalg.norm(scale_ax))
+    assert elem < 1e-10 and norm < 5e-13, (elem, norm)
+
+
+def test_diagonal_block_cholesky_and_inverse(cuda):
+    """One CTA factors a 128 x 128 SPD block and inverts the factor:
+    L L^T = A and L Linv = I at FP32 level; the K-major split of Linv adds
+    back to Linv; a partial block (n = 77) leaves zero padding."""
+    import torch
+    f = _lib_hook("omg_internal_potrf_inv", [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_void_p])
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    for n in (128, 77):
+        g = torch.Generator(device="cuda").manual_seed(n)
+        M = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+        A64 = M @ M.T / n + torch.eye(n, device="cuda", dtype=torch.float64)
+        A = torch.zeros(140, 140, device="cuda", dtype=torch.float32)   # column-major, lda = 140
+        A[:n, :n] = A64.T.float()
+        Li = torch.zeros(128 * 128, device="cuda")
+        Bh = torch.zeros(128 * 128, device="cuda")
+        Bl = torch.zeros(128 * 128, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        us = ctypes.c_float(0)
+        assert f(n, p(A), 140, p(Li), p(Bh), p(Bl), p(err), 20, ctypes.byref(us)) == 0 and int(err.item()) == 0
+        print(f"potrf_inv n={n}: {us.value:.1f} us per launch")
+        L = torch.tril(A.T[:n, :n].double())            # row-major view of the factor
+        assert float(torch.linalg.norm(L @ L.T - A64) / torch.linalg.norm(A64)) < 1e-6
+        Linv = Li.view(128, 128).T.double()               # stored column-major
+        assert float(torch.linalg.norm(L @ Linv[:n, :n] - torch.eye(n, device="cuda", dtype=torch.float64))) < 1e-5
+        if n < 128:
+            assert float(Linv[n:, :].abs().max()) == 0.0 and float(Linv[:, n:].abs().max()) == 0.0
+        assert torch.equal((Bh + Bl).view(128, 128), Li.view(128, 128).T)
