@@ -23,7 +23,7 @@ void launch_prepare_triangles_order(const DevGeom& g, int order, cudaStream_t s)
 void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
                                  cudaStream_t s);
 void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
-                              const double* srec, double* out, cudaStream_t s);
+                              const double* srec, double* out, cudaStream_t s, bool screened = false);
 void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int maxb, const int* dnb,
                           const int* bmesh, const int* binside, const int* orient, int forced, int* dom, int* err,
                           cudaStream_t s);
@@ -96,7 +96,11 @@ void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const doub
 void ratio_max(int64_t n, const double* num, const double* den, double* out, cudaStream_t s);
 int64_t digits_ld(int64_t n);
 void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta, int64_t rows_per_plane,
-                    int64_t ldo, void* out, int* ex, cudaStream_t s);
+                    int64_t ldo, void* out, int* ex, cudaStream_t s,
+                    const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr);
+void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
+                int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double sgn, double* R,
+                int64_t ldr, int* err, cudaStream_t s, const char* prof_name);
 void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
                      int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
                      int64_t ldr, int* err, cudaStream_t s);
@@ -707,7 +711,8 @@ void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integ
         for (int64_t j = 0; j < nd; ++j) OMG_CUDA(cudaMemsetAsync(out + j * ldo, 0, (size_t)rows * 8, s));
     if (nd == 0) return;
     DevBuf sa((size_t)nd * g->h.nmesh * 8, s), dom((size_t)nd * sizeof(int), s);
-    launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s);
+    launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s,
+                             precision == OMG_PREC_MIXED);
     launch_domain_lookup(nd, g->h.nmesh, sa.as<double>(), g->ndom, g->maxb, g->dnb, g->bmesh, g->binside, g->orient,
                          domain, dom.as<int>(), ctx->d_err, s);
     if (allowed_domains) launch_domain_check(nd, dom.as<int>(), allowed_domains, ctx->d_err, s);
@@ -754,7 +759,32 @@ std::vector<std::pair<int64_t, int64_t>> gain_row_ranges(omg_geometry geo, const
 }
 
 void gain_contract(const std::vector<std::pair<int64_t, int64_t>>& merged, const double* Y, int64_t N, int64_t ne,
-                   int64_t nm, const double* DSM, int64_t nd, double* geeg, double* gmeg, cudaStream_t s) {
+                   int64_t nm, const double* DSM, int64_t nd, double* geeg, double* gmeg, cudaStream_t s,
+                   int precision, int* err) {
+    int64_t kdim = 0;
+    for (const auto& r : merged) kdim += r.second - r.first;
+    const int64_t k = ne + nm;
+    if (precision == OMG_PREC_MIXED && nd > 0 && k > 0 && kdim > 0 && merged.size() <= 8) {
+        // FP64-accurate contraction on the tensor cores from fixed-point digits of Y^T and DSM
+        // (7 digits of 7 bits each, levels <= 8), over the source rows only
+        const int nd7 = 7, beta = 7, lmax = 8;
+        const int64_t ld = digits_ld(kdim), ndpad = (nd + 127) / 128 * 128;
+        DevBuf Ad((size_t)nd7 * k * ld * 2, s), Xd((size_t)nd7 * ndpad * ld * 2, s);
+        DevBuf ex((size_t)(k + ndpad) * sizeof(int), s), G((size_t)k * nd * 8, s);
+        int* rexp = ex.as<int>();
+        int* cexp = rexp + k;
+        double* g = G.as<double>();
+        digits_columns(Y, kdim, k, N, nd7, beta, k, ld, Ad.p, rexp, s, &merged);
+        digits_columns(DSM, kdim, nd, N, nd7, beta, ndpad, ld, Xd.p, cexp, s, &merged);
+        OMG_CUDA(cudaMemsetAsync(g, 0, (size_t)k * nd * 8, s));
+        if (nm > 0)   // MEG rows start from DipSource2MEGMat
+            OMG_CUDA(cudaMemcpy2DAsync(g + ne, k * 8, gmeg, nm * 8, nm * 8, nd, cudaMemcpyDeviceToDevice, s));
+        digit_gemm(k, nd, kdim, Ad.p, nd7, rexp, Xd.p, nd7, ndpad, cexp, beta, lmax, g, k, 1.0, g, k, err, s,
+                   "gain_tc");
+        if (ne > 0) OMG_CUDA(cudaMemcpy2DAsync(geeg, ne * 8, g, k * 8, ne * 8, nd, cudaMemcpyDeviceToDevice, s));
+        if (nm > 0) OMG_CUDA(cudaMemcpy2DAsync(gmeg, nm * 8, g + ne, k * 8, nm * 8, nd, cudaMemcpyDeviceToDevice, s));
+        return;
+    }
     if (ne > 0 && nd > 0) {
         if (merged.empty()) OMG_CUDA(cudaMemsetAsync(geeg, 0, (size_t)ne * nd * 8, s));
         for (size_t q = 0; q < merged.size(); ++q) {
@@ -1240,7 +1270,8 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaEventRecord(ev[3], s));
     solver_solve_internal(sv.get(), B.as<double>(), N, k);
     // G = Y^T DSM over the rows where DSM can be nonzero (the source meshes' triangles and vertices)
-    gain_contract(gain_row_ranges(geo, src_meshes), B.as<double>(), N, ne, nm, DSM.as<double>(), nd, geeg, gmeg, s);
+    gain_contract(gain_row_ranges(geo, src_meshes), B.as<double>(), N, ne, nm, DSM.as<double>(), nd, geeg, gmeg, s,
+                  precision, ctx->d_err);
     OMG_CUDA(cudaEventRecord(ev[4], s));
     check_err(ctx, "gain");
     if (st) {

@@ -184,7 +184,7 @@ void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
         solve_mixed_fixed(sv.get(), B.as<double>(), N, k, m.refine_steps, m.est.as<double>());
     }
     gain_contract(m.rows, B.as<double>(), N, ne, nm, DSM.as<double>(), nd, m.geeg.as<double>(), m.gmeg.as<double>(),
-                  s);
+                  s, b->precision, c->d_err);
     if (planning) {
         check_err(c, "batched forward (planning run)");
         m.version = g->version;

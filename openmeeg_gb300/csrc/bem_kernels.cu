@@ -834,6 +834,61 @@ __global__ void mesh_solid_angles_kernel(const double* __restrict__ pts, int64_t
     }
 }
 
+// Same, screened in FP32 for the domain lookup of the mixed path: a closed
+// mesh subtends 0 or +-4 pi, so only the classification |sum| > 2 pi matters;
+// a sum within 1 of 2 pi (a point at the surface, where FP32 could tip the
+// test) is recomputed in FP64, so the domains are those of the FP64 sums.
+__global__ void mesh_solid_angles_screened_kernel(const double* __restrict__ pts, int64_t pstride, int nmesh,
+                                                  const int64_t* __restrict__ tbeg, const double* __restrict__ srec,
+                                                  double* out) {
+    __shared__ float redf[256];
+    __shared__ double red[256];
+    const int64_t i = blockIdx.x;
+    const d3 p = dev::ld3(pts + i * pstride);
+    for (int m = 0; m < nmesh; ++m) {
+        float acc = 0.f;
+        for (int64_t t = tbeg[m] + threadIdx.x; t < tbeg[m + 1]; t += blockDim.x) {
+            const double* s = srec + t * SREC;
+            const float ax = (float)(s[0] - p.x), ay = (float)(s[1] - p.y), az = (float)(s[2] - p.z);
+            const float bx = (float)(s[3] - p.x), by = (float)(s[4] - p.y), bz = (float)(s[5] - p.z);
+            const float cx = (float)(s[6] - p.x), cy = (float)(s[7] - p.y), cz = (float)(s[8] - p.z);
+            const float da = sqrtf(ax * ax + ay * ay + az * az), db = sqrtf(bx * bx + by * by + bz * bz),
+                        dc = sqrtf(cx * cx + cy * cy + cz * cz);
+            const float num = 2.f * (float)s[12] * (ax * (float)s[9] + ay * (float)s[10] + az * (float)s[11]);
+            const float den = da * db * dc + da * (bx * cx + by * cy + bz * cz) + db * (cx * ax + cy * ay + cz * az) +
+                              dc * (ax * bx + ay * by + az * bz);
+            acc += 2.f * atan2f(num, den);
+        }
+        redf[threadIdx.x] = acc;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) redf[threadIdx.x] += redf[threadIdx.x + w];
+            __syncthreads();
+        }
+        const float sum = redf[0];
+        __syncthreads();
+        if (fabsf(fabsf(sum) - 6.2831853f) > 1.f && sum == sum) {   // clear of the 2 pi boundary
+            if (threadIdx.x == 0) out[i * nmesh + m] = fabsf(sum) < 3.1415927f ? 0.0 : (sum > 0 ? 1.0 : -1.0) *
+                                                                                          12.566370614359172;
+            continue;
+        }
+        double accd = 0.0;   // near the surface: the FP64 sum of the reference formula
+        for (int64_t t = tbeg[m] + threadIdx.x; t < tbeg[m + 1]; t += blockDim.x) {
+            const double* s = srec + t * SREC;
+            const d3 r0 = dev::ld3(s) - p, r1 = dev::ld3(s + 3) - p, r2 = dev::ld3(s + 6) - p;
+            accd += dev::solid_angle(r0, r1, r2, dev::norm(r0), dev::norm(r1), dev::norm(r2), dev::ld3(s + 9), s[12]);
+        }
+        red[threadIdx.x] = accd;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[i * nmesh + m] = red[0];
+        __syncthreads();
+    }
+}
+
 // Geometry::domain(point) (geometry.cpp:146-154, domain.cpp:12-17): the first
 // domain all of whose boundaries agree with the point's inside/outside state.
 __global__ void domain_lookup_kernel(int64_t n, int nmesh, const double* __restrict__ sa, int ndom, int maxb,
@@ -1299,10 +1354,13 @@ __global__ void ds2mm_kernel(const double* __restrict__ dip, int64_t nd, const d
 }
 
 void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
-                              const double* srec, double* out, cudaStream_t s) {
+                              const double* srec, double* out, cudaStream_t s, bool screened) {
     if (n == 0) return;
     ProfScope prof_("solid_angles", s);
-    mesh_solid_angles_kernel<<<(unsigned)n, 256, 0, s>>>(pts, pstride, nmesh, tbeg_dev, srec, out);
+    if (screened)
+        mesh_solid_angles_screened_kernel<<<(unsigned)n, 256, 0, s>>>(pts, pstride, nmesh, tbeg_dev, srec, out);
+    else
+        mesh_solid_angles_kernel<<<(unsigned)n, 256, 0, s>>>(pts, pstride, nmesh, tbeg_dev, srec, out);
     check_launch("mesh solid angles");
 }
 

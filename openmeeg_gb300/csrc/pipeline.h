@@ -88,6 +88,8 @@ void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integ
 // the given source meshes' domains can be nonzero.
 std::vector<std::pair<int64_t, int64_t>> gain_row_ranges(omg_geometry geo, const std::vector<int>& src_meshes);
 // G = Y^T DSM restricted to `rows`: EEG rows of Y first (ne), then MEG (nm,
-// accumulated onto gmeg, which already holds DipSource2MEGMat).
+// accumulated onto gmeg, which already holds DipSource2MEGMat).  FP64: CUDA-core
+// FP64 GEMM; mixed: FP64-accurate digit GEMM on the tensor cores.
 void gain_contract(const std::vector<std::pair<int64_t, int64_t>>& rows, const double* Y, int64_t N, int64_t ne,
-                   int64_t nm, const double* DSM, int64_t nd, double* geeg, double* gmeg, cudaStream_t s);
+                   int64_t nm, const double* DSM, int64_t nd, double* geeg, double* gmeg, cudaStream_t s,
+                   int precision, int* err);

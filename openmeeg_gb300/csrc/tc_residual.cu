@@ -53,6 +53,13 @@ constexpr uint32_t TMEM_COLS = 256;
 constexpr int KC = 256;                           // exact-accumulation window
 constexpr int CPW = KC / BK;                      // chunks per window
 constexpr int MAXPAIRS = 64;
+constexpr int MAXRANGES = 8;
+
+// Rows [beg[q], beg[q] + len[q]) concatenated (n == 0: all rows in order).
+struct RowRanges {
+    int n;
+    int64_t beg[MAXRANGES], len[MAXRANGES];
+};
 
 // Instruction descriptor: D=F32, A=B=BF16, both K-major, N=128, M=128.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -75,8 +82,8 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, 
 __global__ void __launch_bounds__(THREADS, 1)
     residual_slices_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tX,
                            const __grid_constant__ PairPlan plan, int N, int k, int kpad, int beta,
-                           const int* __restrict__ rexp, const int* __restrict__ cexp, double* R, int64_t ldr,
-                           int64_t ntiles, int ncb, int* err) {
+                           const int* __restrict__ rexp, const int* __restrict__ cexp, double sgn, double* R,
+                           int64_t ldr, int64_t ntiles, int ncb, int* err) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -224,7 +231,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             const int col = c0 + j;
                             const int v = si[j * (EPI_WARPS * 32)];
                             if (col < k && v != 0)
-                                rp[(int64_t)col * ldr] -= scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
+                                rp[(int64_t)col * ldr] += sgn * scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
                         }
                     }
                 }
@@ -254,7 +261,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // row c of digit plane d: out[(d * rows_per_plane + c) * ldo + j], zero for
 // n <= j < ldo.  Columns c >= ncol (up to rows_per_plane) are zero.
 __global__ void digits_kernel(const double* __restrict__ M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta,
-                              int64_t rows_per_plane, int64_t ldo, __nv_bfloat16* out, int* ex) {
+                              int64_t rows_per_plane, int64_t ldo, __nv_bfloat16* out, int* ex,
+                              const __grid_constant__ RowRanges rr) {
     __shared__ double red[256];
     __shared__ int s_e;
     const int64_t c = blockIdx.x;
@@ -265,8 +273,17 @@ __global__ void digits_kernel(const double* __restrict__ M, int64_t n, int64_t n
         return;
     }
     const double* col = M + c * ldm;
+    // entry j of the digit row: row j of the column, or the j-th row of the ranges
+    auto at = [&](int64_t j) -> double {
+        if (rr.n == 0) return col[j];
+        for (int q = 0; q < rr.n; ++q) {
+            if (j < rr.len[q]) return col[rr.beg[q] + j];
+            j -= rr.len[q];
+        }
+        return 0.0;
+    };
     double m = 0.0;
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, fabs(col[j]));
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, fabs(at(j)));
     red[threadIdx.x] = m;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
@@ -286,7 +303,7 @@ __global__ void digits_kernel(const double* __restrict__ M, int64_t n, int64_t n
     const double grid = scalbn(1.0, nd * beta - e);
     const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
     for (int64_t j = threadIdx.x; j < ldo; j += blockDim.x) {
-        long long Y = j < n ? __double2ll_rn(col[j] * grid) : 0;
+        long long Y = j < n ? __double2ll_rn(at(j) * grid) : 0;
         for (int d = nd - 1; d >= 1; --d) {
             const long long r = ((Y + half) & mask) - half;
             out[((int64_t)d * rows_per_plane + c) * ldo + j] = __float2bfloat16_rn((float)r);
@@ -307,36 +324,49 @@ static inline void check_tcr(const char* what) {
 int64_t digits_ld(int64_t n) { return (n + 63) / 64 * 64; }
 
 void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta, int64_t rows_per_plane,
-                    int64_t ldo, void* out, int* ex, cudaStream_t s) {
+                    int64_t ldo, void* out, int* ex, cudaStream_t s,
+                    const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr) {
     if (rows_per_plane <= 0) return;
     if (nd < 1 || nd * beta > 62 || beta < 2 || beta > 8) throw Error(OMG_ERR_INVALID, "digits: bad digit layout");
     ProfScope prof_("digits", s);
+    tcr::RowRanges rr{};
+    if (ranges) {
+        if (ranges->size() > (size_t)tcr::MAXRANGES) throw Error(OMG_ERR_INVALID, "digits: too many row ranges");
+        int64_t tot = 0;
+        for (const auto& r : *ranges) {
+            rr.beg[rr.n] = r.first;
+            rr.len[rr.n] = r.second - r.first;
+            tot += rr.len[rr.n++];
+        }
+        if (tot != n) throw Error(OMG_ERR_INVALID, "digits: row ranges do not add up");
+    }
     tcr::digits_kernel<<<(unsigned)rows_per_plane, 256, 0, s>>>(M, n, ncol, ldm, nd, beta, rows_per_plane, ldo,
-                                                                static_cast<__nv_bfloat16*>(out), ex);
+                                                                static_cast<__nv_bfloat16*>(out), ex, rr);
     check_tcr("digits");
 }
 
-// R = B - A X.  A: n x n symmetric, given by its digits (nda planes of n rows,
-// row stride ld = digits_ld(n), row i = column i) and row exponents; X: n x k
-// by its digits (ndx planes of kpad rows) and column exponents.
-void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
-                     int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
-                     int64_t ldr, int* err, cudaStream_t s) {
+// R = B + sgn A X^T over a contraction of length kdim, both operands by their
+// digit rows: A (n x kdim) as nda planes of n rows, X (k x kdim) as ndx planes
+// of kpad rows, row stride ld = digits_ld(kdim), with row exponents rexp (A)
+// and cexp (X).  R and B are n x k, column-major.
+void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
+                int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double sgn, double* R,
+                int64_t ldr, int* err, cudaStream_t s, const char* prof_name) {
     if (n <= 0 || k <= 0) return;
-    if (n > (1 << 30) / 8 || kpad % tcr::BN) throw Error(OMG_ERR_INVALID, "residual digits: bad sizes");
-    ProfScope prof_("residual_tc", s);
-    const int64_t ld = digits_ld(n);
+    if (n > (1 << 30) / 8 || kdim <= 0 || kpad % tcr::BN) throw Error(OMG_ERR_INVALID, "digit GEMM: bad sizes");
+    ProfScope prof_(prof_name, s);
+    const int64_t ld = digits_ld(kdim);
     // plan: digit pairs by level, level sums flushed before they could leave int32
     tcr::PairPlan plan{};
     const double win_bound = (double)tcr::KC * std::ldexp(1.0, 2 * beta);
-    if (win_bound >= std::ldexp(1.0, 23)) throw Error(OMG_ERR_INVALID, "residual digits: window not exact");
+    if (win_bound >= std::ldexp(1.0, 23)) throw Error(OMG_ERR_INVALID, "digit GEMM: window not exact");
     auto amax = [&](int d) { return std::ldexp(1.0, d == 1 ? beta : beta - 1); };
     std::vector<std::pair<int, int>> pairs;
     for (int lev = 2; lev <= lmax; ++lev)
         for (int a = std::max(1, lev - ndx); a <= std::min(nda, lev - 1); ++a) pairs.push_back({a, lev - a});
-    if ((int)pairs.size() > tcr::MAXPAIRS) throw Error(OMG_ERR_INVALID, "residual digits: too many digit pairs");
+    if ((int)pairs.size() > tcr::MAXPAIRS) throw Error(OMG_ERR_INVALID, "digit GEMM: too many digit pairs");
     plan.n = (int)pairs.size();
-    const int64_t nchunk = (n + tcr::BK - 1) / tcr::BK;
+    const int64_t nchunk = (kdim + tcr::BK - 1) / tcr::BK;
     plan.nwin = (int)((nchunk + tcr::CPW - 1) / tcr::CPW);
     const double lim = std::ldexp(1.0, 31) * 0.9;
     double run = 0.0;
@@ -357,7 +387,10 @@ void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* r
             run = 0.0;
         }
     }
-    OMG_CUDA(cudaMemcpy2DAsync(R, ldr * 8, B, ldb * 8, n * 8, k, cudaMemcpyDeviceToDevice, s));
+    if (!B)
+        OMG_CUDA(cudaMemset2DAsync(R, ldr * 8, 0, n * 8, k, s));
+    else if (B != R)
+        OMG_CUDA(cudaMemcpy2DAsync(R, ldr * 8, B, ldb * 8, n * 8, k, cudaMemcpyDeviceToDevice, s));
     const CUtensorMap mA = tc::make_map_2d(Ad, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)nda * n, ld, ld, tcr::BK,
                                            tcr::BM);
     const CUtensorMap mX = tc::make_map_2d(Xd, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)ndx * kpad, ld, ld,
@@ -376,9 +409,16 @@ void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* r
     const int64_t ntiles = (int64_t)nrb * ncb;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
     tcr::residual_slices_kernel<<<grid, tcr::THREADS, tcr::SMEM_BYTES, s>>>(mA, mX, plan, (int)n, (int)k, (int)kpad,
-                                                                            beta, rexp, cexp, R, ldr, ntiles, ncb,
-                                                                            err);
-    check_tcr("residual_tc");
+                                                                            beta, rexp, cexp, sgn, R, ldr, ntiles,
+                                                                            ncb, err);
+    check_tcr(prof_name);
+}
+
+// R = B - A X, A symmetric n x n (its digit rows are its digit columns).
+void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
+                     int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
+                     int64_t ldr, int* err, cudaStream_t s) {
+    digit_gemm(n, k, n, Ad, nda, rexp, Xd, ndx, kpad, cexp, beta, lmax, B, ldb, -1.0, R, ldr, err, s, "residual_tc");
 }
 
 }  // namespace omg
