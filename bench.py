@@ -188,9 +188,9 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
       residual_df64 -- R = B - A X in double-float arithmetic: reads the float-pair
         head matrix (8 N^2 bytes), X pairs (8 N k), B (8 N k), writes R (8 N k);
         N^2 k multiply-adds at 12 FP32 operations each (exact product + TwoSum).
-      gemm_tf32x3 -- tcgen05 3xTF32 updates of the factorization and the solves:
-        N^3/3 flops (LDL^T trailing updates) + 2 N^2 k per solve, solves =
-        refinement steps + 1; executed tensor flops are 3x (hi*hi, hi*lo, lo*hi).
+      gemm_syrk -- tcgen05 3xTF32 trailing updates of the FP32 LDL^T: N^3/3
+        algorithmic flops per factorization; executed tensor flops are 3x
+        (hi*hi, hi*lo, lo*hi), against the TF32 dense rate (half of bf16).
     """
     if launches == 0:
         return None
@@ -222,17 +222,46 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
                      "fp32_issue_frac_of_nominal": fp32_ops / t_launch / FP32_ISSUE_NOMINAL,
                      "note": f"HBM fraction of {kind} copy bandwidth; the kernel is FP32-issue bound "
                              f"(12 FP32 ops per multiply-add), see fp32_issue_frac_of_nominal"})
-    elif name == "gemm_tf32x3":
-        solves = int(stats.get("refinement_steps", 1)) + 1
-        flops = (N ** 3 / 3.0 + solves * 2.0 * N * N * k) / per_step
+    elif name == "gemm_syrk":
+        # trailing updates of the FP32 LDL^T on the tensor cores: sum over panels of
+        # 2 (N - k1)^2 / 2 * 128 = ~N^3/3 algorithmic flops per factorization (lower triangle only);
+        # executed TF32 tensor flops are 3x (hi*hi, hi*lo, lo*hi)
+        flops = (N ** 3 / 3.0) / per_step
         achieved = flops / t_launch / 1e12
-        info.update({"bound": "tensor", "achieved": achieved, "peak": bf16_sus, "unit": "TFLOP/s",
-                     "frac": achieved / bf16_sus, "traffic": None, "executed_tf32_tflops": 3 * achieved,
-                     "note": f"algorithmic FP32-equivalent flops vs {kind} bf16 sustained peak (TF32 runs at half "
-                             f"the bf16 rate; 3 TF32 products per FP32-accurate product)"})
+        tf32_peak = bf16 / 2.0
+        info.update({"bound": "tensor", "achieved": 3 * achieved, "peak": tf32_peak, "unit": "TFLOP/s",
+                     "frac": 3 * achieved / tf32_peak, "traffic": None, "algorithmic_fp32_tflops": achieved,
+                     "note": f"executed TF32 tensor flops (3 per FP32-accurate product) vs half the {kind} bf16 "
+                             f"burst peak (the TF32 dense rate is half the bf16 rate)"})
+    elif name == "ff_block":
+        # far-field FP32 Gauss products: 16 x 16 point pairs per triangle pair, S and D from the same
+        # 256 distances (~20 FP32 operations each: 3 differences, 3 FMA, rsqrt, 3 kernels, 3 accumulations)
+        pairs = stats.get("_tri_pairs", 0)
+        ops = 20.0 * 256 * pairs / per_step
+        achieved = ops / t_launch
+        info.update({"bound": "fp32", "achieved": achieved / 1e12, "peak": FP32_ISSUE_NOMINAL / 1e12,
+                     "unit": "T FP32 op/s", "frac": achieved / FP32_ISSUE_NOMINAL, "traffic": None,
+                     "note": "FP32-pipe bound (rsqrt + FMA); peak is the nominal FP32 issue rate, not a measured one"})
+    elif name in ("potrf_inv", "apply_inv"):
+        info.update({"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
+                     "note": "one diagonal block per launch (128 x 128, one CTA), sequential over the blocks: "
+                             "latency bound, no bandwidth or tensor roofline applies"})
     else:
         info.update({"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None})
     return info
+
+
+def tri_pairs(head):
+    """Triangle pairs the head matrix integrates (S for non-barrier pairs, D and D* both ways): the pair
+    loop of the symmetric BEM over nested meshes (self pairs and adjacent pairs)."""
+    T = [t.shape[0] for t in head.triangles]
+    L = len(T)
+    pairs = 0
+    for m in range(L):
+        pairs += T[m] * (T[m] + 1) // 2                 # self pair (upper triangle)
+        if m > 0:
+            pairs += T[m] * T[m - 1]                     # adjacent pair
+    return pairs
 
 
 def run_gpu(args):
@@ -338,9 +367,11 @@ def run_gpu(args):
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
     dname, (dl, dms) = dom
     total_prof_ms = sum(v[1] for v in prof.values())
-    roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx, pk)
-    others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx, pk)
-              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_tf32x3") and n != dname}
+    stx_r = dict(stx)
+    stx_r["_tri_pairs"] = tri_pairs(w.head)
+    roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx_r, pk)
+    others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx_r, pk)
+              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block") and n != dname}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -81,7 +81,8 @@ void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, i
 // tc_gemm.cu
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
-                 int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s);
+                 int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
+                 const char* prof_name = "gemm_tf32x3");
 void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
@@ -475,12 +476,12 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
             float* Tl = Th + m * nb;
             split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
             gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
-                        sv->ctx->d_err, s);
+                        sv->ctx->d_err, s, "gemm_panel");
             float* Wh = sv->W.as<float>() + sv->w_off[b];
             float* Wl = Wh + m * nb;
             split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Wh, Wl, s);
             gemm_tf32x3(m, m, nk, -1.f, Wh, Wl, nb, nb, 0, Wh, Wl, nb, nb, 0, 1.f, A + k1 + k1 * ld, ld, true,
-                        sv->ctx->d_err, s);
+                        sv->ctx->d_err, s, "gemm_syrk");
         }
     }
     sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
@@ -504,7 +505,7 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
         if (m > 0) {
             const float* Wh = sv->W.as<float>() + sv->w_off[b];
             gemm_tf32x3(m, nrhs, nk, -1.f, Wh, Wh + m * nb, nb, nb, 0, Xh, Xl, nb, nb, 0, 1.f, B + k1, ldb, false,
-                        sv->ctx->d_err, s);
+                        sv->ctx->d_err, s, "gemm_solve");
         }
     }
     negate_rows<float>(B, ldb, sv->nP, N, nrhs, s);
@@ -513,7 +514,7 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
         apply_inv_split((int)nk, nb, nrhs, sv->Linv32.as<float>() + bb * nb * nb, true, B + k0, ldb, Xh, Xl, s);
         if (k0 > 0) {
             gemm_tf32x3(k0, nrhs, nk, -1.f, A, Ar, ld, N, k0, Xh, Xl, nb, nb, 0, 1.f, B, ldb, false, sv->ctx->d_err,
-                        s);
+                        s, "gemm_solve");
         }
     }
 }

@@ -247,10 +247,11 @@ static inline void check_tc(const char* what) {
 // (may be null when nprod == 1).  `k0` offsets the K coordinate of A and B.
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
-                 int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s) {
+                 int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
+                 const char* prof_name) {
     if (M <= 0 || N <= 0) return;
     if (K <= 0) throw Error(OMG_ERR_INVALID, "empty K");
-    ProfScope prof_("gemm_tf32x3", s);
+    ProfScope prof_(prof_name, s);
     const int nprod = (Al && Bl) ? 3 : 1;
     // Operands are offset along K by moving the base pointer (k0 multiple of 4 keeps 16-byte alignment).
     if ((a_k0 % 4) || (b_k0 % 4)) throw Error(OMG_ERR_INVALID, "tensor-core K offset not 16-byte aligned");
@@ -374,7 +375,8 @@ extern "C" int omg_internal_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float a
                                         const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb,
                                         float beta, float* C, int64_t ldc, int lower, int* err) {
     try {
-        omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, lower != 0, err, 0);
+        omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, lower != 0, err, 0,
+                         "gemm_tf32x3");
         cudaError_t e = cudaDeviceSynchronize();
         return e == cudaSuccess ? 0 : -2;
     } catch (const omg::Error& e) {
