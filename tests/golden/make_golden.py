@@ -13,6 +13,11 @@ files) for a seeded workload of openmeeg_gb300.workloads:
   config0            EEG/MEG adjoint gains of config0 (ico3, N=4486), 200 dipoles
   config1_200        (--big) EEG/MEG adjoint gains of config1 (ico4, N=17926) for
                      its first 200 dipoles
+  head3_analytic     the reference's sample head Head3 (meshes, domains, dipoles,
+                     128 electrodes, 162 magnetometers) with the analytic EEG and
+                     MEG values its test suite compares against
+                     (tests/analytic/eeg_head3_analytic.txt, meg_analytic.txt);
+                     `--analytic-only` writes just this fixture
 """
 from __future__ import annotations
 
@@ -43,7 +48,35 @@ def save(name, w, R, keep_hm=False):
     print(name, {k: (v.shape if hasattr(v, "shape") else v) for k, v in d.items()}, R["times"])
 
 
+def save_head3_analytic():
+    R = os.environ.get("OMG_REFERENCE_DIR", "/root/reference")
+    d3 = os.path.join(R, "data", "Head3")
+    meshes, domains = io.read_geom(os.path.join(d3, "Head3.geom"))
+    cond = io.read_cond(os.path.join(d3, "Head3.cond"))
+    V, T = [], []
+    for m in meshes:
+        v, t = io.read_tri(m)
+        V.append(v)
+        T.append(t)
+    names = [d[0] for d in domains]
+    d = {"nverts": np.array([v.shape[0] for v in V]), "ntris": np.array([t.shape[0] for t in T]),
+         "vertices": np.vstack(V), "triangles": np.vstack(T),
+         "dom_nb": np.array([len(dm[1]) for dm in domains]),
+         "dom_bounds": np.array([b for dm in domains for b in dm[1]]),
+         "dom_sigma": np.array([cond[n] for n in names]), "dom_names": np.array(names),
+         "dipoles": np.loadtxt(os.path.join(d3, "Head3.dip")),
+         "electrodes": np.loadtxt(os.path.join(d3, "Head3.patches")),
+         "squids": np.loadtxt(os.path.join(d3, "Head3.squids"), usecols=range(1, 8)),
+         "eeg_analytic": np.loadtxt(os.path.join(R, "tests", "analytic", "eeg_head3_analytic.txt")),
+         "meg_analytic": np.loadtxt(os.path.join(R, "tests", "analytic", "meg_analytic.txt"))}
+    np.savez_compressed(os.path.join(OUT, "head3_analytic.npz"), **d)
+    print("head3_analytic", {k: v.shape for k, v in d.items()})
+
+
 def main():
+    save_head3_analytic()
+    if "--analytic-only" in sys.argv:
+        return
     if not ref_runner.available():
         ref_runner.build()
     big = "--big" in sys.argv

@@ -130,3 +130,36 @@ def test_library_fails_loudly_without_gpu():
     rc = lib.omg_context_create(0, ctypes.byref(h))
     assert rc != 0
     assert lib.omg_last_error()
+
+
+def test_analytic_sphere_series_pinned_to_reference_values():
+    """The nested-sphere EEG series and Sarvas's MEG formula reproduce the
+    analytic values the reference's test suite ships for its sample head
+    Head3 (radii .87/.92/1, conductivities 1/.0125/1, 6 dipoles, 128
+    electrodes, 162 magnetometers).  The MEG file holds 8 significant digits;
+    dipole 6 is radial (zero field) and is checked in absolute terms."""
+    from oracle import analytic as an
+    d = golden("head3_analytic")
+    V = an.eeg_sphere([0.87, 0.92, 1.0], [1.0, 0.0125, 1.0], d["dipoles"], d["electrodes"])
+    assert an.rdm(V, d["eeg_analytic"]).max() < 1e-12
+    assert an.mag(V, d["eeg_analytic"]).max() < 1e-12
+    B = an.sarvas(d["dipoles"], d["squids"][:, :6])
+    assert an.rdm(B[:, :5], d["meg_analytic"][:, :5]).max() < 1e-6
+    assert an.mag(B[:, :5], d["meg_analytic"][:, :5]).max() < 1e-6
+    assert np.abs(B[:, 5]).max() < 1e-12 * np.abs(B[:, :5]).max()
+
+
+def test_analytic_series_single_layer_limit():
+    """Three layers of equal conductivity are one homogeneous sphere: the
+    series then equals the closed form of a dipole in a sphere, checked here
+    against a four-layer split of the same sphere."""
+    from oracle import analytic as an
+    rng = np.random.default_rng(5)
+    dip = np.hstack([rng.uniform(-0.4, 0.4, (4, 3)), rng.standard_normal((4, 3))])
+    el = rng.standard_normal((20, 3))
+    el /= np.linalg.norm(el, axis=1, keepdims=True)
+    V3 = an.eeg_sphere([0.8, 0.9, 1.0], [0.7, 0.7, 0.7], dip, el)
+    V4 = an.eeg_sphere([0.6, 0.85, 0.95, 1.0], [0.7, 0.7, 0.7, 0.7], dip, el)
+    V1 = an.eeg_sphere([1.0], [0.7], dip, el)
+    assert np.abs(V3 - V1).max() < 1e-12 * np.abs(V1).max()
+    assert np.abs(V4 - V1).max() < 1e-12 * np.abs(V1).max()
