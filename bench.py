@@ -54,7 +54,7 @@ def peaks():
 class Clocks:
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_power_cap,memory.used")
 
     def __init__(self, device: int):
         self.device = device
@@ -77,7 +77,7 @@ class Clocks:
         except Exception:
             self.proc.kill()
             out = ""
-        sm, mx, reasons = [], [], set()
+        sm, mx, reasons, mem = [], [], set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in out.splitlines():
             f = [x.strip() for x in ln.split(",")]
@@ -86,13 +86,16 @@ class Clocks:
             try:
                 sm.append(float(f[1]))
                 mx.append(float(f[2]))
+                if len(f) > 9:
+                    mem.append(float(f[9]))
             except ValueError:
                 continue
             for n, v in zip(names, f[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "memory_used_max_mib": max(mem) if mem else None}
 
 
 # ---------------------------------------------------------------------------
@@ -513,6 +516,67 @@ def run_batch(args):
     return 0
 
 
+def run_large(args):
+    """config4: 4 layers ico5 (N = 102408), 10000 dipoles, 256 EEG + 306 MEG.  One FP64 drop-in and one
+    mixed-precision time-to-gain on the same GPU, the memory each needed, the mixed result's error against
+    the FP64 one, and both against the analytic nested-sphere series (EEG) and Sarvas's formula (MEG) on a
+    sample of the dipoles."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    __import__("__graft_entry__").build()
+    from oracle import analytic as an
+    from openmeeg_gb300 import api, workloads
+    w = workloads.config4()
+    ctx = api.Context(local)
+    geo = api.Geometry.from_head(w.head, ctx)
+    N = geo.size
+    dev = torch.device("cuda", local)
+    dip = torch.as_tensor(w.dipoles, dtype=torch.float64, device=dev)
+    el = torch.as_tensor(w.electrodes, dtype=torch.float64, device=dev)
+    sq = torch.as_tensor(w.squids, dtype=torch.float64, device=dev)
+    out, res = {}, {}
+    for prec in args.large_precisions.split(","):
+        clocks = Clocks(local)
+        clocks.start()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ge, gm, st = api.forward_gain(geo, dip, el, sq, precision=prec)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        ck = clocks.stop()
+        out[prec] = (ge.cpu().numpy(), gm.cpu().numpy())
+        del ge, gm
+        res[prec] = {"time_to_gain_s": t, "stats": {k: (round(v, 3) if isinstance(v, float) else v)
+                                                    for k, v in st.items()},
+                     "library_peak_bytes": int(st["device_bytes"]), "clocks": ck}
+    ns = min(args.analytic_dipoles, w.dipoles.shape[0])
+    radii = [float(np.linalg.norm(v, axis=1).mean()) for v in w.head.vertices]
+    sig = [d[2] for d in w.head.domains if d[2] > 0]
+    Va = an.eeg_sphere(radii, sig, w.dipoles[:ns], w.electrodes)
+    Ba = an.sarvas(w.dipoles[:ns], w.squids)
+    for prec, (ge, gm) in out.items():
+        res[prec]["analytic_eeg"] = {"rdm_max": float(an.rdm(ge[:, :ns], Va).max()),
+                                     "mag_max": float(an.mag(ge[:, :ns], Va).max()),
+                                     "rdm_median": float(np.median(an.rdm(ge[:, :ns], Va)))}
+        res[prec]["analytic_meg"] = {"rdm_max": float(an.rdm(gm[:, :ns], Ba).max()),
+                                     "mag_max": float(an.mag(gm[:, :ns], Ba).max())}
+    line = {"metric": "time-to-gain (s), config4 large head", "unit": "s", "n_gpus": 1,
+            "config": {"workload": "config4: 4 nested ico5 spheres r .85/.88/.92/1, sigma .33/1.79/.0042/.33, "
+                                   "N=%d, 10000 dipoles r<0.8, 256 EEG, 306 radial MEG at r=1.15" % N, "N": N,
+                       "analytic_sample_dipoles": ns},
+            "results": res}
+    if "fp64" in out and "mixed" in out:
+        e64, m64 = out["fp64"]
+        emx, mmx = out["mixed"]
+        line["value"] = res["mixed"]["time_to_gain_s"]
+        line["speedup_vs_fp64"] = res["fp64"]["time_to_gain_s"] / res["mixed"]["time_to_gain_s"]
+        line["rel_err_vs_fp64"] = {"eeg": float(np.linalg.norm(emx - e64) / np.linalg.norm(e64)),
+                                   "meg": float(np.linalg.norm(mmx - m64) / np.linalg.norm(m64))}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,6 +585,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config1")
     ap.add_argument("--branches", type=int, default=0, help="config3: graph branches (0 = autotune)")
+    ap.add_argument("--large-precisions", default="mixed,fp64", help="config4: precisions to run, in order")
+    ap.add_argument("--analytic-dipoles", type=int, default=500, help="config4: dipoles checked analytically")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--profile-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
@@ -533,6 +599,8 @@ def main():
         return run_reference(args)
     if args.config == "config3":
         return run_batch(args)
+    if args.config == "config4":
+        return run_large(args)
     return run_gpu(args)
 
 

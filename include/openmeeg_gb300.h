@@ -73,9 +73,9 @@ typedef struct {
     double t_factor_ms;
     double t_solve_ms;           /* solves + refinement + gain GEMM */
     int32_t refinement_steps;    /* mixed precision only */
-    int32_t gmres_iterations;    /* mixed precision only */
+    int32_t residual_mode;       /* mixed: 1 tensor-core digits, 2 double-float on CUDA cores; FP64: 0 */
     double  final_residual;      /* max over RHS of ||b - HM x|| / ||b|| (mixed precision) */
-    int64_t device_bytes;        /* peak device workspace of the call */
+    int64_t device_bytes;        /* peak device memory the call's own buffers held */
 } omg_gain_stats;
 
 /* ---- errors / context ---------------------------------------------------- */

@@ -63,7 +63,7 @@ class MeshPair(ctypes.Structure):
 
 class GainStats(ctypes.Structure):
     _fields_ = [("t_total_ms", c_dbl), ("t_headmat_ms", c_dbl), ("t_sources_ms", c_dbl), ("t_factor_ms", c_dbl),
-                ("t_solve_ms", c_dbl), ("refinement_steps", c_i32), ("gmres_iterations", c_i32),
+                ("t_solve_ms", c_dbl), ("refinement_steps", c_i32), ("residual_mode", c_i32),
                 ("final_residual", c_dbl), ("device_bytes", c_i64)]
 
     def as_dict(self):

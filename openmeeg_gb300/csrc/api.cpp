@@ -111,6 +111,7 @@ void launch_domain_check(int64_t n, const int* dom, uint64_t allowed, int* err, 
 using namespace omg;
 
 static thread_local std::string g_last_error;
+std::atomic<int64_t> g_dev_live{0}, g_dev_peak{0};
 void set_last_error(const char* msg) { g_last_error = msg; }
 
 void set_device(omg_context ctx) { OMG_CUDA(cudaSetDevice(ctx->device)); }
@@ -557,7 +558,18 @@ void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
         copy_convert<double, float>(N, N, hm.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
         symmetrize(hm.as<double>(), N, N, s);
         const char* mode = std::getenv("OMG_RESIDUAL");
-        sv->tc_residual = !(mode && std::string(mode) == "df64");
+        sv->tc_residual = sv->residual_choice >= 0 ? sv->residual_choice == 1
+                                                   : !(mode && std::string(mode) == "df64");
+        if (sv->tc_residual && sv->residual_choice < 0) {
+            // the digits (nda planes of N x ld bf16) must fit beside the FP32 factor's panel copies and
+            // remainders (2 x 4 N^2 bytes, allocated once the FP64 matrix is gone); else the double-float
+            // residual from a float pair (8 N^2 bytes) is used
+            size_t free_b = 0, total_b = 0;
+            OMG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            const double dig = (double)sv->nda * N * digits_ld(N) * 2, later = 8.0 * N * N, margin = 4e9;
+            const double after_release = (double)free_b - dig + 8.0 * N * N;
+            if ((double)free_b < dig + margin || after_release < later + margin) sv->tc_residual = false;
+        }
         if (sv->tc_residual) {
             // the FP64 matrix is kept only as fixed-point digits for the tensor-core residual
             const int64_t ldd = digits_ld(N);
@@ -1244,6 +1256,8 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     for (auto& e : ev) OMG_CUDA(cudaEventCreate(&e));
     OMG_CUDA(cudaEventRecord(ev[0], s));
     reset_err(ctx);
+    const int64_t live0 = g_dev_live.load();
+    g_dev_peak.store(live0);
     auto sv = std::make_unique<omg_solver_s>();
     sv->ctx = ctx;
     sv->geo = geo;
@@ -1287,9 +1301,9 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
         st->t_solve_ms = d;
         st->t_total_ms = a + b + c + d;
         st->refinement_steps = sv->last_steps;
-        st->gmres_iterations = 0;
+        st->residual_mode = precision == OMG_PREC_FP64 ? 0 : (sv->tc_residual ? 1 : 2);
         st->final_residual = sv->last_residual;
-        st->device_bytes = (int64_t)(N * N * 8) * (precision == OMG_PREC_MIXED ? 3 : 2) / 2 + N * (k + nd) * 8;
+        st->device_bytes = g_dev_peak.load() - live0;
     }
     for (auto& e : ev) cudaEventDestroy(e);
 }

@@ -55,6 +55,7 @@ struct BatchModel {
     DevBuf est;                  // mixed: final relative correction of the refinement
     NearPlan near;
     int refine_steps = 0;
+    int tc_residual = 1;         // residual kind chosen by the planning run
     std::vector<std::pair<int64_t, int64_t>> rows;   // contraction row ranges
     uint64_t allowed = 0;        // domains whose dipoles the planned rows cover
     uint64_t version = 0;        // geometry version the plan was made for
@@ -145,6 +146,7 @@ void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
     sv->N = N;
     sv->nP = g->d.nP;
     sv->refine_tol = b->refine_tol;
+    sv->residual_choice = planning ? -1 : m.tc_residual;
     DevBuf hm((size_t)N * N * 8, s);
     if (mixed)
         assemble_headmat_mixed(g, b->hm_it, hm.as<double>(), N, &m.near);
@@ -180,6 +182,7 @@ void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
     } else if (planning) {
         solver_solve_internal(sv.get(), B.as<double>(), N, k);
         m.refine_steps = sv->last_steps;
+        m.tc_residual = sv->tc_residual ? 1 : 0;
     } else {
         solve_mixed_fixed(sv.get(), B.as<double>(), N, k, m.refine_steps, m.est.as<double>());
     }
@@ -395,7 +398,8 @@ void tune(omg_batch b, int requested) {
 size_t model_peak_bytes(const BatchModel& m, int precision) {
     const double N = (double)m.geo->d.N, k = (double)(m.ne + m.nm), nd = (double)m.nd;
     const double nt = (double)m.geo->h.nt;
-    double mat = precision == OMG_PREC_MIXED ? 20.0 * N * N : 8.0 * N * N;
+    // mixed: FP64 matrix while converting + FP32 factor + 7 bf16 digit planes, then panel copies and remainders
+    double mat = precision == OMG_PREC_MIXED ? 26.0 * N * N : 8.0 * N * N;
     double scratch = 0.0;   // largest per-pair assembly temporary (S scratch + two D scratch)
     for (const auto& p : m.geo->h.pairs) {
         const double n1 = (double)(m.geo->h.tbeg[p.m1 + 1] - m.geo->h.tbeg[p.m1]);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <vector>
 
@@ -25,6 +26,16 @@ struct omg_context_s {
     int refs = 1;              // the caller's handle + one per live geometry / solver
 };
 
+// Live bytes of all device buffers of the library and their high-water mark
+// (reset by the calls that report a peak footprint).
+extern std::atomic<int64_t> g_dev_live, g_dev_peak;
+inline void note_alloc(int64_t bytes) {
+    const int64_t now = g_dev_live.fetch_add(bytes) + bytes;
+    int64_t pk = g_dev_peak.load();
+    while (now > pk && !g_dev_peak.compare_exchange_weak(pk, now)) {
+    }
+}
+
 // Device buffer.  Temporaries of one call are stream-ordered
 // (cudaMallocAsync/cudaFreeAsync on the call's stream); buffers that outlive
 // the call (geometry, solver) are plain allocations, so freeing them never
@@ -33,23 +44,31 @@ struct DevBuf {
     void* p = nullptr;
     cudaStream_t s = nullptr;
     bool persistent = false;
+    size_t bytes = 0;
     DevBuf() = default;
-    DevBuf(size_t bytes, cudaStream_t st, bool keep = false) : s(st), persistent(keep) {
-        if (!bytes) return;
+    DevBuf(size_t nbytes, cudaStream_t st, bool keep = false) : s(st), persistent(keep) {
+        if (!nbytes) return;
         if (persistent)
-            OMG_CUDA(cudaMalloc(&p, bytes));
+            OMG_CUDA(cudaMalloc(&p, nbytes));
         else
-            OMG_CUDA(cudaMallocAsync(&p, bytes, st));
+            OMG_CUDA(cudaMallocAsync(&p, nbytes, st));
+        bytes = nbytes;
+        note_alloc((int64_t)bytes);
     }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
-    DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s), persistent(o.persistent) { o.p = nullptr; }
+    DevBuf(DevBuf&& o) noexcept : p(o.p), s(o.s), persistent(o.persistent), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
     DevBuf& operator=(DevBuf&& o) noexcept {
         release();
         p = o.p;
         s = o.s;
         persistent = o.persistent;
+        bytes = o.bytes;
         o.p = nullptr;
+        o.bytes = 0;
         return *this;
     }
     ~DevBuf() { release(); }
@@ -61,8 +80,10 @@ struct DevBuf {
             } else {
                 cudaFreeAsync(p, s);
             }
+            g_dev_live.fetch_sub((int64_t)bytes);
         }
         p = nullptr;
+        bytes = 0;
     }
     template <typename T>
     T* as() const { return static_cast<T*>(p); }

@@ -27,6 +27,7 @@ struct omg_solver_s {
     // the FP64 head matrix (nda planes of base-2^beta digits, row exponents);
     // false: double-float residual on the CUDA cores from A64
     bool tc_residual = true;
+    int residual_choice = -1;               // -1: decide at factorization (memory, OMG_RESIDUAL); 0/1: given
     DevBuf Adig, rexp;
     int nda = 7, ndx = 7, beta = 7, lmax = 8;
     bool persistent = false;                // outlives the call that made it (public solver handle)
