@@ -254,6 +254,22 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
     return info
 
 
+def max_over_ranks(value: float, device) -> float:
+    """The slowest rank's time: every rank contributes its own value, all receive the maximum
+    (replicas share no data; this is the only collective of the multi-GPU bench)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, t_max: float) -> float:
+    """Units all ranks processed per second of the slowest rank (weak scaling: fixed work per rank)."""
+    return units_per_rank * world / t_max
+
+
 def tri_pairs(head):
     """Triangle pairs the head matrix integrates (S for non-barrier pairs, D and D* both ways): the pair
     loop of the symmetric BEM over nested meshes (self pairs and adjacent pairs)."""
@@ -338,12 +354,7 @@ def run_gpu(args):
     _lib.profile_enable(False)
     prof = _lib.profile_read()
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps
-    t_max = t_step
-    if world > 1:
-        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-        dist.barrier()
+    t_max = max_over_ranks(t_step, dev) if world > 1 else t_step
 
     def relerr(a, b):
         return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
@@ -577,6 +588,85 @@ def run_large(args):
     return 0
 
 
+def run_adjoint(args):
+    """config2: config1 geometry, 500 dipoles, conductivities sampled log-uniformly within x[0.5, 2].
+    Gain + gradient (d gain / d conductivities and d gain / d dipoles through the torch.autograd.Function)
+    in FP64 and mixed precision; checked against central finite differences (FP64, relative step 1e-6)
+    for the 3 conductivities and a sample of dipole coordinates, and mixed against FP64."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    __import__("__graft_entry__").build()
+    from openmeeg_gb300 import adjoint, api, workloads
+    w = workloads.config2()
+    ctx = api.Context(local)
+    geo = api.Geometry.from_head(w.head, ctx)
+    dev = torch.device("cuda", local)
+    sig0 = torch.tensor([d[2] for d in w.head.domains], dtype=torch.float64)
+    dip0 = torch.as_tensor(w.dipoles, dtype=torch.float64, device=dev)
+    k = w.electrodes.shape[0] + w.squids.shape[0]
+    Gbar = torch.randn(k, dip0.shape[0], generator=torch.Generator().manual_seed(11), dtype=torch.float64).to(dev)
+
+    def loss(sig, dip, prec):
+        return (adjoint.gain(sig, dip, geo, w.head.domains, w.electrodes, w.squids, precision=prec) * Gbar).sum()
+
+    res, grads = {}, {}
+    for prec in ("fp64", "mixed"):
+        sig = sig0.clone().requires_grad_(True)
+        dip = dip0.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L = loss(sig, dip, prec)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        gs, gd = torch.autograd.grad(L, [sig, dip])
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        grads[prec] = (gs.detach().cpu().numpy(), gd.detach().cpu().numpy())
+        res[prec] = {"forward_s": t1 - t0, "backward_s": t2 - t1}
+    # central differences (FP64) for the conductivities
+    gs64 = grads["fp64"][0]
+    fd = np.zeros_like(gs64)
+    with torch.no_grad():
+        for kd in range(len(sig0)):
+            if sig0[kd] == 0:
+                continue
+            h = 1e-6 * float(sig0[kd])
+            sp, sm = sig0.clone(), sig0.clone()
+            sp[kd] += h
+            sm[kd] -= h
+            fd[kd] = (float(loss(sp, dip0, "fp64")) - float(loss(sm, dip0, "fp64"))) / (2 * h)
+    nz = sig0.numpy() > 0
+    sig_err = float(np.max(np.abs(gs64[nz] - fd[nz]) / np.abs(fd[nz])))
+    # central differences for a sample of dipole coordinates: the head matrix and its solves do not
+    # depend on the dipoles, so each difference re-evaluates the full gain at two perturbed dipole sets
+    rng = np.random.default_rng(3)
+    sample = [(int(j), int(c)) for j, c in zip(rng.integers(0, dip0.shape[0], args.fd_dipoles),
+                                               rng.integers(0, 6, args.fd_dipoles))]
+    gd64 = grads["fp64"][1]
+    dip_err = 0.0
+    with torch.no_grad():
+        for j, c in sample:
+            h = 1e-6
+            dp, dm = dip0.clone(), dip0.clone()
+            dp[j, c] += h
+            dm[j, c] -= h
+            f = (float(loss(sig0, dp, "fp64")) - float(loss(sig0, dm, "fp64"))) / (2 * h)
+            dip_err = max(dip_err, abs(gd64[j, c] - f) / max(abs(f), 1e-30))
+    mix_sig = float(np.linalg.norm(grads["mixed"][0] - gs64) / np.linalg.norm(gs64))
+    mix_dip = float(np.linalg.norm(grads["mixed"][1] - gd64) / np.linalg.norm(gd64))
+    line = {"metric": "gain + gradient time (s), config2", "unit": "s", "n_gpus": 1,
+            "value": res["mixed"]["forward_s"] + res["mixed"]["backward_s"], "higher_is_better": False,
+            "config": {"workload": "config2: config1 geometry (N=%d), 500 dipoles, sigma sampled x[0.5,2]" % geo.size,
+                       "fd_step": "1e-6 relative (conductivities), 1e-6 absolute (dipoles)",
+                       "fd_dipole_coordinates": len(sample)},
+            "results": res,
+            "fd_rel_err": {"conductivities_max": sig_err, "dipole_coordinates_max": dip_err},
+            "mixed_vs_fp64_gradient_rel_err": {"conductivities": mix_sig, "dipoles": mix_dip}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -586,6 +676,7 @@ def main():
     ap.add_argument("--config", default="config1")
     ap.add_argument("--branches", type=int, default=0, help="config3: graph branches (0 = autotune)")
     ap.add_argument("--large-precisions", default="mixed,fp64", help="config4: precisions to run, in order")
+    ap.add_argument("--fd-dipoles", type=int, default=4, help="config2: dipole coordinates checked by differences")
     ap.add_argument("--analytic-dipoles", type=int, default=500, help="config4: dipoles checked analytically")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--profile-steps", type=int, default=1)
@@ -601,6 +692,8 @@ def main():
         return run_batch(args)
     if args.config == "config4":
         return run_large(args)
+    if args.config == "config2":
+        return run_adjoint(args)
     return run_gpu(args)
 
 

@@ -82,7 +82,7 @@ void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, i
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
-                 const char* prof_name = "gemm_tf32x3");
+                 const char* prof_name = "gemm_tf32x3", int max_ctas = 0);
 void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
@@ -126,8 +126,27 @@ void release_context(omg_context ctx) {
     cudaFree(ctx->d_err);
     cudaFree(ctx->d_errcol);
     cudaFree(ctx->d_scalar);
+    if (ctx->aux) cudaStreamSynchronize(ctx->aux);
+    release_aux(ctx);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
+}
+
+static int n_sm() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+void ensure_aux(omg_context ctx) {
+    if (!ctx->aux) OMG_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    if (!ctx->ev_a) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_a, cudaEventDisableTiming));
+    if (!ctx->ev_b) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_b, cudaEventDisableTiming));
 }
 
 void release_geometry(omg_geometry geo) {
@@ -466,9 +485,23 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     float* Th = T.as<float>();
     float* Bih = Bi.as<float>();
     float* Bil = Bih + (size_t)nb * nb;
+    // Look-ahead: the trailing update of panel b is split into the next panel's columns (on the
+    // main stream, so panel b+1 can be factored at once) and the rest (on the second stream, with a
+    // few SMs left free), so the latency-bound diagonal-block work of panel b+1 overlaps the bulk
+    // of the update of panel b.  ev_a: panel b's split copies are ready; ev_b: the rest of the
+    // update of panel b-1 is done (the next panel's columns of step b lie inside it).
+    ensure_aux(sv->ctx);
+    cudaStream_t s2 = sv->ctx->aux;
+    cudaEvent_t ev_w = sv->ctx->ev_a, ev_r = sv->ctx->ev_b;
+    bool rest_pending = false;
+    const int reserve = 8;   // SMs the rest update leaves to the panel chain
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
-        if (k0 == nP) negate_lower<float>(A + k0 + k0 * ld, ld, N - k0, s);
+        if (k0 == nP) {   // continue on -(vertex Schur complement): every pending update must be in
+            if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
+            rest_pending = false;
+            negate_lower<float>(A + k0 + k0 * ld, ld, N - k0, s);
+        }
         // L11 and L11^-1 (the inverse also serves the solves)
         potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
                   sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
@@ -481,10 +514,25 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
             float* Wh = sv->W.as<float>() + sv->w_off[b];
             float* Wl = Wh + m * nb;
             split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Wh, Wl, s);
-            gemm_tf32x3(m, m, nk, -1.f, Wh, Wl, nb, nb, 0, Wh, Wl, nb, nb, 0, 1.f, A + k1 + k1 * ld, ld, true,
-                        sv->ctx->d_err, s, "gemm_syrk");
+            const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
+            // the next panel's columns (all rows below k1), after the rest update of panel b-1
+            if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
+            gemm_tf32x3(m, nn, nk, -1.f, Wh, Wl, nb, nb, 0, Wh, Wl, nb, nb, 0, 1.f, A + k1 + k1 * ld, ld, false,
+                        sv->ctx->d_err, s, "gemm_next");
+            rest_pending = false;
+            if (mr > 0) {   // the rest, on the second stream
+                OMG_CUDA(cudaEventRecord(ev_w, s));
+                OMG_CUDA(cudaStreamWaitEvent(s2, ev_w, 0));
+                const float* Rh = Wh + nn * nb;
+                const float* Rl = Wl + nn * nb;
+                gemm_tf32x3(mr, mr, nk, -1.f, Rh, Rl, nb, nb, 0, Rh, Rl, nb, nb, 0, 1.f, A + k2 + k2 * ld, ld, true,
+                            sv->ctx->d_err, s2, "gemm_syrk", std::max(1, n_sm() - reserve));
+                OMG_CUDA(cudaEventRecord(ev_r, s2));
+                rest_pending = true;
+            }
         }
     }
+    if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
     sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
     split_lower_inplace(N, A, ld, sv->A32r.as<float>(), s);
 }

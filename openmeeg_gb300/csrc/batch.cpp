@@ -79,6 +79,8 @@ struct Branch {
     }
     ~Branch() {
         cudaStreamSynchronize(c.own);
+        if (c.aux) cudaStreamSynchronize(c.aux);
+        release_aux(&c);
         cudaFree(c.d_err);
         cudaFree(c.d_errcol);
         cudaFree(c.d_scalar);

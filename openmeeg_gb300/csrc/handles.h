@@ -24,7 +24,18 @@ struct omg_context_s {
     double* d_scalar = nullptr;
     int64_t launches_at_create = 0;
     int refs = 1;              // the caller's handle + one per live geometry / solver
+    // second stream and two events of the factorization's look-ahead (created on first use)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
 };
+
+inline void release_aux(omg_context_s* c) {
+    if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->ev_a) cudaEventDestroy(c->ev_a);
+    if (c->ev_b) cudaEventDestroy(c->ev_b);
+    c->aux = nullptr;
+    c->ev_a = c->ev_b = nullptr;
+}
 
 // Live bytes of all device buffers of the library and their high-water mark
 // (reset by the calls that report a peak footprint).

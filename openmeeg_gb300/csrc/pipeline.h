@@ -67,6 +67,7 @@ inline int guarded(F&& f) {
 }
 
 void set_device(omg_context ctx);
+void ensure_aux(omg_context ctx);
 void release_context(omg_context ctx);
 void release_geometry(omg_geometry geo);
 void reset_err(omg_context ctx);

@@ -248,7 +248,7 @@ static inline void check_tc(const char* what) {
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
-                 const char* prof_name) {
+                 const char* prof_name, int max_ctas) {
     if (M <= 0 || N <= 0) return;
     if (K <= 0) throw Error(OMG_ERR_INVALID, "empty K");
     ProfScope prof_(prof_name, s);
@@ -274,7 +274,7 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     const int64_t tiles_m = (M + tc::BM - 1) / tc::BM, tiles_n = (N + tc::BN - 1) / tc::BN;
     if (tiles_m > (1 << 30) / 2) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM too tall");
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
-    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
     tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, alpha,
                                                                      beta, C, ldc, lower ? 1 : 0, nprod, ntiles, err);
     check_tc("gemm_tf32x3");
@@ -376,7 +376,7 @@ extern "C" int omg_internal_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float a
                                         float beta, float* C, int64_t ldc, int lower, int* err) {
     try {
         omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, lower != 0, err, 0,
-                         "gemm_tf32x3");
+                         "gemm_tf32x3", 0);
         cudaError_t e = cudaDeviceSynchronize();
         return e == cudaSuccess ? 0 : -2;
     } catch (const omg::Error& e) {
