@@ -174,8 +174,13 @@ FP32_ISSUE_NOMINAL = 152 * 128 * 2.07e9
 # on a smaller head, per unit of the kernel's size (the summaries in profiles/ give
 # the command and the raw figures); scaled to the bench workload by that unit.
 NCU_TRAFFIC_PER_UNIT = {
-    # residual B - A X: bytes per N^2 element of the float-pair head matrix
-    "residual_df64": None,
+    # residual B - A X (double-float): bytes per N^2 element of the float-pair head matrix
+    # (ncu at N = 17926: 3.205 GB per launch)
+    "residual_df64": 9.97,
+    # residual from digits: DRAM bytes per byte of one digit plane, per digit pair and column
+    # block of right-hand sides (ncu at N = 4486, 96 right-hand sides: 1.105 GB per launch for
+    # 28 pairs of 40.8 MB planes); column blocks are counted as if they shared nothing in L2
+    "residual_tc": 0.968,
 }
 
 
@@ -208,8 +213,13 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
         kpad = (k + 127) // 128 * 128
         flops = 2.0 * N * N * kpad * pairs
         achieved = flops / t_launch / 1e12
+        ld = (N + 63) // 64 * 64
+        traffic = NCU_TRAFFIC_PER_UNIT["residual_tc"] * pairs * (N * ld * 2.0) * (kpad // 128)
         info.update({"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": None,
+                     "frac": achieved / bf16, "traffic": traffic,
+                     "traffic_note": "DRAM bytes per launch scaled from an ncu capture at N = 4486; "
+                                     "an upper bound when the "
+                                     "column blocks share digit tiles in L2",
                      "algorithmic_fp64_equivalent_flops_per_launch": 2.0 * N * N * k,
                      "executed_bf16_flops_per_launch": flops,
                      "note": f"executed bf16 tensor flops (28 exact digit-pair GEMMs, k padded to {kpad}) vs "

@@ -56,7 +56,7 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, 
 // lower triangle (diagonal included); otherwise column of tiles after column.
 __device__ __forceinline__ void tile_of(int64_t t, int tiles_m, int lower, int& tm, int& tn) {
     if (lower) {
-        int r = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        int r = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);   // FP32 guess, corrected exactly below
         while ((int64_t)r * (r + 1) / 2 > t) --r;
         while ((int64_t)(r + 1) * (r + 2) / 2 <= t) ++r;
         tm = r;

@@ -210,7 +210,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                     uint32_t r[32];
                     tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64 + chunk * 32), r);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) iacc[chunk * 32 + j] += __float2int_rn(__uint_as_float(r[j]));
+                    for (int j = 0; j < 32; ++j)   // |window sum| < 2^22: adding 1.5 * 2^23 puts it in the mantissa
+                        iacc[chunk * 32 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
                 }
                 fence_before();
                 __syncwarp();
