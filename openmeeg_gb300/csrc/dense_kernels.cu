@@ -956,14 +956,19 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
 // B_k <- op(Linv_k) B_k for the n x ncol block at B (ldb), op = transpose if
 // `trans`; also writes the TF32 head/remainder split of the result as K-major
 // rows (column j -> row j of H/L, kpad = nb) for the following tensor-core
-// update.  One warp per column, Linv_k staged in shared memory.
-__global__ void __launch_bounds__(256) apply_inv_split_kernel(int n, int nb, int64_t ncol, const float* __restrict__ Li,
-                                                              int trans, float* B, int64_t ldb, float* H, float* L) {
+// update.  Linv_k is staged once per CTA in shared memory; each CTA then
+// handles four columns at a time, one thread per output row, each dot product
+// split over four independent partial sums.
+constexpr int AI_THREADS = 512, AI_COLS = AI_THREADS / 128;
+
+__global__ void __launch_bounds__(AI_THREADS) apply_inv_split_kernel(int n, int nb, int64_t ncol,
+                                                                     const float* __restrict__ Li, int trans,
+                                                                     float* B, int64_t ldb, float* H, float* L) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int ldm = nb + 1;                        // padded rows: lanes read different rows at the same l
+    const int ldm = nb + 1;                        // padded rows: threads read different rows at the same l
     float* sM = reinterpret_cast<float*>(smraw);   // nb x nb, sM[i*ldm + l] = op(Linv)[i][l]
-    float* sb = sM + nb * ldm;                     // 8 warps x nb
-    for (int e = threadIdx.x; e < nb * nb; e += 256) {
+    float* sb = sM + nb * ldm;                     // AI_COLS x nb
+    for (int e = threadIdx.x; e < nb * nb; e += AI_THREADS) {
         const int r = e % nb, c = e / nb;          // coalesced read of column-major Linv
         const float v = Li[r + c * nb];
         if (trans)
@@ -971,38 +976,44 @@ __global__ void __launch_bounds__(256) apply_inv_split_kernel(int n, int nb, int
         else
             sM[r * ldm + c] = v;
     }
-    __syncthreads();
-    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    float* b = sb + warp * nb;
-    for (int64_t j = (int64_t)blockIdx.x * 8 + warp; j < ncol; j += (int64_t)gridDim.x * 8) {
-        float* bj = B + j * ldb;
-        for (int l = lane; l < nb; l += 32) b[l] = l < n ? bj[l] : 0.f;
-        __syncwarp();
-        for (int i = lane; i < nb; i += 32) {
-            float acc = 0.f;
-            const float* row = sM + i * ldm;
-            for (int l = 0; l < nb; ++l) acc = fmaf(row[l], b[l], acc);
+    const int q = threadIdx.x / 128, i = threadIdx.x % 128;
+    const float* row = sM + i * ldm;
+    float* b = sb + q * nb;
+    for (int64_t j0 = (int64_t)blockIdx.x * AI_COLS; j0 < ncol; j0 += (int64_t)gridDim.x * AI_COLS) {
+        const int64_t j = j0 + q;
+        __syncthreads();   // the staged block (first pass) / the previous columns' reads of b
+        if (j < ncol && i < nb) b[i] = i < n ? B[j * ldb + i] : 0.f;
+        __syncthreads();
+        if (j < ncol && i < nb) {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            for (int l = 0; l < nb; l += 4) {
+                a0 = fmaf(row[l], b[l], a0);
+                a1 = fmaf(row[l + 1], b[l + 1], a1);
+                a2 = fmaf(row[l + 2], b[l + 2], a2);
+                a3 = fmaf(row[l + 3], b[l + 3], a3);
+            }
+            const float acc = (a0 + a1) + (a2 + a3);
             const float h = __uint_as_float(__float_as_uint(acc) & 0xFFFFE000u);
             H[j * nb + i] = (i < n) ? h : 0.f;
             L[j * nb + i] = (i < n) ? acc - h : 0.f;
-            if (i < n) bj[i] = acc;
+            if (i < n) B[j * ldb + i] = acc;
         }
-        __syncwarp();
     }
 }
 
 void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, float* B, int64_t ldb, float* H,
                      float* L, cudaStream_t s) {
     if (ncol <= 0) return;
+    if (nb != 128) throw Error(OMG_ERR_INVALID, "apply_inv_split: block size must be 128");
     ProfScope prof_("apply_inv", s);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(apply_inv_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr = true;
     }
-    const size_t sm = ((size_t)nb * (nb + 1) + 8 * (size_t)nb) * sizeof(float);
-    const unsigned grid = (unsigned)std::min<int64_t>((ncol + 7) / 8, 1024);
-    apply_inv_split_kernel<<<grid, 256, sm, s>>>(n, nb, ncol, Li, trans ? 1 : 0, B, ldb, H, L);
+    const size_t sm = ((size_t)nb * (nb + 1) + AI_COLS * (size_t)nb) * sizeof(float);
+    const unsigned grid = (unsigned)std::min<int64_t>((ncol + AI_COLS - 1) / AI_COLS, 1024);
+    apply_inv_split_kernel<<<grid, AI_THREADS, sm, s>>>(n, nb, ncol, Li, trans ? 1 : 0, B, ldb, H, L);
     check("apply_inv_split");
 }
 
