@@ -226,6 +226,22 @@ int omg_gain_host(omg_context ctx, omg_geometry geo, int32_t precision, const om
                   const double* electrodes, int64_t n_electrodes, const double* squids, int64_t n_squids,
                   double* gain_eeg, double* gain_meg, omg_gain_stats* stats);
 
+/* ---- surface sources -------------------------------------------------------
+ * SurfSourceMat (OpenMEEG/src/assembleSourceMat.cpp:22-64, assembleSourceMat.h:20):
+ * a triangulated source surface (host arrays: vertices n x 3 row-major,
+ * triangles m x 3 0-based) inside one conducting domain of the geometry; out
+ * is N x n_verts column-major in the reference numbering.  The default
+ * integrator is the reference's (3, 0, 0.005); adaptive integration is not
+ * supported.  A source mesh whose vertices lie in different domains is
+ * rejected (the reference's OverlappingSourceMesh). */
+int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts, int64_t n_verts,
+                          const int64_t* tris, int64_t n_tris, const omg_integrator* integ, double* ssm);
+/* SurfSource2MEGMat (OpenMEEG/src/assembleSensors.cpp:102-125): squids on the
+ * device (n x 6), source mesh from host arrays; out n_squids x n_verts,
+ * column-major. */
+int omg_surfsource2megmat_dev(omg_context ctx, const double* verts, int64_t n_verts, const int64_t* tris,
+                              int64_t n_tris, const double* squids, int64_t n_squids, double* ss2mm);
+
 /* ---- batched forward (no reference counterpart) -----------------------------
  * Many head models, each with its own geometry, dipoles and sensors, computed
  * by one captured CUDA graph: every model's forward is the adjoint gain of

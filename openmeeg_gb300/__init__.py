@@ -9,7 +9,8 @@ __version__ = "0.1.0"
 
 _API_NAMES = {"Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
               "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
-              "GainEEGMEGadjoint", "forward_gain", "BatchForward", "OMGError", "kernel_launches"}
+              "GainEEGMEGadjoint", "forward_gain", "BatchForward", "SurfSourceMat", "SurfSource2MEGMat", "OMGError",
+              "kernel_launches"}
 
 
 def __getattr__(name):

@@ -25,7 +25,8 @@ from ._lib import GainStats, GeometryInfo, Integrator, OMGError, check
 
 __all__ = ["Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
            "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
-           "GainEEGMEGadjoint", "forward_gain", "BatchForward", "OMGError", "kernel_launches"]
+           "GainEEGMEGadjoint", "forward_gain", "BatchForward", "SurfSourceMat", "SurfSource2MEGMat", "OMGError",
+           "kernel_launches"]
 
 FP64 = "fp64"
 MIXED = "mixed"
@@ -253,6 +254,36 @@ def DipSource2MEGMat(dipoles, squids, ctx: Optional[Context] = None) -> torch.Te
     s = _as_dev(squids, ctx, 6)
     out = torch.empty((d.shape[0], s.shape[0]), dtype=torch.float64, device=_dev(ctx))
     check(ctx.lib.omg_dipsource2megmat_dev(ctx.handle, _ptr(d), d.shape[0], _ptr(s), s.shape[0], _ptr(out)))
+    return out.T
+
+
+def _mesh_arrays(vertices, triangles):
+    V = np.ascontiguousarray(np.asarray(vertices, np.float64)[:, :3])
+    T = np.ascontiguousarray(np.asarray(triangles, np.int64)[:, :3])
+    return V, T
+
+
+def SurfSourceMat(geom: Geometry, vertices, triangles, integrator: Optional[Integrator] = None) -> torch.Tensor:
+    """SurfSourceMat(geo, source_mesh, integrator) (assembleSourceMat.cpp:22-64): N x n_vertices for a
+    triangulated source surface inside one conducting domain."""
+    V, T = _mesh_arrays(vertices, triangles)
+    it = _default(integrator, 3, 0, 0.005)
+    out = torch.empty((V.shape[0], geom.size), dtype=torch.float64, device=_dev(geom.ctx))   # column-major
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    check(geom.lib.omg_surfsourcemat_dev(geom.ctx.handle, geom.handle, P(V, ctypes.c_double), V.shape[0],
+                                         P(T, ctypes.c_int64), T.shape[0], ctypes.byref(it), _ptr(out)))
+    return out.T
+
+
+def SurfSource2MEGMat(vertices, triangles, squids, ctx: Optional[Context] = None) -> torch.Tensor:
+    """SurfSource2MEGMat(source_mesh, sensors) (assembleSensors.cpp:102-125): n_squids x n_vertices."""
+    ctx = ctx or Context.default()
+    V, T = _mesh_arrays(vertices, triangles)
+    sq = _as_dev(squids, ctx, 6)
+    out = torch.empty((V.shape[0], sq.shape[0]), dtype=torch.float64, device=_dev(ctx))
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    check(ctx.lib.omg_surfsource2megmat_dev(ctx.handle, P(V, ctypes.c_double), V.shape[0], P(T, ctypes.c_int64),
+                                            T.shape[0], _ptr(sq), sq.shape[0], _ptr(out)))
     return out.T
 
 

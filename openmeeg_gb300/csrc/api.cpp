@@ -20,6 +20,8 @@ void profile_enable(bool on);
 std::vector<std::tuple<std::string, int64_t, double>> profile_collect();
 // kernel launchers (bem_kernels.cu)
 void launch_prepare_triangles_order(const DevGeom& g, int order, cudaStream_t s);
+void launch_rows_to_reference(const DevGeom& g, int64_t ncol, const double* in, int64_t ldi, double* out, int64_t ldo,
+                              cudaStream_t s);
 void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi, double* hm, int64_t ld,
                                  cudaStream_t s);
 void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
@@ -34,7 +36,8 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
 void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
                  double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
-                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s);
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s,
+                 double mag = kMagFactor);
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s);
@@ -859,6 +862,81 @@ void gain_contract(const std::vector<std::pair<int64_t, int64_t>>& merged, const
                          gmeg, nm, s);
 }
 
+// A geometry's meshes plus one source surface (SurfSourceMat, SurfSource2MEGMat) as
+// one device geometry: the source's vertices and triangles follow the head's,
+// its triangles carry no unknown, so the block kernels of the head matrix run
+// between a head mesh and the source unchanged.  geo == nullptr: the source alone.
+struct SourceSurface {
+    DevGeom d;
+    std::vector<DevBuf> bufs;
+    int64_t nv0 = 0, nt0 = 0, nvs = 0, nts = 0;
+};
+
+static void build_source_surface(SourceSurface& u, omg_geometry geo, const double* verts, int64_t nvs,
+                                 const int64_t* tris, int64_t nts, int order, cudaStream_t s) {
+    OMG_REQUIRE(verts && tris, "null source mesh");
+    OMG_REQUIRE(nvs >= 3 && nts >= 1, "source mesh needs at least 3 vertices and 1 triangle");
+    for (int64_t i = 0; i < 3 * nts; ++i)
+        OMG_REQUIRE(tris[i] >= 0 && tris[i] < nvs, "source mesh triangle refers to a missing vertex");
+    for (int64_t i = 0; i < 3 * nvs; ++i) OMG_REQUIRE(std::isfinite(verts[i]), "source mesh vertex not finite");
+    const int64_t nv0 = geo ? geo->h.nv : 0, nt0 = geo ? geo->h.nt : 0;
+    u.nv0 = nv0;
+    u.nt0 = nt0;
+    u.nvs = nvs;
+    u.nts = nts;
+    const int64_t nv = nv0 + nvs, nt = nt0 + nts;
+    std::vector<double> V(3 * nv);
+    std::vector<int32_t> T(3 * nt), tpos(nt, -1);
+    if (geo) {
+        std::copy(geo->h.V.begin(), geo->h.V.end(), V.begin());
+        std::copy(geo->h.T.begin(), geo->h.T.end(), T.begin());
+        for (int m = 0; m < geo->h.nmesh; ++m)
+            for (int64_t t = geo->h.tbeg[m]; t < geo->h.tbeg[m + 1]; ++t)
+                if (!geo->h.barrier[m]) tpos[t] = (int32_t)(geo->h.tidx[t] - geo->h.nv);
+    }
+    std::copy(verts, verts + 3 * nvs, V.begin() + 3 * nv0);
+    for (int64_t i = 0; i < 3 * nts; ++i) T[3 * nt0 + i] = (int32_t)(tris[i] + nv0);
+    std::vector<int32_t> beg(nv + 1, 0), tri;
+    std::vector<int8_t> loc;
+    for (int64_t t = 0; t < nt; ++t)
+        for (int j = 0; j < 3; ++j) beg[T[3 * t + j] + 1]++;
+    for (int64_t v = 0; v < nv; ++v) beg[v + 1] += beg[v];
+    tri.assign(beg[nv], 0);
+    loc.assign(beg[nv], 0);
+    std::vector<int32_t> fill(nv, 0);
+    for (int64_t t = 0; t < nt; ++t)
+        for (int j = 0; j < 3; ++j) {
+            const int32_t v = T[3 * t + j];
+            tri[beg[v] + fill[v]] = (int32_t)t;
+            loc[beg[v] + fill[v]] = (int8_t)j;
+            fill[v]++;
+        }
+    DevGeom& d = u.d;
+    d.nv = nv;
+    d.nt = nt;
+    d.nP = geo ? geo->d.nP : 0;
+    d.nPt = geo ? geo->d.nPt : 0;
+    d.N = geo ? geo->d.N : 0;
+    d.Nref = geo ? geo->d.Nref : 0;
+    d.nmesh = (geo ? geo->h.nmesh : 0) + 1;
+    d.V = upload(u.bufs, V, s);
+    d.T = upload(u.bufs, T, s);
+    d.tpos = upload(u.bufs, tpos, s);
+    d.v2t_beg = upload(u.bufs, beg, s);
+    d.v2t_tri = upload(u.bufs, tri, s);
+    d.v2t_loc = upload(u.bufs, loc, s);
+    u.bufs.emplace_back((size_t)nt * SREC * 8, s, true);
+    d.srec = u.bufs.back().as<double>();
+    u.bufs.emplace_back((size_t)nt * PREC * 8, s, true);
+    d.prec = u.bufs.back().as<double>();
+    u.bufs.emplace_back((size_t)nt * QREC * 8, s, true);
+    d.qrec = u.bufs.back().as<double>();
+    u.bufs.emplace_back(std::max<size_t>(1, tri.size()) * 3 * sizeof(double), s, true);
+    d.v2t_q = u.bufs.back().as<double>();
+    launch_prepare_triangles_order(d, order, s);
+    launch_prepare_vertex_curls(d, s);
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -1096,6 +1174,83 @@ int omg_dipsource2megmat_dev(omg_context ctx, const double* dipoles, int64_t n_d
         set_device(ctx);
         launch_ds2mm(dipoles, n_dipoles, squids, n_squids, ds2mm, n_squids, ctx->stream);
         OMG_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+// SurfSourceMat (OpenMEEG/src/assembleSourceMat.cpp:22-64): for each boundary
+// of the domain that holds the source surface, the N block (vertices of the
+// boundary mesh x source vertices, coefficient +-K * orientation) and the D
+// block (its triangles x source vertices, coefficient times -1/sigma).
+int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts, int64_t n_verts,
+                          const int64_t* tris, int64_t n_tris, const omg_integrator* integ, double* ssm) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && ssm, "null argument");
+        set_device(ctx);
+        const omg_integrator it = integ ? *integ : default_hm_integrator();
+        check_integrator(it, false);
+        cudaStream_t s = ctx->stream;
+        reset_err(ctx);
+        SourceSurface u;
+        build_source_surface(u, geo, verts, n_verts, tris, n_tris, it.order, s);
+        const HostGeometry& h = geo->h;
+        // the domain of the source surface: every vertex must lie in the same one
+        DevBuf sa((size_t)n_verts * h.nmesh * 8, s), dom((size_t)n_verts * sizeof(int), s);
+        const double* pts = u.d.V + 3 * u.nv0;
+        launch_mesh_solid_angles(pts, 3, n_verts, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+        launch_domain_lookup(n_verts, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
+                             geo->binside, geo->orient, -1, dom.as<int>(), ctx->d_err, s);
+        std::vector<int> hdom(n_verts);
+        OMG_CUDA(cudaMemcpyAsync(hdom.data(), dom.p, n_verts * sizeof(int), cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+        const int d = hdom[0];
+        OMG_REQUIRE(d >= 0, "the source mesh lies in no domain of the geometry");
+        for (int v : hdom)
+            OMG_REQUIRE(v == d, "the source mesh crosses an interface of the geometry (overlapping source mesh)");
+        const double sigma = h.domains[d].sigma;
+        OMG_REQUIRE(sigma != 0.0, "the source mesh lies in a zero-conductivity domain");
+        const double L = -1.0 / sigma;
+        const int64_t Nint = geo->d.N;
+        DevBuf out((size_t)Nint * n_verts * 8, s);
+        OMG_CUDA(cudaMemsetAsync(out.p, 0, (size_t)Nint * n_verts * 8, s));
+        const int64_t tsb = u.nt0, tse = u.nt0 + n_tris, vsb = u.nv0, vse = u.nv0 + n_verts;
+        for (const auto& b : h.domains[d].bounds) {
+            const int m = b.mesh;
+            const double coeffN = (b.inside ? kK : -kK) * h.orient[m];
+            const int64_t t1b = h.tbeg[m], t1e = h.tbeg[m + 1], n1 = t1e - t1b;
+            {
+                DevBuf S((size_t)n1 * n_tris * 8, s);   // unit-coefficient S block (the source is no unknown)
+                launch_S_block(u.d, t1b, t1e, tsb, tse, false, 1.0, it.order, nullptr, 0, S.as<double>(),
+                               ctx->d_err, s);
+                launch_N_block(u.d, h.vbeg[m], h.vbeg[m + 1], t1b, t1e, vsb, vse, tsb, tse, false, coeffN, nullptr,
+                               Nint, S.as<double>(), out.as<double>(), s, true);
+            }
+            if (!h.barrier[m]) {
+                DevBuf D((size_t)n1 * n_tris * 24, s);
+                launch_D_block(u.d, t1b, t1e, tsb, tse, it.order, D.as<double>(), ctx->d_err, s);
+                launch_D_gather(u.d, t1b, t1e, tsb, tse, vsb, vse, coeffN * L, D.as<double>(), out.as<double>(), Nint,
+                                s, true);
+            }
+        }
+        launch_rows_to_reference(geo->d, n_verts, out.as<double>(), Nint, ssm, geo->d.Nref, s);
+        check_err(ctx, "SurfSourceMat");
+    });
+}
+
+// SurfSource2MEGMat (OpenMEEG/src/assembleSensors.cpp:102-125): the Ferguson
+// field of the source surface's vertices at each sensor along its orientation.
+int omg_surfsource2megmat_dev(omg_context ctx, const double* verts, int64_t n_verts, const int64_t* tris,
+                              int64_t n_tris, const double* squids, int64_t n_squids, double* ss2mm) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && (n_squids == 0 || (squids && ss2mm)), "null argument");
+        set_device(ctx);
+        cudaStream_t s = ctx->stream;
+        SourceSurface u;
+        build_source_surface(u, nullptr, verts, n_verts, tris, n_tris, 3, s);
+        if (n_squids > 0) {
+            DevBuf F((size_t)n_squids * n_tris * 8, s);
+            launch_h2mm(u.d, squids, n_squids, nullptr, nullptr, 0, ss2mm, n_squids, 1, 0, F.as<double>(), s, 1.0);
+        }
+        OMG_CUDA(cudaStreamSynchronize(s));
     });
 }
 

@@ -36,7 +36,8 @@ namespace omg {
 void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
                  double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
-                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s);
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s,
+                 double mag = kMagFactor);
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
 void profile_enable(bool on);

@@ -313,7 +313,7 @@ void launch_D_block(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int
 __global__ void d_gather_kernel(int64_t tab, int64_t na, int64_t tbb, int64_t nb, int64_t vbb, int64_t nvb,
                                 double coeff, const double* __restrict__ tmp, const int32_t* __restrict__ v2t_beg,
                                 const int32_t* __restrict__ v2t_tri, const int8_t* __restrict__ v2t_loc,
-                                const int32_t* __restrict__ tpos, int64_t nP, double* hm, int64_t ld) {
+                                const int32_t* __restrict__ tpos, int64_t nP, double* hm, int64_t ld, int rect) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= na * nvb) return;
     const int64_t iv = idx % nvb, ia = idx / nvb;
@@ -324,15 +324,19 @@ __global__ void d_gather_kernel(int64_t tab, int64_t na, int64_t tbb, int64_t nb
         if (t2 < tbb || t2 >= tbb + nb) continue;
         sum += tmp[(ia * nb + (t2 - tbb)) * 3 + v2t_loc[k]];
     }
-    hm[lower_at(tpos[tab + ia], nP + v, ld)] += coeff * sum;
+    if (rect)   // rectangular output: row = the triangle's unknown, column = the vertex within B
+        hm[tpos[tab + ia] + iv * ld] += coeff * sum;
+    else
+        hm[lower_at(tpos[tab + ia], nP + v, ld)] += coeff * sum;
 }
 
 void launch_D_gather(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int64_t tbe, int64_t vbb, int64_t vbe,
-                     double coeff, const double* tmp, double* hm, int64_t ld, cudaStream_t s) {
+                     double coeff, const double* tmp, double* hm, int64_t ld, cudaStream_t s, bool rect) {
     ProfScope prof_("d_gather", s);
     const int64_t n = (tae - tab) * (vbe - vbb);
     d_gather_kernel<<<nblocks(n, 256), 256, 0, s>>>(tab, tae - tab, tbb, tbe - tbb, vbb, vbe - vbb, coeff, tmp,
-                                                    g.v2t_beg, g.v2t_tri, g.v2t_loc, g.tpos, g.nP, hm, ld);
+                                                    g.v2t_beg, g.v2t_tri, g.v2t_loc, g.tpos, g.nP, hm, ld,
+                                                    rect ? 1 : 0);
     check_launch("D gather");
 }
 
@@ -383,7 +387,7 @@ __global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e
                                int64_t t2b, int64_t t2e, int same, double coeff, const double* __restrict__ hm_src,
                                int64_t ld, const double* __restrict__ tmp, const int32_t* __restrict__ v2t_beg,
                                const int32_t* __restrict__ v2t_tri, const double* __restrict__ vq,
-                               const int32_t* __restrict__ tpos, int64_t nP, double* hm) {
+                               const int32_t* __restrict__ tpos, int64_t nP, double* hm, int rect) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= n1 * n2) return;
     const int64_t i1 = idx % n1, i2 = idx / n1;   // v1 fastest: coalesced writes down a column
@@ -443,17 +447,20 @@ __global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e
             }
         }
     }
-    hm[lower_at(nP + v1, nP + v2, ld)] += result * coeff;
+    if (rect)   // rectangular output: row = v1's unknown, column = v2 within its range
+        hm[(nP + v1) + i2 * ld] += result * coeff;
+    else
+        hm[lower_at(nP + v1, nP + v2, ld)] += result * coeff;
 }
 
 void launch_N_block(const DevGeom& g, int64_t v1b, int64_t v1e, int64_t t1b, int64_t t1e, int64_t v2b, int64_t v2e,
                     int64_t t2b, int64_t t2e, bool same, double coeff, const double* hm_src, int64_t ld,
-                    const double* tmp, double* hm, cudaStream_t s) {
+                    const double* tmp, double* hm, cudaStream_t s, bool rect) {
     const int64_t n = (v1e - v1b) * (v2e - v2b);
     ProfScope prof_("n_block", s);
     n_block_kernel<<<nblocks(n, 256), 256, 0, s>>>(v1b, v1e - v1b, t1b, t1e, v2b, v2e - v2b, t2b, t2e, same ? 1 : 0,
                                                    coeff, hm_src, ld, tmp, g.v2t_beg, g.v2t_tri, g.v2t_q, g.tpos, g.nP,
-                                                   hm);
+                                                   hm, rect ? 1 : 0);
     check_launch("N block");
 }
 
@@ -519,6 +526,24 @@ void launch_symmetrize_to_reference(const DevGeom& g, const double* hm_int, int6
     else
         to_reference_dense_kernel<<<grid, 256, 0, s>>>(g.Nref, g.nv, g.nP, hm_int, ld_int, out, ld_out);
     check_launch("to reference");
+}
+
+// Rows of an internal-numbered N_int x ncol block (column-major, ldi) to the
+// reference numbering [vertices | triangle unknowns], Nref x ncol (ldo).
+__global__ void rows_to_reference_kernel(int64_t Nref, int64_t nv, int64_t nP, int64_t ncol,
+                                         const double* __restrict__ in, int64_t ldi, double* out, int64_t ldo) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= Nref) return;
+    const int64_t a = r < nv ? nP + r : r - nv;
+    for (int64_t c = blockIdx.y; c < ncol; c += gridDim.y) out[r + c * ldo] = in[a + c * ldi];
+}
+
+void launch_rows_to_reference(const DevGeom& g, int64_t ncol, const double* in, int64_t ldi, double* out, int64_t ldo,
+                              cudaStream_t s) {
+    if (ncol <= 0 || g.Nref <= 0) return;
+    dim3 grid(nblocks(g.Nref, 256), (unsigned)std::min<int64_t>(ncol, 32768));
+    rows_to_reference_kernel<<<grid, 256, 0, s>>>(g.Nref, g.nv, g.nP, ncol, in, ldi, out, ldo);
+    check_launch("rows to reference");
 }
 
 // Reference-numbered dense (lower triangle read) -> internal lower triangle,
@@ -1321,7 +1346,7 @@ __global__ void ferguson_gather_kernel(const double* __restrict__ sq, int64_t np
                                        const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
                                        const int8_t* __restrict__ v2t_loc, const int32_t* __restrict__ tmesh,
                                        const double* __restrict__ jump, int64_t nP, int perm, double* out,
-                                       int64_t rs, int64_t cs, int64_t col0) {
+                                       int64_t rs, int64_t cs, int64_t col0, double mag) {
     const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t i = blockIdx.y;
     if (v >= nv || i >= np) return;
@@ -1333,7 +1358,7 @@ __global__ void ferguson_gather_kernel(const double* __restrict__ sq, int64_t np
         const double* s = srec + t * SREC;
         const d3 A = dev::ld3(s + 3 * ((loc + 1) % 3)), B = dev::ld3(s + 3 * ((loc + 2) % 3));
         res = res + (B - A) * (F[i * nt + t] / (2 * s[12]));
-        coeff = kMagFactor * jump[tmesh[t]];
+        coeff = jump ? mag * jump[tmesh[t]] : mag;
     }
     const d3 o = dev::ld3(sq + 6 * i + 3);
     out[(perm ? nP + v : v) * rs + (col0 + i) * cs] = dev::dot(res * coeff, o) / dev::norm(o);
@@ -1420,7 +1445,7 @@ void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand,
 }
 
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
-                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s) {
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s, double mag) {
     ProfScope prof_("h2mm", s);
     if (np == 0) return;
     dim3 grid(nblocks(g.nt, 128), (unsigned)np);
@@ -1428,7 +1453,7 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
     check_launch("Ferguson S");
     dim3 grid2(nblocks(g.nv, 128), (unsigned)np);
     ferguson_gather_kernel<<<grid2, 128, 0, s>>>(sq, np, g.nv, g.nt, F, g.srec, g.v2t_beg, g.v2t_tri, g.v2t_loc,
-                                                 tmesh, jump, g.nP, perm, out, rs, cs, col0);
+                                                 tmesh, jump, g.nP, perm, out, rs, cs, col0, mag);
     check_launch("Ferguson gather");
 }
 

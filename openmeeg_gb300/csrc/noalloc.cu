@@ -35,7 +35,8 @@
 
 namespace omg {
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
-                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s);
+                 double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s,
+                 double mag = kMagFactor);
 }
 
 static __device__ __align__(256) double g_h2mm_scratch[OMG_NOALLOC_SCRATCH_DOUBLES];

@@ -18,6 +18,10 @@ files) for a seeded workload of openmeeg_gb300.workloads:
                      MEG values its test suite compares against
                      (tests/analytic/eeg_head3_analytic.txt, meg_analytic.txt);
                      `--analytic-only` writes just this fixture
+  surface_sources    SurfSourceMat and SurfSource2MEGMat (om_assemble -SSM / -SS2MM)
+                     of a source icosphere (ico1, r = 0.5, off-centre) in the brain of
+                     small_ico1_3l and of small_ico1_4l_out; `--ssm-only` writes just
+                     this fixture
 """
 from __future__ import annotations
 
@@ -73,9 +77,36 @@ def save_head3_analytic():
     print("head3_analytic", {k: v.shape for k, v in d.items()})
 
 
+def save_surface_sources():
+    import subprocess
+    import tempfile
+    from openmeeg_gb300 import synthetic as syn
+    if not ref_runner.available():
+        ref_runner.build()
+    V, T = syn.icosphere(1, inward=False)
+    V = V * 0.5 + np.array([0.05, -0.03, 0.02])
+    d = {"src_vertices": V, "src_triangles": T}
+    for tag, w in (("3l", workloads.small(1, layers=3)), ("4l_out", workloads.small(1, layers=4, inward=False))):
+        wd = tempfile.mkdtemp()
+        ref_runner.write_head(wd, w.head, squids=w.squids)
+        io.write_tri(os.path.join(wd, "src.tri"), V, T)
+        for args in (["om_assemble", "-SSM", "head.geom", "head.cond", "src.tri", "ssm.bin"],
+                     ["om_assemble", "-SS2MM", "src.tri", "meg.txt", "ss2mm.bin"]):
+            subprocess.check_call([os.path.join(ref_runner.REF_BIN, args[0]), *args[1:]], cwd=wd,
+                                  stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        d[f"ssm_{tag}"] = io.read_bin(os.path.join(wd, "ssm.bin"))[1]
+        d[f"ss2mm_{tag}"] = io.read_bin(os.path.join(wd, "ss2mm.bin"))[1]
+        d[f"squids_{tag}"] = w.squids
+    np.savez_compressed(os.path.join(OUT, "surface_sources.npz"), **d)
+    print("surface_sources", {k: v.shape for k, v in d.items()})
+
+
 def main():
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
+        return
+    save_surface_sources()
+    if "--ssm-only" in sys.argv:
         return
     if not ref_runner.available():
         ref_runner.build()
