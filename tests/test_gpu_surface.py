@@ -30,4 +30,4 @@ def test_source_mesh_crossing_an_interface_is_rejected(cuda):
     geo = api.Geometry.from_head(w.head)
     V, T = syn.icosphere(1, inward=False)
     with pytest.raises(OMGError, match="crosses an interface"):
-        api.SurfSourceMat(geo, V * 0.9, T)      # straddles the inner surface (r = 0.87)
+        api.SurfSourceMat(geo, V * 0.3 + np.array([0.75, 0.0, 0.0]), T)   # straddles the inner surface (r = 0.87)
