@@ -242,6 +242,26 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
 int omg_surfsource2megmat_dev(omg_context ctx, const double* verts, int64_t n_verts, const int64_t* tris,
                               int64_t n_tris, const double* squids, int64_t n_squids, double* ss2mm);
 
+/* ---- internal potentials ----------------------------------------------------
+ * Points (device, n x 3) are located in the geometry's domains; those in a
+ * zero-conductivity domain are dropped, as the reference does, and the rest
+ * keep their input order.  *n_kept returns their count; out must hold
+ * n_points x columns doubles and receives an n_kept x columns column-major
+ * matrix (leading dimension n_kept).  A point in no domain is an error.
+ *
+ * Surf2VolMat (OpenMEEG/src/assembleHeadMat.cpp:325-363, assemble.h:33;
+ * PartialBlock, OpenMEEG/include/operators.h:302-331): columns are the Nref
+ * surface unknowns in the reference numbering. */
+int omg_surf2volmat_dev(omg_context ctx, omg_geometry geo, const double* points, int64_t n_points, double* out,
+                        int64_t* n_kept);
+/* DipSource2InternalPotMat (OpenMEEG/src/assembleSourceMat.cpp:154-187,
+ * assembleSourceMat.h:32): columns are the dipoles (device, n x 6); domain -1
+ * takes each dipole's own domain, domain >= 0 forces that domain index (the
+ * reference's domain_name argument). */
+int omg_dipsource2internalpotmat_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                                     const double* points, int64_t n_points, int32_t domain, double* out,
+                                     int64_t* n_kept);
+
 /* ---- batched forward (no reference counterpart) -----------------------------
  * Many head models, each with its own geometry, dipoles and sensors, computed
  * by one captured CUDA graph: every model's forward is the adjoint gain of

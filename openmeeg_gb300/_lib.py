@@ -126,6 +126,8 @@ _PROTOS = [
                               c_i64, P_dbl, c_i64, P_dbl, c_i64, P_dbl, P_dbl, ctypes.POINTER(GainStats)]),
     ("omg_surfsourcemat_dev", c_i32, [c_vp, c_vp, P_dbl, c_i64, P_i64, c_i64, ctypes.POINTER(Integrator), c_vp]),
     ("omg_surfsource2megmat_dev", c_i32, [c_vp, P_dbl, c_i64, P_i64, c_i64, c_vp, c_i64, c_vp]),
+    ("omg_surf2volmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, P_i64]),
+    ("omg_dipsource2internalpotmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, P_i64]),
     ("omg_batch_create", c_i32, [c_vp, c_i32, ctypes.POINTER(BatchModel), c_i32, c_i32, ctypes.POINTER(c_vp)]),
     ("omg_batch_run", c_i32, [c_vp]),
     ("omg_batch_gain_dev", c_i32, [c_vp, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp)]),

@@ -25,7 +25,8 @@ from ._lib import GainStats, GeometryInfo, Integrator, OMGError, check
 
 __all__ = ["Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
            "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
-           "GainEEGMEGadjoint", "forward_gain", "BatchForward", "SurfSourceMat", "SurfSource2MEGMat", "OMGError",
+           "GainEEGMEGadjoint", "forward_gain", "BatchForward", "SurfSourceMat", "SurfSource2MEGMat", "Surf2VolMat",
+           "DipSource2InternalPotMat", "OMGError",
            "kernel_launches"]
 
 FP64 = "fp64"
@@ -203,6 +204,15 @@ def HeadMatPacked(geom: Geometry, integrator: Optional[Integrator] = None) -> to
     return out
 
 
+def _domain_index(geom: Geometry, domain_name: str) -> int:
+    """-1 for "" (each source's own domain), else the index of the named domain."""
+    if not domain_name:
+        return -1
+    if geom.domain_names is None or domain_name not in geom.domain_names:
+        raise OMGError(-1, f"unknown domain {domain_name!r}")
+    return geom.domain_names.index(domain_name)
+
+
 def DipSourceMat(geom: Geometry, dipoles, integrator: Optional[Integrator] = None, domain_name: str = "",
                  adaptive: bool = True) -> torch.Tensor:
     """SourceMatrix<Dipole>(geo, dipoles, Integrator(3,10,0.001), domain) (assembleSourceMat.cpp:66-104).
@@ -213,11 +223,7 @@ def DipSourceMat(geom: Geometry, dipoles, integrator: Optional[Integrator] = Non
     N = geom.size
     out = torch.empty((n, N), dtype=torch.float64, device=_dev(ctx))   # column-major N x n
     it = _default(integrator, 3, 10 if adaptive else 0, 0.001)
-    dom = -1
-    if domain_name:
-        if geom.domain_names is None or domain_name not in geom.domain_names:
-            raise OMGError(-1, f"unknown domain {domain_name!r}")
-        dom = geom.domain_names.index(domain_name)
+    dom = _domain_index(geom, domain_name)
     check(ctx.lib.omg_dipsourcemat_dev(ctx.handle, geom.handle, _ptr(d), n, ctypes.byref(it), dom, _ptr(out)))
     return out.T
 
@@ -285,6 +291,39 @@ def SurfSource2MEGMat(vertices, triangles, squids, ctx: Optional[Context] = None
     check(ctx.lib.omg_surfsource2megmat_dev(ctx.handle, P(V, ctypes.c_double), V.shape[0], P(T, ctypes.c_int64),
                                             T.shape[0], _ptr(sq), sq.shape[0], _ptr(out)))
     return out.T
+
+
+def _kept_rows(buf: torch.Tensor, n_kept: int, cols: int) -> torch.Tensor:
+    """The n_kept x cols column-major matrix at the start of ``buf``."""
+    return buf[:n_kept * cols].view(cols, n_kept).T
+
+
+def Surf2VolMat(geom: Geometry, points) -> torch.Tensor:
+    """Surf2VolMat(geo, points) (assembleHeadMat.cpp:325-363): n_kept x N, the
+    potential at points inside the head from the surface unknowns.  Points in a
+    zero-conductivity domain are dropped (rows keep the input order)."""
+    ctx = geom.ctx
+    p = _as_dev(points, ctx, 3)
+    N = geom.size
+    buf = torch.empty(max(p.shape[0] * N, 1), dtype=torch.float64, device=_dev(ctx))
+    kept = ctypes.c_int64()
+    check(ctx.lib.omg_surf2volmat_dev(ctx.handle, geom.handle, _ptr(p), p.shape[0], _ptr(buf), ctypes.byref(kept)))
+    return _kept_rows(buf, kept.value, N)
+
+
+def DipSource2InternalPotMat(geom: Geometry, dipoles, points, domain_name: str = "") -> torch.Tensor:
+    """DipSource2InternalPotMat(geo, dipoles, points, domain_name) (assembleSourceMat.cpp:154-187):
+    n_kept x n_dipoles, the infinite-medium potential of each dipole at the
+    kept points of its domain."""
+    ctx = geom.ctx
+    d = _as_dev(dipoles, ctx, 6)
+    p = _as_dev(points, ctx, 3)
+    dom = _domain_index(geom, domain_name)
+    buf = torch.empty(max(p.shape[0] * d.shape[0], 1), dtype=torch.float64, device=_dev(ctx))
+    kept = ctypes.c_int64()
+    check(ctx.lib.omg_dipsource2internalpotmat_dev(ctx.handle, geom.handle, _ptr(d), d.shape[0], _ptr(p), p.shape[0],
+                                                   dom, _ptr(buf), ctypes.byref(kept)))
+    return _kept_rows(buf, kept.value, d.shape[0])
 
 
 class Solver:

@@ -40,6 +40,13 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
                  double mag = kMagFactor);
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
+void launch_partial_block(const DevGeom& g, int64_t p0, int64_t npc, const double* pts, const int* pdom,
+                          const int64_t* rows, const int32_t* tmesh, const int64_t* tidx_ref, const int* barrier,
+                          const int* orient, int maxb, const int* dnb, const int* bmesh, const int* binside,
+                          const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s);
+void launch_dipole_internal_pot(const double* pts, const int* pdom, const int64_t* rows, int64_t np, const double* dip,
+                                const int* ddom, int64_t nd, const double* dsigma, double* out, int64_t ldo,
+                                cudaStream_t s);
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s);
 void launch_dsm_vjp(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
                     const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
@@ -1251,6 +1258,95 @@ int omg_surfsource2megmat_dev(omg_context ctx, const double* verts, int64_t n_ve
             launch_h2mm(u.d, squids, n_squids, nullptr, nullptr, 0, ss2mm, n_squids, 1, 0, F.as<double>(), s, 1.0);
         }
         OMG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+// Domain of each point (Geometry::domain, geometry.cpp:146-154) and the
+// output row of the points kept: those in a conducting domain, in input order
+// (points in a zero-conductivity domain are dropped, assembleHeadMat.cpp:333-340).
+struct KeptPoints {
+    DevBuf dom, rows;
+    int64_t kept = 0;
+};
+static void keep_conducting_points(KeptPoints& kp, omg_geometry geo, const double* pts, int64_t n, cudaStream_t s) {
+    const HostGeometry& h = geo->h;
+    kp.dom = DevBuf((size_t)std::max<int64_t>(n, 1) * sizeof(int), s);
+    kp.rows = DevBuf((size_t)std::max<int64_t>(n, 1) * sizeof(int64_t), s);
+    kp.kept = 0;
+    if (n == 0) return;
+    DevBuf sa((size_t)n * h.nmesh * 8, s);
+    launch_mesh_solid_angles(pts, 3, n, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+    launch_domain_lookup(n, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh, geo->binside,
+                         geo->orient, -1, kp.dom.as<int>(), geo->ctx->d_err, s);
+    check_err(geo->ctx, "point domain lookup");
+    std::vector<int> hdom(n);
+    OMG_CUDA(cudaMemcpyAsync(hdom.data(), kp.dom.p, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+    OMG_CUDA(cudaStreamSynchronize(s));
+    std::vector<int64_t> rows(n);
+    for (int64_t i = 0; i < n; ++i) {
+        OMG_REQUIRE(hdom[i] >= 0, "a point lies in no domain of the geometry");
+        rows[i] = h.domains[hdom[i]].sigma != 0.0 ? kp.kept++ : -1;
+    }
+    OMG_CUDA(cudaMemcpyAsync(kp.rows.p, rows.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    OMG_CUDA(cudaStreamSynchronize(s));   // the host vector goes out of scope
+}
+
+// Surf2VolMat (OpenMEEG/src/assembleHeadMat.cpp:325-363): potential at points
+// inside the head from the surface unknowns; n_kept x Nref, column-major with
+// leading dimension n_kept, columns in the reference numbering.
+int omg_surf2volmat_dev(omg_context ctx, omg_geometry geo, const double* points, int64_t n_points, double* out,
+                        int64_t* n_kept) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && n_kept && (n_points == 0 || (points && out)), "null argument");
+        OMG_REQUIRE(n_points >= 0, "negative point count");
+        set_device(ctx);
+        cudaStream_t s = ctx->stream;
+        reset_err(ctx);
+        KeptPoints kp;
+        keep_conducting_points(kp, geo, points, n_points, s);
+        *n_kept = kp.kept;
+        const int64_t ld = kp.kept, Nref = geo->d.Nref;
+        if (kp.kept == 0) return;
+        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)ld * Nref * 8, s));
+        // chunk the points so the P1 scratch stays near 512 MB
+        const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (geo->h.nt * 24)));
+        DevBuf p1((size_t)std::min(per, n_points) * geo->h.nt * 24, s);
+        for (int64_t p0 = 0; p0 < n_points; p0 += per)
+            launch_partial_block(geo->d, p0, std::min(per, n_points - p0), points, kp.dom.as<int>(),
+                                 kp.rows.as<int64_t>(), geo->tmesh, geo->tidx_ref, geo->barrier, geo->orient,
+                                 geo->maxb, geo->dnb, geo->bmesh, geo->binside, geo->dsigma, p1.as<double>(), out, ld,
+                                 s);
+        check_err(ctx, "Surf2VolMat");
+    });
+}
+
+// DipSource2InternalPotMat (OpenMEEG/src/assembleSourceMat.cpp:154-187):
+// n_kept x n_dipoles, column-major with leading dimension n_kept.  domain >= 0
+// places every dipole in that domain (the reference's domain_name argument).
+int omg_dipsource2internalpotmat_dev(omg_context ctx, omg_geometry geo, const double* dipoles, int64_t n_dipoles,
+                                     const double* points, int64_t n_points, int32_t domain, double* out,
+                                     int64_t* n_kept) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && n_kept && (n_points == 0 || points) && (n_dipoles == 0 || dipoles),
+                    "null argument");
+        OMG_REQUIRE(n_points >= 0 && n_dipoles >= 0, "negative size");
+        OMG_REQUIRE(domain >= -1 && domain < geo->ndom, "domain index out of range");
+        set_device(ctx);
+        cudaStream_t s = ctx->stream;
+        reset_err(ctx);
+        KeptPoints kp;
+        keep_conducting_points(kp, geo, points, n_points, s);
+        *n_kept = kp.kept;
+        if (kp.kept == 0 || n_dipoles == 0) return;
+        OMG_REQUIRE(out, "null argument");
+        const HostGeometry& h = geo->h;
+        DevBuf sa((size_t)n_dipoles * h.nmesh * 8, s), ddom((size_t)n_dipoles * sizeof(int), s);
+        launch_mesh_solid_angles(dipoles, 6, n_dipoles, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+        launch_domain_lookup(n_dipoles, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
+                             geo->binside, geo->orient, domain, ddom.as<int>(), ctx->d_err, s);
+        launch_dipole_internal_pot(points, kp.dom.as<int>(), kp.rows.as<int64_t>(), n_points, dipoles, ddom.as<int>(),
+                                   n_dipoles, geo->dsigma, out, kp.kept, s);
+        check_err(ctx, "DipSource2InternalPotMat");
     });
 }
 

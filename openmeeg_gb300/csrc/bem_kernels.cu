@@ -1668,4 +1668,116 @@ void launch_dsm_vjp(const DevGeom& g, int64_t dip0, int64_t ndc, const double* d
     check_launch("DSM vjp reduce");
 }
 
+// ---------------------------------------------------------------------------
+// Internal potentials.  Surf2VolMat (assembleHeadMat.cpp:325-363) through
+// PartialBlock (operators.h:302-331): for a point x in a conducting domain and
+// every mesh m bounding that domain, with c = K * mesh_orientation(domain, m)
+// (domain.h:43-45),
+//   row(x), vertex columns   += -c * P1SingleLayerPotential(triangle)(x)[k]
+//   row(x), triangle column   =  c / sigma * OperatorS(triangle)(x)   (no current barrier)
+// One thread per (triangle, point): the three P1 integrals go to a per-point
+// scratch row (zero where the triangle's mesh does not bound the point's
+// domain) and the S value straight to its column; a second pass sums the
+// scratch over each vertex's triangles in triangle order, as the reference's
+// loop accumulates them.  Rows are the kept points (rows[i] >= 0).
+// ---------------------------------------------------------------------------
+__global__ void partial_block_kernel(int64_t p0, int64_t npc, const double* __restrict__ pts,
+                                     const int* __restrict__ pdom, const int64_t* __restrict__ rows, int64_t nt,
+                                     const double* __restrict__ srec, const double* __restrict__ prec,
+                                     const int32_t* __restrict__ tmesh, const int64_t* __restrict__ tidx_ref,
+                                     const int* __restrict__ barrier, const int* __restrict__ orient, int maxb,
+                                     const int* __restrict__ dnb, const int* __restrict__ bmesh,
+                                     const int* __restrict__ binside, const double* __restrict__ dsigma,
+                                     double* __restrict__ p1tmp, double* out, int64_t ldo) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t il = blockIdx.y;
+    if (t >= nt || il >= npc) return;
+    const int64_t i = p0 + il;
+    double* o3 = p1tmp + (il * nt + t) * 3;
+    o3[0] = o3[1] = o3[2] = 0.0;
+    const int64_t row = rows[i];
+    if (row < 0) return;
+    const int d = pdom[i];
+    const int m = tmesh[t];
+    double c = 0.0;
+    bool on = false;
+    for (int k = 0; k < dnb[d]; ++k)
+        if (bmesh[d * maxb + k] == m) {
+            c = (binside[d * maxb + k] ? kK : -kK) * orient[m];
+            on = true;
+        }
+    if (!on) return;
+    const d3 x = dev::ld3(pts + 3 * i);
+    double v[3];
+    dev::p1_single_layer(prec + t * PREC, x, v);
+    o3[0] = v[0] * -c;
+    o3[1] = v[1] * -c;
+    o3[2] = v[2] * -c;
+    if (!barrier[m]) out[row + tidx_ref[t] * ldo] = (c / dsigma[d]) * dev::operator_S(srec + t * SREC, x);
+}
+
+__global__ void partial_block_gather_kernel(int64_t p0, int64_t npc, const int64_t* __restrict__ rows, int64_t nv,
+                                            int64_t nt, const double* __restrict__ p1tmp,
+                                            const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
+                                            const int8_t* __restrict__ v2t_loc, double* out, int64_t ldo) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t il = blockIdx.y;
+    if (v >= nv || il >= npc) return;
+    const int64_t row = rows[p0 + il];
+    if (row < 0) return;
+    double sum = 0.0;
+    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) sum += p1tmp[(il * nt + v2t_tri[k]) * 3 + v2t_loc[k]];
+    out[row + v * ldo] = sum;
+}
+
+void launch_partial_block(const DevGeom& g, int64_t p0, int64_t npc, const double* pts, const int* pdom,
+                          const int64_t* rows, const int32_t* tmesh, const int64_t* tidx_ref, const int* barrier,
+                          const int* orient, int maxb, const int* dnb, const int* bmesh, const int* binside,
+                          const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s) {
+    if (npc == 0) return;
+    ProfScope prof_("partial_block", s);
+    dim3 grid(nblocks(g.nt, 128), (unsigned)npc);
+    partial_block_kernel<<<grid, 128, 0, s>>>(p0, npc, pts, pdom, rows, g.nt, g.srec, g.prec, tmesh, tidx_ref,
+                                              barrier, orient, maxb, dnb, bmesh, binside, dsigma, p1tmp, out, ldo);
+    check_launch("partial block");
+    dim3 grid2(nblocks(g.nv, 128), (unsigned)npc);
+    partial_block_gather_kernel<<<grid2, 128, 0, s>>>(p0, npc, rows, g.nv, g.nt, p1tmp, g.v2t_beg, g.v2t_tri,
+                                                      g.v2t_loc, out, ldo);
+    check_launch("partial block gather");
+}
+
+// DipSource2InternalPotMat (assembleSourceMat.cpp:154-187): the infinite-medium
+// potential K / sigma * q.(x - r0) / |x - r0|^3 (dipole.h:29-36) of each
+// dipole at each kept point that shares its domain, zero elsewhere.
+__global__ void dipole_internal_pot_kernel(const double* __restrict__ pts, const int* __restrict__ pdom,
+                                           const int64_t* __restrict__ rows, int64_t np,
+                                           const double* __restrict__ dip, const int* __restrict__ ddom, int64_t nd,
+                                           const double* __restrict__ dsigma, double* out, int64_t ldo) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const int64_t row = rows[i];
+    if (row < 0) return;
+    const int d = pdom[i];
+    const d3 x = dev::ld3(pts + 3 * i);
+    for (int64_t j = blockIdx.y; j < nd; j += gridDim.y) {
+        double val = 0.0;
+        if (ddom[j] == d) {
+            const d3 r = x - dev::ld3(dip + 6 * j);
+            const double n2 = dev::dot(r, r);
+            val = (kK / dsigma[d]) * (dev::dot(dev::ld3(dip + 6 * j + 3), r) / (n2 * sqrt(n2)));
+        }
+        out[row + j * ldo] = val;
+    }
+}
+
+void launch_dipole_internal_pot(const double* pts, const int* pdom, const int64_t* rows, int64_t np, const double* dip,
+                                const int* ddom, int64_t nd, const double* dsigma, double* out, int64_t ldo,
+                                cudaStream_t s) {
+    if (np == 0 || nd == 0) return;
+    ProfScope prof_("dipole_internal_pot", s);
+    dim3 grid(nblocks(np, 128), (unsigned)std::min<int64_t>(nd, 32768));
+    dipole_internal_pot_kernel<<<grid, 128, 0, s>>>(pts, pdom, rows, np, dip, ddom, nd, dsigma, out, ldo);
+    check_launch("dipole internal potential");
+}
+
 }  // namespace omg

@@ -551,6 +551,42 @@ int oo_dsm(const oo_geom* g, const double* dip, int64_t ndip, const int* dom_nb,
     return 0;
 }
 
+/* Surf2VolMat (assembleHeadMat.cpp:325-363) through PartialBlock::addD and
+ * PartialBlock::S (operators.h:302-331).  Point i (already kept: conducting
+ * domain) sees the boundary meshes mesh[i*maxb + k], k < nb[i], each with
+ * c = K * mesh_orientation (domain.h:43-45):
+ *   out(i, vertex unknowns) += -c * P1SingleLayerPotential(triangle)(x)
+ *   out(i, triangle unknown)  =  c / cond * OperatorS(triangle)(x)   (no barrier)
+ * out is np x N, column-major. */
+int oo_surf2vol(const oo_geom* g, const double* pts, int64_t np, const int* nb, const int* mesh,
+                const double* coeff, const double* cond, int maxb, double* out) {
+    tri_t* tris = (tri_t*)malloc(sizeof(tri_t) * (size_t)g->nt);
+    for (int64_t t = 0; t < g->nt; ++t) make_tri(g, t, &tris[t]);
+    memset(out, 0, sizeof(double) * (size_t)(np * g->N));
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < np; ++i) {
+        v3 x = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        for (int k = 0; k < nb[i]; ++k) {
+            const int m = mesh[(size_t)i * maxb + k];
+            const double c = coeff[(size_t)i * maxb + k];
+            for (int64_t t = g->mesh_tbeg[m]; t < g->mesh_tbeg[m + 1]; ++t) {
+                p1_t P;
+                p1_make(&P, &tris[t]);
+                const v3 I = p1_eval(&P, x);
+                const double Ij[3] = {I.x, I.y, I.z};
+                for (int j = 0; j < 3; ++j) out[i + np * g->vidx[g->T[3 * t + j]]] += Ij[j] * -c;
+                if (!g->barrier[m]) {
+                    opS_t S;
+                    opS_make(&S, &tris[t]);
+                    out[i + np * g->tidx[t]] = c / cond[i] * opS_eval(&S, x);
+                }
+            }
+        }
+    }
+    free(tris);
+    return 0;
+}
+
 /* Total solid angle of each mesh seen from each point (Mesh::solid_angle,
  * mesh.cpp:239-244); out is npts x nmesh.  Used for Domain::contains. */
 int oo_mesh_solid_angles(const oo_geom* g, const double* pts, int64_t npts, double* out) {

@@ -373,6 +373,53 @@ def dsm(g: OracleGeometry, dipoles: np.ndarray, order=3, levels=10, tol=0.001) -
     return out.T.copy()
 
 
+def _kept_points(g: OracleGeometry, points: np.ndarray):
+    """Points outside zero-conductivity domains, in input order
+    (assembleHeadMat.cpp:331-340, assembleSourceMat.cpp:158-170), with the
+    index of the domain of each (Geometry::domain, geometry.cpp:146-154)."""
+    pts = np.ascontiguousarray(points, np.float64)[:, :3]
+    sas = mesh_solid_angles(g, pts)
+    doms = np.array([g.domain_of_point(pts[i], sas[i]) for i in range(pts.shape[0])], np.int64)
+    keep = np.array([g.domains[d][2] != 0.0 for d in doms], bool)
+    return np.ascontiguousarray(pts[keep]), doms[keep]
+
+
+def surf2volmat(g: OracleGeometry, points: np.ndarray) -> np.ndarray:
+    """Surf2VolMat (assembleHeadMat.cpp:325-363): n_kept x N."""
+    pts, _ = _kept_points(g, points)
+    nb, mesh, coeffD, cond, maxb = dipole_domains(g, pts)
+    n = pts.shape[0]
+    out = np.zeros((g.N, n))   # column-major n x N
+    gs = g.c_struct()
+    # K * mesh_orientation (domain.h:43-45) is the opposite of the DipSourceMat's factorD * orientation
+    lib().oo_surf2vol(ctypes.byref(gs), _ptr(pts), ctypes.c_int64(n), _ptr(nb), _ptr(np.ascontiguousarray(mesh)),
+                      _ptr(np.ascontiguousarray(-coeffD)), _ptr(cond), ctypes.c_int(maxb), _ptr(out))
+    return out.T.copy()
+
+
+def dipsource2internalpotmat(g: OracleGeometry, dipoles: np.ndarray, points: np.ndarray,
+                             domain_name: str = "") -> np.ndarray:
+    """DipSource2InternalPotMat (assembleSourceMat.cpp:154-187): n_kept x n_dipoles,
+    K / sigma * q.(x - r0) / |x - r0|^3 (dipole.h:29-36) where point and dipole
+    share a domain."""
+    pts, pdom = _kept_points(g, points)
+    dip = np.asarray(dipoles, np.float64)
+    if domain_name:
+        ddom = np.full(dip.shape[0], [d[0] for d in g.domains].index(domain_name))
+    else:
+        sas = mesh_solid_angles(g, np.ascontiguousarray(dip[:, :3]))
+        ddom = np.array([g.domain_of_point(dip[j, :3], sas[j]) for j in range(dip.shape[0])])
+    out = np.zeros((pts.shape[0], dip.shape[0]))
+    for j in range(dip.shape[0]):
+        coeff = K / g.domains[ddom[j]][2]
+        for i in range(pts.shape[0]):
+            if pdom[i] == ddom[j]:
+                x = pts[i] - dip[j, :3]
+                n2 = float(x @ x)
+                out[i, j] += coeff * (float(dip[j, 3:6] @ x) / (n2 * np.sqrt(n2)))
+    return out
+
+
 def h2em(g: OracleGeometry, electrodes: np.ndarray) -> np.ndarray:
     """Dense n_e x N Head2EEGMat (the reference stores it sparse)."""
     pos = np.ascontiguousarray(electrodes[:, :3], np.float64)

@@ -18,6 +18,10 @@ files) for a seeded workload of openmeeg_gb300.workloads:
                      MEG values its test suite compares against
                      (tests/analytic/eeg_head3_analytic.txt, meg_analytic.txt);
                      `--analytic-only` writes just this fixture
+  internal_potentials Surf2VolMat and DipSource2InternalPotMat (om_assemble -H2IPM /
+                     -DS2IPM, own domains and a forced one) at points in every layer
+                     and in the air of small_ico1_3l and small_ico1_4l_out;
+                     `--ipm-only` writes just this fixture (and head3_analytic)
   surface_sources    SurfSourceMat and SurfSource2MEGMat (om_assemble -SSM / -SS2MM)
                      of a source icosphere (ico1, r = 0.5, off-centre) in the brain of
                      small_ico1_3l and of small_ico1_4l_out; `--ssm-only` writes just
@@ -101,9 +105,58 @@ def save_surface_sources():
     print("surface_sources", {k: v.shape for k, v in d.items()})
 
 
+def internal_points(head, radii, seed, n_dirs=5):
+    """Points along vertex directions of the innermost mesh (where every nested
+    icosphere reaches its nominal radius, so a radius between two surfaces
+    names the layer) at each radius, plus a few generic points deep in the
+    innermost layer; shuffled so that dropped points sit between kept ones."""
+    rng = np.random.default_rng(seed)
+    V0 = head.vertices[0]
+    dirs = V0[rng.choice(len(V0), n_dirs, replace=False)]
+    dirs = dirs / np.linalg.norm(dirs, axis=1, keepdims=True)
+    P = [d * r for d in dirs for r in radii]
+    g = rng.standard_normal((4, 3))
+    P += list(g / np.linalg.norm(g, axis=1, keepdims=True) * 0.4)
+    P = np.array(P)
+    return P[rng.permutation(len(P))]
+
+
+def save_internal_potentials():
+    """Surf2VolMat (om_assemble -H2IPM) and DipSource2InternalPotMat
+    (-DS2IPM, with and without a forced domain) on two small heads."""
+    import subprocess
+    import tempfile
+    if not ref_runner.available():
+        ref_runner.build()
+    d = {}
+    cases = (("3l", workloads.small(1, layers=3), [0.3, 0.6, 0.895, 0.96, 1.1], "Scalp"),
+             ("4l_out", workloads.small(1, layers=4, inward=False), [0.5, 0.865, 0.9, 0.96, 1.2], "CSF"))
+    for k, (tag, w, radii, forced) in enumerate(cases):
+        wd = tempfile.mkdtemp()
+        ref_runner.write_head(wd, w.head, dipoles=w.dipoles)
+        pts = internal_points(w.head, radii, workloads.SEED + 40 + k)
+        io.write_matrix_txt(os.path.join(wd, "pts.txt"), pts)
+        for args in (["om_assemble", "-H2IPM", "head.geom", "head.cond", "pts.txt", "h2ipm.bin"],
+                     ["om_assemble", "-DS2IPM", "head.geom", "head.cond", "dip.txt", "pts.txt", "ds2ipm.bin"],
+                     ["om_assemble", "-DS2IPM", "head.geom", "head.cond", "dip.txt", "pts.txt", "ds2ipm_f.bin",
+                      forced]):
+            subprocess.check_call([os.path.join(ref_runner.REF_BIN, args[0]), *args[1:]], cwd=wd,
+                                  stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        d[f"points_{tag}"] = pts
+        d[f"h2ipm_{tag}"] = io.read_bin(os.path.join(wd, "h2ipm.bin"))[1]
+        d[f"ds2ipm_{tag}"] = io.read_bin(os.path.join(wd, "ds2ipm.bin"))[1]
+        d[f"ds2ipm_forced_{tag}"] = io.read_bin(os.path.join(wd, "ds2ipm_f.bin"))[1]
+        d[f"forced_{tag}"] = np.array(forced)
+    np.savez_compressed(os.path.join(OUT, "internal_potentials.npz"), **d)
+    print("internal_potentials", {k: v.shape for k, v in d.items()})
+
+
 def main():
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
+        return
+    save_internal_potentials()
+    if "--ipm-only" in sys.argv:
         return
     save_surface_sources()
     if "--ssm-only" in sys.argv:

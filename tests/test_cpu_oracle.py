@@ -51,6 +51,24 @@ def test_oracle_sources_sensors_gains_pinned_to_reference(name):
     assert rel(oracle.gain_meg(HM, D, M, S), G["meg"]) < 1e-12
 
 
+@pytest.mark.parametrize("tag,layers,inward", [("3l", 3, True), ("4l_out", 4, False)])
+def test_oracle_internal_potentials_pinned_to_reference(tag, layers, inward):
+    """Surf2VolMat and DipSource2InternalPotMat (own domains and a forced one)
+    against om_assemble -H2IPM / -DS2IPM; points in the air are dropped."""
+    from oracle import oracle
+    from openmeeg_gb300 import workloads
+    G = golden("internal_potentials")
+    w = workloads.small(1, layers=layers, inward=inward)
+    g = oracle.digest(w.head)
+    pts = G[f"points_{tag}"]
+    H = oracle.surf2volmat(g, pts)
+    assert H.shape == G[f"h2ipm_{tag}"].shape and H.shape[0] < pts.shape[0]
+    assert rel(H, G[f"h2ipm_{tag}"]) < 1e-14
+    assert rel(oracle.dipsource2internalpotmat(g, w.dipoles, pts), G[f"ds2ipm_{tag}"]) < 1e-14
+    forced = str(G[f"forced_{tag}"])
+    assert rel(oracle.dipsource2internalpotmat(g, w.dipoles, pts, forced), G[f"ds2ipm_forced_{tag}"]) < 1e-14
+
+
 def test_oracle_numbering_and_pairs():
     """Unknown count and mesh pairs of nested heads (geometry.cpp:256-295, 405-420)."""
     from oracle import oracle
