@@ -262,6 +262,14 @@ int omg_dipsource2internalpotmat_dev(omg_context ctx, omg_geometry geo, const do
                                      const double* points, int64_t n_points, int32_t domain, double* out,
                                      int64_t* n_kept);
 
+/* EITSourceMat (OpenMEEG/src/assembleSourceMat.cpp:109-152, assembleSourceMat.h:31):
+ * electrode positions (device, n x 3) and radii (device, n; NULL for point
+ * electrodes); the injection triangles and weights follow
+ * Sensors::findInjectionTriangles (OpenMEEG/src/sensors.cpp:167-215).  out is
+ * Nref x n_electrodes, column-major.  Default integrator (3, 0, 0.005). */
+int omg_eitsourcemat_dev(omg_context ctx, omg_geometry geo, const double* positions, const double* radii,
+                         int64_t n_electrodes, const omg_integrator* integ, double* out);
+
 /* ---- batched forward (no reference counterpart) -----------------------------
  * Many head models, each with its own geometry, dipoles and sensors, computed
  * by one captured CUDA graph: every model's forward is the adjoint gain of

@@ -10,7 +10,7 @@ __version__ = "0.1.0"
 _API_NAMES = {"Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
               "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
               "GainEEGMEGadjoint", "forward_gain", "BatchForward", "SurfSourceMat", "SurfSource2MEGMat", "Surf2VolMat",
-              "DipSource2InternalPotMat", "OMGError",
+              "DipSource2InternalPotMat", "EITSourceMat", "OMGError",
               "kernel_launches"}
 
 

@@ -128,6 +128,7 @@ _PROTOS = [
     ("omg_surfsource2megmat_dev", c_i32, [c_vp, P_dbl, c_i64, P_i64, c_i64, c_vp, c_i64, c_vp]),
     ("omg_surf2volmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, P_i64]),
     ("omg_dipsource2internalpotmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, P_i64]),
+    ("omg_eitsourcemat_dev", c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, ctypes.POINTER(Integrator), c_vp]),
     ("omg_batch_create", c_i32, [c_vp, c_i32, ctypes.POINTER(BatchModel), c_i32, c_i32, ctypes.POINTER(c_vp)]),
     ("omg_batch_run", c_i32, [c_vp]),
     ("omg_batch_gain_dev", c_i32, [c_vp, c_i32, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp)]),

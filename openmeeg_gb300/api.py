@@ -26,7 +26,7 @@ from ._lib import GainStats, GeometryInfo, Integrator, OMGError, check
 __all__ = ["Context", "Geometry", "Integrator", "HeadMat", "HeadMatPacked", "DipSourceMat", "Head2EEGMat",
            "Head2MEGMat", "DipSource2MEGMat", "Solver", "GainEEG", "GainMEG", "GainEEGadjoint", "GainMEGadjoint",
            "GainEEGMEGadjoint", "forward_gain", "BatchForward", "SurfSourceMat", "SurfSource2MEGMat", "Surf2VolMat",
-           "DipSource2InternalPotMat", "OMGError",
+           "DipSource2InternalPotMat", "EITSourceMat", "OMGError",
            "kernel_launches"]
 
 FP64 = "fp64"
@@ -324,6 +324,23 @@ def DipSource2InternalPotMat(geom: Geometry, dipoles, points, domain_name: str =
     check(ctx.lib.omg_dipsource2internalpotmat_dev(ctx.handle, geom.handle, _ptr(d), d.shape[0], _ptr(p), p.shape[0],
                                                    dom, _ptr(buf), ctypes.byref(kept)))
     return _kept_rows(buf, kept.value, d.shape[0])
+
+
+def EITSourceMat(geom: Geometry, electrodes, integrator: Optional[Integrator] = None) -> torch.Tensor:
+    """EITSourceMat(geo, electrodes, integrator) (assembleSourceMat.cpp:109-152): N x n_electrodes.
+    ``electrodes`` is n x 3 (point electrodes) or n x 4 (x, y, z, radius), as
+    the columns of an EIT sensors file (sensors.cpp:99-108)."""
+    ctx = geom.ctx
+    e = _as_dev(electrodes, ctx)
+    if e.ndim != 2 or e.shape[1] not in (3, 4):
+        raise OMGError(-1, "electrodes must be n x 3 or n x 4 (x, y, z, radius)")
+    pos = e[:, :3].contiguous()
+    rad = e[:, 3].contiguous() if e.shape[1] == 4 else None
+    it = _default(integrator, 3, 0, 0.005)
+    out = torch.empty((e.shape[0], geom.size), dtype=torch.float64, device=_dev(ctx))   # column-major
+    check(ctx.lib.omg_eitsourcemat_dev(ctx.handle, geom.handle, _ptr(pos), _ptr(rad), e.shape[0], ctypes.byref(it),
+                                       _ptr(out)))
+    return out.T
 
 
 class Solver:

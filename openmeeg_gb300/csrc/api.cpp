@@ -44,6 +44,13 @@ void launch_partial_block(const DevGeom& g, int64_t p0, int64_t npc, const doubl
                           const int64_t* rows, const int32_t* tmesh, const int64_t* tidx_ref, const int* barrier,
                           const int* orient, int maxb, const int* dnb, const int* bmesh, const int* binside,
                           const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s);
+void launch_nearest_triangle(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand,
+                             int64_t* out_tri, cudaStream_t s);
+void launch_eit_rows(const DevGeom& g, const int64_t* inj, int64_t nk, int64_t t2b, int64_t t2e, int64_t vb,
+                     int64_t ve, bool self, bool withS, double coeffD, double coeffS, const int64_t* tidx_ref,
+                     int order, double* tmp, double* R, cudaStream_t s);
+void launch_eit_combine(int64_t Nref, int64_t ne, const int64_t* ebeg, const int64_t* eid, const double* ecoef,
+                        int64_t k0, int64_t nk, const double* R, double* out, cudaStream_t s);
 void launch_dipole_internal_pot(const double* pts, const int* pdom, const int64_t* rows, int64_t np, const double* dip,
                                 const int* ddom, int64_t nd, const double* dsigma, double* out, int64_t ldo,
                                 cudaStream_t s);
@@ -1347,6 +1354,168 @@ int omg_dipsource2internalpotmat_dev(omg_context ctx, omg_geometry geo, const do
         launch_dipole_internal_pot(points, kp.dom.as<int>(), kp.rows.as<int64_t>(), n_points, dipoles, ddom.as<int>(),
                                    n_dipoles, geo->dsigma, out, kp.kept, s);
         check_err(ctx, "DipSource2InternalPotMat");
+    });
+}
+
+// Injection triangles of EIT electrodes (Sensors::findInjectionTriangles,
+// sensors.cpp:167-215): the nearest triangle of the interfaces touching a
+// zero-conductivity domain, and for an electrode of radius r > 0 whose nearest
+// triangle is smaller than 4 pi r^2, a depth-first walk over neighbouring
+// triangles whose centres lie within r.  The walk follows the first three
+// entries of Mesh::adjacent_triangles (mesh.h:164-172): the triangles met twice
+// while scanning the incidence lists (triangle order) of the triangle's
+// vertices -- which include the triangle itself, so one edge neighbour is
+// left out, as in the reference.  Weight pi r^2 / (area of the triangles)
+// for r > 0; 1 / area for a point electrode (assembleSourceMat.cpp:141-150).
+struct Injection {
+    std::vector<int64_t> tri;
+    std::vector<double> coef;
+};
+static std::vector<Injection> injection_triangles(const HostGeometry& h, const std::vector<double>& pos,
+                                                  const std::vector<double>& radii,
+                                                  const std::vector<int64_t>& nearest) {
+    const double pi = 3.14159265358979323846;
+    auto vtx = [&](int64_t v) { return &h.V[3 * v]; };
+    auto area = [&](int64_t t) {
+        const double *a = vtx(h.T[3 * t]), *b = vtx(h.T[3 * t + 1]), *c = vtx(h.T[3 * t + 2]);
+        const double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, w[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        const double n[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+        return std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) / 2.0;
+    };
+    auto mesh_of = [&](int64_t t) {
+        return (int)(std::upper_bound(h.tbeg.begin(), h.tbeg.end(), t) - h.tbeg.begin()) - 1;
+    };
+    auto adjacent = [&](int64_t t) {
+        const int m = mesh_of(t);
+        std::vector<std::pair<int64_t, int>> cnt;
+        std::vector<int64_t> res;
+        for (int j = 0; j < 3; ++j) {
+            const int64_t v = h.T[3 * t + j];
+            for (int q = h.v2t_beg[v]; q < h.v2t_beg[v + 1]; ++q) {
+                const int64_t t2 = h.v2t_tri[q];
+                if (t2 < h.tbeg[m] || t2 >= h.tbeg[m + 1]) continue;
+                auto it = std::find_if(cnt.begin(), cnt.end(), [&](const auto& c) { return c.first == t2; });
+                if (it == cnt.end()) {
+                    cnt.push_back({t2, 1});
+                } else if (++it->second == 2) {
+                    res.push_back(t2);
+                }
+            }
+        }
+        return res;
+    };
+    const size_t ne = nearest.size();
+    std::vector<Injection> out(ne);
+    for (size_t e = 0; e < ne; ++e) {
+        const int64_t t0 = nearest[e];
+        OMG_REQUIRE(t0 >= 0, "no interface touches a zero-conductivity domain");
+        const double r = radii[e];
+        const bool point = std::fabs(r) < 2.2250738585072014e-308;   // almost_equal(radius, 0.0)
+        std::vector<int64_t> tris{t0};
+        if (!point && area(t0) < 4 * pi * r * r) {
+            std::vector<int64_t> seen{t0}, stack{t0};
+            while (!stack.empty()) {
+                const int64_t t = stack.back();
+                stack.pop_back();
+                const double *a = vtx(h.T[3 * t]), *b = vtx(h.T[3 * t + 1]), *c = vtx(h.T[3 * t + 2]);
+                const double d[3] = {(a[0] + b[0] + c[0]) / 3.0 - pos[3 * e], (a[1] + b[1] + c[1]) / 3.0 - pos[3 * e + 1],
+                                     (a[2] + b[2] + c[2]) / 3.0 - pos[3 * e + 2]};
+                if (std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < r) {
+                    if (t != t0) tris.push_back(t);
+                    const std::vector<int64_t> adj = adjacent(t);
+                    for (size_t i = 0; i < std::min<size_t>(3, adj.size()); ++i)
+                        if (std::find(seen.begin(), seen.end(), adj[i]) == seen.end()) {
+                            seen.push_back(adj[i]);
+                            stack.push_back(adj[i]);
+                        }
+                }
+            }
+        }
+        out[e].tri = tris;
+        if (point) {
+            for (int64_t t : tris) out[e].coef.push_back(1.0 / area(t));
+        } else {
+            double tot = 0.0;
+            for (int64_t t : tris) tot += area(t);
+            out[e].coef.assign(tris.size(), pi * r * r / tot);
+        }
+    }
+    return out;
+}
+
+// EITSourceMat (OpenMEEG/src/assembleSourceMat.cpp:109-152): Nref x n_electrodes,
+// column-major; only the transfer-matrix rows of the injection triangles are formed.
+int omg_eitsourcemat_dev(omg_context ctx, omg_geometry geo, const double* positions, const double* radii,
+                         int64_t n_electrodes, const omg_integrator* integ, double* out) {
+    return guarded([&] {
+        OMG_REQUIRE(ctx && geo && (n_electrodes == 0 || (positions && out)), "null argument");
+        OMG_REQUIRE(n_electrodes >= 0, "negative electrode count");
+        set_device(ctx);
+        const omg_integrator it = integ ? *integ : default_hm_integrator();
+        check_integrator(it, false);
+        cudaStream_t s = ctx->stream;
+        reset_err(ctx);
+        const HostGeometry& h = geo->h;
+        const int64_t Nref = geo->d.Nref, ne = n_electrodes;
+        if (ne == 0) return;
+        OMG_REQUIRE(geo->n_eeg_cand > 0, "no interface touches a zero-conductivity domain");
+        ensure_order(geo, it.order);
+        std::vector<double> hpos(3 * ne), hrad(ne, 0.0);
+        OMG_CUDA(cudaMemcpyAsync(hpos.data(), positions, 3 * ne * 8, cudaMemcpyDeviceToHost, s));
+        if (radii) OMG_CUDA(cudaMemcpyAsync(hrad.data(), radii, ne * 8, cudaMemcpyDeviceToHost, s));
+        DevBuf near((size_t)ne * 8, s);
+        launch_nearest_triangle(geo->d, positions, ne, geo->n_eeg_cand, geo->eeg_cand, near.as<int64_t>(), s);
+        std::vector<int64_t> hnear(ne);
+        OMG_CUDA(cudaMemcpyAsync(hnear.data(), near.p, ne * 8, cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+        const std::vector<Injection> inj = injection_triangles(h, hpos, hrad, hnear);
+        // distinct injection triangles, grouped by mesh (ids are positions in `uniq`)
+        std::vector<int64_t> uniq;
+        for (const auto& e : inj) uniq.insert(uniq.end(), e.tri.begin(), e.tri.end());
+        std::sort(uniq.begin(), uniq.end());
+        uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+        std::vector<int64_t> ebeg{0}, eid;
+        std::vector<double> ecoef;
+        for (const auto& e : inj) {
+            for (size_t q = 0; q < e.tri.size(); ++q) {
+                eid.push_back(std::lower_bound(uniq.begin(), uniq.end(), e.tri[q]) - uniq.begin());
+                ecoef.push_back(e.coef[q]);
+            }
+            ebeg.push_back((int64_t)eid.size());
+        }
+        DevBuf d_uniq(uniq.size() * 8, s), d_ebeg(ebeg.size() * 8, s), d_eid(eid.size() * 8, s),
+            d_ecoef(ecoef.size() * 8, s);
+        OMG_CUDA(cudaMemcpyAsync(d_uniq.p, uniq.data(), uniq.size() * 8, cudaMemcpyHostToDevice, s));
+        OMG_CUDA(cudaMemcpyAsync(d_ebeg.p, ebeg.data(), ebeg.size() * 8, cudaMemcpyHostToDevice, s));
+        OMG_CUDA(cudaMemcpyAsync(d_eid.p, eid.data(), eid.size() * 8, cudaMemcpyHostToDevice, s));
+        OMG_CUDA(cudaMemcpyAsync(d_ecoef.p, ecoef.data(), ecoef.size() * 8, cudaMemcpyHostToDevice, s));
+        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)Nref * ne * 8, s));
+        int64_t ntmax = 1;
+        for (int m = 0; m < h.nmesh; ++m) ntmax = std::max<int64_t>(ntmax, h.tbeg[m + 1] - h.tbeg[m]);
+        const int64_t per = std::max<int64_t>(
+            1, std::min<int64_t>({4096, (256ll << 20) / (Nref * 8), (512ll << 20) / (ntmax * 24)}));
+        const int64_t nu = (int64_t)uniq.size();
+        DevBuf R((size_t)std::min(per, nu) * Nref * 8, s), tmp((size_t)std::min(per, nu) * ntmax * 24, s);
+        for (int m = 0; m < h.nmesh; ++m) {
+            if (!h.barrier[m]) continue;   // rows of non-barrier triangles are never filled
+            const int64_t ub = std::lower_bound(uniq.begin(), uniq.end(), h.tbeg[m]) - uniq.begin();
+            const int64_t ue = std::lower_bound(uniq.begin(), uniq.end(), h.tbeg[m + 1]) - uniq.begin();
+            for (int64_t k0 = ub; k0 < ue; k0 += per) {
+                const int64_t nk = std::min(per, ue - k0);
+                OMG_CUDA(cudaMemsetAsync(R.p, 0, (size_t)nk * Nref * 8, s));
+                for (const auto& p : h.pairs) {
+                    if (p.m1 != m) continue;
+                    const int m2 = p.m2;
+                    const bool self = (m2 == m);
+                    launch_eit_rows(geo->d, d_uniq.as<int64_t>() + k0, nk, h.tbeg[m2], h.tbeg[m2 + 1], h.vbeg[m2],
+                                    h.vbeg[m2 + 1], self, !self && !h.barrier[m2], kK * p.orientation, -p.cS,
+                                    geo->tidx_ref, it.order, tmp.as<double>(), R.as<double>(), s);
+                }
+                launch_eit_combine(Nref, ne, d_ebeg.as<int64_t>(), d_eid.as<int64_t>(), d_ecoef.as<double>(), k0, nk,
+                                   R.as<double>(), out, s);
+            }
+        }
+        check_err(ctx, "EITSourceMat");
     });
 }
 

@@ -1780,4 +1780,231 @@ void launch_dipole_internal_pot(const double* pts, const int* pdom, const int64_
     check_launch("dipole internal potential");
 }
 
+// ---------------------------------------------------------------------------
+// EITSourceMat (assembleSourceMat.cpp:109-152).  The reference fills the
+// rows of a transfer matrix for the triangles of current-barrier meshes,
+//   D(K o) over (injection triangle, vertices of mesh2)          (operators.h:83-115, 439-442)
+//   -1/2 Id on the self pair, Id(t, v) = area / 3                (operators.h:200-206, 267-269)
+//   S(-K o sigma_inv) over (injection triangle, triangles of mesh2 != mesh1)   (operators.h:391-425)
+// and sums the rows of each electrode's injection triangles with its weight.
+// Only the rows of injection triangles are computed here: R is row-major,
+// one row of Nref (reference-numbered) columns per injection triangle.
+// ---------------------------------------------------------------------------
+
+// Danielsson's point-triangle distance (danielsson.cpp:26-74) with every
+// operation rounded separately, in the reference's order (Vect3 dotprod and
+// norm, vect3.h:72-73,111): no contraction into fused multiply-adds, so the
+// distances equal the reference's double-precision ones bit for bit.  A point
+// above an edge shared by two triangles is mathematically equidistant from
+// both; which one is "nearest" is decided by the rounding of these
+// operations, and EITSourceMat injects current into that triangle.
+__device__ __forceinline__ double dot_rn(d3 a, d3 b) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ d3 sub_rn(d3 a, d3 b) {
+    return {__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)};
+}
+__device__ double danielsson_rn(d3 p, const d3 P[3]) {
+    int idx[3] = {0, 1, 2};
+    int nb = 3;
+    double al[3] = {0.0, 0.0, 0.0};
+    for (;;) {
+        if (nb == 1) {
+            const d3 d = sub_rn(p, P[idx[0]]);
+            return __dsqrt_rn(dot_rn(d, d));
+        }
+        d3 A0Ai[3];
+        for (int i = 1; i < nb; ++i) A0Ai[i] = sub_rn(P[idx[i]], P[idx[0]]);
+        const d3 A0M = sub_rn(p, P[idx[0]]);
+        if (nb == 2) {
+            al[idx[1]] = __ddiv_rn(dot_rn(A0M, A0Ai[1]), dot_rn(A0Ai[1], A0Ai[1]));
+            al[idx[0]] = __dsub_rn(1.0, al[idx[1]]);
+        } else {
+            const double a00 = dot_rn(A0Ai[1], A0Ai[1]), a10 = dot_rn(A0Ai[1], A0Ai[2]),
+                         a11 = dot_rn(A0Ai[2], A0Ai[2]);
+            const double b0 = dot_rn(A0M, A0Ai[1]), b1 = dot_rn(A0M, A0Ai[2]);
+            const double dd = __dsub_rn(__dmul_rn(a00, a11), __dmul_rn(a10, a10));
+            al[idx[1]] = __ddiv_rn(__dsub_rn(__dmul_rn(b0, a11), __dmul_rn(b1, a10)), dd);
+            al[idx[2]] = __ddiv_rn(__dsub_rn(__dmul_rn(a00, b1), __dmul_rn(a10, b0)), dd);
+            al[idx[0]] = __dsub_rn(__dsub_rn(1.0, al[idx[1]]), al[idx[2]]);
+        }
+        int neg = -1;
+        for (int i = 0; i < nb; ++i)
+            if (al[idx[i]] < 0) {
+                neg = i;
+                break;
+            }
+        if (neg >= 0) {
+            al[idx[neg]] = 0;
+            const int tmp = idx[neg];
+            idx[neg] = idx[nb - 1];
+            idx[nb - 1] = tmp;
+            --nb;
+            continue;
+        }
+        d3 MH = {-A0M.x, -A0M.y, -A0M.z};
+        for (int i = 1; i < nb; ++i) {
+            const double a = al[idx[i]];
+            MH = {__dadd_rn(MH.x, __dmul_rn(a, A0Ai[i].x)), __dadd_rn(MH.y, __dmul_rn(a, A0Ai[i].y)),
+                  __dadd_rn(MH.z, __dmul_rn(a, A0Ai[i].z))};
+        }
+        return __dsqrt_rn(dot_rn(MH, MH));
+    }
+}
+
+// Nearest candidate triangle per electrode (dist_point_geom,
+// danielsson.cpp:107-128): one CTA per electrode, ties to the first candidate
+// (the reference keeps the first strictly smaller distance).
+__global__ void nearest_triangle_kernel(const double* __restrict__ pos, int64_t ncand,
+                                        const int32_t* __restrict__ cand, const double* __restrict__ srec,
+                                        int64_t* out_tri) {
+    __shared__ double sd[256];
+    __shared__ int64_t so[256];
+    const int64_t e = blockIdx.x;
+    const d3 p = dev::ld3(pos + 3 * e);
+    double best = 1.79769313486231570e+308;
+    int64_t bo = INT64_MAX;
+    for (int64_t k = threadIdx.x; k < ncand; k += blockDim.x) {
+        const double* s = srec + (int64_t)cand[k] * SREC;
+        const d3 P[3] = {dev::ld3(s), dev::ld3(s + 3), dev::ld3(s + 6)};
+        const double dist = danielsson_rn(p, P);
+        if (dist < best) {
+            best = dist;
+            bo = k;
+        }
+    }
+    sd[threadIdx.x] = best;
+    so[threadIdx.x] = bo;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const int o = threadIdx.x + w;
+            if (sd[o] < sd[threadIdx.x] || (sd[o] == sd[threadIdx.x] && so[o] < so[threadIdx.x])) {
+                sd[threadIdx.x] = sd[o];
+                so[threadIdx.x] = so[o];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out_tri[e] = so[0] < ncand ? (int64_t)cand[so[0]] : -1;
+}
+
+void launch_nearest_triangle(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand,
+                             int64_t* out_tri, cudaStream_t s) {
+    if (ne == 0) return;
+    ProfScope prof_("nearest_triangle", s);
+    nearest_triangle_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, ncand, cand, g.srec, out_tri);
+    check_launch("nearest triangle");
+}
+
+// tmp[(k nb + j) 3 + l] = integral over injection triangle inj[k] of
+// P1SingleLayerPotential(t2b + j), component l (the D block's pair integral).
+__global__ void eit_d_kernel(const int64_t* __restrict__ inj, int64_t nk, const double* __restrict__ qrec,
+                             const double* __restrict__ prec, int64_t t2b, int64_t nb, int order, double* tmp) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t k = blockIdx.y;
+    if (j >= nb || k >= nk) return;
+    const double* q = qrec + inj[k] * QREC;
+    const double* P = prec + (t2b + j) * PREC;
+    const int np = c_nbpts[order];
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < np; ++i) {
+        double v[3];
+        dev::p1_single_layer(P, dev::ld3(q + 3 * i), v);
+        const double w = c_rules[order][i][3];
+        acc[0] += w * v[0];
+        acc[1] += w * v[1];
+        acc[2] += w * v[2];
+    }
+    double* o = tmp + (k * nb + j) * 3;
+    o[0] = q[48] * acc[0];
+    o[1] = q[48] * acc[1];
+    o[2] = q[48] * acc[2];
+}
+
+// R[k, v] += coeffD * sum over the triangles of [t2b, t2b + nb) holding v (triangle order),
+// then the -1/2 Id term of the self pair.
+__global__ void eit_d_gather_kernel(const int64_t* __restrict__ inj, int64_t nk, int64_t t2b, int64_t nb, int64_t vb,
+                                    int64_t nvb, double coeffD, int self, const double* __restrict__ tmp,
+                                    const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
+                                    const int8_t* __restrict__ v2t_loc, const int32_t* __restrict__ T,
+                                    const double* __restrict__ srec, double* R, int64_t Nref) {
+    const int64_t iv = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t k = blockIdx.y;
+    if (iv >= nvb || k >= nk) return;
+    const int64_t v = vb + iv;
+    double sum = 0.0;
+    for (int q = v2t_beg[v]; q < v2t_beg[v + 1]; ++q) {
+        const int64_t t2 = v2t_tri[q];
+        if (t2 < t2b || t2 >= t2b + nb) continue;
+        sum += tmp[(k * nb + (t2 - t2b)) * 3 + v2t_loc[q]];
+    }
+    double r = R[k * Nref + v] + coeffD * sum;
+    if (self) {
+        const int64_t u = inj[k];
+        if (T[3 * u] == v || T[3 * u + 1] == v || T[3 * u + 2] == v) r += -0.5 * (srec[u * SREC + 12] / 3.0);
+    }
+    R[k * Nref + v] = r;
+}
+
+// R[k, tidx(t2)] = coeffS * integral over t2 of OperatorS(inj[k]).
+__global__ void eit_s_kernel(const int64_t* __restrict__ inj, int64_t nk, const double* __restrict__ srec,
+                             const double* __restrict__ qrec, int64_t t2b, int64_t nb, int order,
+                             const int64_t* __restrict__ tidx_ref, double coeffS, double* R, int64_t Nref) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t k = blockIdx.y;
+    if (j >= nb || k >= nk) return;
+    const double* sr = srec + inj[k] * SREC;
+    const double* q = qrec + (t2b + j) * QREC;
+    const int np = c_nbpts[order];
+    double acc = 0.0;
+    for (int i = 0; i < np; ++i) acc += c_rules[order][i][3] * dev::operator_S(sr, dev::ld3(q + 3 * i));
+    R[k * Nref + tidx_ref[t2b + j]] = (q[48] * acc) * coeffS;
+}
+
+void launch_eit_rows(const DevGeom& g, const int64_t* inj, int64_t nk, int64_t t2b, int64_t t2e, int64_t vb,
+                     int64_t ve, bool self, bool withS, double coeffD, double coeffS, const int64_t* tidx_ref,
+                     int order, double* tmp, double* R, cudaStream_t s) {
+    if (nk == 0) return;
+    ProfScope prof_("eit_rows", s);
+    const int64_t nb = t2e - t2b;
+    dim3 grid(nblocks(nb, 128), (unsigned)nk);
+    eit_d_kernel<<<grid, 128, 0, s>>>(inj, nk, g.qrec, g.prec, t2b, nb, order, tmp);
+    check_launch("EIT D");
+    dim3 grid2(nblocks(ve - vb, 128), (unsigned)nk);
+    eit_d_gather_kernel<<<grid2, 128, 0, s>>>(inj, nk, t2b, nb, vb, ve - vb, coeffD, self ? 1 : 0, tmp, g.v2t_beg,
+                                              g.v2t_tri, g.v2t_loc, g.T, g.srec, R, g.Nref);
+    check_launch("EIT D gather");
+    if (withS) {
+        eit_s_kernel<<<grid, 128, 0, s>>>(inj, nk, g.srec, g.qrec, t2b, nb, order, tidx_ref, coeffS, R, g.Nref);
+        check_launch("EIT S");
+    }
+}
+
+// out[i, e] += sum over the electrode's injection entries q with k0 <= id[q] < k0 + nk
+// of coef[q] * R[id[q] - k0, i], in the electrode's triangle order.
+__global__ void eit_combine_kernel(int64_t Nref, int64_t ne, const int64_t* __restrict__ ebeg,
+                                   const int64_t* __restrict__ eid, const double* __restrict__ ecoef, int64_t k0,
+                                   int64_t nk, const double* __restrict__ R, double* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= Nref) return;
+    for (int64_t e = blockIdx.y; e < ne; e += gridDim.y) {
+        double acc = out[i + e * Nref];
+        for (int64_t q = ebeg[e]; q < ebeg[e + 1]; ++q) {
+            const int64_t k = eid[q] - k0;
+            if (k >= 0 && k < nk) acc += R[k * Nref + i] * ecoef[q];
+        }
+        out[i + e * Nref] = acc;
+    }
+}
+
+void launch_eit_combine(int64_t Nref, int64_t ne, const int64_t* ebeg, const int64_t* eid, const double* ecoef,
+                        int64_t k0, int64_t nk, const double* R, double* out, cudaStream_t s) {
+    if (ne == 0 || Nref == 0) return;
+    ProfScope prof_("eit_combine", s);
+    dim3 grid(nblocks(Nref, 256), (unsigned)std::min<int64_t>(ne, 32768));
+    eit_combine_kernel<<<grid, 256, 0, s>>>(Nref, ne, ebeg, eid, ecoef, k0, nk, R, out);
+    check_launch("EIT combine");
+}
+
 }  // namespace omg

@@ -13,7 +13,9 @@
  * Geometry arrives pre-digested (unknown numbering, mesh pairs, coefficients,
  * deflation parts) from oracle/oracle.py, which restates the Geometry logic.
  *
- * Build: gcc -O2 -fopenmp -fPIC -shared om_oracle.c -o _ref_oracle/libomoracle.so -lm
+ * Build (oracle.py build()): gcc -O2 -ffp-contract=off -fopenmp -fPIC -shared -std=c11 om_oracle.c -lm.
+ * With contraction off the arithmetic is the reference's own (no fused multiply-adds)
+ * on x86 and Arm hosts alike.
  */
 #include <math.h>
 #include <stdint.h>
@@ -579,6 +581,53 @@ int oo_surf2vol(const oo_geom* g, const double* pts, int64_t np, const int* nb, 
                     opS_t S;
                     opS_make(&S, &tris[t]);
                     out[i + np * g->tidx[t]] = c / cond[i] * opS_eval(&S, x);
+                }
+            }
+        }
+    }
+    free(tris);
+    return 0;
+}
+
+/* Rows of the EITSourceMat transfer matrix (assembleSourceMat.cpp:115-134) for
+ * the triangles tri[0..n): for each communicating pair (mesh1, mesh2) whose
+ * mesh1 holds the triangle and is a current barrier,
+ *   D:  row(vertex of t2 in mesh2) += cD[p] * integral over t of P1SingleLayerPotential(t2)
+ *   Id: row(vertex of t) += -1/2 * area(t) / 3                  (mesh1 == mesh2)
+ *   S:  row(triangle unknown of t2) = cS[p] * integral over t2 of OperatorS(t)   (mesh1 != mesh2)
+ * rows is n x N, row-major (only the N unknown columns are kept). */
+int oo_eit_rows(const oo_geom* g, const int64_t* tri, int64_t n, const double* cD, const double* cS,
+                const oo_integrator* I, double* rows) {
+    const int64_t N = g->N;
+    tri_t* tris = (tri_t*)malloc(sizeof(tri_t) * (size_t)g->nt);
+    for (int64_t t = 0; t < g->nt; ++t) make_tri(g, t, &tris[t]);
+    memset(rows, 0, sizeof(double) * (size_t)(n * N));
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t t = tri[k];
+        int m1 = 0;
+        while (t >= g->mesh_tbeg[m1 + 1]) ++m1;
+        if (!g->barrier[m1]) continue;
+        double* row = rows + (size_t)k * N;
+        for (int p = 0; p < g->npairs; ++p) {
+            if (g->pairs[2 * p] != m1) continue;
+            const int m2 = g->pairs[2 * p + 1];
+            for (int64_t t2 = g->mesh_tbeg[m2]; t2 < g->mesh_tbeg[m2 + 1]; ++t2) {
+                p1_t P;
+                p1_make(&P, &tris[t2]);
+                double total[3];
+                integrate(f_p1, &P, 3, &tris[t], I, total);
+                for (int i = 0; i < 3; ++i) row[g->vidx[g->T[3 * t2 + i]]] += total[i] * cD[p];
+            }
+            if (m2 == m1) {
+                for (int i = 0; i < 3; ++i) row[g->vidx[g->T[3 * t + i]]] += tris[t].area / 3.0 * -0.5;
+            } else if (!g->barrier[m2]) {
+                opS_t S;
+                opS_make(&S, &tris[t]);
+                for (int64_t t2 = g->mesh_tbeg[m2]; t2 < g->mesh_tbeg[m2 + 1]; ++t2) {
+                    double v;
+                    integrate(f_opS, &S, 1, &tris[t2], I, &v);
+                    row[g->tidx[t2]] = v * cS[p];
                 }
             }
         }

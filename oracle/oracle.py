@@ -46,7 +46,8 @@ def build(force: bool = False) -> str:
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = LIB_PATH + f".{os.getpid()}.tmp"
-    subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11", src, "-o", tmp, "-lm"])
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", src, "-o", tmp,
+                           "-lm"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -420,8 +421,9 @@ def dipsource2internalpotmat(g: OracleGeometry, dipoles: np.ndarray, points: np.
     return out
 
 
-def h2em(g: OracleGeometry, electrodes: np.ndarray) -> np.ndarray:
-    """Dense n_e x N Head2EEGMat (the reference stores it sparse)."""
+def _nearest(g: OracleGeometry, electrodes: np.ndarray):
+    """Nearest triangle of the interfaces touching air (dist_point_geom,
+    danielsson.cpp:107-128) and its barycentric weights, per point."""
     pos = np.ascontiguousarray(electrodes[:, :3], np.float64)
     meshes = np.array(g.eeg_meshes(), np.int32)
     ne = pos.shape[0]
@@ -430,10 +432,90 @@ def h2em(g: OracleGeometry, electrodes: np.ndarray) -> np.ndarray:
     gs = g.c_struct()
     lib().oo_h2em(ctypes.byref(gs), _ptr(pos), ctypes.c_int64(ne), ctypes.c_int(len(meshes)), _ptr(meshes),
                   _ptr(tri), _ptr(w))
+    return tri, w
+
+
+def h2em(g: OracleGeometry, electrodes: np.ndarray) -> np.ndarray:
+    """Dense n_e x N Head2EEGMat (the reference stores it sparse)."""
+    tri, w = _nearest(g, electrodes)
+    ne = tri.shape[0]
     M = np.zeros((ne, g.N))
     for i in range(ne):
         for j in range(3):
             M[i, g.vidx[g.T[tri[i], j]]] = w[i, j]
+    return M
+
+
+def _tri_area(g: OracleGeometry, t) -> float:
+    a, b, c = g.V[g.T[t]]
+    return float(np.linalg.norm(np.cross(b - a, c - a)) / 2.0)
+
+
+def injection_triangles(g: OracleGeometry, electrodes: np.ndarray):
+    """Sensors::findInjectionTriangles (sensors.cpp:167-215) for electrodes
+    given as n x 3 (points) or n x 4 (x, y, z, radius): per electrode the list
+    of (triangle, weight) that EITSourceMat sums (assembleSourceMat.cpp:141-150).
+    The walk over neighbours uses the first three entries of
+    Mesh::adjacent_triangles (mesh.h:164-172), which include the triangle itself."""
+    el = np.asarray(electrodes, np.float64)
+    radii = el[:, 3] if el.shape[1] >= 4 else np.zeros(el.shape[0])
+    nearest, _ = _nearest(g, el)
+    inc = {}
+    for m in range(g.nmesh):
+        for t in range(g.mesh_tbeg[m], g.mesh_tbeg[m + 1]):
+            for v in g.T[t]:
+                inc.setdefault(int(v), []).append(t)
+
+    def adjacent(t):
+        cnt, res = {}, []
+        for v in g.T[t]:
+            for t2 in inc[int(v)]:
+                cnt[t2] = cnt.get(t2, 0) + 1
+                if cnt[t2] == 2:
+                    res.append(t2)
+        return res
+
+    out = []
+    for e in range(el.shape[0]):
+        t0, r = int(nearest[e]), float(radii[e])
+        tris = [t0]
+        point = abs(r) < 2.2250738585072014e-308
+        if not point and _tri_area(g, t0) < 4 * math.pi * r * r:
+            seen, stack = {t0}, [t0]
+            while stack:
+                t = stack.pop()
+                if np.linalg.norm(g.V[g.T[t]].sum(axis=0) / 3.0 - el[e, :3]) < r:
+                    if t != t0:
+                        tris.append(t)
+                    for t2 in adjacent(t)[:3]:
+                        if t2 not in seen:
+                            seen.add(t2)
+                            stack.append(t2)
+        if point:
+            out.append([(t, 1.0 / _tri_area(g, t)) for t in tris])
+        else:
+            w = math.pi * r * r / sum(_tri_area(g, t) for t in tris)
+            out.append([(t, w) for t in tris])
+    return out
+
+
+def eitsourcemat(g: OracleGeometry, electrodes: np.ndarray, order=3) -> np.ndarray:
+    """EITSourceMat (assembleSourceMat.cpp:109-152): N x n_electrodes."""
+    inj = injection_triangles(g, electrodes)
+    uniq = sorted({t for lst in inj for (t, _) in lst})
+    pos = {t: k for k, t in enumerate(uniq)}
+    orient = np.sign(g.coefs[:, 1])                       # the pair's relative orientation (cN = o K sigma)
+    cD = np.ascontiguousarray(K * orient)
+    cS = np.ascontiguousarray(-g.coefs[:, 0])             # -K o sigma_inv
+    rows = np.zeros((len(uniq), g.N))
+    gs = g.c_struct()
+    tri = np.ascontiguousarray(np.array(uniq, np.int64))
+    lib().oo_eit_rows(ctypes.byref(gs), _ptr(tri), ctypes.c_int64(len(uniq)), _ptr(cD), _ptr(cS),
+                      ctypes.byref(_integ(order, 0, 0.005)), _ptr(rows))
+    M = np.zeros((g.N, len(inj)))
+    for e, lst in enumerate(inj):
+        for (t, w) in lst:
+            M[:, e] += rows[pos[t]] * w
     return M
 
 

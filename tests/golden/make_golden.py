@@ -18,10 +18,14 @@ files) for a seeded workload of openmeeg_gb300.workloads:
                      MEG values its test suite compares against
                      (tests/analytic/eeg_head3_analytic.txt, meg_analytic.txt);
                      `--analytic-only` writes just this fixture
+  eit_sources        EITSourceMat (om_assemble -EITSM) for point electrodes and for
+                     electrodes with radii on small_ico1_3l, small_ico1_4l_out and
+                     small_ico2_3l_pert; `--eit-only` writes just this fixture (and
+                     head3_analytic)
   internal_potentials Surf2VolMat and DipSource2InternalPotMat (om_assemble -H2IPM /
                      -DS2IPM, own domains and a forced one) at points in every layer
                      and in the air of small_ico1_3l and small_ico1_4l_out;
-                     `--ipm-only` writes just this fixture (and head3_analytic)
+                     `--ipm-only` writes this fixture and the ones above
   surface_sources    SurfSourceMat and SurfSource2MEGMat (om_assemble -SSM / -SS2MM)
                      of a source icosphere (ico1, r = 0.5, off-centre) in the brain of
                      small_ico1_3l and of small_ico1_4l_out; `--ssm-only` writes just
@@ -151,9 +155,42 @@ def save_internal_potentials():
     print("internal_potentials", {k: v.shape for k, v in d.items()})
 
 
+def save_eit():
+    """EITSourceMat (om_assemble -EITSM) for point electrodes (3 columns) and
+    for electrodes with radii (4 columns, some zero, some spanning several
+    scalp triangles) on three small heads."""
+    import subprocess
+    import tempfile
+    if not ref_runner.available():
+        ref_runner.build()
+    d = {}
+    cases = (("3l", workloads.small(1, layers=3)), ("4l_out", workloads.small(1, layers=4, inward=False)),
+             ("ico2_pert", workloads.small(2, layers=3, perturb=True)))
+    for k, (tag, w) in enumerate(cases):
+        rng = np.random.default_rng(workloads.SEED + 60 + k)
+        el = w.electrodes[:, :3]
+        rad = rng.choice([0.0, 0.05, 0.12, 0.2, 0.33], size=el.shape[0])
+        wd = tempfile.mkdtemp()
+        ref_runner.write_head(wd, w.head)
+        io.write_matrix_txt(os.path.join(wd, "el3.txt"), el)
+        io.write_matrix_txt(os.path.join(wd, "el4.txt"), np.hstack([el, rad[:, None]]))
+        for args in (["om_assemble", "-EITSM", "head.geom", "head.cond", "el3.txt", "eit3.bin"],
+                     ["om_assemble", "-EITSM", "head.geom", "head.cond", "el4.txt", "eit4.bin"]):
+            subprocess.check_call([os.path.join(ref_runner.REF_BIN, args[0]), *args[1:]], cwd=wd,
+                                  stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        d[f"electrodes_{tag}"] = np.hstack([el, rad[:, None]])
+        d[f"eit_points_{tag}"] = io.read_bin(os.path.join(wd, "eit3.bin"))[1]
+        d[f"eit_radii_{tag}"] = io.read_bin(os.path.join(wd, "eit4.bin"))[1]
+    np.savez_compressed(os.path.join(OUT, "eit_sources.npz"), **d)
+    print("eit_sources", {k: v.shape for k, v in d.items()})
+
+
 def main():
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
+        return
+    save_eit()
+    if "--eit-only" in sys.argv:
         return
     save_internal_potentials()
     if "--ipm-only" in sys.argv:

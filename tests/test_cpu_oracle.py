@@ -69,6 +69,21 @@ def test_oracle_internal_potentials_pinned_to_reference(tag, layers, inward):
     assert rel(oracle.dipsource2internalpotmat(g, w.dipoles, pts, forced), G[f"ds2ipm_forced_{tag}"]) < 1e-14
 
 
+@pytest.mark.parametrize("tag,kw", [("3l", dict(layers=3)), ("4l_out", dict(layers=4, inward=False)),
+                                    ("ico2_pert", dict(subdiv=2, layers=3, perturb=True))])
+def test_oracle_eit_source_pinned_to_reference(tag, kw):
+    """EITSourceMat against om_assemble -EITSM, point electrodes and electrodes
+    with radii (flood-filled injection triangles)."""
+    from oracle import oracle
+    from openmeeg_gb300 import workloads
+    G = golden("eit_sources")
+    w = workloads.small(**{"subdiv": 1, **kw})
+    g = oracle.digest(w.head)
+    el = G[f"electrodes_{tag}"]
+    assert rel(oracle.eitsourcemat(g, el[:, :3]), G[f"eit_points_{tag}"]) < 1e-14
+    assert rel(oracle.eitsourcemat(g, el), G[f"eit_radii_{tag}"]) < 1e-14
+
+
 def test_oracle_numbering_and_pairs():
     """Unknown count and mesh pairs of nested heads (geometry.cpp:256-295, 405-420)."""
     from oracle import oracle
