@@ -677,6 +677,106 @@ def run_adjoint(args):
     return 0
 
 
+def run_next(args):
+    """The rows beside the forward path on the config1 head (ico4, N=17926):
+    SurfSourceMat and SurfSource2MEGMat (an ico3 source surface, 642 vertices,
+    in the brain), Surf2VolMat and DipSource2InternalPotMat (5000 points over
+    the whole head and its surroundings, 2000 dipoles), EITSourceMat (64
+    electrodes of radius 0.05).  Per row: CUDA-event time per call over
+    --steps calls after --warmup, kernel launches, the analytic-kernel
+    evaluations of the call and their rate, and, where the oracle restates
+    the row, the oracle's CPU time on a bounded sample scaled to the call."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    __import__("__graft_entry__").build()
+    from openmeeg_gb300 import api, workloads
+    from openmeeg_gb300 import synthetic as syn
+    w = workloads.config1()
+    ctx = api.Context(local)
+    ctx.bind_current_stream()
+    geo = api.Geometry.from_head(w.head, ctx)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(17)
+    Vs, Ts = syn.icosphere(3, inward=False)
+    Vs = Vs * 0.5 + np.array([0.03, -0.02, 0.01])
+    u = rng.standard_normal((5000, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    pts = u * (rng.random(5000) ** (1.0 / 3.0) * 1.1)[:, None]
+    dip = w.dipoles
+    el = np.hstack([w.electrodes[:, :3], np.full((w.electrodes.shape[0], 1), 0.05)])
+    pts_d = torch.as_tensor(pts, device=dev)
+    dip_d = torch.as_tensor(dip, device=dev)
+    el_d = torch.as_tensor(el, device=dev)
+    sq_d = torch.as_tensor(w.squids, device=dev)
+    T_in = w.head.triangles[0].shape[0]
+    Ttot = sum(t.shape[0] for t in w.head.triangles)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        out = None
+        for _ in range(args.warmup):
+            out = fn()
+        torch.cuda.synchronize()
+        l0 = ctx.launches()
+        e0.record()
+        for _ in range(args.steps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, (ctx.launches() - l0) / args.steps, out
+
+    rows = {}
+    clocks = Clocks(local)
+    clocks.start()
+    ms, nl, A = timed(lambda: api.SurfSourceMat(geo, Vs, Ts))
+    ev = 2 * 16 * T_in * Ts.shape[0]            # S and D pair integrals of the brain's boundary vs the source
+    rows["SurfSourceMat"] = {"ms": ms, "launches": nl, "shape": list(A.shape), "evaluations": ev,
+                             "evals_per_s": ev / (ms / 1e3), "cpu": None,
+                             "note": "16-point S and D pair integrals (brain boundary x source triangles)"}
+    ms, nl, A = timed(lambda: api.SurfSource2MEGMat(Vs, Ts, sq_d, ctx))
+    rows["SurfSource2MEGMat"] = {"ms": ms, "launches": nl, "shape": list(A.shape),
+                                 "evaluations": sq_d.shape[0] * Ts.shape[0],
+                                 "evals_per_s": sq_d.shape[0] * Ts.shape[0] / (ms / 1e3), "cpu": None}
+    ms, nl, A = timed(lambda: api.Surf2VolMat(geo, pts_d))
+    kept = A.shape[0]
+    rows["Surf2VolMat"] = {"ms": ms, "launches": nl, "shape": list(A.shape), "points": pts.shape[0],
+                           "evaluations": kept * Ttot, "evals_per_s": kept * Ttot / (ms / 1e3),
+                           "note": "upper bound: P1 + S per (kept point, triangle of its domain's boundary); "
+                                   "one thread per (point, triangle) of the whole head"}
+    ms, nl, A = timed(lambda: api.DipSource2InternalPotMat(geo, dip_d, pts_d))
+    rows["DipSource2InternalPotMat"] = {"ms": ms, "launches": nl, "shape": list(A.shape),
+                                        "evaluations": kept * dip.shape[0],
+                                        "evals_per_s": kept * dip.shape[0] / (ms / 1e3)}
+    ms, nl, A = timed(lambda: api.EITSourceMat(geo, el_d))
+    rows["EITSourceMat"] = {"ms": ms, "launches": nl, "shape": list(A.shape)}
+    ck = clocks.stop()
+    if not args.no_cpu:
+        from oracle import oracle
+        g = oracle.digest(w.head)
+        nthr = oracle.num_threads()
+        for name, fn, n_sample, n_full in (
+                ("Surf2VolMat", lambda k: oracle.surf2volmat(g, pts[:k]), 400, pts.shape[0]),
+                ("DipSource2InternalPotMat", lambda k: oracle.dipsource2internalpotmat(g, dip[:20], pts[:k]), 200,
+                 pts.shape[0] * dip.shape[0] / 20),
+                ("EITSourceMat", lambda k: oracle.eitsourcemat(g, el[:k]), 8, el.shape[0])):
+            s = time.perf_counter()
+            fn(n_sample)
+            t = (time.perf_counter() - s) * n_full / n_sample
+            rows[name]["cpu"] = {"value_ms": t * 1e3, "cores": nthr, "kind": "port",
+                                 "sample": f"{n_sample} of the call's units, scaled linearly"}
+            rows[name]["speedup_vs_cpu"] = t * 1e3 / rows[name]["ms"]
+    line = {"metric": "time per call (ms) of the rows beside the forward path, config1 head", "unit": "ms",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"config1 head (N={geo.size}); ico3 source surface (642 vertices) in the brain; "
+                                   f"5000 points (r < 1.1), {dip.shape[0]} dipoles, 64 EIT electrodes (r = 0.05), "
+                                   f"{sq_d.shape[0]} magnetometers"},
+            "rows": rows, "clocks": ck}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -704,6 +804,8 @@ def main():
         return run_large(args)
     if args.config == "config2":
         return run_adjoint(args)
+    if args.config == "next":
+        return run_next(args)
     return run_gpu(args)
 
 

@@ -511,7 +511,7 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     cudaStream_t s2 = sv->ctx->aux;
     cudaEvent_t ev_w = sv->ctx->ev_a, ev_r = sv->ctx->ev_b;
     bool rest_pending = false;
-    const int reserve = 8;   // SMs the rest update leaves to the panel chain
+    const int reserve = 8;   // SMs the rest update leaves to the panel chain (more made the factorization slower)
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
         if (k0 == nP) {   // continue on -(vertex Schur complement): every pending update must be in
@@ -1281,8 +1281,9 @@ static void keep_conducting_points(KeptPoints& kp, omg_geometry geo, const doubl
     kp.rows = DevBuf((size_t)std::max<int64_t>(n, 1) * sizeof(int64_t), s);
     kp.kept = 0;
     if (n == 0) return;
+    // FP32-screened solid angles: sums clear of the 2 pi boundary classify as in FP64, the rest are FP64 sums
     DevBuf sa((size_t)n * h.nmesh * 8, s);
-    launch_mesh_solid_angles(pts, 3, n, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+    launch_mesh_solid_angles(pts, 3, n, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s, true);
     launch_domain_lookup(n, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh, geo->binside,
                          geo->orient, -1, kp.dom.as<int>(), geo->ctx->d_err, s);
     check_err(geo->ctx, "point domain lookup");
@@ -1348,7 +1349,9 @@ int omg_dipsource2internalpotmat_dev(omg_context ctx, omg_geometry geo, const do
         OMG_REQUIRE(out, "null argument");
         const HostGeometry& h = geo->h;
         DevBuf sa((size_t)n_dipoles * h.nmesh * 8, s), ddom((size_t)n_dipoles * sizeof(int), s);
-        launch_mesh_solid_angles(dipoles, 6, n_dipoles, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
+        if (domain < 0)
+            launch_mesh_solid_angles(dipoles, 6, n_dipoles, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s,
+                                     true);
         launch_domain_lookup(n_dipoles, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
                              geo->binside, geo->orient, domain, ddom.as<int>(), ctx->d_err, s);
         launch_dipole_internal_pot(points, kp.dom.as<int>(), kp.rows.as<int64_t>(), n_points, dipoles, ddom.as<int>(),

@@ -701,241 +701,242 @@ void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_
 
 // ---------------------------------------------------------------------------
 // Diagonal block of the FP32 factorization: Cholesky of the n x n (n <= 128)
-// block A11 and the inverse of its factor, in one CTA of 512 threads.  The
-// block lives in registers, distributed 2D-cyclically: thread (tr, tc) =
-// (tid / 32, tid % 32) holds rows tr + 16 i (i < 8) x columns tc + 32 q
-// (q < 4).  Both are right-looking in steps of 4 columns with one barrier per
-// step: the owners of the 4 columns (resp. rows of the inverse) publish them
-// to shared memory, every thread factors the 4 x 4 diagonal block itself and
-// applies the rank-4 update to the elements it holds.
+// block A11 and the inverse of its factor, in one CTA of 512 threads, blocked
+// by 32 columns (4 block steps J):
+//   1. warp 0 factors the 32 x 32 diagonal block in registers (lane i holds
+//      row i, shifted so the current column is in a fixed register; column j
+//      is broadcast by shuffles), no CTA barrier inside;
+//   2. warp 0 inverts that block (lane c solves column c of X_JJ) while the
+//      threads of warps 1-3 solve one panel row each, L_rJ = A_rJ L_JJ^-T, by
+//      forward substitution (rows below the block);
+//   3. all threads apply the rank-32 update to the trailing lower triangle
+//      in 4 x 4 register tiles, reading the panel from a k-major copy;
+// then the off-diagonal blocks of the inverse, X_IJ = -X_II sum_{K=J}^{I-1}
+// L_IK X_KJ, block row by block row.  The block lives in shared memory
+// (row-major, padded); columns past n act as the identity.
 // Outputs: L11 over A11 (lower), Linv column-major (ldi = 128, zero above the
 // diagonal and beyond n) for the solves, and Linv as TF32 head/remainder
 // K-major rows (128 x 128 each, zero padded) for the tensor-core panel solve
 // L21 = A21 Linv^T.  A pivot that is not positive is reported as
 // OMG_ERR_NOT_DEFINITE at its column (and replaced by 1 so the kernel ends).
 // ---------------------------------------------------------------------------
-constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512, PI_W = 4;
+constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512, PI_BS = 32, PI_TLD = 33;
+constexpr size_t PI_SMEM =
+    ((size_t)2 * PI_NB * PI_LD + (size_t)PI_BS * PI_NB + 3 * PI_BS * PI_TLD + PI_NB + 2 * PI_BS) * sizeof(float);
 
-__global__ void __launch_bounds__(PI_THREADS) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
+__global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
                                                                int64_t* err_col, int64_t col_offset, float* Linv,
                                                                float* Bh, float* Bl) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    float* sL = reinterpret_cast<float*>(smraw);   // row-major: sL[r * PI_LD + c]
-    float* buf = sL + PI_NB * PI_LD;                // 2 x PI_W x 128: published columns / rows
-    const int tid = threadIdx.x, tr = tid / 32, tc = tid % 32;
-    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
+    float* sA = reinterpret_cast<float*>(smraw);   // 128 x PI_LD row-major: A, then L
+    float* sX = sA + PI_NB * PI_LD;                 // 128 x PI_LD row-major: X = L^-1
+    float* sP = sX + PI_NB * PI_LD;                 // 32 x 128: panel column block, k-major (sP[k * 128 + r])
+    float* sT = sP + PI_BS * PI_NB;                 // 3 x 32 x PI_TLD: T blocks of the inverse
+    float* sInv = sT + 3 * PI_BS * PI_TLD;          // 1 / L[j][j]
+    float* sCol = sInv + PI_NB;                     // 2 x 32: column broadcast of the diagonal factor
+    const unsigned FULL = 0xffffffffu;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+#pragma unroll 8
+    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // 32 iterations: loads batched by the unroll
         const int r = e % PI_NB, c = e / PI_NB;    // coalesced down the columns of A
-        sL[r * PI_LD + c] = (r < n && c < n && r >= c) ? A[r + (int64_t)c * lda] : 0.f;
+        float v = 0.f;
+        if (r >= c) v = (r < n && c < n) ? A[r + (int64_t)c * lda] : (r == c ? 1.f : 0.f);
+        sA[r * PI_LD + c] = v;
+        sX[r * PI_LD + c] = 0.f;
     }
     __syncthreads();
-    float v[8][4];
+    for (int J = 0; J < 4; ++J) {
+        const int j0 = J * PI_BS;
+        if (warp == 0) {   // ---- 1. Cholesky of the diagonal block
+            // lane i holds row i, shifted left by one column per step so that the current column
+            // sits in r[0]; column j of L is broadcast through shared memory at positions relative
+            // to the pivot (l_(j+m)j at cb[m - 1]), read back as 8 aligned float4 (static offsets)
+            float r[PI_BS];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+            for (int m = 0; m < PI_BS; ++m) r[m] = (m <= lane) ? sA[(j0 + lane) * PI_LD + j0 + m] : 0.f;
+            int bad = -1;
+#pragma unroll 1
+            for (int j = 0; j < PI_BS; ++j) {
+                float d = __shfl_sync(FULL, r[0], j);
+                if (!(d > 0.f)) {
+                    if (bad < 0) bad = j;
+                    d = 1.f;
+                }
+                const float inv = rsqrtf(d);
+                const float l = (lane == j) ? d * inv : (lane > j ? r[0] * inv : 0.f);
+                float* cb = sCol + (j & 1) * PI_BS;
+                if (lane > j) cb[lane - j - 1] = l;
+                __syncwarp();
+                sA[(j0 + lane) * PI_LD + j0 + j] = l;   // rows above j write their zero upper element
+                if (lane == j) sInv[j0 + j] = inv;
+                // a[i][j + m] -= l_ij l_(j+m)j; slots past the block read stale values and are never pivots
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[i][q] = sL[(tr + 16 * i) * PI_LD + tc + 32 * q];
-    // ---- Cholesky, 4 columns per step
-    for (int c0 = 0; c0 < n; c0 += PI_W) {
-        float* col = buf + ((c0 / PI_W) & 1) * PI_W * PI_NB;   // col[k * 128 + r] = a[r][c0 + k]
-        const int qj = c0 >> 5, k_own = tc - (c0 & 31);
-        if (k_own >= 0 && k_own < PI_W) {
+                for (int q = 0; q < PI_BS / 4; ++q) {
+                    const float4 c4 = reinterpret_cast<const float4*>(cb)[q];
+                    const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                float x = v[i][0];
+                    for (int t = 0; t < 4; ++t) {
+                        const int m = 4 * q + t + 1;
+                        if (m < PI_BS) r[m - 1] = fmaf(-l, cv[t], r[m]);
+                    }
+                }
+                r[PI_BS - 1] = 0.f;
+            }
+            if (bad >= 0 && lane == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
+                *err_col = col_offset + j0 + bad;
+        }
+        __syncthreads();
+        const int below = PI_NB - j0 - PI_BS;
+        if (warp == 0) {   // ---- 2a. X_JJ = L_JJ^-1, column `lane`
+            float x[PI_BS];
 #pragma unroll
-                for (int q = 1; q < 4; ++q) x = (q == qj) ? v[i][q] : x;
-                col[k_own * PI_NB + tr + 16 * i] = x;
+            for (int r = 0; r < PI_BS; ++r) {
+                const float* Lr = sA + (j0 + r) * PI_LD + j0;
+                float acc0 = (r == lane) ? 1.f : 0.f, acc1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < r; ++k) {
+                    if (k & 1)
+                        acc1 = fmaf(-Lr[k], x[k], acc1);
+                    else
+                        acc0 = fmaf(-Lr[k], x[k], acc0);
+                }
+                x[r] = (acc0 + acc1) * sInv[j0 + r];
+            }
+#pragma unroll
+            for (int r = 0; r < PI_BS; ++r) sX[(j0 + r) * PI_LD + j0 + lane] = x[r];
+        } else if (tid - 32 < below) {   // ---- 2b. one panel row: L_rJ L_JJ^T = A_rJ
+            const int r = j0 + PI_BS + (tid - 32);
+            float l[PI_BS];
+#pragma unroll
+            for (int j = 0; j < PI_BS; ++j) {
+                const float* Lj = sA + (j0 + j) * PI_LD + j0;
+                float acc0 = sA[r * PI_LD + j0 + j], acc1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < j; ++k) {
+                    if (k & 1)
+                        acc1 = fmaf(-l[k], Lj[k], acc1);
+                    else
+                        acc0 = fmaf(-l[k], Lj[k], acc0);
+                }
+                l[j] = (acc0 + acc1) * sInv[j0 + j];
+            }
+#pragma unroll
+            for (int j = 0; j < PI_BS; ++j) {
+                sA[r * PI_LD + j0 + j] = l[j];
+                sP[j * PI_NB + r] = l[j];
             }
         }
         __syncthreads();
-        // the 4 x 4 diagonal block, factored by every thread (columns past n act as identity)
-        float l[PI_W][PI_W];
+        if (below > 0) {   // ---- 3. trailing update, lower 4 x 4 tiles
+            const int tm = below / 4, ntiles = tm * (tm + 1) / 2;
+            for (int t = tid; t < ntiles; t += PI_THREADS) {
+                int ti = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+                while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+                while (ti * (ti + 1) / 2 > t) --ti;
+                const int tj = t - ti * (ti + 1) / 2;
+                const int r0 = j0 + PI_BS + 4 * ti, c0 = j0 + PI_BS + 4 * tj;
+                float acc[4][4];
 #pragma unroll
-        for (int a = 0; a < PI_W; ++a)
+                for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int b = 0; b <= a; ++b) l[a][b] = (c0 + a < n) ? col[b * PI_NB + c0 + a] : (a == b ? 1.f : 0.f);
-        float il[PI_W];   // 1 / l[k][k]
+                    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 8
+                for (int k = 0; k < PI_BS; ++k) {
+                    const float4 a = *reinterpret_cast<const float4*>(sP + k * PI_NB + r0);
+                    const float4 b = *reinterpret_cast<const float4*>(sP + k * PI_NB + c0);
+                    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-        for (int k = 0; k < PI_W; ++k) {
-            float d = l[k][k];
+                    for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int m = 0; m < k; ++m) d = fmaf(-l[k][m], l[k][m], d);
-            if (!(d > 0.f)) {
-                if (tid == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0) *err_col = col_offset + c0 + k;
-                d = 1.f;
-            }
-            l[k][k] = sqrtf(d);
-            il[k] = 1.f / l[k][k];
-#pragma unroll
-            for (int a = k + 1; a < PI_W; ++a) {
-                float x = l[a][k];
-#pragma unroll
-                for (int m = 0; m < k; ++m) x = fmaf(-l[a][m], l[k][m], x);
-                l[a][k] = x * il[k];
-            }
-        }
-        // L values of the 4 columns for the rows / columns this thread holds (x D^-T = a);
-        // rows (warp-uniform) and column groups above the step are skipped
-        const int t0 = c0 + PI_W;
-        float lr[8][PI_W], lc[4][PI_W];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int r = tr + 16 * i;
-#pragma unroll
-            for (int k = 0; k < PI_W; ++k) lr[i][k] = 0.f;
-            if (r >= t0) {
-#pragma unroll
-                for (int k = 0; k < PI_W; ++k) {
-                    float x = col[k * PI_NB + r];
-#pragma unroll
-                    for (int m = 0; m < k; ++m) x = fmaf(-lr[i][m], l[k][m], x);
-                    lr[i][k] = x * il[k];
-                }
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int c = tc + 32 * q;
-#pragma unroll
-            for (int k = 0; k < PI_W; ++k) lc[q][k] = 0.f;
-            if (32 * q + 31 >= t0) {
-#pragma unroll
-                for (int k = 0; k < PI_W; ++k) {
-                    float x = c >= t0 ? col[k * PI_NB + c] : 0.f;
-#pragma unroll
-                    for (int m = 0; m < k; ++m) x = fmaf(-lc[q][m], l[k][m], x);
-                    lc[q][k] = x * il[k];
-                }
-            }
-        }
-        // rank-4 update of the trailing elements (zero L values elsewhere)
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (tr + 16 * i < t0) continue;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                if (32 * q + 31 < t0) continue;
-#pragma unroll
-                for (int k = 0; k < PI_W; ++k) v[i][q] = fmaf(-lr[i][k], lc[q][k], v[i][q]);
-            }
-        }
-        if (k_own >= 0 && k_own < PI_W) {   // the 4 columns are final
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int r = tr + 16 * i;
-                float x = 0.f;
-#pragma unroll
-                for (int k = 0; k < PI_W; ++k) {
-                    if (k == k_own) x = r >= c0 + PI_W ? lr[i][k] : 0.f;
-#pragma unroll
-                    for (int a = k; a < PI_W; ++a)
-                        if (k == k_own && r == c0 + a) x = l[a][k];
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (q == qj && r >= c0) v[i][q] = x;
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (c0 + j <= r0 + i) sA[(r0 + i) * PI_LD + c0 + j] -= acc[i][j];
             }
+            __syncthreads();
         }
     }
-    __syncthreads();
+    // ---- off-diagonal blocks of the inverse, block row I
+    for (int I = 1; I < 4; ++I) {
+        for (int t = tid; t < I * 64; t += PI_THREADS) {   // T_IJ = sum_{K=J}^{I-1} L_IK X_KJ
+            const int J = t / 64, ti = (t % 64) / 8, tj = t % 8;
+            const int r0 = PI_BS * I + 4 * ti, c0 = PI_BS * J + 4 * tj;
+            float acc[4][4];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+            for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int r = tr + 16 * i, c = tc + 32 * q;
-            sL[r * PI_LD + c] = (r >= c && r < n && c < n) ? v[i][q] : 0.f;
+                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+            for (int k = PI_BS * J; k < PI_BS * I; ++k) {
+                float av[4], bv[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) av[i] = sA[(r0 + i) * PI_LD + k];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) bv[j] = sX[k * PI_LD + c0 + j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+            }
+            float* T = sT + J * PI_BS * PI_TLD;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) T[(4 * ti + i) * PI_TLD + 4 * tj + j] = acc[i][j];
         }
-    __syncthreads();
+        __syncthreads();
+        for (int t = tid; t < I * 64; t += PI_THREADS) {   // X_IJ = -X_II T_IJ
+            const int J = t / 64, ti = (t % 64) / 8, tj = t % 8;
+            const int r0 = PI_BS * I + 4 * ti, c0 = PI_BS * J + 4 * tj;
+            const float* T = sT + J * PI_BS * PI_TLD;
+            float acc[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+            for (int k = 0; k < PI_BS; ++k) {
+                float av[4], bv[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) av[i] = sX[(r0 + i) * PI_LD + PI_BS * I + k];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) bv[j] = T[k * PI_TLD + 4 * tj + j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) sX[(r0 + i) * PI_LD + c0 + j] = -acc[i][j];
+        }
+        __syncthreads();
+    }
     for (int e = tid; e < n * n; e += PI_THREADS) {
         const int r = e % n, c = e / n;
-        if (r >= c) A[r + (int64_t)c * lda] = sL[r * PI_LD + c];
+        if (r >= c) A[r + (int64_t)c * lda] = sA[r * PI_LD + c];
     }
-    // ---- inverse: L X = I, right-looking over the rows of X, 4 rows per step
+    for (int e = tid; e < PI_NB * PI_NB / 4; e += PI_THREADS) {   // float4 stores (64 KB-aligned blocks)
+        {   // column-major Linv: 4 rows of one column
+            const int r = (e % 32) * 4, c = e / 32;
+            float v[4];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[i][q] = (tr + 16 * i == tc + 32 * q && tc + 32 * q < n) ? 1.f : 0.f;
-    for (int r0 = 0; r0 < n; r0 += PI_W) {
-        float* row = buf + ((r0 / PI_W) & 1) * PI_W * PI_NB;   // row[k * 128 + c] = w[r0 + k][c]
-        const int ij = r0 >> 4, k_own = tr - (r0 & 15);
-        if (k_own >= 0 && k_own < PI_W) {
+            for (int q = 0; q < 4; ++q) v[q] = (r + q < n && c < n) ? sX[(r + q) * PI_LD + c] : 0.f;
+            reinterpret_cast<float4*>(Linv)[e] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+        {   // K-major rows: B[rr][cc] = Linv[rr][cc], 4 columns of one row
+            const int rr = e / 32, cc = (e % 32) * 4;
+            float h[4], w[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                float x = v[0][q];
-#pragma unroll
-                for (int i = 1; i < 8; ++i) x = (i == ij) ? v[i][q] : x;
-                row[k_own * PI_NB + tc + 32 * q] = x;
+                w[q] = (rr < n && cc + q < n) ? sX[rr * PI_LD + cc + q] : 0.f;
+                h[q] = __uint_as_float(__float_as_uint(w[q]) & 0xFFFFE000u);
             }
+            reinterpret_cast<float4*>(Bh)[e] = make_float4(h[0], h[1], h[2], h[3]);
+            reinterpret_cast<float4*>(Bl)[e] = make_float4(w[0] - h[0], w[1] - h[1], w[2] - h[2], w[3] - h[3]);
         }
-        __syncthreads();
-        // rows r0..r0+3 of X for the columns this thread holds: D x = w
-        float l[PI_W][PI_W];
-#pragma unroll
-        for (int a = 0; a < PI_W; ++a)
-#pragma unroll
-            for (int b = 0; b <= a; ++b)
-                l[a][b] = (r0 + a < n) ? sL[(r0 + a) * PI_LD + r0 + b] : (a == b ? 1.f : 0.f);
-        // X is lower triangular: column groups right of the step hold zeros (skipped)
-        float xr[4][PI_W];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int c = tc + 32 * q;
-#pragma unroll
-            for (int k = 0; k < PI_W; ++k) xr[q][k] = 0.f;
-            if (32 * q <= r0 + PI_W - 1) {
-#pragma unroll
-                for (int k = 0; k < PI_W; ++k) {
-                    float x = row[k * PI_NB + c];
-#pragma unroll
-                    for (int m = 0; m < k; ++m) x = fmaf(-l[k][m], xr[q][m], x);
-                    xr[q][k] = x / l[k][k];
-                }
-            }
-        }
-        if (k_own >= 0 && k_own < PI_W) {   // the 4 rows are final
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                float x = xr[q][0];
-#pragma unroll
-                for (int k = 1; k < PI_W; ++k) x = (k == k_own) ? xr[q][k] : x;
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    if (i == ij) v[i][q] = x;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int r = tr + 16 * i;
-            if (r >= r0 + PI_W && r < n) {
-                float lk[PI_W];
-#pragma unroll
-                for (int k = 0; k < PI_W; ++k) lk[k] = sL[r * PI_LD + r0 + k];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (32 * q > r0 + PI_W - 1) continue;
-#pragma unroll
-                    for (int k = 0; k < PI_W; ++k) v[i][q] = fmaf(-lk[k], xr[q][k], v[i][q]);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    float* sX = sL;   // the factor is no longer needed: reuse its storage for X
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int r = tr + 16 * i, c = tc + 32 * q;
-            sX[r * PI_LD + c] = (r >= c && r < n && c < n) ? v[i][q] : 0.f;
-        }
-    __syncthreads();
-    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
-        const int r = e % PI_NB, c = e / PI_NB;
-        Linv[r + c * PI_NB] = sX[r * PI_LD + c];    // column-major
-        const int rr = e / PI_NB, cc = e % PI_NB;   // K-major rows: B[rr][cc] = Linv[rr][cc]
-        const float w = sX[rr * PI_LD + cc];
-        const float h = __uint_as_float(__float_as_uint(w) & 0xFFFFE000u);
-        Bh[rr * PI_NB + cc] = h;
-        Bl[rr * PI_NB + cc] = w - h;
     }
 }
 
@@ -943,7 +944,7 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
                float* Bl, cudaStream_t s) {
     if (n <= 0 || n > PI_NB) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
     ProfScope prof_("potrf_inv", s);
-    const size_t sm = ((size_t)PI_NB * PI_LD + 2 * PI_W * PI_NB) * sizeof(float);
+    const size_t sm = PI_SMEM;
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(potrf_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
