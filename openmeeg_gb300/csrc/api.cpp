@@ -33,8 +33,9 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
                 const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
                 const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
                 double tol, int perm, double* out, int64_t ldo, double* p1tmp, int mixed, cudaStream_t s);
-void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
-                 double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
+void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int nseg, const int64_t* seg, const int32_t* cand,
+                 int perm, double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals,
+                 cudaStream_t s);
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
                  double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s,
                  double mag = kMagFactor);
@@ -250,8 +251,13 @@ static void upload_geometry(omg_geometry g) {
     for (int m = 0; m < h.nmesh; ++m) jump[m] = h.conductivity_jump(m);
     g->jump = upload(g->bufs, jump, s);
     std::vector<int32_t> cand;
-    for (int m : h.eeg_meshes)
+    std::vector<int64_t> seg{0};   // one candidate segment per interface, in the reference's visiting order
+    for (int m : h.eeg_meshes) {
         for (int64_t t = h.tbeg[m]; t < h.tbeg[m + 1]; ++t) cand.push_back((int32_t)t);
+        seg.push_back((int64_t)cand.size());
+    }
+    g->n_eeg_seg = (int)seg.size() - 1;
+    g->eeg_seg = upload(g->bufs, seg, s);
     g->n_eeg_cand = (int64_t)cand.size();
     g->eeg_cand = upload(g->bufs, cand, s);
     g->ndom = (int)h.domains.size();
@@ -609,11 +615,33 @@ static void solve_ldlt(omg_solver sv, const T* A, int64_t ld, T* B, int64_t ldb,
 constexpr int NB64 = 128;   // FP64 diagonal block (128 x 129 x 8 B of shared memory)
 constexpr int NB32 = 128;   // FP32 diagonal block
 
+// A current barrier that encloses a non-conductive hole (a barrier mesh that is
+// not outermost, geometry.cpp:424-461) leaves the constant potential on its
+// vertices in the head matrix's null space: the N block of a closed mesh and
+// the solid angles the D blocks sum to both vanish on it, and the reference
+// deflates only the outermost meshes (assembleHeadMat.cpp:27-60), so its head
+// matrix is singular there.  The solver deflates each such mesh as the
+// reference deflates an outermost one (M(v1, v2) += M(i0, i0) / n over the
+// mesh's vertex block), which selects the solution orthogonal to that
+// constant and changes nothing else; sensor rows and the gains do not see the
+// direction.  The HeadMat returned to callers is left as the reference's.
+static void deflate_enclosed_barriers(omg_solver sv, double* hm, int64_t ld) {
+    const HostGeometry& h = sv->geo->h;
+    for (int m = 0; m < h.nmesh; ++m) {
+        if (!h.barrier[m] || h.outermost[m]) continue;
+        const int64_t nb = h.vbeg[m + 1] - h.vbeg[m];
+        if (nb > 0)
+            launch_deflate(sv->geo->d, {{h.vbeg[m], h.vbeg[m + 1]}}, h.vbeg[m], nb, hm, ld, sv->ctx->d_scalar,
+                           sv->ctx->stream);
+    }
+}
+
 // Factor the internal-order HeadMat held in `hm` (FP64, lower), taking ownership.
 void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
     if (check) reset_err(sv->ctx);   // unchecked (captured) factorizations keep earlier flags
+    deflate_enclosed_barriers(sv, hm.as<double>(), N);
     if (sv->precision == OMG_PREC_FP64) {
         sv->A64 = std::move(hm);
         factor_ldlt<double>(sv, sv->A64.as<double>(), N, NB64);
@@ -1161,7 +1189,8 @@ int omg_head2eegmat_dev(omg_context ctx, omg_geometry geo, const double* electro
         set_device(ctx);
         reset_err(ctx);
         if (h2em) OMG_CUDA(cudaMemsetAsync(h2em, 0, (size_t)n_electrodes * geo->h.N * 8, ctx->stream));
-        launch_h2em(geo->d, electrodes, n_electrodes, geo->n_eeg_cand, geo->eeg_cand, 0, h2em, n_electrodes, 1, 0,
+        launch_h2em(geo->d, electrodes, n_electrodes, geo->n_eeg_seg, geo->eeg_seg, geo->eeg_cand, 0, h2em,
+                    n_electrodes, 1, 0,
                     sparse_cols, sparse_vals, ctx->stream);
         check_err(ctx, "Head2EEGMat");
     });
@@ -1743,7 +1772,8 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
     if (ne > 0) {
         OMG_REQUIRE(geo->n_eeg_cand > 0, "no interface touches a zero-conductivity domain");
-        launch_h2em(geo->d, el, ne, geo->n_eeg_cand, geo->eeg_cand, 1, B.as<double>(), 1, N, 0, nullptr, nullptr, s);
+        launch_h2em(geo->d, el, ne, geo->n_eeg_seg, geo->eeg_seg, geo->eeg_cand, 1, B.as<double>(), 1, N, 0, nullptr,
+                    nullptr, s);
     }
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
     if (nm > 0) launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);

@@ -33,8 +33,9 @@
 #include "pipeline.h"
 
 namespace omg {
-void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
-                 double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s);
+void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int nseg, const int64_t* seg, const int32_t* cand,
+                 int perm, double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals,
+                 cudaStream_t s);
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
                  double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s,
                  double mag = kMagFactor);
@@ -157,8 +158,9 @@ void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
         assemble_headmat_internal(g, b->hm_it, hm.as<double>(), N);
     DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
     OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
-    if (ne > 0) launch_h2em(g->d, m.el.as<double>(), ne, g->n_eeg_cand, g->eeg_cand, 1, B.as<double>(), 1, N, 0,
-                            nullptr, nullptr, s);
+    if (ne > 0)
+        launch_h2em(g->d, m.el.as<double>(), ne, g->n_eeg_seg, g->eeg_seg, g->eeg_cand, 1, B.as<double>(), 1, N, 0,
+                    nullptr, nullptr, s);
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * g->h.nt * 8, s);
     if (nm > 0)
         launch_h2mm(g->d, m.sq.as<double>(), nm, g->tmesh, g->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);

@@ -1237,31 +1237,44 @@ __global__ void dsm_gather_kernel(int64_t dip0, int64_t ndc, int64_t nv, int64_t
     if (any) out[(perm ? nP + v : v) + (dip0 + il) * ldo] = sum;
 }
 
-// ---- Head2EEGMat: nearest triangle by Danielsson's point-triangle distance
-// (danielsson.cpp:26-128); one CTA per electrode, fixed-order min reduction.
-__device__ double danielsson(d3 p, const d3 P[3], double al[3]) {
+// Danielsson's point-triangle distance (danielsson.cpp:26-74) with every
+// operation rounded separately, in the reference's order (Vect3 dotprod and
+// norm, vect3.h:72-73,111): no contraction into fused multiply-adds, so the
+// distances equal the reference's double-precision ones bit for bit.  A point
+// above an edge shared by two triangles is mathematically equidistant from
+// both; which one is "nearest" is decided by the rounding of these
+// operations, and EITSourceMat injects current into that triangle (and
+// Head2EEGMat, with several interfaces, pairs it with another's weights).
+__device__ __forceinline__ double dot_rn(d3 a, d3 b) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ d3 sub_rn(d3 a, d3 b) {
+    return {__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)};
+}
+__device__ double danielsson_rn(d3 p, const d3 P[3], double al[3]) {
     int idx[3] = {0, 1, 2};
     int nb = 3;
     al[0] = al[1] = al[2] = 0.0;
     for (;;) {
         if (nb == 1) {
             al[idx[0]] = 1.0;
-            return dev::norm(p - P[idx[0]]);
+            const d3 d = sub_rn(p, P[idx[0]]);
+            return __dsqrt_rn(dot_rn(d, d));
         }
         d3 A0Ai[3];
-        for (int i = 1; i < nb; ++i) A0Ai[i] = P[idx[i]] - P[idx[0]];
-        const d3 A0M = p - P[idx[0]];
+        for (int i = 1; i < nb; ++i) A0Ai[i] = sub_rn(P[idx[i]], P[idx[0]]);
+        const d3 A0M = sub_rn(p, P[idx[0]]);
         if (nb == 2) {
-            al[idx[1]] = dev::dot(A0M, A0Ai[1]) / dev::dot(A0Ai[1], A0Ai[1]);
-            al[idx[0]] = 1.0 - al[idx[1]];
+            al[idx[1]] = __ddiv_rn(dot_rn(A0M, A0Ai[1]), dot_rn(A0Ai[1], A0Ai[1]));
+            al[idx[0]] = __dsub_rn(1.0, al[idx[1]]);
         } else {
-            const double a00 = dev::dot(A0Ai[1], A0Ai[1]), a10 = dev::dot(A0Ai[1], A0Ai[2]),
-                         a11 = dev::dot(A0Ai[2], A0Ai[2]);
-            const double b0 = dev::dot(A0M, A0Ai[1]), b1 = dev::dot(A0M, A0Ai[2]);
-            const double dd = a00 * a11 - a10 * a10;
-            al[idx[1]] = (b0 * a11 - b1 * a10) / dd;
-            al[idx[2]] = (a00 * b1 - a10 * b0) / dd;
-            al[idx[0]] = 1.0 - al[idx[1]] - al[idx[2]];
+            const double a00 = dot_rn(A0Ai[1], A0Ai[1]), a10 = dot_rn(A0Ai[1], A0Ai[2]),
+                         a11 = dot_rn(A0Ai[2], A0Ai[2]);
+            const double b0 = dot_rn(A0M, A0Ai[1]), b1 = dot_rn(A0M, A0Ai[2]);
+            const double dd = __dsub_rn(__dmul_rn(a00, a11), __dmul_rn(a10, a10));
+            al[idx[1]] = __ddiv_rn(__dsub_rn(__dmul_rn(b0, a11), __dmul_rn(b1, a10)), dd);
+            al[idx[2]] = __ddiv_rn(__dsub_rn(__dmul_rn(a00, b1), __dmul_rn(a10, b0)), dd);
+            al[idx[0]] = __dsub_rn(__dsub_rn(1.0, al[idx[1]]), al[idx[2]]);
         }
         int neg = -1;
         for (int i = 0; i < nb; ++i)
@@ -1277,55 +1290,79 @@ __device__ double danielsson(d3 p, const d3 P[3], double al[3]) {
             --nb;
             continue;
         }
-        d3 MH = A0M * -1.0;
-        for (int i = 1; i < nb; ++i) MH = MH + A0Ai[i] * al[idx[i]];
-        return dev::norm(MH);
+        d3 MH = {-A0M.x, -A0M.y, -A0M.z};
+        for (int i = 1; i < nb; ++i) {
+            const double a = al[idx[i]];
+            MH = {__dadd_rn(MH.x, __dmul_rn(a, A0Ai[i].x)), __dadd_rn(MH.y, __dmul_rn(a, A0Ai[i].y)),
+                  __dadd_rn(MH.z, __dmul_rn(a, A0Ai[i].z))};
+        }
+        return __dsqrt_rn(dot_rn(MH, MH));
     }
 }
 
-__global__ void h2em_kernel(const double* __restrict__ pos, int64_t ncand, const int32_t* __restrict__ cand,
-                            const double* __restrict__ srec, const int32_t* __restrict__ T, int64_t nP, int perm,
-                            double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals) {
+// ---- Head2EEGMat (assembleSensors.cpp:25-39): nearest triangle by Danielsson's
+// point-triangle distance over the interfaces that touch a zero-conductivity
+// domain (dist_point_geom, danielsson.cpp:107-128), one CTA per electrode, a
+// fixed-order min reduction per interface (candidate segment).  The interfaces
+// are visited in the reference's order and each one leaves the weights of its
+// own nearest triangle in the shared result, so the electrode's weights are
+// those of the last interface's nearest triangle while its triangle is the
+// overall nearest (first strictly smaller distance) -- as the reference does.
+__global__ void h2em_kernel(const double* __restrict__ pos, int nseg, const int64_t* __restrict__ seg,
+                            const int32_t* __restrict__ cand, const double* __restrict__ srec,
+                            const int32_t* __restrict__ T, int64_t nP, int perm, double* dense, int64_t rs,
+                            int64_t cs, int64_t col0, int64_t* scols, double* svals) {
     __shared__ double sd[256];
     __shared__ int64_t so[256];
     __shared__ double sa[256][3];
     const int64_t e = blockIdx.x;
     const d3 p = dev::ld3(pos + 3 * e);
-    double best = 1.79769313486231570e+308, bal[3] = {0, 0, 0};
-    int64_t bo = INT64_MAX;
-    for (int64_t k = threadIdx.x; k < ncand; k += blockDim.x) {
-        const double* s = srec + (int64_t)cand[k] * SREC;
-        const d3 P[3] = {dev::ld3(s), dev::ld3(s + 3), dev::ld3(s + 6)};
-        double al[3];
-        const double dist = danielsson(p, P, al);
-        if (dist < best) {
-            best = dist;
-            bo = k;
-            bal[0] = al[0]; bal[1] = al[1]; bal[2] = al[2];
-        }
-    }
-    sd[threadIdx.x] = best;
-    so[threadIdx.x] = bo;
-    sa[threadIdx.x][0] = bal[0]; sa[threadIdx.x][1] = bal[1]; sa[threadIdx.x][2] = bal[2];
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            const int o = threadIdx.x + w;
-            if (sd[o] < sd[threadIdx.x] || (sd[o] == sd[threadIdx.x] && so[o] < so[threadIdx.x])) {
-                sd[threadIdx.x] = sd[o];
-                so[threadIdx.x] = so[o];
-                sa[threadIdx.x][0] = sa[o][0]; sa[threadIdx.x][1] = sa[o][1]; sa[threadIdx.x][2] = sa[o][2];
+    double gbest = 1.79769313486231570e+308, w[3] = {0, 0, 0};
+    int64_t gtri = -1;
+    for (int q = 0; q < nseg; ++q) {
+        double best = 1.79769313486231570e+308, bal[3] = {0, 0, 0};
+        int64_t bo = INT64_MAX;
+        for (int64_t k = seg[q] + threadIdx.x; k < seg[q + 1]; k += blockDim.x) {
+            const double* s = srec + (int64_t)cand[k] * SREC;
+            const d3 P[3] = {dev::ld3(s), dev::ld3(s + 3), dev::ld3(s + 6)};
+            double al[3];
+            const double dist = danielsson_rn(p, P, al);
+            if (dist < best) {
+                best = dist;
+                bo = k;
+                bal[0] = al[0]; bal[1] = al[1]; bal[2] = al[2];
             }
+        }
+        sd[threadIdx.x] = best;
+        so[threadIdx.x] = bo;
+        sa[threadIdx.x][0] = bal[0]; sa[threadIdx.x][1] = bal[1]; sa[threadIdx.x][2] = bal[2];
+        __syncthreads();
+        for (int wd = blockDim.x / 2; wd > 0; wd >>= 1) {
+            if (threadIdx.x < wd) {
+                const int o = threadIdx.x + wd;
+                if (sd[o] < sd[threadIdx.x] || (sd[o] == sd[threadIdx.x] && so[o] < so[threadIdx.x])) {
+                    sd[threadIdx.x] = sd[o];
+                    so[threadIdx.x] = so[o];
+                    sa[threadIdx.x][0] = sa[o][0]; sa[threadIdx.x][1] = sa[o][1]; sa[threadIdx.x][2] = sa[o][2];
+                }
+            }
+            __syncthreads();
+        }
+        if (so[0] != INT64_MAX) {
+            if (sd[0] < gbest) {
+                gbest = sd[0];
+                gtri = cand[so[0]];
+            }
+            w[0] = sa[0][0]; w[1] = sa[0][1]; w[2] = sa[0][2];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const int64_t t = cand[so[0]];
+    if (threadIdx.x == 0 && gtri >= 0) {
         for (int j = 0; j < 3; ++j) {
-            const int64_t v = T[3 * t + j];
-            if (dense) dense[(perm ? nP + v : v) * rs + (col0 + e) * cs] = sa[0][j];
+            const int64_t v = T[3 * gtri + j];
+            if (dense) dense[(perm ? nP + v : v) * rs + (col0 + e) * cs] = w[j];
             if (scols) scols[3 * e + j] = v;
-            if (svals) svals[3 * e + j] = sa[0][j];
+            if (svals) svals[3 * e + j] = w[j];
         }
     }
 }
@@ -1435,11 +1472,12 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
     check_launch("DSM gather");
 }
 
-void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand, int perm,
-                 double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals, cudaStream_t s) {
+void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int nseg, const int64_t* seg, const int32_t* cand,
+                 int perm, double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals,
+                 cudaStream_t s) {
     if (ne == 0) return;
     ProfScope prof_("h2em", s);
-    h2em_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, ncand, cand, g.srec, g.T, g.nP, perm, dense, rs, cs, col0, scols,
+    h2em_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, nseg, seg, cand, g.srec, g.T, g.nP, perm, dense, rs, cs, col0, scols,
                                              svals);
     check_launch("H2EM");
 }
@@ -1791,67 +1829,6 @@ void launch_dipole_internal_pot(const double* pts, const int* pdom, const int64_
 // one row of Nref (reference-numbered) columns per injection triangle.
 // ---------------------------------------------------------------------------
 
-// Danielsson's point-triangle distance (danielsson.cpp:26-74) with every
-// operation rounded separately, in the reference's order (Vect3 dotprod and
-// norm, vect3.h:72-73,111): no contraction into fused multiply-adds, so the
-// distances equal the reference's double-precision ones bit for bit.  A point
-// above an edge shared by two triangles is mathematically equidistant from
-// both; which one is "nearest" is decided by the rounding of these
-// operations, and EITSourceMat injects current into that triangle.
-__device__ __forceinline__ double dot_rn(d3 a, d3 b) {
-    return __dadd_rn(__dadd_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)), __dmul_rn(a.z, b.z));
-}
-__device__ __forceinline__ d3 sub_rn(d3 a, d3 b) {
-    return {__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y), __dsub_rn(a.z, b.z)};
-}
-__device__ double danielsson_rn(d3 p, const d3 P[3]) {
-    int idx[3] = {0, 1, 2};
-    int nb = 3;
-    double al[3] = {0.0, 0.0, 0.0};
-    for (;;) {
-        if (nb == 1) {
-            const d3 d = sub_rn(p, P[idx[0]]);
-            return __dsqrt_rn(dot_rn(d, d));
-        }
-        d3 A0Ai[3];
-        for (int i = 1; i < nb; ++i) A0Ai[i] = sub_rn(P[idx[i]], P[idx[0]]);
-        const d3 A0M = sub_rn(p, P[idx[0]]);
-        if (nb == 2) {
-            al[idx[1]] = __ddiv_rn(dot_rn(A0M, A0Ai[1]), dot_rn(A0Ai[1], A0Ai[1]));
-            al[idx[0]] = __dsub_rn(1.0, al[idx[1]]);
-        } else {
-            const double a00 = dot_rn(A0Ai[1], A0Ai[1]), a10 = dot_rn(A0Ai[1], A0Ai[2]),
-                         a11 = dot_rn(A0Ai[2], A0Ai[2]);
-            const double b0 = dot_rn(A0M, A0Ai[1]), b1 = dot_rn(A0M, A0Ai[2]);
-            const double dd = __dsub_rn(__dmul_rn(a00, a11), __dmul_rn(a10, a10));
-            al[idx[1]] = __ddiv_rn(__dsub_rn(__dmul_rn(b0, a11), __dmul_rn(b1, a10)), dd);
-            al[idx[2]] = __ddiv_rn(__dsub_rn(__dmul_rn(a00, b1), __dmul_rn(a10, b0)), dd);
-            al[idx[0]] = __dsub_rn(__dsub_rn(1.0, al[idx[1]]), al[idx[2]]);
-        }
-        int neg = -1;
-        for (int i = 0; i < nb; ++i)
-            if (al[idx[i]] < 0) {
-                neg = i;
-                break;
-            }
-        if (neg >= 0) {
-            al[idx[neg]] = 0;
-            const int tmp = idx[neg];
-            idx[neg] = idx[nb - 1];
-            idx[nb - 1] = tmp;
-            --nb;
-            continue;
-        }
-        d3 MH = {-A0M.x, -A0M.y, -A0M.z};
-        for (int i = 1; i < nb; ++i) {
-            const double a = al[idx[i]];
-            MH = {__dadd_rn(MH.x, __dmul_rn(a, A0Ai[i].x)), __dadd_rn(MH.y, __dmul_rn(a, A0Ai[i].y)),
-                  __dadd_rn(MH.z, __dmul_rn(a, A0Ai[i].z))};
-        }
-        return __dsqrt_rn(dot_rn(MH, MH));
-    }
-}
-
 // Nearest candidate triangle per electrode (dist_point_geom,
 // danielsson.cpp:107-128): one CTA per electrode, ties to the first candidate
 // (the reference keeps the first strictly smaller distance).
@@ -1867,7 +1844,8 @@ __global__ void nearest_triangle_kernel(const double* __restrict__ pos, int64_t 
     for (int64_t k = threadIdx.x; k < ncand; k += blockDim.x) {
         const double* s = srec + (int64_t)cand[k] * SREC;
         const d3 P[3] = {dev::ld3(s), dev::ld3(s + 3), dev::ld3(s + 6)};
-        const double dist = danielsson_rn(p, P);
+        double al[3];
+        const double dist = danielsson_rn(p, P, al);
         if (dist < best) {
             best = dist;
             bo = k;

@@ -10,6 +10,7 @@
 //   pair coefficients       OpenMEEG/src/assembleHeadMat.cpp:92-95
 //   nestedness              OpenMEEG/src/geometry.cpp:369-401
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <fstream>
@@ -318,6 +319,98 @@ void read_tri(const std::string& path, std::vector<double>& V, std::vector<int64
 
 }  // namespace
 
+// .geom v1.1 (GeomFile.h:160-300): an optional "Meshes" section of named
+// mesh files, "Interfaces" given either as mesh files (one mesh each) or as
+// lists of +/-mesh names, and "Domains" as lists of +/-interface names (a '-'
+// means inside, '+' or no sign outside; "shared" ends the list).  Entries
+// without a "Name:" get the names "1", "2", ... in order.  Meshes are .tri or
+// .off files.  Interfaces must consist of one mesh each here, and meshes may
+// not share vertices.
+namespace {
+
+struct GeomEntry {
+    std::string name, rest;   // rest: the line after "Keyword name:" (or the whole line)
+};
+
+GeomEntry split_entry(const std::string& line, const std::string& keyword, unsigned index) {
+    std::string s = line;
+    s.erase(0, s.find_first_not_of(" \t\r"));
+    GeomEntry e;
+    e.name = std::to_string(index + 1);
+    if (s.compare(0, keyword.size(), keyword) == 0) {
+        std::string after = s.substr(keyword.size());
+        auto c = after.find(':');
+        if (c != std::string::npos) {
+            std::string nm = after.substr(0, c);
+            nm.erase(0, nm.find_first_not_of(" \t"));
+            nm.erase(nm.find_last_not_of(" \t\r") == std::string::npos ? 0 : nm.find_last_not_of(" \t\r") + 1);
+            if (!nm.empty()) e.name = nm;
+            e.rest = after.substr(c + 1);
+            return e;
+        }
+    }
+    e.rest = s;
+    return e;
+}
+
+std::string entry_filename(const std::string& rest, const std::string& dir) {
+    std::string fn;
+    auto q1 = rest.find('"');
+    if (q1 != std::string::npos) {
+        fn = rest.substr(q1 + 1, rest.find('"', q1 + 1) - q1 - 1);
+    } else {
+        std::istringstream es(rest);
+        es >> fn;
+    }
+    if (fn.empty()) throw Error(OMG_ERR_IO, "missing file name in geometry file");
+    return fn[0] == '/' ? fn : dir + fn;
+}
+
+std::vector<std::string> tokens_of(const std::string& s) {
+    std::istringstream is(s);
+    std::vector<std::string> out;
+    std::string t;
+    while (is >> t) out.push_back(t);
+    return out;
+}
+
+// OFF (MeshIOs/off.h): "OFF", "nv nt 0", nv vertices, nt lines "3 i j k".
+void read_off(const std::string& path, std::vector<double>& V, std::vector<int64_t>& T) {
+    std::ifstream f(path);
+    if (!f) throw Error(OMG_ERR_IO, "cannot open mesh " + path);
+    std::string magic;
+    f >> magic;
+    if (magic != "OFF") throw Error(OMG_ERR_IO, "not an OFF file: " + path);
+    std::string tok;
+    int64_t nv = 0, nt = 0, ne = 0;
+    while (f >> tok && tok[0] == '#') std::getline(f, tok);   // comments before the counts
+    nv = std::stoll(tok);
+    f >> nt >> ne;
+    if (!f || nv <= 0 || nt <= 0) throw Error(OMG_ERR_IO, "bad OFF header in " + path);
+    V.resize(3 * nv);
+    for (int64_t i = 0; i < 3 * nv; ++i) f >> V[i];
+    T.resize(3 * nt);
+    for (int64_t i = 0; i < nt; ++i) {
+        int64_t k;
+        f >> k >> T[3 * i] >> T[3 * i + 1] >> T[3 * i + 2];
+        if (k != 3) throw Error(OMG_ERR_UNSUPPORTED, "OFF faces must be triangles: " + path);
+    }
+    if (!f) throw Error(OMG_ERR_IO, "truncated OFF file " + path);
+}
+
+void read_mesh_file(const std::string& path, std::vector<double>& V, std::vector<int64_t>& T) {
+    const auto dot = path.find_last_of('.');
+    const std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
+    if (ext == "tri")
+        read_tri(path, V, T);
+    else if (ext == "off")
+        read_off(path, V, T);
+    else
+        throw Error(OMG_ERR_UNSUPPORTED, "mesh format not supported (only .tri and .off): " + path);
+}
+
+}  // namespace
+
 HostGeometry load_geometry_files(const std::string& geom, const std::string& cond) {
     std::ifstream f(geom);
     if (!f) throw Error(OMG_ERR_IO, "cannot open geometry file " + geom);
@@ -331,61 +424,91 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
         std::string s = strip_comment(line);
         if (s.find_first_not_of(" \t\r") != std::string::npos) lines.push_back(s);
     }
-    std::vector<std::string> meshes;
+    std::vector<std::string> mesh_names, mesh_files;
+    std::vector<std::string> iface_names;
+    std::vector<std::vector<std::pair<std::string, bool>>> iface_meshes;   // (mesh name, normal orientation)
     std::vector<std::string> dnames;
-    std::vector<int32_t> nb, bounds;
+    std::vector<std::vector<std::pair<std::string, bool>>> dbounds;        // (interface name, inside)
+    bool mesh_section = false;
     for (size_t i = 0; i < lines.size(); ++i) {
-        std::istringstream is(lines[i]);
-        std::string key;
-        is >> key;
-        if (key == "Interfaces") {
-            int n;
-            is >> n;
+        std::vector<std::string> head = tokens_of(lines[i]);
+        const std::string& key = head[0];
+        if (key == "MeshFile") {
+            throw Error(OMG_ERR_UNSUPPORTED, "geometry given as one mesh file (MeshFile) is not supported");
+        } else if (key == "Meshes") {
+            mesh_section = true;
+            const int n = std::stoi(head.at(1));
             for (int k = 0; k < n; ++k) {
-                const std::string& e = lines[++i];
-                std::string fn;
-                auto q1 = e.find('"');
-                if (q1 != std::string::npos)
-                    fn = e.substr(q1 + 1, e.find('"', q1 + 1) - q1 - 1);
-                else {
-                    std::istringstream es(e);
-                    std::string tok;
-                    while (es >> tok) fn = tok;
+                GeomEntry e = split_entry(lines.at(++i), "Mesh", (unsigned)k);
+                mesh_names.push_back(e.name);
+                mesh_files.push_back(entry_filename(e.rest, dir));
+            }
+        } else if (key == "Interfaces") {
+            const int n = std::stoi(head.at(1));
+            for (int k = 0; k < n; ++k) {
+                GeomEntry e = split_entry(lines.at(++i), "Interface", (unsigned)k);
+                iface_names.push_back(e.name);
+                if (!mesh_section) {   // meshes given as interfaces
+                    mesh_names.push_back(e.name);
+                    mesh_files.push_back(entry_filename(e.rest, dir));
+                    iface_meshes.push_back({{e.name, true}});
+                } else {
+                    std::vector<std::pair<std::string, bool>> om;
+                    for (std::string t : tokens_of(e.rest)) {
+                        bool normal = true;
+                        if (t[0] == '+' || t[0] == '-') {
+                            normal = t[0] == '+';
+                            t = t.substr(1);
+                        }
+                        om.push_back({t, normal});
+                    }
+                    iface_meshes.push_back(om);
                 }
-                meshes.push_back(fn.size() && fn[0] == '/' ? fn : dir + fn);
             }
         } else if (key == "Domains") {
-            int n;
-            is >> n;
+            const int n = std::stoi(head.at(1));
             for (int k = 0; k < n; ++k) {
-                std::string e = lines[++i];
-                e = e.substr(e.find("Domain") + 6);
-                std::string name, rest;
-                auto c = e.find(':');
-                if (c != std::string::npos) {
-                    name = e.substr(0, c);
-                    rest = e.substr(c + 1);
-                } else {
-                    std::istringstream es(e);
-                    es >> name;
-                    std::getline(es, rest);
+                GeomEntry e = split_entry(lines.at(++i), "Domain", (unsigned)k);
+                std::vector<std::pair<std::string, bool>> b;
+                for (std::string t : tokens_of(e.rest)) {
+                    if (t == "shared") break;
+                    bool inside = false;
+                    if (t[0] == '+' || t[0] == '-') {
+                        inside = t[0] == '-';
+                        t = t.substr(1);
+                    }
+                    b.push_back({t, inside});
                 }
-                name.erase(0, name.find_first_not_of(" \t"));
-                name.erase(name.find_last_not_of(" \t") + 1);
-                std::istringstream rs(rest);
-                std::string tok;
-                int cnt = 0;
-                while (rs >> tok) {
-                    if (tok == "shared") break;
-                    bounds.push_back(std::stoi(tok));
-                    ++cnt;
-                }
-                dnames.push_back(name);
-                nb.push_back(cnt);
+                dnames.push_back(e.name);
+                dbounds.push_back(b);
             }
         }
     }
-    if (meshes.empty() || dnames.empty()) throw Error(OMG_ERR_IO, "no interfaces or domains in " + geom);
+    if (mesh_files.empty() || dnames.empty()) throw Error(OMG_ERR_IO, "no interfaces or domains in " + geom);
+    auto find = [](const std::vector<std::string>& v, const std::string& x) {
+        return (int)(std::find(v.begin(), v.end(), x) - v.begin());
+    };
+    // interface -> its single mesh
+    std::vector<int> iface_mesh(iface_names.size());
+    for (size_t k = 0; k < iface_names.size(); ++k) {
+        if (iface_meshes[k].size() != 1)
+            throw Error(OMG_ERR_UNSUPPORTED, "interface " + iface_names[k] +
+                                                 " is made of several meshes (non-nested shared-vertex geometries "
+                                                 "are not supported)");
+        const int m = find(mesh_names, iface_meshes[k][0].first);
+        if (m == (int)mesh_names.size()) throw Error(OMG_ERR_INVALID, "unknown mesh " + iface_meshes[k][0].first);
+        iface_mesh[k] = m;
+    }
+    std::vector<int32_t> nb, bounds;
+    for (size_t d = 0; d < dnames.size(); ++d) {
+        for (const auto& b : dbounds[d]) {
+            const int k = find(iface_names, b.first);
+            if (k == (int)iface_names.size())
+                throw Error(OMG_ERR_INVALID, "domain " + dnames[d] + " refers to an unknown interface " + b.first);
+            bounds.push_back(b.second ? -(iface_mesh[k] + 1) : (iface_mesh[k] + 1));
+        }
+        nb.push_back((int32_t)dbounds[d].size());
+    }
     std::map<std::string, double> sig;
     std::ifstream fc(cond);
     if (!fc) throw Error(OMG_ERR_IO, "cannot open conductivity file " + cond);
@@ -403,17 +526,27 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
     }
     std::vector<double> V;
     std::vector<int64_t> T, nv, nt;
-    for (const auto& m : meshes) {
+    for (const auto& m : mesh_files) {
         std::vector<double> v;
         std::vector<int64_t> t;
-        read_tri(m, v, t);
+        read_mesh_file(m, v, t);
         V.insert(V.end(), v.begin(), v.end());
         T.insert(T.end(), t.begin(), t.end());
         nv.push_back((int64_t)v.size() / 3);
         nt.push_back((int64_t)t.size() / 3);
     }
-    return build_geometry((int)meshes.size(), nv.data(), V.data(), nt.data(), T.data(), (int)dnames.size(), nb.data(),
-                          bounds.data(), sigma.data(), dnames);
+    // the reference merges vertices with equal coordinates across meshes (Geometry::add_vertex,
+    // geometry.h:100-108); such shared vertices are outside this build's scope
+    {
+        std::vector<std::array<double, 3>> pts(V.size() / 3);
+        for (size_t i = 0; i < pts.size(); ++i) pts[i] = {V[3 * i], V[3 * i + 1], V[3 * i + 2]};
+        std::sort(pts.begin(), pts.end());
+        if (std::adjacent_find(pts.begin(), pts.end()) != pts.end())
+            throw Error(OMG_ERR_UNSUPPORTED, "meshes share vertices (non-nested shared-vertex geometries are not "
+                                             "supported)");
+    }
+    return build_geometry((int)mesh_files.size(), nv.data(), V.data(), nt.data(), T.data(), (int)dnames.size(),
+                          nb.data(), bounds.data(), sigma.data(), dnames);
 }
 
 }  // namespace omg

@@ -122,6 +122,8 @@ struct omg_geometry_s {
     double* jump = nullptr;
     int32_t* eeg_cand = nullptr;
     int64_t n_eeg_cand = 0;
+    int64_t* eeg_seg = nullptr;   // candidate offsets of each interface touching a zero-conductivity domain
+    int n_eeg_seg = 0;
     // domain tables
     int ndom = 0, maxb = 1;
     int* dnb = nullptr;

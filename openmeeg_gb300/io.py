@@ -22,7 +22,9 @@ import struct
 import numpy as np
 
 __all__ = ["read_bin", "write_bin", "packed_upper", "unpack_upper", "write_tri", "read_tri", "write_geom",
-           "write_cond", "write_matrix_txt", "read_matrix_txt", "read_geom", "read_cond"]
+           "write_cond", "write_matrix_txt", "read_matrix_txt", "read_sensors_txt", "read_geom", "read_geom_full",
+           "read_cond",
+           "read_off", "read_mesh", "load_head"]
 
 _U32_MAX = 2**32 - 1
 
@@ -145,37 +147,122 @@ def write_cond(path: str, domains) -> None:
             f.write(f"{name} {_fmt(sigma)}\n")
 
 
-def read_geom(path: str):
-    """Parse a ``.geom`` v1.1 file whose interfaces are single meshes.
-    Returns (mesh_paths, domains without conductivities)."""
+def read_off(path: str):
+    """OFF mesh (MeshIOs/off.h): 'OFF', 'nv nt 0', vertices, faces '3 i j k'."""
+    with open(path) as f:
+        tok = [t for ln in f for t in ln.split("#", 1)[0].split()]
+    if tok[0] != "OFF":
+        raise ValueError(f"{path}: not an OFF file")
+    nv, nt = int(tok[1]), int(tok[2])
+    V = np.array(tok[4:4 + 3 * nv], dtype=np.float64).reshape(nv, 3)
+    F = np.array(tok[4 + 3 * nv:4 + 3 * nv + 4 * nt], dtype=np.int64).reshape(nt, 4)
+    if np.any(F[:, 0] != 3):
+        raise ValueError(f"{path}: OFF faces must be triangles")
+    return V, F[:, 1:].copy()
+
+
+def read_mesh(path: str):
+    """A .tri or .off mesh: (vertices n x 3, triangles m x 3, 0-based)."""
+    if path.endswith(".tri"):
+        return read_tri(path)
+    if path.endswith(".off"):
+        return read_off(path)
+    raise ValueError(f"{path}: only .tri and .off meshes are supported")
+
+
+def _entry(line: str, keyword: str, index: int):
+    """('Keyword name: rest' | 'Keyword: rest' | 'rest') -> (name, rest); unnamed entries are
+    named by their position, 1-based (GeomFile.h:87-91, 114-119)."""
+    s = line.strip()
+    if s.startswith(keyword):
+        after = s[len(keyword):]
+        if ":" in after:
+            name, rest = after.split(":", 1)
+            return (name.strip() or str(index + 1)), rest
+    return str(index + 1), s
+
+
+def _fname(rest: str, base: str) -> str:
+    fn = rest.split('"')[1] if '"' in rest else rest.split()[0]
+    return fn if os.path.isabs(fn) else os.path.join(base, fn)
+
+
+def read_geom_full(path: str):
+    """Parse a ``.geom`` v1.1 file (GeomFile.h:160-300): an optional "Meshes"
+    section, "Interfaces" given as mesh files or as lists of +/-mesh names, and
+    "Domains" as lists of +/-interface names ('-' = inside).  Returns
+    (meshes [(name, path)], interfaces [(name, [(mesh index, +1/-1)])],
+    domains [(name, [(interface index, inside)])])."""
     base = os.path.dirname(os.path.abspath(path))
-    lines = [ln.split("#", 1)[0].strip() if not ln.lstrip().startswith("#") else ""
-             for ln in open(path).read().splitlines()]
     head = open(path).readline()
     if "1.1" not in head:
         raise ValueError("only .geom version 1.1 is supported")
+    lines = [ln.split("#", 1)[0].strip() for ln in open(path).read().splitlines()]
     lines = [ln for ln in lines if ln]
-    meshes, domains = [], []
+    meshes, ifaces, domains = [], [], []
+    mesh_section = False
     i = 0
     while i < len(lines):
-        ln = lines[i]
-        if ln.startswith("Interfaces"):
-            n = int(ln.split()[1])
-            for k in range(n):
+        key = lines[i].split()[0]
+        if key == "MeshFile":
+            raise ValueError("geometries given as one mesh file (MeshFile) are not supported")
+        if key == "Meshes":
+            mesh_section = True
+            for k in range(int(lines[i].split()[1])):
                 i += 1
-                ent = lines[i]
-                fn = ent.split('"')[1] if '"' in ent else ent.split()[-1]
-                meshes.append(fn if os.path.isabs(fn) else os.path.join(base, fn))
-        elif ln.startswith("Domains"):
-            n = int(ln.split()[1])
-            for k in range(n):
+                name, rest = _entry(lines[i], "Mesh", k)
+                meshes.append((name, _fname(rest, base)))
+        elif key == "Interfaces":
+            for k in range(int(lines[i].split()[1])):
                 i += 1
-                ent = lines[i][len("Domain"):].strip()
-                name, rest = ent.split(":", 1) if ":" in ent else (ent.split()[0], " ".join(ent.split()[1:]))
-                bounds = [int(t) for t in rest.split() if t != "shared"]
-                domains.append((name.strip(), bounds))
+                name, rest = _entry(lines[i], "Interface", k)
+                if not mesh_section:
+                    meshes.append((name, _fname(rest, base)))
+                    ifaces.append((name, [(len(meshes) - 1, 1)]))
+                else:
+                    om = []
+                    for t in rest.split():
+                        sign = -1 if t[0] == "-" else 1
+                        t = t[1:] if t[0] in "+-" else t
+                        om.append(([m[0] for m in meshes].index(t), sign))
+                    ifaces.append((name, om))
+        elif key == "Domains":
+            for k in range(int(lines[i].split()[1])):
+                i += 1
+                name, rest = _entry(lines[i], "Domain", k)
+                b = []
+                for t in rest.split():
+                    if t == "shared":
+                        break
+                    inside = t[0] == "-"
+                    t = t[1:] if t[0] in "+-" else t
+                    b.append(([f[0] for f in ifaces].index(t), inside))
+                domains.append((name, b))
         i += 1
-    return meshes, domains
+    return meshes, ifaces, domains
+
+
+def read_geom(path: str):
+    """A ``.geom`` v1.1 file whose interfaces are single meshes: (mesh paths,
+    domains as (name, [signed 1-based mesh ids])), '-' = inside."""
+    meshes, ifaces, domains = read_geom_full(path)
+    for name, om in ifaces:
+        if len(om) != 1:
+            raise ValueError(f"interface {name} is made of several meshes")
+    doms = [(name, [-(ifaces[k][1][0][0] + 1) if inside else ifaces[k][1][0][0] + 1 for k, inside in b])
+            for name, b in domains]
+    return [p for _, p in meshes], doms
+
+
+def load_head(geom_path: str, cond_path: str):
+    """Meshes, names and domains (with conductivities) of a .geom/.cond pair, as
+    the head description that ``Geometry.from_head`` and the oracle take."""
+    from .synthetic import NestedHead
+    meshes, ifaces, _ = read_geom_full(geom_path)
+    paths, doms = read_geom(geom_path)
+    cond = read_cond(cond_path)
+    V, T = zip(*[read_mesh(p) for p in paths])
+    return NestedHead(list(V), list(T), [n for n, _ in meshes], [(n, b, cond[n]) for n, b in doms])
 
 
 def read_cond(path: str) -> dict:
@@ -195,12 +282,24 @@ def write_matrix_txt(path: str, M: np.ndarray) -> None:
 
 
 def read_matrix_txt(path: str) -> np.ndarray:
+    """A plain numeric text matrix (dipole files and the like; the reference's
+    ASCII Matrix reader): one row per non-empty line, '#' comments."""
     rows = []
     for ln in open(path):
         ln = ln.split("#", 1)[0].strip()
         if ln:
-            tok = ln.split()
-            if tok[0].count(".") != 1:  # labelled line
-                tok = tok[1:]
-            rows.append([float(t) for t in tok])
+            rows.append([float(t) for t in ln.split()])
     return np.array(rows, dtype=np.float64)
+
+
+def read_sensors_txt(path: str):
+    """A sensors file (Sensors::load, sensors.cpp:36-120): the lines are
+    labelled unless the first token of some line is a number with exactly one
+    '.'; labels, when present, are the first token of every line.  Returns
+    (labels or None, values n x columns)."""
+    lines = [ln.split("#", 1)[0].split() for ln in open(path)]
+    lines = [t for t in lines if t]
+    labeled = not any(t[0].count(".") == 1 for t in lines)
+    if labeled:
+        return [t[0] for t in lines], np.array([[float(x) for x in t[1:]] for t in lines], dtype=np.float64)
+    return None, np.array([[float(x) for x in t] for t in lines], dtype=np.float64)

@@ -694,24 +694,37 @@ static double dpc(v3 p, const tri_t* T, double alphas[3], int nb, int idx[3], in
  * global triangle id, out_w[3i..3i+2] the weights of its vertices 0..2. */
 int oo_h2em(const oo_geom* g, const double* pos, int64_t ne, int nm, const int* meshes, int64_t* out_tri,
             double* out_w) {
+    /* dist_point_geom (danielsson.cpp:107-128) visits the interfaces in order;
+     * each dist_point_interface call leaves the weights of its own nearest
+     * triangle in the shared `alphas`, so the weights returned are those of the
+     * last interface's nearest triangle, while the triangle is the overall
+     * nearest (first strictly smaller distance). */
     #pragma omp parallel for schedule(dynamic, 1)
     for (int64_t i = 0; i < ne; ++i) {
         v3 p = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
         double best = 1.79769313486231570e+308;
         for (int k = 0; k < nm; ++k) {
             int m = meshes[k];
+            double mbest = 1.79769313486231570e+308;
+            int64_t mt = -1;
+            double mw[3] = {0, 0, 0};
             for (int64_t t = g->mesh_tbeg[m]; t < g->mesh_tbeg[m + 1]; ++t) {
                 tri_t T;
                 make_tri(g, t, &T);
                 double al[3] = {0, 0, 0};
                 int idx[3] = {0, 1, 2}, inside = 1;
                 double dist = dpc(p, &T, al, 3, idx, &inside);
-                if (dist < best) {
-                    best = dist;
-                    out_tri[i] = t;
-                    out_w[3 * i] = al[0]; out_w[3 * i + 1] = al[1]; out_w[3 * i + 2] = al[2];
+                if (dist < mbest) {
+                    mbest = dist;
+                    mt = t;
+                    mw[0] = al[0]; mw[1] = al[1]; mw[2] = al[2];
                 }
             }
+            if (mbest < best) {
+                best = mbest;
+                out_tri[i] = mt;
+            }
+            out_w[3 * i] = mw[0]; out_w[3 * i + 1] = mw[1]; out_w[3 * i + 2] = mw[2];
         }
     }
     return 0;

@@ -94,3 +94,31 @@ def run_pipeline(head, dipoles, electrodes=None, squids=None, workdir=None, dsm_
         import shutil
         shutil.rmtree(d, ignore_errors=True)
     return out
+
+
+def run_pipeline_files(geom, cond, dip, eeg=None, meg=None, threads=None,
+                       want=("hm", "dsm", "h2em", "h2mm", "ds2mm", "eeg", "meg")):
+    """Same stages as run_pipeline on existing input files (absolute paths)."""
+    from openmeeg_gb300 import io
+    d = tempfile.mkdtemp(prefix="omref_")
+    out = {}
+    stages = [("hm", ["om_assemble", "-HM", geom, cond, "hm.bin"]),
+              ("dsm", ["om_assemble", "-DSM", geom, cond, dip, "dsm.bin"])]
+    if eeg:
+        stages.append(("h2em", ["om_assemble", "-H2EM", geom, cond, eeg, "h2em.bin"]))
+    if meg:
+        stages += [("h2mm", ["om_assemble", "-H2MM", geom, cond, meg, "h2mm.bin"]),
+                   ("ds2mm", ["om_assemble", "-DS2MM", dip, meg, "ds2mm.bin"])]
+    if eeg:
+        stages.append(("eeg", ["om_gain", "-EEGadjoint", geom, cond, dip, "hm.bin", "h2em.bin", "eeg.bin"]))
+    if meg:
+        stages.append(("meg", ["om_gain", "-MEGadjoint", geom, cond, dip, "hm.bin", "h2mm.bin", "ds2mm.bin",
+                               "meg.bin"]))
+    for key, args in stages:
+        _run(d, *args, threads=threads)
+        if key in want:
+            out[key] = io.read_bin(os.path.join(d, f"{key}.bin"))[1]
+    import shutil
+    shutil.rmtree(d, ignore_errors=True)
+    return out
+

@@ -18,6 +18,11 @@ files) for a seeded workload of openmeeg_gb300.workloads:
                      MEG values its test suite compares against
                      (tests/analytic/eeg_head3_analytic.txt, meg_analytic.txt);
                      `--analytic-only` writes just this fixture
+  reference_heads    the reference's sample heads HeadNNb1 (two extra spheres inside the
+                     brain: non-nested) and HeadMN1-3 (several non-conductive domains)
+                     through om_assemble / om_gain with their own dipoles, patches and
+                     squids, with the geometry files' texts; `--heads-only` writes just
+                     this fixture (and head3_analytic)
   eit_sources        EITSourceMat (om_assemble -EITSM) for point electrodes and for
                      electrodes with radii on small_ico1_3l, small_ico1_4l_out and
                      small_ico2_3l_pert; `--eit-only` writes just this fixture (and
@@ -185,9 +190,48 @@ def save_eit():
     print("eit_sources", {k: v.shape for k, v in d.items()})
 
 
+REFERENCE_HEADS = ("HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3")
+
+
+def save_reference_heads():
+    """The reference's non-nested (two extra spheres in the brain) and
+    multiple-non-conductive sample heads, run through its own pipeline with its
+    own dipoles, EEG patches and MEG squids.  The .geom / .cond / mesh texts are
+    stored so that a test can rebuild the files without the reference."""
+    R = os.environ.get("OMG_REFERENCE_DIR", "/root/reference")
+    if not ref_runner.available():
+        ref_runner.build()
+    d = {}
+    for name in REFERENCE_HEADS:
+        base = os.path.join(R, "data", name)
+        geom, cond = os.path.join(base, name + ".geom"), os.path.join(base, name + ".cond")
+        dip, eeg, meg = (os.path.join(base, name + ext) for ext in (".dip", ".patches", ".squids"))
+        out = ref_runner.run_pipeline_files(geom, cond, dip, eeg, meg)
+        meshes, _, _ = io.read_geom_full(geom)
+        d[f"{name}_files"] = np.array([os.path.basename(geom), os.path.basename(cond)] +
+                                      [os.path.basename(p) for _, p in meshes])
+        d[f"{name}_texts"] = np.array([open(geom).read(), open(cond).read()] + [open(p).read() for _, p in meshes])
+        d[f"{name}_dipoles"] = io.read_matrix_txt(dip)
+        d[f"{name}_electrodes"] = io.read_sensors_txt(eeg)[1]
+        d[f"{name}_squids"] = io.read_sensors_txt(meg)[1]
+        if name in ("HeadNNb1", "HeadMN3"):   # head matrices and H2MM of two of the four (fixture size)
+            d[f"{name}_hm_packed"] = io.packed_upper(out["hm"])
+        for k in ("dsm", "h2em", "h2mm", "ds2mm", "eeg", "meg"):
+            if k != "h2mm" or name in ("HeadNNb1", "HeadMN3"):
+                d[f"{name}_{k}"] = out[k]
+        ana = os.path.join(R, "tests", "analytic", f"eeg_head{name[4:]}_analytic.txt")
+        if os.path.exists(ana):   # the analytic EEG values the reference's tests compare against
+            d[f"{name}_eeg_analytic"] = np.loadtxt(ana)
+        print(name, {k: out[k].shape for k in out})
+    np.savez_compressed(os.path.join(OUT, "reference_heads.npz"), **d)
+
+
 def main():
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
+        return
+    save_reference_heads()
+    if "--heads-only" in sys.argv:
         return
     save_eit()
     if "--eit-only" in sys.argv:

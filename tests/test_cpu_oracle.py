@@ -84,6 +84,71 @@ def test_oracle_eit_source_pinned_to_reference(tag, kw):
     assert rel(oracle.eitsourcemat(g, el), G[f"eit_radii_{tag}"]) < 1e-14
 
 
+@pytest.mark.parametrize("name", ["HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3"])
+def test_oracle_reference_heads_pinned_to_reference(name, tmp_path):
+    """The reference's non-nested and multiple-non-conductive sample heads, read
+    from its own files through io.load_head: matrices at rounding level; gains
+    at 1e-10, except on the two heads whose head matrix is singular (see
+    tests/test_gpu_reference_heads.py), where the null direction the sensors do
+    not see leaves the solvers 3e-6 apart -- checked at 1e-4 and against the
+    reference's analytic EEG values with its tolerances."""
+    import warnings
+    from oracle import analytic, oracle
+    from openmeeg_gb300 import io
+    G = golden("reference_heads")
+    for fn, tx in zip(G[f"{name}_files"], G[f"{name}_texts"]):
+        (tmp_path / str(fn)).write_text(str(tx))
+    f = [str(x) for x in G[f"{name}_files"]]
+    head = io.load_head(str(tmp_path / f[0]), str(tmp_path / f[1]))
+    g = oracle.digest(head)
+    HM = oracle.headmat(g)
+    if f"{name}_hm_packed" in G:
+        assert rel(HM, io.unpack_upper(G[f"{name}_hm_packed"], g.N)) < 1e-14
+    D = oracle.dsm(g, G[f"{name}_dipoles"])
+    E = oracle.h2em(g, G[f"{name}_electrodes"])
+    M = oracle.h2mm(g, G[f"{name}_squids"])
+    S = oracle.ds2mm(G[f"{name}_dipoles"], G[f"{name}_squids"])
+    assert rel(D, G[f"{name}_dsm"]) < 1e-14
+    assert rel(E, G[f"{name}_h2em"]) < 1e-14
+    if f"{name}_h2mm" in G:
+        assert rel(M, G[f"{name}_h2mm"]) < 1e-11
+    assert rel(S, G[f"{name}_ds2mm"]) < 1e-14
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")   # LAPACK's ill-conditioning warning on the singular heads
+        ge, gm = oracle.gain_eeg(HM, D, E), oracle.gain_meg(HM, D, M, S)
+    tol = 1e-4 if name in ("HeadMN1", "HeadMN2") else 1e-10
+    assert rel(ge, G[f"{name}_eeg"]) < tol and rel(gm, G[f"{name}_meg"]) < tol
+    if f"{name}_eeg_analytic" in G:
+        ana = G[f"{name}_eeg_analytic"]
+        assert np.all(analytic.rdm(ge, ana) < 0.10) and np.all(analytic.mag(ge, ana) < 0.10)
+
+
+def test_text_formats(tmp_path):
+    """Named .geom v1.1 (Meshes / Interfaces of +-mesh names / Domains of
+    +-interface names), OFF meshes, sensor labels and plain dipole rows."""
+    from openmeeg_gb300 import io
+    from openmeeg_gb300 import synthetic as syn
+    V, T = syn.icosphere(1, inward=False)
+    with open(tmp_path / "a.off", "w") as f:
+        f.write(f"OFF\n{V.shape[0]} {T.shape[0]} 0\n")
+        f.writelines(f"{x} {y} {z}\n" for x, y, z in V * 0.5)
+        f.writelines(f"3 {a} {b} {c}\n" for a, b, c in T)
+    io.write_tri(str(tmp_path / "b.tri"), V, T)
+    (tmp_path / "h.geom").write_text(
+        "# Domain Description 1.1\nMeshes 2\nMesh inner: \"a.off\"\nMesh outer: \"b.tri\"\n"
+        "Interfaces 2\nInterface In: +inner\nInterface Out: outer\n"
+        "Domains 3\nDomain BRAIN: -In\nDomain SKIN: +In -Out\nDomain AIR: Out shared\n")
+    (tmp_path / "h.cond").write_text("BRAIN 1\nSKIN 0.5\nAIR 0\n")
+    head = io.load_head(str(tmp_path / "h.geom"), str(tmp_path / "h.cond"))
+    assert head.names == ["inner", "outer"] and np.allclose(head.vertices[0], V * 0.5)
+    assert head.domains == [("BRAIN", [-1], 1.0), ("SKIN", [1, -2], 0.5), ("AIR", [2], 0.0)]
+    (tmp_path / "s.txt").write_text("E1 0.1 0.2 0.3\nE2 1 2.5 3\n")
+    labels, vals = io.read_sensors_txt(str(tmp_path / "s.txt"))
+    assert labels == ["E1", "E2"] and vals.shape == (2, 3)
+    (tmp_path / "d.txt").write_text("0 0 0.4250  0.7 0 0.7\n")
+    assert io.read_matrix_txt(str(tmp_path / "d.txt")).shape == (1, 6)
+
+
 def test_oracle_numbering_and_pairs():
     """Unknown count and mesh pairs of nested heads (geometry.cpp:256-295, 405-420)."""
     from oracle import oracle
