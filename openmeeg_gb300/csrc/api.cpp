@@ -27,8 +27,8 @@ void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi
 void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
                               const double* srec, double* out, cudaStream_t s, bool screened = false);
 void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int maxb, const int* dnb,
-                          const int* bmesh, const int* binside, const int* orient, int forced, int* dom, int* err,
-                          cudaStream_t s);
+                          const int* bmesh, const int* binside, const int* borient, const int* bgrp, int forced,
+                          int* dom, int* err, cudaStream_t s);
 void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, const int32_t* tmesh,
                 const int64_t* tidx_ref, const int* barrier, const int* orient, const int* dom, int maxb,
                 const int* dnb, const int* bmesh, const int* binside, const double* dsigma, int order, int levels,
@@ -41,6 +41,13 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
                  double mag = kMagFactor);
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
+void launch_fold_hm(int64_t Ng, int64_t nP, const int64_t* gbeg, const int64_t* gcopy, const double* hl, int64_t ldl,
+                    double* hg, int64_t ldg, cudaStream_t s);
+void launch_fold_rows(int64_t Ng, int64_t nP, const int64_t* gbeg, const int64_t* gcopy, int64_t ncol, const double* in,
+                      int64_t ldi, double* out, int64_t ldo, cudaStream_t s);
+void launch_fold_to_reference(int64_t Nref, int64_t nvg, int64_t nP, const int64_t* gbeg, const int64_t* gcopy,
+                              int64_t ncol, const double* in, int64_t ldi, double* out, int64_t rs, int64_t cs,
+                              cudaStream_t s);
 void launch_partial_block(const DevGeom& g, int64_t p0, int64_t npc, const double* pts, const int* pdom,
                           const int64_t* rows, const int32_t* tmesh, const int64_t* tidx_ref, const int* barrier,
                           const int* orient, int maxb, const int* dnb, const int* bmesh, const int* binside,
@@ -216,6 +223,7 @@ static void upload_geometry(omg_geometry g) {
     HostGeometry& h = g->h;
     DevGeom& d = g->d;
     d.nv = h.nv;
+    d.nvg = h.nvg;
     d.nt = h.nt;
     d.nPt = h.nP;
     d.nP = (h.nP + kPad - 1) / kPad * kPad;
@@ -228,7 +236,7 @@ static void upload_geometry(omg_geometry g) {
     for (int m = 0; m < h.nmesh; ++m)
         for (int64_t t = h.tbeg[m]; t < h.tbeg[m + 1]; ++t) {
             tmesh[t] = m;
-            if (!h.barrier[m]) tpos[t] = (int32_t)(h.tidx[t] - h.nv);
+            if (!h.barrier[m]) tpos[t] = (int32_t)(h.tidx[t] - h.nvg);
         }
     d.tpos = upload(g->bufs, tpos, s);
     g->bufs.emplace_back((size_t)h.nt * SREC * 8, s, true);
@@ -245,15 +253,28 @@ static void upload_geometry(omg_geometry g) {
     g->tmesh = upload(g->bufs, tmesh, s);
     g->tidx_ref = upload(g->bufs, h.tidx, s);
     g->barrier = upload(g->bufs, h.barrier, s);
-    g->orient = upload(g->bufs, h.orient, s);
     g->tbeg = upload(g->bufs, h.tbeg, s);
+    if (h.shared) {   // copy -> distinct vertex, and its inverse
+        d.vglob = upload(g->bufs, h.vglob, s);
+        std::vector<int64_t> gb(h.nvg + 1, 0), gc(h.nv);
+        for (int64_t v = 0; v < h.nv; ++v) gb[h.vglob[v] + 1]++;
+        for (int64_t u = 0; u < h.nvg; ++u) gb[u + 1] += gb[u];
+        std::vector<int64_t> fill(gb.begin(), gb.end() - 1);
+        for (int64_t v = 0; v < h.nv; ++v) gc[fill[h.vglob[v]]++] = v;
+        g->gbeg = upload(g->bufs, gb, s);
+        g->gcopy = upload(g->bufs, gc, s);
+    }
+    g->dg = d;
+    g->dg.nv = h.nvg;
+    g->dg.N = d.nP + h.nvg;
     std::vector<double> jump(h.nmesh);
     for (int m = 0; m < h.nmesh; ++m) jump[m] = h.conductivity_jump(m);
     g->jump = upload(g->bufs, jump, s);
     std::vector<int32_t> cand;
     std::vector<int64_t> seg{0};   // one candidate segment per interface, in the reference's visiting order
-    for (int m : h.eeg_meshes) {
-        for (int64_t t = h.tbeg[m]; t < h.tbeg[m + 1]; ++t) cand.push_back((int32_t)t);
+    for (int i : h.eeg_ifaces) {
+        for (const auto& om : h.ifaces[i])
+            for (int64_t t = h.tbeg[om.first]; t < h.tbeg[om.first + 1]; ++t) cand.push_back((int32_t)t);
         seg.push_back((int64_t)cand.size());
     }
     g->n_eeg_seg = (int)seg.size() - 1;
@@ -263,19 +284,25 @@ static void upload_geometry(omg_geometry g) {
     g->ndom = (int)h.domains.size();
     g->maxb = 1;
     for (const auto& dm : h.domains) g->maxb = std::max(g->maxb, (int)dm.bounds.size());
-    std::vector<int> dnb(g->ndom), bm(g->ndom * g->maxb, -1), bi(g->ndom * g->maxb, 0);
+    std::vector<int> dnb(g->ndom), bm(g->ndom * g->maxb, -1), bi(g->ndom * g->maxb, 0), bo(g->ndom * g->maxb, 1),
+        bg(g->ndom * g->maxb + 1, -1);
     std::vector<double> sig(g->ndom);
     for (int k = 0; k < g->ndom; ++k) {
         dnb[k] = (int)h.domains[k].bounds.size();
         sig[k] = h.domains[k].sigma;
         for (int j = 0; j < dnb[k]; ++j) {
-            bm[k * g->maxb + j] = h.domains[k].bounds[j].mesh;
-            bi[k * g->maxb + j] = h.domains[k].bounds[j].inside ? 1 : 0;
+            const Boundary& b = h.domains[k].bounds[j];
+            bm[k * g->maxb + j] = b.mesh;
+            bi[k * g->maxb + j] = b.inside ? 1 : 0;
+            bo[k * g->maxb + j] = b.o;
+            bg[k * g->maxb + j] = b.group;
         }
     }
     g->dnb = upload(g->bufs, dnb, s);
     g->bmesh = upload(g->bufs, bm, s);
     g->binside = upload(g->bufs, bi, s);
+    g->orient = upload(g->bufs, bo, s);
+    g->bgrp = upload(g->bufs, bg, s);
     g->dsigma = upload(g->bufs, sig, s);
     launch_prepare_triangles_order(d, 3, s);
     launch_prepare_vertex_curls(d, s);
@@ -449,6 +476,30 @@ static void assemble(omg_geometry g, const omg_integrator& integ, int precision,
         assemble_headmat_mixed(g, integ, hm, ld);
     else
         assemble_headmat_internal(g, integ, hm, ld);
+}
+
+// The head matrix in the solver's numbering (distinct vertices, lower
+// triangle, ld = dg.N): assembled on the per-mesh vertex copies and, when
+// meshes share vertices, folded (P^T H P).
+static DevBuf assemble_system(omg_geometry g, const omg_integrator& integ, int precision, bool persistent) {
+    cudaStream_t s = g->ctx->stream;
+    const int64_t Nl = g->d.N, Ng = g->dg.N;
+    if (!g->h.shared) {
+        DevBuf hm((size_t)Ng * Ng * 8, s, persistent);
+        assemble(g, integ, precision, hm.as<double>(), Ng);
+        return hm;
+    }
+    DevBuf hl((size_t)Nl * Nl * 8, s);
+    assemble(g, integ, precision, hl.as<double>(), Nl);
+    DevBuf hm((size_t)Ng * Ng * 8, s, persistent);
+    launch_fold_hm(Ng, g->d.nP, g->gbeg, g->gcopy, hl.as<double>(), Nl, hm.as<double>(), Ng, s);
+    return hm;
+}
+
+static void require_distinct_vertices(omg_geometry g, const char* what) {
+    if (g->h.shared)
+        throw Error(OMG_ERR_UNSUPPORTED, std::string(what) + " is not available for geometries whose meshes share "
+                                                            "vertices");
 }
 
 // ---------------------------------------------------------------------------
@@ -627,6 +678,7 @@ constexpr int NB32 = 128;   // FP32 diagonal block
 // direction.  The HeadMat returned to callers is left as the reference's.
 static void deflate_enclosed_barriers(omg_solver sv, double* hm, int64_t ld) {
     const HostGeometry& h = sv->geo->h;
+    if (h.shared) return;   // vertex blocks of meshes are contiguous only without shared vertices
     for (int m = 0; m < h.nmesh; ++m) {
         if (!h.barrier[m] || h.outermost[m]) continue;
         const int64_t nb = h.vbeg[m + 1] - h.vbeg[m];
@@ -810,17 +862,29 @@ void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integ
     cudaStream_t s = ctx->stream;
     check_integrator(integ, true);
     OMG_REQUIRE(domain >= -1 && domain < g->ndom, "domain index out of range");
-    const int64_t rows = perm ? g->d.N : g->h.N;
+    const int64_t rows = perm ? g->dg.N : g->h.N;
     if (ldo == rows)
         OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)rows * nd * 8, s));
     else
         for (int64_t j = 0; j < nd; ++j) OMG_CUDA(cudaMemsetAsync(out + j * ldo, 0, (size_t)rows * 8, s));
     if (nd == 0) return;
+    // meshes sharing vertices: rows on the vertex copies (internal numbering), summed per distinct vertex below
+    DevBuf loc;
+    double* dst = out;
+    int64_t ldd = ldo;
+    int dperm = perm;
+    if (g->h.shared) {
+        loc = DevBuf((size_t)g->d.N * nd * 8, s);
+        OMG_CUDA(cudaMemsetAsync(loc.p, 0, (size_t)g->d.N * nd * 8, s));
+        dst = loc.as<double>();
+        ldd = g->d.N;
+        dperm = 1;
+    }
     DevBuf sa((size_t)nd * g->h.nmesh * 8, s), dom((size_t)nd * sizeof(int), s);
     launch_mesh_solid_angles(dip, 6, nd, g->h.nmesh, g->tbeg, g->d.srec, sa.as<double>(), s,
                              precision == OMG_PREC_MIXED);
     launch_domain_lookup(nd, g->h.nmesh, sa.as<double>(), g->ndom, g->maxb, g->dnb, g->bmesh, g->binside, g->orient,
-                         domain, dom.as<int>(), ctx->d_err, s);
+                         g->bgrp, domain, dom.as<int>(), ctx->d_err, s);
     if (allowed_domains) launch_domain_check(nd, dom.as<int>(), allowed_domains, ctx->d_err, s);
     if (meshes_used) {   // which meshes carry nonzero DSM rows: boundaries of the dipoles' domains
         std::vector<int> hdom(nd);
@@ -840,16 +904,24 @@ void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integ
     for (int64_t d0 = 0; d0 < nd; d0 += per) {
         const int64_t n = std::min(per, nd - d0);
         launch_dsm(g->d, d0, n, dip, g->tmesh, g->tidx_ref, g->barrier, g->orient, dom.as<int>(), g->maxb, g->dnb,
-                   g->bmesh, g->binside, g->dsigma, integ.order, integ.levels, integ.tol, perm, out, ldo,
+                   g->bmesh, g->binside, g->dsigma, integ.order, integ.levels, integ.tol, dperm, dst, ldd,
                    p1.as<double>(), precision == OMG_PREC_MIXED ? 1 : 0, s);
+    }
+    if (g->h.shared) {
+        if (perm)
+            launch_fold_rows(g->dg.N, g->d.nP, g->gbeg, g->gcopy, nd, loc.as<double>(), g->d.N, out, ldo, s);
+        else
+            launch_fold_to_reference(g->h.N, g->h.nvg, g->d.nP, g->gbeg, g->gcopy, nd, loc.as<double>(), g->d.N, out,
+                                     1, ldo, s);
     }
 }
 
 std::vector<std::pair<int64_t, int64_t>> gain_row_ranges(omg_geometry geo, const std::vector<int>& src_meshes) {
+    if (geo->h.shared) return {{0, geo->dg.N}};   // vertex rows of a mesh are not contiguous
     std::vector<std::pair<int64_t, int64_t>> kr;
     for (int m : src_meshes) {
         if (!geo->h.barrier[m])
-            kr.push_back({geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv, geo->h.tidx[geo->h.tbeg[m]] - geo->h.nv +
+            kr.push_back({geo->h.tidx[geo->h.tbeg[m]] - geo->h.nvg, geo->h.tidx[geo->h.tbeg[m]] - geo->h.nvg +
                                                                        (geo->h.tbeg[m + 1] - geo->h.tbeg[m])});
         kr.push_back({geo->d.nP + geo->h.vbeg[m], geo->d.nP + geo->h.vbeg[m + 1]});
     }
@@ -1103,7 +1175,7 @@ int omg_geometry_destroy(omg_geometry geo) {
 int omg_geometry_get_info(omg_geometry geo, omg_geometry_info* info) {
     return guarded([&] {
         OMG_REQUIRE(geo && info, "null argument");
-        info->n_vertices = geo->h.nv;
+        info->n_vertices = geo->h.nvg;
         info->n_triangles = geo->h.nt;
         info->n_unknowns = geo->h.N;
         info->n_triangle_unknowns = geo->h.nP;
@@ -1146,10 +1218,9 @@ int omg_headmat_dev(omg_context ctx, omg_geometry geo, const omg_integrator* int
         set_device(ctx);
         reset_err(ctx);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
-        const int64_t N = geo->d.N;
-        DevBuf tmp((size_t)N * N * 8, ctx->stream);
-        assemble(geo, it, precision, tmp.as<double>(), N);
-        launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, hm, ld, false, ctx->stream);
+        const int64_t N = geo->dg.N;
+        DevBuf tmp = assemble_system(geo, it, precision, false);
+        launch_symmetrize_to_reference(geo->dg, tmp.as<double>(), N, hm, ld, false, ctx->stream);
         check_err(ctx, "HeadMat");
     });
 }
@@ -1160,10 +1231,9 @@ int omg_headmat_packed_dev(omg_context ctx, omg_geometry geo, const omg_integrat
         set_device(ctx);
         reset_err(ctx);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
-        const int64_t N = geo->d.N;
-        DevBuf tmp((size_t)N * N * 8, ctx->stream);
-        assemble_headmat_internal(geo, it, tmp.as<double>(), N);
-        launch_symmetrize_to_reference(geo->d, tmp.as<double>(), N, packed, 0, true, ctx->stream);
+        const int64_t N = geo->dg.N;
+        DevBuf tmp = assemble_system(geo, it, OMG_PREC_FP64, false);
+        launch_symmetrize_to_reference(geo->dg, tmp.as<double>(), N, packed, 0, true, ctx->stream);
         check_err(ctx, "HeadMat");
     });
 }
@@ -1202,10 +1272,20 @@ int omg_head2megmat_dev(omg_context ctx, omg_geometry geo, const double* squids,
         set_device(ctx);
         reset_err(ctx);
         if (n_squids == 0) return;
-        OMG_CUDA(cudaMemsetAsync(h2mm, 0, (size_t)n_squids * geo->h.N * 8, ctx->stream));
         DevBuf F((size_t)n_squids * geo->h.nt * 8, ctx->stream);
-        launch_h2mm(geo->d, squids, n_squids, geo->tmesh, geo->jump, 0, h2mm, n_squids, 1, 0, F.as<double>(),
-                    ctx->stream);
+        if (geo->h.shared) {   // on the vertex copies (internal numbering), then summed per distinct vertex
+            const int64_t Nl = geo->d.N;
+            DevBuf loc((size_t)Nl * n_squids * 8, ctx->stream);
+            OMG_CUDA(cudaMemsetAsync(loc.p, 0, (size_t)Nl * n_squids * 8, ctx->stream));
+            launch_h2mm(geo->d, squids, n_squids, geo->tmesh, geo->jump, 1, loc.as<double>(), 1, Nl, 0,
+                        F.as<double>(), ctx->stream);
+            launch_fold_to_reference(geo->h.N, geo->h.nvg, geo->d.nP, geo->gbeg, geo->gcopy, n_squids, loc.as<double>(),
+                                     Nl, h2mm, n_squids, 1, ctx->stream);
+        } else {
+            OMG_CUDA(cudaMemsetAsync(h2mm, 0, (size_t)n_squids * geo->h.N * 8, ctx->stream));
+            launch_h2mm(geo->d, squids, n_squids, geo->tmesh, geo->jump, 0, h2mm, n_squids, 1, 0, F.as<double>(),
+                        ctx->stream);
+        }
         check_err(ctx, "Head2MEGMat");
     });
 }
@@ -1229,6 +1309,7 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && ssm, "null argument");
         set_device(ctx);
+        require_distinct_vertices(geo, "SurfSourceMat");
         const omg_integrator it = integ ? *integ : default_hm_integrator();
         check_integrator(it, false);
         cudaStream_t s = ctx->stream;
@@ -1241,7 +1322,7 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
         const double* pts = u.d.V + 3 * u.nv0;
         launch_mesh_solid_angles(pts, 3, n_verts, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
         launch_domain_lookup(n_verts, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
-                             geo->binside, geo->orient, -1, dom.as<int>(), ctx->d_err, s);
+                             geo->binside, geo->orient, geo->bgrp, -1, dom.as<int>(), ctx->d_err, s);
         std::vector<int> hdom(n_verts);
         OMG_CUDA(cudaMemcpyAsync(hdom.data(), dom.p, n_verts * sizeof(int), cudaMemcpyDeviceToHost, s));
         OMG_CUDA(cudaStreamSynchronize(s));
@@ -1258,7 +1339,7 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
         const int64_t tsb = u.nt0, tse = u.nt0 + n_tris, vsb = u.nv0, vse = u.nv0 + n_verts;
         for (const auto& b : h.domains[d].bounds) {
             const int m = b.mesh;
-            const double coeffN = (b.inside ? kK : -kK) * h.orient[m];
+            const double coeffN = (b.inside ? kK : -kK) * b.o;
             const int64_t t1b = h.tbeg[m], t1e = h.tbeg[m + 1], n1 = t1e - t1b;
             {
                 DevBuf S((size_t)n1 * n_tris * 8, s);   // unit-coefficient S block (the source is no unknown)
@@ -1314,7 +1395,7 @@ static void keep_conducting_points(KeptPoints& kp, omg_geometry geo, const doubl
     DevBuf sa((size_t)n * h.nmesh * 8, s);
     launch_mesh_solid_angles(pts, 3, n, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s, true);
     launch_domain_lookup(n, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh, geo->binside,
-                         geo->orient, -1, kp.dom.as<int>(), geo->ctx->d_err, s);
+                         geo->orient, geo->bgrp, -1, kp.dom.as<int>(), geo->ctx->d_err, s);
     check_err(geo->ctx, "point domain lookup");
     std::vector<int> hdom(n);
     OMG_CUDA(cudaMemcpyAsync(hdom.data(), kp.dom.p, n * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1335,6 +1416,7 @@ int omg_surf2volmat_dev(omg_context ctx, omg_geometry geo, const double* points,
                         int64_t* n_kept) {
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && n_kept && (n_points == 0 || (points && out)), "null argument");
+        require_distinct_vertices(geo, "Surf2VolMat");
         OMG_REQUIRE(n_points >= 0, "negative point count");
         set_device(ctx);
         cudaStream_t s = ctx->stream;
@@ -1382,7 +1464,7 @@ int omg_dipsource2internalpotmat_dev(omg_context ctx, omg_geometry geo, const do
             launch_mesh_solid_angles(dipoles, 6, n_dipoles, h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s,
                                      true);
         launch_domain_lookup(n_dipoles, h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
-                             geo->binside, geo->orient, domain, ddom.as<int>(), ctx->d_err, s);
+                             geo->binside, geo->orient, geo->bgrp, domain, ddom.as<int>(), ctx->d_err, s);
         launch_dipole_internal_pot(points, kp.dom.as<int>(), kp.rows.as<int64_t>(), n_points, dipoles, ddom.as<int>(),
                                    n_dipoles, geo->dsigma, out, kp.kept, s);
         check_err(ctx, "DipSource2InternalPotMat");
@@ -1481,6 +1563,7 @@ int omg_eitsourcemat_dev(omg_context ctx, omg_geometry geo, const double* positi
                          int64_t n_electrodes, const omg_integrator* integ, double* out) {
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && (n_electrodes == 0 || (positions && out)), "null argument");
+        require_distinct_vertices(geo, "EITSourceMat");
         OMG_REQUIRE(n_electrodes >= 0, "negative electrode count");
         set_device(ctx);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
@@ -1556,6 +1639,7 @@ int omg_geometry_get_layout(omg_geometry geo, int32_t max_meshes, omg_mesh_layou
         OMG_REQUIRE(geo && out, "null argument");
         const HostGeometry& h = geo->h;
         OMG_REQUIRE(max_meshes >= h.nmesh, "output too small");
+        require_distinct_vertices(geo, "the mesh layout");
         for (int m = 0; m < h.nmesh; ++m) {
             omg_mesh_layout& L = out[m];
             L.vbeg = h.vbeg[m];
@@ -1592,7 +1676,7 @@ int omg_dipole_domains_dev(omg_context ctx, omg_geometry geo, const double* dipo
         DevBuf sa((size_t)n_dipoles * geo->h.nmesh * 8, s);
         launch_mesh_solid_angles(dipoles, 6, n_dipoles, geo->h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
         launch_domain_lookup(n_dipoles, geo->h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
-                             geo->binside, geo->orient, -1, domains, ctx->d_err, s);
+                             geo->binside, geo->orient, geo->bgrp, -1, domains, ctx->d_err, s);
         OMG_CUDA(cudaStreamSynchronize(s));
     });
 }
@@ -1601,6 +1685,7 @@ int omg_head2megmat_mesh_dev(omg_context ctx, omg_geometry geo, const double* sq
                              double* out) {
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && (n_squids == 0 || (squids && out)), "null argument");
+        require_distinct_vertices(geo, "the per-mesh Head2MEGMat");
         OMG_REQUIRE(mesh >= 0 && mesh < geo->h.nmesh, "mesh index out of range");
         set_device(ctx);
         reset_err(ctx);
@@ -1620,6 +1705,7 @@ int omg_dipsourcemat_vjp_dev(omg_context ctx, omg_geometry geo, const double* di
                              const omg_integrator* integ, int32_t domain, const double* U, int64_t ldu, double* out) {
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && (n_dipoles == 0 || (dipoles && U && out)), "null argument");
+        require_distinct_vertices(geo, "the DipSourceMat vector-Jacobian product");
         OMG_REQUIRE(ldu >= geo->h.N, "ldu must be >= N");
         OMG_REQUIRE(domain >= -1 && domain < geo->ndom, "domain index out of range");
         set_device(ctx);
@@ -1631,7 +1717,7 @@ int omg_dipsourcemat_vjp_dev(omg_context ctx, omg_geometry geo, const double* di
         DevBuf sa((size_t)n_dipoles * geo->h.nmesh * 8, s), dom((size_t)n_dipoles * sizeof(int), s);
         launch_mesh_solid_angles(dipoles, 6, n_dipoles, geo->h.nmesh, geo->tbeg, geo->d.srec, sa.as<double>(), s);
         launch_domain_lookup(n_dipoles, geo->h.nmesh, sa.as<double>(), geo->ndom, geo->maxb, geo->dnb, geo->bmesh,
-                             geo->binside, geo->orient, domain, dom.as<int>(), ctx->d_err, s);
+                             geo->binside, geo->orient, geo->bgrp, domain, dom.as<int>(), ctx->d_err, s);
         const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (geo->h.nt * 48)));
         DevBuf part((size_t)std::min(per, n_dipoles) * geo->h.nt * 48, s);
         for (int64_t d0 = 0; d0 < n_dipoles; d0 += per) {
@@ -1671,12 +1757,11 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
         sv->ctx = ctx;
         sv->geo = geo;
         sv->precision = precision;
-        sv->N = geo->d.N;
+        sv->N = geo->dg.N;
         sv->nP = geo->d.nP;
         sv->persistent = true;
-        DevBuf hm((size_t)sv->N * sv->N * 8, ctx->stream, true);
         const omg_integrator it = integ ? *integ : default_hm_integrator();
-        assemble(geo, it, precision, hm.as<double>(), sv->N);
+        DevBuf hm = assemble_system(geo, it, precision, true);
         check_err(ctx, "HeadMat");
         solver_factor(sv.get(), std::move(hm));
         ctx->refs++;
@@ -1696,11 +1781,11 @@ int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double*
         sv->ctx = ctx;
         sv->geo = geo;
         sv->precision = precision;
-        sv->N = geo->d.N;
+        sv->N = geo->dg.N;
         sv->nP = geo->d.nP;
         sv->persistent = true;
         DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream, true);
-        launch_from_reference_dense(geo->d, hm, ld, A.as<double>(), sv->N, ctx->stream);
+        launch_from_reference_dense(geo->dg, hm, ld, A.as<double>(), sv->N, ctx->stream);
         solver_factor(sv.get(), std::move(A));
         ctx->refs++;
         geo->refs++;
@@ -1714,7 +1799,7 @@ int omg_solver_solve_dev(omg_solver sv, double* b, int64_t ldb, int64_t nrhs) {
         OMG_REQUIRE(ldb >= sv->geo->h.N && nrhs >= 0, "bad right-hand side shape");
         set_device(sv->ctx);
         cudaStream_t s = sv->ctx->stream;
-        const int64_t N = sv->N, nv = sv->geo->h.nv, nP = sv->nP, nPt = sv->geo->d.nPt;
+        const int64_t N = sv->N, nv = sv->geo->h.nvg, nP = sv->nP, nPt = sv->geo->d.nPt;
         // reference -> internal numbering: triangle rows [nv, nv+nPt) first, zero padding, then vertices [0, nv)
         DevBuf X((size_t)N * nrhs * 8, s);
         double* x = X.as<double>();
@@ -1751,7 +1836,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
                           const omg_integrator& dsm_it, const double* dip, int64_t nd, const double* el, int64_t ne,
                           const double* sq, int64_t nm, double* geeg, double* gmeg, omg_gain_stats* st) {
     cudaStream_t s = ctx->stream;
-    const int64_t N = geo->d.N, k = ne + nm;
+    const int64_t N = geo->dg.N, k = ne + nm;
     cudaEvent_t ev[6];
     for (auto& e : ev) OMG_CUDA(cudaEventCreate(&e));
     OMG_CUDA(cudaEventRecord(ev[0], s));
@@ -1764,8 +1849,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     sv->precision = precision;
     sv->N = N;
     sv->nP = geo->d.nP;
-    DevBuf hm((size_t)N * N * 8, s);
-    assemble(geo, hm_it, precision, hm.as<double>(), N);
+    DevBuf hm = assemble_system(geo, hm_it, precision, false);
     OMG_CUDA(cudaEventRecord(ev[1], s));
     // right-hand sides (internal numbering) and DSM
     DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
@@ -1776,7 +1860,15 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
                     nullptr, s);
     }
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
-    if (nm > 0) launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
+    if (nm > 0 && geo->h.shared) {   // on the vertex copies, then summed per distinct vertex
+        const int64_t Nl = geo->d.N;
+        DevBuf loc((size_t)Nl * nm * 8, s);
+        OMG_CUDA(cudaMemsetAsync(loc.p, 0, (size_t)Nl * nm * 8, s));
+        launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, loc.as<double>(), 1, Nl, 0, F.as<double>(), s);
+        launch_fold_rows(N, geo->d.nP, geo->gbeg, geo->gcopy, nm, loc.as<double>(), Nl, B.as<double>() + ne * N, N, s);
+    } else if (nm > 0) {
+        launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
+    }
     if (precision == OMG_PREC_MIXED) ensure_gg_tables(geo);
     std::vector<int> src_meshes;
     dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, &src_meshes);

@@ -447,6 +447,8 @@ int omg_batch_create(omg_context ctx, int32_t n_models, const omg_batch_model* m
         for (int32_t i = 0; i < n_models; ++i) {
             const omg_batch_model& in = models[i];
             OMG_REQUIRE(in.geometry, "null geometry in batch");
+            if (in.geometry->h.shared)
+                throw Error(OMG_ERR_UNSUPPORTED, "batched forward of geometries whose meshes share vertices");
             OMG_REQUIRE(in.geometry->ctx->device == ctx->device, "batch geometries must live on the context's device");
             OMG_REQUIRE(in.n_dipoles >= 0 && in.n_electrodes >= 0 && in.n_squids >= 0, "negative count");
             OMG_REQUIRE(in.n_dipoles == 0 || in.dipoles, "null dipoles");

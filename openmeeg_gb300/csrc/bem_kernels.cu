@@ -916,10 +916,13 @@ __global__ void mesh_solid_angles_screened_kernel(const double* __restrict__ pts
 
 // Geometry::domain(point) (geometry.cpp:146-154, domain.cpp:12-17): the first
 // domain all of whose boundaries agree with the point's inside/outside state.
+// A boundary is an interface: the solid angles of its meshes are summed with
+// their orientations (Interface::solid_angle, interface.cpp:40-45); the
+// domain's per-mesh entries of one interface share a group index.
 __global__ void domain_lookup_kernel(int64_t n, int nmesh, const double* __restrict__ sa, int ndom, int maxb,
                                      const int* __restrict__ dnb, const int* __restrict__ bmesh,
-                                     const int* __restrict__ binside, const int* __restrict__ orient, int forced,
-                                     int* dom, int* err) {
+                                     const int* __restrict__ binside, const int* __restrict__ borient,
+                                     const int* __restrict__ bgrp, int forced, int* dom, int* err) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (forced >= 0) {
@@ -929,10 +932,14 @@ __global__ void domain_lookup_kernel(int64_t n, int nmesh, const double* __restr
     int found = -1;
     for (int d = 0; d < ndom && found < 0; ++d) {
         bool ok = true;
+        double acc = 0.0;
         for (int k = 0; k < dnb[d]; ++k) {
-            const int m = bmesh[d * maxb + k];
-            const bool c = interface_contains(orient[m] * sa[i * nmesh + m]);
-            if (c != (binside[d * maxb + k] != 0)) ok = false;
+            const int q = d * maxb + k;
+            acc += borient[q] * sa[i * nmesh + bmesh[q]];
+            if (k + 1 == dnb[d] || bgrp[q + 1] != bgrp[q]) {   // end of this interface's meshes
+                if (interface_contains(acc) != (binside[q] != 0)) ok = false;
+                acc = 0.0;
+            }
         }
         if (ok) found = d;
     }
@@ -1165,7 +1172,7 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
     bool on = false;
     for (int k = 0; k < dnb[d]; ++k)
         if (bmesh[d * maxb + k] == m) {
-            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[m];
+            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[d * maxb + k];
             on = true;
         }
     if (!on) return;
@@ -1310,8 +1317,8 @@ __device__ double danielsson_rn(d3 p, const d3 P[3], double al[3]) {
 // overall nearest (first strictly smaller distance) -- as the reference does.
 __global__ void h2em_kernel(const double* __restrict__ pos, int nseg, const int64_t* __restrict__ seg,
                             const int32_t* __restrict__ cand, const double* __restrict__ srec,
-                            const int32_t* __restrict__ T, int64_t nP, int perm, double* dense, int64_t rs,
-                            int64_t cs, int64_t col0, int64_t* scols, double* svals) {
+                            const int32_t* __restrict__ T, const int64_t* __restrict__ vglob, int64_t nP, int perm,
+                            double* dense, int64_t rs, int64_t cs, int64_t col0, int64_t* scols, double* svals) {
     __shared__ double sd[256];
     __shared__ int64_t so[256];
     __shared__ double sa[256][3];
@@ -1359,7 +1366,7 @@ __global__ void h2em_kernel(const double* __restrict__ pos, int nseg, const int6
     }
     if (threadIdx.x == 0 && gtri >= 0) {
         for (int j = 0; j < 3; ++j) {
-            const int64_t v = T[3 * gtri + j];
+            const int64_t v = vglob ? vglob[T[3 * gtri + j]] : T[3 * gtri + j];   // distinct vertex
             if (dense) dense[(perm ? nP + v : v) * rs + (col0 + e) * cs] = w[j];
             if (scols) scols[3 * e + j] = v;
             if (svals) svals[3 * e + j] = w[j];
@@ -1427,12 +1434,12 @@ void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int
 }
 
 void launch_domain_lookup(int64_t n, int nmesh, const double* sa, int ndom, int maxb, const int* dnb,
-                          const int* bmesh, const int* binside, const int* orient, int forced, int* dom, int* err,
-                          cudaStream_t s) {
+                          const int* bmesh, const int* binside, const int* borient, const int* bgrp, int forced,
+                          int* dom, int* err, cudaStream_t s) {
     ProfScope prof_("domain_lookup", s);
     if (n == 0) return;
-    domain_lookup_kernel<<<nblocks(n, 128), 128, 0, s>>>(n, nmesh, sa, ndom, maxb, dnb, bmesh, binside, orient,
-                                                         forced, dom, err);
+    domain_lookup_kernel<<<nblocks(n, 128), 128, 0, s>>>(n, nmesh, sa, ndom, maxb, dnb, bmesh, binside, borient,
+                                                         bgrp, forced, dom, err);
     check_launch("domain lookup");
 }
 
@@ -1464,7 +1471,7 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
     if (ndc == 0) return;
     dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
     dsm_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, tmesh, tidx_ref, barrier, orient, dom, maxb, dnb,
-                                    bmesh, binside, dsigma, order, levels, tol, g.nv, g.nP, perm, out, ldo, p1tmp, mixed);
+                                    bmesh, binside, dsigma, order, levels, tol, g.nvg, g.nP, perm, out, ldo, p1tmp, mixed);
     check_launch("DSM");
     dim3 grid2(nblocks(g.nv, 128), (unsigned)ndc);
     dsm_gather_kernel<<<grid2, 128, 0, s>>>(dip0, ndc, g.nv, g.nt, p1tmp, g.v2t_beg, g.v2t_tri, g.v2t_loc, g.nP,
@@ -1477,8 +1484,8 @@ void launch_h2em(const DevGeom& g, const double* pos, int64_t ne, int nseg, cons
                  cudaStream_t s) {
     if (ne == 0) return;
     ProfScope prof_("h2em", s);
-    h2em_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, nseg, seg, cand, g.srec, g.T, g.nP, perm, dense, rs, cs, col0, scols,
-                                             svals);
+    h2em_kernel<<<(unsigned)ne, 256, 0, s>>>(pos, nseg, seg, cand, g.srec, g.T, g.vglob, g.nP, perm, dense, rs, cs,
+                                             col0, scols, svals);
     check_launch("H2EM");
 }
 
@@ -1647,7 +1654,7 @@ __global__ void dsm_vjp_kernel(int64_t dip0, int64_t ndc, const double* __restri
     bool on = false;
     for (int k = 0; k < dnb[d]; ++k)
         if (bmesh[d * maxb + k] == m) {
-            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[m];
+            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[d * maxb + k];
             on = true;
         }
     if (!on) return;
@@ -1741,7 +1748,7 @@ __global__ void partial_block_kernel(int64_t p0, int64_t npc, const double* __re
     bool on = false;
     for (int k = 0; k < dnb[d]; ++k)
         if (bmesh[d * maxb + k] == m) {
-            c = (binside[d * maxb + k] ? kK : -kK) * orient[m];
+            c = (binside[d * maxb + k] ? kK : -kK) * orient[d * maxb + k];
             on = true;
         }
     if (!on) return;
@@ -1983,6 +1990,112 @@ void launch_eit_combine(int64_t Nref, int64_t ne, const int64_t* ebeg, const int
     dim3 grid(nblocks(Nref, 256), (unsigned)std::min<int64_t>(ne, 32768));
     eit_combine_kernel<<<grid, 256, 0, s>>>(Nref, ne, ebeg, eid, ecoef, k0, nk, R, out);
     check_launch("EIT combine");
+}
+
+// ---------------------------------------------------------------------------
+// Shared vertices.  Assembly runs on per-mesh vertex copies (every mesh keeps
+// its own vertices, so each block kernel sees a contiguous range); the
+// reference's unknowns are the distinct vertices.  With P the copy -> distinct
+// vertex map, the reference's head matrix is P^T H P (its N block adds the
+// cross-mesh term of a vertex shared by two meshes once with factor 1/2, which
+// is the two symmetric copy entries with factor 1/4), its source rows are P^T
+// times the copies' rows.  gbeg/gcopy: for distinct vertex u, its copies.
+// Internal positions: triangles (and padding) i < nP are their own copies;
+// vertex u sits at nP + u (distinct) or nP + v (copy).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void copies_of(int64_t i, int64_t nP, const int64_t* gbeg, const int64_t* gcopy,
+                                          int64_t& k0, int64_t& k1) {
+    if (i < nP) {
+        k0 = -1 - i;   // encodes the single copy i
+        k1 = k0 + 1;
+    } else {
+        k0 = gbeg[i - nP];
+        k1 = gbeg[i - nP + 1];
+    }
+}
+__device__ __forceinline__ int64_t copy_at(int64_t k, int64_t nP, const int64_t* gcopy) {
+    return k < 0 ? -1 - k : nP + gcopy[k];
+}
+
+// Hg (lower triangle, Ng x Ng) = P^T Hl P from the lower triangle of Hl (symmetric).
+__global__ void fold_hm_kernel(int64_t Ng, int64_t nP, const int64_t* __restrict__ gbeg,
+                               const int64_t* __restrict__ gcopy, const double* __restrict__ hl, int64_t ldl,
+                               double* hg, int64_t ldg) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= Ng) return;
+    int64_t a0, a1;
+    copies_of(i, nP, gbeg, gcopy, a0, a1);
+    for (int64_t j = blockIdx.y; j <= i; j += gridDim.y) {
+        int64_t b0, b1;
+        copies_of(j, nP, gbeg, gcopy, b0, b1);
+        double acc = 0.0;
+        for (int64_t ka = a0; ka < a1; ++ka) {
+            const int64_t a = copy_at(ka, nP, gcopy);
+            for (int64_t kb = b0; kb < b1; ++kb) acc += hl[lower_at(a, copy_at(kb, nP, gcopy), ldl)];
+        }
+        hg[i + j * ldg] = acc;
+    }
+}
+
+// out (Ng x ncol) = P^T in (Nl x ncol): rows of the copies summed.
+__global__ void fold_rows_kernel(int64_t Ng, int64_t nP, const int64_t* __restrict__ gbeg,
+                                 const int64_t* __restrict__ gcopy, int64_t ncol, const double* __restrict__ in,
+                                 int64_t ldi, double* out, int64_t ldo) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= Ng) return;
+    int64_t a0, a1;
+    copies_of(i, nP, gbeg, gcopy, a0, a1);
+    for (int64_t c = blockIdx.y; c < ncol; c += gridDim.y) {
+        double acc = 0.0;
+        for (int64_t k = a0; k < a1; ++k) acc += in[copy_at(k, nP, gcopy) + c * ldi];
+        out[i + c * ldo] = acc;
+    }
+}
+
+void launch_fold_hm(int64_t Ng, int64_t nP, const int64_t* gbeg, const int64_t* gcopy, const double* hl, int64_t ldl,
+                    double* hg, int64_t ldg, cudaStream_t s) {
+    ProfScope prof_("fold", s);
+    dim3 grid(nblocks(Ng, 256), (unsigned)std::min<int64_t>(Ng, 32768));
+    fold_hm_kernel<<<grid, 256, 0, s>>>(Ng, nP, gbeg, gcopy, hl, ldl, hg, ldg);
+    check_launch("fold head matrix");
+}
+
+void launch_fold_rows(int64_t Ng, int64_t nP, const int64_t* gbeg, const int64_t* gcopy, int64_t ncol, const double* in,
+                      int64_t ldi, double* out, int64_t ldo, cudaStream_t s) {
+    if (ncol <= 0) return;
+    ProfScope prof_("fold", s);
+    dim3 grid(nblocks(Ng, 256), (unsigned)std::min<int64_t>(ncol, 32768));
+    fold_rows_kernel<<<grid, 256, 0, s>>>(Ng, nP, gbeg, gcopy, ncol, in, ldi, out, ldo);
+    check_launch("fold rows");
+}
+
+// out[r * rs + c * cs] (reference numbering r < Nref: distinct vertices, then
+// triangle unknowns) = sum over the copies of unknown r of in[copy + c * ldi]
+// (internal copy numbering).
+__global__ void fold_to_reference_kernel(int64_t Nref, int64_t nvg, int64_t nP, const int64_t* __restrict__ gbeg,
+                                         const int64_t* __restrict__ gcopy, int64_t ncol,
+                                         const double* __restrict__ in, int64_t ldi, double* out, int64_t rs,
+                                         int64_t cs) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= Nref) return;
+    const int64_t i = r < nvg ? nP + r : r - nvg;
+    int64_t a0, a1;
+    copies_of(i, nP, gbeg, gcopy, a0, a1);
+    for (int64_t c = blockIdx.y; c < ncol; c += gridDim.y) {
+        double acc = 0.0;
+        for (int64_t k = a0; k < a1; ++k) acc += in[copy_at(k, nP, gcopy) + c * ldi];
+        out[r * rs + c * cs] = acc;
+    }
+}
+
+void launch_fold_to_reference(int64_t Nref, int64_t nvg, int64_t nP, const int64_t* gbeg, const int64_t* gcopy,
+                              int64_t ncol, const double* in, int64_t ldi, double* out, int64_t rs, int64_t cs,
+                              cudaStream_t s) {
+    if (ncol <= 0) return;
+    ProfScope prof_("fold", s);
+    dim3 grid(nblocks(Nref, 256), (unsigned)std::min<int64_t>(ncol, 32768));
+    fold_to_reference_kernel<<<grid, 256, 0, s>>>(Nref, nvg, nP, gbeg, gcopy, ncol, in, ldi, out, rs, cs);
+    check_launch("fold to reference");
 }
 
 }  // namespace omg

@@ -57,9 +57,9 @@ double mesh_solid_angle(const HostGeometry& g, int m, const double p[3]) {
 
 }  // namespace
 
-int HostGeometry::mesh_orientation(int d, int m) const {
+int HostGeometry::mesh_orientation(int d, int m) const {   // domain.h:43-45, 95-101
     for (const auto& b : domains[d].bounds)
-        if (b.mesh == m) return b.inside ? orient[m] : -orient[m];
+        if (b.mesh == m) return b.inside ? b.o : -b.o;
     return 0;
 }
 
@@ -106,25 +106,52 @@ void HostGeometry::recompute_coefficients() {
 void HostGeometry::finalize() {
     nv = (int64_t)V.size() / 3;
     nt = (int64_t)T.size() / 3;
-    // Interface orientation (interface.cpp:55-95): bounding-box centre solid angle.
-    orient.assign(nmesh, 1);
-    for (int m = 0; m < nmesh; ++m) {
+    // distinct vertices: copies with equal coordinates are one unknown (Geometry::add_vertex,
+    // geometry.h:100-108), numbered in order of first appearance
+    {
+        std::map<std::array<double, 3>, int64_t> seen;
+        vglob.assign(nv, 0);
+        for (int64_t v = 0; v < nv; ++v) {
+            auto it = seen.emplace(std::array<double, 3>{V[3 * v], V[3 * v + 1], V[3 * v + 2]}, (int64_t)seen.size());
+            vglob[v] = it.first->second;
+        }
+        nvg = (int64_t)seen.size();
+        shared = nvg < nv;
+    }
+    // Interface orientation (interface.cpp:55-95): the solid angle at the bounding-box centre of the
+    // interface, summed over its oriented meshes, must be -4 pi or 0; +4 pi flips the interface.
+    for (size_t i = 0; i < ifaces.size(); ++i) {
         double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-        for (int64_t v = vbeg[m]; v < vbeg[m + 1]; ++v)
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = std::min(lo[k], V[3 * v + k]);
-                hi[k] = std::max(hi[k], V[3 * v + k]);
-            }
+        for (const auto& om : ifaces[i])
+            for (int64_t v = vbeg[om.first]; v < vbeg[om.first + 1]; ++v)
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = std::min(lo[k], V[3 * v + k]);
+                    hi[k] = std::max(hi[k], V[3 * v + k]);
+                }
         double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
-        double s = mesh_solid_angle(*this, m, c);
+        double s = 0.0;
+        for (const auto& om : ifaces[i]) s += om.second * mesh_solid_angle(*this, om.first, c);
         if (almost_equal(s, 4 * M_PI)) {
-            orient[m] = -1;
+            for (auto& om : ifaces[i]) om.second = -om.second;
             s = -s;
         }
         if (!(almost_equal(s, 0.0) || almost_equal(s, -4 * M_PI)))
-            throw Error(OMG_ERR_INVALID, "interface " + std::to_string(m + 1) +
+            throw Error(OMG_ERR_INVALID, "interface " + std::to_string(i + 1) +
                                              " is not closed or its bounding-box centre lies outside it");
     }
+    // domain boundaries, mesh by mesh
+    orient.assign(nmesh, 0);
+    for (auto& d : domains) {
+        d.bounds.clear();
+        for (size_t k = 0; k < d.ifb.size(); ++k)
+            for (const auto& om : ifaces[d.ifb[k].iface])
+                d.bounds.push_back({om.first, d.ifb[k].inside, om.second, (int)k});
+    }
+    for (const auto& itf : ifaces)
+        for (const auto& om : itf)
+            if (orient[om.first] == 0) orient[om.first] = om.second;
+    for (int m = 0; m < nmesh; ++m)
+        if (orient[m] == 0) orient[m] = 1;
     // mark_current_barriers (geometry.cpp:424-536)
     barrier.assign(nmesh, 0);
     outermost.assign(nmesh, 0);
@@ -190,17 +217,17 @@ void HostGeometry::finalize() {
             if (b.inside) outer = false;
         if (outer) continue;
         int n_in = 0;
-        for (const auto& b : d.bounds)
+        for (const auto& b : d.ifb)
             if (b.inside) ++n_in;
         if (n_in >= 2) nested = false;
     }
     // numbering (geometry.cpp:256-295)
     tidx.assign(nt, -1);
-    int64_t idx = nv;
+    int64_t idx = nvg;
     for (int m = 0; m < nmesh; ++m)
         if (!barrier[m])
             for (int64_t t = tbeg[m]; t < tbeg[m + 1]; ++t) tidx[t] = idx++;
-    nP = idx - nv;
+    nP = idx - nvg;
     int64_t nbar = 0;
     for (int m = 0; m < nmesh; ++m)
         if (barrier[m]) {
@@ -216,10 +243,10 @@ void HostGeometry::finalize() {
             if (outermost[m]) om.push_back(m);
         part_outermost.push_back(om);
     }
-    eeg_meshes.clear();
+    eeg_ifaces.clear();   // dist_point_geom (danielsson.cpp:107-128): boundaries of zero-conductivity domains
     for (const auto& d : domains)
         if (d.sigma == 0.0)
-            for (const auto& b : d.bounds) eeg_meshes.push_back(b.mesh);
+            for (const auto& b : d.ifb) eeg_ifaces.push_back(b.iface);
     // vertex -> triangle adjacency
     v2t_beg.assign(nv + 1, 0);
     for (int64_t t = 0; t < nt; ++t)
@@ -237,12 +264,28 @@ void HostGeometry::finalize() {
         }
 }
 
+static HostGeometry build_geometry_impl(int nmesh, const int64_t* nverts, const double* verts, const int64_t* ntris,
+                                       const int64_t* tris, const std::vector<std::vector<std::pair<int, int>>>& ifaces,
+                                       int ndom, const int32_t* nb, const int32_t* bounds, const double* sigma,
+                                       const std::vector<std::string>& dom_names);
+
+// Meshes given as interfaces (one mesh each, normal orientation).
 HostGeometry build_geometry(int nmesh, const int64_t* nverts, const double* verts, const int64_t* ntris,
                             const int64_t* tris, int ndom, const int32_t* nb, const int32_t* bounds,
                             const double* sigma, const std::vector<std::string>& dom_names) {
+    std::vector<std::vector<std::pair<int, int>>> ifaces;
+    for (int m = 0; m < nmesh; ++m) ifaces.push_back({{m, 1}});
+    return build_geometry_impl(nmesh, nverts, verts, ntris, tris, ifaces, ndom, nb, bounds, sigma, dom_names);
+}
+
+static HostGeometry build_geometry_impl(int nmesh, const int64_t* nverts, const double* verts, const int64_t* ntris,
+                                       const int64_t* tris, const std::vector<std::vector<std::pair<int, int>>>& ifaces,
+                                       int ndom, const int32_t* nb, const int32_t* bounds, const double* sigma,
+                                       const std::vector<std::string>& dom_names) {
     OMG_REQUIRE(nmesh > 0 && ndom > 0, "geometry needs at least one mesh and one domain");
     HostGeometry g;
     g.nmesh = nmesh;
+    g.ifaces = ifaces;
     g.vbeg.assign(nmesh + 1, 0);
     g.tbeg.assign(nmesh + 1, 0);
     for (int m = 0; m < nmesh; ++m) {
@@ -279,13 +322,31 @@ HostGeometry build_geometry(int nmesh, const int64_t* nverts, const double* vert
         dom.sigma = sigma[d];
         for (int j = 0; j < nb[d]; ++j, ++k) {
             int b = bounds[k];
-            OMG_REQUIRE(b != 0 && std::abs(b) <= nmesh, "domain boundary refers to an unknown interface");
-            dom.bounds.push_back({std::abs(b) - 1, b < 0});   // GeomFile.h:289-291
+            OMG_REQUIRE(b != 0 && std::abs(b) <= (int)g.ifaces.size(), "domain boundary refers to an unknown interface");
+            dom.ifb.push_back({std::abs(b) - 1, b < 0});   // GeomFile.h:289-291
         }
         g.domains.push_back(dom);
     }
     g.finalize();
     return g;
+}
+
+HostGeometry build_geometry_interfaces(int nmesh, const int64_t* nverts, const double* verts, const int64_t* ntris,
+                                       const int64_t* tris, int nif, const int32_t* if_nm, const int32_t* if_meshes,
+                                       int ndom, const int32_t* nb, const int32_t* bounds, const double* sigma,
+                                       const std::vector<std::string>& dom_names) {
+    OMG_REQUIRE(nif > 0, "geometry needs at least one interface");
+    std::vector<std::vector<std::pair<int, int>>> ifaces(nif);
+    int k = 0;
+    for (int i = 0; i < nif; ++i) {
+        OMG_REQUIRE(if_nm[i] > 0, "empty interface");
+        for (int j = 0; j < if_nm[i]; ++j, ++k) {
+            const int m = if_meshes[k];
+            OMG_REQUIRE(m != 0 && std::abs(m) <= nmesh, "interface refers to an unknown mesh");
+            ifaces[i].push_back({std::abs(m) - 1, m > 0 ? 1 : -1});
+        }
+    }
+    return build_geometry_impl(nmesh, nverts, verts, ntris, tris, ifaces, ndom, nb, bounds, sigma, dom_names);
 }
 
 // ---- file loaders -----------------------------------------------------------
@@ -324,8 +385,8 @@ void read_tri(const std::string& path, std::vector<double>& V, std::vector<int64
 // lists of +/-mesh names, and "Domains" as lists of +/-interface names (a '-'
 // means inside, '+' or no sign outside; "shared" ends the list).  Entries
 // without a "Name:" get the names "1", "2", ... in order.  Meshes are .tri or
-// .off files.  Interfaces must consist of one mesh each here, and meshes may
-// not share vertices.
+// .off files.  Vertices with equal coordinates in several meshes are one
+// unknown (shared vertices).
 namespace {
 
 struct GeomEntry {
@@ -488,16 +549,14 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
     auto find = [](const std::vector<std::string>& v, const std::string& x) {
         return (int)(std::find(v.begin(), v.end(), x) - v.begin());
     };
-    // interface -> its single mesh
-    std::vector<int> iface_mesh(iface_names.size());
+    std::vector<int32_t> if_nm, if_meshes;
     for (size_t k = 0; k < iface_names.size(); ++k) {
-        if (iface_meshes[k].size() != 1)
-            throw Error(OMG_ERR_UNSUPPORTED, "interface " + iface_names[k] +
-                                                 " is made of several meshes (non-nested shared-vertex geometries "
-                                                 "are not supported)");
-        const int m = find(mesh_names, iface_meshes[k][0].first);
-        if (m == (int)mesh_names.size()) throw Error(OMG_ERR_INVALID, "unknown mesh " + iface_meshes[k][0].first);
-        iface_mesh[k] = m;
+        if_nm.push_back((int32_t)iface_meshes[k].size());
+        for (const auto& om : iface_meshes[k]) {
+            const int m = find(mesh_names, om.first);
+            if (m == (int)mesh_names.size()) throw Error(OMG_ERR_INVALID, "unknown mesh " + om.first);
+            if_meshes.push_back(om.second ? m + 1 : -(m + 1));
+        }
     }
     std::vector<int32_t> nb, bounds;
     for (size_t d = 0; d < dnames.size(); ++d) {
@@ -505,7 +564,7 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
             const int k = find(iface_names, b.first);
             if (k == (int)iface_names.size())
                 throw Error(OMG_ERR_INVALID, "domain " + dnames[d] + " refers to an unknown interface " + b.first);
-            bounds.push_back(b.second ? -(iface_mesh[k] + 1) : (iface_mesh[k] + 1));
+            bounds.push_back(b.second ? -(k + 1) : (k + 1));
         }
         nb.push_back((int32_t)dbounds[d].size());
     }
@@ -535,18 +594,9 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
         nv.push_back((int64_t)v.size() / 3);
         nt.push_back((int64_t)t.size() / 3);
     }
-    // the reference merges vertices with equal coordinates across meshes (Geometry::add_vertex,
-    // geometry.h:100-108); such shared vertices are outside this build's scope
-    {
-        std::vector<std::array<double, 3>> pts(V.size() / 3);
-        for (size_t i = 0; i < pts.size(); ++i) pts[i] = {V[3 * i], V[3 * i + 1], V[3 * i + 2]};
-        std::sort(pts.begin(), pts.end());
-        if (std::adjacent_find(pts.begin(), pts.end()) != pts.end())
-            throw Error(OMG_ERR_UNSUPPORTED, "meshes share vertices (non-nested shared-vertex geometries are not "
-                                             "supported)");
-    }
-    return build_geometry((int)mesh_files.size(), nv.data(), V.data(), nt.data(), T.data(), (int)dnames.size(),
-                          nb.data(), bounds.data(), sigma.data(), dnames);
+    return build_geometry_interfaces((int)mesh_files.size(), nv.data(), V.data(), nt.data(), T.data(),
+                                     (int)iface_names.size(), if_nm.data(), if_meshes.data(), (int)dnames.size(),
+                                     nb.data(), bounds.data(), sigma.data(), dnames);
 }
 
 }  // namespace omg

@@ -111,13 +111,17 @@ struct omg_geometry_s {
     omg_context ctx = nullptr;
     int refs = 1;              // the caller's handle + one per live solver
     HostGeometry h;
-    DevGeom d;
+    DevGeom d;                  // assembly: every mesh with its own vertex copies
+    DevGeom dg;                 // the reference's unknowns (distinct vertices); == d unless meshes share vertices
+    int64_t* gbeg = nullptr;    // distinct vertex u -> its copies gcopy[gbeg[u] .. gbeg[u + 1])
+    int64_t* gcopy = nullptr;
+    int* bgrp = nullptr;        // per domain boundary entry: index of its interface within the domain
     std::vector<DevBuf> bufs;
     // mesh-level device tables
     int32_t* tmesh = nullptr;
     int64_t* tidx_ref = nullptr;
     int* barrier = nullptr;
-    int* orient = nullptr;
+    int* orient = nullptr;      // per domain boundary entry (ndom x maxb): the mesh's orientation in its interface
     int64_t* tbeg = nullptr;
     double* jump = nullptr;
     int32_t* eeg_cand = nullptr;

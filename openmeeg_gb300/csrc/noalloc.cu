@@ -68,6 +68,8 @@ extern "C" int omg_head2megmat_noalloc_dev(omg_context ctx, omg_geometry geo, co
         OMG_REQUIRE(ctx && geo, "null argument");
         OMG_REQUIRE(n_squids >= 0, "negative sensor count");
         OMG_REQUIRE(n_squids == 0 || (squids && h2mm), "null sensors or output");
+        if (geo->h.shared)   // the per-distinct-vertex sum needs a buffer of the vertex copies
+            throw Error(OMG_ERR_UNSUPPORTED, "geometries whose meshes share vertices need omg_head2megmat_dev");
         OMG_CUDA(cudaSetDevice(ctx->device));
         double* scratch = scratch_address(ctx->device);
         if (n_squids == 0) return OMG_OK;

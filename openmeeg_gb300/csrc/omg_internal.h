@@ -43,14 +43,26 @@ constexpr int MAXQ = 16;
 // Host geometry: restates OpenMEEG's Geometry bookkeeping for meshes given as
 // interfaces (OpenMEEG/src/geometry.cpp, interface.cpp, domain.h).
 // --------------------------------------------------------------------------
+// A domain boundary is an interface (a list of oriented meshes) and a side;
+// `bounds` lists it mesh by mesh: the mesh, the side, the mesh's orientation
+// in that interface (after the interface's global reorientation) and the
+// index of the interface boundary within the domain (consecutive entries of
+// one interface share it).
 struct Boundary {
     int mesh;
+    bool inside;
+    int o = 1;
+    int group = 0;
+};
+struct InterfaceBound {
+    int iface;
     bool inside;
 };
 struct Domain {
     std::string name;
     std::vector<Boundary> bounds;
     double sigma;
+    std::vector<InterfaceBound> ifb;
 };
 struct MeshPair {
     int m1, m2, orientation;
@@ -59,7 +71,11 @@ struct MeshPair {
 
 struct HostGeometry {
     int nmesh = 0;
-    int64_t nv = 0, nt = 0;
+    int64_t nv = 0, nt = 0;         // nv: vertices of all meshes, each mesh with its own copies
+    int64_t nvg = 0;                // distinct vertices (the reference's unknowns); == nv when no mesh shares one
+    std::vector<int64_t> vglob;     // mesh vertex copy -> distinct vertex (equal coordinates, geometry.h:100-108)
+    bool shared = false;            // some meshes share vertices
+    std::vector<std::vector<std::pair<int, int>>> ifaces;   // interfaces: (mesh, orientation +-1)
     std::vector<double> V;          // nv x 3
     std::vector<int32_t> T;         // nt x 3 global vertex ids
     std::vector<int64_t> vbeg, tbeg;
@@ -68,8 +84,8 @@ struct HostGeometry {
     std::vector<Domain> domains;
     std::vector<MeshPair> pairs;
     std::vector<std::vector<int>> part_outermost;   // outermost meshes of each independent part
-    std::vector<int> eeg_meshes;                    // meshes of interfaces bounding sigma==0 domains
-    // numbering (reference order): vertex v -> v; triangle t -> tidx[t] (>= N for barrier meshes)
+    std::vector<int> eeg_ifaces;                    // interfaces bounding sigma==0 domains, in visiting order
+    // numbering (reference order): vertex copy v -> vglob[v]; triangle t -> tidx[t] (>= N for barrier meshes)
     std::vector<int64_t> tidx;
     int64_t N = 0, nP = 0;          // unknowns, triangle unknowns
     bool nested = true;
@@ -87,6 +103,13 @@ struct HostGeometry {
 HostGeometry build_geometry(int nmesh, const int64_t* nverts, const double* verts, const int64_t* ntris,
                             const int64_t* tris, int ndom, const int32_t* nb, const int32_t* bounds,
                             const double* sigma, const std::vector<std::string>& dom_names);
+// Interfaces of several oriented meshes: interface i lists if_nm[i] signed
+// 1-based mesh ids (+: normal orientation, -: opposite); domain boundaries are
+// signed 1-based interface ids (-: inside).
+HostGeometry build_geometry_interfaces(int nmesh, const int64_t* nverts, const double* verts, const int64_t* ntris,
+                                       const int64_t* tris, int nif, const int32_t* if_nm, const int32_t* if_meshes,
+                                       int ndom, const int32_t* nb, const int32_t* bounds, const double* sigma,
+                                       const std::vector<std::string>& dom_names);
 HostGeometry load_geometry_files(const std::string& geom, const std::string& cond);
 
 // --------------------------------------------------------------------------
@@ -101,10 +124,11 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
 constexpr int64_t kPad = 128;
 struct DevGeom {
     int64_t nv = 0, nt = 0;
+    int64_t nvg = 0;    // distinct vertices (reference numbering); == nv unless meshes share vertices
     int64_t N = 0;      // internal size nP + nv
     int64_t nP = 0;     // padded offset of the vertex unknowns
     int64_t nPt = 0;    // triangle unknowns
-    int64_t Nref = 0;   // reference size nPt + nv
+    int64_t Nref = 0;   // reference size nPt + nvg
     int nmesh = 0;
     double* V = nullptr;          // nv x 3
     int32_t* T = nullptr;         // nt x 3
@@ -116,6 +140,7 @@ struct DevGeom {
     int32_t* v2t_tri = nullptr;
     int8_t* v2t_loc = nullptr;
     double* v2t_q = nullptr;      // per vertex-triangle slot: curl of the P1 basis over the area, 3 doubles
+    int64_t* vglob = nullptr;     // copy -> distinct vertex; null when no mesh shares a vertex
 };
 
 // Device kernel launchers (assembly.cu / sources.cu / dense.cu).

@@ -19,7 +19,9 @@ files) for a seeded workload of openmeeg_gb300.workloads:
                      (tests/analytic/eeg_head3_analytic.txt, meg_analytic.txt);
                      `--analytic-only` writes just this fixture
   reference_heads    the reference's sample heads HeadNNb1 (two extra spheres inside the
-                     brain: non-nested) and HeadMN1-3 (several non-conductive domains)
+                     brain: non-nested), HeadNNa1 / HeadNNc1 (the brain cut into two
+                     hemispheres whose interfaces share the cut mesh and its vertices) and
+                     HeadMN1-3 (several non-conductive domains)
                      through om_assemble / om_gain with their own dipoles, patches and
                      squids, with the geometry files' texts; `--heads-only` writes just
                      this fixture (and head3_analytic)
@@ -190,7 +192,7 @@ def save_eit():
     print("eit_sources", {k: v.shape for k, v in d.items()})
 
 
-REFERENCE_HEADS = ("HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3")
+REFERENCE_HEADS = ("HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3", "HeadNNa1", "HeadNNc1")
 
 
 def save_reference_heads():
@@ -214,10 +216,10 @@ def save_reference_heads():
         d[f"{name}_dipoles"] = io.read_matrix_txt(dip)
         d[f"{name}_electrodes"] = io.read_sensors_txt(eeg)[1]
         d[f"{name}_squids"] = io.read_sensors_txt(meg)[1]
-        if name in ("HeadNNb1", "HeadMN3"):   # head matrices and H2MM of two of the four (fixture size)
+        if name in ("HeadNNb1", "HeadMN3", "HeadNNa1"):   # head matrices and H2MM of three (fixture size)
             d[f"{name}_hm_packed"] = io.packed_upper(out["hm"])
         for k in ("dsm", "h2em", "h2mm", "ds2mm", "eeg", "meg"):
-            if k != "h2mm" or name in ("HeadNNb1", "HeadMN3"):
+            if k != "h2mm" or name in ("HeadNNb1", "HeadMN3", "HeadNNa1"):
                 d[f"{name}_{k}"] = out[k]
         ana = os.path.join(R, "tests", "analytic", f"eeg_head{name[4:]}_analytic.txt")
         if os.path.exists(ana):   # the analytic EEG values the reference's tests compare against

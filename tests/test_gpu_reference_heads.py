@@ -1,7 +1,10 @@
 """The reference's own sample heads beyond nested spheres, loaded through the
 library's .geom parser from the reference's files (rebuilt from the fixture
 texts): HeadNNb1 (two spheres inside the brain -- a domain outside two
-interfaces) and HeadMN1-3 (several non-conductive domains: a non-conductive
+interfaces), HeadNNa1 / HeadNNc1 (the brain cut into two hemispheres: each
+hemisphere's interface is its half-sphere mesh plus the cut mesh, oriented
+oppositely in the two, so meshes share the cut's vertices) and HeadMN1-3
+(several non-conductive domains: a non-conductive
 brain or two non-conductive hemispheres inside the skull, so inner meshes are
 current barriers).  Each matrix of the forward path is compared with the
 reference's om_assemble output and each gain with om_gain
@@ -25,7 +28,7 @@ from conftest import golden, rel
 
 pytestmark = pytest.mark.gpu
 
-HEADS = ["HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3"]
+HEADS = ["HeadNNb1", "HeadNNa1", "HeadNNc1", "HeadMN1", "HeadMN2", "HeadMN3"]
 SINGULAR = {"HeadMN1", "HeadMN2"}
 
 
