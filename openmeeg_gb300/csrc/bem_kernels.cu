@@ -598,7 +598,7 @@ void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi
 // ===========================================================================
 constexpr int GREC = 64;   // floats per triangle: centroid (3 doubles), 16 offsets, normal, h, area (double)
 // The 16-point rule of c_rules[3] rounded to FP32 (weights, barycentric nodes).
-__constant__ float c_w16[16] = {0.144315607677786f, 0.095091634267284f, 0.095091634267284f, 0.095091634267284f, 0.032458497623198f, 0.032458497623198f, 0.032458497623198f, 0.103217370534718f, 0.103217370534718f, 0.103217370534718f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f};
+__constant__ __align__(8) float c_w16[16] = {0.144315607677786f, 0.095091634267284f, 0.095091634267284f, 0.095091634267284f, 0.032458497623198f, 0.032458497623198f, 0.032458497623198f, 0.103217370534718f, 0.103217370534718f, 0.103217370534718f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f};
 __constant__ float c_b16[16][3] = {
     {0.333333333333333f, 0.333333333333333f, 0.333333333333333f},
     {0.081414823414554f, 0.459292588292722f, 0.459292588292722f},
@@ -646,10 +646,52 @@ void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s) {
     check_launch("prepare_gg");
 }
 
+// Packed FP32 pairs (two lanes per 64-bit register) and the sm_100-family
+// FP32x2 instructions on them: one issue slot performs two FP32 operations.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk2(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float lo2(f2 x) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x));
+    return a;
+}
+__device__ __forceinline__ float hi2(f2 x) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x));
+    return b;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// 1/sqrt(x) as the single approximate instruction (about 2 ulp, like rsqrtf);
+// flushing denormals is harmless here: x is a squared distance between
+// points of separated triangles.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 constexpr int FF_TI = 128, FF_TJ = 32;
 
 // One thread per t1 row, looping over the CTA's FF_TJ staged t2 records.
-__global__ void __launch_bounds__(FF_TI) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
+__global__ void __launch_bounds__(FF_TI, 4) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
                                                          int64_t t2b, int64_t n2, int same, int wantS, int wantD12,
                                                          int wantD21, double cS, const int32_t* __restrict__ tpos,
                                                          double* hm, int64_t ld, double* stmp, double* d12,
@@ -667,12 +709,18 @@ __global__ void __launch_bounds__(FF_TI) ff_block_kernel(const float* __restrict
     const float* g1 = grec + (t1b + i) * GREC;
     const double* c1p = reinterpret_cast<const double*>(g1);
     const double c1x = c1p[0], c1y = c1p[1], c1z = c1p[2];
-    float p1[16][3];
+    // the 16 points of t1 in packed pairs (even p in the low lane, odd p in the high lane): the inner
+    // products run two point pairs per FP32x2 instruction
+    f2 P1x[8], P1y[8], P1z[8];
 #pragma unroll
-    for (int p = 0; p < 16; ++p) {
-        p1[p][0] = g1[6 + 3 * p]; p1[p][1] = g1[7 + 3 * p]; p1[p][2] = g1[8 + 3 * p];
+    for (int k = 0; k < 8; ++k) {
+        P1x[k] = pk2(g1[6 + 6 * k], g1[9 + 6 * k]);
+        P1y[k] = pk2(g1[7 + 6 * k], g1[10 + 6 * k]);
+        P1z[k] = pk2(g1[8 + 6 * k], g1[11 + 6 * k]);
     }
+    const f2* W = reinterpret_cast<const f2*>(c_w16);   // weight pairs, read from the constant bank
     const float n1x = g1[54], n1y = g1[55], n1z = g1[56], h1 = g1[57];
+    const f2 N1x = pk2(n1x, n1x), N1y = pk2(n1y, n1y), N1z = pk2(n1z, n1z);
     const double A1 = reinterpret_cast<const double*>(g1 + 58)[0];
     for (int jj = 0; jj < nj; ++jj) {
         const int64_t j = j0 + jj;
@@ -689,29 +737,37 @@ __global__ void __launch_bounds__(FF_TI) ff_block_kernel(const float* __restrict
         }
         const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
         const float n2x = g2[54], n2y = g2[55], n2z = g2[56];
-        float acc21[16];
+        const f2 N2x = pk2(n2x, n2x), N2y = pk2(n2y, n2y), N2z = pk2(n2z, n2z);
+        f2 A21[8];
 #pragma unroll
-        for (int p = 0; p < 16; ++p) acc21[p] = 0.f;
+        for (int k = 0; k < 8; ++k) A21[k] = pk2(0.f, 0.f);
         float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
         for (int q = 0; q < 16; ++q) {
             const float yx = fx + g2[6 + 3 * q], yy = fy + g2[7 + 3 * q], yz = fz + g2[8 + 3 * q];
             const float wq = c_w16[q];
-            float sq = 0.f, k12 = 0.f;
+            const f2 Yx = pk2(yx, yx), Yy = pk2(yy, yy), Yz = pk2(yz, yz), NWq = pk2(-wq, -wq);
+            f2 SQ = pk2(0.f, 0.f), K12 = pk2(0.f, 0.f);
 #pragma unroll
-            for (int p = 0; p < 16; ++p) {
-                const float rx = yx - p1[p][0], ry = yy - p1[p][1], rz = yz - p1[p][2];
-                const float ir = rsqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-                const float ir3 = ir * ir * ir;
-                const float wp = c_w16[p];
-                sq = fmaf(wp, ir, sq);
-                k12 = fmaf(wp * ir3, fmaf(rx, n2x, fmaf(ry, n2y, rz * n2z)), k12);
-                acc21[p] = fmaf(-wq * ir3, fmaf(rx, n1x, fmaf(ry, n1y, rz * n1z)), acc21[p]);
+            for (int k = 0; k < 8; ++k) {
+                const f2 rx = sub2(Yx, P1x[k]), ry = sub2(Yy, P1y[k]), rz = sub2(Yz, P1z[k]);
+                const f2 r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+                const f2 ir = pk2(rsqrt_ftz(lo2(r2)), rsqrt_ftz(hi2(r2)));
+                const f2 ir3 = mul2(mul2(ir, ir), ir);
+                SQ = fma2(W[k], ir, SQ);
+                K12 = fma2(mul2(W[k], ir3), fma2(rx, N2x, fma2(ry, N2y, mul2(rz, N2z))), K12);
+                A21[k] = fma2(mul2(NWq, ir3), fma2(rx, N1x, fma2(ry, N1y, mul2(rz, N1z))), A21[k]);
             }
-            s = fmaf(wq, sq, s);
-            const float kq = wq * k12;
+            s = fmaf(wq, lo2(SQ) + hi2(SQ), s);
+            const float kq = wq * (lo2(K12) + hi2(K12));
             e0 = fmaf(kq, c_b16[q][0], e0);
             e1 = fmaf(kq, c_b16[q][1], e1);
             e2 = fmaf(kq, c_b16[q][2], e2);
+        }
+        float acc21[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            acc21[2 * k] = lo2(A21[k]);
+            acc21[2 * k + 1] = hi2(A21[k]);
         }
         const double AA = A1 * reinterpret_cast<const double*>(g2 + 58)[0];
         if (wantS) {
