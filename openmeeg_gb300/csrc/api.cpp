@@ -107,7 +107,8 @@ void trsm_cols(int64_t nrhs, int n, const T* L, int64_t ldl, bool trans, T* B, i
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
-                 const char* prof_name = "gemm_tf32x3", int max_ctas = 0);
+                 const char* prof_name = "gemm_tf32x3", int max_ctas = 0, float* Sh = nullptr, float* Sl = nullptr,
+                 int64_t s_row0 = 0, int s_kpad = 0);
 void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
@@ -569,30 +570,37 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     cudaEvent_t ev_w = sv->ctx->ev_a, ev_r = sv->ctx->ev_b;
     bool rest_pending = false;
     const int reserve = 8;   // SMs the rest update leaves to the panel chain (more made the factorization slower)
+    bool have_t = false;     // Th/Tl already hold this panel's A21 split (written by the previous next-panel update)
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
         if (k0 == nP) {   // continue on -(vertex Schur complement): every pending update must be in
             if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
             rest_pending = false;
             negate_lower<float>(A + k0 + k0 * ld, ld, N - k0, s);
+            have_t = false;
         }
         // L11 and L11^-1 (the inverse also serves the solves)
         potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
                   sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
         if (m > 0) {
-            // L21 = A21 L11^-T on the tensor cores, then its split for the trailing update
+            // L21 = A21 L11^-T on the tensor cores; its epilogue also writes the K-major split of L21
+            // (W, kept for the trailing updates and the forward solves)
             float* Tl = Th + m * nb;
-            split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
-            gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
-                        sv->ctx->d_err, s, "gemm_panel");
+            if (!have_t) split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
             float* Wh = sv->W.as<float>() + sv->w_off[b];
             float* Wl = Wh + m * nb;
-            split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Wh, Wl, s);
+            gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
+                        sv->ctx->d_err, s, "gemm_panel", 0, Wh, Wl, 0, nb);
             const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
-            // the next panel's columns (all rows below k1), after the rest update of panel b-1
+            // the next panel's columns (all rows below k1), after the rest update of panel b-1; the rows below
+            // the next diagonal block are final here and are also written as the next panel's A21 split,
+            // unless the next panel starts the vertex part (negated first)
+            const bool fuse_t = mr > 0 && k1 != nP;
             if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
             gemm_tf32x3(m, nn, nk, -1.f, Wh, Wl, nb, nb, 0, Wh, Wl, nb, nb, 0, 1.f, A + k1 + k1 * ld, ld, false,
-                        sv->ctx->d_err, s, "gemm_next");
+                        sv->ctx->d_err, s, "gemm_next", 0, fuse_t ? Th : nullptr, fuse_t ? Th + mr * nb : nullptr, nn,
+                        nb);
+            have_t = fuse_t;
             rest_pending = false;
             if (mr > 0) {   // the rest, on the second stream
                 OMG_CUDA(cudaEventRecord(ev_w, s));

@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                        const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
                        int K, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod, int64_t ntiles,
-                       int* err) {
+                       int* err, float* Sh, float* Sl, int s_row0, int s_kpad) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -200,14 +200,34 @@ __global__ void __launch_bounds__(THREADS, 1)
                 break;
             }
             fence_after();
+            // optional K-major TF32 head / remainder copy of rows >= s_row0 (row stride s_kpad, zero past N)
+            float* const sh = (Sh && row >= s_row0 && row < M) ? Sh + (int64_t)(row - s_row0) * s_kpad + n0 : nullptr;
 #pragma unroll
             for (int chunk = 0; chunk < 2; ++chunk) {
                 uint32_t r[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64 + chunk * 32), r);
+                float v[32];
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (chunk * 32 + j < jmax)
-                        __stcg(cp + (chunk * 32 + j) * ld32, fmaf(alpha, __uint_as_float(r[j]), beta * cv[chunk * 32 + j]));
+                for (int j = 0; j < 32; ++j) {
+                    v[j] = fmaf(alpha, __uint_as_float(r[j]), beta * cv[chunk * 32 + j]);
+                    if (chunk * 32 + j < jmax) __stcg(cp + (chunk * 32 + j) * ld32, v[j]);
+                }
+                if (sh && n0 + chunk * 32 < s_kpad) {
+                    float* const shc = sh + chunk * 32;
+                    float* const slc = Sl + (shc - Sh);
+#pragma unroll
+                    for (int j4 = 0; j4 < 8; ++j4) {
+                        float h[4], l[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float x = (chunk * 32 + 4 * j4 + u < jmax) ? v[4 * j4 + u] : 0.f;
+                            h[u] = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+                            l[u] = x - h[u];
+                        }
+                        reinterpret_cast<float4*>(shc)[j4] = make_float4(h[0], h[1], h[2], h[3]);
+                        reinterpret_cast<float4*>(slc)[j4] = make_float4(l[0], l[1], l[2], l[3]);
+                    }
+                }
             }
             fence_before();
             __syncwarp();
@@ -248,7 +268,12 @@ static inline void check_tc(const char* what) {
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
-                 const char* prof_name, int max_ctas) {
+                 const char* prof_name, int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad) {
+    if (Sh) {   // the copy covers whole 128-column tiles: one tile column, 16-byte aligned rows
+        if (!Sl || lower || N > tc::BN || s_kpad != tc::BN || s_row0 < 0 ||
+            (reinterpret_cast<uintptr_t>(Sh) % 16) || (reinterpret_cast<uintptr_t>(Sl) % 16))
+            throw Error(OMG_ERR_INVALID, "tensor-core GEMM split copy: unsupported shape");
+    }
     if (M <= 0 || N <= 0) return;
     if (K <= 0) throw Error(OMG_ERR_INVALID, "empty K");
     ProfScope prof_(prof_name, s);
@@ -276,7 +301,8 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
     tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, alpha,
-                                                                     beta, C, ldc, lower ? 1 : 0, nprod, ntiles, err);
+                                                                     beta, C, ldc, lower ? 1 : 0, nprod, ntiles, err, Sh,
+                                                                     Sl, (int)s_row0, s_kpad);
     check_tc("gemm_tf32x3");
 }
 
@@ -376,7 +402,23 @@ extern "C" int omg_internal_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float a
                                         float beta, float* C, int64_t ldc, int lower, int* err) {
     try {
         omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, lower != 0, err, 0,
-                         "gemm_tf32x3", 0);
+                         "gemm_tf32x3", 0, nullptr, nullptr, 0, 0);
+        cudaError_t e = cudaDeviceSynchronize();
+        return e == cudaSuccess ? 0 : -2;
+    } catch (const omg::Error& e) {
+        return e.code;
+    }
+}
+
+// Test hook: the same with the K-major TF32 split copy of C's rows >= s_row0
+// written by the epilogue (N <= 128, row stride 128).
+extern "C" int omg_internal_gemm_tf32x3_split(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
+                                              const float* Al, int64_t lda, const float* Bh, const float* Bl,
+                                              int64_t ldb, float beta, float* C, int64_t ldc, float* Sh, float* Sl,
+                                              int64_t s_row0, int* err) {
+    try {
+        omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, false, err, 0,
+                         "gemm_tf32x3", 0, Sh, Sl, s_row0, 128);
         cudaError_t e = cudaDeviceSynchronize();
         return e == cudaSuccess ? 0 : -2;
     } catch (const omg::Error& e) {

@@ -69,6 +69,35 @@ def test_tc_gemm_lower_update(cuda):
     assert _run(640, 640, 128, -1.0, 1.0, True, True) < 1e-5
 
 
+@pytest.mark.parametrize("M,N,K,row0", [(1000, 128, 128, 0), (777, 90, 128, 128), (4300, 128, 96, 40)])
+def test_tc_gemm_epilogue_split_copy(cuda, M, N, K, row0):
+    """The epilogue's K-major TF32 head/remainder copy of C's rows >= row0 (row
+    stride 128, zero past N) equals the split of the C it writes, bit for bit."""
+    import torch
+    from openmeeg_gb300 import _lib
+    f = _lib.load().omg_internal_gemm_tf32x3_split
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
+                  ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p,
+                  ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+    g = torch.Generator(device="cuda").manual_seed(M)
+    A = torch.randn(M, K, device="cuda", generator=g)
+    B = torch.randn(N, K, device="cuda", generator=g)
+    Ah, Al = _split(A)
+    Bh, Bl = _split(B)
+    C = torch.randn(N, M, device="cuda", generator=g)          # column-major M x N
+    Sh = torch.full((M - row0, 128), 7.0, device="cuda")         # garbage that must be overwritten
+    Sl = torch.full((M - row0, 128), 7.0, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert f(M, N, K, -1.0, p(Ah), p(Al), K, p(Bh), p(Bl), K, 1.0, p(C), M, p(Sh), p(Sl), row0, p(err)) == 0
+    assert int(err.item()) == 0
+    rows = C.T[row0:]                                            # (M - row0) x N, row-major
+    h, l = _split(rows.contiguous())
+    assert torch.equal(Sh[:, :N], h) and torch.equal(Sl[:, :N], l)
+    assert float(Sh[:, N:].abs().max() if N < 128 else 0.0) == 0.0 and float(Sl[:, N:].abs().max() if N < 128 else 0.0) == 0.0
+
+
 @pytest.mark.parametrize("M,N,K,lower", [(5000, 1000, 64, False), (4100, 4100, 128, True)])
 def test_tc_gemm_many_tiles_per_cta(cuda, M, N, K, lower):
     # more tiles than SMs: every CTA walks several tiles through both TMEM accumulators
