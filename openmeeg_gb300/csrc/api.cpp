@@ -109,6 +109,11 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
                  const char* prof_name = "gemm_tf32x3", int max_ctas = 0, float* Sh = nullptr, float* Sl = nullptr,
                  int64_t s_row0 = 0, int s_kpad = 0);
+void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float* A1h, const float* A1l, int64_t lda1,
+                      const float* B1h, const float* B1l, int64_t ldb1, int64_t K2, const float* A2h,
+                      const float* A2l, int64_t lda2, const float* B2h, const float* B2l, int64_t ldb2, float beta,
+                      float* C, int64_t ldc, bool lower, int* err, cudaStream_t s, const char* prof_name,
+                      int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad);
 void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
@@ -569,49 +574,87 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     cudaStream_t s2 = sv->ctx->aux;
     cudaEvent_t ev_w = sv->ctx->ev_a, ev_r = sv->ctx->ev_b;
     bool rest_pending = false;
-    const int reserve = 8;   // SMs the rest update leaves to the panel chain (more made the factorization slower)
-    bool have_t = false;     // Th/Tl already hold this panel's A21 split (written by the previous next-panel update)
-    for (size_t b = 0; b < nblocks; ++b) {
-        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
-        if (k0 == nP) {   // continue on -(vertex Schur complement): every pending update must be in
+    const int reserve = 24;   // SMs the rest update leaves to the panel chain (measured optimum at config1)
+    bool have_t = false;     // Th/Tl already hold this panel's A21 split (written by the update before it)
+    // Panels are taken in groups of two (never across the start of the vertex part): the trailing
+    // update of a group runs once with K = 256, which halves the traffic of reading and writing the
+    // trailing matrix compared with one update per panel.
+    std::vector<size_t> groups;
+    for (size_t b = 0; b < nblocks;) {
+        groups.push_back(b);
+        b += (b + 1 < nblocks && sv->bounds[b + 1] != nP) ? 2 : 1;
+    }
+    groups.push_back(nblocks);
+    auto wh = [&](size_t p) { return sv->W.as<float>() + sv->w_off[p]; };
+    auto wl = [&](size_t p) { return wh(p) + (N - sv->bounds[p + 1]) * nb; };
+    // C -= sum over the group's panels of W_p(rows from r0) W_p(rows from c0)^T (one or two K segments)
+    auto group_update = [&](size_t gb, size_t ge, int64_t M, int64_t Nc, int64_t r0, int64_t c0, float* C, bool lower,
+                            cudaStream_t st, const char* name, int max_ctas, float* Sh, float* Sl, int64_t s_row0) {
+        const int64_t o1 = sv->bounds[gb + 1], nk1 = o1 - sv->bounds[gb];
+        if (ge - gb == 1) {
+            gemm_tf32x3(M, Nc, nk1, -1.f, wh(gb) + (r0 - o1) * nb, wl(gb) + (r0 - o1) * nb, nb, nb, 0,
+                        wh(gb) + (c0 - o1) * nb, wl(gb) + (c0 - o1) * nb, nb, nb, 0, 1.f, C, ld, lower, sv->ctx->d_err,
+                        st, name, max_ctas, Sh, Sl, s_row0, nb);
+        } else {
+            const int64_t o2 = sv->bounds[gb + 2], nk2 = o2 - o1;
+            gemm_tf32x3_pair(M, Nc, -1.f, nk1, wh(gb) + (r0 - o1) * nb, wl(gb) + (r0 - o1) * nb, nb,
+                             wh(gb) + (c0 - o1) * nb, wl(gb) + (c0 - o1) * nb, nb, nk2, wh(gb + 1) + (r0 - o2) * nb,
+                             wl(gb + 1) + (r0 - o2) * nb, nb, wh(gb + 1) + (c0 - o2) * nb, wl(gb + 1) + (c0 - o2) * nb,
+                             nb, 1.f, C, ld, lower, sv->ctx->d_err, st, name, max_ctas, Sh, Sl, s_row0, nb);
+        }
+    };
+    for (size_t g = 0; g + 1 < groups.size(); ++g) {
+        const size_t gb = groups[g], ge = groups[g + 1];
+        if (sv->bounds[gb] == nP) {   // continue on -(vertex Schur complement): every pending update must be in
             if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
             rest_pending = false;
-            negate_lower<float>(A + k0 + k0 * ld, ld, N - k0, s);
+            negate_lower<float>(A + nP + nP * ld, ld, N - nP, s);
             have_t = false;
         }
-        // L11 and L11^-1 (the inverse also serves the solves)
-        potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
-                  sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
-        if (m > 0) {
+        for (size_t b = gb; b < ge; ++b) {
+            const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
+            // L11 and L11^-1 (the inverse also serves the solves)
+            potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
+                      sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
+            if (m == 0) continue;
             // L21 = A21 L11^-T on the tensor cores; its epilogue also writes the K-major split of L21
             // (W, kept for the trailing updates and the forward solves)
             float* Tl = Th + m * nb;
             if (!have_t) split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
-            float* Wh = sv->W.as<float>() + sv->w_off[b];
-            float* Wl = Wh + m * nb;
             gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
-                        sv->ctx->d_err, s, "gemm_panel", 0, Wh, Wl, 0, nb);
-            const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
-            // the next panel's columns (all rows below k1), after the rest update of panel b-1; the rows below
-            // the next diagonal block are final here and are also written as the next panel's A21 split,
-            // unless the next panel starts the vertex part (negated first)
-            const bool fuse_t = mr > 0 && k1 != nP;
-            if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
-            gemm_tf32x3(m, nn, nk, -1.f, Wh, Wl, nb, nb, 0, Wh, Wl, nb, nb, 0, 1.f, A + k1 + k1 * ld, ld, false,
-                        sv->ctx->d_err, s, "gemm_next", 0, fuse_t ? Th : nullptr, fuse_t ? Th + mr * nb : nullptr, nn,
-                        nb);
-            have_t = fuse_t;
-            rest_pending = false;
-            if (mr > 0) {   // the rest, on the second stream
-                OMG_CUDA(cudaEventRecord(ev_w, s));
-                OMG_CUDA(cudaStreamWaitEvent(s2, ev_w, 0));
-                const float* Rh = Wh + nn * nb;
-                const float* Rl = Wl + nn * nb;
-                gemm_tf32x3(mr, mr, nk, -1.f, Rh, Rl, nb, nb, 0, Rh, Rl, nb, nb, 0, 1.f, A + k2 + k2 * ld, ld, true,
-                            sv->ctx->d_err, s2, "gemm_syrk", std::max(1, n_sm() - reserve));
-                OMG_CUDA(cudaEventRecord(ev_r, s2));
-                rest_pending = true;
+                        sv->ctx->d_err, s, "gemm_panel", 0, wh(b), wl(b), 0, nb);
+            have_t = false;
+            if (b + 1 < ge) {   // the group's second panel (all rows below k1), with its A21 split
+                const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
+                gemm_tf32x3(m, nn, nk, -1.f, wh(b), wl(b), nb, nb, 0, wh(b), wl(b), nb, nb, 0, 1.f,
+                            A + k1 + k1 * ld, ld, false, sv->ctx->d_err, s, "gemm_next", 0, mr > 0 ? Th : nullptr,
+                            mr > 0 ? Th + mr * nb : nullptr, nn, nb);
+                have_t = mr > 0;
             }
+        }
+        if (ge == nblocks) break;
+        // look-ahead: the next group's columns (all rows below their start), after the rest update of the
+        // previous group, on the main stream; the first one's rows below its diagonal block are also written
+        // as its A21 split unless the next group starts the vertex part (negated first)
+        const size_t ng = groups[g + 2];
+        if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
+        rest_pending = false;
+        for (size_t p = ge; p < ng; ++p) {
+            const int64_t kp0 = sv->bounds[p], kp1 = sv->bounds[p + 1], M = N - kp0, w = kp1 - kp0;
+            const bool fuse_t = p == ge && N - kp1 > 0 && kp0 != nP;
+            group_update(gb, ge, M, w, kp0, kp0, A + kp0 + kp0 * ld, false, s, "gemm_next", 0,
+                         fuse_t ? Th : nullptr, fuse_t ? Th + (N - kp1) * nb : nullptr, w);
+            if (p == ge) have_t = fuse_t;
+        }
+        // the rest, on the second stream
+        const int64_t kr = sv->bounds[ng], mr = N - kr;
+        if (mr > 0) {
+            OMG_CUDA(cudaEventRecord(ev_w, s));
+            OMG_CUDA(cudaStreamWaitEvent(s2, ev_w, 0));
+            group_update(gb, ge, mr, mr, kr, kr, A + kr + kr * ld, true, s2, "gemm_syrk", std::max(1, n_sm() - reserve),
+                         nullptr, nullptr, 0);
+            OMG_CUDA(cudaEventRecord(ev_r, s2));
+            rest_pending = true;
         }
     }
     if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));

@@ -67,11 +67,15 @@ __device__ __forceinline__ void tile_of(int64_t t, int tiles_m, int lower, int& 
     }
 }
 
+// K may come in two segments with their own operand maps (the second set is
+// used for the chunks past K0 when K > K0): an update by two panels at once.
 __global__ void __launch_bounds__(THREADS, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
-                       const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
-                       int K, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod, int64_t ntiles,
-                       int* err, float* Sh, float* Sl, int s_row0, int s_kpad) {
+                       const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl,
+                       const __grid_constant__ CUtensorMap tAh2, const __grid_constant__ CUtensorMap tAl2,
+                       const __grid_constant__ CUtensorMap tBh2, const __grid_constant__ CUtensorMap tBl2, int M,
+                       int N, int K, int K0, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod,
+                       int64_t ntiles, int* err, float* Sh, float* Sl, int s_row0, int s_kpad) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -81,7 +85,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t sbase = (dev::smem_u32(smem_raw) + 1023u) & ~1023u;   // 1024-byte aligned ring
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int tiles_m = (M + BM - 1) / BM;
-    const int nk = (K + BK - 1) / BK;
+    const int nk0 = (K0 + BK - 1) / BK;                       // chunks of the first segment
+    const int nk = nk0 + (K - K0 + BK - 1) / BK;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             dev::mbar_init(&full_bar[s], 1);
@@ -122,12 +127,14 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     const uint32_t st = sbase + slot * STAGE_BYTES;
+                    const bool seg2 = c >= nk0;
+                    const int x = (seg2 ? c - nk0 : c) * BK;
                     dev::mbar_expect_tx(&full_bar[slot], bytes_per_stage);
-                    tma_load_2d(st, &tAh, c * BK, tm * BM, &full_bar[slot]);
-                    tma_load_2d(st + 2 * TILE_BYTES, &tBh, c * BK, tn * BN, &full_bar[slot]);
+                    tma_load_2d(st, seg2 ? &tAh2 : &tAh, x, tm * BM, &full_bar[slot]);
+                    tma_load_2d(st + 2 * TILE_BYTES, seg2 ? &tBh2 : &tBh, x, tn * BN, &full_bar[slot]);
                     if (nprod == 3) {
-                        tma_load_2d(st + TILE_BYTES, &tAl, c * BK, tm * BM, &full_bar[slot]);
-                        tma_load_2d(st + 3 * TILE_BYTES, &tBl, c * BK, tn * BN, &full_bar[slot]);
+                        tma_load_2d(st + TILE_BYTES, seg2 ? &tAl2 : &tAl, x, tm * BM, &full_bar[slot]);
+                        tma_load_2d(st + 3 * TILE_BYTES, seg2 ? &tBl2 : &tBl, x, tn * BN, &full_bar[slot]);
                     }
                     s_issued = g + 1;
                 }
@@ -300,9 +307,52 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     if (tiles_m > (1 << 30) / 2) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM too tall");
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
-    tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, alpha,
-                                                                     beta, C, ldc, lower ? 1 : 0, nprod, ntiles, err, Sh,
-                                                                     Sl, (int)s_row0, s_kpad);
+    tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, mAh, mAl, mBh, mBl, (int)M,
+                                                                     (int)N, (int)K, (int)K, alpha, beta, C, ldc,
+                                                                     lower ? 1 : 0, nprod, ntiles, err, Sh, Sl,
+                                                                     (int)s_row0, s_kpad);
+    check_tc("gemm_tf32x3");
+}
+
+// C(M x N, ldc) = beta C + alpha (A1 B1^T + A2 B2^T): two K segments (K1, K2, each
+// a multiple of 32 but the last) in one pass over C; all operands split
+// (3xTF32), K-major with row strides lda1 / ldb1 / lda2 / ldb2.
+void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float* A1h, const float* A1l, int64_t lda1,
+                      const float* B1h, const float* B1l, int64_t ldb1, int64_t K2, const float* A2h,
+                      const float* A2l, int64_t lda2, const float* B2h, const float* B2l, int64_t ldb2, float beta,
+                      float* C, int64_t ldc, bool lower, int* err, cudaStream_t s, const char* prof_name,
+                      int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad) {
+    if (M <= 0 || N <= 0) return;
+    if (K1 <= 0 || K2 <= 0 || (K1 % tc::BK)) throw Error(OMG_ERR_INVALID, "tensor-core GEMM segments");
+    if (Sh) {
+        if (!Sl || lower || N > tc::BN || s_kpad != tc::BN || s_row0 < 0 ||
+            (reinterpret_cast<uintptr_t>(Sh) % 16) || (reinterpret_cast<uintptr_t>(Sl) % 16))
+            throw Error(OMG_ERR_INVALID, "tensor-core GEMM split copy: unsupported shape");
+    }
+    ProfScope prof_(prof_name, s);
+    const CUtensorMap m1h = tc::make_map(A1h, M, K1, lda1), m1l = tc::make_map(A1l, M, K1, lda1);
+    const CUtensorMap n1h = tc::make_map(B1h, N, K1, ldb1), n1l = tc::make_map(B1l, N, K1, ldb1);
+    const CUtensorMap m2h = tc::make_map(A2h, M, K2, lda2), m2l = tc::make_map(A2l, M, K2, lda2);
+    const CUtensorMap n2h = tc::make_map(B2h, N, K2, ldb2), n2l = tc::make_map(B2l, N, K2, ldb2);
+    static bool attr = false;
+    static int n_sm = 0;
+    if (!attr) {
+        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (n_sm <= 0) n_sm = 1;
+        attr = true;
+    }
+    if (lower && M != N) throw Error(OMG_ERR_INVALID, "lower-triangle tensor-core update needs M == N");
+    if (ldc > (int64_t)(1 << 24)) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM leading dimension too large");
+    const int64_t tiles_m = (M + tc::BM - 1) / tc::BM, tiles_n = (N + tc::BN - 1) / tc::BN;
+    const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
+    tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(m1h, m1l, n1h, n1l, m2h, m2l, n2h, n2l, (int)M,
+                                                                     (int)N, (int)(K1 + K2), (int)K1, alpha, beta, C,
+                                                                     ldc, lower ? 1 : 0, 3, ntiles, err, Sh, Sl,
+                                                                     (int)s_row0, s_kpad);
     check_tc("gemm_tf32x3");
 }
 
