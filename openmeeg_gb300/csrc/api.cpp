@@ -108,21 +108,20 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
                  const char* prof_name = "gemm_tf32x3", int max_ctas = 0, float* Sh = nullptr, float* Sl = nullptr,
-                 int64_t s_row0 = 0, int s_kpad = 0);
+                 int64_t s_row0 = 0, int s_kpad = 0, float* Cr = nullptr, float* Xh = nullptr, float* Xl = nullptr,
+                 int64_t x_row0 = 0, bool pdl = false);
 void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float* A1h, const float* A1l, int64_t lda1,
                       const float* B1h, const float* B1l, int64_t ldb1, int64_t K2, const float* A2h,
                       const float* A2l, int64_t lda2, const float* B2h, const float* B2l, int64_t ldb2, float beta,
                       float* C, int64_t ldc, bool lower, int* err, cudaStream_t s, const char* prof_name,
-                      int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad);
+                      int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad, bool pdl = false);
 void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
-void split_lower_inplace(int64_t n, float* A, int64_t lda, float* R, cudaStream_t s);
-void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_t lda, float* Linv, cudaStream_t s);
 void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
                float* Bl, cudaStream_t s);
-void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, float* B, int64_t ldb, float* H,
-                     float* L, cudaStream_t s);
+void apply_inv_blocks(int64_t nblocks, int nb, int n_last, int64_t ncol, const float* Li, bool trans, float* B,
+                      int64_t ldb, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
                    cudaStream_t s);
 void ratio_max(int64_t n, const double* num, const double* den, double* out, cudaStream_t s);
@@ -540,10 +539,12 @@ constexpr int NB32_TC = 128;   // tensor-core path: panel width = GEMM K = 4 x 3
 
 // FP32 factorization with the panel solves and trailing updates on the
 // tensor cores (3xTF32): each diagonal block is factored and inverted in one
-// CTA, the panel is L21 = A21 L11^-T by the tcgen05 GEMM, L21 is split into
-// K-major TF32 heads/remainders (kept for the forward solves) and the
-// trailing block is updated by the tcgen05 GEMM; at the end the whole factor
-// is split in place (heads) + remainders (A32r) for the backward solves.
+// CTA, the panel is L21 = A21 L11^-T by the tcgen05 GEMM, whose epilogue
+// writes L21 as TF32 heads (in A) + remainders (A32r) and its K-major split
+// copy (W), and the trailing block is updated by the tcgen05 GEMM from W.  At
+// the end the diagonal-block inverses are folded into the solve operators:
+// W_b <- L21_b Linv_b (forward sweeps) and the block rows
+// L[k0:k1, 0:k0] <- Linv_b L[k0:k1, 0:k0] in A / A32r (backward sweeps).
 static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N, nP = sv->nP;
@@ -560,11 +561,11 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     for (size_t b = 0; b < nblocks; ++b) sv->w_off[b + 1] = sv->w_off[b] + 2 * (N - sv->bounds[b + 1]) * nb;
     sv->W = DevBuf((size_t)std::max<int64_t>(1, sv->w_off[nblocks]) * sizeof(float), s, sv->persistent);
     sv->Linv32 = DevBuf((size_t)nblocks * nb * nb * sizeof(float), s, sv->persistent);
+    sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
+    float* Ar = sv->A32r.as<float>();
     DevBuf T((size_t)2 * std::max<int64_t>(1, N) * nb * sizeof(float), s);   // A21 split, K-major
-    DevBuf Bi((size_t)2 * nb * nb * sizeof(float), s);                        // L11^-1 split, K-major
+    DevBuf Bi((size_t)2 * nblocks * nb * nb * sizeof(float), s);             // L11^-1 split, K-major, per block
     float* Th = T.as<float>();
-    float* Bih = Bi.as<float>();
-    float* Bil = Bih + (size_t)nb * nb;
     // Look-ahead: the trailing update of panel b is split into the next panel's columns (on the
     // main stream, so panel b+1 can be factored at once) and the rest (on the second stream, with a
     // few SMs left free), so the latency-bound diagonal-block work of panel b+1 overlaps the bulk
@@ -594,13 +595,13 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
         if (ge - gb == 1) {
             gemm_tf32x3(M, Nc, nk1, -1.f, wh(gb) + (r0 - o1) * nb, wl(gb) + (r0 - o1) * nb, nb, nb, 0,
                         wh(gb) + (c0 - o1) * nb, wl(gb) + (c0 - o1) * nb, nb, nb, 0, 1.f, C, ld, lower, sv->ctx->d_err,
-                        st, name, max_ctas, Sh, Sl, s_row0, nb);
+                        st, name, max_ctas, Sh, Sl, s_row0, nb, nullptr, nullptr, nullptr, 0, st == s);
         } else {
             const int64_t o2 = sv->bounds[gb + 2], nk2 = o2 - o1;
             gemm_tf32x3_pair(M, Nc, -1.f, nk1, wh(gb) + (r0 - o1) * nb, wl(gb) + (r0 - o1) * nb, nb,
                              wh(gb) + (c0 - o1) * nb, wl(gb) + (c0 - o1) * nb, nb, nk2, wh(gb + 1) + (r0 - o2) * nb,
                              wl(gb + 1) + (r0 - o2) * nb, nb, wh(gb + 1) + (c0 - o2) * nb, wl(gb + 1) + (c0 - o2) * nb,
-                             nb, 1.f, C, ld, lower, sv->ctx->d_err, st, name, max_ctas, Sh, Sl, s_row0, nb);
+                             nb, 1.f, C, ld, lower, sv->ctx->d_err, st, name, max_ctas, Sh, Sl, s_row0, nb, st == s);
         }
     };
     for (size_t g = 0; g + 1 < groups.size(); ++g) {
@@ -614,15 +615,18 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
         for (size_t b = gb; b < ge; ++b) {
             const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
             // L11 and L11^-1 (the inverse also serves the solves)
+            float* Bih = Bi.as<float>() + 2 * b * nb * nb;
+            float* Bil = Bih + (size_t)nb * nb;
             potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
                       sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
             if (m == 0) continue;
-            // L21 = A21 L11^-T on the tensor cores; its epilogue also writes the K-major split of L21
-            // (W, kept for the trailing updates and the forward solves)
+            // L21 = A21 L11^-T on the tensor cores, written as heads (A) + remainders (A32r); its epilogue
+            // also writes the K-major split of L21 (W, kept for the trailing updates and the forward solves)
             float* Tl = Th + m * nb;
             if (!have_t) split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
             gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
-                        sv->ctx->d_err, s, "gemm_panel", 0, wh(b), wl(b), 0, nb);
+                        sv->ctx->d_err, s, "gemm_panel", 0, wh(b), wl(b), 0, nb, Ar + k1 + k0 * ld, nullptr, nullptr, 0,
+                        true);
             have_t = false;
             if (b + 1 < ge) {   // the group's second panel (all rows below k1), with its A21 split
                 const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
@@ -658,11 +662,37 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
         }
     }
     if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
-    sv->A32r = DevBuf((size_t)ld * N * sizeof(float), s, sv->persistent);
-    split_lower_inplace(N, A, ld, sv->A32r.as<float>(), s);
+    // Fold the diagonal-block inverses into the solve operators, in place (each tile of these products
+    // reads only the rows of W, or the columns of the block row, that it writes):
+    //   W_b(i, c) <- sum_l L21_b(i, l) Linv_b(l, c)         as C^T = Linv_b^T W_b^T (heads in W_b, remainders
+    //                                                         in its second half)
+    //   A(k0 + k, m) <- sum_l Linv_b(k, l) A(k0 + l, m)      for m < k0 (heads in A, remainders in A32r)
+    DevBuf LC((size_t)2 * nblocks * nb * nb * sizeof(float), s);   // Linv_b split as stored (column-major)
+    float* LCh = LC.as<float>();
+    float* LCl = LCh + nblocks * nb * nb;
+    split_cols(nb, (int64_t)nblocks * nb, nb, sv->Linv32.as<float>(), nb, LCh, LCl, s);
+    for (size_t b = 0; b < nblocks; ++b) {
+        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
+        if (m > 0)
+            gemm_tf32x3(nk, m, nk, 1.f, LCh + b * nb * nb, LCl + b * nb * nb, nb, nb, 0, wh(b), wl(b), nb, nb, 0,
+                        0.f, wh(b), nb, false, sv->ctx->d_err, s, "fold_w", 0, nullptr, nullptr, 0, 0, wl(b), nullptr,
+                        nullptr, 0, true);
+        if (k0 > 0) {
+            const float* Rh = Bi.as<float>() + 2 * b * nb * nb;   // Linv_b split, K-major rows
+            gemm_tf32x3(nk, k0, nk, 1.f, Rh, Rh + nb * nb, nb, nb, 0, A, Ar, ld, N, k0, 0.f, A + k0, ld, false,
+                        sv->ctx->d_err, s, "fold_rows", 0, nullptr, nullptr, 0, 0, Ar + k0, nullptr, nullptr, 0, true);
+        }
+    }
 }
 
-// FP32 solve on the tensor cores: B <- HM^-1 B (internal numbering).
+// FP32 solve on the tensor cores: B <- HM^-1 B (internal numbering).  With
+// the diagonal-block inverses folded into W and the block rows of A, each
+// sweep is a chain of tensor-core updates by the not yet inverted blocks
+// (forward: b~_k = b_k - sum_{j<k} L_kj Linv_j b~_j; backward alike with
+// Linv_k L_kj), each update writing the K-major split of the block that the
+// next update takes (band copy); the inverses are then applied to all blocks
+// at once.  All blocks but the last have 128 rows (the vertex part starts on
+// a multiple of 128).
 static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N, ld = sv->ld32;
@@ -670,27 +700,36 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
     const float* Ar = sv->A32r.as<float>();
     const int nb = NB32_TC;
     const size_t nblocks = sv->bounds.size() - 1;
-    DevBuf X((size_t)2 * nb * nrhs * sizeof(float), s);
-    float* Xh = X.as<float>();
-    float* Xl = Xh + (size_t)nb * nrhs;
-    for (size_t b = 0; b < nblocks; ++b) {   // L y = b
-        const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
-        apply_inv_split((int)nk, nb, nrhs, sv->Linv32.as<float>() + b * nb * nb, false, B + k0, ldb, Xh, Xl, s);
-        if (m > 0) {
-            const float* Wh = sv->W.as<float>() + sv->w_off[b];
-            gemm_tf32x3(m, nrhs, nk, -1.f, Wh, Wh + m * nb, nb, nb, 0, Xh, Xl, nb, nb, 0, 1.f, B + k1, ldb, false,
-                        sv->ctx->d_err, s, "gemm_solve");
-        }
+    for (size_t b = 0; b + 1 < nblocks; ++b)
+        if (sv->bounds[b + 1] - sv->bounds[b] != nb) throw Error(OMG_ERR_UNSUPPORTED, "solver blocks not 128 wide");
+    const int n_last = (int)(N - sv->bounds[nblocks - 1]);
+    const size_t xs = (size_t)nb * nrhs;
+    DevBuf X(4 * xs * sizeof(float), s);
+    float* xb[2] = {X.as<float>(), X.as<float>() + 2 * xs};   // heads, then remainders
+    int cur = 0;
+    // L y = b
+    split_cols((int)std::min<int64_t>(nb, N), nrhs, nb, B, ldb, xb[0], xb[0] + xs, s);
+    for (size_t b = 0; b + 1 < nblocks; ++b) {
+        const int64_t k1 = sv->bounds[b + 1], nk = k1 - sv->bounds[b], m = N - k1;
+        const float* Wh = sv->W.as<float>() + sv->w_off[b];
+        float* xn = xb[cur ^ 1];
+        gemm_tf32x3(m, nrhs, nk, -1.f, Wh, Wh + m * nb, nb, nb, 0, xb[cur], xb[cur] + xs, nb, nb, 0, 1.f, B + k1,
+                    ldb, false, sv->ctx->d_err, s, "gemm_solve", 0, nullptr, nullptr, 0, 0, nullptr, xn, xn + xs, 0, true);
+        cur ^= 1;
     }
+    apply_inv_blocks((int64_t)nblocks, nb, n_last, nrhs, sv->Linv32.as<float>(), false, B, ldb, s);
     negate_rows<float>(B, ldb, sv->nP, N, nrhs, s);
-    for (size_t bb = nblocks; bb-- > 0;) {   // L^T x = y, right-looking
-        const int64_t k0 = sv->bounds[bb], k1 = sv->bounds[bb + 1], nk = k1 - k0;
-        apply_inv_split((int)nk, nb, nrhs, sv->Linv32.as<float>() + bb * nb * nb, true, B + k0, ldb, Xh, Xl, s);
-        if (k0 > 0) {
-            gemm_tf32x3(k0, nrhs, nk, -1.f, A, Ar, ld, N, k0, Xh, Xl, nb, nb, 0, 1.f, B, ldb, false, sv->ctx->d_err,
-                        s, "gemm_solve");
-        }
+    // L^T x = y, right-looking
+    const int64_t kl = sv->bounds[nblocks - 1];
+    split_cols(n_last, nrhs, nb, B + kl, ldb, xb[cur], xb[cur] + xs, s);
+    for (size_t bb = nblocks - 1; bb >= 1; --bb) {
+        const int64_t k0 = sv->bounds[bb], nk = sv->bounds[bb + 1] - k0;
+        float* xn = xb[cur ^ 1];
+        gemm_tf32x3(k0, nrhs, nk, -1.f, A, Ar, ld, N, k0, xb[cur], xb[cur] + xs, nb, nb, 0, 1.f, B, ldb, false,
+                    sv->ctx->d_err, s, "gemm_solve", 0, nullptr, nullptr, 0, 0, nullptr, xn, xn + xs, k0 - nb, true);
+        cur ^= 1;
     }
+    apply_inv_blocks((int64_t)nblocks, nb, n_last, nrhs, sv->Linv32.as<float>(), true, B, ldb, s);
 }
 
 // In place: B <- HM^-1 B (internal numbering), HM = L diag(+I_P, -I_V) L^T.

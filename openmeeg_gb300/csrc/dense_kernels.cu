@@ -642,64 +642,6 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 }
 
 // ---------------------------------------------------------------------------
-// Explicit inverses of the diagonal blocks of a lower-triangular factor
-// (block b starts at b*128; the factor may be split as head + remainder).
-// One CTA per block; each warp solves L x = e_c for its columns c with the
-// block staged in shared memory.  Output: Linv (nblk x 128 x 128, column-
-// major, zero above the diagonal).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) inv_lower_blocks_kernel(int64_t N, int nb, const float* __restrict__ A,
-                                                               const float* __restrict__ Ar, int64_t lda,
-                                                               float* Linv) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    float* sL = reinterpret_cast<float*>(smraw);   // n x n row-major: sL[j*n + l] = L[j][l]
-    float* sx = sL + nb * nb;                      // 8 warps x n
-    const int64_t k0 = (int64_t)blockIdx.x * nb;
-    const int n = (int)((N - k0) < nb ? (N - k0) : nb);
-    const float* Ab = A + k0 + k0 * lda;
-    const float* Rb = Ar ? Ar + k0 + k0 * lda : nullptr;
-    for (int e = threadIdx.x; e < n * n; e += 256) {
-        const int r = e % n, c = e / n;
-        sL[r * n + c] = (r >= c) ? (Rb ? Ab[r + c * lda] + Rb[r + c * lda] : Ab[r + c * lda]) : 0.f;
-    }
-    __syncthreads();
-    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    float* x = sx + warp * n;
-    float* out = Linv + (int64_t)blockIdx.x * nb * nb;
-    for (int c = warp; c < nb; c += 8) {
-        if (c >= n) {   // identity on the unused part of a short last block
-            for (int i = lane; i < nb; i += 32) out[i + c * nb] = (i == c) ? 1.f : 0.f;
-            continue;
-        }
-        for (int l = lane; l < n; l += 32) x[l] = 0.f;
-        __syncwarp();
-        for (int j = c; j < n; ++j) {
-            float acc = 0.f;
-            for (int l = c + lane; l < j; l += 32) acc += sL[j * n + l] * x[l];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) x[j] = ((j == c ? 1.f : 0.f) - acc) / sL[j * n + j];
-            __syncwarp();
-        }
-        for (int i = lane; i < nb; i += 32) out[i + c * nb] = (i < n) ? x[i] : 0.f;
-        __syncwarp();
-    }
-}
-
-void inv_lower_blocks(int64_t N, int nb, const float* A, const float* Ar, int64_t lda, float* Linv, cudaStream_t s) {
-    ProfScope prof_("inv_blocks", s);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(inv_lower_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr = true;
-    }
-    const unsigned nblk_ = (unsigned)((N + nb - 1) / nb);
-    const size_t sm = ((size_t)nb * nb + 8 * (size_t)nb) * sizeof(float);
-    inv_lower_blocks_kernel<<<nblk_, 256, sm, s>>>(N, nb, A, Ar, lda, Linv);
-    check("inv_lower_blocks");
-}
-
-// ---------------------------------------------------------------------------
 // Diagonal block of the FP32 factorization: Cholesky of the n x n (n <= 128)
 // block A11 and the inverse of its factor, in one CTA of 512 threads, blocked
 // by 32 columns (4 block steps J):
@@ -954,68 +896,102 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
     check("potrf_inv");
 }
 
-// B_k <- op(Linv_k) B_k for the n x ncol block at B (ldb), op = transpose if
-// `trans`; also writes the TF32 head/remainder split of the result as K-major
-// rows (column j -> row j of H/L, kpad = nb) for the following tensor-core
-// update.  Linv_k is staged once per CTA in shared memory; each CTA then
-// handles four columns at a time, one thread per output row, each dot product
-// split over four independent partial sums.
-constexpr int AI_THREADS = 512, AI_COLS = AI_THREADS / 128;
+// B <- blockdiag(op(Linv_b)) B over all diagonal blocks at once, op =
+// transpose if `trans`: block b covers rows b*128 .. b*128 + n_b - 1 (n_b =
+// 128 but for the last block, n_last) of the N x ncol matrix B (ldb); Linv_b
+// are the column-major 128 x 128 inverses, zero outside n_b x n_b.  Grid
+// (column groups, blocks): each CTA stages op(Linv_b) once in shared memory
+// (column-major, sM[i + l*ldm]) and then takes 32 columns per pass; each
+// thread accumulates a 4 x 4 tile (rows 4*tr.., columns 4*tc..) from 128-bit
+// shared loads (one operand read per four products).
+constexpr int AB_THREADS = 256, AB_COLS = 32, AB_NB = 128, AB_LDM = AB_NB + 4;
+constexpr size_t AB_SMEM = (size_t)(AB_NB + AB_COLS) * AB_LDM * sizeof(float);
 
-__global__ void __launch_bounds__(AI_THREADS) apply_inv_split_kernel(int n, int nb, int64_t ncol,
-                                                                     const float* __restrict__ Li, int trans,
-                                                                     float* B, int64_t ldb, float* H, float* L) {
+__global__ void __launch_bounds__(AB_THREADS) apply_inv_blocks_kernel(int nblocks, int n_last, int64_t ncol,
+                                                                      const float* __restrict__ Li, int trans,
+                                                                      float* B, int64_t ldb) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    const int ldm = nb + 1;                        // padded rows: threads read different rows at the same l
-    float* sM = reinterpret_cast<float*>(smraw);   // nb x nb, sM[i*ldm + l] = op(Linv)[i][l]
-    float* sb = sM + nb * ldm;                     // AI_COLS x nb
-    for (int e = threadIdx.x; e < nb * nb; e += AI_THREADS) {
-        const int r = e % nb, c = e / nb;          // coalesced read of column-major Linv
-        const float v = Li[r + c * nb];
+    float* sM = reinterpret_cast<float*>(smraw);   // sM[i + l*AB_LDM] = op(Linv_b)[i][l]
+    float* sB = sM + AB_NB * AB_LDM;               // sB[c*AB_LDM + l] = B(b*128 + l, j0 + c)
+    const int blk = blockIdx.y;
+    const int n = blk == nblocks - 1 ? n_last : AB_NB;
+    const float* L = Li + (int64_t)blk * AB_NB * AB_NB;
+    float* Bb = B + (int64_t)blk * AB_NB;
+    for (int e = threadIdx.x; e < AB_NB * AB_NB; e += AB_THREADS) {
+        const int r = e % AB_NB, c = e / AB_NB;   // coalesced read of column-major Linv
+        const float v = L[r + c * AB_NB];
         if (trans)
-            sM[c * ldm + r] = v;
+            sM[c + r * AB_LDM] = v;
         else
-            sM[r * ldm + c] = v;
+            sM[r + c * AB_LDM] = v;
     }
-    const int q = threadIdx.x / 128, i = threadIdx.x % 128;
-    const float* row = sM + i * ldm;
-    float* b = sb + q * nb;
-    for (int64_t j0 = (int64_t)blockIdx.x * AI_COLS; j0 < ncol; j0 += (int64_t)gridDim.x * AI_COLS) {
-        const int64_t j = j0 + q;
-        __syncthreads();   // the staged block (first pass) / the previous columns' reads of b
-        if (j < ncol && i < nb) b[i] = i < n ? B[j * ldb + i] : 0.f;
+    const int tr = threadIdx.x % 32, tc = threadIdx.x / 32;   // tc is uniform in a warp: broadcast reads of sB
+    const int64_t npass = (ncol + AB_COLS - 1) / AB_COLS;
+    for (int64_t p = blockIdx.x; p < npass; p += gridDim.x) {
+        const int64_t j0 = p * AB_COLS;
+        __syncthreads();   // the staged block (first pass) / the previous pass's reads of sB
+        for (int e = threadIdx.x; e < AB_NB * AB_COLS; e += AB_THREADS) {
+            const int l = e % AB_NB, c = e / AB_NB;
+            sB[c * AB_LDM + l] = (l < n && j0 + c < ncol) ? Bb[l + (j0 + c) * ldb] : 0.f;
+        }
         __syncthreads();
-        if (j < ncol && i < nb) {
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-            for (int l = 0; l < nb; l += 4) {
-                a0 = fmaf(row[l], b[l], a0);
-                a1 = fmaf(row[l + 1], b[l + 1], a1);
-                a2 = fmaf(row[l + 2], b[l + 2], a2);
-                a3 = fmaf(row[l + 3], b[l + 3], a3);
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[i][c] = 0.f;
+#pragma unroll 2
+        for (int l = 0; l < AB_NB; l += 4) {
+            float4 a[4], bv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) a[u] = *reinterpret_cast<const float4*>(sM + 4 * tr + (l + u) * AB_LDM);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bv[c] = *reinterpret_cast<const float4*>(sB + (4 * tc + c) * AB_LDM + l);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float b4[4] = {bv[c].x, bv[c].y, bv[c].z, bv[c].w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    acc[0][c] = fmaf(a[u].x, b4[u], acc[0][c]);
+                    acc[1][c] = fmaf(a[u].y, b4[u], acc[1][c]);
+                    acc[2][c] = fmaf(a[u].z, b4[u], acc[2][c]);
+                    acc[3][c] = fmaf(a[u].w, b4[u], acc[3][c]);
+                }
             }
-            const float acc = (a0 + a1) + (a2 + a3);
-            const float h = __uint_as_float(__float_as_uint(acc) & 0xFFFFE000u);
-            H[j * nb + i] = (i < n) ? h : 0.f;
-            L[j * nb + i] = (i < n) ? acc - h : 0.f;
-            if (i < n) B[j * ldb + i] = acc;
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int64_t j = j0 + 4 * tc + c;
+            if (j >= ncol) continue;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (4 * tr + i < n) Bb[4 * tr + i + j * ldb] = acc[i][c];
         }
     }
 }
 
-void apply_inv_split(int n, int nb, int64_t ncol, const float* Li, bool trans, float* B, int64_t ldb, float* H,
-                     float* L, cudaStream_t s) {
-    if (ncol <= 0) return;
-    if (nb != 128) throw Error(OMG_ERR_INVALID, "apply_inv_split: block size must be 128");
+void apply_inv_blocks(int64_t nblocks, int nb, int n_last, int64_t ncol, const float* Li, bool trans, float* B,
+                      int64_t ldb, cudaStream_t s) {
+    if (nblocks <= 0 || ncol <= 0) return;
+    if (nb != AB_NB || n_last < 1 || n_last > nb || nblocks > 65535)
+        throw Error(OMG_ERR_INVALID, "apply_inv_blocks: unsupported block layout");
     ProfScope prof_("apply_inv", s);
     static bool attr = false;
+    static int n_sm = 0;
     if (!attr) {
-        cudaFuncSetAttribute(apply_inv_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(apply_inv_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)AB_SMEM);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (n_sm <= 0) n_sm = 1;
         attr = true;
     }
-    const size_t sm = ((size_t)nb * (nb + 1) + AI_COLS * (size_t)nb) * sizeof(float);
-    const unsigned grid = (unsigned)std::min<int64_t>((ncol + AI_COLS - 1) / AI_COLS, 1024);
-    apply_inv_split_kernel<<<grid, AI_THREADS, sm, s>>>(n, nb, ncol, Li, trans ? 1 : 0, B, ldb, H, L);
-    check("apply_inv_split");
+    // about two CTAs per SM in all: fewer passes per CTA than stagings of Linv_b
+    const int64_t npass = (ncol + AB_COLS - 1) / AB_COLS;
+    const int64_t groups = std::max<int64_t>(1, std::min<int64_t>(npass, (2 * n_sm + nblocks - 1) / nblocks));
+    dim3 grid((unsigned)groups, (unsigned)nblocks);
+    apply_inv_blocks_kernel<<<grid, AB_THREADS, AB_SMEM, s>>>((int)nblocks, n_last, ncol, Li, trans ? 1 : 0, B, ldb);
+    check("apply_inv_blocks");
 }
 
 }  // namespace omg

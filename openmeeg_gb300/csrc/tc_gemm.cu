@@ -67,6 +67,23 @@ __device__ __forceinline__ void tile_of(int64_t t, int tiles_m, int lower, int& 
     }
 }
 
+// Optional epilogue outputs besides C (null pointers: off).
+//  Sh/Sl  K-major TF32 head / remainder copy of C's rows >= s_row0: row i of C
+//         becomes row i - s_row0 (row stride s_kpad), zero past column N.
+//  Cr     C receives the TF32 head of each value and Cr (same layout) the
+//         remainder (beta must be 0).
+//  Xh/Xl  K-major head / remainder copy of the 128-row band of C starting at
+//         row x_row0 (a multiple of 128), transposed: column j of the band
+//         becomes row j (stride 128), rows past M written as zero.
+struct EpiArgs {
+    float* Sh;
+    float* Sl;
+    float* Cr;
+    float* Xh;
+    float* Xl;
+    int s_row0, s_kpad, x_row0;
+};
+
 // K may come in two segments with their own operand maps (the second set is
 // used for the chunks past K0 when K > K0): an update by two panels at once.
 __global__ void __launch_bounds__(THREADS, 1)
@@ -75,7 +92,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                        const __grid_constant__ CUtensorMap tAh2, const __grid_constant__ CUtensorMap tAl2,
                        const __grid_constant__ CUtensorMap tBh2, const __grid_constant__ CUtensorMap tBl2, int M,
                        int N, int K, int K0, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod,
-                       int64_t ntiles, int* err, float* Sh, float* Sl, int s_row0, int s_kpad) {
+                       int64_t ntiles, int* err, const EpiArgs ep) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -87,7 +104,17 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int tiles_m = (M + BM - 1) / BM;
     const int nk0 = (K0 + BK - 1) / BK;                       // chunks of the first segment
     const int nk = nk0 + (K - K0 + BK - 1) / BK;
+    // Programmatic dependent launch: the next kernel in the stream may be scheduled now (it waits for this
+    // grid's completion before touching memory); no-op when not launched with that attribute.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (threadIdx.x == 0) {
+        // descriptor fetches overlap the setup below
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tAh)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tBh)) : "memory");
+        if (nprod == 3) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tAl)) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tBl)) : "memory");
+        }
         for (int s = 0; s < STAGES; ++s) {
             dev::mbar_init(&full_bar[s], 1);
             dev::mbar_init(&empty_bar[s], 1);
@@ -111,6 +138,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     fence_before();
     __syncthreads();
     fence_after();
+    // the previous kernel's writes (operands, C) are complete and visible past this point
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t tmem = tmem_holder;
     const uint32_t bytes_per_stage = (nprod == 3 ? 4u : 2u) * TILE_BYTES;
 
@@ -208,26 +237,59 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             fence_after();
             // optional K-major TF32 head / remainder copy of rows >= s_row0 (row stride s_kpad, zero past N)
-            float* const sh = (Sh && row >= s_row0 && row < M) ? Sh + (int64_t)(row - s_row0) * s_kpad + n0 : nullptr;
+            float* const sh =
+                (ep.Sh && row >= ep.s_row0 && row < M) ? ep.Sh + (int64_t)(row - ep.s_row0) * ep.s_kpad + n0 : nullptr;
+            float* const crp = ep.Cr ? ep.Cr + (cp - C) : nullptr;
+            // optional transposed copy of the band [x_row0, x_row0 + 128): column j -> row j
+            const bool xband = ep.Xh && row >= ep.x_row0 && row < ep.x_row0 + BM;
+            const int xmax = xband ? min(64, N - n0) : 0;
+            float* const xh = xband ? ep.Xh + ((int64_t)n0 * BM + (row - ep.x_row0)) : nullptr;
+            float* const xl = xband ? ep.Xl + (xh - ep.Xh) : nullptr;
+            // 16 columns per step in a loop that is not unrolled: the tile's instructions are fetched once
+            // (a fully unrolled 64-column epilogue spent most of a tile's time on instruction fetch); the
+            // prefetched C values move down by 16 registers per step, so cv[0..15] are the step's columns
+            const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64);
+#pragma unroll 1
+            for (int jb = 0; jb < 64; jb += 16) {
+                uint32_t r[16];
+                tmem_ld16(tb + (uint32_t)jb, r);
+                float v[16];
 #pragma unroll
-            for (int chunk = 0; chunk < 2; ++chunk) {
-                uint32_t r[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64 + chunk * 32), r);
-                float v[32];
+                for (int j = 0; j < 16; ++j) v[j] = fmaf(alpha, __uint_as_float(r[j]), beta * cv[j]);
+                float* const cpj = cp + jb * ld32;
+                if (crp) {
+                    float* const crj = crp + jb * ld32;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    v[j] = fmaf(alpha, __uint_as_float(r[j]), beta * cv[chunk * 32 + j]);
-                    if (chunk * 32 + j < jmax) __stcg(cp + (chunk * 32 + j) * ld32, v[j]);
+                    for (int j = 0; j < 16; ++j)
+                        if (jb + j < jmax) {
+                            const float h = __uint_as_float(__float_as_uint(v[j]) & 0xFFFFE000u);
+                            __stcg(cpj + j * ld32, h);
+                            __stcg(crj + j * ld32, v[j] - h);
+                        }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (jb + j < jmax) __stcg(cpj + j * ld32, v[j]);
                 }
-                if (sh && n0 + chunk * 32 < s_kpad) {
-                    float* const shc = sh + chunk * 32;
-                    float* const slc = Sl + (shc - Sh);
+                if (jb < xmax) {
 #pragma unroll
-                    for (int j4 = 0; j4 < 8; ++j4) {
+                    for (int j = 0; j < 16; ++j)
+                        if (jb + j < xmax) {
+                            const float x = row < M ? v[j] : 0.f;
+                            const float h = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+                            xh[(int64_t)(jb + j) * BM] = h;
+                            xl[(int64_t)(jb + j) * BM] = x - h;
+                        }
+                }
+                if (sh && n0 + jb < ep.s_kpad) {
+                    float* const shc = sh + jb;
+                    float* const slc = ep.Sl + (shc - ep.Sh);
+#pragma unroll
+                    for (int j4 = 0; j4 < 4; ++j4) {
                         float h[4], l[4];
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
-                            const float x = (chunk * 32 + 4 * j4 + u < jmax) ? v[4 * j4 + u] : 0.f;
+                            const float x = (jb + 4 * j4 + u < jmax) ? v[4 * j4 + u] : 0.f;
                             h[u] = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
                             l[u] = x - h[u];
                         }
@@ -235,6 +297,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                         reinterpret_cast<float4*>(slc)[j4] = make_float4(l[0], l[1], l[2], l[3]);
                     }
                 }
+#pragma unroll
+                for (int j = 0; j < 48; ++j) cv[j] = cv[j + 16];
             }
             fence_before();
             __syncwarp();
@@ -269,18 +333,51 @@ static inline void check_tc(const char* what) {
     count_launch();
 }
 
+// Launch of the kernel; with `pdl` (programmatic dependent launch) it may be
+// scheduled while the previous kernel in the stream finishes: the kernel
+// waits for that kernel's completion before it touches memory.
+template <typename... Args>
+static void launch_gemm(bool pdl, unsigned grid, cudaStream_t s, Args... args) {
+    if (!pdl) {
+        tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(tc::THREADS);
+    cfg.dynamicSmemBytes = tc::SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, tc::gemm_tf32x3_kernel, args...);
+}
+
+// Checks the optional epilogue outputs against the shape and packs them.
+static tc::EpiArgs epi_args(int64_t M, float beta, bool lower, int64_t N, float* Sh, float* Sl, int64_t s_row0,
+                            int s_kpad, float* Cr, float* Xh, float* Xl, int64_t x_row0) {
+    if (Sh) {   // the copy covers whole 128-column tiles: one tile column, 16-byte aligned rows
+        if (!Sl || lower || N > tc::BN || s_kpad != tc::BN || s_row0 < 0 ||
+            (reinterpret_cast<uintptr_t>(Sh) % 16) || (reinterpret_cast<uintptr_t>(Sl) % 16))
+            throw Error(OMG_ERR_INVALID, "tensor-core GEMM split copy: unsupported shape");
+    }
+    if (Cr && beta != 0.f) throw Error(OMG_ERR_INVALID, "tensor-core GEMM head/remainder output needs beta = 0");
+    if (Xh && (!Xl || lower || x_row0 < 0 || x_row0 % tc::BM || (M > 0 && x_row0 >= M)))
+        throw Error(OMG_ERR_INVALID, "tensor-core GEMM band copy: unsupported shape");
+    return tc::EpiArgs{Sh, Sl, Cr, Xh, Xl, (int)s_row0, s_kpad, (int)x_row0};
+}
+
 // C(M x N, ldc) = beta*C + alpha * A B^T.  A: M x K (K-major, row stride lda),
 // B: N x K (K-major, row stride ldb); *h are TF32 heads, *l the remainders
 // (may be null when nprod == 1).  `k0` offsets the K coordinate of A and B.
 void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, const float* Al, int64_t lda,
                  int64_t a_kext, int64_t a_k0, const float* Bh, const float* Bl, int64_t ldb, int64_t b_kext,
                  int64_t b_k0, float beta, float* C, int64_t ldc, bool lower, int* err, cudaStream_t s,
-                 const char* prof_name, int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad) {
-    if (Sh) {   // the copy covers whole 128-column tiles: one tile column, 16-byte aligned rows
-        if (!Sl || lower || N > tc::BN || s_kpad != tc::BN || s_row0 < 0 ||
-            (reinterpret_cast<uintptr_t>(Sh) % 16) || (reinterpret_cast<uintptr_t>(Sl) % 16))
-            throw Error(OMG_ERR_INVALID, "tensor-core GEMM split copy: unsupported shape");
-    }
+                 const char* prof_name, int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad, float* Cr,
+                 float* Xh, float* Xl, int64_t x_row0, bool pdl) {
+    const tc::EpiArgs ep = epi_args(M, beta, lower, N, Sh, Sl, s_row0, s_kpad, Cr, Xh, Xl, x_row0);
     if (M <= 0 || N <= 0) return;
     if (K <= 0) throw Error(OMG_ERR_INVALID, "empty K");
     ProfScope prof_(prof_name, s);
@@ -307,10 +404,8 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     if (tiles_m > (1 << 30) / 2) throw Error(OMG_ERR_UNSUPPORTED, "tensor-core GEMM too tall");
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
-    tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mAh, mAl, mBh, mBl, mAh, mAl, mBh, mBl, (int)M,
-                                                                     (int)N, (int)K, (int)K, alpha, beta, C, ldc,
-                                                                     lower ? 1 : 0, nprod, ntiles, err, Sh, Sl,
-                                                                     (int)s_row0, s_kpad);
+    launch_gemm(pdl, grid, s, mAh, mAl, mBh, mBl, mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, (int)K, alpha, beta, C,
+                ldc, lower ? 1 : 0, nprod, ntiles, err, ep);
     check_tc("gemm_tf32x3");
 }
 
@@ -321,14 +416,10 @@ void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float
                       const float* B1h, const float* B1l, int64_t ldb1, int64_t K2, const float* A2h,
                       const float* A2l, int64_t lda2, const float* B2h, const float* B2l, int64_t ldb2, float beta,
                       float* C, int64_t ldc, bool lower, int* err, cudaStream_t s, const char* prof_name,
-                      int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad) {
+                      int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad, bool pdl) {
+    const tc::EpiArgs ep = epi_args(M, beta, lower, N, Sh, Sl, s_row0, s_kpad, nullptr, nullptr, nullptr, 0);
     if (M <= 0 || N <= 0) return;
     if (K1 <= 0 || K2 <= 0 || (K1 % tc::BK)) throw Error(OMG_ERR_INVALID, "tensor-core GEMM segments");
-    if (Sh) {
-        if (!Sl || lower || N > tc::BN || s_kpad != tc::BN || s_row0 < 0 ||
-            (reinterpret_cast<uintptr_t>(Sh) % 16) || (reinterpret_cast<uintptr_t>(Sl) % 16))
-            throw Error(OMG_ERR_INVALID, "tensor-core GEMM split copy: unsupported shape");
-    }
     ProfScope prof_(prof_name, s);
     const CUtensorMap m1h = tc::make_map(A1h, M, K1, lda1), m1l = tc::make_map(A1l, M, K1, lda1);
     const CUtensorMap n1h = tc::make_map(B1h, N, K1, ldb1), n1l = tc::make_map(B1l, N, K1, ldb1);
@@ -349,10 +440,8 @@ void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float
     const int64_t tiles_m = (M + tc::BM - 1) / tc::BM, tiles_n = (N + tc::BN - 1) / tc::BN;
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
-    tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(m1h, m1l, n1h, n1l, m2h, m2l, n2h, n2l, (int)M,
-                                                                     (int)N, (int)(K1 + K2), (int)K1, alpha, beta, C,
-                                                                     ldc, lower ? 1 : 0, 3, ntiles, err, Sh, Sl,
-                                                                     (int)s_row0, s_kpad);
+    launch_gemm(pdl, grid, s, m1h, m1l, n1h, n1l, m2h, m2l, n2h, n2l, (int)M, (int)N, (int)(K1 + K2), (int)K1, alpha,
+                beta, C, ldc, lower ? 1 : 0, 3, ntiles, err, ep);
     check_tc("gemm_tf32x3");
 }
 
@@ -404,43 +493,23 @@ void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld,
 // (ncol x kpad) heads/remainders.
 __global__ void split_cols_kernel(int nk, int64_t ncol, int kpad, const float* __restrict__ X, int64_t ldx, float* H,
                                   float* L) {
-    const int64_t j = blockIdx.y;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kpad; k += gridDim.x * blockDim.x) {
-        const float v = k < nk ? X[k + j * ldx] : 0.f;
-        float h, l;
-        split_tf32(v, h, l);
-        H[j * kpad + k] = h;
-        L[j * kpad + k] = l;
+    for (int64_t j = blockIdx.y; j < ncol; j += gridDim.y) {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < kpad; k += gridDim.x * blockDim.x) {
+            const float v = k < nk ? X[k + j * ldx] : 0.f;
+            float h, l;
+            split_tf32(v, h, l);
+            H[j * kpad + k] = h;
+            L[j * kpad + k] = l;
+        }
     }
 }
 
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s) {
     if (ncol <= 0) return;
     ProfScope prof_("split_cols", s);
-    dim3 grid((unsigned)((kpad + 127) / 128), (unsigned)ncol);
+    dim3 grid((unsigned)((kpad + 127) / 128), (unsigned)std::min<int64_t>(ncol, 65535));
     split_cols_kernel<<<grid, 128, 0, s>>>(nk, ncol, kpad, X, ldx, H, L);
     check_tc("split_cols");
-}
-
-// In place on the lower triangle of a column-major n x n matrix A: A <- head,
-// R <- remainder.
-__global__ void split_lower_inplace_kernel(int64_t n, float* A, int64_t lda, float* R) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    for (int64_t j = blockIdx.y; j <= i; j += gridDim.y) {
-        float h, l;
-        split_tf32(A[i + j * lda], h, l);
-        A[i + j * lda] = h;
-        R[i + j * lda] = l;
-    }
-}
-
-void split_lower_inplace(int64_t n, float* A, int64_t lda, float* R, cudaStream_t s) {
-    if (n <= 0) return;
-    ProfScope prof_("split_lower", s);
-    dim3 grid((unsigned)((n + 255) / 256), (unsigned)std::min<int64_t>(n, 32768));
-    split_lower_inplace_kernel<<<grid, 256, 0, s>>>(n, A, lda, R);
-    check_tc("split_lower");
 }
 
 }  // namespace omg
@@ -452,7 +521,7 @@ extern "C" int omg_internal_gemm_tf32x3(int64_t M, int64_t N, int64_t K, float a
                                         float beta, float* C, int64_t ldc, int lower, int* err) {
     try {
         omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, lower != 0, err, 0,
-                         "gemm_tf32x3", 0, nullptr, nullptr, 0, 0);
+                         "gemm_tf32x3", 0, nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr, 0, false);
         cudaError_t e = cudaDeviceSynchronize();
         return e == cudaSuccess ? 0 : -2;
     } catch (const omg::Error& e) {
@@ -468,7 +537,24 @@ extern "C" int omg_internal_gemm_tf32x3_split(int64_t M, int64_t N, int64_t K, f
                                               int64_t s_row0, int* err) {
     try {
         omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, false, err, 0,
-                         "gemm_tf32x3", 0, Sh, Sl, s_row0, 128);
+                         "gemm_tf32x3", 0, Sh, Sl, s_row0, 128, nullptr, nullptr, nullptr, 0, false);
+        cudaError_t e = cudaDeviceSynchronize();
+        return e == cudaSuccess ? 0 : -2;
+    } catch (const omg::Error& e) {
+        return e.code;
+    }
+}
+
+// Test hook: the same with C written as TF32 heads and Cr as the remainders
+// (when Cr is not null, beta = 0) and/or the transposed head / remainder copy
+// of the 128-row band of C at x_row0 (Xh/Xl: N rows of 128, zero past M).
+extern "C" int omg_internal_gemm_tf32x3_epi(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
+                                            const float* Al, int64_t lda, const float* Bh, const float* Bl,
+                                            int64_t ldb, float beta, float* C, int64_t ldc, float* Cr, float* Xh,
+                                            float* Xl, int64_t x_row0, int* err) {
+    try {
+        omg::gemm_tf32x3(M, N, K, alpha, Ah, Al, lda, K, 0, Bh, Bl, ldb, K, 0, beta, C, ldc, false, err, 0,
+                         "gemm_tf32x3", 0, nullptr, nullptr, 0, 0, Cr, Xh, Xl, x_row0, false);
         cudaError_t e = cudaDeviceSynchronize();
         return e == cudaSuccess ? 0 : -2;
     } catch (const omg::Error& e) {

@@ -98,6 +98,69 @@ def test_tc_gemm_epilogue_split_copy(cuda, M, N, K, row0):
     assert float(Sh[:, N:].abs().max() if N < 128 else 0.0) == 0.0 and float(Sl[:, N:].abs().max() if N < 128 else 0.0) == 0.0
 
 
+def _epi_hook():
+    return _lib_hook("omg_internal_gemm_tf32x3_epi",
+                     [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p,
+                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                      ctypes.c_float, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                      ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p])
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 128), (700, 300, 96), (17000, 215, 128)])
+def test_tc_gemm_epilogue_head_remainder(cuda, M, N, K):
+    """C written as TF32 heads with the remainders in Cr: Ch + Cr is the
+    3xTF32 product, and the pair is the exact split of that sum."""
+    import torch
+    f = _epi_hook()
+    g = torch.Generator(device="cuda").manual_seed(N)
+    A = torch.randn(M, K, device="cuda", generator=g)
+    B = torch.randn(N, K, device="cuda", generator=g)
+    Ah, Al = _split(A)
+    Bh, Bl = _split(B)
+    C = torch.full((N, M), 3.0, device="cuda")                   # column-major M x N, overwritten (beta = 0)
+    Cr = torch.full((N, M), 3.0, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+    assert f(M, N, K, 1.0, p(Ah), p(Al), K, p(Bh), p(Bl), K, 0.0, p(C), M, p(Cr), None, None, 0, p(err)) == 0
+    assert int(err.item()) == 0
+    v = C + Cr
+    h, l = _split(v.contiguous())
+    assert torch.equal(h, C) and torch.equal(l, Cr)
+    ref = A.double() @ B.double().T
+    assert float(torch.linalg.norm(v.double().T - ref) / torch.linalg.norm(ref)) < 1e-5
+    # beta != 0 with a remainder output is refused
+    assert f(M, N, K, 1.0, p(Ah), p(Al), K, p(Bh), p(Bl), K, 1.0, p(C), M, p(Cr), None, None, 0, p(err)) == -1
+
+
+@pytest.mark.parametrize("M,N,K,row0", [(1000, 215, 128, 0), (1000, 215, 128, 384), (90, 300, 64, 0),
+                                        (4096, 64, 128, 3968)])
+def test_tc_gemm_epilogue_band_copy(cuda, M, N, K, row0):
+    """The transposed band copy: row j of Xh/Xl (stride 128) is the TF32 split
+    of column j of C's rows row0 .. row0+127, zero at rows past M."""
+    import torch
+    f = _epi_hook()
+    g = torch.Generator(device="cuda").manual_seed(M + row0)
+    A = torch.randn(M, K, device="cuda", generator=g)
+    B = torch.randn(N, K, device="cuda", generator=g)
+    Ah, Al = _split(A)
+    Bh, Bl = _split(B)
+    C = torch.randn(N, M, device="cuda", generator=g)            # column-major M x N
+    Xh = torch.full((N, 128), 7.0, device="cuda")                # garbage that must be overwritten
+    Xl = torch.full((N, 128), 7.0, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+    assert f(M, N, K, -1.0, p(Ah), p(Al), K, p(Bh), p(Bl), K, 1.0, p(C), M, None, p(Xh), p(Xl), row0, p(err)) == 0
+    assert int(err.item()) == 0
+    rows = min(128, M - row0)
+    band = C[:, row0:row0 + rows].contiguous()                   # N x rows: column j of the band as row j
+    h, l = _split(band)
+    assert torch.equal(Xh[:, :rows], h) and torch.equal(Xl[:, :rows], l)
+    if rows < 128:
+        assert float(Xh[:, rows:].abs().max()) == 0.0 and float(Xl[:, rows:].abs().max()) == 0.0
+    # a band that does not start on a tile row is refused
+    assert f(M, N, K, -1.0, p(Ah), p(Al), K, p(Bh), p(Bl), K, 1.0, p(C), M, None, p(Xh), p(Xl), 8, p(err)) == -1
+
+
 @pytest.mark.parametrize("M,N,K,lower", [(5000, 1000, 64, False), (4100, 4100, 128, True)])
 def test_tc_gemm_many_tiles_per_cta(cuda, M, N, K, lower):
     # more tiles than SMs: every CTA walks several tiles through both TMEM accumulators
