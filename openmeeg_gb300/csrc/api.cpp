@@ -851,10 +851,10 @@ static void mixed_residual(omg_solver sv, const double* x, int64_t nrhs, const d
 }
 
 // Mixed precision: x = HM^-1 b by FP32 solves refined against the FP64 HM.
-// x0 = A32^-1 b; then r = b - A x (FP64-accurate, double-float residual),
-// d = A32^-1 r, x += d, until every column's correction is below refine_tol
-// relative to the column (the error of the final x is then about the
-// contraction factor times that, far below it).
+// x0 = A32^-1 b; then r = b - A x (FP64-accurate residual), d = A32^-1 r,
+// x += d, until the predicted error of x (the largest relative column
+// correction times the contraction factor of the iteration) is below
+// refine_tol.
 static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
@@ -894,7 +894,15 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
             if (hx[j] > 0) est = std::max(est, hd[j] / hx[j]);
             if (it > 0 && hb[j] > 0) last_res = std::max(last_res, hr[j] / hb[j]);
         }
-        if (it > 0 && !(est > sv->refine_tol)) break;
+        // The error left in x after this correction is about est times the contraction factor of the
+        // refinement, estimated as est / (the previous correction) (est_0 = 1: the first solve starts from 0).
+        if (it > 0) {
+            const double rho = std::min(1.0, est / (it == 1 ? 1.0 : prev_est));
+            if (!(est * rho > sv->refine_tol)) {
+                est *= rho;   // reported: the predicted relative error of x
+                break;
+            }
+        }
         if (it > 1 && !(est < prev_est)) break;   // stagnation: report below
         prev_est = est;
     }
@@ -907,8 +915,9 @@ static void solve_mixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
 }
 
 // Mixed solve with a fixed number of residual steps and no host read-back
-// (stream-capture safe): the last correction's max relative column size is
-// left in d_est for the caller to test after the stream completes.
+// (stream-capture safe): the max relative column size of the last correction
+// and of the one before it are left in d_est[0] and d_est[1] for the caller to
+// test after the stream completes (predicted error d_est[0] * d_est[0] / d_est[1]).
 void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int residual_steps, double* d_est) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N;
@@ -928,10 +937,13 @@ void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int 
         scale_to_f32(N, nrhs, r, N, B32.as<float>(), N, rn.as<double>(), sc.as<double>(), s);
         solve_ldlt_tc(sv, B32.as<float>(), N, nrhs);
         axpy_f32(N, nrhs, B32.as<float>(), N, x, N, sc.as<double>(), s);
+        if (it + 1 >= residual_steps) {   // the last two corrections (the first, from x = 0, has size 1)
+            col_norms_f32(N, nrhs, B32.as<float>(), N, sc.as<double>(), dn.as<double>(), s);
+            col_norms(N, nrhs, x, N, xn.as<double>(), s);
+            ratio_max(nrhs, dn.as<double>(), xn.as<double>(), d_est + (it == residual_steps ? 0 : 1), s);
+        }
     }
-    col_norms_f32(N, nrhs, B32.as<float>(), N, sc.as<double>(), dn.as<double>(), s);
-    col_norms(N, nrhs, x, N, xn.as<double>(), s);
-    ratio_max(nrhs, dn.as<double>(), xn.as<double>(), d_est, s);
+    if (residual_steps == 0) OMG_CUDA(cudaMemcpyAsync(d_est + 1, d_est, sizeof(double), cudaMemcpyDeviceToDevice, s));
     copy_convert<double, double>(N, nrhs, x, N, B, ldb, false, 1.0, s);
 }
 

@@ -54,7 +54,7 @@ struct BatchModel {
     int64_t nd = 0, ne = 0, nm = 0;
     DevBuf dip, el, sq;          // inputs (persistent, row-major)
     DevBuf geeg, gmeg;           // outputs (column-major ne x nd, nm x nd)
-    DevBuf est;                  // mixed: final relative correction of the refinement
+    DevBuf est;                  // mixed: last and previous relative corrections of the refinement
     NearPlan near;
     int refine_steps = 0;
     int tc_residual = 1;         // residual kind chosen by the planning run
@@ -307,11 +307,12 @@ void check_run(omg_batch b) {
     }
     if (b->precision == OMG_PREC_MIXED)
         for (size_t q = 0; q < b->models.size(); ++q) {
-            double e = 0.0;
-            OMG_CUDA(cudaMemcpy(&e, b->models[q]->est.p, sizeof(double), cudaMemcpyDeviceToHost));
+            double c[2] = {0.0, 1.0};
+            OMG_CUDA(cudaMemcpy(c, b->models[q]->est.p, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+            const double e = c[0] * std::min(1.0, c[0] / c[1]);   // predicted error, as in the single-model solve
             if (!(e <= b->refine_tol))
                 throw Error(OMG_ERR_NOT_CONVERGED, "batched forward: model " + std::to_string(q) +
-                                                       " ended its refinement at relative correction " +
+                                                       " ended its refinement at predicted relative error " +
                                                        std::to_string(e));
         }
 }
@@ -466,7 +467,7 @@ int omg_batch_create(omg_context ctx, int32_t n_models, const omg_batch_model* m
             m->sq = DevBuf((size_t)std::max<int64_t>(1, m->nm) * 48, s, true);
             m->geeg = DevBuf((size_t)std::max<int64_t>(1, m->ne * m->nd) * 8, s, true);
             m->gmeg = DevBuf((size_t)std::max<int64_t>(1, m->nm * m->nd) * 8, s, true);
-            m->est = DevBuf(sizeof(double), s, true);
+            m->est = DevBuf(2 * sizeof(double), s, true);
             if (m->nd) OMG_CUDA(cudaMemcpyAsync(m->dip.p, in.dipoles, m->nd * 48, cudaMemcpyHostToDevice, s));
             if (m->ne) OMG_CUDA(cudaMemcpyAsync(m->el.p, in.electrodes, m->ne * 24, cudaMemcpyHostToDevice, s));
             if (m->nm) OMG_CUDA(cudaMemcpyAsync(m->sq.p, in.squids, m->nm * 48, cudaMemcpyHostToDevice, s));

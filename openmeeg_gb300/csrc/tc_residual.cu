@@ -261,16 +261,58 @@ __global__ void __launch_bounds__(THREADS, 1)
 // balanced base-2^beta digits (first |d| <= 2^beta, others <= 2^(beta-1)), written as bf16
 // row c of digit plane d: out[(d * rows_per_plane + c) * ldo + j], zero for
 // n <= j < ldo.  Columns c >= ncol (up to rows_per_plane) are zero.
-__global__ void digits_kernel(const double* __restrict__ M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta,
-                              int64_t rows_per_plane, int64_t ldo, __nv_bfloat16* out, int* ex,
-                              const __grid_constant__ RowRanges rr) {
-    __shared__ double red[256];
+// x 2^k rounded to the nearest integer (ties to even), exactly, by integer
+// arithmetic on the bits of x (|x 2^k| < 2^62): the same value as
+// __double2ll_rn(x * 2^k) without the FP64 pipe.
+__device__ __forceinline__ long long scaled_rn(double x, int k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7FF);
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (E ? (1ull << 52) : 0ull);
+    const int sh = (E ? E : 1) - 1075 + k;   // |x 2^k| = m 2^sh
+    unsigned long long q;
+    if (sh >= 0) {
+        q = m << sh;
+    } else if (sh < -63) {
+        q = 0;   // below 2^-11
+    } else {
+        const int r = -sh;
+        const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
+        q = m >> r;
+        if (rem > half || (rem == half && (q & 1))) ++q;
+    }
+    return (b >> 63) ? -(long long)q : (long long)q;
+}
+
+// bf16 bits of a small integer (|r| < 2^8, exact in bf16): 1.5 * 2^23 + r
+// has r in its low mantissa bits, the subtraction leaves float(r) exactly.
+__device__ __forceinline__ unsigned short small_int_bf16(long long r) {
+    const float f = __int_as_float(0x4B400000 + (int)r) - 12582912.0f;
+    return (unsigned short)(__float_as_uint(f) >> 16);
+}
+
+// Digits of the columns of a column-major FP64 matrix: column c (rows j < n)
+// is scaled by 2^-e_c (e_c: exponent of its largest magnitude, frexp
+// convention), rounded to a multiple of 2^-(nd beta) and cut into `nd`
+// balanced base-2^beta digits (first |d| <= 2^beta, others <= 2^(beta-1)), written as bf16
+// row c of digit plane d: out[(d * rows_per_plane + c) * ldo + j], zero for
+// n <= j < ldo.  Columns c >= ncol (up to rows_per_plane) are zero.  One CTA
+// per column, four consecutive rows per thread (8-byte stores per plane);
+// integer arithmetic only (the largest magnitude by its bit pattern, the
+// scaling and rounding on the significand).
+constexpr int DG_THREADS = 256;
+
+__global__ void __launch_bounds__(DG_THREADS) digits_kernel(const double* __restrict__ M, int64_t n, int64_t ncol,
+                                                            int64_t ldm, int nd, int beta, int64_t rows_per_plane,
+                                                            int64_t ldo, __nv_bfloat16* out, int* ex,
+                                                            const __grid_constant__ RowRanges rr) {
+    __shared__ unsigned long long red[DG_THREADS / 32];
     __shared__ int s_e;
     const int64_t c = blockIdx.x;
+    uint2* const o2 = reinterpret_cast<uint2*>(out);   // 4 bf16 per store (ldo is a multiple of 64)
     if (c >= ncol) {
         for (int d = 0; d < nd; ++d)
-            for (int64_t j = threadIdx.x; j < ldo; j += blockDim.x)
-                out[((int64_t)d * rows_per_plane + c) * ldo + j] = __float2bfloat16_rn(0.f);
+            for (int64_t j = 4 * threadIdx.x; j < ldo; j += 4 * DG_THREADS)
+                o2[(((int64_t)d * rows_per_plane + c) * ldo + j) / 4] = make_uint2(0u, 0u);
         return;
     }
     const double* col = M + c * ldm;
@@ -283,34 +325,43 @@ __global__ void digits_kernel(const double* __restrict__ M, int64_t n, int64_t n
         }
         return 0.0;
     };
-    double m = 0.0;
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, fabs(at(j)));
-    red[threadIdx.x] = m;
+    unsigned long long mb = 0;   // |x| bits: ordered like |x| for finite x
+    for (int64_t j = threadIdx.x; j < n; j += DG_THREADS)
+        mb = max(mb, (unsigned long long)__double_as_longlong(at(j)) & 0x7FFFFFFFFFFFFFFFull);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    if (threadIdx.x % 32 == 0) red[threadIdx.x / 32] = mb;
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
-        __syncthreads();
-    }
     if (threadIdx.x == 0) {
+        unsigned long long m = red[0];
+        for (int w = 1; w < DG_THREADS / 32; ++w) m = max(m, red[w]);
         int e = 0;
-        frexp(red[0], &e);   // max = f 2^e, f in [0.5, 1): every |entry| 2^-e < 1
+        frexp(__longlong_as_double((long long)m), &e);   // max = f 2^e, f in [0.5, 1): every |entry| 2^-e < 1
         s_e = e;
         ex[c] = e;
     }
     __syncthreads();
-    const int e = s_e;
+    const int k = nd * beta - s_e;
     // one rounding to the digit grid 2^-(nd beta), then balanced base-2^beta digits
     // by integer arithmetic (|Y| <= 2^(nd beta) <= 2^62)
-    const double grid = scalbn(1.0, nd * beta - e);
     const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
-    for (int64_t j = threadIdx.x; j < ldo; j += blockDim.x) {
-        long long Y = j < n ? __double2ll_rn(at(j) * grid) : 0;
-        for (int d = nd - 1; d >= 1; --d) {
-            const long long r = ((Y + half) & mask) - half;
-            out[((int64_t)d * rows_per_plane + c) * ldo + j] = __float2bfloat16_rn((float)r);
-            Y = (Y - r) >> beta;
+    for (int64_t j0 = 4 * threadIdx.x; j0 < ldo; j0 += 4 * DG_THREADS) {
+        long long Y[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) Y[u] = j0 + u < n ? scaled_rn(at(j0 + u), k) : 0;
+        for (int d = nd - 1; d >= 0; --d) {
+            unsigned int h[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                long long r = Y[u];
+                if (d > 0) {
+                    r = ((Y[u] + half) & mask) - half;
+                    Y[u] = (Y[u] - r) >> beta;
+                }
+                h[u] = small_int_bf16(r);
+            }
+            o2[(((int64_t)d * rows_per_plane + c) * ldo + j0) / 4] = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
         }
-        out[c * ldo + j] = __float2bfloat16_rn((float)Y);
     }
 }
 
@@ -328,7 +379,8 @@ void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int n
                     int64_t ldo, void* out, int* ex, cudaStream_t s,
                     const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr) {
     if (rows_per_plane <= 0) return;
-    if (nd < 1 || nd * beta > 62 || beta < 2 || beta > 8) throw Error(OMG_ERR_INVALID, "digits: bad digit layout");
+    if (nd < 1 || nd * beta > 62 || beta < 2 || beta > 8 || ldo % 4 || ldo < n)
+        throw Error(OMG_ERR_INVALID, "digits: bad digit layout");
     ProfScope prof_("digits", s);
     tcr::RowRanges rr{};
     if (ranges) {
@@ -341,8 +393,9 @@ void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int n
         }
         if (tot != n) throw Error(OMG_ERR_INVALID, "digits: row ranges do not add up");
     }
-    tcr::digits_kernel<<<(unsigned)rows_per_plane, 256, 0, s>>>(M, n, ncol, ldm, nd, beta, rows_per_plane, ldo,
-                                                                static_cast<__nv_bfloat16*>(out), ex, rr);
+    tcr::digits_kernel<<<(unsigned)rows_per_plane, tcr::DG_THREADS, 0, s>>>(M, n, ncol, ldm, nd, beta, rows_per_plane,
+                                                                           ldo, static_cast<__nv_bfloat16*>(out), ex,
+                                                                           rr);
     check_tcr("digits");
 }
 
@@ -454,4 +507,16 @@ extern "C" int omg_internal_residual_tc(int64_t n, int64_t k, const double* A, c
     cudaFree(rexp);
     cudaFree(cexp);
     return rc;
+}
+
+// Test hook: the digit planes of a column-major FP64 matrix (device
+// pointers): nd planes of rows_per_plane rows of ldo bf16, column exponents.
+extern "C" int omg_internal_digits(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta,
+                                   int64_t rows_per_plane, int64_t ldo, void* out, int* ex) {
+    try {
+        omg::digits_columns(M, n, ncol, ldm, nd, beta, rows_per_plane, ldo, out, ex, 0);
+        return cudaDeviceSynchronize() == cudaSuccess ? 0 : -2;
+    } catch (const omg::Error& e) {
+        return e.code;
+    }
 }

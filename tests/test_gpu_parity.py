@@ -120,9 +120,10 @@ def test_solver_matches_dense_solve(cuda, precision):
     if precision == "fp64":
         assert rel(X, ref) < 1e-11
     else:
-        # the mixed solver refines against its own (mixed-assembled) head matrix
+        # the mixed solver refines against its own (mixed-assembled) head matrix until the predicted
+        # error (last correction times the contraction factor) is below its tolerance, 1e-6
         Hm = api.HeadMat(geo, precision="mixed").cpu().numpy()
-        assert rel(X, np.linalg.solve(Hm, B)) < 1e-9
+        assert rel(X, np.linalg.solve(Hm, B)) < 1e-7
         assert rel(X, ref) < 1e-6
     # factoring a caller-provided HeadMat gives the same solution
     X2 = api.Solver(geo, precision="fp64", hm=HM).solve(B).cpu().numpy()

@@ -212,6 +212,67 @@ def test_tc_residual_is_fp64_accurate(cuda, n, k):
     assert elem < 1e-10 and norm < 5e-13, (elem, norm)
 
 
+def _digits_ref(col, nd, beta, ldo):
+    """Digit rows of one column as the kernel defines them: e = frexp exponent
+    of the largest magnitude, Y = x 2^(nd beta - e) rounded half to even, then
+    balanced base-2^beta digits from the lowest up (plane 0 takes the rest)."""
+    m = float(np.max(np.abs(col))) if col.size else 0.0
+    e = int(np.frexp(m)[1])
+    Y = [int(v) for v in np.rint(np.ldexp(col, nd * beta - e))]   # exact: power-of-two scaling, rint ties to even
+    Y += [0] * (ldo - len(Y))
+    planes = np.zeros((nd, ldo))
+    half, mask = 1 << (beta - 1), (1 << beta) - 1
+    for d in range(nd - 1, 0, -1):
+        r = [((y + half) & mask) - half for y in Y]
+        planes[d] = r
+        Y = [(y - ri) >> beta for y, ri in zip(Y, r)]
+    planes[0] = Y
+    return planes, e
+
+
+def test_digit_planes_bit_exact(cuda):
+    """The digit planes and column exponents of the integer-arithmetic digit
+    kernel equal the definition evaluated in exact integers: columns with zero,
+    signed zeros, subnormals, exact ties of the rounding and entries over 600
+    binary orders; n not a multiple of 4; padding rows and columns zero."""
+    import torch
+    f = _lib_hook("omg_internal_digits", [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
+                                          ctypes.c_void_p, ctypes.c_void_p])
+    rng = np.random.default_rng(5)
+    n, ncol, ldm, nd, beta = 301, 9, 305, 7, 7
+    ldo, rpp = 320, 12
+    M = np.zeros((ncol, ldm))
+    M[0, :n] = rng.standard_normal(n)
+    M[1, :n] = rng.standard_normal(n) * np.exp2(rng.integers(-300, 300, n).astype(float))
+    M[2, :n] = 0.0
+    M[2, 5] = -0.0
+    M[3, :n] = rng.standard_normal(n) * 1e-310                      # subnormal column
+    M[4, :n] = rng.standard_normal(n)
+    M[4, 0] = 1.0
+    M[4, 1:20] = (np.arange(19) + 0.5) * np.exp2(-48)                 # exact ties of the digit grid
+    M[4, 20:40] = -(np.arange(20) + 0.5) * np.exp2(-48)
+    M[5, :n] = -rng.random(n) * 3e8
+    M[6, :n] = rng.standard_normal(n)
+    M[6, 7] = -4.0                                                   # the largest magnitude negative
+    M[7, :n] = np.exp2(rng.integers(-60, 0, n).astype(float))
+    M[8, :n] = rng.standard_normal(n) * 1e-3
+    Md = torch.tensor(M, device="cuda", dtype=torch.float64)
+    out = torch.full((nd * rpp * ldo,), 7, dtype=torch.int16, device="cuda")   # garbage to be overwritten
+    ex = torch.zeros(rpp, dtype=torch.int32, device="cuda")
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert f(p(Md), n, ncol, ldm, nd, beta, rpp, ldo, p(out), p(ex)) == 0
+    got = out.view(torch.bfloat16).float().cpu().numpy().reshape(nd, rpp, ldo)
+    exg = ex.cpu().numpy()
+    for c in range(ncol):
+        ref, e = _digits_ref(M[c, :n], nd, beta, ldo)
+        assert exg[c] == e, (c, exg[c], e)
+        assert np.array_equal(got[:, c, :], ref), c
+    assert not got[:, ncol:, :].any()
+    # layouts the 8-byte stores cannot take are refused
+    assert f(p(Md), n, ncol, ldm, nd, beta, rpp, 302, p(out), p(ex)) == -1
+
+
 def test_diagonal_block_cholesky_and_inverse(cuda):
     """One CTA factors a 128 x 128 SPD block and inverts the factor:
     L L^T = A and L Linv = I at FP32 level; the K-major split of Linv adds
