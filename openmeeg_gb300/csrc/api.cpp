@@ -1979,6 +1979,12 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     solver_factor(sv.get(), std::move(hm));
     OMG_CUDA(cudaEventRecord(ev[3], s));
     solver_solve_internal(sv.get(), B.as<double>(), N, k);
+    // the factor is not needed past the solves: its memory (the FP32 factor, its copies and the digit planes,
+    // most of the device at the largest heads) is returned before the contraction allocates its digits
+    const int sv_steps = sv->last_steps;
+    const double sv_residual = sv->last_residual;
+    const bool sv_tc = sv->tc_residual;
+    sv.reset();
     // G = Y^T DSM over the rows where DSM can be nonzero (the source meshes' triangles and vertices)
     gain_contract(gain_row_ranges(geo, src_meshes), B.as<double>(), N, ne, nm, DSM.as<double>(), nd, geeg, gmeg, s,
                   precision, ctx->d_err);
@@ -1995,9 +2001,9 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
         st->t_factor_ms = c;
         st->t_solve_ms = d;
         st->t_total_ms = a + b + c + d;
-        st->refinement_steps = sv->last_steps;
-        st->residual_mode = precision == OMG_PREC_FP64 ? 0 : (sv->tc_residual ? 1 : 2);
-        st->final_residual = sv->last_residual;
+        st->refinement_steps = sv_steps;
+        st->residual_mode = precision == OMG_PREC_FP64 ? 0 : (sv_tc ? 1 : 2);
+        st->final_residual = sv_residual;
         st->device_bytes = g_dev_peak.load() - live0;
     }
     for (auto& e : ev) cudaEventDestroy(e);

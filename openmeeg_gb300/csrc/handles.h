@@ -59,10 +59,28 @@ struct DevBuf {
     DevBuf() = default;
     DevBuf(size_t nbytes, cudaStream_t st, bool keep = false) : s(st), persistent(keep) {
         if (!nbytes) return;
-        if (persistent)
-            OMG_CUDA(cudaMalloc(&p, nbytes));
-        else
-            OMG_CUDA(cudaMallocAsync(&p, nbytes, st));
+        cudaError_t e = persistent ? cudaMalloc(&p, nbytes) : cudaMallocAsync(&p, nbytes, st);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (e == cudaErrorMemoryAllocation && cudaStreamIsCapturing(st, &cs) == cudaSuccess &&
+            cs == cudaStreamCaptureStatusNone) {
+            // memory freed into the stream-ordered pool stays with the pool, in blocks that may not take
+            // this request: wait for the pending frees, hand the pool's unused memory back, try once more
+            cudaGetLastError();
+            cudaDeviceSynchronize();
+            int dev = 0;
+            cudaMemPool_t pool;
+            if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+                cudaMemPoolTrimTo(pool, 0);
+            e = persistent ? cudaMalloc(&p, nbytes) : cudaMallocAsync(&p, nbytes, st);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            size_t fr = 0, tot = 0;
+            cudaMemGetInfo(&fr, &tot);
+            throw ::omg::Error(e == cudaErrorMemoryAllocation ? OMG_ERR_NOMEM : OMG_ERR_CUDA,
+                               "device allocation of " + std::to_string(nbytes >> 20) + " MiB (" +
+                                   std::to_string(fr >> 20) + " MiB free): " + cudaGetErrorString(e));
+        }
         bytes = nbytes;
         note_alloc((int64_t)bytes);
     }
