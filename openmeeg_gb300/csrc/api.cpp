@@ -223,6 +223,13 @@ void check_integrator(const omg_integrator& it, bool allow_adaptive) {
 // ---------------------------------------------------------------------------
 // Geometry upload
 // ---------------------------------------------------------------------------
+
+// The block of meshes (m1, m2) of the matrix (lower storage at the triangles' positions) is contiguous along
+// mesh 2's index when mesh 2's triangles come after mesh 1's (a self block: along the first index).
+static bool s_along_b(const HostGeometry& h, int m1, int m2) {
+    return m1 != m2 && h.tidx[h.tbeg[m2]] > h.tidx[h.tbeg[m1]];
+}
+
 static void upload_geometry(omg_geometry g) {
     cudaStream_t s = g->ctx->stream;
     HostGeometry& h = g->h;
@@ -345,11 +352,13 @@ void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, doub
             Scoeff = p.cS;
         }
         if (Scoeff != 0.0) {   // set_N_block from the S already in the matrix
-            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / Scoeff, hm, ld, nullptr, hm, s);
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / Scoeff, hm, ld, nullptr, hm, s,
+                           false, s_along_b(h, m1, m2));
         } else {               // ... or from a temporary unit S block (current barriers)
             DevBuf tmp((size_t)(t1e - t1b) * (t2e - t2b) * 8, s);
             launch_S_block(d, t1b, t1e, t2b, t2e, same, 1.0, order, nullptr, 0, tmp.as<double>(), ctx->d_err, s);
-            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN, nullptr, ld, tmp.as<double>(), hm, s);
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN, nullptr, ld, tmp.as<double>(), hm, s,
+                           false, true);
         }
         auto dblock = [&](int ma, int mb) {
             const int64_t tab = h.tbeg[ma], tae = h.tbeg[ma + 1], tbb = h.tbeg[mb], tbe = h.tbeg[mb + 1];
@@ -448,10 +457,11 @@ void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double*
             }
         }
         if (sInHM)
-            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / p.cS, hm, ld, nullptr, hm, s);
+            launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN / p.cS, hm, ld, nullptr, hm, s,
+                           false, s_along_b(h, m1, m2));
         else
             launch_N_block(d, v1b, v1e, t1b, t1e, v2b, v2e, t2b, t2e, same, p.cN, nullptr, ld, stmp.as<double>(), hm,
-                           s);
+                           s, false, true);
         if (wantD12) launch_D_gather(d, t1b, t1e, t2b, t2e, v2b, v2e, p.cD, d12.as<double>(), hm, ld, s);
         if (wantD21) launch_D_gather(d, t2b, t2e, t1b, t1e, v1b, v1e, p.cD, d21.as<double>(), hm, ld, s);
     }
@@ -1448,7 +1458,7 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
                 launch_S_block(u.d, t1b, t1e, tsb, tse, false, 1.0, it.order, nullptr, 0, S.as<double>(),
                                ctx->d_err, s);
                 launch_N_block(u.d, h.vbeg[m], h.vbeg[m + 1], t1b, t1e, vsb, vse, tsb, tse, false, coeffN, nullptr,
-                               Nint, S.as<double>(), out.as<double>(), s, true);
+                               Nint, S.as<double>(), out.as<double>(), s, true, true);
             }
             if (!h.barrier[m]) {
                 DevBuf D((size_t)n1 * n_tris * 24, s);

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "handles.h"
 #include "omg_internal.h"
 
 namespace omg {
@@ -378,75 +379,71 @@ void launch_prepare_vertex_curls(const DevGeom& g, cudaStream_t s) {
     check_launch("vertex curls");
 }
 
-// One thread per vertex pair; the v2 slots (triangle position + curl) are
-// kept in registers (v2 is warp-uniform for consecutive v1), every S entry is
-// read once per triangle pair.
-constexpr int NB_MAXD = 8;
+// N block (operatorN, operators.h: the hypersingular operator by the curl
+// identity): N(v1, v2) = -f sum_{a ni v1} sum_{b ni v2} (q_a(v1) . q_b(v2)) S(a, b),
+// f = 1/4 (1/2 on a vertex shared by both sides of a non-self block), in two
+// contractions with the sparse curl matrices instead of 36 curl products per
+// vertex pair:
+//   1. U_k(x, v) = sum_{y ni v} q_y,k(v) S(x, y), k = x, y, z, for every
+//      triangle x of one side and vertex v of the other (x is the side along
+//      which S is contiguous in memory: coalesced reads, warp-uniform loops);
+//   2. N(vx, v) = -f sum_{x ni vx} sum_k q_x,k(vx) U_k(x, v).
+// S(a, b) (a on mesh 1, b on mesh 2) is the block of the matrix (lower
+// storage at the triangles' positions) or a dense a-major temporary.
+__device__ __forceinline__ double n_block_s(const double* __restrict__ hm_src, int64_t ld,
+                                            const double* __restrict__ tmp, int64_t nt2, const int32_t* __restrict__ tpos,
+                                            int64_t t1b, int64_t t2b, int64_t a, int64_t b) {
+    return hm_src ? hm_src[lower_at(tpos[a], tpos[b], ld)] : tmp[(a - t1b) * nt2 + (b - t2b)];
+}
 
-__global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e, int64_t v2b, int64_t n2,
-                               int64_t t2b, int64_t t2e, int same, double coeff, const double* __restrict__ hm_src,
-                               int64_t ld, const double* __restrict__ tmp, const int32_t* __restrict__ v2t_beg,
-                               const int32_t* __restrict__ v2t_tri, const double* __restrict__ vq,
-                               const int32_t* __restrict__ tpos, int64_t nP, double* hm, int rect) {
+__global__ void n_curl_s_kernel(int64_t txb, int64_t nx, int64_t vyb, int64_t nvy, int64_t tyb, int64_t tye,
+                                int swap, const double* __restrict__ hm_src, int64_t ld, const double* __restrict__ tmp,
+                                int64_t nt2, int64_t t1b, int64_t t2b, const int32_t* __restrict__ v2t_beg,
+                                const int32_t* __restrict__ v2t_tri, const double* __restrict__ vq,
+                                const int32_t* __restrict__ tpos, double* __restrict__ U) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (idx >= n1 * n2) return;
-    const int64_t i1 = idx % n1, i2 = idx / n1;   // v1 fastest: coalesced writes down a column
-    if (same && i2 > i1) return;
-    const int64_t v1 = v1b + i1, v2 = v2b + i2;
-    const double factor = same ? 0.25 : (v1 == v2 ? 0.5 : 0.25);
-    const int64_t nt2 = t2e - t2b;
-    double result = 0.0;
-    const int b0 = v2t_beg[v2], b1 = v2t_beg[v2 + 1];
-    if (b1 - b0 <= NB_MAXD) {
-        int64_t key[NB_MAXD];
-        double qx[NB_MAXD], qy[NB_MAXD], qz[NB_MAXD];
-        int nb = 0;
-#pragma unroll
-        for (int m = 0; m < NB_MAXD; ++m) {
-            key[m] = 0;
-            qx[m] = qy[m] = qz[m] = 0.0;
-            if (m < b1 - b0) {
-                const int64_t b = v2t_tri[b0 + m];
-                if (b >= t2b && b < t2e) {   // compact the slots of this mesh to the front
-#pragma unroll
-                    for (int w = 0; w < NB_MAXD; ++w)
-                        if (w == nb) {
-                            key[w] = hm_src ? (int64_t)tpos[b] : (b - t2b);
-                            qx[w] = vq[3 * (int64_t)(b0 + m)];
-                            qy[w] = vq[3 * (int64_t)(b0 + m) + 1];
-                            qz[w] = vq[3 * (int64_t)(b0 + m) + 2];
-                        }
-                    ++nb;
-                }
-            }
-        }
-        for (int k1 = v2t_beg[v1]; k1 < v2t_beg[v1 + 1]; ++k1) {
-            const int64_t a = v2t_tri[k1];
-            if (a < t1b || a >= t1e) continue;
-            const double px = vq[3 * (int64_t)k1], py = vq[3 * (int64_t)k1 + 1], pz = vq[3 * (int64_t)k1 + 2];
-            const int64_t ta = hm_src ? (int64_t)tpos[a] : (a - t1b) * nt2;
-#pragma unroll
-            for (int m = 0; m < NB_MAXD; ++m) {
-                if (m < nb) {
-                    const double sv = hm_src ? hm_src[lower_at(ta, key[m], ld)] : tmp[ta + key[m]];
-                    result -= factor * (px * qx[m] + py * qy[m] + pz * qz[m]) * sv;
-                }
-            }
-        }
-    } else {   // vertex of unusually high degree
-        for (int k1 = v2t_beg[v1]; k1 < v2t_beg[v1 + 1]; ++k1) {
-            const int64_t a = v2t_tri[k1];
-            if (a < t1b || a >= t1e) continue;
-            const double px = vq[3 * (int64_t)k1], py = vq[3 * (int64_t)k1 + 1], pz = vq[3 * (int64_t)k1 + 2];
-            for (int k2 = b0; k2 < b1; ++k2) {
-                const int64_t b = v2t_tri[k2];
-                if (b < t2b || b >= t2e) continue;
-                const double sv = hm_src ? hm_src[lower_at(tpos[a], tpos[b], ld)] : tmp[(a - t1b) * nt2 + (b - t2b)];
-                result -= factor * (px * vq[3 * (int64_t)k2] + py * vq[3 * (int64_t)k2 + 1] +
-                                    pz * vq[3 * (int64_t)k2 + 2]) * sv;
-            }
-        }
+    if (idx >= nx * nvy) return;
+    const int64_t ix = idx % nx, iv = idx / nx;   // x fastest
+    const int64_t x = txb + ix, v = vyb + iv;
+    double u0 = 0.0, u1 = 0.0, u2 = 0.0;
+    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
+        const int64_t y = v2t_tri[k];
+        if (y < tyb || y >= tye) continue;
+        const double sv = swap ? n_block_s(hm_src, ld, tmp, nt2, tpos, t1b, t2b, y, x)
+                               : n_block_s(hm_src, ld, tmp, nt2, tpos, t1b, t2b, x, y);
+        u0 = fma(vq[3 * (int64_t)k], sv, u0);
+        u1 = fma(vq[3 * (int64_t)k + 1], sv, u1);
+        u2 = fma(vq[3 * (int64_t)k + 2], sv, u2);
     }
+    double* Uv = U + iv * 3 * nx + ix;
+    Uv[0] = u0;
+    Uv[nx] = u1;
+    Uv[2 * nx] = u2;
+}
+
+__global__ void n_curl_u_kernel(int64_t vxb, int64_t nvx, int64_t txb, int64_t txe, int64_t vyb, int64_t nvy, int same,
+                                int swap, double coeff, const double* __restrict__ U, int64_t nx,
+                                const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
+                                const double* __restrict__ vq, int64_t nP, double* hm, int64_t ld, int rect) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= nvx * nvy) return;
+    const int64_t jx = idx % nvx, jy = idx / nvx;   // vx fastest
+    const int64_t i1 = swap ? jy : jx, i2 = swap ? jx : jy;
+    if (same && i2 > i1) return;
+    const int64_t vx = vxb + jx, vy = vyb + jy;
+    const int64_t v1 = swap ? vy : vx, v2 = swap ? vx : vy;
+    const double factor = same ? 0.25 : (v1 == v2 ? 0.5 : 0.25);
+    const double* Uy = U + jy * 3 * nx;
+    double r = 0.0;
+    for (int k = v2t_beg[vx]; k < v2t_beg[vx + 1]; ++k) {
+        const int64_t x = v2t_tri[k];
+        if (x < txb || x >= txe) continue;
+        const int64_t ix = x - txb;
+        r = fma(vq[3 * (int64_t)k], Uy[ix], r);
+        r = fma(vq[3 * (int64_t)k + 1], Uy[nx + ix], r);
+        r = fma(vq[3 * (int64_t)k + 2], Uy[2 * nx + ix], r);
+    }
+    const double result = -factor * r;
     if (rect)   // rectangular output: row = v1's unknown, column = v2 within its range
         hm[(nP + v1) + i2 * ld] += result * coeff;
     else
@@ -455,12 +452,24 @@ __global__ void n_block_kernel(int64_t v1b, int64_t n1, int64_t t1b, int64_t t1e
 
 void launch_N_block(const DevGeom& g, int64_t v1b, int64_t v1e, int64_t t1b, int64_t t1e, int64_t v2b, int64_t v2e,
                     int64_t t2b, int64_t t2e, bool same, double coeff, const double* hm_src, int64_t ld,
-                    const double* tmp, double* hm, cudaStream_t s, bool rect) {
-    const int64_t n = (v1e - v1b) * (v2e - v2b);
+                    const double* tmp, double* hm, cudaStream_t s, bool rect, bool s_contiguous_b) {
+    const int64_t n1 = v1e - v1b, n2 = v2e - v2b;
+    if (n1 <= 0 || n2 <= 0) return;
     ProfScope prof_("n_block", s);
-    n_block_kernel<<<nblocks(n, 256), 256, 0, s>>>(v1b, v1e - v1b, t1b, t1e, v2b, v2e - v2b, t2b, t2e, same ? 1 : 0,
-                                                   coeff, hm_src, ld, tmp, g.v2t_beg, g.v2t_tri, g.v2t_q, g.tpos, g.nP,
-                                                   hm, rect ? 1 : 0);
+    // x: the triangles along which S is contiguous (b for a dense temporary, the later mesh in the matrix)
+    const int swap = s_contiguous_b ? 1 : 0;
+    const int64_t txb = swap ? t2b : t1b, txe = swap ? t2e : t1e, nx = txe - txb;
+    const int64_t vxb = swap ? v2b : v1b, nvx = swap ? n2 : n1;
+    const int64_t vyb = swap ? v1b : v2b, nvy = swap ? n1 : n2;
+    const int64_t tyb = swap ? t1b : t2b, tye = swap ? t1e : t2e;
+    DevBuf U((size_t)nx * nvy * 3 * sizeof(double), s);
+    n_curl_s_kernel<<<nblocks(nx * nvy, 256), 256, 0, s>>>(txb, nx, vyb, nvy, tyb, tye, swap, hm_src, ld, tmp,
+                                                           t2e - t2b, t1b, t2b, g.v2t_beg, g.v2t_tri, g.v2t_q, g.tpos,
+                                                           U.as<double>());
+    check_launch("N block (S by curls)");
+    n_curl_u_kernel<<<nblocks(nvx * nvy, 256), 256, 0, s>>>(vxb, nvx, txb, txe, vyb, nvy, same ? 1 : 0, swap, coeff,
+                                                            U.as<double>(), nx, g.v2t_beg, g.v2t_tri, g.v2t_q, g.nP,
+                                                            hm, ld, rect ? 1 : 0);
     check_launch("N block");
 }
 

@@ -158,9 +158,11 @@ void launch_D_block(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int
 // rect: out(row = triangle unknown, col = vertex - vbb), column-major with ld, instead of the HM lower triangle
 void launch_D_gather(const DevGeom& g, int64_t tab, int64_t tae, int64_t tbb, int64_t tbe, int64_t vbb, int64_t vbe,
                      double coeff, const double* tmp, double* hm, int64_t ld, cudaStream_t s, bool rect = false);
+// s_contiguous_b: S(a, b) is contiguous along b (dense a-major temporaries; a block of the matrix whose mesh 2
+// comes after mesh 1 in the internal order) rather than along a
 void launch_N_block(const DevGeom& g, int64_t v1b, int64_t v1e, int64_t t1b, int64_t t1e, int64_t v2b, int64_t v2e,
                     int64_t t2b, int64_t t2e, bool same, double coeff, const double* hm_src, int64_t ld,
-                    const double* tmp, double* hm, cudaStream_t s, bool rect = false);
+                    const double* tmp, double* hm, cudaStream_t s, bool rect, bool s_contiguous_b);
 void launch_deflate(const DevGeom& g, const std::vector<std::pair<int64_t, int64_t>>& vranges, int64_t i_first,
                     int64_t nb, double* hm, int64_t ld, double* scratch, cudaStream_t s);
 void launch_symmetrize_to_reference(const DevGeom& g, const double* hm_int, int64_t ld_int, double* out,
