@@ -700,7 +700,7 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
 constexpr int FF_TI = 128, FF_TJ = 32;
 
 // One thread per t1 row, looping over the CTA's FF_TJ staged t2 records.
-__global__ void __launch_bounds__(FF_TI, 4) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
+__global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
                                                          int64_t t2b, int64_t n2, int same, int wantS, int wantD12,
                                                          int wantD21, double cS, const int32_t* __restrict__ tpos,
                                                          double* hm, int64_t ld, double* stmp, double* d12,
@@ -729,7 +729,6 @@ __global__ void __launch_bounds__(FF_TI, 4) ff_block_kernel(const float* __restr
     }
     const f2* W = reinterpret_cast<const f2*>(c_w16);   // weight pairs, read from the constant bank
     const float n1x = g1[54], n1y = g1[55], n1z = g1[56], h1 = g1[57];
-    const f2 N1x = pk2(n1x, n1x), N1y = pk2(n1y, n1y), N1z = pk2(n1z, n1z);
     const double A1 = reinterpret_cast<const double*>(g1 + 58)[0];
     for (int jj = 0; jj < nj; ++jj) {
         const int64_t j = j0 + jj;
@@ -746,15 +745,25 @@ __global__ void __launch_bounds__(FF_TI, 4) ff_block_kernel(const float* __restr
         }
         const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
         const float n2x = g2[54], n2y = g2[55], n2z = g2[56];
-        const f2 N2x = pk2(n2x, n2x), N2y = pk2(n2y, n2y), N2z = pk2(n2z, n2z);
-        f2 A21[8];
+        // r = d + Q_q - P_k (d: centroid difference, P_k / Q_q: the points' offsets in the planes of t1 / t2,
+        // so P_k . n1 = Q_q . n2 = 0): r . n2 = d . n2 - P_k . n2 depends on k only and r . n1 = d . n1 + Q_q . n1
+        // on q only, folded into the weights: WD[k] = w_k (r . n2), cq = -w_q (r . n1)
+        const float dn2 = fmaf(fx, n2x, fmaf(fy, n2y, fz * n2z));
+        const float dn1 = fmaf(fx, n1x, fmaf(fy, n1y, fz * n1z));
+        const f2 DN2 = pk2(dn2, dn2), N2x = pk2(n2x, n2x), N2y = pk2(n2y, n2y), N2z = pk2(n2z, n2z);
+        f2 WD[8], A21[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) A21[k] = pk2(0.f, 0.f);
+        for (int k = 0; k < 8; ++k) {
+            WD[k] = mul2(W[k], sub2(DN2, fma2(P1x[k], N2x, fma2(P1y[k], N2y, mul2(P1z[k], N2z)))));
+            A21[k] = pk2(0.f, 0.f);
+        }
         float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
         for (int q = 0; q < 16; ++q) {
-            const float yx = fx + g2[6 + 3 * q], yy = fy + g2[7 + 3 * q], yz = fz + g2[8 + 3 * q];
+            const float qx = g2[6 + 3 * q], qy = g2[7 + 3 * q], qz = g2[8 + 3 * q];
+            const float yx = fx + qx, yy = fy + qy, yz = fz + qz;
             const float wq = c_w16[q];
-            const f2 Yx = pk2(yx, yx), Yy = pk2(yy, yy), Yz = pk2(yz, yz), NWq = pk2(-wq, -wq);
+            const float cq = -wq * (dn1 + fmaf(qx, n1x, fmaf(qy, n1y, qz * n1z)));
+            const f2 Yx = pk2(yx, yx), Yy = pk2(yy, yy), Yz = pk2(yz, yz), CQ = pk2(cq, cq);
             f2 SQ = pk2(0.f, 0.f), K12 = pk2(0.f, 0.f);
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -763,8 +772,8 @@ __global__ void __launch_bounds__(FF_TI, 4) ff_block_kernel(const float* __restr
                 const f2 ir = pk2(rsqrt_ftz(lo2(r2)), rsqrt_ftz(hi2(r2)));
                 const f2 ir3 = mul2(mul2(ir, ir), ir);
                 SQ = fma2(W[k], ir, SQ);
-                K12 = fma2(mul2(W[k], ir3), fma2(rx, N2x, fma2(ry, N2y, mul2(rz, N2z))), K12);
-                A21[k] = fma2(mul2(NWq, ir3), fma2(rx, N1x, fma2(ry, N1y, mul2(rz, N1z))), A21[k]);
+                K12 = fma2(WD[k], ir3, K12);
+                A21[k] = fma2(CQ, ir3, A21[k]);
             }
             s = fmaf(wq, lo2(SQ) + hi2(SQ), s);
             const float kq = wq * (lo2(K12) + hi2(K12));
