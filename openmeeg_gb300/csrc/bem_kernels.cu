@@ -816,22 +816,61 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
 }
 
 // Near pairs: the FP64 analytic kernels of the reference (same outer rule).
-__global__ void near_pairs_kernel(const int2* __restrict__ near, int count, const double* __restrict__ srec,
-                                  const double* __restrict__ prec, const double* __restrict__ qrec, int64_t t1b,
-                                  int64_t n1, int64_t t2b, int64_t n2, int same, int wantS, int wantD12, int wantD21,
-                                  double cS, int order, const int32_t* __restrict__ tpos, double* hm, int64_t ld,
-                                  double* stmp, double* d12, double* d21) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    const int64_t i = near[k].x, j = near[k].y;
+// One lane per (pair, point of the rule): 16 lanes hold a pair, each lane
+// evaluates the analytic integrals at its point (S and D21 over t1 at the
+// points of t2, with shared distances and solid angle; D12 over t2 at the
+// points of t1) and the weighted values are summed across the 16 lanes by
+// shuffles.  Short per-thread chains and many warps hide the latency of the
+// FP64 transcendentals.
+constexpr int NP_LANES = 16;
+
+__global__ void __launch_bounds__(128) near_pairs_kernel(
+    const int2* __restrict__ near, int count, const double* __restrict__ srec, const double* __restrict__ prec,
+    const double* __restrict__ qrec, int64_t t1b, int64_t n1, int64_t t2b, int64_t n2, int same, int wantS,
+    int wantD12, int wantD21, double cS, int order, const int32_t* __restrict__ tpos, double* hm, int64_t ld,
+    double* stmp, double* d12, double* d21) {
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / NP_LANES;   // pair
+    const int m = threadIdx.x % NP_LANES;                                            // point of the rule
+    const bool live = g < count;   // every lane takes part in the shuffles
+    int64_t i = 0, j = 0;
+    if (live) {
+        i = near[g].x;
+        j = near[g].y;
+    }
     const int64_t a = t1b + i, b = t2b + j;
-    const int np = c_nbpts[order];
+    const bool wantP = (wantD21 || (same && wantD12)) && !(same && i == j);
+    double sv = 0.0, p[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+    if (live && m < c_nbpts[order]) {
+        const double w = c_rules[order][m][3];
+        if (wantS || wantP) {
+            const d3 x2 = dev::ld3(qrec + b * QREC + 3 * m);
+            double v[3] = {0, 0, 0};
+            if (wantS && wantP)
+                sv = w * dev::operator_S_p1(srec + a * SREC, prec + a * PREC, x2, v);
+            else if (wantS)
+                sv = w * dev::operator_S(srec + a * SREC, x2);
+            else
+                dev::p1_single_layer(prec + a * PREC, x2, v);
+            p[0] = w * v[0]; p[1] = w * v[1]; p[2] = w * v[2];
+        }
+        if (wantD12) {   // integral over t1 of P1SLP(t2)
+            double v[3];
+            dev::p1_single_layer(prec + b * PREC, dev::ld3(qrec + a * QREC + 3 * m), v);
+            e[0] = w * v[0]; e[1] = w * v[1]; e[2] = w * v[2];
+        }
+    }
+#pragma unroll
+    for (int o = NP_LANES / 2; o > 0; o >>= 1) {
+        sv += __shfl_xor_sync(0xffffffffu, sv, o);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], o);
+            e[c] += __shfl_xor_sync(0xffffffffu, e[c], o);
+        }
+    }
+    if (!live || m != 0) return;
     if (wantS) {
-        const double* S1 = srec + a * SREC;
-        const double* q2 = qrec + b * QREC;
-        double acc = 0.0;
-        for (int m = 0; m < np; ++m) acc += c_rules[order][m][3] * dev::operator_S(S1, dev::ld3(q2 + 3 * m));
-        const double val = q2[48] * acc;
+        const double val = qrec[b * QREC + 48] * sv;
         if (hm)
             hm[lower_at(tpos[a], tpos[b], ld)] = val * cS;
         else {
@@ -839,31 +878,15 @@ __global__ void near_pairs_kernel(const int2* __restrict__ near, int count, cons
             if (same) stmp[j * n2 + i] = val;
         }
     }
-    if (wantD12) {   // integral over t1 of P1SLP(t2)
-        const double* q1 = qrec + a * QREC;
-        const double* P2 = prec + b * PREC;
-        double acc[3] = {0, 0, 0};
-        for (int m = 0; m < np; ++m) {
-            double v[3];
-            dev::p1_single_layer(P2, dev::ld3(q1 + 3 * m), v);
-            const double w = c_rules[order][m][3];
-            acc[0] += w * v[0]; acc[1] += w * v[1]; acc[2] += w * v[2];
-        }
+    if (wantD12) {
+        const double A = qrec[a * QREC + 48];
         double* o = d12 + (i * n2 + j) * 3;
-        o[0] = q1[48] * acc[0]; o[1] = q1[48] * acc[1]; o[2] = q1[48] * acc[2];
+        o[0] = A * e[0]; o[1] = A * e[1]; o[2] = A * e[2];
     }
-    if ((wantD21 || (same && wantD12)) && !(same && i == j)) {   // integral over t2 of P1SLP(t1)
-        const double* q2 = qrec + b * QREC;
-        const double* P1 = prec + a * PREC;
-        double acc[3] = {0, 0, 0};
-        for (int m = 0; m < np; ++m) {
-            double v[3];
-            dev::p1_single_layer(P1, dev::ld3(q2 + 3 * m), v);
-            const double w = c_rules[order][m][3];
-            acc[0] += w * v[0]; acc[1] += w * v[1]; acc[2] += w * v[2];
-        }
+    if (wantP) {
+        const double A = qrec[b * QREC + 48];
         double* o = same ? d12 + (j * n2 + i) * 3 : d21 + (j * n1 + i) * 3;
-        o[0] = q2[48] * acc[0]; o[1] = q2[48] * acc[1]; o[2] = q2[48] * acc[2];
+        o[0] = A * p[0]; o[1] = A * p[1]; o[2] = A * p[2];
     }
 }
 
@@ -884,8 +907,10 @@ void launch_near_pairs(const DevGeom& g, const int2* near, int count, int64_t t1
                        int64_t t2e, bool same, bool wantS, bool wantD12, bool wantD21, double cS, int order,
                        double* hm, int64_t ld, double* stmp, double* d12, double* d21, cudaStream_t s) {
     if (count <= 0) return;
+    if (order < 0 || order > 3) throw Error(OMG_ERR_INVALID, "near pairs: rule of more than 16 points");
     ProfScope prof_("near_pairs", s);
-    near_pairs_kernel<<<nblocks(count, 128), 128, 0, s>>>(near, count, g.srec, g.prec, g.qrec, t1b, t1e - t1b, t2b,
+    near_pairs_kernel<<<nblocks((int64_t)count * NP_LANES, 128), 128, 0, s>>>(near, count, g.srec, g.prec, g.qrec,
+                                                                              t1b, t1e - t1b, t2b,
                                                           t2e - t2b, same ? 1 : 0, wantS ? 1 : 0, wantD12 ? 1 : 0,
                                                           wantD21 ? 1 : 0, cS, order, g.tpos, hm, ld, stmp, d12, d21);
     check_launch("near pairs");

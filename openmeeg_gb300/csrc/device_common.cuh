@@ -75,6 +75,39 @@ __device__ __forceinline__ void p1_single_layer(const double* p, d3 x, double ou
     out[2] = (omega * dot(cross(r0, r1), n) + 0.5 * h * dot(D0, S)) * inv;
 }
 
+// operator_S and p1_single_layer of one triangle at one point (the S and P1
+// records hold the same vertices, normal and area), with the vertex
+// distances and the solid-angle arctangent computed once; each result is the
+// expression of its own routine.
+__device__ __forceinline__ double operator_S_p1(const double* s, const double* p, d3 x, double out[3]) {
+    const d3 r0 = ld3(s) - x, r1 = ld3(s + 3) - x, r2 = ld3(s + 6) - x;
+    const double d0 = norm(r0), d1 = norm(r1), d2 = norm(r2);
+    const d3 n = ld3(s + 9);
+    const double area = s[12];
+    const double h = dot(r0, n);
+    const double dd = 2 * area * h;   // = 2 h area exactly (doubling is exact)
+    const double omega = atan2(dd, d0 * d1 * d2 + (d0 * dot(r1, r2) + d1 * dot(r2, r0) + d2 * dot(r0, r1)));
+    double sum = dot(r0, ld3(s + 16)) * atanh(s[13] / (d0 + d1));
+    sum += dot(r1, ld3(s + 19)) * atanh(s[14] / (d1 + d2));
+    sum += dot(r2, ld3(s + 22)) * atanh(s[15] / (d2 + d0));
+    const double S = 2 * sum - h * ((fabs(dd) < 1e-10) ? 0.0 : 2 * omega);
+    if (fabs(h) < 1e-10) {
+        out[0] = out[1] = out[2] = 0.0;
+        return S;
+    }
+    const d3 D0 = ld3(p + 13), D1 = ld3(p + 16), D2 = ld3(p + 19);
+    const d3 U0 = ld3(p + 22), U1 = ld3(p + 25), U2 = ld3(p + 28);
+    const double l0 = log((d1 + dot(r1, U0)) / (d0 + dot(r0, U0)));
+    const double l1 = log((d2 + dot(r2, U1)) / (d1 + dot(r1, U1)));
+    const double l2 = log((d0 + dot(r0, U2)) / (d2 + dot(r2, U2)));
+    const d3 L = U0 * l0 + U1 * l1 + U2 * l2;
+    const double inv = 1.0 / area;
+    out[0] = (omega * dot(cross(r1, r2), n) + 0.5 * h * dot(D1, L)) * inv;
+    out[1] = (omega * dot(cross(r2, r0), n) + 0.5 * h * dot(D2, L)) * inv;
+    out[2] = (omega * dot(cross(r0, r1), n) + 0.5 * h * dot(D0, L)) * inv;
+    return S;
+}
+
 // ---------------------------------------------------------------------------
 // Bulk copy (TMA engine, non-tensor form) into shared memory, completed on an
 // mbarrier.  Waits are bounded: a wait that gives up reports OMG_ERR_TIMEOUT
