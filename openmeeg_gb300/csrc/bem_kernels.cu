@@ -1243,11 +1243,66 @@ __device__ bool dsm_first_level_f32(int kind, double tol, const DsmTriF& T, floa
     return true;
 }
 
+// Pair (dipole i, triangle t) of the DipSourceMat: the triangle's geometry
+// for the integrator and the boundary coefficient, or false when the pair
+// contributes nothing (dipole in no domain or a zero-conductivity one,
+// triangle not on a boundary of the dipole's domain).
+struct DsmPair {
+    DsmTri T;
+    d3 r0, q, R0, R1, R2;
+    double area, coeffD, sigma;
+    int m;
+};
+
+__device__ __forceinline__ bool dsm_pair(int64_t i, int64_t t, const double* __restrict__ dip,
+                                         const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
+                                         const int* __restrict__ orient, const int* __restrict__ dom, int maxb,
+                                         const int* __restrict__ dnb, const int* __restrict__ bmesh,
+                                         const int* __restrict__ binside, const double* __restrict__ dsigma,
+                                         DsmPair& P) {
+    const int d = dom[i];
+    if (d < 0) return false;
+    P.sigma = dsigma[d];
+    if (P.sigma == 0.0) return false;
+    P.m = tmesh[t];
+    bool on = false;
+    for (int k = 0; k < dnb[d]; ++k)
+        if (bmesh[d * maxb + k] == P.m) {
+            P.coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[d * maxb + k];
+            on = true;
+        }
+    if (!on) return false;
+    const double* s = srec + t * SREC;
+    P.R0 = dev::ld3(s);
+    P.R1 = dev::ld3(s + 3);
+    P.R2 = dev::ld3(s + 6);
+    P.T.p0 = P.R0;
+    P.T.n = dev::ld3(s + 9);
+    P.T.e10 = P.R1 - P.R0;
+    P.T.e20 = P.R2 - P.R0;
+    const double c11 = dev::dot(P.T.e10, P.T.e10), c12 = dev::dot(P.T.e10, P.T.e20),
+                 c22 = dev::dot(P.T.e20, P.T.e20);
+    const double inv_det = 1.0 / (c11 * c22 - c12 * c12);
+    P.T.d11 = c22 * inv_det;
+    P.T.d12 = -c12 * inv_det;
+    P.T.d22 = c11 * inv_det;
+    P.r0 = dev::ld3(dip + 6 * i);
+    P.q = dev::ld3(dip + 6 * i + 3);
+    P.area = s[12];
+    return true;
+}
+
 // SourceMatrix<Dipole> (assembleSourceMat.cpp:66-104) with
 // operatorPotentialDerivative / operatorPotential (operators.cpp:40-88):
 // one thread per (dipole, triangle).  P0 rows are written directly (one
 // triangle per row); the three P1 contributions go to `p1tmp` for a
 // fixed-order vertex gather (the reference accumulates them atomically).
+// Mixed precision: a pair whose first adaptive level FP32 settles is written
+// here; the others are listed (with which of the two integrals is left) for
+// the FP64 adaptive integration in dsm_fallback_kernel, so the warps of that
+// deep recursion are not held up by pairs that need none.
+constexpr int DSM_T_BITS = 29;   // triangle index bits of a list entry; the two top bits: integrals left
+
 __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__ dip, int64_t nt,
                            const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
                            const int64_t* __restrict__ tidx_ref, const int* __restrict__ barrier,
@@ -1255,74 +1310,90 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
                            const int* __restrict__ dnb, const int* __restrict__ bmesh,
                            const int* __restrict__ binside, const double* __restrict__ dsigma, int order, int levels,
                            double tol, int64_t nv, int64_t nP, int perm, double* out, int64_t ldo, double* p1tmp,
-                           int mixed) {
+                           int mixed, int2* left, int* nleft) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t il = blockIdx.y;
     if (t >= nt || il >= ndc) return;
     const int64_t i = dip0 + il;
     double* o3 = p1tmp + (il * nt + t) * 3;
     o3[0] = o3[1] = o3[2] = 0.0;
-    const int d = dom[i];
-    if (d < 0) return;
-    const double sigma = dsigma[d];
-    if (sigma == 0.0) return;
-    const int m = tmesh[t];
-    double coeffD = 0.0;
-    bool on = false;
-    for (int k = 0; k < dnb[d]; ++k)
-        if (bmesh[d * maxb + k] == m) {
-            coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[d * maxb + k];
-            on = true;
-        }
-    if (!on) return;
-    const double* s = srec + t * SREC;
-    const d3 R0 = dev::ld3(s), R1 = dev::ld3(s + 3), R2 = dev::ld3(s + 6);
-    DsmTri T;
-    T.p0 = R0;
-    T.n = dev::ld3(s + 9);
-    T.e10 = R1 - R0;
-    T.e20 = R2 - R0;
-    const double c11 = dev::dot(T.e10, T.e10), c12 = dev::dot(T.e10, T.e20), c22 = dev::dot(T.e20, T.e20);
-    const double inv_det = 1.0 / (c11 * c22 - c12 * c12);
-    T.d11 = c22 * inv_det;
-    T.d12 = -c12 * inv_det;
-    T.d22 = c11 * inv_det;
-    const d3 r0 = dev::ld3(dip + 6 * i), q = dev::ld3(dip + 6 * i + 3);
-    const double area = s[12];
-    double v[3];
-    bool f32v = false, f32p = false;
-    double pf[3];
+    DsmPair P;
+    if (!dsm_pair(i, t, dip, srec, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) return;
+    const bool p0row = !barrier[P.m];
+    const int64_t ref = tidx_ref[t];
+    const int64_t row = perm ? ref - nv : ref;
     if (mixed && order == 3 && levels > 0) {
-        const d3 c = (R0 + R1 + R2) * (1.0 / 3.0);
-        const d3 xcd = c - r0;
+        const d3 c = (P.R0 + P.R1 + P.R2) * (1.0 / 3.0);
+        const d3 xcd = c - P.r0;
         const float3 xc = make_float3((float)xcd.x, (float)xcd.y, (float)xcd.z);
-        const float3 qf = make_float3((float)q.x, (float)q.y, (float)q.z);
-        const d3 a0 = R0 - c, a1 = R1 - c, a2 = R2 - c;
+        const float3 qf = make_float3((float)P.q.x, (float)P.q.y, (float)P.q.z);
+        const d3 a0 = P.R0 - c, a1 = P.R1 - c, a2 = P.R2 - c;
         const float3 F0 = make_float3((float)a0.x, (float)a0.y, (float)a0.z);
         const float3 F1 = make_float3((float)a1.x, (float)a1.y, (float)a1.z);
         const float3 F2 = make_float3((float)a2.x, (float)a2.y, (float)a2.z);
         DsmTriF TF;
         TF.p0 = F0;
-        TF.n = make_float3((float)T.n.x, (float)T.n.y, (float)T.n.z);
-        TF.e10 = make_float3((float)T.e10.x, (float)T.e10.y, (float)T.e10.z);
-        TF.e20 = make_float3((float)T.e20.x, (float)T.e20.y, (float)T.e20.z);
-        TF.d11 = (float)T.d11; TF.d12 = (float)T.d12; TF.d22 = (float)T.d22;
-        f32v = dsm_first_level_f32(0, tol, TF, xc, qf, F0, F1, F2, (float)area, v);
-        if (!barrier[m]) f32p = dsm_first_level_f32(1, tol, TF, xc, qf, F0, F1, F2, (float)area, pf);
+        TF.n = make_float3((float)P.T.n.x, (float)P.T.n.y, (float)P.T.n.z);
+        TF.e10 = make_float3((float)P.T.e10.x, (float)P.T.e10.y, (float)P.T.e10.z);
+        TF.e20 = make_float3((float)P.T.e20.x, (float)P.T.e20.y, (float)P.T.e20.z);
+        TF.d11 = (float)P.T.d11; TF.d12 = (float)P.T.d12; TF.d22 = (float)P.T.d22;
+        double v[3], pf[3];
+        const bool f32v = dsm_first_level_f32(0, tol, TF, xc, qf, F0, F1, F2, (float)P.area, v);
+        const bool f32p = p0row && dsm_first_level_f32(1, tol, TF, xc, qf, F0, F1, F2, (float)P.area, pf);
+        if (f32v) {
+            o3[0] = v[0] * P.coeffD;
+            o3[1] = v[1] * P.coeffD;
+            o3[2] = v[2] * P.coeffD;
+        }
+        if (f32p) out[row + i * ldo] = pf[0] * (P.coeffD / P.sigma);
+        const int need = (f32v ? 0 : 1) | (p0row && !f32p ? 2 : 0);
+        if (need) left[atomicAdd(nleft, 1)] = make_int2((int)il, (int)t | (need << DSM_T_BITS));
+        return;
     }
-    if (!f32v) dsm_adaptive(0, order, levels, tol, T, r0, q, R0, R1, R2, area, v);
-    o3[0] = v[0] * coeffD;
-    o3[1] = v[1] * coeffD;
-    o3[2] = v[2] * coeffD;
-    if (!barrier[m]) {
+    double v[3];
+    dsm_adaptive(0, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, v);
+    o3[0] = v[0] * P.coeffD;
+    o3[1] = v[1] * P.coeffD;
+    o3[2] = v[2] * P.coeffD;
+    if (p0row) {
         double p[3];
-        if (f32p)
-            p[0] = pf[0];
-        else
-            dsm_adaptive(1, order, levels, tol, T, r0, q, R0, R1, R2, area, p);
-        const int64_t ref = tidx_ref[t];
-        const int64_t row = perm ? ref - nv : ref;
-        out[row + i * ldo] = p[0] * (coeffD / sigma);
+        dsm_adaptive(1, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, p);
+        out[row + i * ldo] = p[0] * (P.coeffD / P.sigma);
+    }
+}
+
+// The listed pairs of the mixed first pass: FP64 adaptive integration of the
+// integrals FP32 did not settle (grid-stride over the device-side count).
+__global__ void dsm_fallback_kernel(int64_t dip0, int64_t nt, const double* __restrict__ dip,
+                                    const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
+                                    const int64_t* __restrict__ tidx_ref, const int* __restrict__ orient,
+                                    const int* __restrict__ dom, int maxb, const int* __restrict__ dnb,
+                                    const int* __restrict__ bmesh, const int* __restrict__ binside,
+                                    const double* __restrict__ dsigma, int order, int levels, double tol, int64_t nv,
+                                    int perm, double* out, int64_t ldo, double* p1tmp, const int2* __restrict__ left,
+                                    const int* __restrict__ nleft) {
+    const int n = *nleft;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int2 e = left[idx];
+        const int64_t il = e.x, t = e.y & ((1 << DSM_T_BITS) - 1);
+        const int need = (int)((unsigned)e.y >> DSM_T_BITS);
+        const int64_t i = dip0 + il;
+        DsmPair P;
+        if (!dsm_pair(i, t, dip, srec, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) continue;
+        if (need & 1) {
+            double v[3];
+            dsm_adaptive(0, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, v);
+            double* o3 = p1tmp + (il * nt + t) * 3;
+            o3[0] = v[0] * P.coeffD;
+            o3[1] = v[1] * P.coeffD;
+            o3[2] = v[2] * P.coeffD;
+        }
+        if (need & 2) {
+            double p[3];
+            dsm_adaptive(1, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, p);
+            const int64_t ref = tidx_ref[t];
+            out[(perm ? ref - nv : ref) + i * ldo] = p[0] * (P.coeffD / P.sigma);
+        }
     }
 }
 
@@ -1568,10 +1639,30 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
                 double tol, int perm, double* out, int64_t ldo, double* p1tmp, int mixed, cudaStream_t s) {
     ProfScope prof_("dsm", s);
     if (ndc == 0) return;
+    if (g.nt >= ((int64_t)1 << DSM_T_BITS) || ndc > INT32_MAX) throw Error(OMG_ERR_UNSUPPORTED, "DSM: too many triangles");
+    const bool two_pass = mixed && order == 3 && levels > 0;
+    // the pairs FP32 does not settle (at most one entry per pair) and their count
+    DevBuf left(two_pass ? (size_t)ndc * g.nt * sizeof(int2) : 0, s), nleft(two_pass ? sizeof(int) : 0, s);
+    if (two_pass) OMG_CUDA(cudaMemsetAsync(nleft.p, 0, sizeof(int), s));
     dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
     dsm_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, tmesh, tidx_ref, barrier, orient, dom, maxb, dnb,
-                                    bmesh, binside, dsigma, order, levels, tol, g.nvg, g.nP, perm, out, ldo, p1tmp, mixed);
+                                    bmesh, binside, dsigma, order, levels, tol, g.nvg, g.nP, perm, out, ldo, p1tmp, mixed,
+                                    left.as<int2>(), nleft.as<int>());
     check_launch("DSM");
+    if (two_pass) {
+        static int n_sm = 0;
+        if (!n_sm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+            if (n_sm <= 0) n_sm = 1;
+        }
+        dsm_fallback_kernel<<<(unsigned)(n_sm * 8), 128, 0, s>>>(dip0, g.nt, dip, g.srec, tmesh, tidx_ref, orient, dom,
+                                                                  maxb, dnb, bmesh, binside, dsigma, order, levels,
+                                                                  tol, g.nvg, perm, out, ldo, p1tmp, left.as<int2>(),
+                                                                  nleft.as<int>());
+        check_launch("DSM (FP64 pairs)");
+    }
     dim3 grid2(nblocks(g.nv, 128), (unsigned)ndc);
     dsm_gather_kernel<<<grid2, 128, 0, s>>>(dip0, ndc, g.nv, g.nt, p1tmp, g.v2t_beg, g.v2t_tri, g.v2t_loc, g.nP,
                                             perm, out, ldo);
