@@ -1186,6 +1186,19 @@ int omg_context_create(int device, omg_context* out) {
         OMG_CUDA(cudaMalloc(&ctx->d_errcol, sizeof(int64_t)));
         OMG_CUDA(cudaMalloc(&ctx->d_scalar, sizeof(double) * 4));
         OMG_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int) * 4));
+        // The temporaries of a call (head matrix, factor, digit planes: ~9 GB at N = 17926) are stream-ordered
+        // allocations of the device's default pool; with its default release threshold of zero every
+        // synchronization hands them back to the system and the next call maps them again (about 11 ms per
+        // call at that size).  The pool keeps up to a quarter of the device's memory between calls; the rest
+        // still goes back at each synchronization, and an allocation that fails trims the pool and retries.
+        cudaMemPool_t pool;
+        size_t fr = 0, tot = 0;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess && cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+            uint64_t keep = 0;
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            keep = std::max<uint64_t>(keep, tot / 4);
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
         ctx->launches_at_create = kernel_launch_count();
         *out = ctx.release();
     });
