@@ -169,11 +169,17 @@ def run_reference(args):
 # Nominal FP32 CUDA-core issue rate of a GB300 (152 SMs x 128 lanes x 2.07 GHz),
 # used only to state how busy an FP32-pipe kernel keeps the cores.
 FP32_ISSUE_NOMINAL = 152 * 128 * 2.07e9
+FP64_NOMINAL = 1.25e12   # GB300 dense FP64 (FMA = 2 flops)
+# executed FP64 flops per near pair (DADD + DMUL + 2 DFMA thread instructions) of near_pairs_kernel, ncu at config1
+# (launch 3: 93,224 pairs, 1.735 GFLOP)
+FP64_FLOPS_PER_NEAR_PAIR = 1.735e9 / 93224
 
 # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum)
 # on a smaller head, per unit of the kernel's size (the summaries in profiles/ give
 # the command and the raw figures); scaled to the bench workload by that unit.
 NCU_TRAFFIC_PER_UNIT = {
+    # near pairs: DRAM bytes per near pair (ncu at config1, launch 3: 6.49 MB for 93,224 pairs)
+    "near_pairs": 6.49e6 / 93224,
     # residual B - A X (double-float): bytes per N^2 element of the float-pair head matrix
     # (ncu at N = 17926: 3.205 GB per launch)
     "residual_df64": 9.97,
@@ -247,14 +253,27 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
                      "note": f"executed TF32 tensor flops (3 per FP32-accurate product) vs half the {kind} bf16 "
                              f"burst peak (the TF32 dense rate is half the bf16 rate)"})
     elif name == "ff_block":
-        # far-field FP32 Gauss products: 16 x 16 point pairs per triangle pair, S and D from the same
-        # 256 distances (~20 FP32 operations each: 3 differences, 3 FMA, rsqrt, 3 kernels, 3 accumulations)
+        # far-field FP32 Gauss products: 16 x 16 point pairs per triangle pair, S and both D from the same
+        # 256 distances, 12 FP32 operations each (3 differences, 3 for r^2, rsqrt, 2 for r^-3, 3 accumulations:
+        # the normal components r.n fold into per-point weights since the points lie in their triangles' planes)
         pairs = stats.get("_tri_pairs", 0)
-        ops = 20.0 * 256 * pairs / per_step
+        ops = 12.0 * 256 * pairs / per_step
         achieved = ops / t_launch
         info.update({"bound": "fp32", "achieved": achieved / 1e12, "peak": FP32_ISSUE_NOMINAL / 1e12,
                      "unit": "T FP32 op/s", "frac": achieved / FP32_ISSUE_NOMINAL, "traffic": None,
                      "note": "FP32-pipe bound (rsqrt + FMA); peak is the nominal FP32 issue rate, not a measured one"})
+    elif name == "near_pairs":
+        # FP64 analytic near-pair integrals (OperatorS, P1 single layer both ways at the 16 points of the rule):
+        # FP64 operations executed per near pair from an ncu capture (thread-level DADD + DMUL + 2 DFMA, the
+        # library's log/atan2/sqrt/division sequences included) against the nominal FP64 rate
+        pairs = stats.get("_near_pairs", 0)
+        flops = FP64_FLOPS_PER_NEAR_PAIR * pairs / per_step
+        achieved = flops / t_launch
+        info.update({"bound": "fp64", "achieved": achieved / 1e12, "peak": FP64_NOMINAL / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / FP64_NOMINAL, "traffic": NCU_TRAFFIC_PER_UNIT["near_pairs"] * pairs / per_step,
+                     "near_pairs_per_launch": pairs / per_step,
+                     "note": "executed FP64 flops (ncu op counts per near pair) vs the nominal GB300 FP64 rate "
+                             "(1.25 TFLOP/s; no measured FP64 peak); the same capture shows the FP64 pipe 88% active"})
     elif name in ("potrf_inv", "apply_inv"):
         info.update({"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
                      "note": "one diagonal block per launch (128 x 128, one CTA), sequential over the blocks: "
@@ -291,6 +310,34 @@ def tri_pairs(head):
         if m > 0:
             pairs += T[m] * T[m - 1]                     # adjacent pair
     return pairs
+
+
+def near_pairs_count(head, rho=2.0):
+    """Near triangle pairs of the mixed head matrix (those integrated by the FP64 analytic kernels): centroid
+    distance below rho times the larger of the two triangles' longest edges, over the self pairs (j >= i) and
+    the adjacent mesh pairs, as the far-field kernel lists them."""
+    from scipy.spatial import cKDTree
+    cen, hmax = [], []
+    for V, T in zip(head.vertices, head.triangles):
+        P = V[T]
+        cen.append(P.mean(axis=1))
+        e = np.stack([np.linalg.norm(P[:, 1] - P[:, 0], axis=1), np.linalg.norm(P[:, 2] - P[:, 1], axis=1),
+                      np.linalg.norm(P[:, 0] - P[:, 2], axis=1)], axis=1)
+        hmax.append(e.max(axis=1))
+    count = 0
+    for m in range(len(cen)):
+        for m2 in ([m] if m == 0 else [m - 1, m]):
+            r = rho * max(hmax[m].max(), hmax[m2].max())
+            pairs = cKDTree(cen[m]).query_ball_tree(cKDTree(cen[m2]), r)
+            for i, js in enumerate(pairs):
+                if not js:
+                    continue
+                js = np.asarray(js)
+                if m2 == m:
+                    js = js[js >= i]
+                d = np.linalg.norm(cen[m2][js] - cen[m][i], axis=1)
+                count += int(np.count_nonzero(d < rho * np.maximum(hmax[m][i], hmax[m2][js])))
+    return count
 
 
 def run_gpu(args):
@@ -393,9 +440,11 @@ def run_gpu(args):
     total_prof_ms = sum(v[1] for v in prof.values())
     stx_r = dict(stx)
     stx_r["_tri_pairs"] = tri_pairs(w.head)
+    stx_r["_near_pairs"] = near_pairs_count(w.head)
     roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx_r, pk)
     others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx_r, pk)
-              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block") and n != dname}
+              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block", "near_pairs")
+              and n != dname}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
