@@ -1178,14 +1178,17 @@ struct DsmTriF {
     float3 p0, e10, e20, n;   // p0 relative to the centroid
     float d11, d12, d22;
 };
-__device__ __forceinline__ void dsm_eval_f(int kind, const DsmTriF& T, float3 xc, float3 q, float3 v, float out[3]) {
+__device__ __forceinline__ float3 fmid(float3 a, float3 b) {
+    return make_float3(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z));
+}
+// Both integrands of the first level at once, sharing the point's distance:
+// out[0..2] the kind-0 values (P1-weighted normal derivative), out[3] the
+// kind-1 value (potential); the expressions of the separate evaluations.
+__device__ __forceinline__ void dsm_eval2_f(const DsmTriF& T, float3 xc, float3 q, float3 v, float out[4]) {
     const float3 x = make_float3(xc.x + v.x, xc.y + v.y, xc.z + v.z);   // r - r0
     const float n2 = x.x * x.x + x.y * x.y + x.z * x.z;
     const float qx = q.x * x.x + q.y * x.y + q.z * x.z;
-    if (kind == 1) {
-        out[0] = qx / (n2 * sqrtf(n2));
-        return;
-    }
+    out[3] = qx / (n2 * sqrtf(n2));
     const float inv = 1.f / n2;
     const float3 g = make_float3(q.x - 3.f * qx * x.x * inv, q.y - 3.f * qx * x.y * inv, q.z - 3.f * qx * x.z * inv);
     const float gn = (g.x * T.n.x + g.y * T.n.y + g.z * T.n.z) * (inv * sqrtf(inv));
@@ -1197,50 +1200,87 @@ __device__ __forceinline__ void dsm_eval_f(int kind, const DsmTriF& T, float3 xc
     out[1] = gn * l1;
     out[2] = gn * l2;
 }
-__device__ __forceinline__ void dsm_rule_f(int kind, const DsmTriF& T, float3 xc, float3 q, float3 P0, float3 P1,
-                                           float3 P2, float area, float res[3]) {
-    float acc[3] = {0.f, 0.f, 0.f};
+__device__ __forceinline__ void dsm_rule2_f(const DsmTriF& T, float3 xc, float3 q, float3 P0, float3 P1, float3 P2,
+                                            float area, float res[4]) {
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
     for (int k = 0; k < 16; ++k) {
         const float b0 = c_b16[k][0], b1 = c_b16[k][1], b2 = c_b16[k][2];
         const float3 v = make_float3(b0 * P0.x + b1 * P1.x + b2 * P2.x, b0 * P0.y + b1 * P1.y + b2 * P2.y,
                                      b0 * P0.z + b1 * P1.z + b2 * P2.z);
-        float e[3];
-        dsm_eval_f(kind, T, xc, q, v, e);
+        float e[4];
+        dsm_eval2_f(T, xc, q, v, e);
         const float w = c_w16[k];
-        acc[0] = fmaf(w, e[0], acc[0]);
-        if (kind == 0) {
-            acc[1] = fmaf(w, e[1], acc[1]);
-            acc[2] = fmaf(w, e[2], acc[2]);
-        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, e[c], acc[c]);
     }
-    res[0] = area * acc[0]; res[1] = area * acc[1]; res[2] = area * acc[2];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) res[c] = area * acc[c];
 }
-__device__ __forceinline__ float3 fmid(float3 a, float3 b) {
-    return make_float3(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z));
-}
-// Returns true (and the refined value) when FP32 settles the first level.
-__device__ bool dsm_first_level_f32(int kind, double tol, const DsmTriF& T, float3 xc, float3 q, float3 R0,
-                                    float3 R1, float3 R2, float area, double result[3]) {
-    float coarse[3];
-    dsm_rule_f(kind, T, xc, q, R0, R1, R2, area, coarse);
+// The first adaptive level of both integrals in one pass over the 80 points
+// (the 16-point rule on the triangle and on its four halves-of-edges
+// subtriangles): okv / okp tell whether FP32 settles the kind-0 (v, three
+// values) / kind-1 (p) integral, i.e. |coarse - refined| <= tol |coarse| / 2;
+// v and p are then the refined values.
+__device__ void dsm_first_level2_f32(double tol, const DsmTriF& T, float3 xc, float3 q, float3 R0, float3 R1,
+                                     float3 R2, float area, double v[3], double p[1], bool& okv, bool& okp) {
+    float coarse[4];
+    dsm_rule2_f(T, xc, q, R0, R1, R2, area, coarse);
     const float3 m0 = fmid(R1, R2), m1 = fmid(R2, R0), m2 = fmid(R0, R1);
-    float a[3], b[3], c[3], d[3];
     const float sub = 0.25f * area;
-    dsm_rule_f(kind, T, xc, q, R0, m1, m2, sub, a);
-    dsm_rule_f(kind, T, xc, q, m0, R1, m2, sub, b);
-    dsm_rule_f(kind, T, xc, q, m0, m1, R2, sub, c);
-    dsm_rule_f(kind, T, xc, q, m0, m1, m2, sub, d);
-    const int dim = kind == 0 ? 3 : 1;
-    double ref[3], dn = 0.0, cn = 0.0;
-    for (int k = 0; k < dim; ++k) {
-        ref[k] = (double)a[k] + (double)b[k] + (double)c[k] + (double)d[k];
+    float a[4], b[4], c[4], d[4];
+    dsm_rule2_f(T, xc, q, R0, m1, m2, sub, a);
+    dsm_rule2_f(T, xc, q, m0, R1, m2, sub, b);
+    dsm_rule2_f(T, xc, q, m0, m1, R2, sub, c);
+    dsm_rule2_f(T, xc, q, m0, m1, m2, sub, d);
+    double ref[4], dnv = 0.0, cnv = 0.0;
+    for (int k = 0; k < 4; ++k) ref[k] = (double)a[k] + (double)b[k] + (double)c[k] + (double)d[k];
+    for (int k = 0; k < 3; ++k) {
         const double e = (double)coarse[k] - ref[k];
-        dn += e * e;
-        cn += (double)coarse[k] * (double)coarse[k];
+        dnv += e * e;
+        cnv += (double)coarse[k] * (double)coarse[k];
     }
-    if (!(sqrt(dn) <= 0.5 * tol * sqrt(cn))) return false;
-    for (int k = 0; k < dim; ++k) result[k] = ref[k];
-    return true;
+    const double ep = (double)coarse[3] - ref[3];
+    okv = sqrt(dnv) <= 0.5 * tol * sqrt(cnv);
+    okp = fabs(ep) <= 0.5 * tol * fabs((double)coarse[3]);
+    for (int k = 0; k < 3; ++k) v[k] = ref[k];
+    p[0] = ref[3];
+}
+
+// FP32 first-level record of a triangle (coordinates relative to its
+// centroid, kept in FP64), built once per DipSourceMat launch.
+struct DsmRecF {
+    DsmTriF T;
+    float3 F1, F2;   // vertices 1 and 2 relative to the centroid (vertex 0 is T.p0)
+    float area;
+    double cx, cy, cz;
+};
+
+__global__ void dsm_prepare_f_kernel(int64_t nt, const double* __restrict__ srec, DsmRecF* rec) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const double* s = srec + t * SREC;
+    const d3 R0 = dev::ld3(s), R1 = dev::ld3(s + 3), R2 = dev::ld3(s + 6), n = dev::ld3(s + 9);
+    const d3 e10 = R1 - R0, e20 = R2 - R0;
+    const double c11 = dev::dot(e10, e10), c12 = dev::dot(e10, e20), c22 = dev::dot(e20, e20);
+    const double inv_det = 1.0 / (c11 * c22 - c12 * c12);
+    const d3 c = (R0 + R1 + R2) * (1.0 / 3.0);
+    const d3 a0 = R0 - c, a1 = R1 - c, a2 = R2 - c;
+    DsmRecF r;
+    r.T.p0 = make_float3((float)a0.x, (float)a0.y, (float)a0.z);
+    r.T.n = make_float3((float)n.x, (float)n.y, (float)n.z);
+    r.T.e10 = make_float3((float)e10.x, (float)e10.y, (float)e10.z);
+    r.T.e20 = make_float3((float)e20.x, (float)e20.y, (float)e20.z);
+    r.T.d11 = (float)(c22 * inv_det);
+    r.T.d12 = (float)(-c12 * inv_det);
+    r.T.d22 = (float)(c11 * inv_det);
+    r.F1 = make_float3((float)a1.x, (float)a1.y, (float)a1.z);
+    r.F2 = make_float3((float)a2.x, (float)a2.y, (float)a2.z);
+    r.area = (float)s[12];
+    r.cx = c.x;
+    r.cy = c.y;
+    r.cz = c.z;
+    rec[t] = r;
 }
 
 // Pair (dipole i, triangle t) of the DipSourceMat: the triangle's geometry
@@ -1254,12 +1294,12 @@ struct DsmPair {
     int m;
 };
 
-__device__ __forceinline__ bool dsm_pair(int64_t i, int64_t t, const double* __restrict__ dip,
-                                         const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
-                                         const int* __restrict__ orient, const int* __restrict__ dom, int maxb,
-                                         const int* __restrict__ dnb, const int* __restrict__ bmesh,
-                                         const int* __restrict__ binside, const double* __restrict__ dsigma,
-                                         DsmPair& P) {
+// The boundary coefficient of the pair, or false when it contributes nothing.
+__device__ __forceinline__ bool dsm_pair_coeff(int64_t i, int64_t t, const int32_t* __restrict__ tmesh,
+                                               const int* __restrict__ orient, const int* __restrict__ dom, int maxb,
+                                               const int* __restrict__ dnb, const int* __restrict__ bmesh,
+                                               const int* __restrict__ binside, const double* __restrict__ dsigma,
+                                               DsmPair& P) {
     const int d = dom[i];
     if (d < 0) return false;
     P.sigma = dsigma[d];
@@ -1271,7 +1311,16 @@ __device__ __forceinline__ bool dsm_pair(int64_t i, int64_t t, const double* __r
             P.coeffD = (binside[d * maxb + k] ? -kK : kK) * orient[d * maxb + k];
             on = true;
         }
-    if (!on) return false;
+    return on;
+}
+
+__device__ __forceinline__ bool dsm_pair(int64_t i, int64_t t, const double* __restrict__ dip,
+                                         const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
+                                         const int* __restrict__ orient, const int* __restrict__ dom, int maxb,
+                                         const int* __restrict__ dnb, const int* __restrict__ bmesh,
+                                         const int* __restrict__ binside, const double* __restrict__ dsigma,
+                                         DsmPair& P) {
+    if (!dsm_pair_coeff(i, t, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) return false;
     const double* s = srec + t * SREC;
     P.R0 = dev::ld3(s);
     P.R1 = dev::ld3(s + 3);
@@ -1310,7 +1359,7 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
                            const int* __restrict__ dnb, const int* __restrict__ bmesh,
                            const int* __restrict__ binside, const double* __restrict__ dsigma, int order, int levels,
                            double tol, int64_t nv, int64_t nP, int perm, double* out, int64_t ldo, double* p1tmp,
-                           int mixed, int2* left, int* nleft) {
+                           int mixed, const DsmRecF* __restrict__ recf, int2* left, int* nleft) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t il = blockIdx.y;
     if (t >= nt || il >= ndc) return;
@@ -1318,28 +1367,19 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
     double* o3 = p1tmp + (il * nt + t) * 3;
     o3[0] = o3[1] = o3[2] = 0.0;
     DsmPair P;
-    if (!dsm_pair(i, t, dip, srec, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) return;
-    const bool p0row = !barrier[P.m];
     const int64_t ref = tidx_ref[t];
     const int64_t row = perm ? ref - nv : ref;
     if (mixed && order == 3 && levels > 0) {
-        const d3 c = (P.R0 + P.R1 + P.R2) * (1.0 / 3.0);
-        const d3 xcd = c - P.r0;
-        const float3 xc = make_float3((float)xcd.x, (float)xcd.y, (float)xcd.z);
-        const float3 qf = make_float3((float)P.q.x, (float)P.q.y, (float)P.q.z);
-        const d3 a0 = P.R0 - c, a1 = P.R1 - c, a2 = P.R2 - c;
-        const float3 F0 = make_float3((float)a0.x, (float)a0.y, (float)a0.z);
-        const float3 F1 = make_float3((float)a1.x, (float)a1.y, (float)a1.z);
-        const float3 F2 = make_float3((float)a2.x, (float)a2.y, (float)a2.z);
-        DsmTriF TF;
-        TF.p0 = F0;
-        TF.n = make_float3((float)P.T.n.x, (float)P.T.n.y, (float)P.T.n.z);
-        TF.e10 = make_float3((float)P.T.e10.x, (float)P.T.e10.y, (float)P.T.e10.z);
-        TF.e20 = make_float3((float)P.T.e20.x, (float)P.T.e20.y, (float)P.T.e20.z);
-        TF.d11 = (float)P.T.d11; TF.d12 = (float)P.T.d12; TF.d22 = (float)P.T.d22;
-        double v[3], pf[3];
-        const bool f32v = dsm_first_level_f32(0, tol, TF, xc, qf, F0, F1, F2, (float)P.area, v);
-        const bool f32p = p0row && dsm_first_level_f32(1, tol, TF, xc, qf, F0, F1, F2, (float)P.area, pf);
+        if (!dsm_pair_coeff(i, t, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) return;
+        const bool p0row = !barrier[P.m];
+        const DsmRecF R = recf[t];
+        const double* dp = dip + 6 * i;
+        const float3 xc = make_float3((float)(R.cx - dp[0]), (float)(R.cy - dp[1]), (float)(R.cz - dp[2]));
+        const float3 qf = make_float3((float)dp[3], (float)dp[4], (float)dp[5]);
+        double v[3], pf[1];
+        bool f32v, f32p;
+        dsm_first_level2_f32(tol, R.T, xc, qf, R.T.p0, R.F1, R.F2, R.area, v, pf, f32v, f32p);
+        f32p = f32p && p0row;
         if (f32v) {
             o3[0] = v[0] * P.coeffD;
             o3[1] = v[1] * P.coeffD;
@@ -1350,6 +1390,8 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
         if (need) left[atomicAdd(nleft, 1)] = make_int2((int)il, (int)t | (need << DSM_T_BITS));
         return;
     }
+    if (!dsm_pair(i, t, dip, srec, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) return;
+    const bool p0row = !barrier[P.m];
     double v[3];
     dsm_adaptive(0, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, v);
     o3[0] = v[0] * P.coeffD;
@@ -1642,12 +1684,17 @@ void launch_dsm(const DevGeom& g, int64_t dip0, int64_t ndc, const double* dip, 
     if (g.nt >= ((int64_t)1 << DSM_T_BITS) || ndc > INT32_MAX) throw Error(OMG_ERR_UNSUPPORTED, "DSM: too many triangles");
     const bool two_pass = mixed && order == 3 && levels > 0;
     // the pairs FP32 does not settle (at most one entry per pair) and their count
-    DevBuf left(two_pass ? (size_t)ndc * g.nt * sizeof(int2) : 0, s), nleft(two_pass ? sizeof(int) : 0, s);
-    if (two_pass) OMG_CUDA(cudaMemsetAsync(nleft.p, 0, sizeof(int), s));
+    DevBuf left(two_pass ? (size_t)ndc * g.nt * sizeof(int2) : 0, s), nleft(two_pass ? sizeof(int) : 0, s),
+        recf(two_pass ? (size_t)g.nt * sizeof(DsmRecF) : 0, s);
+    if (two_pass) {
+        OMG_CUDA(cudaMemsetAsync(nleft.p, 0, sizeof(int), s));
+        dsm_prepare_f_kernel<<<nblocks(g.nt, 128), 128, 0, s>>>(g.nt, g.srec, static_cast<DsmRecF*>(recf.p));
+        check_launch("DSM records");
+    }
     dim3 grid(nblocks(g.nt, 128), (unsigned)ndc);
     dsm_kernel<<<grid, 128, 0, s>>>(dip0, ndc, dip, g.nt, g.srec, tmesh, tidx_ref, barrier, orient, dom, maxb, dnb,
                                     bmesh, binside, dsigma, order, levels, tol, g.nvg, g.nP, perm, out, ldo, p1tmp, mixed,
-                                    left.as<int2>(), nleft.as<int>());
+                                    static_cast<const DsmRecF*>(recf.p), left.as<int2>(), nleft.as<int>());
     check_launch("DSM");
     if (two_pass) {
         static int n_sm = 0;
