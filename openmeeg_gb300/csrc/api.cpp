@@ -173,6 +173,17 @@ static int n_sm() {
     return n;
 }
 
+// Points the context's stream at another stream for a scope (the library's calls take the context's
+// stream), restoring it at scope exit.
+struct StreamSwap {
+    omg_context ctx;
+    cudaStream_t saved;
+    StreamSwap(omg_context c, cudaStream_t st) : ctx(c), saved(c->stream) { c->stream = st; }
+    ~StreamSwap() { ctx->stream = saved; }
+    StreamSwap(const StreamSwap&) = delete;
+    StreamSwap& operator=(const StreamSwap&) = delete;
+};
+
 void ensure_aux(omg_context ctx) {
     if (!ctx->aux) OMG_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
     if (!ctx->ev_a) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_a, cudaEventDisableTiming));
@@ -587,6 +598,14 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     bool rest_pending = false;
     const int reserve = 24;   // SMs the rest update leaves to the panel chain (measured optimum at config1)
     bool have_t = false;     // Th/Tl already hold this panel's A21 split (written by the update before it)
+    // fold of block row b for the backward solves (block row <- Linv_b x block row, heads in A, remainders in
+    // A32r); run after the factorization (interleaved with the rest updates it delayed the panel chain)
+    auto fold_rows = [&](size_t b, cudaStream_t st) {
+        const int64_t k0 = sv->bounds[b], nk = sv->bounds[b + 1] - k0;
+        const float* Rh = Bi.as<float>() + 2 * b * nb * nb;   // Linv_b split, K-major rows
+        gemm_tf32x3(nk, k0, nk, 1.f, Rh, Rh + nb * nb, nb, nb, 0, A, Ar, ld, N, k0, 0.f, A + k0, ld, false,
+                    sv->ctx->d_err, st, "fold_rows", 0, nullptr, nullptr, 0, 0, Ar + k0, nullptr, nullptr, 0, true);
+    };
     // Panels are taken in groups of two (never across the start of the vertex part): the trailing
     // update of a group runs once with K = 256, which halves the traffic of reading and writing the
     // trailing matrix compared with one update per panel.
@@ -681,18 +700,20 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     float* LCh = LC.as<float>();
     float* LCl = LCh + nblocks * nb * nb;
     split_cols(nb, (int64_t)nblocks * nb, nb, sv->Linv32.as<float>(), nb, LCh, LCl, s);
+    // the panel folds on the main stream, the block-row folds on the second one: disjoint memory, and each
+    // product is a few latency-bound waves, so two at a time fill the GPU
+    OMG_CUDA(cudaEventRecord(ev_w, s));
+    OMG_CUDA(cudaStreamWaitEvent(s2, ev_w, 0));
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
         if (m > 0)
             gemm_tf32x3(nk, m, nk, 1.f, LCh + b * nb * nb, LCl + b * nb * nb, nb, nb, 0, wh(b), wl(b), nb, nb, 0,
                         0.f, wh(b), nb, false, sv->ctx->d_err, s, "fold_w", 0, nullptr, nullptr, 0, 0, wl(b), nullptr,
                         nullptr, 0, true);
-        if (k0 > 0) {
-            const float* Rh = Bi.as<float>() + 2 * b * nb * nb;   // Linv_b split, K-major rows
-            gemm_tf32x3(nk, k0, nk, 1.f, Rh, Rh + nb * nb, nb, nb, 0, A, Ar, ld, N, k0, 0.f, A + k0, ld, false,
-                        sv->ctx->d_err, s, "fold_rows", 0, nullptr, nullptr, 0, 0, Ar + k0, nullptr, nullptr, 0, true);
-        }
+        if (k0 > 0) fold_rows(b, s2);
     }
+    OMG_CUDA(cudaEventRecord(ev_r, s2));
+    OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));   // before the split buffers are released on the main stream
 }
 
 // FP32 solve on the tensor cores: B <- HM^-1 B (internal numbering).  With
@@ -968,8 +989,22 @@ void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) 
 // ---------------------------------------------------------------------------
 // Sources / sensors
 // ---------------------------------------------------------------------------
+// Meshes whose rows of the DipSourceMat can be nonzero: the boundaries of the dipoles' domains (host copy of the
+// per-dipole domain indices).
+static std::vector<int> meshes_of_domains(omg_geometry g, const std::vector<int>& hdom) {
+    std::vector<char> used(g->h.nmesh, 0);
+    for (int d : hdom)
+        if (d >= 0 && g->h.domains[d].sigma != 0.0)
+            for (const auto& b : g->h.domains[d].bounds) used[b.mesh] = 1;
+    std::vector<int> out;
+    for (int m = 0; m < g->h.nmesh; ++m)
+        if (used[m]) out.push_back(m);
+    return out;
+}
+
 void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain, int perm,
-                  double* out, int64_t ldo, int precision, std::vector<int>* meshes_used, uint64_t allowed_domains) {
+                  double* out, int64_t ldo, int precision, std::vector<int>* meshes_used, uint64_t allowed_domains,
+                  DevBuf* dom_out) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     check_integrator(integ, true);
@@ -1002,13 +1037,7 @@ void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integ
         std::vector<int> hdom(nd);
         OMG_CUDA(cudaMemcpyAsync(hdom.data(), dom.p, nd * sizeof(int), cudaMemcpyDeviceToHost, s));
         OMG_CUDA(cudaStreamSynchronize(s));
-        std::vector<char> used(g->h.nmesh, 0);
-        for (int d : hdom)
-            if (d >= 0 && g->h.domains[d].sigma != 0.0)
-                for (const auto& b : g->h.domains[d].bounds) used[b.mesh] = 1;
-        meshes_used->clear();
-        for (int m = 0; m < g->h.nmesh; ++m)
-            if (used[m]) meshes_used->push_back(m);
+        *meshes_used = meshes_of_domains(g, hdom);
     }
     // chunk the dipoles so the P1 scratch stays near 512 MB
     const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (g->h.nt * 24)));
@@ -1026,6 +1055,7 @@ void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integ
             launch_fold_to_reference(g->h.N, g->h.nvg, g->d.nP, g->gbeg, g->gcopy, nd, loc.as<double>(), g->d.N, out,
                                      1, ldo, s);
     }
+    if (dom_out) *dom_out = std::move(dom);   // the per-dipole domains, for a read-back by the caller
 }
 
 std::vector<std::pair<int64_t, int64_t>> gain_row_ranges(omg_geometry geo, const std::vector<int>& src_meshes) {
@@ -1962,7 +1992,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
                           const double* sq, int64_t nm, double* geeg, double* gmeg, omg_gain_stats* st) {
     cudaStream_t s = ctx->stream;
     const int64_t N = geo->dg.N, k = ne + nm;
-    cudaEvent_t ev[6];
+    cudaEvent_t ev[7];
     for (auto& e : ev) OMG_CUDA(cudaEventCreate(&e));
     OMG_CUDA(cudaEventRecord(ev[0], s));
     reset_err(ctx);
@@ -1974,30 +2004,43 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     sv->precision = precision;
     sv->N = N;
     sv->nP = geo->d.nP;
+    // right-hand sides (internal numbering) and DSM: allocated on the main stream, which uses them last
+    DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
+    DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
+    OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
+    if (precision == OMG_PREC_MIXED) ensure_gg_tables(geo);
+    // The sources (sensor right-hand sides, DipSourceMat, DipSource2MEGMat) do not depend on the head matrix:
+    // they are enqueued first, on the second stream, and run while the main stream assembles the head matrix
+    // (whose FP64 near pairs leave the FP32 pipes free); the main stream joins them before the factorization.
+    ensure_aux(ctx);
+    cudaStream_t s2 = ctx->aux;
+    OMG_CUDA(cudaEventRecord(ev[5], s));
+    OMG_CUDA(cudaStreamWaitEvent(s2, ev[5], 0));
+    DevBuf dom;
+    {
+        StreamSwap on_aux(ctx, s2);   // the library calls below take the context's stream
+        if (ne > 0) {
+            OMG_REQUIRE(geo->n_eeg_cand > 0, "no interface touches a zero-conductivity domain");
+            launch_h2em(geo->d, el, ne, geo->n_eeg_seg, geo->eeg_seg, geo->eeg_cand, 1, B.as<double>(), 1, N, 0,
+                        nullptr, nullptr, s2);
+        }
+        if (nm > 0 && geo->h.shared) {   // on the vertex copies, then summed per distinct vertex
+            const int64_t Nl = geo->d.N;
+            DevBuf loc((size_t)Nl * nm * 8, s2);
+            OMG_CUDA(cudaMemsetAsync(loc.p, 0, (size_t)Nl * nm * 8, s2));
+            launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, loc.as<double>(), 1, Nl, 0, F.as<double>(), s2);
+            launch_fold_rows(N, geo->d.nP, geo->gbeg, geo->gcopy, nm, loc.as<double>(), Nl, B.as<double>() + ne * N,
+                             N, s2);
+        } else if (nm > 0) {
+            launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s2);
+        }
+        dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, nullptr, 0, &dom);
+        if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s2);
+        OMG_CUDA(cudaEventRecord(ev[6], s2));
+    }
     DevBuf hm = assemble_system(geo, hm_it, precision, false);
     OMG_CUDA(cudaEventRecord(ev[1], s));
-    // right-hand sides (internal numbering) and DSM
-    DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
-    OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
-    if (ne > 0) {
-        OMG_REQUIRE(geo->n_eeg_cand > 0, "no interface touches a zero-conductivity domain");
-        launch_h2em(geo->d, el, ne, geo->n_eeg_seg, geo->eeg_seg, geo->eeg_cand, 1, B.as<double>(), 1, N, 0, nullptr,
-                    nullptr, s);
-    }
-    DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
-    if (nm > 0 && geo->h.shared) {   // on the vertex copies, then summed per distinct vertex
-        const int64_t Nl = geo->d.N;
-        DevBuf loc((size_t)Nl * nm * 8, s);
-        OMG_CUDA(cudaMemsetAsync(loc.p, 0, (size_t)Nl * nm * 8, s));
-        launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, loc.as<double>(), 1, Nl, 0, F.as<double>(), s);
-        launch_fold_rows(N, geo->d.nP, geo->gbeg, geo->gcopy, nm, loc.as<double>(), Nl, B.as<double>() + ne * N, N, s);
-    } else if (nm > 0) {
-        launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
-    }
-    if (precision == OMG_PREC_MIXED) ensure_gg_tables(geo);
-    std::vector<int> src_meshes;
-    dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, &src_meshes);
-    if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s);
+    OMG_CUDA(cudaStreamWaitEvent(s, ev[6], 0));
     OMG_CUDA(cudaEventRecord(ev[2], s));
     solver_factor(sv.get(), std::move(hm));
     OMG_CUDA(cudaEventRecord(ev[3], s));
@@ -2009,8 +2052,13 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     const bool sv_tc = sv->tc_residual;
     sv.reset();
     // G = Y^T DSM over the rows where DSM can be nonzero (the source meshes' triangles and vertices)
-    gain_contract(gain_row_ranges(geo, src_meshes), B.as<double>(), N, ne, nm, DSM.as<double>(), nd, geeg, gmeg, s,
-                  precision, ctx->d_err);
+    std::vector<int> hdom(nd);
+    if (nd > 0) {
+        OMG_CUDA(cudaMemcpyAsync(hdom.data(), dom.p, nd * sizeof(int), cudaMemcpyDeviceToHost, s));
+        OMG_CUDA(cudaStreamSynchronize(s));
+    }
+    gain_contract(gain_row_ranges(geo, meshes_of_domains(geo, hdom)), B.as<double>(), N, ne, nm, DSM.as<double>(), nd,
+                  geeg, gmeg, s, precision, ctx->d_err);
     OMG_CUDA(cudaEventRecord(ev[4], s));
     check_err(ctx, "gain");
     if (st) {

@@ -85,7 +85,7 @@ void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs);
 void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int residual_steps, double* d_est);
 void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain, int perm,
                   double* out, int64_t ldo, int precision = OMG_PREC_FP64, std::vector<int>* meshes_used = nullptr,
-                  uint64_t allowed_domains = 0);
+                  uint64_t allowed_domains = 0, DevBuf* dom_out = nullptr);
 // Row ranges (internal numbering, merged) where the DipSourceMat of dipoles in
 // the given source meshes' domains can be nonzero.
 std::vector<std::pair<int64_t, int64_t>> gain_row_ranges(omg_geometry geo, const std::vector<int>& src_meshes);
