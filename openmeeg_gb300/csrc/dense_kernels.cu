@@ -856,9 +856,9 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
         }
         __syncthreads();
     }
-    for (int e = tid; e < n * n; e += PI_THREADS) {
-        const int r = e % n, c = e / n;
-        if (r >= c) A[r + (int64_t)c * lda] = sA[r * PI_LD + c];
+    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // no division by the runtime size
+        const int r = e % PI_NB, c = e / PI_NB;
+        if (r >= c && r < n) A[r + (int64_t)c * lda] = sA[r * PI_LD + c];
     }
     for (int e = tid; e < PI_NB * PI_NB / 4; e += PI_THREADS) {   // float4 stores (64 KB-aligned blocks)
         {   // column-major Linv: 4 rows of one column
