@@ -491,7 +491,7 @@ void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double*
 
 void ensure_gg_tables(omg_geometry g) {
     if (!g->grec) {
-        g->bufs.emplace_back((size_t)g->h.nt * 64 * sizeof(float), g->ctx->stream, true);
+        g->bufs.emplace_back((size_t)g->h.nt * kFarRecFloats * sizeof(float), g->ctx->stream, true);
         g->grec = g->bufs.back().as<float>();
         launch_prepare_gg(g->d, g->grec, g->ctx->stream);
     }

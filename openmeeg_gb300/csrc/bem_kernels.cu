@@ -605,7 +605,8 @@ void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi
 // distances are shared.  Near pairs are appended to a list and recomputed
 // with the FP64 analytic kernels.
 // ===========================================================================
-constexpr int GREC = 64;   // floats per triangle: centroid (3 doubles), 16 offsets, normal, h, area (double)
+// floats per triangle: centroid (3 doubles), 16-point offsets, normal, h, area (double), 7-point offsets
+constexpr int GREC = kFarRecFloats, GREC_P7 = 64;
 // The 16-point rule of c_rules[3] rounded to FP32 (weights, barycentric nodes).
 __constant__ __align__(8) float c_w16[16] = {0.144315607677786f, 0.095091634267284f, 0.095091634267284f, 0.095091634267284f, 0.032458497623198f, 0.032458497623198f, 0.032458497623198f, 0.103217370534718f, 0.103217370534718f, 0.103217370534718f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f};
 __constant__ float c_b16[16][3] = {
@@ -625,6 +626,18 @@ __constant__ float c_b16[16][3] = {
     {0.008394777409957f, 0.263112829634639f, 0.728492392955404f},
     {0.263112829634639f, 0.008394777409957f, 0.728492392955404f},
     {0.263112829634639f, 0.728492392955404f, 0.008394777409957f}};
+// The 7-point rule of c_rules[2] rounded to FP32, for well-separated pairs; weights padded with a zero eighth
+// lane (the packed pair (6, 6) counts point 6 once).
+__constant__ __align__(8) float c_w7[8] = {0.2250f, 0.132394152788506f, 0.132394152788506f, 0.132394152788506f,
+                                           0.125939180544828f, 0.125939180544828f, 0.125939180544828f, 0.f};
+__constant__ float c_b7[7][3] = {{0.333333333333333f, 0.333333333333333f, 0.333333333333333f},
+                                 {0.470142064105115f, 0.470142064105115f, 0.059715871789770f},
+                                 {0.470142064105115f, 0.059715871789770f, 0.470142064105115f},
+                                 {0.059715871789770f, 0.470142064105115f, 0.470142064105115f},
+                                 {0.101286507323456f, 0.101286507323456f, 0.797426985353088f},
+                                 {0.101286507323456f, 0.797426985353088f, 0.101286507323456f},
+                                 {0.797426985353088f, 0.101286507323456f, 0.101286507323456f}};
+
 
 __global__ void prepare_gg_kernel(int64_t nt, const double* __restrict__ V, const int32_t* __restrict__ T,
                                   float* grec) {
@@ -647,6 +660,11 @@ __global__ void prepare_gg_kernel(int64_t nt, const double* __restrict__ V, cons
     g[57] = (float)fmax(dev::norm(p1 - p0), fmax(dev::norm(p2 - p1), dev::norm(p0 - p2)));
     reinterpret_cast<double*>(g + 58)[0] = 0.5 * nrm;
     g[60] = g[61] = g[62] = g[63] = 0.f;
+    for (int k = 0; k < 7; ++k) {
+        const d3 v = bary_point(c_rules[2][k], p0, p1, p2) - c;
+        g[GREC_P7 + 3 * k] = (float)v.x; g[GREC_P7 + 3 * k + 1] = (float)v.y; g[GREC_P7 + 3 * k + 2] = (float)v.z;
+    }
+    for (int k = GREC_P7 + 21; k < GREC; ++k) g[k] = 0.f;
 }
 
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s) {
@@ -698,6 +716,7 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
 }
 
 constexpr int FF_TI = 128, FF_TJ = 32;
+constexpr float kFarTier7 = 64.f;   // squared: pairs at >= 8 max edges take the 7-point rule
 
 // One thread per t1 row, looping over the CTA's FF_TJ staged t2 records.
 __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
@@ -751,41 +770,95 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
         const float dn2 = fmaf(fx, n2x, fmaf(fy, n2y, fz * n2z));
         const float dn1 = fmaf(fx, n1x, fmaf(fy, n1y, fz * n1z));
         const f2 DN2 = pk2(dn2, dn2), N2x = pk2(n2x, n2x), N2y = pk2(n2y, n2y), N2z = pk2(n2z, n2z);
-        f2 WD[8], A21[8];
+        float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f, u0 = 0.f, u1 = 0.f, u2 = 0.f;   // u: D21
+        if (dist2 >= kFarTier7 * hmax * hmax) {
+            // well separated (>= 8 max edges): the 7 x 7 product rule, within 1e-8 of the 16 x 16 one there;
+            // t1's 7 points from its record (L1), packed (0,1) (2,3) (4,5) (6,6) with a zero weight on the last lane
+            const f2* W7 = reinterpret_cast<const f2*>(c_w7);
+            const float* p7 = g1 + GREC_P7;
+            f2 Px[4], Py[4], Pz[4], WD7[4], A7[4];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            WD[k] = mul2(W[k], sub2(DN2, fma2(P1x[k], N2x, fma2(P1y[k], N2y, mul2(P1z[k], N2z)))));
-            A21[k] = pk2(0.f, 0.f);
-        }
-        float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f;
-        for (int q = 0; q < 16; ++q) {
-            const float qx = g2[6 + 3 * q], qy = g2[7 + 3 * q], qz = g2[8 + 3 * q];
-            const float yx = fx + qx, yy = fy + qy, yz = fz + qz;
-            const float wq = c_w16[q];
-            const float cq = -wq * (dn1 + fmaf(qx, n1x, fmaf(qy, n1y, qz * n1z)));
-            const f2 Yx = pk2(yx, yx), Yy = pk2(yy, yy), Yz = pk2(yz, yz), CQ = pk2(cq, cq);
-            f2 SQ = pk2(0.f, 0.f), K12 = pk2(0.f, 0.f);
+            for (int k = 0; k < 4; ++k) {
+                const int u = 2 * k, v = 2 * k + 1 < 7 ? 2 * k + 1 : 6;
+                Px[k] = pk2(p7[3 * u], p7[3 * v]);
+                Py[k] = pk2(p7[3 * u + 1], p7[3 * v + 1]);
+                Pz[k] = pk2(p7[3 * u + 2], p7[3 * v + 2]);
+                WD7[k] = mul2(W7[k], sub2(DN2, fma2(Px[k], N2x, fma2(Py[k], N2y, mul2(Pz[k], N2z)))));
+                A7[k] = pk2(0.f, 0.f);
+            }
+            const float* q7 = g2 + GREC_P7;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                const float qx = q7[3 * q], qy = q7[3 * q + 1], qz = q7[3 * q + 2];
+                const float wq = c_w7[q];
+                const float cq = -wq * (dn1 + fmaf(qx, n1x, fmaf(qy, n1y, qz * n1z)));
+                const f2 Yx = pk2(fx + qx, fx + qx), Yy = pk2(fy + qy, fy + qy), Yz = pk2(fz + qz, fz + qz),
+                         CQ = pk2(cq, cq);
+                f2 SQ = pk2(0.f, 0.f), K12 = pk2(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const f2 rx = sub2(Yx, Px[k]), ry = sub2(Yy, Py[k]), rz = sub2(Yz, Pz[k]);
+                    const f2 r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+                    const f2 ir = pk2(rsqrt_ftz(lo2(r2)), rsqrt_ftz(hi2(r2)));
+                    const f2 ir3 = mul2(mul2(ir, ir), ir);
+                    SQ = fma2(W7[k], ir, SQ);
+                    K12 = fma2(WD7[k], ir3, K12);
+                    A7[k] = fma2(CQ, ir3, A7[k]);
+                }
+                s = fmaf(wq, lo2(SQ) + hi2(SQ), s);
+                const float kq = wq * (lo2(K12) + hi2(K12));
+                e0 = fmaf(kq, c_b7[q][0], e0);
+                e1 = fmaf(kq, c_b7[q][1], e1);
+                e2 = fmaf(kq, c_b7[q][2], e2);
+            }
+            if (wantD21 || (same && wantD12)) {
+#pragma unroll
+                for (int p = 0; p < 7; ++p) {
+                    const float a = c_w7[p] * ((p & 1) ? hi2(A7[p / 2]) : lo2(A7[p / 2]));
+                    u0 = fmaf(a, c_b7[p][0], u0);
+                    u1 = fmaf(a, c_b7[p][1], u1);
+                    u2 = fmaf(a, c_b7[p][2], u2);
+                }
+            }
+        } else {
+            f2 WD[8], A21[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const f2 rx = sub2(Yx, P1x[k]), ry = sub2(Yy, P1y[k]), rz = sub2(Yz, P1z[k]);
-                const f2 r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
-                const f2 ir = pk2(rsqrt_ftz(lo2(r2)), rsqrt_ftz(hi2(r2)));
-                const f2 ir3 = mul2(mul2(ir, ir), ir);
-                SQ = fma2(W[k], ir, SQ);
-                K12 = fma2(WD[k], ir3, K12);
-                A21[k] = fma2(CQ, ir3, A21[k]);
+                WD[k] = mul2(W[k], sub2(DN2, fma2(P1x[k], N2x, fma2(P1y[k], N2y, mul2(P1z[k], N2z)))));
+                A21[k] = pk2(0.f, 0.f);
             }
-            s = fmaf(wq, lo2(SQ) + hi2(SQ), s);
-            const float kq = wq * (lo2(K12) + hi2(K12));
-            e0 = fmaf(kq, c_b16[q][0], e0);
-            e1 = fmaf(kq, c_b16[q][1], e1);
-            e2 = fmaf(kq, c_b16[q][2], e2);
-        }
-        float acc21[16];
+            for (int q = 0; q < 16; ++q) {
+                const float qx = g2[6 + 3 * q], qy = g2[7 + 3 * q], qz = g2[8 + 3 * q];
+                const float yx = fx + qx, yy = fy + qy, yz = fz + qz;
+                const float wq = c_w16[q];
+                const float cq = -wq * (dn1 + fmaf(qx, n1x, fmaf(qy, n1y, qz * n1z)));
+                const f2 Yx = pk2(yx, yx), Yy = pk2(yy, yy), Yz = pk2(yz, yz), CQ = pk2(cq, cq);
+                f2 SQ = pk2(0.f, 0.f), K12 = pk2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            acc21[2 * k] = lo2(A21[k]);
-            acc21[2 * k + 1] = hi2(A21[k]);
+                for (int k = 0; k < 8; ++k) {
+                    const f2 rx = sub2(Yx, P1x[k]), ry = sub2(Yy, P1y[k]), rz = sub2(Yz, P1z[k]);
+                    const f2 r2 = fma2(rx, rx, fma2(ry, ry, mul2(rz, rz)));
+                    const f2 ir = pk2(rsqrt_ftz(lo2(r2)), rsqrt_ftz(hi2(r2)));
+                    const f2 ir3 = mul2(mul2(ir, ir), ir);
+                    SQ = fma2(W[k], ir, SQ);
+                    K12 = fma2(WD[k], ir3, K12);
+                    A21[k] = fma2(CQ, ir3, A21[k]);
+                }
+                s = fmaf(wq, lo2(SQ) + hi2(SQ), s);
+                const float kq = wq * (lo2(K12) + hi2(K12));
+                e0 = fmaf(kq, c_b16[q][0], e0);
+                e1 = fmaf(kq, c_b16[q][1], e1);
+                e2 = fmaf(kq, c_b16[q][2], e2);
+            }
+            if (wantD21 || (same && wantD12)) {
+#pragma unroll
+                for (int p = 0; p < 16; ++p) {
+                    const float a = c_w16[p] * ((p & 1) ? hi2(A21[p / 2]) : lo2(A21[p / 2]));
+                    u0 = fmaf(a, c_b16[p][0], u0);
+                    u1 = fmaf(a, c_b16[p][1], u1);
+                    u2 = fmaf(a, c_b16[p][2], u2);
+                }
+            }
         }
         const double AA = A1 * reinterpret_cast<const double*>(g2 + 58)[0];
         if (wantS) {
@@ -801,16 +874,8 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
             o[0] = (double)e0 * AA; o[1] = (double)e1 * AA; o[2] = (double)e2 * AA;
         }
         if (wantD21 || (same && wantD12)) {
-            float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-#pragma unroll
-            for (int p = 0; p < 16; ++p) {
-                const float a = c_w16[p] * acc21[p];
-                f0 = fmaf(a, c_b16[p][0], f0);
-                f1 = fmaf(a, c_b16[p][1], f1);
-                f2 = fmaf(a, c_b16[p][2], f2);
-            }
             double* o = same ? d12 + (j * n2 + i) * 3 : d21 + (j * n1 + i) * 3;
-            o[0] = (double)f0 * AA; o[1] = (double)f1 * AA; o[2] = (double)f2 * AA;
+            o[0] = (double)u0 * AA; o[1] = (double)u1 * AA; o[2] = (double)u2 * AA;
         }
     }
 }

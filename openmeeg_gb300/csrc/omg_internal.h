@@ -38,6 +38,7 @@ constexpr int SREC = 28;   // OperatorS data: p0 p1 p2 n area len[3] en[3] (25 u
 constexpr int PREC = 32;   // P1SingleLayerPotential data: p0 p1 p2 n area D[3] U[3] (31 used)
 constexpr int QREC = 52;   // 16 quadrature points (48) + area (1), order-3 rule
 constexpr int MAXQ = 16;
+constexpr int kFarRecFloats = 96;   // floats per triangle of the mixed far-field records (GREC)
 
 // --------------------------------------------------------------------------
 // Host geometry: restates OpenMEEG's Geometry bookkeeping for meshes given as
