@@ -1,0 +1,67 @@
+"""The two tiers of the mixed far field: pairs whose centroids are at least 8
+of their largest edges apart are integrated with the 7 x 7 product rule, the
+others with the 16 x 16 one.  On pairs of the config1 head beyond that
+distance the 7 x 7 rule reproduces the 16 x 16 one far below FP32 rounding:
+single layer within 1e-8 relative, double layer (both directions) within 2e-8
+of the sum of the absolute terms.  The rules are read from the kernel's own
+constant tables."""
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "..", "openmeeg_gb300", "csrc", "bem_kernels.cu")
+
+
+def _rules():
+    src = open(SRC).read()
+    i = src.index("c_rules[4][16][4] = {")
+    nums = [float(x) for x in re.findall(r"-?\d+\.\d+", src[i:src.index("};", i)])]
+    orders = []
+    pos = 0
+    for n in (3, 6, 7, 16):
+        orders.append(np.array(nums[pos:pos + 4 * n]).reshape(n, 4))
+        pos += 4 * n
+    return orders[2], orders[3]
+
+
+def _integrals(P, nrm, a, b, R):
+    pa, pb = R[:, :3] @ P[a], R[:, :3] @ P[b]
+    w = R[:, 3][:, None] * R[:, 3][None, :]
+    r = pb[None, :, :] - pa[:, None, :]
+    d = np.linalg.norm(r, axis=2)
+    s = (w / d).sum()
+    t2 = w * (r @ nrm[b]) / d ** 3          # double layer of t2 seen from t1's points
+    t1 = w * (r @ nrm[a]) / d ** 3          # ... and of t1 seen from t2's points
+    return s, t2.sum(), np.abs(t2).sum(), t1.sum(), np.abs(t1).sum()
+
+
+def test_far_tier_rule_matches_16_point_rule():
+    from openmeeg_gb300 import workloads
+    R7, R16 = _rules()
+    assert R7.shape == (7, 4) and R16.shape == (16, 4)
+    assert abs(R7[:, 3].sum() - 1) < 1e-12 and abs(R16[:, 3].sum() - 1) < 1e-12
+    head = workloads.config1().head
+    rng = np.random.default_rng(3)
+    worst_s = worst_d = 0.0
+    n = 0
+    for m in range(len(head.triangles)):
+        V, T = head.vertices[m], head.triangles[m]
+        P = V[T]
+        nrm = np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0])
+        nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+        h = np.max(np.linalg.norm(P - np.roll(P, 1, axis=1), axis=2), axis=1)
+        cen = P.mean(axis=1)
+        for _ in range(4000):
+            a, b = rng.integers(0, len(T), 2)
+            if np.linalg.norm(cen[a] - cen[b]) < 8.0 * max(h[a], h[b]):
+                continue
+            s7, d7, _, e7, _ = _integrals(P, nrm, a, b, R7)
+            s16, d16, dabs, e16, eabs = _integrals(P, nrm, a, b, R16)
+            worst_s = max(worst_s, abs(s7 - s16) / abs(s16))
+            worst_d = max(worst_d, abs(d7 - d16) / dabs, abs(e7 - e16) / eabs)
+            n += 1
+    assert n > 5000
+    assert worst_s < 1e-8, worst_s
+    assert worst_d < 2e-8, worst_d
