@@ -196,8 +196,8 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
     library's stream).
 
     Algorithmic work:
-      residual_tc -- R = B - A X from fixed-point digits on the tensor cores: 7 x 7 bf16
-        digit planes, 28 digit pairs up to level 8, each an N x N x k_pad integer GEMM
+      residual_tc -- R = B - A X from fixed-point digits on the tensor cores: 6 + 6 bf16
+        digit planes, 21 digit pairs up to level 7, each an N x N x k_pad integer GEMM
         (k_pad = k rounded up to 128); the FP64-equivalent work is 2 N^2 k.
       residual_df64 -- R = B - A X in double-float arithmetic: reads the float-pair
         head matrix (8 N^2 bytes), X pairs (8 N k), B (8 N k), writes R (8 N k);
@@ -213,9 +213,9 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
     per_step = launches / steps
     info = {"kernel": name, "launches_per_step": per_step, "mean_launch_ms": ms / launches}
     if name == "residual_tc":
-        # R = B - A X from 7 + 7 bf16 digit planes, 28 digit pairs (levels <= 8): every pair is a full
+        # R = B - A X from 6 + 6 bf16 digit planes, 21 digit pairs (levels <= 7): every pair is a full
         # N x N x k integer GEMM on the tensor cores, padded to 128-column tiles of the k right-hand sides
-        pairs = 28
+        pairs = 21
         kpad = (k + 127) // 128 * 128
         flops = 2.0 * N * N * kpad * pairs
         achieved = flops / t_launch / 1e12
@@ -228,7 +228,7 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
                                      "column blocks share digit tiles in L2",
                      "algorithmic_fp64_equivalent_flops_per_launch": 2.0 * N * N * k,
                      "executed_bf16_flops_per_launch": flops,
-                     "note": f"executed bf16 tensor flops (28 exact digit-pair GEMMs, k padded to {kpad}) vs "
+                     "note": f"executed bf16 tensor flops (21 exact digit-pair GEMMs, k padded to {kpad}) vs "
                              f"{kind} bf16 burst peak"})
     elif name == "residual_df64":
         nbytes = 8.0 * N * N + 24.0 * N * k

@@ -1085,21 +1085,21 @@ void gain_contract(const std::vector<std::pair<int64_t, int64_t>>& merged, const
     for (const auto& r : merged) kdim += r.second - r.first;
     const int64_t k = ne + nm;
     if (precision == OMG_PREC_MIXED && nd > 0 && k > 0 && kdim > 0 && merged.size() <= 8) {
-        // FP64-accurate contraction on the tensor cores from fixed-point digits of Y^T and DSM
-        // (7 digits of 7 bits each, levels <= 8), over the source rows only
-        const int nd7 = 7, beta = 7, lmax = 8;
+        // FP64-level contraction on the tensor cores from fixed-point digits of Y^T and DSM (the solver's
+        // digits: 6 of 7 bits each, pairs up to level 7), over the source rows only
+        const int ndg = 6, beta = 7, lmax = 7;
         const int64_t ld = digits_ld(kdim), ndpad = (nd + 127) / 128 * 128;
-        DevBuf Ad((size_t)nd7 * k * ld * 2, s), Xd((size_t)nd7 * ndpad * ld * 2, s);
+        DevBuf Ad((size_t)ndg * k * ld * 2, s), Xd((size_t)ndg * ndpad * ld * 2, s);
         DevBuf ex((size_t)(k + ndpad) * sizeof(int), s), G((size_t)k * nd * 8, s);
         int* rexp = ex.as<int>();
         int* cexp = rexp + k;
         double* g = G.as<double>();
-        digits_columns(Y, kdim, k, N, nd7, beta, k, ld, Ad.p, rexp, s, &merged);
-        digits_columns(DSM, kdim, nd, N, nd7, beta, ndpad, ld, Xd.p, cexp, s, &merged);
+        digits_columns(Y, kdim, k, N, ndg, beta, k, ld, Ad.p, rexp, s, &merged);
+        digits_columns(DSM, kdim, nd, N, ndg, beta, ndpad, ld, Xd.p, cexp, s, &merged);
         OMG_CUDA(cudaMemsetAsync(g, 0, (size_t)k * nd * 8, s));
         if (nm > 0)   // MEG rows start from DipSource2MEGMat
             OMG_CUDA(cudaMemcpy2DAsync(g + ne, k * 8, gmeg, nm * 8, nm * 8, nd, cudaMemcpyDeviceToDevice, s));
-        digit_gemm(k, nd, kdim, Ad.p, nd7, rexp, Xd.p, nd7, ndpad, cexp, beta, lmax, g, k, 1.0, g, k, err, s,
+        digit_gemm(k, nd, kdim, Ad.p, ndg, rexp, Xd.p, ndg, ndpad, cexp, beta, lmax, g, k, 1.0, g, k, err, s,
                    "gain_tc");
         if (ne > 0) OMG_CUDA(cudaMemcpy2DAsync(geeg, ne * 8, g, k * 8, ne * 8, nd, cudaMemcpyDeviceToDevice, s));
         if (nm > 0) OMG_CUDA(cudaMemcpy2DAsync(gmeg, nm * 8, g + ne, k * 8, nm * 8, nd, cudaMemcpyDeviceToDevice, s));

@@ -29,7 +29,10 @@ struct omg_solver_s {
     bool tc_residual = true;
     int residual_choice = -1;               // -1: decide at factorization (memory, OMG_RESIDUAL); 0/1: given
     DevBuf Adig, rexp;
-    int nda = 7, ndx = 7, beta = 7, lmax = 8;
+    // 6 digits of 7 bits per operand, digit pairs up to level 7 (21 pairs): residual entries within ~2^-42 of
+    // n max|A_i.| max|X_.c| -- below what a plain FP64 product accumulates over n ~ 1e4-1e5 terms, and far below
+    // what one refinement step needs (its correction is ~1e-4 of x)
+    int nda = 6, ndx = 6, beta = 7, lmax = 7;
     bool persistent = false;                // outlives the call that made it (public solver handle)
     double refine_tol = 1e-6;               // stop when corrections are this small relative to x
     int max_refine = 10;
