@@ -186,6 +186,11 @@ struct StreamSwap {
 
 void ensure_aux(omg_context ctx) {
     if (!ctx->aux) OMG_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+    if (!ctx->hi) {
+        int least = 0, greatest = 0;
+        OMG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        OMG_CUDA(cudaStreamCreateWithPriority(&ctx->hi, cudaStreamNonBlocking, greatest));
+    }
     if (!ctx->ev_a) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_a, cudaEventDisableTiming));
     if (!ctx->ev_b) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_b, cudaEventDisableTiming));
 }
@@ -2009,9 +2014,10 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * geo->h.nt * 8, s);
     OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
     if (precision == OMG_PREC_MIXED) ensure_gg_tables(geo);
-    // The sources (sensor right-hand sides, DipSourceMat, DipSource2MEGMat) do not depend on the head matrix:
-    // they are enqueued first, on the second stream, and run while the main stream assembles the head matrix
-    // (whose FP64 near pairs leave the FP32 pipes free); the main stream joins them before the factorization.
+    // The sources do not depend on the head matrix.  The sensor right-hand sides are enqueued first on the
+    // second stream (joined before the solves); the DipSourceMat and DipSource2MEGMat go to the second stream
+    // after the factorization and run under the latency-bound chains of the FP32 solves, which leave most SMs
+    // idle (joined before the contraction).
     ensure_aux(ctx);
     cudaStream_t s2 = ctx->aux;
     OMG_CUDA(cudaEventRecord(ev[5], s));
@@ -2034,8 +2040,6 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
         } else if (nm > 0) {
             launch_h2mm(geo->d, sq, nm, geo->tmesh, geo->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s2);
         }
-        dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, nullptr, 0, &dom);
-        if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s2);
         OMG_CUDA(cudaEventRecord(ev[6], s2));
     }
     DevBuf hm = assemble_system(geo, hm_it, precision, false);
@@ -2044,7 +2048,23 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaEventRecord(ev[2], s));
     solver_factor(sv.get(), std::move(hm));
     OMG_CUDA(cudaEventRecord(ev[3], s));
-    solver_solve_internal(sv.get(), B.as<double>(), N, k);
+    {   // after the factorization's last work on the second stream (stream order)
+        StreamSwap on_aux(ctx, s2);
+        dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, nullptr, 0, &dom);
+        if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s2);
+        OMG_CUDA(cudaEventRecord(ev[6], s2));
+    }
+    {   // the solves on the highest-priority stream, ordered after the main stream's work and back
+        OMG_CUDA(cudaEventRecord(ev[5], s));
+        OMG_CUDA(cudaStreamWaitEvent(ctx->hi, ev[5], 0));
+        {
+            StreamSwap on_hi(ctx, ctx->hi);
+            solver_solve_internal(sv.get(), B.as<double>(), N, k);
+            OMG_CUDA(cudaEventRecord(ev[5], ctx->hi));
+        }
+        OMG_CUDA(cudaStreamWaitEvent(s, ev[5], 0));
+    }
+    OMG_CUDA(cudaStreamWaitEvent(s, ev[6], 0));
     // the factor is not needed past the solves: its memory (the FP32 factor, its copies and the digit planes,
     // most of the device at the largest heads) is returned before the contraction allocates its digits
     const int sv_steps = sv->last_steps;

@@ -27,9 +27,14 @@ struct omg_context_s {
     // second stream and two events of the factorization's look-ahead (created on first use)
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    // highest-priority stream of the latency-bound solve chains (their CTAs go first onto SMs that free up
+    // while other work runs on the second stream; created on first use)
+    cudaStream_t hi = nullptr;
 };
 
 inline void release_aux(omg_context_s* c) {
+    if (c->hi) cudaStreamDestroy(c->hi);
+    c->hi = nullptr;
     if (c->aux) cudaStreamDestroy(c->aux);
     if (c->ev_a) cudaEventDestroy(c->ev_a);
     if (c->ev_b) cudaEventDestroy(c->ev_b);
