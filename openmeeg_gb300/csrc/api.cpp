@@ -128,7 +128,8 @@ void ratio_max(int64_t n, const double* num, const double* den, double* out, cud
 int64_t digits_ld(int64_t n);
 void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta, int64_t rows_per_plane,
                     int64_t ldo, void* out, int* ex, cudaStream_t s,
-                    const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr);
+                    const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr, float* lower32 = nullptr,
+                    int64_t ld32 = 0);
 void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
                 int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double sgn, double* R,
                 int64_t ldr, int* err, cudaStream_t s, const char* prof_name);
@@ -826,7 +827,6 @@ void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
     } else {
         sv->ld32 = (N + 31) / 32 * 32;
         sv->A32 = DevBuf((size_t)sv->ld32 * N * sizeof(float), s, sv->persistent);
-        copy_convert<double, float>(N, N, hm.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
         symmetrize(hm.as<double>(), N, N, s);
         const char* mode = std::getenv("OMG_RESIDUAL");
         sv->tc_residual = sv->residual_choice >= 0 ? sv->residual_choice == 1
@@ -846,9 +846,12 @@ void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
             const int64_t ldd = digits_ld(N);
             sv->Adig = DevBuf((size_t)sv->nda * N * ldd * 2, s, sv->persistent);
             sv->rexp = DevBuf((size_t)N * sizeof(int), s, sv->persistent);
-            digits_columns(hm.as<double>(), N, N, N, sv->nda, sv->beta, N, ldd, sv->Adig.p, sv->rexp.as<int>(), s);
+            // (the same pass over the columns writes the FP32 lower triangle to be factored)
+            digits_columns(hm.as<double>(), N, N, N, sv->nda, sv->beta, N, ldd, sv->Adig.p, sv->rexp.as<int>(), s,
+                           nullptr, sv->A32.as<float>(), sv->ld32);
         } else {
             // ... or as an exact float pair (hi + lo) for the double-float residual
+            copy_convert<double, float>(N, N, hm.as<double>(), N, sv->A32.as<float>(), sv->ld32, true, 1.0f, s);
             sv->A64 = DevBuf((size_t)2 * N * N * sizeof(float), s, sv->persistent);
             split_f64(N, N, hm.as<double>(), N, sv->A64.as<float>(), sv->A64.as<float>() + (size_t)N * N, N, s);
         }

@@ -298,13 +298,15 @@ __device__ __forceinline__ unsigned short small_int_bf16(long long r) {
 // n <= j < ldo.  Columns c >= ncol (up to rows_per_plane) are zero.  One CTA
 // per column, four consecutive rows per thread (8-byte stores per plane);
 // integer arithmetic only (the largest magnitude by its bit pattern, the
-// scaling and rounding on the significand).
+// scaling and rounding on the significand).  Optionally also writes the
+// column's entries on and below the diagonal, rounded to FP32, to lower32.
 constexpr int DG_THREADS = 256;
 
 __global__ void __launch_bounds__(DG_THREADS) digits_kernel(const double* __restrict__ M, int64_t n, int64_t ncol,
                                                             int64_t ldm, int nd, int beta, int64_t rows_per_plane,
                                                             int64_t ldo, __nv_bfloat16* out, int* ex,
-                                                            const __grid_constant__ RowRanges rr) {
+                                                            const __grid_constant__ RowRanges rr, float* lower32,
+                                                            int64_t ld32) {
     __shared__ unsigned long long red[DG_THREADS / 32];
     __shared__ int s_e;
     const int64_t c = blockIdx.x;
@@ -348,7 +350,11 @@ __global__ void __launch_bounds__(DG_THREADS) digits_kernel(const double* __rest
     for (int64_t j0 = 4 * threadIdx.x; j0 < ldo; j0 += 4 * DG_THREADS) {
         long long Y[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) Y[u] = j0 + u < n ? scaled_rn(at(j0 + u), k) : 0;
+        for (int u = 0; u < 4; ++u) {
+            const double x = j0 + u < n ? at(j0 + u) : 0.0;
+            Y[u] = j0 + u < n ? scaled_rn(x, k) : 0;
+            if (lower32 && j0 + u >= c && j0 + u < n) lower32[j0 + u + c * ld32] = (float)x;   // lower triangle
+        }
         for (int d = nd - 1; d >= 0; --d) {
             unsigned int h[4];
 #pragma unroll
@@ -377,10 +383,12 @@ int64_t digits_ld(int64_t n) { return (n + 63) / 64 * 64; }
 
 void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int nd, int beta, int64_t rows_per_plane,
                     int64_t ldo, void* out, int* ex, cudaStream_t s,
-                    const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr) {
+                    const std::vector<std::pair<int64_t, int64_t>>* ranges = nullptr, float* lower32 = nullptr,
+                    int64_t ld32 = 0) {
     if (rows_per_plane <= 0) return;
     if (nd < 1 || nd * beta > 62 || beta < 2 || beta > 8 || ldo % 4 || ldo < n)
         throw Error(OMG_ERR_INVALID, "digits: bad digit layout");
+    if (lower32 && (ranges || ld32 < n)) throw Error(OMG_ERR_INVALID, "digits: FP32 copy of a full square matrix only");
     ProfScope prof_("digits", s);
     tcr::RowRanges rr{};
     if (ranges) {
@@ -395,7 +403,7 @@ void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int n
     }
     tcr::digits_kernel<<<(unsigned)rows_per_plane, tcr::DG_THREADS, 0, s>>>(M, n, ncol, ldm, nd, beta, rows_per_plane,
                                                                            ldo, static_cast<__nv_bfloat16*>(out), ex,
-                                                                           rr);
+                                                                           rr, lower32, ld32);
     check_tcr("digits");
 }
 
