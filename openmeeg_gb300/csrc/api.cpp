@@ -119,7 +119,9 @@ void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
 void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
-               float* Bl, cudaStream_t s);
+               float* Bl, cudaStream_t s, bool store_l = true);
+void diag_update(float* A, int64_t lda, int n, const float* P0h, const float* P0l, const float* P1h, const float* P1l,
+                 cudaStream_t s);
 void apply_inv_blocks(int64_t nblocks, int nb, int n_last, int64_t ncol, const float* Li, bool trans, float* B,
                       int64_t ldb, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
@@ -192,8 +194,8 @@ void ensure_aux(omg_context ctx) {
         OMG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         OMG_CUDA(cudaStreamCreateWithPriority(&ctx->hi, cudaStreamNonBlocking, greatest));
     }
-    if (!ctx->ev_a) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_a, cudaEventDisableTiming));
-    if (!ctx->ev_b) OMG_CUDA(cudaEventCreateWithFlags(&ctx->ev_b, cudaEventDisableTiming));
+    for (cudaEvent_t* e : {&ctx->ev_a, &ctx->ev_b, &ctx->ev_c, &ctx->ev_d, &ctx->ev_e})
+        if (!*e) OMG_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
 }
 
 void release_geometry(omg_geometry geo) {
@@ -593,17 +595,28 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     DevBuf T((size_t)2 * std::max<int64_t>(1, N) * nb * sizeof(float), s);   // A21 split, K-major
     DevBuf Bi((size_t)2 * nblocks * nb * nb * sizeof(float), s);             // L11^-1 split, K-major, per block
     float* Th = T.as<float>();
-    // Look-ahead: the trailing update of panel b is split into the next panel's columns (on the
-    // main stream, so panel b+1 can be factored at once) and the rest (on the second stream, with a
-    // few SMs left free), so the latency-bound diagonal-block work of panel b+1 overlaps the bulk
-    // of the update of panel b.  ev_a: panel b's split copies are ready; ev_b: the rest of the
-    // update of panel b-1 is done (the next panel's columns of step b lie inside it).
+    // Three streams.  The chain of diagonal blocks and panel solves runs on the highest-priority
+    // stream (sc).  The look-ahead updates of the next panels' columns run on the main stream (s):
+    // the rows below the next diagonal block, while the chain updates that block by the latest panels
+    // itself (a small FP32 kernel) and factors it.  The rest of each group's trailing update
+    // runs on the second stream (s2) with a few SMs left free for the other two.
+    //   ev_p (sc): the latest panel solve is done (its W rows are ready)
+    //   ev_l (s):  the rows below the next diagonal block and their A21 split are ready
+    //   ev_g (s):  the look-ahead update of the next group's second panel is done
+    //   ev_r (s2): the rest update of the previous group is done
     ensure_aux(sv->ctx);
-    cudaStream_t s2 = sv->ctx->aux;
-    cudaEvent_t ev_w = sv->ctx->ev_a, ev_r = sv->ctx->ev_b;
+    cudaStream_t s2 = sv->ctx->aux, sc = sv->ctx->hi;
+    cudaEvent_t ev_r = sv->ctx->ev_b, ev_p = sv->ctx->ev_c, ev_l = sv->ctx->ev_d, ev_g = sv->ctx->ev_e;
+    OMG_CUDA(cudaEventRecord(ev_l, s));   // the head matrix is ready
+    OMG_CUDA(cudaStreamWaitEvent(sc, ev_l, 0));
     bool rest_pending = false;
-    const int reserve = 24;   // SMs the rest update leaves to the panel chain (measured optimum at config1)
-    bool have_t = false;     // Th/Tl already hold this panel's A21 split (written by the update before it)
+    const int reserve = 24;   // SMs the rest update leaves to the chain and the look-ahead (config1 sweep: 16-24
+                              // best, 32 +0.2 ms, 48 +1.1 ms)
+    bool have_t = false;     // Th/Tl hold this panel's A21 split (written by the look-ahead update on s)
+    bool wait_g = false;     // the group's second diagonal block waits for its look-ahead update (ev_g)
+    bool g_recorded = false; // ev_g recorded in this call (a wait on an older record would cross a graph capture)
+    const float* fp[4] = {nullptr, nullptr, nullptr, nullptr};   // panels (heads, remainders) whose update
+                                                                  // of the next diagonal block is pending
     // fold of block row b for the backward solves (block row <- Linv_b x block row, heads in A, remainders in
     // A32r); run after the factorization (interleaved with the rest updates it delayed the panel chain)
     auto fold_rows = [&](size_t b, cudaStream_t st) {
@@ -625,77 +638,120 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     auto wl = [&](size_t p) { return wh(p) + (N - sv->bounds[p + 1]) * nb; };
     // C -= sum over the group's panels of W_p(rows from r0) W_p(rows from c0)^T (one or two K segments)
     auto group_update = [&](size_t gb, size_t ge, int64_t M, int64_t Nc, int64_t r0, int64_t c0, float* C, bool lower,
-                            cudaStream_t st, const char* name, int max_ctas, float* Sh, float* Sl, int64_t s_row0) {
+                            cudaStream_t st, const char* name, int max_ctas, float* Sh, float* Sl, int64_t s_row0,
+                            bool pdl) {
         const int64_t o1 = sv->bounds[gb + 1], nk1 = o1 - sv->bounds[gb];
         if (ge - gb == 1) {
             gemm_tf32x3(M, Nc, nk1, -1.f, wh(gb) + (r0 - o1) * nb, wl(gb) + (r0 - o1) * nb, nb, nb, 0,
                         wh(gb) + (c0 - o1) * nb, wl(gb) + (c0 - o1) * nb, nb, nb, 0, 1.f, C, ld, lower, sv->ctx->d_err,
-                        st, name, max_ctas, Sh, Sl, s_row0, nb, nullptr, nullptr, nullptr, 0, st == s);
+                        st, name, max_ctas, Sh, Sl, s_row0, nb, nullptr, nullptr, nullptr, 0, pdl);
         } else {
             const int64_t o2 = sv->bounds[gb + 2], nk2 = o2 - o1;
             gemm_tf32x3_pair(M, Nc, -1.f, nk1, wh(gb) + (r0 - o1) * nb, wl(gb) + (r0 - o1) * nb, nb,
                              wh(gb) + (c0 - o1) * nb, wl(gb) + (c0 - o1) * nb, nb, nk2, wh(gb + 1) + (r0 - o2) * nb,
                              wl(gb + 1) + (r0 - o2) * nb, nb, wh(gb + 1) + (c0 - o2) * nb, wl(gb + 1) + (c0 - o2) * nb,
-                             nb, 1.f, C, ld, lower, sv->ctx->d_err, st, name, max_ctas, Sh, Sl, s_row0, nb, st == s);
+                             nb, 1.f, C, ld, lower, sv->ctx->d_err, st, name, max_ctas, Sh, Sl, s_row0, nb, pdl);
         }
     };
     for (size_t g = 0; g + 1 < groups.size(); ++g) {
         const size_t gb = groups[g], ge = groups[g + 1];
         if (sv->bounds[gb] == nP) {   // continue on -(vertex Schur complement): every pending update must be in
-            if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
-            rest_pending = false;
-            negate_lower<float>(A + nP + nP * ld, ld, N - nP, s);
+            if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(sc, ev_r, 0));
+            OMG_CUDA(cudaStreamWaitEvent(sc, ev_l, 0));
+            if (g_recorded) OMG_CUDA(cudaStreamWaitEvent(sc, ev_g, 0));
+            negate_lower<float>(A + nP + nP * ld, ld, N - nP, sc);
             have_t = false;
+            wait_g = false;
+            for (auto& q : fp) q = nullptr;
         }
         for (size_t b = gb; b < ge; ++b) {
             const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
-            // L11 and L11^-1 (the inverse also serves the solves)
+            // L11 and L11^-1 (the inverse also serves the solves), after the pending panel updates
+            if (b == gb + 1 && wait_g) OMG_CUDA(cudaStreamWaitEvent(sc, ev_g, 0));
             float* Bih = Bi.as<float>() + 2 * b * nb * nb;
             float* Bil = Bih + (size_t)nb * nb;
+            if (fp[0]) diag_update(A + k0 + k0 * ld, ld, (int)nk, fp[0], fp[1], fp[2], fp[3], sc);
             potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
-                      sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, s);
+                      sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, sc, false);
+            for (auto& q : fp) q = nullptr;
             if (m == 0) continue;
             // L21 = A21 L11^-T on the tensor cores, written as heads (A) + remainders (A32r); its epilogue
             // also writes the K-major split of L21 (W, kept for the trailing updates and the forward solves)
             float* Tl = Th + m * nb;
-            if (!have_t) split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, s);
+            if (!have_t)
+                split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, sc);
+            else
+                OMG_CUDA(cudaStreamWaitEvent(sc, ev_l, 0));
             gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
-                        sv->ctx->d_err, s, "gemm_panel", 0, wh(b), wl(b), 0, nb, Ar + k1 + k0 * ld, nullptr, nullptr, 0,
-                        true);
+                        sv->ctx->d_err, sc, "gemm_panel", 0, wh(b), wl(b), 0, nb, Ar + k1 + k0 * ld, nullptr, nullptr,
+                        0, true);
+            OMG_CUDA(cudaEventRecord(ev_p, sc));
             have_t = false;
-            if (b + 1 < ge) {   // the group's second panel (all rows below k1), with its A21 split
+            if (b + 1 < ge) {   // the group's second panel: the chain updates its diagonal block by this panel,
+                                // the rows below it (with their A21 split) are updated beside it on s
                 const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
-                gemm_tf32x3(m, nn, nk, -1.f, wh(b), wl(b), nb, nb, 0, wh(b), wl(b), nb, nb, 0, 1.f,
-                            A + k1 + k1 * ld, ld, false, sv->ctx->d_err, s, "gemm_next", 0, mr > 0 ? Th : nullptr,
-                            mr > 0 ? Th + mr * nb : nullptr, nn, nb);
-                have_t = mr > 0;
+                if (mr > 0) {
+                    OMG_CUDA(cudaStreamWaitEvent(s, ev_p, 0));
+                    gemm_tf32x3(mr, nn, nk, -1.f, wh(b) + (k2 - k1) * nb, wl(b) + (k2 - k1) * nb, nb, nb, 0, wh(b),
+                                wl(b), nb, nb, 0, 1.f, A + k2 + k1 * ld, ld, false, sv->ctx->d_err, s, "gemm_next", 0,
+                                Th, Th + mr * nb, 0, nb, nullptr, nullptr, nullptr, 0, true);
+                    OMG_CUDA(cudaEventRecord(ev_l, s));
+                    have_t = true;
+                }
+                fp[0] = wh(b);
+                fp[1] = wl(b);
             }
         }
         if (ge == nblocks) break;
-        // look-ahead: the next group's columns (all rows below their start), after the rest update of the
-        // previous group, on the main stream; the first one's rows below its diagonal block are also written
-        // as its A21 split unless the next group starts the vertex part (negated first)
+        // look-ahead on s: the next group's columns, after the group's last panel and the rest update of
+        // the previous group (whose region holds them); the chain waits for that rest update too, before
+        // the next one is queued on the same event
         const size_t ng = groups[g + 2];
-        if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
+        OMG_CUDA(cudaStreamWaitEvent(s, ev_p, 0));
+        if (rest_pending) {
+            OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
+            OMG_CUDA(cudaStreamWaitEvent(sc, ev_r, 0));
+        }
         rest_pending = false;
+        const bool split_diag = sv->bounds[ge] != nP;   // the vertex part is negated as a whole first
+        wait_g = false;
         for (size_t p = ge; p < ng; ++p) {
-            const int64_t kp0 = sv->bounds[p], kp1 = sv->bounds[p + 1], M = N - kp0, w = kp1 - kp0;
-            const bool fuse_t = p == ge && N - kp1 > 0 && kp0 != nP;
-            group_update(gb, ge, M, w, kp0, kp0, A + kp0 + kp0 * ld, false, s, "gemm_next", 0,
-                         fuse_t ? Th : nullptr, fuse_t ? Th + (N - kp1) * nb : nullptr, w);
-            if (p == ge) have_t = fuse_t;
+            const int64_t kp0 = sv->bounds[p], kp1 = sv->bounds[p + 1], w = kp1 - kp0;
+            if (p == ge && split_diag) {   // rows below the diagonal block, with their A21 split
+                const int64_t Mr = N - kp1;
+                if (Mr > 0)
+                    group_update(gb, ge, Mr, w, kp1, kp0, A + kp1 + kp0 * ld, false, s, "gemm_next", 0, Th,
+                                 Th + Mr * nb, 0, true);
+                have_t = Mr > 0;
+            } else {
+                group_update(gb, ge, N - kp0, w, kp0, kp0, A + kp0 + kp0 * ld, false, s, "gemm_next", 0, nullptr,
+                             nullptr, 0, true);
+                if (p == ge) have_t = false;
+            }
+            OMG_CUDA(cudaEventRecord(p == ge ? ev_l : ev_g, s));
+            if (p > ge) wait_g = g_recorded = true;
+        }
+        if (split_diag) {   // the update of the next diagonal block by this group's panels
+            const int64_t kc = sv->bounds[ge];
+            fp[0] = wh(gb) + (kc - sv->bounds[gb + 1]) * nb;
+            fp[1] = wl(gb) + (kc - sv->bounds[gb + 1]) * nb;
+            if (ge - gb == 2) {
+                fp[2] = wh(gb + 1) + (kc - sv->bounds[gb + 2]) * nb;
+                fp[3] = wl(gb + 1) + (kc - sv->bounds[gb + 2]) * nb;
+            }
         }
         // the rest, on the second stream
         const int64_t kr = sv->bounds[ng], mr = N - kr;
         if (mr > 0) {
-            OMG_CUDA(cudaEventRecord(ev_w, s));
-            OMG_CUDA(cudaStreamWaitEvent(s2, ev_w, 0));
+            OMG_CUDA(cudaStreamWaitEvent(s2, ev_p, 0));
             group_update(gb, ge, mr, mr, kr, kr, A + kr + kr * ld, true, s2, "gemm_syrk", std::max(1, n_sm() - reserve),
-                         nullptr, nullptr, 0);
+                         nullptr, nullptr, 0, false);
             OMG_CUDA(cudaEventRecord(ev_r, s2));
             rest_pending = true;
         }
     }
+    OMG_CUDA(cudaEventRecord(ev_p, sc));
+    OMG_CUDA(cudaStreamWaitEvent(s, ev_p, 0));
     if (rest_pending) OMG_CUDA(cudaStreamWaitEvent(s, ev_r, 0));
     // Fold the diagonal-block inverses into the solve operators, in place (each tile of these products
     // reads only the rows of W, or the columns of the block row, that it writes):
@@ -708,8 +764,8 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     split_cols(nb, (int64_t)nblocks * nb, nb, sv->Linv32.as<float>(), nb, LCh, LCl, s);
     // the panel folds on the main stream, the block-row folds on the second one: disjoint memory, and each
     // product is a few latency-bound waves, so two at a time fill the GPU
-    OMG_CUDA(cudaEventRecord(ev_w, s));
-    OMG_CUDA(cudaStreamWaitEvent(s2, ev_w, 0));
+    OMG_CUDA(cudaEventRecord(ev_l, s));
+    OMG_CUDA(cudaStreamWaitEvent(s2, ev_l, 0));
     for (size_t b = 0; b < nblocks; ++b) {
         const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
         if (m > 0)

@@ -656,7 +656,9 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 // then the off-diagonal blocks of the inverse, X_IJ = -X_II sum_{K=J}^{I-1}
 // L_IK X_KJ, block row by block row.  The block lives in shared memory
 // (row-major, padded); columns past n act as the identity.
-// Outputs: L11 over A11 (lower), Linv column-major (ldi = 128, zero above the
+
+// Outputs: L11 over A11 (lower; left out when store_l is false: the
+// factorization's solves use only the inverse), Linv column-major (ldi = 128, zero above the
 // diagonal and beyond n) for the solves, and Linv as TF32 head/remainder
 // K-major rows (128 x 128 each, zero padded) for the tensor-core panel solve
 // L21 = A21 Linv^T.  A pivot that is not positive is reported as
@@ -668,7 +670,7 @@ constexpr size_t PI_SMEM =
 
 __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
                                                                int64_t* err_col, int64_t col_offset, float* Linv,
-                                                               float* Bh, float* Bl) {
+                                                               float* Bh, float* Bl, int store_l) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float* sA = reinterpret_cast<float*>(smraw);   // 128 x PI_LD row-major: A, then L
     float* sX = sA + PI_NB * PI_LD;                 // 128 x PI_LD row-major: X = L^-1
@@ -678,7 +680,7 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
     float* sCol = sInv + PI_NB;                     // 2 x 32: column broadcast of the diagonal factor
     const unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-#pragma unroll 8
+#pragma unroll 16
     for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // 32 iterations: loads batched by the unroll
         const int r = e % PI_NB, c = e / PI_NB;    // coalesced down the columns of A
         float v = 0.f;
@@ -856,9 +858,11 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
         }
         __syncthreads();
     }
-    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // no division by the runtime size
-        const int r = e % PI_NB, c = e / PI_NB;
-        if (r >= c && r < n) A[r + (int64_t)c * lda] = sA[r * PI_LD + c];
+    if (store_l) {
+        for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // no division by the runtime size
+            const int r = e % PI_NB, c = e / PI_NB;
+            if (r >= c && r < n) A[r + (int64_t)c * lda] = sA[r * PI_LD + c];
+        }
     }
     for (int e = tid; e < PI_NB * PI_NB / 4; e += PI_THREADS) {   // float4 stores (64 KB-aligned blocks)
         {   // column-major Linv: 4 rows of one column
@@ -883,7 +887,7 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
 }
 
 void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
-               float* Bl, cudaStream_t s) {
+               float* Bl, cudaStream_t s, bool store_l) {
     if (n <= 0 || n > PI_NB) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
     ProfScope prof_("potrf_inv", s);
     const size_t sm = PI_SMEM;
@@ -892,8 +896,81 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
         cudaFuncSetAttribute(potrf_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
-    potrf_inv_kernel<<<1, PI_THREADS, sm, s>>>(A, lda, n, err, err_col, col_offset, Linv, Bh, Bl);
+    potrf_inv_kernel<<<1, PI_THREADS, sm, s>>>(A, lda, n, err, err_col, col_offset, Linv, Bh, Bl, store_l ? 1 : 0);
     check("potrf_inv");
+}
+
+// Symmetric update of an n x n (n <= 128) diagonal block by up to two panels
+// of the factorization, A11 -= P0 P0^T + P1 P1^T, lower triangle, FP32 FMA in
+// a fixed order (panel 0, then panel 1, k ascending).  Each panel is given as
+// the TF32 head and remainder rows of its K-major split (n rows of 128
+// values; head + remainder = the FP32 panel).  One CTA per lower 32 x 32
+// block (10), 256 threads, 2 x 2 outputs each; both 32-row slices of a panel
+// are staged in shared memory (row-major, padded: the threads of a warp read
+// 16 different rows of one column, conflict free).
+constexpr int DU_LD = 129;
+__global__ void __launch_bounds__(256) diag_update_kernel(float* A, int64_t lda, int n, const float* __restrict__ P0h,
+                                                         const float* __restrict__ P0l,
+                                                         const float* __restrict__ P1h,
+                                                         const float* __restrict__ P1l) {
+    __shared__ float sI[32 * DU_LD], sJ[32 * DU_LD];
+    int I = 0, t = blockIdx.x;   // lower block (I, J) number t = I (I + 1) / 2 + J
+    while (t > I) t -= ++I;
+    const int J = t, tid = threadIdx.x;
+    const int r0 = 32 * I + 2 * (tid >> 4), c0 = 32 * J + 2 * (tid & 15);
+    float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int p = 0; p < 2; ++p) {
+        const float* Ph = p ? P1h : P0h;
+        const float* Pl = p ? P1l : P0l;
+        if (!Ph) break;
+        if (p) __syncthreads();
+#pragma unroll 4
+        for (int e = tid; e < 2 * 32 * 32; e += 256) {   // (slice, row, 4 values): float4 reads along the rows
+            const int q = e & 31, row = (e >> 5) & 31, sl = e >> 10;
+            const int gr = 32 * (sl ? J : I) + row;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (gr < n) {
+                const float4 h = *reinterpret_cast<const float4*>(Ph + (int64_t)gr * 128 + 4 * q);
+                const float4 l = *reinterpret_cast<const float4*>(Pl + (int64_t)gr * 128 + 4 * q);
+                v = make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
+            }
+            float* d = (sl ? sJ : sI) + row * DU_LD + 4 * q;
+            d[0] = v.x;
+            d[1] = v.y;
+            d[2] = v.z;
+            d[3] = v.w;
+        }
+        __syncthreads();
+        const float* a0 = sI + (r0 - 32 * I) * DU_LD;
+        const float* b0 = sJ + (c0 - 32 * J) * DU_LD;
+#pragma unroll 8
+        for (int k = 0; k < 128; ++k) {
+            const float x0 = a0[k], x1 = a0[DU_LD + k], y0 = b0[k], y1 = b0[DU_LD + k];
+            acc[0][0] = fmaf(x0, y0, acc[0][0]);
+            acc[0][1] = fmaf(x0, y1, acc[0][1]);
+            acc[1][0] = fmaf(x1, y0, acc[1][0]);
+            acc[1][1] = fmaf(x1, y1, acc[1][1]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int r = r0 + i, c = c0 + j;
+            if (r >= c && r < n) A[r + (int64_t)c * lda] -= acc[i][j];
+        }
+}
+
+void diag_update(float* A, int64_t lda, int n, const float* P0h, const float* P0l, const float* P1h, const float* P1l,
+                 cudaStream_t s) {
+    if (n <= 0 || n > 128) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
+    for (const float* q : {P0h, P0l, P1h, P1l})
+        if (reinterpret_cast<uintptr_t>(q) % 16) throw Error(OMG_ERR_INVALID, "panel rows not 16-byte aligned");
+    if (!P0h || !P0l || !P1h != !P1l) throw Error(OMG_ERR_INVALID, "panel update needs heads and remainders");
+    ProfScope prof_("diag_update", s);
+    const int nb32 = (n + 31) / 32;
+    diag_update_kernel<<<nb32 * (nb32 + 1) / 2, 256, 0, s>>>(A, lda, n, P0h, P0l, P1h, P1l);
+    check("diag_update");
 }
 
 // B <- blockdiag(op(Linv_b)) B over all diagonal blocks at once, op =
@@ -997,11 +1074,14 @@ void apply_inv_blocks(int64_t nblocks, int nb, int n_last, int64_t ncol, const f
 }  // namespace omg
 
 // Test hook (not part of the public header): factor and invert one diagonal
-// block (device pointers).  With reps > 1 the call is then repeated on
-// scratch copies and the mean launch time (microseconds, CUDA events on the
-// default stream) is returned through *us.
+// block (device pointers), after the update by the panels P0, P1 when given
+// (diag_update: head / remainder rows, 128 values each; null for none).  With
+// reps > 1 the call is then repeated on scratch copies and the mean time of
+// the launches (microseconds, CUDA events on the default stream) is returned
+// through *us.
 extern "C" int omg_internal_potrf_inv(int n, float* A, int64_t lda, float* Linv, float* Bh, float* Bl, int* err,
-                                      int reps, float* us) {
+                                      int reps, float* us, const float* P0h, const float* P0l, const float* P1h,
+                                      const float* P1l) {
     int64_t* col = nullptr;
     float* scratch = nullptr;
     int* err2 = nullptr;
@@ -1015,15 +1095,18 @@ extern "C" int omg_internal_potrf_inv(int n, float* A, int64_t lda, float* Linv,
             cudaMemcpy2D(scratch, 128 * sizeof(float), A, lda * sizeof(float), n * sizeof(float), n,
                          cudaMemcpyDeviceToDevice);
         }
-        omg::potrf_inv(A, lda, n, err, col, 0, Linv, Bh, Bl, 0);
+        if (P0h) omg::diag_update(A, lda, n, P0h, P0l, P1h, P1l, 0);
+        omg::potrf_inv(A, lda, n, err, col, 0, Linv, Bh, Bl, 0, true);
         if (reps > 1) {
             cudaEvent_t e0, e1;
             cudaEventCreate(&e0);
             cudaEventCreate(&e1);
             float* s1 = scratch + 128 * 128;
             cudaEventRecord(e0, 0);
-            for (int r = 1; r < reps; ++r)   // same work on a scratch block (values no longer matter)
-                omg::potrf_inv(scratch, 128, n, err2, col, 0, s1, s1 + 128 * 128, s1 + 2 * 128 * 128, 0);
+            for (int r = 1; r < reps; ++r) {   // same work on a scratch block (values no longer matter)
+                if (P0h) omg::diag_update(scratch, 128, n, P0h, P0l, P1h, P1l, 0);
+                omg::potrf_inv(scratch, 128, n, err2, col, 0, s1, s1 + 128 * 128, s1 + 2 * 128 * 128, 0, false);
+            }
             cudaEventRecord(e1, 0);
             cudaEventSynchronize(e1);
             float ms = 0.f;

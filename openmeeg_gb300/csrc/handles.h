@@ -24,9 +24,9 @@ struct omg_context_s {
     double* d_scalar = nullptr;
     int64_t launches_at_create = 0;
     int refs = 1;              // the caller's handle + one per live geometry / solver
-    // second stream and two events of the factorization's look-ahead (created on first use)
+    // second stream and the events of the factorization's look-ahead (created on first use)
     cudaStream_t aux = nullptr;
-    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr, ev_e = nullptr;
     // highest-priority stream of the latency-bound solve chains (their CTAs go first onto SMs that free up
     // while other work runs on the second stream; created on first use)
     cudaStream_t hi = nullptr;
@@ -36,10 +36,10 @@ inline void release_aux(omg_context_s* c) {
     if (c->hi) cudaStreamDestroy(c->hi);
     c->hi = nullptr;
     if (c->aux) cudaStreamDestroy(c->aux);
-    if (c->ev_a) cudaEventDestroy(c->ev_a);
-    if (c->ev_b) cudaEventDestroy(c->ev_b);
+    for (cudaEvent_t e : {c->ev_a, c->ev_b, c->ev_c, c->ev_d, c->ev_e})
+        if (e) cudaEventDestroy(e);
     c->aux = nullptr;
-    c->ev_a = c->ev_b = nullptr;
+    c->ev_a = c->ev_b = c->ev_c = c->ev_d = c->ev_e = nullptr;
 }
 
 // Live bytes of all device buffers of the library and their high-water mark

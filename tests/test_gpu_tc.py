@@ -280,8 +280,9 @@ def test_diagonal_block_cholesky_and_inverse(cuda):
     import torch
     f = _lib_hook("omg_internal_potrf_inv", [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
-                                             ctypes.c_void_p])
+                                             ctypes.c_void_p] + [ctypes.c_void_p] * 4)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
+    none4 = [None] * 4
     for n in (128, 77):
         g = torch.Generator(device="cuda").manual_seed(n)
         M = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
@@ -293,7 +294,8 @@ def test_diagonal_block_cholesky_and_inverse(cuda):
         Bl = torch.zeros(128 * 128, device="cuda")
         err = torch.zeros(1, dtype=torch.int32, device="cuda")
         us = ctypes.c_float(0)
-        assert f(n, p(A), 140, p(Li), p(Bh), p(Bl), p(err), 20, ctypes.byref(us)) == 0 and int(err.item()) == 0
+        assert f(n, p(A), 140, p(Li), p(Bh), p(Bl), p(err), 20, ctypes.byref(us), *none4) == 0
+        assert int(err.item()) == 0
         print(f"potrf_inv n={n}: {us.value:.1f} us per launch")
         L = torch.tril(A.T[:n, :n].double())            # row-major view of the factor
         assert float(torch.linalg.norm(L @ L.T - A64) / torch.linalg.norm(A64)) < 1e-6
@@ -302,3 +304,45 @@ def test_diagonal_block_cholesky_and_inverse(cuda):
         if n < 128:
             assert float(Linv[n:, :].abs().max()) == 0.0 and float(Linv[:, n:].abs().max()) == 0.0
         assert torch.equal((Bh + Bl).view(128, 128), Li.view(128, 128).T)
+
+
+def test_diagonal_block_panel_update(cuda):
+    """The diagonal-block update applies A11 -= P0 P0^T + P1 P1^T from the
+    head / remainder rows of one or two panels (n rows of 128 values) before
+    the block is factored: L L^T equals the updated block at FP32 level (full
+    and partial blocks), and nothing outside the n x n block is written."""
+    import torch
+    f = _lib_hook("omg_internal_potrf_inv", [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_void_p] + [ctypes.c_void_p] * 4)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def split(P):
+        h = (P.view(torch.int32) & -8192).view(torch.float32)   # TF32 head: low 13 mantissa bits cleared
+        return h.contiguous(), (P - h).contiguous()
+
+    for n, npanels in ((128, 2), (128, 1), (77, 2)):
+        g = torch.Generator(device="cuda").manual_seed(1000 + n + npanels)
+        M = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+        Af = M @ M.T / n + torch.eye(n, device="cuda", dtype=torch.float64)   # the block after the update
+        Ps = [torch.randn(n, 128, device="cuda", generator=g).mul_(0.1) for _ in range(npanels)]
+        Ain = Af.clone()
+        for P in Ps:
+            Ain += P.double() @ P.double().T
+        A = torch.zeros(140, 140, device="cuda", dtype=torch.float32)
+        A[:n, :n] = Ain.T.float()
+        Li = torch.zeros(128 * 128, device="cuda")
+        Bh = torch.zeros(128 * 128, device="cuda")
+        Bl = torch.zeros(128 * 128, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        hl = [split(P) for P in Ps]
+        args = [p(t) for pair in hl for t in pair] + [None] * (4 - 2 * len(hl))
+        us = ctypes.c_float(0)
+        assert f(n, p(A), 140, p(Li), p(Bh), p(Bl), p(err), 20, ctypes.byref(us), *args) == 0
+        assert int(err.item()) == 0
+        print(f"potrf_inv n={n} with {npanels} panel update(s): {us.value:.1f} us per launch")
+        L = torch.tril(A.T[:n, :n].double())
+        assert float(torch.linalg.norm(L @ L.T - Af) / torch.linalg.norm(Af)) < 2e-6
+        Linv = Li.view(128, 128).T.double()
+        assert float(torch.linalg.norm(L @ Linv[:n, :n] - torch.eye(n, device="cuda", dtype=torch.float64))) < 1e-5
+        assert float(A[n:, :].abs().max()) == 0.0 and float(A[:, n:].abs().max()) == 0.0
