@@ -600,13 +600,15 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     // the rows below the next diagonal block, while the chain updates that block by the latest panels
     // itself (a small FP32 kernel) and factors it.  The rest of each group's trailing update
     // runs on the second stream (s2) with a few SMs left free for the other two.
-    //   ev_p (sc): the latest panel solve is done (its W rows are ready)
+    //   ev_p (sc): the first 128 rows of the latest panel solve are done (the rest follow on s)
+    //   ev_q (s):  the latest panel solve is complete (all its W rows)
     //   ev_l (s):  the rows below the next diagonal block and their A21 split are ready
     //   ev_g (s):  the look-ahead update of the next group's second panel is done
     //   ev_r (s2): the rest update of the previous group is done
     ensure_aux(sv->ctx);
     cudaStream_t s2 = sv->ctx->aux, sc = sv->ctx->hi;
     cudaEvent_t ev_r = sv->ctx->ev_b, ev_p = sv->ctx->ev_c, ev_l = sv->ctx->ev_d, ev_g = sv->ctx->ev_e;
+    cudaEvent_t ev_q = sv->ctx->ev_a;
     OMG_CUDA(cudaEventRecord(ev_l, s));   // the head matrix is ready
     OMG_CUDA(cudaStreamWaitEvent(sc, ev_l, 0));
     bool rest_pending = false;
@@ -682,16 +684,23 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
                 split_panel_kmajor(m, (int)nk, nb, A + k1 + k0 * ld, ld, Th, Tl, sc);
             else
                 OMG_CUDA(cudaStreamWaitEvent(sc, ev_l, 0));
-            gemm_tf32x3(m, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
+            // the first 128 rows (the next diagonal block's update needs them) on the chain, the rest on s
+            const int64_t mt = std::min<int64_t>(m, nb);
+            gemm_tf32x3(mt, nk, nb, 1.f, Th, Tl, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f, A + k1 + k0 * ld, ld, false,
                         sv->ctx->d_err, sc, "gemm_panel", 0, wh(b), wl(b), 0, nb, Ar + k1 + k0 * ld, nullptr, nullptr,
                         0, true);
             OMG_CUDA(cudaEventRecord(ev_p, sc));
+            OMG_CUDA(cudaStreamWaitEvent(s, ev_p, 0));
+            if (m > mt)
+                gemm_tf32x3(m - mt, nk, nb, 1.f, Th + mt * nb, Tl + mt * nb, nb, nb, 0, Bih, Bil, nb, nb, 0, 0.f,
+                            A + k1 + mt + k0 * ld, ld, false, sv->ctx->d_err, s, "gemm_panel", 0, wh(b) + mt * nb,
+                            wl(b) + mt * nb, 0, nb, Ar + k1 + mt + k0 * ld, nullptr, nullptr, 0, true);
+            OMG_CUDA(cudaEventRecord(ev_q, s));
             have_t = false;
             if (b + 1 < ge) {   // the group's second panel: the chain updates its diagonal block by this panel,
                                 // the rows below it (with their A21 split) are updated beside it on s
                 const int64_t k2 = sv->bounds[b + 2], nn = k2 - k1, mr = N - k2;
                 if (mr > 0) {
-                    OMG_CUDA(cudaStreamWaitEvent(s, ev_p, 0));
                     gemm_tf32x3(mr, nn, nk, -1.f, wh(b) + (k2 - k1) * nb, wl(b) + (k2 - k1) * nb, nb, nb, 0, wh(b),
                                 wl(b), nb, nb, 0, 1.f, A + k2 + k1 * ld, ld, false, sv->ctx->d_err, s, "gemm_next", 0,
                                 Th, Th + mr * nb, 0, nb, nullptr, nullptr, nullptr, 0, true);
@@ -743,7 +752,7 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
         // the rest, on the second stream
         const int64_t kr = sv->bounds[ng], mr = N - kr;
         if (mr > 0) {
-            OMG_CUDA(cudaStreamWaitEvent(s2, ev_p, 0));
+            OMG_CUDA(cudaStreamWaitEvent(s2, ev_q, 0));
             group_update(gb, ge, mr, mr, kr, kr, A + kr + kr * ld, true, s2, "gemm_syrk", std::max(1, n_sm() - reserve),
                          nullptr, nullptr, 0, false);
             OMG_CUDA(cudaEventRecord(ev_r, s2));
