@@ -653,9 +653,11 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 //      forward substitution (rows below the block);
 //   3. all threads apply the rank-32 update to the trailing lower triangle
 //      in 4 x 4 register tiles, reading the panel from a k-major copy;
-// then the off-diagonal blocks of the inverse, X_IJ = -X_II sum_{K=J}^{I-1}
-// L_IK X_KJ, block row by block row.  The block lives in shared memory
-// (row-major, padded); columns past n act as the identity.
+// the off-diagonal blocks of the inverse, X_JK = -X_JJ sum_{M=K}^{J-1} L_JM
+// X_MK, are computed block row by block row inside the same loop: the sums
+// by warps 1-15 while warp 0 factors diagonal block J (step 1), the products
+// with X_JJ beside the trailing update (step 3).  The block lives in shared
+// memory (row-major, padded); columns past n act as the identity.
 
 // Outputs: L11 over A11 (lower; left out when store_l is false: the
 // factorization's solves use only the inverse), Linv column-major (ldi = 128, zero above the
@@ -667,6 +669,61 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512, PI_BS = 32, PI_TLD = 33;
 constexpr size_t PI_SMEM =
     ((size_t)2 * PI_NB * PI_LD + (size_t)PI_BS * PI_NB + 3 * PI_BS * PI_TLD + PI_NB + 2 * PI_BS) * sizeof(float);
+
+// Block row J of the inverse X = L^-1 (32-row blocks), one 4 x 4 tile t of
+// the J x 64 tiles of its blocks K < J: T_JK = sum_{M=K}^{J-1} L_JM X_MK (the
+// rows of L in sA, of X in sX, T into sT), then X_JK = -X_JJ T_JK.
+__device__ __forceinline__ void pi_inv_rowblock_t(const float* sA, const float* sX, float* sT, int J, int t) {
+    const int K = t / 64, ti = (t % 64) / 8, tj = t % 8;
+    const int r0 = PI_BS * J + 4 * ti, c0 = PI_BS * K + 4 * tj;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int k = PI_BS * K; k < PI_BS * J; ++k) {
+        float av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) av[i] = sA[(r0 + i) * PI_LD + k];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = sX[k * PI_LD + c0 + j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    float* T = sT + K * PI_BS * PI_TLD;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) T[(4 * ti + i) * PI_TLD + 4 * tj + j] = acc[i][j];
+}
+
+__device__ __forceinline__ void pi_inv_rowblock_x(float* sX, const float* sT, int J, int t) {
+    const int K = t / 64, ti = (t % 64) / 8, tj = t % 8;
+    const int r0 = PI_BS * J + 4 * ti, c0 = PI_BS * K + 4 * tj;
+    const float* T = sT + K * PI_BS * PI_TLD;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int k = 0; k < PI_BS; ++k) {
+        float av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) av[i] = sX[(r0 + i) * PI_LD + PI_BS * J + k];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = T[k * PI_TLD + 4 * tj + j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sX[(r0 + i) * PI_LD + c0 + j] = -acc[i][j];
+}
 
 __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
                                                                int64_t* err_col, int64_t col_offset, float* Linv,
@@ -728,6 +785,8 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
             }
             if (bad >= 0 && lane == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
                 *err_col = col_offset + j0 + bad;
+        } else if (J > 0) {   // ---- 1'. meanwhile T_JK = sum_{M=K}^{J-1} L_JM X_MK for K < J (inverse, block row J)
+            for (int t = tid - 32; t < J * 64; t += PI_THREADS - 32) pi_inv_rowblock_t(sA, sX, sT, J, t);
         }
         __syncthreads();
         const int below = PI_NB - j0 - PI_BS;
@@ -800,63 +859,10 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
                     for (int j = 0; j < 4; ++j)
                         if (c0 + j <= r0 + i) sA[(r0 + i) * PI_LD + c0 + j] -= acc[i][j];
             }
-            __syncthreads();
         }
-    }
-    // ---- off-diagonal blocks of the inverse, block row I
-    for (int I = 1; I < 4; ++I) {
-        for (int t = tid; t < I * 64; t += PI_THREADS) {   // T_IJ = sum_{K=J}^{I-1} L_IK X_KJ
-            const int J = t / 64, ti = (t % 64) / 8, tj = t % 8;
-            const int r0 = PI_BS * I + 4 * ti, c0 = PI_BS * J + 4 * tj;
-            float acc[4][4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-            for (int k = PI_BS * J; k < PI_BS * I; ++k) {
-                float av[4], bv[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) av[i] = sA[(r0 + i) * PI_LD + k];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) bv[j] = sX[k * PI_LD + c0 + j];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-            }
-            float* T = sT + J * PI_BS * PI_TLD;
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) T[(4 * ti + i) * PI_TLD + 4 * tj + j] = acc[i][j];
-        }
-        __syncthreads();
-        for (int t = tid; t < I * 64; t += PI_THREADS) {   // X_IJ = -X_II T_IJ
-            const int J = t / 64, ti = (t % 64) / 8, tj = t % 8;
-            const int r0 = PI_BS * I + 4 * ti, c0 = PI_BS * J + 4 * tj;
-            const float* T = sT + J * PI_BS * PI_TLD;
-            float acc[4][4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-            for (int k = 0; k < PI_BS; ++k) {
-                float av[4], bv[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) av[i] = sX[(r0 + i) * PI_LD + PI_BS * I + k];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) bv[j] = T[k * PI_TLD + 4 * tj + j];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) sX[(r0 + i) * PI_LD + c0 + j] = -acc[i][j];
-        }
-        __syncthreads();
+        if (J > 0)   // ---- 3'. X_JK = -X_JJ T_JK, K < J (disjoint from the trailing update)
+            for (int t = tid; t < J * 64; t += PI_THREADS) pi_inv_rowblock_x(sX, sT, J, t);
+        if (below > 0 || J > 0) __syncthreads();
     }
     if (store_l) {
         for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // no division by the runtime size
