@@ -716,7 +716,7 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
 }
 
 constexpr int FF_TI = 128, FF_TJ = 32;
-constexpr float kFarTier7 = 64.f;   // squared: pairs at >= 8 max edges take the 7-point rule
+constexpr float kFarTier7 = 36.f;   // squared: pairs at >= 6 max edges take the 7-point rule
 
 // One thread per t1 row, looping over the CTA's FF_TJ staged t2 records.
 __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restrict__ grec, int64_t t1b, int64_t n1,
@@ -772,7 +772,7 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
         const f2 DN2 = pk2(dn2, dn2), N2x = pk2(n2x, n2x), N2y = pk2(n2y, n2y), N2z = pk2(n2z, n2z);
         float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f, u0 = 0.f, u1 = 0.f, u2 = 0.f;   // u: D21
         if (dist2 >= kFarTier7 * hmax * hmax) {
-            // well separated (>= 8 max edges): the 7 x 7 product rule, within 1e-8 of the 16 x 16 one there;
+            // well separated (>= 6 max edges): the 7 x 7 product rule, within 1e-7 of the 16 x 16 one there;
             // t1's 7 points from its record (L1), packed (0,1) (2,3) (4,5) (6,6) with a zero weight on the last lane
             const f2* W7 = reinterpret_cast<const f2*>(c_w7);
             const float* p7 = g1 + GREC_P7;

@@ -1,10 +1,11 @@
-"""The two tiers of the mixed far field: pairs whose centroids are at least 8
+"""The two tiers of the mixed far field: pairs whose centroids are at least 6
 of their largest edges apart are integrated with the 7 x 7 product rule, the
 others with the 16 x 16 one.  On pairs of the config1 head beyond that
-distance the 7 x 7 rule reproduces the 16 x 16 one far below FP32 rounding:
-single layer within 1e-8 relative, double layer (both directions) within 2e-8
-of the sum of the absolute terms.  The rules are read from the kernel's own
-constant tables."""
+distance the 7 x 7 rule reproduces the 16 x 16 one below FP32 rounding:
+single layer within 1e-8 relative, double layer (both directions) within 1e-7
+of the sum of the absolute terms (measured 4.8e-9 and 4.4e-8 at 6-8 edges,
+6.2e-10 and 4.4e-9 beyond 8; at 4-5 edges the double layer would reach
+5.7e-7).  The rules are read from the kernel's own constant tables."""
 import os
 import re
 
@@ -55,7 +56,7 @@ def test_far_tier_rule_matches_16_point_rule():
         cen = P.mean(axis=1)
         for _ in range(4000):
             a, b = rng.integers(0, len(T), 2)
-            if np.linalg.norm(cen[a] - cen[b]) < 8.0 * max(h[a], h[b]):
+            if np.linalg.norm(cen[a] - cen[b]) < 6.0 * max(h[a], h[b]):
                 continue
             s7, d7, _, e7, _ = _integrals(P, nrm, a, b, R7)
             s16, d16, dabs, e16, eabs = _integrals(P, nrm, a, b, R16)
@@ -64,4 +65,4 @@ def test_far_tier_rule_matches_16_point_rule():
             n += 1
     assert n > 5000
     assert worst_s < 1e-8, worst_s
-    assert worst_d < 2e-8, worst_d
+    assert worst_d < 1e-7, worst_d
