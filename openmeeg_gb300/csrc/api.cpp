@@ -119,9 +119,9 @@ void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
 void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
-               float* Bl, cudaStream_t s, bool store_l = true);
+               float* Bl, cudaStream_t s, bool store_l = true, bool pdl = false);
 void diag_update(float* A, int64_t lda, int n, const float* P0h, const float* P0l, const float* P1h, const float* P1l,
-                 cudaStream_t s);
+                 cudaStream_t s, bool pdl = false);
 void apply_inv_blocks(int64_t nblocks, int nb, int n_last, int64_t ncol, const float* Li, bool trans, float* B,
                       int64_t ldb, cudaStream_t s);
 void col_norms_f32(int64_t m, int64_t n, const float* A, int64_t lda, const double* scale, double* out,
@@ -672,9 +672,10 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
             if (b == gb + 1 && wait_g) OMG_CUDA(cudaStreamWaitEvent(sc, ev_g, 0));
             float* Bih = Bi.as<float>() + 2 * b * nb * nb;
             float* Bil = Bih + (size_t)nb * nb;
-            if (fp[0]) diag_update(A + k0 + k0 * ld, ld, (int)nk, fp[0], fp[1], fp[2], fp[3], sc);
+            // programmatic dependent launches: each starts while its predecessor on the chain drains
+            if (fp[0]) diag_update(A + k0 + k0 * ld, ld, (int)nk, fp[0], fp[1], fp[2], fp[3], sc, true);
             potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
-                      sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, sc, false);
+                      sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, sc, false, fp[0] != nullptr);
             for (auto& q : fp) q = nullptr;
             if (m == 0) continue;
             // L21 = A21 L11^-T on the tensor cores, written as heads (A) + remainders (A32r); its epilogue

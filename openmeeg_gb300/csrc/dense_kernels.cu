@@ -23,6 +23,28 @@ static inline void check(const char* what) {
 }
 static inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// Launch with programmatic dependent launch when `pdl`: the kernel may start while its predecessor on the
+// stream finishes and waits for it (griddepcontrol.wait) before it reads that kernel's outputs.
+template <typename... KArgs, typename... Args>
+static void launch_maybe_pdl(bool pdl, void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                             cudaStream_t s, Args... args) {
+    if (!pdl) {
+        kern<<<grid, block, smem, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, (KArgs)args...);
+}
+
 // ---------------------------------------------------------------------------
 // C = alpha * op(A) * op(B) + beta * C (column-major).  LOWER restricts the
 // output to entries with global row >= global column (row0/col0 give the
@@ -737,6 +759,8 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
     float* sCol = sInv + PI_NB;                     // 2 x 32: column broadcast of the diagonal factor
     const unsigned FULL = 0xffffffffu;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    asm volatile("griddepcontrol.launch_dependents;");
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // the block's last update (no-op without PDL)
 #pragma unroll 16
     for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // 32 iterations: loads batched by the unroll
         const int r = e % PI_NB, c = e / PI_NB;    // coalesced down the columns of A
@@ -893,7 +917,7 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
 }
 
 void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
-               float* Bl, cudaStream_t s, bool store_l) {
+               float* Bl, cudaStream_t s, bool store_l, bool pdl) {
     if (n <= 0 || n > PI_NB) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
     ProfScope prof_("potrf_inv", s);
     const size_t sm = PI_SMEM;
@@ -902,7 +926,8 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
         cudaFuncSetAttribute(potrf_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         attr = true;
     }
-    potrf_inv_kernel<<<1, PI_THREADS, sm, s>>>(A, lda, n, err, err_col, col_offset, Linv, Bh, Bl, store_l ? 1 : 0);
+    launch_maybe_pdl(pdl, potrf_inv_kernel, 1, PI_THREADS, sm, s, A, lda, n, err, err_col, col_offset, Linv, Bh, Bl,
+                     store_l ? 1 : 0);
     check("potrf_inv");
 }
 
@@ -920,6 +945,8 @@ __global__ void __launch_bounds__(256) diag_update_kernel(float* A, int64_t lda,
                                                          const float* __restrict__ P1h,
                                                          const float* __restrict__ P1l) {
     __shared__ float sI[32 * DU_LD], sJ[32 * DU_LD];
+    asm volatile("griddepcontrol.launch_dependents;");
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // the panel rows (no-op without PDL)
     int I = 0, t = blockIdx.x;   // lower block (I, J) number t = I (I + 1) / 2 + J
     while (t > I) t -= ++I;
     const int J = t, tid = threadIdx.x;
@@ -968,14 +995,14 @@ __global__ void __launch_bounds__(256) diag_update_kernel(float* A, int64_t lda,
 }
 
 void diag_update(float* A, int64_t lda, int n, const float* P0h, const float* P0l, const float* P1h, const float* P1l,
-                 cudaStream_t s) {
+                 cudaStream_t s, bool pdl) {
     if (n <= 0 || n > 128) throw Error(OMG_ERR_INVALID, "diagonal block must have 1..128 columns");
     for (const float* q : {P0h, P0l, P1h, P1l})
         if (reinterpret_cast<uintptr_t>(q) % 16) throw Error(OMG_ERR_INVALID, "panel rows not 16-byte aligned");
     if (!P0h || !P0l || !P1h != !P1l) throw Error(OMG_ERR_INVALID, "panel update needs heads and remainders");
     ProfScope prof_("diag_update", s);
     const int nb32 = (n + 31) / 32;
-    diag_update_kernel<<<nb32 * (nb32 + 1) / 2, 256, 0, s>>>(A, lda, n, P0h, P0l, P1h, P1l);
+    launch_maybe_pdl(pdl, diag_update_kernel, nb32 * (nb32 + 1) / 2, 256, 0, s, A, lda, n, P0h, P0l, P1h, P1l);
     check("diag_update");
 }
 
@@ -1101,8 +1128,8 @@ extern "C" int omg_internal_potrf_inv(int n, float* A, int64_t lda, float* Linv,
             cudaMemcpy2D(scratch, 128 * sizeof(float), A, lda * sizeof(float), n * sizeof(float), n,
                          cudaMemcpyDeviceToDevice);
         }
-        if (P0h) omg::diag_update(A, lda, n, P0h, P0l, P1h, P1l, 0);
-        omg::potrf_inv(A, lda, n, err, col, 0, Linv, Bh, Bl, 0, true);
+        if (P0h) omg::diag_update(A, lda, n, P0h, P0l, P1h, P1l, 0, false);
+        omg::potrf_inv(A, lda, n, err, col, 0, Linv, Bh, Bl, 0, true, false);
         if (reps > 1) {
             cudaEvent_t e0, e1;
             cudaEventCreate(&e0);
@@ -1110,8 +1137,9 @@ extern "C" int omg_internal_potrf_inv(int n, float* A, int64_t lda, float* Linv,
             float* s1 = scratch + 128 * 128;
             cudaEventRecord(e0, 0);
             for (int r = 1; r < reps; ++r) {   // same work on a scratch block (values no longer matter)
-                if (P0h) omg::diag_update(scratch, 128, n, P0h, P0l, P1h, P1l, 0);
-                omg::potrf_inv(scratch, 128, n, err2, col, 0, s1, s1 + 128 * 128, s1 + 2 * 128 * 128, 0, false);
+                if (P0h) omg::diag_update(scratch, 128, n, P0h, P0l, P1h, P1l, 0, false);
+                omg::potrf_inv(scratch, 128, n, err2, col, 0, s1, s1 + 128 * 128, s1 + 2 * 128 * 128, 0, false,
+                               false);
             }
             cudaEventRecord(e1, 0);
             cudaEventSynchronize(e1);
