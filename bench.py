@@ -241,6 +241,17 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
                      "fp32_issue_frac_of_nominal": fp32_ops / t_launch / FP32_ISSUE_NOMINAL,
                      "note": f"HBM fraction of {kind} copy bandwidth; the kernel is FP32-issue bound "
                              f"(12 FP32 ops per multiply-add), see fp32_issue_frac_of_nominal"})
+    elif name == "gemm_solve":
+        # the FP32 solves: a dependent chain of tensor-core updates per sweep (one per 128-row block), each
+        # sweep nrhs N^2 algorithmic flops (forward: sum over blocks of 2 (N - k1) nrhs 128), executed TF32
+        # tensor flops 3x; latency-bound (each update waits for the previous one's band copy)
+        flops = 4.0 * k * N ** 2 / per_step   # two solves of two sweeps each per gain
+        achieved = flops / t_launch / 1e12
+        tf32_peak = bf16 / 2.0
+        info.update({"bound": "tensor", "achieved": 3 * achieved, "peak": tf32_peak, "unit": "TFLOP/s",
+                     "frac": 3 * achieved / tf32_peak, "traffic": None, "algorithmic_fp32_tflops": achieved,
+                     "note": "dependent chain of 128-deep updates (141 per sweep at config1): latency-bound, "
+                             f"executed TF32 tensor flops vs half the {kind} bf16 burst peak"})
     elif name == "gemm_syrk":
         # trailing updates of the FP32 LDL^T on the tensor cores: sum over panels of
         # 2 (N - k1)^2 / 2 * 128 = ~N^3/3 algorithmic flops per factorization (lower triangle only);
@@ -253,11 +264,13 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
                      "note": f"executed TF32 tensor flops (3 per FP32-accurate product) vs half the {kind} bf16 "
                              f"burst peak (the TF32 dense rate is half the bf16 rate)"})
     elif name == "ff_block":
-        # far-field FP32 Gauss products: 16 x 16 point pairs per triangle pair, S and both D from the same
-        # 256 distances, 12 FP32 operations each (3 differences, 3 for r^2, rsqrt, 2 for r^-3, 3 accumulations:
-        # the normal components r.n fold into per-point weights since the points lie in their triangles' planes)
-        pairs = stats.get("_tri_pairs", 0)
-        ops = 12.0 * 256 * pairs / per_step
+        # far-field FP32 Gauss products: 16 x 16 point pairs per triangle pair below 6 max edges, 7 x 7 from
+        # there on; S and both D from the same distances, 12 FP32 operations per point pair (3 differences,
+        # 3 for r^2, rsqrt, 2 for r^-3, 3 accumulations: the normal components r.n fold into per-point weights
+        # since the points lie in their triangles' planes)
+        n16 = stats.get("_pairs_6", 0) - stats.get("_near_pairs", 0)
+        n7 = stats.get("_tri_pairs", 0) - stats.get("_pairs_6", 0)
+        ops = 12.0 * (256 * n16 + 49 * n7) / per_step
         achieved = ops / t_launch
         info.update({"bound": "fp32", "achieved": achieved / 1e12, "peak": FP32_ISSUE_NOMINAL / 1e12,
                      "unit": "T FP32 op/s", "frac": achieved / FP32_ISSUE_NOMINAL, "traffic": None,
@@ -312,7 +325,7 @@ def tri_pairs(head):
     return pairs
 
 
-def near_pairs_count(head, rho=2.0):
+def near_pairs_count(head, rho=1.5):
     """Near triangle pairs of the mixed head matrix (those integrated by the FP64 analytic kernels): centroid
     distance below rho times the larger of the two triangles' longest edges, over the self pairs (j >= i) and
     the adjacent mesh pairs, as the far-field kernel lists them."""
@@ -441,6 +454,7 @@ def run_gpu(args):
     stx_r = dict(stx)
     stx_r["_tri_pairs"] = tri_pairs(w.head)
     stx_r["_near_pairs"] = near_pairs_count(w.head)
+    stx_r["_pairs_6"] = near_pairs_count(w.head, 6.0)   # pairs below the 7-point far-field tier
     roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx_r, pk)
     others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx_r, pk)
               for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block", "near_pairs")

@@ -403,8 +403,13 @@ void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, doub
 
 
 // Mixed precision: far pairs by the FP32 product rule, near pairs (centroid
-// distance < kRhoFar x larger max edge) by the FP64 analytic kernels.
-constexpr float kRhoFar = 2.0f;
+// distance < kRhoFar x larger max edge) by the FP64 analytic kernels.  From
+// 1.5 max edges on, the 16 x 16 rule stays within 1.1e-7 (single layer) and
+// 1.5e-6 (double layer, of the sum of the absolute terms) of a twice
+// subdivided rule on the config1 head (below 1.5 the double layer reaches
+// 3e-3); the config1 gain error against the FP64 drop-in stays 3.0e-8 (EEG)
+// and 7.1e-10 (MEG), as with a split at 2 edges.
+constexpr float kRhoFar = 1.5f;
 
 void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld, NearPlan* plan) {
     omg_context ctx = g->ctx;

@@ -66,3 +66,61 @@ def test_far_tier_rule_matches_16_point_rule():
     assert n > 5000
     assert worst_s < 1e-8, worst_s
     assert worst_d < 1e-7, worst_d
+
+
+def _subdivided_points(P, R, levels):
+    tris = [P]
+    for _ in range(levels):
+        nxt = []
+        for a, b, c in tris:
+            ab, bc, ca = (a + b) / 2, (b + c) / 2, (c + a) / 2
+            nxt += [np.array([a, ab, ca]), np.array([ab, b, bc]), np.array([ca, bc, c]), np.array([ab, bc, ca])]
+        tris = nxt
+    return (np.concatenate([R[:, :3] @ t for t in tris]),
+            np.concatenate([R[:, 3] / 4 ** levels for _ in tris]))
+
+
+def test_near_far_split_rule_accuracy():
+    """Pairs at 1.5 or more of their largest edges go to the FP32 16 x 16 rule
+    (nearer pairs to the FP64 analytic kernels).  There the rule stays within
+    2e-7 (single layer) and 3e-6 (double layer, of the sum of the absolute
+    terms) of the same rule on twice subdivided triangles; nearer pairs would
+    not (the double layer at 1 to 1.5 edges is off by more than 1e-4)."""
+    from scipy.spatial import cKDTree
+    from openmeeg_gb300 import workloads
+    _, R16 = _rules()
+    head = workloads.config1().head
+    V, T = head.vertices[0], head.triangles[0]
+    P = V[T]
+    nrm = np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    h = np.max(np.linalg.norm(P - np.roll(P, 1, axis=1), axis=2), axis=1)
+    cen = P.mean(axis=1)
+    tree = cKDTree(cen)
+    rng = np.random.default_rng(5)
+
+    def integ(a, b, lev):
+        xa, wa = _subdivided_points(P[a], R16, lev)
+        xb, wb = _subdivided_points(P[b], R16, lev)
+        r = xb[None] - xa[:, None]
+        d = np.linalg.norm(r, axis=2)
+        w = wa[:, None] * wb[None]
+        t = w * (r @ nrm[b]) / d ** 3
+        return (w / d).sum(), t.sum(), np.abs(t).sum()
+
+    worst = {"far": [0.0, 0.0], "near": [0.0, 0.0]}
+    counts = {"far": 0, "near": 0}
+    for a in rng.permutation(len(T))[:200]:
+        for b in tree.query_ball_point(cen[a], 2.5 * h.max()):
+            q = np.linalg.norm(cen[a] - cen[b]) / max(h[a], h[b])
+            band = "far" if 1.5 <= q < 2.5 else ("near" if 1.0 <= q < 1.5 else None)
+            if band is None or counts[band] >= 80:
+                continue
+            s1, d1, _ = integ(a, b, 0)
+            s2, d2, ad2 = integ(a, b, 2)
+            worst[band][0] = max(worst[band][0], abs(s1 - s2) / abs(s2))
+            worst[band][1] = max(worst[band][1], abs(d1 - d2) / ad2)
+            counts[band] += 1
+    assert counts["far"] >= 80 and counts["near"] >= 40
+    assert worst["far"][0] < 2e-7 and worst["far"][1] < 3e-6, worst["far"]
+    assert worst["near"][1] > 1e-4, worst["near"]
