@@ -13,9 +13,9 @@ device.  `value` is seconds per step (lower is better).  The FP64 drop-in is
 timed on the same box in the same run, and the mixed result's relative error
 against it is reported (target <= 1e-6).
 
-`--impl reference` times the reference CPU path's restatement (the oracle
-port, all host threads) on a bounded sample of the same workload and scales
-it to the full workload.
+`--impl reference` runs the reference CPU pipeline restated by the oracle
+port (HeadMat, sensor matrices, the DSPTRF/DSPTRS adjoint solve, DipSourceMat,
+contraction) once on the full workload, unscaled, on all host threads.
 
 Inputs exceed the 129 MB L2 (the 2.6 GB head matrix is rebuilt every step),
 so no explicit L2 flush is done between steps.
@@ -99,66 +99,125 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle port on a bounded sample, scaled to config1
+# CPU baseline: the reference's pipeline restated by the oracle port
 # ---------------------------------------------------------------------------
-def cpu_sample_time(threads: int | None = None):
-    """Times the oracle (C restatement + LAPACK) on a sample of config1 and
-    scales each stage to the full workload by its operation count."""
+def workload_config(name: str, N: int, nd: int, ne: int, nm: int) -> dict:
+    """The `config` object of the bench line; both arms print the same one for the same workload."""
+    shape = {"config0": "3-layer ico3 head", "config1": "3-layer ico4 SH-perturbed head"}.get(name, name)
+    return {"workload": f"{name}: {shape}, N={N}, {nd} dipoles, {ne} EEG, {nm} MEG", "N": N, "dipoles": nd,
+            "eeg": ne, "meg": nm, "parallelism": "none (one head model per process; replicas under torchrun)",
+            "l2": "inputs > L2 (the head matrix, 8 N^2 bytes, is rebuilt every step); no flush"}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_cache_path(config: str) -> str:
+    import tempfile
+    return os.path.join(tempfile.gettempdir(), f"omg_bench_reference_{config}.json")
+
+
+def cpu_pipeline(w, threads: int):
+    """The reference's time-to-gain pipeline on the CPU at full size
+    (oracle.forward_pipeline: HeadMat, H2EM, H2MM, DS2MM, then the
+    GainEEGMEGadjoint solve by DSPTRF/DSPTRS, DipSourceMat and the
+    contraction), all host threads.  Returns (seconds without the geometry
+    set-up, per-stage seconds)."""
     from oracle import oracle
+    oracle.set_threads(threads)
+    oracle.openblas_threads(threads)
+    _, _, t = oracle.forward_pipeline(w.head, w.dipoles, w.electrodes, w.squids if len(w.squids) else None)
+    return sum(v for k, v in t.items() if k != "geometry"), t
+
+
+def cpu_sample_time(config: str, threads: int):
+    """Bounded CPU sample for the GPU line: the whole pipeline measured on the
+    config0 head (N = 4486, 200 dipoles, 64 EEG, 32 MEG; ~10-20 s of CPU work)
+    and each measured stage scaled to the bench workload by its operation count
+    (pair integrals ~ T^2, the DSPTRF factorization ~ N^3, solves ~ N^2 k,
+    DipSourceMat ~ dipoles x triangles, contraction ~ k N dipoles, sensor
+    matrices ~ sensors x N)."""
     from openmeeg_gb300 import workloads
-    if threads:
-        oracle.set_threads(threads)
-    nthr = oracle.num_threads()
-    w1 = workloads.config1()
     w0 = workloads.config0()
-    g1 = oracle.digest(w1.head)
-    g0 = oracle.digest(w0.head)
-    T0 = w0.head.triangles[0].shape[0]
-    T1 = w1.head.triangles[0].shape[0]
-    t = {}
-    s = time.perf_counter()
-    HM0 = oracle.headmat(g0)
-    t["headmat"] = (time.perf_counter() - s) * (T1 / T0) ** 2           # S and D pair counts scale as T^2
-    s = time.perf_counter()
-    oracle.solve_adjoint(HM0, np.ones((64 + 151, g0.N)))
-    t["solve"] = (time.perf_counter() - s) * (g1.N / g0.N) ** 3          # symmetric-indefinite solve ~ N^3
-    nd = 100
-    s = time.perf_counter()
-    D = oracle.dsm(g1, w1.dipoles[:nd])
-    t["dsm"] = (time.perf_counter() - s) * (w1.dipoles.shape[0] / nd)   # per-dipole columns
-    s = time.perf_counter()
-    oracle.h2em(g1, w1.electrodes)
-    oracle.h2mm(g1, w1.squids)
-    oracle.ds2mm(w1.dipoles, w1.squids)
-    t["sensors"] = time.perf_counter() - s
-    t["gain_gemm"] = 2.0 * 215 * g1.N * w1.dipoles.shape[0] / 20e9       # GEMM at ~20 GFLOP/s
-    total = sum(t.values())
-    sample = (f"config0 HeadMat (N={g0.N}) x{(T1 / T0) ** 2:.0f} pair-count scale; LAPACK solve N={g0.N}, 215 rhs "
-              f"x(N ratio)^3; DSM of {nd} config1 dipoles x{w1.dipoles.shape[0] // nd}; config1 sensor matrices; "
-              f"gain GEMM modelled")
-    return total, t, sample, nthr
+    w1 = getattr(workloads, config)()
+    _, t0 = cpu_pipeline(w0, threads)
+    T0 = sum(t.shape[0] for t in w0.head.triangles)
+    T1 = sum(t.shape[0] for t in w1.head.triangles)
+    N0 = sum(v.shape[0] for v in w0.head.vertices) + T0 - w0.head.triangles[-1].shape[0]
+    N1 = sum(v.shape[0] for v in w1.head.vertices) + T1 - w1.head.triangles[-1].shape[0]
+    k0 = w0.electrodes.shape[0] + w0.squids.shape[0]
+    k1 = w1.electrodes.shape[0] + w1.squids.shape[0]
+    nd0, nd1 = w0.dipoles.shape[0], w1.dipoles.shape[0]
+    scale = {"headmat": (T1 / T0) ** 2, "factor_solve": (N1 / N0) ** 3, "dsm": (nd1 / nd0) * (T1 / T0),
+             "contract": (k1 * N1 * nd1) / (k0 * N0 * nd0), "h2em": N1 / N0,
+             "h2mm": (w1.squids.shape[0] * N1) / max(1, w0.squids.shape[0] * N0),
+             "ds2mm": (w1.squids.shape[0] * nd1) / max(1, w0.squids.shape[0] * nd0)}
+    parts = {k: v * scale[k] for k, v in t0.items() if k in scale}
+    sample = (f"the whole pipeline on the config0 head (N={N0}, {nd0} dipoles, {k0} sensor rows) measured stage by "
+              f"stage ({sum(v for k, v in t0.items() if k != 'geometry'):.1f} s), each stage scaled to {config} by "
+              f"its operation count (pair integrals T^2, DSPTRF N^3, DSM dipoles x T, contraction k N dipoles)")
+    return sum(parts.values()), parts, sample
+
+
+def read_reference_cache(config: str, cfg: dict):
+    """The measurement an earlier `--impl reference` run of the same workload left in this
+    machine's temp directory (within the last 12 hours), or None."""
+    p = reference_cache_path(config)
+    try:
+        d = json.load(open(p))
+    except (OSError, ValueError):
+        return None
+    if d.get("config") != cfg or time.time() - d.get("when", 0) > 12 * 3600:
+        return None
+    return d
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU pipeline for the bench workload,
+    restated by the oracle port (C restatement of the assembly, LAPACK DSPTRF/
+    DSPTRS for the solve), at full size and unscaled, on all host threads.  One
+    full pipeline is several minutes of CPU work, so each invocation runs it
+    once: the line reports the single step it ran (steps 1, warmup 0) beside the
+    requested counts."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    times = []
-    for i in range(args.warmup + args.steps):
-        total, parts, sample, nthr = cpu_sample_time()
-        if i >= args.warmup:
-            times.append(total)
-    v = float(np.mean(times))
+    from openmeeg_gb300 import workloads
+    from oracle import oracle
+    w = getattr(workloads, args.config)()
+    g = oracle.digest(w.head)
+    nd, ne, nm = w.dipoles.shape[0], w.electrodes.shape[0], w.squids.shape[0]
+    cfg = workload_config(args.config, g.N, nd, ne, nm)
+    threads = cpu_threads()
+    t_wall0 = time.perf_counter()
+    v, parts = cpu_pipeline(w, threads)
+    wall = time.perf_counter() - t_wall0
+    sample = (f"the whole {args.config} workload, unscaled: one run of the reference pipeline (HeadMat, H2EM, "
+              f"H2MM, DS2MM, GainEEGMEGadjoint with DSPTRF/DSPTRS on the packed head matrix, DipSourceMat of all "
+              f"{nd} dipoles, contraction) by the oracle port")
+    cpu = {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample,
+           "stages_s": {k: round(x, 3) for k, x in parts.items()}}
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded nested icosphere heads)",
-        "config": {"workload": "config1: 3-layer ico4 SH-perturbed head, N=17926, 2000 dipoles, 64 EEG, 151 MEG",
-                   "parallelism": "cpu"},
-        "cpu_baseline": {"value": v, "unit": "s", "cores": nthr, "kind": "port", "sample": sample,
-                         "stages_s": {k: round(x, 3) for k, x in parts.items()}},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": 1,
+        "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup, "ms_per_step": v * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded nested icosphere heads, dipoles, Fibonacci sensors)",
+        "config": cfg, "cpu_baseline": cpu,
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "timed_wall_s": wall,
+        "note": "one full, unscaled pipeline per invocation (several minutes of CPU work); no warm-up: the CPU "
+                "path has no device state to warm",
     }
+    try:
+        with open(reference_cache_path(args.config), "w") as f:
+            json.dump({"config": cfg, "value": v, "cores": threads, "stages_s": line["cpu_baseline"]["stages_s"],
+                       "when": time.time()}, f)
+    except OSError:
+        pass
     print(json.dumps(line))
     return 0
 
@@ -460,11 +519,20 @@ def run_gpu(args):
               for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block", "near_pairs")
               and n != dname}
 
+    cfg = workload_config(args.config, N, nd, ne, nm)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        total, parts, sample, nthr = cpu_sample_time()
-        cpu = {"value": total, "unit": "s", "cores": nthr, "kind": "port", "sample": sample,
-               "stages_s": {k: round(x, 3) for k, x in parts.items()}}
+        cached = read_reference_cache(args.config, cfg)
+        if cached:
+            cpu = {"value": cached["value"], "unit": "s", "cores": cached["cores"], "kind": "port",
+                   "sample": "the whole workload, unscaled: measured by this machine's bench.py --impl reference "
+                             f"run {int(time.time() - cached['when'])} s before this line",
+                   "stages_s": cached["stages_s"]}
+        else:
+            threads = cpu_threads()
+            total, parts, sample = cpu_sample_time(args.config, threads)
+            cpu = {"value": total, "unit": "s", "cores": threads, "kind": "port", "sample": sample,
+                   "stages_s": {k: round(x, 3) for k, x in parts.items()}}
 
     if rank == 0:
         line = {
@@ -472,10 +540,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64 (mixed); f64 drop-in timed beside it",
             "data": "synthetic (seeded nested icosphere heads, dipoles, Fibonacci sensors)",
-            "config": {"workload": f"{args.config}: 3-layer ico4 SH-perturbed head, N={N}, {nd} dipoles, {ne} EEG, "
-                                   f"{nm} MEG", "N": N, "dipoles": nd, "eeg": ne, "meg": nm,
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "inputs > L2 (2.6 GB head matrix rebuilt each step); no flush"},
+            "config": cfg,
             "fp64_s": t_fp64, "speedup_vs_fp64": t_fp64 / t_step,
             "rel_err_vs_fp64": {"eeg": err_eeg, "meg": err_meg},
             "mixed_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stx.items()},
@@ -508,10 +573,8 @@ def run_batch(args):
     torch.cuda.set_device(local)
     __import__("__graft_entry__").build()
     from openmeeg_gb300 import api, workloads
-    os.environ.setdefault("OMG_TUNE_CACHE", os.path.join(ROOT, "gpurun_out", "tune_cache.txt")
-                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "")
-    if not os.environ["OMG_TUNE_CACHE"]:
-        del os.environ["OMG_TUNE_CACHE"]
+    import tempfile
+    os.environ.setdefault("OMG_TUNE_CACHE", os.path.join(tempfile.gettempdir(), "omg_tune_cache.txt"))
     ws = workloads.config3_models()
     ctx = api.Context(local)
     geos = [api.Geometry.from_head(w.head, ctx) for w in ws]

@@ -148,7 +148,8 @@ int omg_head2megmat_dev(omg_context ctx, omg_geometry geo, const double* squids,
  * allocation.  Limit: n_squids x n_triangles <= OMG_NOALLOC_SCRATCH_DOUBLES.
  * The first call on a device sets up the scratch address (make it before any
  * stream capture); calls that overlap on the GPU share the array and race.
- * Output and arguments as omg_head2megmat_dev. */
+ * The call returns after its work on the context's stream has finished, as
+ * omg_head2megmat_dev does.  Output and arguments as omg_head2megmat_dev. */
 #define OMG_NOALLOC_SCRATCH_DOUBLES (4 * 1024 * 1024)
 int omg_head2megmat_noalloc_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids,
                                 double* h2mm);

@@ -1657,9 +1657,9 @@ __global__ void h2em_kernel(const double* __restrict__ pos, int nseg, const int6
 __global__ void ferguson_s_kernel(const double* __restrict__ sq, int64_t np, int64_t nt,
                                   const double* __restrict__ srec, double* F) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t i = blockIdx.y;
-    if (t >= nt || i >= np) return;
-    F[i * nt + t] = dev::operator_S(srec + t * SREC, dev::ld3(sq + 6 * i));
+    if (t >= nt) return;
+    for (int64_t i = blockIdx.y; i < np; i += gridDim.y)
+        F[i * nt + t] = dev::operator_S(srec + t * SREC, dev::ld3(sq + 6 * i));
 }
 
 __global__ void ferguson_gather_kernel(const double* __restrict__ sq, int64_t np, int64_t nv, int64_t nt,
@@ -1669,34 +1669,36 @@ __global__ void ferguson_gather_kernel(const double* __restrict__ sq, int64_t np
                                        const double* __restrict__ jump, int64_t nP, int perm, double* out,
                                        int64_t rs, int64_t cs, int64_t col0, double mag) {
     const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t i = blockIdx.y;
-    if (v >= nv || i >= np) return;
-    d3 res = dev::mk(0, 0, 0);
-    double coeff = 0.0;
-    for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
-        const int64_t t = v2t_tri[k];
-        const int loc = v2t_loc[k];
-        const double* s = srec + t * SREC;
-        const d3 A = dev::ld3(s + 3 * ((loc + 1) % 3)), B = dev::ld3(s + 3 * ((loc + 2) % 3));
-        res = res + (B - A) * (F[i * nt + t] / (2 * s[12]));
-        coeff = jump ? mag * jump[tmesh[t]] : mag;
+    if (v >= nv) return;
+    for (int64_t i = blockIdx.y; i < np; i += gridDim.y) {
+        d3 res = dev::mk(0, 0, 0);
+        double coeff = 0.0;
+        for (int k = v2t_beg[v]; k < v2t_beg[v + 1]; ++k) {
+            const int64_t t = v2t_tri[k];
+            const int loc = v2t_loc[k];
+            const double* s = srec + t * SREC;
+            const d3 A = dev::ld3(s + 3 * ((loc + 1) % 3)), B = dev::ld3(s + 3 * ((loc + 2) % 3));
+            res = res + (B - A) * (F[i * nt + t] / (2 * s[12]));
+            coeff = jump ? mag * jump[tmesh[t]] : mag;
+        }
+        const d3 o = dev::ld3(sq + 6 * i + 3);
+        out[(perm ? nP + v : v) * rs + (col0 + i) * cs] = dev::dot(res * coeff, o) / dev::norm(o);
     }
-    const d3 o = dev::ld3(sq + 6 * i + 3);
-    out[(perm ? nP + v : v) * rs + (col0 + i) * cs] = dev::dot(res * coeff, o) / dev::norm(o);
 }
 
 // ---- DipSource2MEGMat (assembleSensors.cpp:133-159): Biot-Savart primary field.
 __global__ void ds2mm_kernel(const double* __restrict__ dip, int64_t nd, const double* __restrict__ sq, int64_t np,
                              double* out, int64_t ldo) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t j = blockIdx.y;
-    if (i >= np || j >= nd) return;
-    const d3 r = dev::ld3(dip + 6 * j), q = dev::ld3(dip + 6 * j + 3);
-    const d3 diff = dev::ld3(sq + 6 * i) - r;
-    const double nd3 = dev::norm(diff);
-    const d3 f = dev::cross(q, diff) * (1.0 / (nd3 * nd3 * nd3));
+    if (i >= np) return;
     const d3 o = dev::ld3(sq + 6 * i + 3);
-    out[i + j * ldo] = dev::dot(f, o) * kMagFactor / dev::norm(o);
+    for (int64_t j = blockIdx.y; j < nd; j += gridDim.y) {
+        const d3 r = dev::ld3(dip + 6 * j), q = dev::ld3(dip + 6 * j + 3);
+        const d3 diff = dev::ld3(sq + 6 * i) - r;
+        const double nd3 = dev::norm(diff);
+        const d3 f = dev::cross(q, diff) * (1.0 / (nd3 * nd3 * nd3));
+        out[i + j * ldo] = dev::dot(f, o) * kMagFactor / dev::norm(o);
+    }
 }
 
 void launch_mesh_solid_angles(const double* pts, int64_t pstride, int64_t n, int nmesh, const int64_t* tbeg_dev,
@@ -1795,10 +1797,10 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
                  double* out, int64_t rs, int64_t cs, int64_t col0, double* F, cudaStream_t s, double mag) {
     ProfScope prof_("h2mm", s);
     if (np == 0) return;
-    dim3 grid(nblocks(g.nt, 128), (unsigned)np);
+    dim3 grid(nblocks(g.nt, 128), (unsigned)std::min<int64_t>(np, 32768));
     ferguson_s_kernel<<<grid, 128, 0, s>>>(sq, np, g.nt, g.srec, F);
     check_launch("Ferguson S");
-    dim3 grid2(nblocks(g.nv, 128), (unsigned)np);
+    dim3 grid2(nblocks(g.nv, 128), (unsigned)std::min<int64_t>(np, 32768));
     ferguson_gather_kernel<<<grid2, 128, 0, s>>>(sq, np, g.nv, g.nt, F, g.srec, g.v2t_beg, g.v2t_tri, g.v2t_loc,
                                                  tmesh, jump, g.nP, perm, out, rs, cs, col0, mag);
     check_launch("Ferguson gather");
@@ -1808,7 +1810,7 @@ void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, d
                   cudaStream_t s) {
     ProfScope prof_("ds2mm", s);
     if (nd == 0 || np == 0) return;
-    dim3 grid(nblocks(np, 128), (unsigned)nd);
+    dim3 grid(nblocks(np, 128), (unsigned)std::min<int64_t>(nd, 32768));
     ds2mm_kernel<<<grid, 128, 0, s>>>(dip, nd, sq, np, out, ldo);
     check_launch("DS2MM");
 }

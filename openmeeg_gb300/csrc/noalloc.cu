@@ -24,6 +24,8 @@
 //    wrong results; serialise them (one stream, or one call at a time).
 //  - Nothing in the array needs to start at zero: the Ferguson pass writes
 //    every entry it later reads.  The output matrix is cleared by the call.
+//  - The call waits for its work on the context's stream to finish before it
+//    returns, as omg_head2megmat_dev does.
 //  - No cudaMalloc, cudaMallocAsync, cudaFree or allocating library routine
 //    is called.
 #include <cuda_runtime.h>
@@ -31,7 +33,7 @@
 #include <mutex>
 #include <string>
 
-#include "handles.h"
+#include "pipeline.h"
 
 namespace omg {
 void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* tmesh, const double* jump, int perm,
@@ -64,15 +66,15 @@ double* scratch_address(int device) {
 
 extern "C" int omg_head2megmat_noalloc_dev(omg_context ctx, omg_geometry geo, const double* squids, int64_t n_squids,
                                            double* h2mm) {
-    try {
+    return guarded([&] {
         OMG_REQUIRE(ctx && geo, "null argument");
         OMG_REQUIRE(n_squids >= 0, "negative sensor count");
         OMG_REQUIRE(n_squids == 0 || (squids && h2mm), "null sensors or output");
         if (geo->h.shared)   // the per-distinct-vertex sum needs a buffer of the vertex copies
             throw Error(OMG_ERR_UNSUPPORTED, "geometries whose meshes share vertices need omg_head2megmat_dev");
-        OMG_CUDA(cudaSetDevice(ctx->device));
+        set_device(ctx);
         double* scratch = scratch_address(ctx->device);
-        if (n_squids == 0) return OMG_OK;
+        if (n_squids == 0) return;
         const int64_t need = n_squids * geo->h.nt;
         if (need > (int64_t)OMG_NOALLOC_SCRATCH_DOUBLES)
             throw Error(OMG_ERR_INVALID, "n_squids x n_triangles = " + std::to_string(need) +
@@ -83,12 +85,5 @@ extern "C" int omg_head2megmat_noalloc_dev(omg_context ctx, omg_geometry geo, co
         omg::launch_h2mm(geo->d, squids, n_squids, geo->tmesh, geo->jump, 0, h2mm, n_squids, 1, 0, scratch, s);
         OMG_CUDA(cudaStreamSynchronize(s));
         OMG_CUDA(cudaGetLastError());
-        return OMG_OK;
-    } catch (const Error& e) {
-        set_last_error(e.what());
-        return e.code;
-    } catch (const std::exception& e) {
-        set_last_error(e.what());
-        return OMG_ERR_INVALID;
-    }
+    });
 }

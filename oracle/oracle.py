@@ -548,6 +548,141 @@ def solve_adjoint(HM: np.ndarray, rhs_rows: np.ndarray) -> np.ndarray:
     return sla.solve(HM, rhs_rows.T, assume_a="sym").T
 
 
+_openblas_lib = None
+
+
+def _openblas():
+    """scipy's bundled OpenBLAS: the BLAS/LAPACK the reference build links
+    (``oracle/ref/Makefile``), with its LAPACKE entry points prefixed ``scipy_``."""
+    global _openblas_lib
+    if _openblas_lib is None:
+        import glob
+
+        import scipy
+        d = os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs")
+        cands = sorted(glob.glob(os.path.join(d, "libscipy_openblas-*.so*")))
+        if not cands:
+            raise RuntimeError(f"scipy's bundled OpenBLAS not found under {d}")
+        lib_ = ctypes.CDLL(cands[0])
+        lib_.scipy_LAPACKE_dsptrf.argtypes = [ctypes.c_int, ctypes.c_char, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p]
+        lib_.scipy_LAPACKE_dsptrf.restype = ctypes.c_int
+        lib_.scipy_LAPACKE_dsptrs.argtypes = [ctypes.c_int, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib_.scipy_LAPACKE_dsptrs.restype = ctypes.c_int
+        lib_.scipy_LAPACKE_dsptri.argtypes = [ctypes.c_int, ctypes.c_char, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p]
+        lib_.scipy_LAPACKE_dsptri.restype = ctypes.c_int
+        lib_.scipy_openblas_get_num_threads.restype = ctypes.c_int
+        _openblas_lib = lib_
+    return _openblas_lib
+
+
+def openblas_threads(n: int | None = None) -> int:
+    """Sets (when n is given) and returns the OpenBLAS thread count."""
+    ob = _openblas()
+    if n:
+        ob.scipy_openblas_set_num_threads(ctypes.c_int(n))
+    return int(ob.scipy_openblas_get_num_threads())
+
+
+def solve_lin_packed(packed: np.ndarray, n: int, rhs: np.ndarray) -> np.ndarray:
+    """SymMatrix::solveLin (OpenMEEGMaths/src/symmatrix.cpp:133-152): a copy of
+    the packed-upper matrix factored by DSPTRF('U') (Bunch-Kaufman), then DSPTRS
+    on the n x k right-hand sides.  Returns the n x k solution."""
+    if n * (n + 1) // 2 != packed.size:
+        raise ValueError("packed size does not match n")
+    ob = _openblas()
+    A = np.array(packed, dtype=np.float64, copy=True)
+    piv = np.zeros(n, dtype=np.int32)
+    info = ob.scipy_LAPACKE_dsptrf(102, b"U", n, A.ctypes.data, piv.ctypes.data)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"DSPTRF info = {info}")
+    B = np.asfortranarray(rhs, dtype=np.float64).copy(order="F")
+    k = B.shape[1]
+    info = ob.scipy_LAPACKE_dsptrs(102, b"U", n, k, A.ctypes.data, piv.ctypes.data, B.ctypes.data, n)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"DSPTRS info = {info}")
+    return B
+
+
+def invert_packed(packed: np.ndarray, n: int) -> np.ndarray:
+    """SymMatrix::invert (OpenMEEGMaths/include/symmatrix.h:280-300), what
+    om_minverser runs: DSPTRF('U') then DSPTRI on packed-upper storage.
+    Returns the packed-upper inverse."""
+    if n * (n + 1) // 2 != packed.size:
+        raise ValueError("packed size does not match n")
+    ob = _openblas()
+    A = np.array(packed, dtype=np.float64, copy=True)
+    piv = np.zeros(n, dtype=np.int32)
+    info = ob.scipy_LAPACKE_dsptrf(102, b"U", n, A.ctypes.data, piv.ctypes.data)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"DSPTRF info = {info}")
+    info = ob.scipy_LAPACKE_dsptri(102, b"U", n, A.ctypes.data, piv.ctypes.data)
+    if info != 0:
+        raise np.linalg.LinAlgError(f"DSPTRI info = {info}")
+    return A
+
+
+def gain_eeg_direct(HMinv, DSM, H2EM):
+    """GainEEG (OpenMEEG/include/gain.h:69-76) as om_gain -EEG evaluates it
+    (apps/gain.cpp:65-80): the sparse rows times the explicit inverse first,
+    then the source matrix."""
+    return (H2EM @ HMinv) @ DSM
+
+
+def gain_meg_direct(HMinv, DSM, H2MM, DS2MM):
+    """GainMEG (gain.h:60-67, apps/gain.cpp:105-122): DS2MM + (H2MM HMinv) DSM."""
+    return DS2MM + (H2MM @ HMinv) @ DSM
+
+
+def forward_pipeline(head, dipoles, electrodes=None, squids=None, clock=None):
+    """The reference's time-to-gain pipeline on the CPU, stage by stage and at
+    full size: ``om_assemble -HM`` (packed SymMatrix), ``-H2EM``, ``-H2MM``,
+    ``-DS2MM``, then ``om_gain -EEGMEGadjoint`` (GainEEGMEGadjoint,
+    OpenMEEG/include/gain.h:117-136): one DSPTRF/DSPTRS solve for the stacked
+    sensor rows, the dipole sources, their contraction and DS2MM.  Returns the
+    gains and the wall time of every stage."""
+    import time
+    clock = clock or time.perf_counter
+    t = {}
+    s = clock()
+    g = digest(head)
+    t["geometry"] = clock() - s
+    s = clock()
+    P = headmat_packed(g)
+    t["headmat"] = clock() - s
+    rows = []
+    H2EM = H2MM = DS2MM = None
+    if electrodes is not None:
+        s = clock()
+        H2EM = h2em(g, electrodes)
+        t["h2em"] = clock() - s
+        rows.append(H2EM)
+    if squids is not None:
+        s = clock()
+        H2MM = h2mm(g, squids)
+        t["h2mm"] = clock() - s
+        s = clock()
+        DS2MM = ds2mm(dipoles, squids)
+        t["ds2mm"] = clock() - s
+        rows.append(H2MM)
+    s = clock()
+    Y = solve_lin_packed(P, g.N, np.vstack(rows).T)          # N x (ne + nm)
+    t["factor_solve"] = clock() - s
+    del P
+    s = clock()
+    D = dsm(g, dipoles)
+    t["dsm"] = clock() - s
+    s = clock()
+    G = Y.T @ D
+    ne = 0 if H2EM is None else H2EM.shape[0]
+    geeg = G[:ne] if H2EM is not None else None
+    gmeg = G[ne:] + DS2MM if H2MM is not None else None
+    t["contract"] = clock() - s
+    return geeg, gmeg, t
+
+
 def gain_eeg(HM, DSM, H2EM):
     """GainEEGadjoint semantics (gain.h:78-89): (HM^-1 H2EM^T)^T DSM."""
     return solve_adjoint(HM, H2EM) @ DSM

@@ -15,13 +15,16 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(HERE, "_ref", "bin")
+# Where the reference sources are read from (this recipe builds them where they
+# lie); OMG_REFERENCE_DIR overrides it.
+REFERENCE_DIR = os.environ.get("OMG_REFERENCE_DIR", "/root/reference")
 
 
 def available() -> bool:
     return os.path.exists(os.path.join(REF_BIN, "om_assemble"))
 
 
-def build(ref_src: str = "/root/reference", jobs: int = 8) -> bool:
+def build(ref_src: str = REFERENCE_DIR, jobs: int = 8) -> bool:
     if not os.path.isdir(ref_src):
         return False
     subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={ref_src}", f"-j{jobs}"],

@@ -33,6 +33,10 @@ files) for a seeded workload of openmeeg_gb300.workloads:
                      -DS2IPM, own domains and a forced one) at points in every layer
                      and in the air of small_ico1_3l and small_ico1_4l_out;
                      `--ipm-only` writes this fixture and the ones above
+  direct_gains       om_minverser + om_gain -EEG / -MEG (the explicit-inverse pipeline of the
+                     reference's own tests) on small_ico1_3l, small_ico2_3l_pert and config0,
+                     with the reference's packed inverse of small_ico1_3l; `--direct-only`
+                     writes just this fixture
   surface_sources    SurfSourceMat and SurfSource2MEGMat (om_assemble -SSM / -SS2MM)
                      of a source icosphere (ico1, r = 0.5, off-centre) in the brain of
                      small_ico1_3l and of small_ico1_4l_out; `--ssm-only` writes just
@@ -68,7 +72,7 @@ def save(name, w, R, keep_hm=False):
 
 
 def save_head3_analytic():
-    R = os.environ.get("OMG_REFERENCE_DIR", "/root/reference")
+    R = ref_runner.REFERENCE_DIR
     d3 = os.path.join(R, "data", "Head3")
     meshes, domains = io.read_geom(os.path.join(d3, "Head3.geom"))
     cond = io.read_cond(os.path.join(d3, "Head3.cond"))
@@ -192,6 +196,40 @@ def save_eit():
     print("eit_sources", {k: v.shape for k, v in d.items()})
 
 
+def save_direct_gains():
+    """The documented pipeline of the reference's own tests (TestHead.cmake): om_minverser
+    (DSPTRF + DSPTRI) then om_gain -EEG / -MEG with the explicit inverse, on small_ico1_3l,
+    small_ico2_3l_pert and config0."""
+    import subprocess
+    import tempfile
+    if not ref_runner.available():
+        ref_runner.build()
+    d = {}
+    cases = (("ico1_3l", workloads.small(1, layers=3)), ("ico2_3l_pert", workloads.small(2, layers=3, perturb=True)),
+             ("config0", workloads.config0()))
+    for tag, w in cases:
+        wd = tempfile.mkdtemp()
+        ref_runner.write_head(wd, w.head, w.dipoles, w.electrodes, w.squids)
+        g, c = "head.geom", "head.cond"
+        for args in (["om_assemble", "-HM", g, c, "hm.bin"], ["om_minverser", "hm.bin", "hminv.bin"],
+                     ["om_assemble", "-DSM", g, c, "dip.txt", "dsm.bin"],
+                     ["om_assemble", "-H2EM", g, c, "eeg.txt", "h2em.bin"],
+                     ["om_assemble", "-H2MM", g, c, "meg.txt", "h2mm.bin"],
+                     ["om_assemble", "-DS2MM", "dip.txt", "meg.txt", "ds2mm.bin"],
+                     ["om_gain", "-EEG", "hminv.bin", "dsm.bin", "h2em.bin", "geeg.bin"],
+                     ["om_gain", "-MEG", "hminv.bin", "dsm.bin", "h2mm.bin", "ds2mm.bin", "gmeg.bin"]):
+            subprocess.check_call([os.path.join(ref_runner.REF_BIN, args[0]), *args[1:]], cwd=wd,
+                                  stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        d[f"eeg_{tag}"] = io.read_bin(os.path.join(wd, "geeg.bin"))[1]
+        d[f"meg_{tag}"] = io.read_bin(os.path.join(wd, "gmeg.bin"))[1]
+        if tag == "ico1_3l":   # the reference's explicit inverse of the smallest head (N = 286)
+            d[f"hminv_packed_{tag}"] = io.packed_upper(io.read_bin(os.path.join(wd, "hminv.bin"))[1])
+        import shutil
+        shutil.rmtree(wd, ignore_errors=True)
+    np.savez_compressed(os.path.join(OUT, "direct_gains.npz"), **d)
+    print("direct_gains", {k: v.shape for k, v in d.items()})
+
+
 REFERENCE_HEADS = ("HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3", "HeadNNa1", "HeadNNc1")
 
 
@@ -200,7 +238,7 @@ def save_reference_heads():
     multiple-non-conductive sample heads, run through its own pipeline with its
     own dipoles, EEG patches and MEG squids.  The .geom / .cond / mesh texts are
     stored so that a test can rebuild the files without the reference."""
-    R = os.environ.get("OMG_REFERENCE_DIR", "/root/reference")
+    R = ref_runner.REFERENCE_DIR
     if not ref_runner.available():
         ref_runner.build()
     d = {}
@@ -229,6 +267,9 @@ def save_reference_heads():
 
 
 def main():
+    if "--direct-only" in sys.argv:
+        save_direct_gains()
+        return
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
         return
@@ -244,6 +285,7 @@ def main():
     save_surface_sources()
     if "--ssm-only" in sys.argv:
         return
+    save_direct_gains()
     if not ref_runner.available():
         ref_runner.build()
     big = "--big" in sys.argv

@@ -31,6 +31,56 @@ def test_oracle_headmat_pinned_to_reference(name):
     assert rel(HM, ref) < 1e-14
 
 
+@pytest.mark.parametrize("name", ["small_ico1_3l", "small_ico1_4l_out", "small_ico2_3l_pert", "config0"])
+def test_oracle_forward_pipeline_pinned_to_reference(name):
+    """The reference pipeline the CPU baseline times (packed head matrix,
+    DSPTRF/DSPTRS solve of the stacked sensor rows, DipSourceMat, contraction)
+    gives the reference's own gains."""
+    from oracle import oracle
+    from openmeeg_gb300 import workloads
+    G = golden(name)
+    w = workloads.config0() if name == "config0" else _w(name)
+    ge, gm, t = oracle.forward_pipeline(w.head, w.dipoles, w.electrodes, w.squids)
+    assert rel(ge, G["eeg"]) < 1e-12
+    assert rel(gm, G["meg"]) < 1e-12
+    assert {"headmat", "factor_solve", "dsm", "contract"} <= set(t)
+
+
+def test_oracle_direct_gains_pinned_to_reference():
+    """om_minverser + om_gain -EEG / -MEG: the oracle's DSPTRF + DSPTRI inverse
+    of the reference's head matrix equals the reference's own inverse, and the
+    direct-form gains from it equal the reference's direct-form gains."""
+    from oracle import oracle
+    from openmeeg_gb300 import io
+    D = golden("direct_gains")
+    G = golden("small_ico1_3l")
+    w = _w("small_ico1_3l")
+    g = oracle.digest(w.head)
+    inv = oracle.invert_packed(G["hm_packed"], g.N)
+    assert rel(inv, D["hminv_packed_ico1_3l"]) < 1e-13
+    HMinv = io.unpack_upper(inv, g.N)
+    assert rel(oracle.gain_eeg_direct(HMinv, G["dsm"], G["h2em"]), D["eeg_ico1_3l"]) < 1e-13
+    assert rel(oracle.gain_meg_direct(HMinv, G["dsm"], G["h2mm"], G["ds2mm"]), D["meg_ico1_3l"]) < 1e-13
+    # the explicit-inverse and the adjoint pipelines agree
+    assert rel(D["eeg_ico1_3l"], G["eeg"]) < 1e-12 and rel(D["meg_ico1_3l"], G["meg"]) < 1e-12
+
+
+def test_packed_bunch_kaufman_solve():
+    """DSPTRF/DSPTRS on packed-upper storage (SymMatrix::solveLin) on an
+    indefinite symmetric matrix, against a dense solve."""
+    from oracle import oracle
+    from openmeeg_gb300 import io
+    rng = np.random.default_rng(1)
+    n = 200
+    A = rng.standard_normal((n, n))
+    A = A + A.T + np.diag(np.where(np.arange(n) % 2 == 0, 20.0, -20.0))
+    B = rng.standard_normal((n, 5))
+    X = oracle.solve_lin_packed(io.packed_upper(A), n, B)
+    assert rel(X, np.linalg.solve(A, B)) < 1e-12
+    with pytest.raises(ValueError):
+        oracle.solve_lin_packed(io.packed_upper(A)[:-1], n, B)
+
+
 @pytest.mark.parametrize("name", ["small_ico1_3l", "small_ico1_4l_out", "small_ico2_3l_pert"])
 def test_oracle_sources_sensors_gains_pinned_to_reference(name):
     from oracle import oracle

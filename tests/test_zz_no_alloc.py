@@ -57,7 +57,8 @@ def test_noalloc_refuses_requests_beyond_its_scratch(cuda):
     nt = sum(t.shape[0] for t in w.head.triangles)
     n = (4 * 1024 * 1024) // nt + 1          # one sensor more than the scratch holds
     s = torch.as_tensor(synthetic.radial_magnetometers(n, 1.2), dtype=torch.float64, device=cuda).contiguous()
-    out = torch.zeros((1, 1), dtype=torch.float64, device=cuda)
+    out = torch.full((4, 4), 7.0, dtype=torch.float64, device=cuda)
     rc = _call(lib, geo, s, out)
     assert rc == -1
     assert b"scratch" in lib.omg_last_error()
+    assert torch.all(out == 7.0)              # refused before anything is written
