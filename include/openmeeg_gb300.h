@@ -227,6 +227,30 @@ int omg_gain_host(omg_context ctx, omg_geometry geo, int32_t precision, const om
                   const double* electrodes, int64_t n_electrodes, const double* squids, int64_t n_squids,
                   double* gain_eeg, double* gain_meg, omg_gain_stats* stats);
 
+/* ---- gains from an explicit inverse ----------------------------------------
+ * GainEEG (OpenMEEG/include/gain.h:69-76; om_gain -EEG, apps/gain.cpp:65-80):
+ * gain = (H2EM HMinv) DSM for the inverse head matrix HMinv that om_minverser
+ * writes (SymMatrix::invert, OpenMEEGMaths/include/symmatrix.h:280-300).
+ * hminv: N x N column-major with leading dimension ld (packed = 0), or
+ * SymMatrix packed-upper storage, entry (i, j), i <= j, at i + j(j+1)/2
+ * (packed = 1, ld ignored).  H2EM is the sparse matrix of the reference's
+ * SparseMatrix in coordinate form: nnz (row, column, value) triplets with rows
+ * in [0, n_electrodes) and columns in [0, N) (device arrays; duplicates add).
+ * dsm: N x n_dipoles (leading dimension N); gain: n_electrodes x n_dipoles.
+ * precision OMG_PREC_FP64: FP64 CUDA-core products; OMG_PREC_MIXED: the
+ * FP64-accurate fixed-point digit GEMM on the tensor cores. */
+int omg_gain_eeg_dev(omg_context ctx, int64_t N, const double* hminv, int64_t ld, int32_t packed,
+                     const double* dsm, int64_t n_dipoles, int64_t n_electrodes, int64_t nnz,
+                     const int64_t* h2em_rows, const int64_t* h2em_cols, const double* h2em_vals, int32_t precision,
+                     double* gain);
+/* GainMEG (OpenMEEG/include/gain.h:60-67; om_gain -MEG, apps/gain.cpp:105-122):
+ * gain = DS2MM + (H2MM HMinv) DSM.  h2mm: n_squids x N, ds2mm: n_squids x
+ * n_dipoles (leading dimensions = row counts); other arguments as
+ * omg_gain_eeg_dev. */
+int omg_gain_meg_dev(omg_context ctx, int64_t N, const double* hminv, int64_t ld, int32_t packed,
+                     const double* dsm, int64_t n_dipoles, const double* h2mm, int64_t n_squids, const double* ds2mm,
+                     int32_t precision, double* gain);
+
 /* ---- surface sources -------------------------------------------------------
  * SurfSourceMat (OpenMEEG/src/assembleSourceMat.cpp:22-64, assembleSourceMat.h:20):
  * a triangulated source surface (host arrays: vertices n x 3 row-major,

@@ -107,6 +107,9 @@ _PROTOS = [
     ("omg_head2eegmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     ("omg_head2megmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
     ("omg_head2megmat_noalloc_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp]),
+    ("omg_gain_eeg_dev", c_i32, [c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_i32,
+                                 c_vp]),
+    ("omg_gain_meg_dev", c_i32, [c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp, c_i32, c_vp]),
     ("omg_dipsource2megmat_dev", c_i32, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp]),
     ("omg_geometry_get_layout", c_i32, [c_vp, c_i32, ctypes.POINTER(MeshLayout)]),
     ("omg_geometry_get_pairs", c_i32, [c_vp, c_i32, ctypes.POINTER(MeshPair), P_i32]),

@@ -14,6 +14,7 @@ raise ``OMGError`` carrying the C status, where the reference raises its
 from __future__ import annotations
 
 import ctypes
+import math
 import sys
 from typing import Optional, Sequence
 
@@ -492,14 +493,90 @@ class BatchForward:
 
 # ---- reference class names (gain.h:60-136) --------------------------------
 
-def GainEEG(HMinv, DSM, H2EM):
-    """GainEEG(HeadMatInv, SourceMat, Head2EEGMat) = H2EM HMinv DSM (gain.h:69-76)."""
-    return torch.as_tensor(H2EM) @ torch.as_tensor(HMinv) @ torch.as_tensor(DSM)
+def _inverse_operand(HMinv, ctx: Context):
+    """(device tensor, N, ld, packed): a dense N x N inverse in column-major
+    order, or a 1-D SymMatrix packed-upper array of N(N+1)/2 entries."""
+    t = HMinv if isinstance(HMinv, torch.Tensor) else torch.as_tensor(np.asarray(HMinv))
+    t = t.to(_dev(ctx), torch.float64)
+    if t.ndim == 1:
+        n = int((math.isqrt(8 * t.numel() + 1) - 1) // 2)
+        if n * (n + 1) // 2 != t.numel():
+            raise ValueError("packed inverse: length is not N(N+1)/2")
+        return t.contiguous(), n, n, 1
+    if t.ndim != 2 or t.shape[0] != t.shape[1]:
+        raise ValueError("inverse head matrix must be N x N or packed")
+    return t.T.contiguous(), t.shape[0], t.shape[0], 0     # row-major storage of t^T = column-major t
 
 
-def GainMEG(HMinv, DSM, H2MM, DS2MM):
-    """GainMEG = DS2MM + H2MM HMinv DSM (gain.h:60-67)."""
-    return torch.as_tensor(DS2MM) + torch.as_tensor(H2MM) @ torch.as_tensor(HMinv) @ torch.as_tensor(DSM)
+def _cols_dev(M, ctx: Context, rows: int) -> torch.Tensor:
+    """An (rows x n) matrix as a column-major device buffer (n x rows contiguous)."""
+    t = M if isinstance(M, torch.Tensor) else torch.as_tensor(np.asarray(M))
+    t = t.to(_dev(ctx), torch.float64)
+    if t.ndim != 2 or t.shape[0] != rows:
+        raise ValueError(f"expected a matrix with {rows} rows")
+    return t.T.contiguous()
+
+
+def _sparse_rows(H2EM, ctx: Context, N: int):
+    """(n_rows, rows, cols, vals) device triplets of a sparse sensor matrix given
+    dense (n x N), as a torch sparse tensor, or as the (dense, columns, values)
+    triple Head2EEGMat(sparse=True) returns."""
+    dev = _dev(ctx)
+    if isinstance(H2EM, tuple):
+        cols, vals = H2EM[1], H2EM[2]
+        cols = torch.as_tensor(cols).to(dev, torch.int64)
+        vals = torch.as_tensor(vals).to(dev, torch.float64)
+        n = cols.shape[0]
+        rows = torch.arange(n, device=dev, dtype=torch.int64)[:, None].expand_as(cols)
+        return n, rows.reshape(-1).contiguous(), cols.reshape(-1).contiguous(), vals.reshape(-1).contiguous()
+    t = H2EM if isinstance(H2EM, torch.Tensor) else torch.as_tensor(np.asarray(H2EM))
+    if t.is_sparse:
+        t = t.coalesce()
+        idx = t.indices().to(dev, torch.int64)
+        return t.shape[0], idx[0].contiguous(), idx[1].contiguous(), t.values().to(dev, torch.float64).contiguous()
+    t = t.to(dev, torch.float64)
+    if t.ndim != 2 or t.shape[1] != N:
+        raise ValueError(f"sensor matrix must have {N} columns")
+    nz = torch.nonzero(t, as_tuple=True)
+    return t.shape[0], nz[0].contiguous(), nz[1].contiguous(), t[nz].contiguous()
+
+
+def GainEEG(HMinv, DSM, H2EM, precision=FP64, ctx: Optional[Context] = None) -> torch.Tensor:
+    """GainEEG(HeadMatInv, SourceMat, Head2EEGMat) = (H2EM HMinv) DSM
+    (gain.h:69-76, om_gain -EEG) on the library's kernels.  HMinv: N x N or
+    SymMatrix packed upper; H2EM: dense, torch sparse, or Head2EEGMat(...,
+    sparse=True)'s triple.  Returns n_electrodes x n_dipoles."""
+    ctx = ctx or Context.default()
+    H, N, ld, packed = _inverse_operand(HMinv, ctx)
+    D = _cols_dev(DSM, ctx, N)
+    ne, r, c, v = _sparse_rows(H2EM, ctx, N)
+    nd = D.shape[0]
+    out = torch.empty((nd, ne), dtype=torch.float64, device=_dev(ctx))   # column-major ne x nd
+    check(ctx.lib.omg_gain_eeg_dev(ctx.handle, N, _ptr(H), ld, packed, _ptr(D), nd, ne, r.numel(), _ptr(r), _ptr(c),
+                                   _ptr(v), _prec(precision), _ptr(out)))
+    return out.T
+
+
+def GainMEG(HMinv, DSM, H2MM, DS2MM, precision=FP64, ctx: Optional[Context] = None) -> torch.Tensor:
+    """GainMEG(HeadMatInv, SourceMat, Head2MEGMat, Source2MEGMat) =
+    DS2MM + (H2MM HMinv) DSM (gain.h:60-67, om_gain -MEG) on the library's
+    kernels.  Returns n_squids x n_dipoles."""
+    ctx = ctx or Context.default()
+    H, N, ld, packed = _inverse_operand(HMinv, ctx)
+    D = _cols_dev(DSM, ctx, N)
+    nd = D.shape[0]
+    V = torch.as_tensor(H2MM if isinstance(H2MM, torch.Tensor) else np.asarray(H2MM)).to(_dev(ctx), torch.float64)
+    nm = V.shape[0]
+    if V.ndim != 2 or V.shape[1] != N:
+        raise ValueError(f"Head2MEGMat must have {N} columns")
+    Vc = V.T.contiguous()                                  # column-major nm x N
+    S = _cols_dev(DS2MM, ctx, nm)
+    if S.shape[0] != nd:
+        raise ValueError("DipSource2MEGMat must have one column per dipole")
+    out = torch.empty((nd, nm), dtype=torch.float64, device=_dev(ctx))
+    check(ctx.lib.omg_gain_meg_dev(ctx.handle, N, _ptr(H), ld, packed, _ptr(D), nd, _ptr(Vc), nm, _ptr(S),
+                                   _prec(precision), _ptr(out)))
+    return out.T
 
 
 def GainEEGadjoint(geom: Geometry, dipoles, electrodes, precision=FP64):

@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libomg_gb300.so")
-SOURCES = ["bem_kernels.cu", "dense_kernels.cu", "api.cpp", "batch.cpp", "geometry.cpp", "noalloc.cu", "tc_gemm.cu", "tc_residual.cu"]
+SOURCES = ["bem_kernels.cu", "dense_kernels.cu", "api.cpp", "batch.cpp", "geometry.cpp", "gain_direct.cu", "noalloc.cu",
+           "tc_gemm.cu", "tc_residual.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
