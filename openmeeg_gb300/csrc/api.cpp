@@ -135,6 +135,11 @@ void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int n
 void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
                 int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double sgn, double* R,
                 int64_t ldr, int* err, cudaStream_t s, const char* prof_name);
+// tc_solve.cu
+size_t sweep_scratch_bytes(int64_t nblocks, int64_t nrhs);
+void solve_sweep_tc(bool backward, int64_t N, int64_t nblocks, const float* W, int64_t w_rows, const float* A,
+                    const float* Ar, int64_t ld, float* B, int64_t ldb, int64_t nrhs, void* scratch, int* err,
+                    cudaStream_t s);
 void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
                      int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
                      int64_t ldr, int* err, cudaStream_t s);
@@ -797,10 +802,11 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
 // the diagonal-block inverses folded into W and the block rows of A, each
 // sweep is a chain of tensor-core updates by the not yet inverted blocks
 // (forward: b~_k = b_k - sum_{j<k} L_kj Linv_j b~_j; backward alike with
-// Linv_k L_kj), each update writing the K-major split of the block that the
-// next update takes (band copy); the inverses are then applied to all blocks
-// at once.  All blocks but the last have 128 rows (the vertex part starts on
-// a multiple of 128).
+// Linv_k L_kj); the inverses are then applied to all blocks at once.  Each
+// sweep runs as one persistent launch (tc_solve.cu); the fallback is one
+// tensor-core update per block, each writing the K-major split of the block
+// that the next update takes (band copy).  All blocks but the last have 128
+// rows (the vertex part starts on a multiple of 128).
 static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
     cudaStream_t s = sv->ctx->stream;
     const int64_t N = sv->N, ld = sv->ld32;
@@ -811,6 +817,22 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
     for (size_t b = 0; b + 1 < nblocks; ++b)
         if (sv->bounds[b + 1] - sv->bounds[b] != nb) throw Error(OMG_ERR_UNSUPPORTED, "solver blocks not 128 wide");
     const int n_last = (int)(N - sv->bounds[nblocks - 1]);
+    // W_b's heads start at K-major row 2 b N - 128 b (b + 1) (the layout the persistent sweep addresses)
+    bool w_layout = true;
+    for (size_t b = 0; b < nblocks; ++b)
+        w_layout = w_layout && sv->w_off[b] == (2 * (int64_t)b * N - 128 * (int64_t)b * (int64_t)(b + 1)) * nb;
+    if (w_layout && !std::getenv("OMG_SOLVE_CHAIN")) {
+        // one persistent launch per sweep (tc_solve.cu); OMG_SOLVE_CHAIN=1 selects the chain of one
+        // tensor-core update per block below (kept as the reference the sweep is tested against)
+        DevBuf scratch(sweep_scratch_bytes((int64_t)nblocks, nrhs), s);
+        solve_sweep_tc(false, N, (int64_t)nblocks, sv->W.as<float>(), sv->w_off[nblocks] / nb, nullptr, nullptr, 0, B,
+                       ldb, nrhs, scratch.p, sv->ctx->d_err, s);
+        apply_inv_blocks((int64_t)nblocks, nb, n_last, nrhs, sv->Linv32.as<float>(), false, B, ldb, s);
+        negate_rows<float>(B, ldb, sv->nP, N, nrhs, s);
+        solve_sweep_tc(true, N, (int64_t)nblocks, nullptr, 0, A, Ar, ld, B, ldb, nrhs, scratch.p, sv->ctx->d_err, s);
+        apply_inv_blocks((int64_t)nblocks, nb, n_last, nrhs, sv->Linv32.as<float>(), true, B, ldb, s);
+        return;
+    }
     const size_t xs = (size_t)nb * nrhs;
     DevBuf X(4 * xs * sizeof(float), s);
     float* xb[2] = {X.as<float>(), X.as<float>() + 2 * xs};   // heads, then remainders

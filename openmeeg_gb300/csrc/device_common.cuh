@@ -163,7 +163,10 @@ __device__ __forceinline__ bool stage_two(void* dstA, const void* srcA, uint32_t
     int any_fail = __syncthreads_or(!ok);
     if (any_fail) {
         if (threadIdx.x == 0) atomicExch(err, -8 /* OMG_ERR_TIMEOUT */);
-        mbar_wait_bounded(bar, 0);   // give in-flight copies a last bounded chance to land
+        // the copies may still be landing in this block's shared memory: drain them (a much longer, still
+        // bounded wait) before the block returns and its shared memory is reused
+        mbar_wait_bounded(bar, 0, 1u << 28);
+        __syncthreads();
         return false;
     }
     return true;

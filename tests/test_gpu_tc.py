@@ -346,3 +346,30 @@ def test_diagonal_block_panel_update(cuda):
         Linv = Li.view(128, 128).T.double()
         assert float(torch.linalg.norm(L @ Linv[:n, :n] - torch.eye(n, device="cuda", dtype=torch.float64))) < 1e-5
         assert float(A[n:, :].abs().max()) == 0.0 and float(A[:, n:].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("nrhs", [1, 215, 300])
+@pytest.mark.parametrize("name", ["ico2", "config0"])
+def test_persistent_sweep_solve(cuda, name, nrhs, monkeypatch):
+    """The mixed solver's triangular sweeps as one persistent launch each
+    (tiles of 64 right-hand sides claimed in dependency order, flags between
+    them) against the chain of one tensor-core update per block, and against a
+    dense FP64 solve; 215 and 300 right-hand sides take 4 and 5 column groups."""
+    from openmeeg_gb300 import api, workloads
+    w = workloads.small(2, layers=3, perturb=True) if name == "ico2" else workloads.config0()
+    geo = api.Geometry.from_head(w.head)
+    HM = api.HeadMat(geo, precision="mixed").cpu().numpy()
+    rng = np.random.default_rng(nrhs)
+    B = rng.standard_normal((HM.shape[0], nrhs))
+    sv = api.Solver(geo, precision="mixed")
+    X = sv.solve(B).cpu().numpy()
+    monkeypatch.setenv("OMG_SOLVE_CHAIN", "1")
+    Xc = sv.solve(B).cpu().numpy()
+    monkeypatch.delenv("OMG_SOLVE_CHAIN")
+    ref = np.linalg.solve(HM, B)
+    # both stop refining once the predicted error is below the solver's tolerance, 1e-6
+    e_sweep = np.linalg.norm(X - ref) / np.linalg.norm(ref)
+    e_chain = np.linalg.norm(Xc - ref) / np.linalg.norm(ref)
+    assert e_sweep <= 1e-6 and e_chain <= 1e-6, (e_sweep, e_chain)
+    X2 = sv.solve(B).cpu().numpy()          # flags and counters are reset for every sweep
+    assert np.array_equal(X, X2)
