@@ -225,10 +225,6 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-# Nominal FP32 CUDA-core issue rate of a GB300 (152 SMs x 128 lanes x 2.07 GHz),
-# used only to state how busy an FP32-pipe kernel keeps the cores.
-FP32_ISSUE_NOMINAL = 152 * 128 * 2.07e9
-FP64_NOMINAL = 1.25e12   # GB300 dense FP64 (FMA = 2 flops)
 # executed FP64 flops per near pair (DADD + DMUL + 2 DFMA thread instructions) of near_pairs_kernel, ncu at config1
 # (launch 3: 93,224 pairs, 1.735 GFLOP)
 FP64_FLOPS_PER_NEAR_PAIR = 1.735e9 / 93224
@@ -249,7 +245,34 @@ NCU_TRAFFIC_PER_UNIT = {
 }
 
 
-def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
+def pipe_peaks():
+    """Measured FMA instruction rates (per lane per second) of the FP32 and FP64
+    pipes of this GPU (the library's probe kernel: 8 independent FMA chains per
+    thread, 8 CTAs of 256 threads per SM, CUDA events); the rooflines of the
+    CUDA-core kernels are taken against these."""
+    import ctypes
+    from openmeeg_gb300 import _lib
+    lib = _lib.load()
+    lib.omg_internal_pipe_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    out = []
+    for kind in (0, 1):
+        v = ctypes.c_double()
+        if lib.omg_internal_pipe_peak(kind, ctypes.byref(v)) != 0:
+            raise RuntimeError("pipe peak probe failed")
+        out.append(v.value)
+    return {"fp32_fma_per_s": out[0], "fp64_fma_per_s": out[1]}
+
+
+def assembly_evaluations(head):
+    """Kernel evaluations of one head matrix (16-point rule): E_S = 16 (L T^2 / 2 + (L - 1) T^2) OperatorS and
+    E_D = 16 (3 L - 4) T^2 P1 single-layer evaluations for L nested meshes of T triangles each (self pairs,
+    adjacent pairs, barrier temporaries)."""
+    L = len(head.triangles)
+    T = head.triangles[0].shape[0]
+    return 16 * (L * T * T // 2 + (L - 1) * T * T), 16 * (3 * L - 4) * T * T
+
+
+def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_, pipes):
     """Roofline of one kernel over the timed region: achieved = algorithmic work
     per launch / mean launch duration (CUDA events around each launch on the
     library's stream).
@@ -297,9 +320,22 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
         info.update({"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": (tr * N * N) if tr else None,
                      "algorithmic_bytes_per_launch": nbytes,
-                     "fp32_issue_frac_of_nominal": fp32_ops / t_launch / FP32_ISSUE_NOMINAL,
+                     "fp32_issue_frac_of_measured": fp32_ops / t_launch / pipes["fp32_fma_per_s"],
                      "note": f"HBM fraction of {kind} copy bandwidth; the kernel is FP32-issue bound "
-                             f"(12 FP32 ops per multiply-add), see fp32_issue_frac_of_nominal"})
+                             f"(12 FP32 ops per multiply-add), see fp32_issue_frac_of_measured"})
+    elif name == "solve_sweep":
+        # one triangular sweep per launch (2 sweeps per solve, 2 solves per gain): nrhs N^2 algorithmic FP32
+        # flops per sweep (sum over blocks of 2 x 128 x rows below x nrhs), executed 3x as TF32 products;
+        # bounded by its dependency chain (one 128-row block product + epilogue + flag hand-over per block)
+        flops = k * N ** 2
+        achieved = flops / t_launch / 1e12
+        tf32_peak = bf16 / 2.0
+        info.update({"bound": "tensor (dependency chain)", "achieved": 3 * achieved, "peak": tf32_peak,
+                     "unit": "TFLOP/s", "frac": 3 * achieved / tf32_peak, "traffic": None,
+                     "algorithmic_fp32_tflops": achieved,
+                     "chain_us_per_block": t_launch * 1e6 / ((N + 127) // 128),
+                     "note": f"persistent sweep: executed TF32 tensor flops vs half the {kind} bf16 burst peak; the "
+                             f"141-block dependency chain bounds it (chain_us_per_block)"})
     elif name == "gemm_solve":
         # the FP32 solves: a dependent chain of tensor-core updates per sweep (one per 128-row block), each
         # sweep nrhs N^2 algorithmic flops (forward: sum over blocks of 2 (N - k1) nrhs 128), executed TF32
@@ -331,9 +367,10 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
         n7 = stats.get("_tri_pairs", 0) - stats.get("_pairs_6", 0)
         ops = 12.0 * (256 * n16 + 49 * n7) / per_step
         achieved = ops / t_launch
-        info.update({"bound": "fp32", "achieved": achieved / 1e12, "peak": FP32_ISSUE_NOMINAL / 1e12,
-                     "unit": "T FP32 op/s", "frac": achieved / FP32_ISSUE_NOMINAL, "traffic": None,
-                     "note": "FP32-pipe bound (rsqrt + FMA); peak is the nominal FP32 issue rate, not a measured one"})
+        peak = pipes["fp32_fma_per_s"]
+        info.update({"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12,
+                     "unit": "T FP32 op/s", "frac": achieved / peak, "traffic": None,
+                     "note": "FP32-pipe bound (rsqrt + FMA); peak: measured FP32 FMA instruction rate of this GPU"})
     elif name == "near_pairs":
         # FP64 analytic near-pair integrals (OperatorS, P1 single layer both ways at the 16 points of the rule):
         # FP64 operations executed per near pair from an ncu capture (thread-level DADD + DMUL + 2 DFMA, the
@@ -341,11 +378,25 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_):
         pairs = stats.get("_near_pairs", 0)
         flops = FP64_FLOPS_PER_NEAR_PAIR * pairs / per_step
         achieved = flops / t_launch
-        info.update({"bound": "fp64", "achieved": achieved / 1e12, "peak": FP64_NOMINAL / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / FP64_NOMINAL, "traffic": NCU_TRAFFIC_PER_UNIT["near_pairs"] * pairs / per_step,
+        peak = 2.0 * pipes["fp64_fma_per_s"]
+        info.update({"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": NCU_TRAFFIC_PER_UNIT["near_pairs"] * pairs / per_step,
                      "near_pairs_per_launch": pairs / per_step,
-                     "note": "executed FP64 flops (ncu op counts per near pair) vs the nominal GB300 FP64 rate "
-                             "(1.25 TFLOP/s; no measured FP64 peak); the same capture shows the FP64 pipe 88% active"})
+                     "evals_per_s": 16 * 3 * pairs / per_step / t_launch,
+                     "note": "executed FP64 flops (ncu op counts per near pair) vs the measured FP64 FMA rate of "
+                             "this GPU (x2 flops); evals_per_s counts the 16 OperatorS + 32 P1 single-layer "
+                             "evaluations of each near pair"})
+    elif name == "dsm":
+        # DipSourceMat: the first adaptive level of every (dipole, triangle) pair in FP32 (both integrands at
+        # the 16 rule points of the triangle and of its 4 halves: 80 points), the pairs that level does not
+        # settle by the FP64 recursion; runs on the second stream under the solves
+        T = stats.get("_triangles", 0)
+        evals = 80.0 * nd * T / per_step
+        info.update({"bound": "fp32 (FP64 on the unsettled pairs)", "achieved": None, "peak": None, "unit": None,
+                     "frac": None, "traffic": None, "evals_per_s": evals / t_launch,
+                     "note": "first-level integrand evaluations (80 points per dipole-triangle pair) per second; "
+                             "the launch overlaps the solves on the second stream, so its event time includes "
+                             "waiting for SMs"})
     elif name in ("potrf_inv", "apply_inv"):
         info.update({"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
                      "note": "one diagonal block per launch (128 x 128, one CTA), sequential over the blocks: "
@@ -505,19 +556,31 @@ def run_gpu(args):
         w.dipoles.nbytes + w.electrodes.nbytes + (w.squids.nbytes if nm else 0)
     d2h = 8 * nd * (ne + nm)
 
-    # roofline of the dominant kernel over the timed region
+    # roofline of the dominant kernel over the timed region: the largest kernel on the main streams
+    # (DipSourceMat runs on the second stream under the solves; its event time includes waiting for SMs)
     pk = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
+    pipes = pipe_peaks()
+    main = {n: v for n, v in prof.items() if n != "dsm"}
+    dom = max(main.items(), key=lambda kv: kv[1][1]) if main else ("none", (0, 0.0))
     dname, (dl, dms) = dom
     total_prof_ms = sum(v[1] for v in prof.values())
     stx_r = dict(stx)
     stx_r["_tri_pairs"] = tri_pairs(w.head)
     stx_r["_near_pairs"] = near_pairs_count(w.head)
     stx_r["_pairs_6"] = near_pairs_count(w.head, 6.0)   # pairs below the 7-point far-field tier
-    roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx_r, pk)
-    others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx_r, pk)
-              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block", "near_pairs")
+    stx_r["_triangles"] = sum(t.shape[0] for t in w.head.triangles)
+    roof = roofline_entry(dname, dl, dms, args.profile_steps, N, ne + nm, nd, stx_r, pk, pipes)
+    roof["dominant_rule"] = "largest profiled kernel on the main streams (DipSourceMat overlaps on the second one)"
+    others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx_r, pk, pipes)
+              for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block", "near_pairs",
+                                                 "solve_sweep", "dsm")
               and n != dname}
+    e_s, e_d = assembly_evaluations(w.head)
+    assembly = {"evaluations_per_headmat": {"E_S": e_s, "E_D": e_d},
+                "mixed_evals_per_s": (e_s + e_d) / (stx["t_headmat_ms"] / 1e3),
+                "fp64_evals_per_s": (e_s + e_d) / (st64["t_headmat_ms"] / 1e3),
+                "note": "E_S + E_D kernel evaluations of the 16-point rule per head matrix over the head-matrix "
+                        "stage time (mixed: FP32 far pairs, FP64 analytic near pairs; FP64: all analytic)"}
 
     cfg = workload_config(args.config, N, nd, ne, nm)
     cpu = None
@@ -541,8 +604,6 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32+f64 (mixed); f64 drop-in timed beside it",
             "data": "synthetic (seeded nested icosphere heads, dipoles, Fibonacci sensors)",
             "config": cfg,
-            "fp64_s": t_fp64, "speedup_vs_fp64": t_fp64 / t_step,
-            "rel_err_vs_fp64": {"eeg": err_eeg, "meg": err_meg},
             "mixed_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stx.items()},
             "fp64_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st64.items()},
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -554,8 +615,14 @@ def run_gpu(args):
             "profile_note": "per-kernel CUDA-event times from separate profiled steps (not the timed ones)",
             "roofline": roof,
             "roofline_other": others,
+            "assembly": assembly,
+            "pipe_peaks_measured": pipes,
             "clocks": ck,
             "cpu_baseline": cpu,
+            # last, so that the end of the line carries the metric's own comparison
+            "fp64_s": t_fp64, "fp64_steps": len(f64_times),
+            "rel_err_vs_fp64": {"eeg": err_eeg, "meg": err_meg},
+            "speedup_vs_fp64": t_fp64 / t_step,
         }
         print(json.dumps(line))
     if world > 1:
@@ -734,7 +801,7 @@ def run_adjoint(args):
     torch.cuda.set_device(local)
     __import__("__graft_entry__").build()
     from openmeeg_gb300 import adjoint, api, workloads
-    w = workloads.config2()
+    w = workloads.config2(base=args.head)
     ctx = api.Context(local)
     geo = api.Geometry.from_head(w.head, ctx)
     dev = torch.device("cuda", local)
@@ -793,7 +860,8 @@ def run_adjoint(args):
     mix_dip = float(np.linalg.norm(grads["mixed"][1] - gd64) / np.linalg.norm(gd64))
     line = {"metric": "gain + gradient time (s), config2", "unit": "s", "n_gpus": 1,
             "value": res["mixed"]["forward_s"] + res["mixed"]["backward_s"], "higher_is_better": False,
-            "config": {"workload": "config2: config1 geometry (N=%d), 500 dipoles, sigma sampled x[0.5,2]" % geo.size,
+            "config": {"workload": "config2: %s geometry (N=%d), 500 dipoles, sigma sampled x[0.5,2]" % (args.head,
+                                                                                                      geo.size),
                        "fd_step": "1e-6 relative (conductivities), 1e-6 absolute (dipoles)",
                        "fd_dipole_coordinates": len(sample)},
             "results": res,
@@ -818,7 +886,7 @@ def run_next(args):
     __import__("__graft_entry__").build()
     from openmeeg_gb300 import api, workloads
     from openmeeg_gb300 import synthetic as syn
-    w = workloads.config1()
+    w = getattr(workloads, args.head)()
     ctx = api.Context(local)
     ctx.bind_current_stream()
     geo = api.Geometry.from_head(w.head, ctx)
@@ -895,7 +963,7 @@ def run_next(args):
     line = {"metric": "time per call (ms) of the rows beside the forward path, config1 head", "unit": "ms",
             "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"config1 head (N={geo.size}); ico3 source surface (642 vertices) in the brain; "
+            "config": {"workload": f"{args.head} head (N={geo.size}); ico3 source surface (642 vertices) in the brain; "
                                    f"5000 points (r < 1.1), {dip.shape[0]} dipoles, 64 EIT electrodes (r = 0.05), "
                                    f"{sq_d.shape[0]} magnetometers"},
             "rows": rows, "clocks": ck}
@@ -914,7 +982,9 @@ def main():
     ap.add_argument("--large-precisions", default="mixed,fp64", help="config4: precisions to run, in order")
     ap.add_argument("--fd-dipoles", type=int, default=4, help="config2: dipole coordinates checked by differences")
     ap.add_argument("--analytic-dipoles", type=int, default=500, help="config4: dipoles checked analytically")
-    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--head", default="config1", choices=["config0", "config1"],
+                    help="config2 / next: the head the rows run on (config0: a small profiling case)")
+    ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--profile-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")

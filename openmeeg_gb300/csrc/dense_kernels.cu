@@ -1158,3 +1158,66 @@ extern "C" int omg_internal_potrf_inv(int n, float* A, int64_t lda, float* Linv,
     cudaFree(scratch);
     return rc;
 }
+
+namespace omg {
+
+// ---------------------------------------------------------------------------
+// Pipe peaks for the rooflines of the CUDA-core kernels (no measured FP32 /
+// FP64 figure comes with the machine): every thread runs 8 independent FMA
+// chains for `iters` steps, a grid of 8 CTAs of 256 threads per SM.  Returns
+// FMA instructions (per lane) per second, timed with CUDA events.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) fma_peak_kernel(int iters, T a, T b, T* out) {
+    T x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = (T)(threadIdx.x + c);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = x[c] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += x[c];
+    if (s == (T)-1.2345) out[0] = s;   // keeps the chains alive; never true for these inputs
+}
+
+template <typename T>
+static double fma_peak(int iters) {
+    int dev = 0, n_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    T* out = nullptr;
+    OMG_CUDA(cudaMalloc(&out, sizeof(T)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const unsigned grid = (unsigned)n_sm * 8;
+    fma_peak_kernel<T><<<grid, 256>>>(iters / 10, (T)0.999, (T)0.001, out);   // warm-up
+    count_launch(2);
+    cudaEventRecord(e0);
+    fma_peak_kernel<T><<<grid, 256>>>(iters, (T)0.999, (T)0.001, out);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    OMG_CUDA(cudaGetLastError());
+    return (double)grid * 256 * 8 * iters / (ms * 1e-3);
+}
+
+}  // namespace omg
+
+// Measurement hook (not part of the public header): FMA instructions per
+// second of the FP32 (kind 0) or FP64 (kind 1) pipe of the current device.
+extern "C" int omg_internal_pipe_peak(int kind, double* fma_per_s) {
+    try {
+        *fma_per_s = kind == 0 ? omg::fma_peak<float>(1 << 16) : omg::fma_peak<double>(1 << 12);
+        return 0;
+    } catch (const omg::Error& e) {
+        return e.code;
+    }
+}
+

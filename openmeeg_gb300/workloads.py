@@ -48,8 +48,10 @@ def config1(n_dipoles: int = 2000) -> Workload:
                     syn.fibonacci_points(64, 1.0), syn.radial_magnetometers(151, 1.2))
 
 
-def config2(n_dipoles: int = 500) -> Workload:
-    w = config1(n_dipoles)
+def config2(n_dipoles: int = 500, base: str = "config1") -> Workload:
+    """config1's geometry (or `base`'s, e.g. config0 for a small profiling case)
+    with conductivities sampled log-uniformly within x[0.5, 2] of nominal."""
+    w = config1(n_dipoles) if base == "config1" else config0(n_dipoles)
     rng = np.random.default_rng(SEED + 4)
     sig = [d[2] for d in w.head.domains]
     new = []
