@@ -1233,6 +1233,79 @@ __device__ void dsm_adaptive(int kind, int order, int levels, double tol, const 
     result[0] = total[0]; result[1] = total[1]; result[2] = total[2];
 }
 
+// The same integration by a group of four lanes (lanes 4 g .. 4 g + 3 of a
+// warp, `mask` their bits): each node's four children are integrated one per
+// lane, each child's rule summed in the order of dsm_rule, and the values are
+// exchanged by shuffles, so every refinement decision and every sum is the
+// one of dsm_adaptive; the four lanes run the same control flow.
+__device__ void dsm_adaptive_g4(int kind, int order, int levels, double tol, const DsmTri& T, d3 r0, d3 q, d3 R0,
+                                d3 R1, d3 R2, double area, double result[3], unsigned mask, int lane4) {
+    double coarse[3];
+    dsm_rule(kind, order, T, r0, q, R0, R1, R2, area, coarse);
+    if (levels == 0) {
+        result[0] = coarse[0]; result[1] = coarse[1]; result[2] = coarse[2];
+        return;
+    }
+    const int base = (threadIdx.x & 31) & ~3;
+    uint32_t st_path[DSM_STACK];
+    int8_t st_depth[DSM_STACK], st_level[DSM_STACK];
+    double st_c[DSM_STACK][3];
+    int sp = 0;
+    st_path[0] = 0; st_depth[0] = 0; st_level[0] = (int8_t)levels;
+    st_c[0][0] = coarse[0]; st_c[0][1] = coarse[1]; st_c[0][2] = coarse[2];
+    sp = 1;
+    double total[3] = {0.0, 0.0, 0.0};
+    const int dim = kind == 0 ? 3 : 1;
+    while (sp > 0) {
+        --sp;
+        const uint32_t path = st_path[sp];
+        const int depth = st_depth[sp], level = st_level[sp];
+        const double c0 = st_c[sp][0], c1 = st_c[sp][1], c2 = st_c[sp][2];
+        d3 P0 = R0, P1 = R1, P2 = R2;
+        double a = area;
+        for (int d = 0; d < depth; ++d) {
+            subtriangle(P0, P1, P2, (path >> (2 * d)) & 3);
+            a *= 0.25;
+        }
+        const double sub = 0.25 * a;
+        double mine[3];
+        {
+            d3 Q0 = P0, Q1 = P1, Q2 = P2;
+            subtriangle(Q0, Q1, Q2, lane4);
+            dsm_rule(kind, order, T, r0, q, Q0, Q1, Q2, sub, mine);
+        }
+        double integ[4][3];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) integ[c][k] = __shfl_sync(mask, mine[k], base + c);
+        double ref[3] = {0.0, 0.0, 0.0};
+        for (int c = 0; c < 4; ++c)
+            for (int k = 0; k < dim; ++k) ref[k] += integ[c][k];
+        double dn, cn;
+        if (dim == 1) {
+            dn = fabs(c0 - ref[0]);
+            cn = fabs(c0);
+        } else {
+            const double e0 = c0 - ref[0], e1 = c1 - ref[1], e2 = c2 - ref[2];
+            dn = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+            cn = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+        }
+        if (dn <= tol * cn || level == 0) {
+            for (int k = 0; k < dim; ++k) total[k] += ref[k];
+            continue;
+        }
+        for (int c = 3; c >= 0; --c) {
+            st_path[sp] = path | ((uint32_t)c << (2 * depth));
+            st_depth[sp] = (int8_t)(depth + 1);
+            st_level[sp] = (int8_t)(level - 1);
+            st_c[sp][0] = integ[c][0]; st_c[sp][1] = integ[c][1]; st_c[sp][2] = integ[c][2];
+            ++sp;
+        }
+    }
+    result[0] = total[0]; result[1] = total[1]; result[2] = total[2];
+}
+
 
 // Mixed precision: the first adaptive level in FP32 with coordinates relative
 // to the triangle centroid.  The FP32 value is kept only when the acceptance
@@ -1298,16 +1371,20 @@ __device__ void dsm_first_level2_f32(double tol, const DsmTriF& T, float3 xc, fl
     dsm_rule2_f(T, xc, q, m0, R1, m2, sub, b);
     dsm_rule2_f(T, xc, q, m0, m1, R2, sub, c);
     dsm_rule2_f(T, xc, q, m0, m1, m2, sub, d);
-    double ref[4], dnv = 0.0, cnv = 0.0;
-    for (int k = 0; k < 4; ++k) ref[k] = (double)a[k] + (double)b[k] + (double)c[k] + (double)d[k];
+    // the sums and the test in FP32 (GB300's FP64 pipe runs at 1/64 of the FP32 rate): their rounding,
+    // ~1e-7 of |coarse|, is far inside the factor-2 margin of the test (tol / 2 = 5e-4 of |coarse|)
+    float ref[4], dnv = 0.f, cnv = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ref[k] = (a[k] + b[k]) + (c[k] + d[k]);
+#pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const double e = (double)coarse[k] - ref[k];
-        dnv += e * e;
-        cnv += (double)coarse[k] * (double)coarse[k];
+        const float e = coarse[k] - ref[k];
+        dnv = fmaf(e, e, dnv);
+        cnv = fmaf(coarse[k], coarse[k], cnv);
     }
-    const double ep = (double)coarse[3] - ref[3];
-    okv = sqrt(dnv) <= 0.5 * tol * sqrt(cnv);
-    okp = fabs(ep) <= 0.5 * tol * fabs((double)coarse[3]);
+    const float ht = 0.5f * (float)tol;
+    okv = dnv <= ht * ht * cnv;
+    okp = fabsf(coarse[3] - ref[3]) <= ht * fabsf(coarse[3]);
     for (int k = 0; k < 3; ++k) v[k] = ref[k];
     p[0] = ref[3];
 }
@@ -1445,12 +1522,15 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
         bool f32v, f32p;
         dsm_first_level2_f32(tol, R.T, xc, qf, R.T.p0, R.F1, R.F2, R.area, v, pf, f32v, f32p);
         f32p = f32p && p0row;
+        // FP32-accurate values: scaled in FP32 (an FP64 division per pair costs more than the pair's
+        // FP32 work on GB300)
+        const float cf = (float)P.coeffD;
         if (f32v) {
-            o3[0] = v[0] * P.coeffD;
-            o3[1] = v[1] * P.coeffD;
-            o3[2] = v[2] * P.coeffD;
+            o3[0] = (double)((float)v[0] * cf);
+            o3[1] = (double)((float)v[1] * cf);
+            o3[2] = (double)((float)v[2] * cf);
         }
-        if (f32p) out[row + i * ldo] = pf[0] * (P.coeffD / P.sigma);
+        if (f32p) out[row + i * ldo] = (double)((float)pf[0] * (cf / (float)P.sigma));
         const int need = (f32v ? 0 : 1) | (p0row && !f32p ? 2 : 0);
         if (need) left[atomicAdd(nleft, 1)] = make_int2((int)il, (int)t | (need << DSM_T_BITS));
         return;
@@ -1470,7 +1550,8 @@ __global__ void dsm_kernel(int64_t dip0, int64_t ndc, const double* __restrict__
 }
 
 // The listed pairs of the mixed first pass: FP64 adaptive integration of the
-// integrals FP32 did not settle (grid-stride over the device-side count).
+// integrals FP32 did not settle (grid-stride over the device-side count, four
+// lanes per pair; block size a multiple of 32).
 __global__ void dsm_fallback_kernel(int64_t dip0, int64_t nt, const double* __restrict__ dip,
                                     const double* __restrict__ srec, const int32_t* __restrict__ tmesh,
                                     const int64_t* __restrict__ tidx_ref, const int* __restrict__ orient,
@@ -1479,8 +1560,12 @@ __global__ void dsm_fallback_kernel(int64_t dip0, int64_t nt, const double* __re
                                     const double* __restrict__ dsigma, int order, int levels, double tol, int64_t nv,
                                     int perm, double* out, int64_t ldo, double* p1tmp, const int2* __restrict__ left,
                                     const int* __restrict__ nleft) {
+    // one group of four lanes per listed pair (the children of every node are integrated in parallel)
     const int n = *nleft;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31, lane4 = lane & 3;
+    const unsigned mask = 0xFu << (lane & ~3);
+    const int groups = (int)(gridDim.x * blockDim.x / 4);
+    for (int idx = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 4); idx < n; idx += groups) {
         const int2 e = left[idx];
         const int64_t il = e.x, t = e.y & ((1 << DSM_T_BITS) - 1);
         const int need = (int)((unsigned)e.y >> DSM_T_BITS);
@@ -1489,17 +1574,19 @@ __global__ void dsm_fallback_kernel(int64_t dip0, int64_t nt, const double* __re
         if (!dsm_pair(i, t, dip, srec, tmesh, orient, dom, maxb, dnb, bmesh, binside, dsigma, P)) continue;
         if (need & 1) {
             double v[3];
-            dsm_adaptive(0, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, v);
-            double* o3 = p1tmp + (il * nt + t) * 3;
-            o3[0] = v[0] * P.coeffD;
-            o3[1] = v[1] * P.coeffD;
-            o3[2] = v[2] * P.coeffD;
+            dsm_adaptive_g4(0, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, v, mask, lane4);
+            if (lane4 == 0) {
+                double* o3 = p1tmp + (il * nt + t) * 3;
+                o3[0] = v[0] * P.coeffD;
+                o3[1] = v[1] * P.coeffD;
+                o3[2] = v[2] * P.coeffD;
+            }
         }
         if (need & 2) {
             double p[3];
-            dsm_adaptive(1, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, p);
+            dsm_adaptive_g4(1, order, levels, tol, P.T, P.r0, P.q, P.R0, P.R1, P.R2, P.area, p, mask, lane4);
             const int64_t ref = tidx_ref[t];
-            out[(perm ? ref - nv : ref) + i * ldo] = p[0] * (P.coeffD / P.sigma);
+            if (lane4 == 0) out[(perm ? ref - nv : ref) + i * ldo] = p[0] * (P.coeffD / P.sigma);
         }
     }
 }
