@@ -2093,8 +2093,9 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
                           const double* sq, int64_t nm, double* geeg, double* gmeg, omg_gain_stats* st) {
     cudaStream_t s = ctx->stream;
     const int64_t N = geo->dg.N, k = ne + nm;
-    cudaEvent_t ev[7];
+    cudaEvent_t ev[7], ev_src;
     for (auto& e : ev) OMG_CUDA(cudaEventCreate(&e));
+    OMG_CUDA(cudaEventCreateWithFlags(&ev_src, cudaEventDisableTiming));
     OMG_CUDA(cudaEventRecord(ev[0], s));
     reset_err(ctx);
     const int64_t live0 = g_dev_live.load();
@@ -2144,11 +2145,13 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaEventRecord(ev[2], s));
     solver_factor(sv.get(), std::move(hm));
     OMG_CUDA(cudaEventRecord(ev[3], s));
-    {   // after the factorization's last work on the second stream (stream order)
+    {   // after the factorization's last work on the second stream (stream order); every stage of the
+        // pipeline is throughput-bound, so the sources run where they take the least (under the assembly
+        // they slowed the FP64-bound near-pair kernel by more than they saved later)
         StreamSwap on_aux(ctx, s2);
         dsm_internal(geo, dip, nd, dsm_it, -1, 1, DSM.as<double>(), N, precision, nullptr, 0, &dom);
         if (nm > 0) launch_ds2mm(dip, nd, sq, nm, gmeg, nm, s2);
-        OMG_CUDA(cudaEventRecord(ev[6], s2));
+        OMG_CUDA(cudaEventRecord(ev_src, s2));
     }
     {   // the solves on the highest-priority stream, ordered after the main stream's work and back
         OMG_CUDA(cudaEventRecord(ev[5], s));
@@ -2160,7 +2163,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
         }
         OMG_CUDA(cudaStreamWaitEvent(s, ev[5], 0));
     }
-    OMG_CUDA(cudaStreamWaitEvent(s, ev[6], 0));
+    OMG_CUDA(cudaStreamWaitEvent(s, ev_src, 0));
     // the factor is not needed past the solves: its memory (the FP32 factor, its copies and the digit planes,
     // most of the device at the largest heads) is returned before the contraction allocates its digits
     const int sv_steps = sv->last_steps;
@@ -2194,6 +2197,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
         st->device_bytes = g_dev_peak.load() - live0;
     }
     for (auto& e : ev) cudaEventDestroy(e);
+    cudaEventDestroy(ev_src);
 }
 
 int omg_gain_dev(omg_context ctx, omg_geometry geo, int32_t precision, const omg_integrator* hm_integ,
