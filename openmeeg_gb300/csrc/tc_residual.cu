@@ -20,10 +20,17 @@
 // matrix itself carries the mixed assembly's ~1e-8 error).
 //
 // Persistent and warp-specialized like the 3xTF32 GEMM: warp 0 streams
-// 128 x 64 bf16 tiles of the A digits and of the X digits (TMA, 128-byte
-// swizzle) through a four-stage ring, warp 1 issues
-// tcgen05.mma.cta_group::1.kind::f16 (M=128, N=128, K=16) into two TMEM
-// accumulators (one per window, alternating), warps 2-9 drain the windows.
+// 128 x 64 bf16 tiles of the A digits and up to 256 x 64 tiles of the X
+// digits (TMA, 128-byte swizzle) through a three-stage ring, warp 1 issues
+// tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = nmma <= 256, K = 16) into
+// two TMEM accumulators of 256 columns (one per window, alternating), warps
+// 2-17 drain the windows (warp w: TMEM lanes 32 (w % 4) .. +31, columns
+// 64 ((w - 2) / 4) .. +63).  An output tile covers up to 256 columns, so a
+// residual with <= 256 right-hand sides streams each A digit plane once per
+// digit pair it takes part in (3.5 times per plane on average for 21 pairs
+// of 6 digits), not once per pair and 128-column block.  Keeping the level
+// sums of all six levels on chip at once, which would stream each plane once,
+// needs 6 accumulators of the tile's width: more than the 512 TMEM columns.
 // Output tiles of one row block are adjacent in the walk, so the CTAs that
 // share a row block stream the same A digits at the same time (L2 reuse).
 // Every wait is bounded; on timeout the kernel records OMG_ERR_TIMEOUT, all
@@ -41,15 +48,17 @@ namespace tcr {
 using tc::fence_after;
 using tc::fence_before;
 
-constexpr int BM = 128, BN = 128, BK = 64;        // BK bf16 = 128 bytes per swizzled row
-constexpr int STAGES = 4;
-constexpr int TILE_BYTES = BM * BK * 2;           // 16 KiB
-constexpr int STAGE_BYTES = 2 * TILE_BYTES;       // A digits, X digits
-constexpr int SMEM_INT_BYTES = 64 * 256 * 4;      // per-thread spill of the level sums (64 columns x 256 threads)
+constexpr int BM = 128, BN = 256, BK = 64;        // BN: widest tile (MMA N); BK bf16 = 128 bytes per swizzled row
+constexpr int STAGES = 3;
+constexpr int TILE_A = BM * BK * 2;               // 16 KiB
+constexpr int TILE_X = BN * BK * 2;               // 32 KiB (room for the widest tile)
+constexpr int STAGE_BYTES = TILE_A + TILE_X;
+constexpr int EPI_WARPS = 16;
+constexpr int THREADS = 64 + EPI_WARPS * 32;      // 576
+constexpr int SPILL = 32;                         // level-sum columns a thread hands to the FP64 pass at a time
+constexpr int SMEM_INT_BYTES = SPILL * EPI_WARPS * 32 * 4;   // 64 KiB
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + SMEM_INT_BYTES + 1024;
-constexpr int THREADS = 320;
-constexpr int EPI_WARPS = 8;
-constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t TMEM_COLS = 512;
 constexpr int KC = 256;                           // exact-accumulation window
 constexpr int CPW = KC / BK;                      // chunks per window
 constexpr int MAXPAIRS = 64;
@@ -61,9 +70,10 @@ struct RowRanges {
     int64_t beg[MAXRANGES], len[MAXRANGES];
 };
 
-// Instruction descriptor: D=F32, A=B=BF16, both K-major, N=128, M=128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// Instruction descriptor: D=F32, A=B=BF16, both K-major, M=128, N=n (a multiple of 16, <= 256).
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
 
 struct PairPlan {
     int n;                       // digit pairs, ordered by level s + t
@@ -72,18 +82,18 @@ struct PairPlan {
     uint8_t s[MAXPAIRS], t[MAXPAIRS];
 };
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
             tmem),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     residual_slices_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tX,
                            const __grid_constant__ PairPlan plan, int N, int k, int kpad, int beta,
                            const int* __restrict__ rexp, const int* __restrict__ cexp, double sgn, double* R,
-                           int64_t ldr, int64_t ntiles, int ncb, int* err) {
+                           int64_t ldr, int64_t ntiles, int ncb, int nmma, int* err) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -127,7 +137,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int rb = (int)(t / ncb), cb = (int)(t % ncb);
                 for (int u = 0; u < units && !s_abort; ++u) {
                     const int p = u / plan.nwin, w = u % plan.nwin;
-                    const int ya = (plan.s[p] - 1) * N + rb * BM, yx = (plan.t[p] - 1) * kpad + cb * BN;
+                    const int ya = (plan.s[p] - 1) * N + rb * BM, yx = (plan.t[p] - 1) * kpad + cb * nmma;
                     for (int c = 0; c < CPW; ++c, ++g) {
                         const int slot = (int)(g % STAGES);
                         if (!tc::wait_or_abort(&empty_bar[slot], (uint32_t)(((g / STAGES) & 1) ^ 1), &s_abort)) {
@@ -136,9 +146,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                         }
                         const uint32_t st = sbase + slot * STAGE_BYTES;
                         const int x = (w * CPW + c) * BK;
-                        dev::mbar_expect_tx(&full_bar[slot], STAGE_BYTES);
+                        dev::mbar_expect_tx(&full_bar[slot], TILE_A + nmma * BK * 2);
                         tc::tma_load_2d(st, &tA, x, ya, &full_bar[slot]);
-                        tc::tma_load_2d(st + TILE_BYTES, &tX, x, yx, &full_bar[slot]);
+                        tc::tma_load_2d(st + TILE_A, &tX, x, yx, &full_bar[slot]);
                         s_issued = g + 1;
                     }
                 }
@@ -148,6 +158,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {   // ---- MMA issuer
             int64_t g = 0, lu = 0;
             bool ok = true;
+            const uint32_t idesc = idesc_bf16(nmma);
             for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 for (int u = 0; u < units && ok; ++u, ++lu) {
                     const uint32_t ab = (uint32_t)(lu & 1), aph = (uint32_t)((lu >> 1) & 1);
@@ -166,11 +177,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                         s_consumed = g + 1;
                         fence_after();
                         const uint32_t st = sbase + slot * STAGE_BYTES;
-                        const uint64_t dA = tc::sdesc_sw128(st), dX = tc::sdesc_sw128(st + TILE_BYTES);
+                        const uint64_t dA = tc::sdesc_sw128(st), dX = tc::sdesc_sw128(st + TILE_A);
 #pragma unroll
                         for (int kk = 0; kk < BK / 16; ++kk) {
                             const uint64_t off = (uint64_t)(kk * 32) >> 4;   // 16 bf16 = 32 bytes
-                            mma_bf16(acc, dA + off, dX + off, (c | kk) != 0 ? 1u : 0u);
+                            mma_bf16(acc, dA + off, dX + off, idesc, (c | kk) != 0 ? 1u : 0u);
                         }
                         tc::mma_commit(&empty_bar[slot]);
                     }
@@ -182,14 +193,17 @@ __global__ void __launch_bounds__(THREADS, 1)
             tc::mma_commit(&fin_bar);
             if (!dev::mbar_wait_bounded(&fin_bar, 0)) s_abort = 1;
         }
-    } else {   // ---- epilogue: warp w owns TMEM lanes 32 * (w % 4) .. +31 and 64 of the 128 columns
+    } else {   // ---- epilogue: warp w owns TMEM lanes 32 (w % 4) .. +31 and columns 64 ((w - 2) / 4) .. +63
         const int q = warp & 3;
-        const int half = (warp - 2) / 4;
+        const int grp = (warp - 2) >> 2;
+        const bool active = grp * 64 < nmma;   // warp-uniform: columns past the MMA width hold nothing
+        int* const si = s_int + (warp - 2) * 32 + lane;
         int64_t lu = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int rb = (int)(t / ncb), cb = (int)(t % ncb);
             const int row = rb * BM + q * 32 + lane;
-            const int c0 = cb * BN + half * 64;
+            const int c0 = cb * nmma + grp * 64;
+            const int cend = min(64, nmma - grp * 64);   // the group's columns inside this tile
             const int er = row < N ? rexp[row] : 0;
             int iacc[64];
 #pragma unroll
@@ -205,34 +219,39 @@ __global__ void __launch_bounds__(THREADS, 1)
                     break;
                 }
                 fence_after();
+                if (active) {
 #pragma unroll
-                for (int chunk = 0; chunk < 2; ++chunk) {
-                    uint32_t r[32];
-                    tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(half * 64 + chunk * 32), r);
+                    for (int chunk = 0; chunk < 4; ++chunk) {
+                        uint32_t r[16];
+                        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + ab * BN + (uint32_t)(grp * 64 + chunk * 16),
+                                      r);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j)   // |window sum| < 2^22: adding 1.5 * 2^23 puts it in the mantissa
-                        iacc[chunk * 32 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
+                        for (int j = 0; j < 16; ++j)   // |window sum| < 2^22: adding 1.5 * 2^23 puts it in the mantissa
+                            iacc[chunk * 16 + j] += __float_as_int(__uint_as_float(r[j]) + 12582912.0f) - 0x4B400000;
+                    }
                 }
                 fence_before();
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&tempty_bar[ab]);
                 const int p = u / plan.nwin, w = u % plan.nwin;
-                if (w == plan.nwin - 1 && ((plan.flush >> p) & 1ull)) {   // level sum -> R (FP64)
-                    // through shared memory so the (rare) FP64 pass does not hold 64 more registers
-                    int* si = s_int + (warp - 2) * 32 + lane;
-#pragma unroll
-                    for (int j = 0; j < 64; ++j) {
-                        si[j * (EPI_WARPS * 32)] = iacc[j];
-                        iacc[j] = 0;
-                    }
+                if (active && w == plan.nwin - 1 && ((plan.flush >> p) & 1ull)) {   // level sum -> R (FP64)
+                    // 32 columns at a time through shared memory, so the (rare) FP64 pass holds few registers
                     const int lev = plan.s[p] + plan.t[p];
-                    if (row < N) {
-                        double* rp = R + row;
-                        for (int j = 0; j < 64; ++j) {
-                            const int col = c0 + j;
-                            const int v = si[j * (EPI_WARPS * 32)];
-                            if (col < k && v != 0)
-                                rp[(int64_t)col * ldr] += sgn * scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
+#pragma unroll
+                    for (int h = 0; h < 64 / SPILL; ++h) {
+#pragma unroll
+                        for (int j = 0; j < SPILL; ++j) {
+                            si[j * (EPI_WARPS * 32)] = iacc[h * SPILL + j];
+                            iacc[h * SPILL + j] = 0;
+                        }
+                        if (row < N) {
+                            for (int j = 0; j < SPILL; ++j) {
+                                const int col = c0 + h * SPILL + j;
+                                const int v = si[j * (EPI_WARPS * 32)];
+                                if (h * SPILL + j < cend && col < k && v != 0) {
+                                    R[row + (int64_t)col * ldr] += sgn * scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
+                                }
+                            }
                         }
                     }
                 }
@@ -415,7 +434,7 @@ void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, con
                 int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double sgn, double* R,
                 int64_t ldr, int* err, cudaStream_t s, const char* prof_name) {
     if (n <= 0 || k <= 0) return;
-    if (n > (1 << 30) / 8 || kdim <= 0 || kpad % tcr::BN) throw Error(OMG_ERR_INVALID, "digit GEMM: bad sizes");
+    if (n > (1 << 30) / 8 || kdim <= 0 || kpad < k || kpad % 16) throw Error(OMG_ERR_INVALID, "digit GEMM: bad sizes");
     ProfScope prof_(prof_name, s);
     const int64_t ld = digits_ld(kdim);
     // plan: digit pairs by level, level sums flushed before they could leave int32
@@ -453,10 +472,6 @@ void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, con
         OMG_CUDA(cudaMemset2DAsync(R, ldr * 8, 0, n * 8, k, s));
     else if (B != R)
         OMG_CUDA(cudaMemcpy2DAsync(R, ldr * 8, B, ldb * 8, n * 8, k, cudaMemcpyDeviceToDevice, s));
-    const CUtensorMap mA = tc::make_map_2d(Ad, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)nda * n, ld, ld, tcr::BK,
-                                           tcr::BM);
-    const CUtensorMap mX = tc::make_map_2d(Xd, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)ndx * kpad, ld, ld,
-                                           tcr::BK, tcr::BN);
     static bool attr = false;
     static int n_sm = 0;
     if (!attr) {
@@ -467,12 +482,22 @@ void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, con
         if (n_sm <= 0) n_sm = 1;
         attr = true;
     }
-    const int nrb = (int)((n + tcr::BM - 1) / tcr::BM), ncb = (int)((k + tcr::BN - 1) / tcr::BN);
+    // tile width: all columns in one tile (each A digit plane streamed once per digit pair) unless that leaves
+    // more than half the SMs idle; then narrower tiles (multiples of 16 columns, >= 64)
+    const int nrb = (int)((n + tcr::BM - 1) / tcr::BM);
+    int ncb = (int)((k + tcr::BN - 1) / tcr::BN);
+    auto width = [&](int nc) { return (int)(((k + nc - 1) / nc + 15) / 16 * 16); };
+    while (2 * (int64_t)nrb * ncb < n_sm && width(ncb + 1) >= 64) ++ncb;
+    const int nmma = width(ncb);
+    const CUtensorMap mA = tc::make_map_2d(Ad, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)nda * n, ld, ld, tcr::BK,
+                                           tcr::BM);
+    const CUtensorMap mX = tc::make_map_2d(Xd, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)ndx * kpad, ld, ld,
+                                           tcr::BK, nmma);
     const int64_t ntiles = (int64_t)nrb * ncb;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
     tcr::residual_slices_kernel<<<grid, tcr::THREADS, tcr::SMEM_BYTES, s>>>(mA, mX, plan, (int)n, (int)k, (int)kpad,
                                                                             beta, rexp, cexp, sgn, R, ldr, ntiles,
-                                                                            ncb, err);
+                                                                            ncb, nmma, err);
     check_tcr(prof_name);
 }
 
