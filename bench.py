@@ -944,6 +944,20 @@ def run_next(args):
                                         "evals_per_s": kept * dip.shape[0] / (ms / 1e3)}
     ms, nl, A = timed(lambda: api.EITSourceMat(geo, el_d))
     rows["EITSourceMat"] = {"ms": ms, "launches": nl, "shape": list(A.shape)}
+    # CorticalMat / CorticalMat2 on the config0 head (N = 4486, 64 electrodes, cortex = the brain's boundary): one
+    # KKT system each (N + rows outside the cortex [+ electrodes] unknowns), FP64 LU with partial pivoting
+    w0 = workloads.config0()
+    geo0 = api.Geometry.from_head(w0.head, ctx)
+    M0 = api.Head2EEGMat(geo0, torch.as_tensor(w0.electrodes[:, :3], device=dev), sparse=True)
+    ncx = w0.head.vertices[0].shape[0] + w0.head.triangles[0].shape[0]
+    for name, fn, extra in (("CorticalMat", lambda: api.CorticalMat(geo0, M0, "Brain", 1e-4, 1.58e-2), 0),
+                            ("CorticalMat2", lambda: api.CorticalMat2(geo0, M0, "Brain", 12.4), M0[1].shape[0])):
+        ms, nl, A = timed(fn)
+        nk = 2 * geo0.size - ncx + extra
+        rows[name] = {"ms": ms, "launches": nl, "shape": list(A.shape), "kkt_unknowns": nk,
+                      "lu_gflop": 2.0 * nk ** 3 / 3 / 1e9, "fp64_tflops": 2.0 * nk ** 3 / 3 / (ms / 1e3) / 1e12,
+                      "cpu": None, "note": "config0 head; alpha 1e-4 / beta 1.58e-2 and gamma 12.4 as in the "
+                                           "reference's tests (TestHead.cmake:94-96)"}
     ck = clocks.stop()
     if not args.no_cpu:
         from oracle import oracle
@@ -960,6 +974,15 @@ def run_next(args):
             rows[name]["cpu"] = {"value_ms": t * 1e3, "cores": nthr, "kind": "port",
                                  "sample": f"{n_sample} of the call's units, scaled linearly"}
             rows[name]["speedup_vs_cpu"] = t * 1e3 / rows[name]["ms"]
+        # the reference's CorticalMat (SVD projector, SVD pseudo-inverse) as the oracle restates it, whole call
+        g0 = oracle.digest(w0.head)
+        Md = oracle.h2em(g0, w0.electrodes)
+        s = time.perf_counter()
+        oracle.corticalmat(g0, Md, "Brain", 1e-4, 1.58e-2)
+        t = time.perf_counter() - s
+        rows["CorticalMat"]["cpu"] = {"value_ms": t * 1e3, "cores": os.cpu_count(), "kind": "port",
+                                      "sample": "the whole call (LAPACK SVDs through numpy on all host cores)"}
+        rows["CorticalMat"]["speedup_vs_cpu"] = t * 1e3 / rows["CorticalMat"]["ms"]
     line = {"metric": "time per call (ms) of the rows beside the forward path, config1 head", "unit": "ms",
             "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "dtype": "f64", "data": "synthetic (seeded)",

@@ -37,6 +37,7 @@ extern "C" {
 #define OMG_ERR_IO               -6  /* file could not be read or parsed */
 #define OMG_ERR_UNSUPPORTED      -7  /* valid request outside this build's scope */
 #define OMG_ERR_TIMEOUT          -8  /* a bounded device-side wait gave up */
+#define OMG_ERR_SINGULAR         -9  /* a dense LU met an exact zero pivot (LAPACK dgetrf info > 0) */
 
 #define OMG_PREC_FP64             0  /* all-FP64 drop-in */
 #define OMG_PREC_MIXED            1  /* FP32 far field + FP32 factorization + FP64-residual refinement */
@@ -250,6 +251,45 @@ int omg_gain_eeg_dev(omg_context ctx, int64_t N, const double* hminv, int64_t ld
 int omg_gain_meg_dev(omg_context ctx, int64_t N, const double* hminv, int64_t ld, int32_t packed,
                      const double* dsm, int64_t n_dipoles, const double* h2mm, int64_t n_squids, const double* ds2mm,
                      int32_t precision, double* gain);
+
+/* ---- cortical mapping -------------------------------------------------------
+ * CorticalMat (OpenMEEG/src/assembleHeadMat.cpp:168-236; om_assemble -CM with
+ * zero or two numbers): out = P pinv(P^T A P) P^T M^T, N x n_electrodes
+ * column-major (N: the reference's unknowns), mapping electrode potentials to
+ * the unknowns.  M is Head2EEGMat (n_electrodes x N) as device triplets, as for
+ * omg_gain_eeg_dev; P projects on the null space of the head-matrix rows
+ * outside the cortex (the head matrix assembled without the cortex mesh's own
+ * block, assembleHeadMat.cpp:137-166); A = M^T M + alpha RR_vertices +
+ * beta RR_triangles with RR the gradient norms of every mesh
+ * (Mesh::gradient_norm2, mesh.cpp:160-205); alpha < 0 selects
+ * alpha = ||M^T M||_F / (1000 ||RR_vertices||_F) and beta = 50000 alpha.  The
+ * cortex is the one mesh of the one interface bounding `domain` (an index into
+ * the geometry's domains), else OMG_ERR_INVALID.  Computed as the KKT system
+ * [A mat^T; mat 0] [X; L] = [M^T; 0] by an FP64 LU with partial pivoting: the
+ * same X whenever P^T A P has the rank of P.  projector_in (optional, N x N,
+ * device): a projector from the reference's cache file, used instead of the
+ * head matrix (X = P (P A P + I - P)^-1 P M^T); projector_out (optional, N x N):
+ * receives P = I - mat^T (mat mat^T)^-1 mat, the matrix the reference caches. */
+int omg_corticalmat_dev(omg_context ctx, omg_geometry geo, const omg_integrator* integ, int32_t domain,
+                        int64_t n_electrodes, int64_t nnz, const int64_t* h2em_rows, const int64_t* h2em_cols,
+                        const double* h2em_vals, double alpha, double beta, const double* projector_in,
+                        double* projector_out, double* out);
+/* CorticalMat2 (assembleHeadMat.cpp:238-323; om_assemble -CM with one number):
+ * out = (G^-1 H^T (H G^-1 H^T)^-1) restricted to the electrode columns,
+ * N x n_electrodes, with H = [the head-matrix rows outside the cortex; M] and G
+ * the gradient norms whose triangle-triangle entries the reference scales by
+ * gamma once per ordered pair (gamma^2 off the diagonal).  Solved as
+ * [G H^T; H 0] [X; L] = [0; E].  rows_in (optional, device, n_rows x N
+ * column-major): the head-matrix rows from the reference's cache file instead
+ * of assembling them; rows_out (optional, n_rows x N): receives them.  An
+ * exactly singular system returns OMG_ERR_SINGULAR. */
+int omg_corticalmat2_dev(omg_context ctx, omg_geometry geo, const omg_integrator* integ, int32_t domain,
+                         int64_t n_electrodes, int64_t nnz, const int64_t* h2em_rows, const int64_t* h2em_cols,
+                         const double* h2em_vals, double gamma, const double* rows_in, double* rows_out,
+                         double* out);
+/* n_rows: the head-matrix rows outside the cortex of `domain` (N minus the
+ * cortex's vertices and triangles). */
+int omg_cortical_rows(omg_geometry geo, int32_t domain, int64_t* n_rows);
 
 /* ---- surface sources -------------------------------------------------------
  * SurfSourceMat (OpenMEEG/src/assembleSourceMat.cpp:22-64, assembleSourceMat.h:20):

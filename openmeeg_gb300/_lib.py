@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libomg_gb300.so")
 OMG_OK = 0
 ERRORS = {
     -1: "OMG_ERR_INVALID", -2: "OMG_ERR_CUDA", -3: "OMG_ERR_NOT_DEFINITE", -4: "OMG_ERR_NOT_CONVERGED",
-    -5: "OMG_ERR_NOMEM", -6: "OMG_ERR_IO", -7: "OMG_ERR_UNSUPPORTED", -8: "OMG_ERR_TIMEOUT",
+    -5: "OMG_ERR_NOMEM", -6: "OMG_ERR_IO", -7: "OMG_ERR_UNSUPPORTED", -8: "OMG_ERR_TIMEOUT", -9: "OMG_ERR_SINGULAR",
 }
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -110,6 +110,11 @@ _PROTOS = [
     ("omg_gain_eeg_dev", c_i32, [c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_i32,
                                  c_vp]),
     ("omg_gain_meg_dev", c_i32, [c_vp, c_i64, c_vp, c_i64, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp, c_i32, c_vp]),
+    ("omg_corticalmat_dev", c_i32, [c_vp, c_vp, ctypes.POINTER(Integrator), c_i32, c_i64, c_i64, c_vp, c_vp, c_vp,
+                                    ctypes.c_double, ctypes.c_double, c_vp, c_vp, c_vp]),
+    ("omg_corticalmat2_dev", c_i32, [c_vp, c_vp, ctypes.POINTER(Integrator), c_i32, c_i64, c_i64, c_vp, c_vp, c_vp,
+                                     ctypes.c_double, c_vp, c_vp, c_vp]),
+    ("omg_cortical_rows", c_i32, [c_vp, c_i32, P_i64]),
     ("omg_dipsource2megmat_dev", c_i32, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp]),
     ("omg_geometry_get_layout", c_i32, [c_vp, c_i32, ctypes.POINTER(MeshLayout)]),
     ("omg_geometry_get_pairs", c_i32, [c_vp, c_i32, ctypes.POINTER(MeshPair), P_i32]),

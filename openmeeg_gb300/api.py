@@ -126,6 +126,9 @@ class Geometry:
             check(self.lib.omg_geometry_load(self.ctx.handle, geom_file.encode(), cond_file.encode(), ctypes.byref(h)))
             self.handle = h
         self.domain_names = None
+        if _handle is None:   # the domains in the .geom file's order, as the library numbers them
+            from . import io
+            self.domain_names = [d[0] for d in io.read_geom_full(geom_file)[2]]
 
     @classmethod
     def from_meshes(cls, vertices: Sequence[np.ndarray], triangles: Sequence[np.ndarray], domains,
@@ -576,6 +579,80 @@ def GainMEG(HMinv, DSM, H2MM, DS2MM, precision=FP64, ctx: Optional[Context] = No
     out = torch.empty((nd, nm), dtype=torch.float64, device=_dev(ctx))
     check(ctx.lib.omg_gain_meg_dev(ctx.handle, N, _ptr(H), ld, packed, _ptr(D), nd, _ptr(Vc), nm, _ptr(S),
                                    _prec(precision), _ptr(out)))
+    return out.T
+
+
+def _cortical_domain(geom: Geometry, domain_name: str) -> int:
+    if geom.domain_names is None or domain_name not in geom.domain_names:
+        raise OMGError(-1, f"CorticalMat: unknown domain {domain_name!r}")   # Geometry::domain throws
+    return geom.domain_names.index(domain_name)
+
+
+def CorticalMat(geom: Geometry, M, domain_name: str = "CORTEX", alpha: float = -1.0, beta: float = -1.0,
+                filename: str = "", integrator: Optional[Integrator] = None) -> torch.Tensor:
+    """CorticalMat(geo, M, domain_name, alpha, beta, filename, integrator)
+    (assembleHeadMat.cpp:168-236, om_assemble -CM): N x n_electrodes.  M is
+    Head2EEGMat (dense, torch sparse or the sparse triple).  alpha < 0 picks
+    alpha and beta automatically.  `filename` caches the null-space projector
+    as the reference does: read from the file when it exists (.bin), else
+    computed and written there."""
+    from . import io
+    import os
+    ctx = geom.ctx
+    N = geom.size
+    dev = _dev(ctx)
+    ne, r, c, v = _sparse_rows(M, ctx, N)
+    dom = _cortical_domain(geom, domain_name)
+    it = _default(integrator, 3, 0, 0.005)
+    pin = pout = None
+    if filename and os.path.exists(filename):
+        P = torch.as_tensor(io.read_bin(filename)[1]).to(dev, torch.float64)
+        if tuple(P.shape) != (N, N):
+            raise OMGError(-6, f"CorticalMat: {filename} is not an {N} x {N} projector")
+        pin = P.T.contiguous()
+    elif filename:
+        pout = torch.empty((N, N), dtype=torch.float64, device=dev)
+    out = torch.empty((ne, N), dtype=torch.float64, device=dev)   # column-major N x ne
+    check(ctx.lib.omg_corticalmat_dev(ctx.handle, geom.handle, ctypes.byref(it), dom, ne, r.numel(), _ptr(r),
+                                      _ptr(c), _ptr(v), float(alpha), float(beta), _ptr(pin), _ptr(pout), _ptr(out)))
+    if pout is not None:
+        io.write_bin(filename, pout.T.cpu().numpy())
+    return out.T
+
+
+def CorticalMat2(geom: Geometry, M, domain_name: str = "CORTEX", gamma: float = 1.0, filename: str = "",
+                 integrator: Optional[Integrator] = None) -> torch.Tensor:
+    """CorticalMat2(geo, M, domain_name, gamma, filename, integrator)
+    (assembleHeadMat.cpp:238-323, om_assemble -CM with one number):
+    N x n_electrodes.  `filename` caches H (the head-matrix rows outside the
+    cortex followed by M) as the reference does: its head-matrix rows are read
+    from the file when it exists, else H is written there."""
+    from . import io
+    import os
+    ctx = geom.ctx
+    N = geom.size
+    dev = _dev(ctx)
+    ne, r, c, v = _sparse_rows(M, ctx, N)
+    dom = _cortical_domain(geom, domain_name)
+    it = _default(integrator, 3, 0, 0.005)
+    nl = ctypes.c_int64()
+    check(ctx.lib.omg_cortical_rows(geom.handle, dom, ctypes.byref(nl)))
+    nl = nl.value
+    rin = rout = None
+    if filename and os.path.exists(filename):
+        H = torch.as_tensor(io.read_bin(filename)[1])
+        if tuple(H.shape) != (nl + ne, N):
+            raise OMGError(-6, f"CorticalMat2: {filename} is not an {nl + ne} x {N} matrix")
+        rin = H[:nl].to(dev, torch.float64).T.contiguous()       # column-major nl x N
+    elif filename:
+        rout = torch.empty((N, max(nl, 1)), dtype=torch.float64, device=dev)
+    out = torch.empty((ne, N), dtype=torch.float64, device=dev)
+    check(ctx.lib.omg_corticalmat2_dev(ctx.handle, geom.handle, ctypes.byref(it), dom, ne, r.numel(), _ptr(r),
+                                       _ptr(c), _ptr(v), float(gamma), _ptr(rin), _ptr(rout), _ptr(out)))
+    if rout is not None:   # the reference saves H = [rows; M] (assembleHeadMat.cpp:273-279)
+        Md = torch.zeros((ne, N), dtype=torch.float64, device=dev)
+        Md.index_put_((r, c), v, accumulate=True)
+        io.write_bin(filename, torch.cat([rout.T[:nl], Md]).cpu().numpy())
     return out.T
 
 

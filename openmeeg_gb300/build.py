@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libomg_gb300.so")
 SOURCES = ["bem_kernels.cu", "dense_kernels.cu", "api.cpp", "batch.cpp", "geometry.cpp", "gain_direct.cu", "noalloc.cu",
            "tc_gemm.cu", "tc_residual.cu",
-           "tc_solve.cu"]
+           "tc_solve.cu", "lu.cu", "cortical.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -355,7 +355,8 @@ void ensure_order(omg_geometry g, int order) {
 // ---------------------------------------------------------------------------
 // HeadMat assembly into the internal lower triangle (assembleHeadMat.cpp:73-115)
 // ---------------------------------------------------------------------------
-void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld) {
+void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld,
+                               int skip_self_mesh) {
     omg_context ctx = g->ctx;
     cudaStream_t s = ctx->stream;
     const HostGeometry& h = g->h;
@@ -368,6 +369,7 @@ void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, doub
     for (const auto& p : h.pairs) {
         const int m1 = p.m1, m2 = p.m2;
         const bool same = (m1 == m2);
+        if (same && m1 == skip_self_mesh) continue;
         const int64_t t1b = h.tbeg[m1], t1e = h.tbeg[m1 + 1], t2b = h.tbeg[m2], t2e = h.tbeg[m2 + 1];
         const int64_t v1b = h.vbeg[m1], v1e = h.vbeg[m1 + 1], v2b = h.vbeg[m2], v2e = h.vbeg[m2 + 1];
         double Scoeff = 0.0;

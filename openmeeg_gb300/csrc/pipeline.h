@@ -80,7 +80,9 @@ omg_integrator default_dsm_integrator();
 void check_integrator(const omg_integrator& it, bool allow_adaptive);
 void ensure_order(omg_geometry g, int order);
 void ensure_gg_tables(omg_geometry g);
-void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld);
+// skip_self_mesh >= 0: that mesh's own block is left out (HeadMatrix with AllButBlock, assembleHeadMat.cpp:65-69)
+void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld,
+                               int skip_self_mesh = -1);
 void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld,
                             NearPlan* plan = nullptr);
 void solver_factor(omg_solver sv, DevBuf&& hm, bool check = true);

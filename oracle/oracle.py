@@ -698,3 +698,178 @@ def set_threads(n: int):
 
 def num_threads() -> int:
     return int(lib().oo_num_threads())
+
+
+# ---------------------------------------------------------------------------
+# Cortical mapping (OpenMEEG/src/assembleHeadMat.cpp:137-323)
+# ---------------------------------------------------------------------------
+
+def cortex_mesh(g: OracleGeometry, domain_name: str) -> int:
+    """The single mesh of the single interface bounding `domain_name`
+    (assembleHeadMat.cpp:179-183: om_error otherwise)."""
+    for (name, bounds, _) in g.domains:
+        if name == domain_name:
+            if len(bounds) != 1:
+                raise ValueError("CorticalMat: the source domain must be bounded by one interface")
+            return bounds[0][0]
+    raise ValueError(f"no domain {domain_name!r}")
+
+
+def headmatrix_rows(g: OracleGeometry, cortex: int, order=3, extension=0):
+    """HeadMatrix(geo, Cortex, integrator, extension) (assembleHeadMat.cpp:137-166):
+    the head matrix with the cortex mesh's own block left out, deflated, and
+    only the rows of the other meshes (their vertices, then their triangles
+    unless a current barrier), in mesh order, plus `extension` zero rows."""
+    keep = [p for p in range(g.pairs.shape[0]) if not (g.pairs[p, 0] == cortex and g.pairs[p, 1] == cortex)]
+    saved = (g.pairs, g.coefs)
+    g.pairs = np.ascontiguousarray(saved[0][keep])
+    g.coefs = np.ascontiguousarray(saved[1][keep])
+    try:
+        HM = headmat(g, order=order)
+    finally:
+        g.pairs, g.coefs = saved
+    rows = []
+    for m in range(g.nmesh):
+        if m == cortex:
+            continue
+        rows += [int(g.vidx[v]) for v in range(g.mesh_vbeg[m], g.mesh_vbeg[m + 1])]
+        if not g.barrier[m]:
+            rows += [int(g.tidx[t]) for t in range(g.mesh_tbeg[m], g.mesh_tbeg[m + 1])]
+    out = np.zeros((len(rows) + extension, g.N))
+    out[:len(rows)] = HM[rows]
+    return out, rows
+
+
+def gradient_norm2(g: OracleGeometry) -> np.ndarray:
+    """Sum over the meshes of Mesh::gradient_norm2 (mesh.cpp:160-205), dense
+    N x N symmetric: P1 terms on the vertices (with OpenMEEG's P1gradient,
+    mesh.h:240-248, triangle edges triangle.h:86-94,154), P0 terms between
+    adjacent triangles of meshes that are not outermost."""
+    V, T = g.V, g.T
+    A = np.zeros((g.N, g.N))
+
+    def p1grad(p0, p1, p2):
+        c = np.cross(p1, p2)
+        return c / float(np.dot(p0, c))
+
+    def area_normal(t):
+        a, b, c = V[T[t]]
+        nn = np.cross(b - a, c - a)
+        nrm = float(np.linalg.norm(nn))
+        return 0.5 * nrm, nn / nrm
+
+    opp = ((1, 2), (2, 0), (0, 1))
+    for m in range(g.nmesh):
+        t0, t1 = int(g.mesh_tbeg[m]), int(g.mesh_tbeg[m + 1])
+        inc = {}
+        for t in range(t0, t1):
+            for k in range(3):
+                inc.setdefault(int(T[t, k]), []).append((t, k))
+        for v in range(int(g.mesh_vbeg[m]), int(g.mesh_vbeg[m + 1])):
+            i = int(g.vidx[v])
+            for (t, k) in inc.get(v, []):
+                a, _ = area_normal(t)
+                gr = p1grad(V[v], V[T[t, opp[k][0]]], V[T[t, opp[k][1]]])
+                A[i, i] += float(np.dot(gr, gr)) * a * a
+        for t in range(t0, t1):
+            a, _ = area_normal(t)
+            for e in range(3):
+                v1, v2, v3 = T[t, (e + 1) % 3], T[t, (e + 2) % 3], T[t, e]
+                i1, i2 = int(g.vidx[v1]), int(g.vidx[v2])
+                if i1 < i2:
+                    val = float(np.dot(p1grad(V[v1], V[v2], V[v3]), p1grad(V[v2], V[v3], V[v1]))) * a * a
+                    A[i1, i2] += val
+                    A[i2, i1] = A[i1, i2]
+        if not g.outermost[m]:
+            for t in range(t0, t1):
+                it = int(g.tidx[t])
+                A[it, it] = 0.0
+                a1, n1 = area_normal(t)
+                c1 = V[T[t]].mean(axis=0)
+                adj = []   # Mesh::adjacent_triangles (mesh.h:164-172): triangles sharing two vertices, t itself too
+                cnt = {}
+                for x in T[t]:
+                    for (t2, _) in inc[int(x)]:
+                        cnt[t2] = cnt.get(t2, 0) + 1
+                        if cnt[t2] == 2:
+                            adj.append(t2)
+                for t2 in adj:
+                    it2 = int(g.tidx[t2])
+                    if it < it2:
+                        a2, n2 = area_normal(t2)
+                        c2 = V[T[t2]].sum(axis=0) / 3
+                        d = c1 - c2
+                        A[it, it2] += float(np.dot(n1, n2)) ** 2 / float(np.dot(d, d)) * a1 * a2
+                        A[it2, it] = A[it, it2]
+    return A
+
+
+def _pinverse(Z: np.ndarray) -> np.ndarray:
+    """Matrix::pinverse(0) (OpenMEEGMaths/src/matrix.cpp:45-80): SVD, singular
+    values above max(m, n) * s_max * eps kept."""
+    if Z.shape[1] > Z.shape[0]:
+        return _pinverse(Z.T).T
+    U, s, Vt = np.linalg.svd(Z, full_matrices=False)
+    tol = max(Z.shape) * s[0] * np.finfo(float).eps
+    r = int((s > tol).sum())
+    if r == 0:
+        return np.zeros((Z.shape[1], Z.shape[0]))
+    return (Vt[:r].T / s[:r]) @ U[:, :r].T
+
+
+def nullspace_projector(mat: np.ndarray) -> np.ndarray:
+    """matop.h:15-32: V^T S V with S = 1 on the last Nc - Nl diagonal entries."""
+    Nl = mat.shape[0]
+    _, _, Vt = np.linalg.svd(mat, full_matrices=True)
+    return Vt[Nl:].T @ Vt[Nl:]
+
+
+def corticalmat(g: OracleGeometry, M: np.ndarray, domain_name: str, alpha=-1.0, beta=-1.0, order=3,
+                projector=None):
+    """CorticalMat (assembleHeadMat.cpp:168-236) for the dense Head2EEGMat M
+    (n_electrodes x N): X = P pinv(P^T (M^T M + alphas RR) P) P^T M^T.
+    Returns (X, P)."""
+    cortex = cortex_mesh(g, domain_name)
+    if projector is None:
+        mat, _ = headmatrix_rows(g, cortex, order=order)
+        projector = nullspace_projector(mat)
+    P = projector
+    RR = gradient_norm2(g)
+    MM = M.T @ M
+    nv = int(g.V.shape[0])
+    if alpha < 0:
+        alpha = np.linalg.norm(MM) / (1.0e3 * np.linalg.norm(RR[:nv, :nv]))
+        beta = alpha * 50000.0
+    d = np.zeros(g.N)
+    d[:nv] = alpha
+    for m in range(g.nmesh):
+        if not g.barrier[m]:
+            d[g.tidx[g.mesh_tbeg[m]:g.mesh_tbeg[m + 1]]] = beta
+    Z = P.T @ (MM + d[:, None] * RR) @ P
+    return P @ _pinverse(Z) @ (P.T @ M.T), P
+
+
+def corticalmat2(g: OracleGeometry, M: np.ndarray, domain_name: str, gamma: float, order=3, H=None):
+    """CorticalMat2 (assembleHeadMat.cpp:238-323): (G^-1 H^T (H G^-1 H^T)^-1)
+    restricted to the electrode columns, H = [head-matrix rows outside the
+    cortex; M], G the gradient norms with every triangle-triangle entry scaled
+    by gamma once per ordered pair (gamma^2 off the diagonal, as the
+    reference's loop over a symmetric matrix does).  Returns (X, H)."""
+    cortex = cortex_mesh(g, domain_name)
+    ne = M.shape[0]
+    if H is None:
+        H, _ = headmatrix_rows(g, cortex, order=order, extension=ne)
+    H = H.copy()
+    Nl = H.shape[0] - ne
+    H[Nl:] = M
+    G = gradient_norm2(g)
+    for m in range(g.nmesh):
+        if not g.barrier[m]:
+            idx = g.tidx[g.mesh_tbeg[m]:g.mesh_tbeg[m + 1]]
+            blk = np.ix_(idx, idx)
+            scale = np.full((len(idx), len(idx)), gamma * gamma)
+            np.fill_diagonal(scale, gamma)
+            G[blk] *= scale
+    Gi = np.linalg.inv(G)
+    full = Gi @ H.T @ np.linalg.inv(H @ Gi @ H.T)
+    return full[:, Nl:Nl + ne], H

@@ -230,6 +230,84 @@ def save_direct_gains():
     print("direct_gains", {k: v.shape for k, v in d.items()})
 
 
+HEAD1_INPUTS = ("Head1.geom", "Head1.cond", "cortex.1.tri", "skull.1.tri", "scalp.1.tri", "Head1.dip",
+                "Head1.patches", "Head1.squids", "Head1.tri")
+HEAD1_MATS = ("Head1.hm", "Head1.hm_inv", "Head1.dsm", "Head1.h2em", "Head1.h2mm", "Head1.ds2mm", "Head1.dgem",
+              "Head1.dgmm", "Head1.ssm", "Head1.sgem")
+
+
+def save_head1():
+    """The reference's own golden files for its Head1 test head
+    (tests/initialTest/Head1.*: MATLAB v7.3 / HDF5, written by its MatlabIO) and
+    the inputs they were made from (data/Head1), copied into tests/golden/head1/
+    so the tests can read them (openmeeg_gb300.matio) without the reference."""
+    import shutil
+    R = ref_runner.REFERENCE_DIR
+    dst = os.path.join(OUT, "head1")
+    os.makedirs(dst, exist_ok=True)
+    for f in HEAD1_INPUTS:
+        shutil.copyfile(os.path.join(R, "data", "Head1", f), os.path.join(dst, f))
+    for f in HEAD1_MATS:
+        shutil.copyfile(os.path.join(R, "tests", "initialTest", f), os.path.join(dst, f))
+    print("head1", sorted(os.listdir(dst)))
+
+
+def cortical_probe(head) -> np.ndarray:
+    """The seeded random vector the config0 cortical fixtures are projected on."""
+    n = sum(v.shape[0] for v in head.vertices) + sum(t.shape[0] for t in head.triangles[:-1])
+    return np.random.default_rng(2024).standard_normal(n)
+
+
+def save_cortical():
+    """om_assemble -CM (CorticalMat with automatic and given alpha / beta,
+    CorticalMat2 with gamma) on the reference's Head1 with its EEG patches and
+    its test's "Brain" domain and parameters (TestHead.cmake:94-96), and on the
+    seeded small_ico1_3l head.  Head1's mesh / .geom / .cond texts and patches
+    are stored so a test can rebuild the files without the reference.  Head1's
+    CorticalMat2 is not kept: two of its 32 patches give linearly dependent rows
+    of Head2EEGMat (rank 31), so H G^-1 H^T is singular and the reference's
+    inverse of it returns rounding noise."""
+    import subprocess
+    import tempfile
+    R = ref_runner.REFERENCE_DIR
+    if not ref_runner.available():
+        ref_runner.build()
+    d = {}
+    variants = (("auto", []), ("ab", ["1e-4", "1.58e-2"]), ("gamma", ["12.4"]))
+
+    def run(wd, geom, cond, eeg, tag, args):
+        subprocess.check_call([os.path.join(ref_runner.REF_BIN, "om_assemble"), "-CM", geom, cond, eeg, "Brain",
+                               "cm.bin", *args], cwd=wd, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        return io.read_bin(os.path.join(wd, "cm.bin"))[1]
+
+    base = os.path.join(R, "data", "Head1")
+    files = ["Head1.geom", "Head1.cond", "cortex.1.tri", "skull.1.tri", "scalp.1.tri", "Head1.patches"]
+    d["head1_files"] = np.array(files)
+    d["head1_texts"] = np.array([open(os.path.join(base, f)).read() for f in files])
+    for tag, args in variants[:2]:
+        d[f"head1_{tag}"] = run(base, "Head1.geom", "Head1.cond", "Head1.patches", tag, args)
+    w = workloads.small(1, layers=3)
+    wd = tempfile.mkdtemp()
+    ref_runner.write_head(wd, w.head, w.dipoles, w.electrodes, w.squids)
+    for tag, args in variants:
+        d[f"ico1_3l_{tag}"] = run(wd, "head.geom", "head.cond", "eeg.txt", tag, args)
+    import shutil
+    shutil.rmtree(wd, ignore_errors=True)
+    # config0 (N = 4486, 64 electrodes): too large to store whole; kept as the column 2-norms and the
+    # projection X^T u on a seeded random vector u (cortical_probe)
+    w = workloads.config0()
+    wd = tempfile.mkdtemp()
+    ref_runner.write_head(wd, w.head, w.dipoles, w.electrodes, w.squids)
+    u = cortical_probe(w.head)
+    for tag, args in variants:
+        X = run(wd, "head.geom", "head.cond", "eeg.txt", tag, args)
+        d[f"config0_{tag}_norms"] = np.linalg.norm(X, axis=0)
+        d[f"config0_{tag}_proj"] = X.T @ u
+    shutil.rmtree(wd, ignore_errors=True)
+    np.savez_compressed(os.path.join(OUT, "cortical.npz"), **d)
+    print("cortical", {k: v.shape for k, v in d.items()})
+
+
 REFERENCE_HEADS = ("HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3", "HeadNNa1", "HeadNNc1")
 
 
@@ -270,6 +348,12 @@ def main():
     if "--direct-only" in sys.argv:
         save_direct_gains()
         return
+    if "--cortical-only" in sys.argv:
+        save_cortical()
+        return
+    if "--head1-only" in sys.argv:
+        save_head1()
+        return
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
         return
@@ -286,6 +370,8 @@ def main():
     if "--ssm-only" in sys.argv:
         return
     save_direct_gains()
+    save_cortical()
+    save_head1()
     if not ref_runner.available():
         ref_runner.build()
     big = "--big" in sys.argv

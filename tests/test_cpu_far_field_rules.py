@@ -124,3 +124,72 @@ def test_near_far_split_rule_accuracy():
     assert counts["far"] >= 80 and counts["near"] >= 40
     assert worst["far"][0] < 2e-7 and worst["far"][1] < 3e-6, worst["far"]
     assert worst["near"][1] > 1e-4, worst["near"]
+
+
+def _mesh_geom(V, T):
+    P = V[T]
+    nrm = np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    h = np.max(np.linalg.norm(P - np.roll(P, 1, axis=1), axis=2), axis=1)
+    return P, nrm, h, P.mean(axis=1)
+
+
+def _split_band_worst(A, B, R16, rng, per_band=60, same=False):
+    """Worst deviation of the 16 x 16 rule from the twice subdivided rule on
+    pairs (t1 of mesh A, t2 of mesh B) at 1.5 to 2.5 of their larger max edge."""
+    from scipy.spatial import cKDTree
+    PA, nA, hA, cA = A
+    PB, nB, hB, cB = B
+    tree = cKDTree(cB)
+    hmax = max(hA.max(), hB.max())
+
+    def integ(a, b, lev):
+        xa, wa = _subdivided_points(PA[a], R16, lev)
+        xb, wb = _subdivided_points(PB[b], R16, lev)
+        r = xb[None] - xa[:, None]
+        d = np.linalg.norm(r, axis=2)
+        w = wa[:, None] * wb[None]
+        t2 = w * (r @ nB[b]) / d ** 3
+        t1 = w * (r @ nA[a]) / d ** 3
+        return (w / d).sum(), t2.sum(), np.abs(t2).sum(), t1.sum(), np.abs(t1).sum()
+
+    ws = wd = 0.0
+    n = 0
+    for a in rng.permutation(len(PA)):
+        for b in tree.query_ball_point(cA[a], 2.5 * hmax):
+            if same and a == b:
+                continue
+            q = np.linalg.norm(cA[a] - cB[b]) / max(hA[a], hB[b])
+            if not 1.5 <= q < 2.5:
+                continue
+            s1, d1, _, e1, _ = integ(a, b, 0)
+            s2, d2, ad2, e2, ae2 = integ(a, b, 2)
+            ws = max(ws, abs(s1 - s2) / abs(s2))
+            wd = max(wd, abs(d1 - d2) / ad2, abs(e1 - e2) / ae2)
+            n += 1
+            if n >= per_band:
+                return ws, wd, n
+    return ws, wd, n
+
+
+def test_near_far_split_rule_across_surfaces_and_perturbed_meshes():
+    """The 1.5-edge split on pairs between adjacent layers of the config1 head
+    (nearly parallel, one layer's triangles facing the next) and on pairs within
+    and between the layers of the perturbed ico2 head (irregular triangles):
+    the 16 x 16 rule stays within the bounds the within-mesh check holds it to
+    (single layer 2e-7, double layer both ways 3e-6 of the absolute sum)."""
+    from openmeeg_gb300 import workloads
+    _, R16 = _rules()
+    rng = np.random.default_rng(11)
+    heads = (("config1", workloads.config1().head), ("ico2_pert", workloads.small(2, layers=3, perturb=True).head))
+    checked = 0
+    for tag, head in heads:
+        meshes = [_mesh_geom(V, T) for V, T in zip(head.vertices, head.triangles)]
+        pairs = [(m, m + 1) for m in range(len(meshes) - 1)]
+        if tag == "ico2_pert":
+            pairs += [(m, m) for m in range(len(meshes))]
+        for m1, m2 in pairs:
+            ws, wd, n = _split_band_worst(meshes[m1], meshes[m2], R16, rng, same=(m1 == m2))
+            checked += n
+            assert ws < 2e-7 and wd < 3e-6, (tag, m1, m2, n, ws, wd)
+    assert checked >= 100
