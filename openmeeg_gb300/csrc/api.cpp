@@ -956,6 +956,48 @@ void solver_factor(omg_solver sv, DevBuf&& hm, bool check) {
     if (check) check_err(sv->ctx, "factorization");
 }
 
+namespace omg {
+void lu_factor(int64_t n, double* A, int64_t lda, int* ipiv, std::vector<int64_t>& perm, int* err, cudaStream_t s);
+void lu_solve(int64_t n, int64_t nrhs, const double* LU, int64_t lda, const int64_t* perm_dev, double* B, int64_t ldb,
+              cudaStream_t s);
+}  // namespace omg
+
+void solver_factor_or_pivot(omg_solver sv, DevBuf&& hm, const std::function<DevBuf()>& again) {
+    try {
+        solver_factor(sv, std::move(hm));
+        return;
+    } catch (const Error& e) {
+        if (e.code != OMG_ERR_NOT_DEFINITE) throw;
+    }
+    // a pivot of the wrong sign: the whole matrix, rebuilt, by LU with partial pivoting in FP64
+    cudaStream_t s = sv->ctx->stream;
+    sv->A64.release();
+    sv->A32.release();
+    sv->A32r.release();
+    sv->W.release();
+    sv->Linv32.release();
+    sv->Adig.release();
+    sv->rexp.release();
+    sv->w_off.clear();
+    reset_err(sv->ctx);
+    DevBuf A = again();
+    const int64_t N = sv->N;
+    deflate_enclosed_barriers(sv, A.as<double>(), N);
+    symmetrize(A.as<double>(), N, N, s);
+    DevBuf ipiv((size_t)N * sizeof(int), s);
+    std::vector<int64_t> perm;
+    lu_factor(N, A.as<double>(), N, ipiv.as<int>(), perm, sv->ctx->d_err, s);
+    sv->perm = DevBuf((size_t)N * sizeof(int64_t), s, sv->persistent);
+    OMG_CUDA(cudaMemcpyAsync(sv->perm.p, perm.data(), (size_t)N * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    sv->A64 = std::move(A);
+    sv->lu = true;
+    int e = 0;
+    OMG_CUDA(cudaMemcpyAsync(&e, sv->ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OMG_CUDA(cudaStreamSynchronize(s));
+    if (e == OMG_ERR_SINGULAR) throw Error(OMG_ERR_SINGULAR, "factorization: the head matrix is singular");
+    check_err(sv->ctx, "pivoted factorization");
+}
+
 // Scratch of one refinement residual: X digits + column exponents, or X as a float pair.
 static size_t mixed_residual_scratch(omg_solver sv, int64_t nrhs) {
     const int64_t N = sv->N;
@@ -1083,7 +1125,12 @@ void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int 
 
 void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     if (nrhs <= 0) return;
-    if (sv->precision == OMG_PREC_FP64)
+    if (sv->lu) {
+        lu_solve(sv->N, nrhs, sv->A64.as<double>(), sv->N, sv->perm.as<int64_t>(), B, ldb, sv->ctx->stream);
+        sv->last_steps = 0;
+        sv->last_residual = 0.0;
+        sv->last_correction = 0.0;
+    } else if (sv->precision == OMG_PREC_FP64)
         solve_ldlt<double>(sv, sv->A64.as<double>(), sv->N, B, ldb, nrhs);
     else
         solve_mixed(sv, B, ldb, nrhs);
@@ -2021,7 +2068,7 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
         const omg_integrator it = integ ? *integ : default_hm_integrator();
         DevBuf hm = assemble_system(geo, it, precision, true);
         check_err(ctx, "HeadMat");
-        solver_factor(sv.get(), std::move(hm));
+        solver_factor_or_pivot(sv.get(), std::move(hm), [&] { return assemble_system(geo, it, precision, true); });
         ctx->refs++;
         geo->refs++;
         *out = sv.release();
@@ -2042,9 +2089,12 @@ int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double*
         sv->N = geo->dg.N;
         sv->nP = geo->d.nP;
         sv->persistent = true;
-        DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream, true);
-        launch_from_reference_dense(geo->dg, hm, ld, A.as<double>(), sv->N, ctx->stream);
-        solver_factor(sv.get(), std::move(A));
+        auto copy_in = [&] {
+            DevBuf A((size_t)sv->N * sv->N * 8, ctx->stream, true);
+            launch_from_reference_dense(geo->dg, hm, ld, A.as<double>(), sv->N, ctx->stream);
+            return A;
+        };
+        solver_factor_or_pivot(sv.get(), copy_in(), copy_in);
         ctx->refs++;
         geo->refs++;
         *out = sv.release();
@@ -2145,7 +2195,7 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaEventRecord(ev[1], s));
     OMG_CUDA(cudaStreamWaitEvent(s, ev[6], 0));
     OMG_CUDA(cudaEventRecord(ev[2], s));
-    solver_factor(sv.get(), std::move(hm));
+    solver_factor_or_pivot(sv.get(), std::move(hm), [&] { return assemble_system(geo, hm_it, precision, false); });
     OMG_CUDA(cudaEventRecord(ev[3], s));
     {   // after the factorization's last work on the second stream (stream order); every stage of the
         // pipeline is throughput-bound, so the sources run where they take the least (under the assembly

@@ -7,6 +7,8 @@
 #include <utility>
 #include <vector>
 
+#include <functional>
+
 #include "handles.h"
 
 struct omg_solver_s {
@@ -39,6 +41,11 @@ struct omg_solver_s {
     int last_steps = 0;
     double last_residual = 0.0;
     double last_correction = 0.0;
+    // pivoted fallback: the quasi-definite LDL^T met a pivot of the wrong sign, so A64 holds the FP64 LU
+    // factors with partial pivoting of the whole matrix (any nonsingular matrix, as the reference's
+    // Bunch-Kaufman DSPTRF) and perm its row order
+    bool lu = false;
+    DevBuf perm;
 };
 
 // Near-pair lists of a geometry's mixed-precision assembly, one per mesh pair.
@@ -86,6 +93,9 @@ void assemble_headmat_internal(omg_geometry g, const omg_integrator& integ, doub
 void assemble_headmat_mixed(omg_geometry g, const omg_integrator& integ, double* hm, int64_t ld,
                             NearPlan* plan = nullptr);
 void solver_factor(omg_solver sv, DevBuf&& hm, bool check = true);
+// solver_factor; on OMG_ERR_NOT_DEFINITE the matrix `again()` returns (the same head matrix, rebuilt) is
+// factored by the pivoted FP64 LU instead
+void solver_factor_or_pivot(omg_solver sv, DevBuf&& hm, const std::function<DevBuf()>& again);
 void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs);
 void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int residual_steps, double* d_est);
 void dsm_internal(omg_geometry g, const double* dip, int64_t nd, const omg_integrator& integ, int domain, int perm,

@@ -130,6 +130,31 @@ def test_solver_matches_dense_solve(cuda, precision):
     assert rel(X2, ref) < 1e-11
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solver_pivots_when_the_matrix_is_not_quasi_definite(cuda, precision):
+    """A head matrix whose triangle block has a diagonal entry of the wrong sign
+    is no longer quasi-definite: the LDL^T without pivoting stops there
+    (OMG_ERR_NOT_DEFINITE) and the solver refactors the matrix by the FP64 LU
+    with partial pivoting, which solves any nonsingular matrix as the
+    reference's Bunch-Kaufman does; an exactly singular one is reported."""
+    from openmeeg_gb300._lib import OMGError
+    api = _api()
+    w = _w("small_ico1_3l")
+    geo = api.Geometry.from_head(w.head)
+    HM = api.HeadMat(geo).cpu().numpy()
+    nv = sum(v.shape[0] for v in w.head.vertices)   # reference numbering: vertices, then triangles
+    A = HM.copy()
+    A[nv + 5, nv + 5] = -10.0 * abs(A[nv + 5, nv + 5])
+    B = np.random.default_rng(1).standard_normal((A.shape[0], 3))
+    X = api.Solver(geo, precision=precision, hm=A).solve(B).cpu().numpy()
+    assert rel(X, np.linalg.solve(A, B)) < 1e-10
+    A[:, nv + 7] = 0.0
+    A[nv + 7, :] = 0.0
+    with pytest.raises(OMGError) as e:
+        api.Solver(geo, precision=precision, hm=A)
+    assert e.value.code == -9
+
+
 def test_headmat_config0_matches_oracle(cuda):
     from oracle import oracle
     api = _api()
