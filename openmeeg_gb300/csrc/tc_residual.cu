@@ -40,6 +40,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "handles.h"
 #include "tcgen05.cuh"
 
 namespace omg {
@@ -75,8 +76,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
+constexpr int MAXGROUPS = 6;
+
 struct PairPlan {
     int n;                       // digit pairs, ordered by level s + t
+    int ngroups;                 // work items per output tile: level-aligned runs of pairs, each summed into its
+    int gbeg[MAXGROUPS + 1];     // own output slice (pairs gbeg[g] .. gbeg[g + 1] - 1)
     int nwin;                    // windows per pair (K = nwin * KC, zero-padded)
     uint64_t flush;              // bit p: subtract the level sum after pair p
     uint8_t s[MAXPAIRS], t[MAXPAIRS];
@@ -93,7 +98,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     residual_slices_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tX,
                            const __grid_constant__ PairPlan plan, int N, int k, int kpad, int beta,
                            const int* __restrict__ rexp, const int* __restrict__ cexp, double sgn, double* R,
-                           int64_t ldr, int64_t ntiles, int ncb, int nmma, int* err) {
+                           int64_t ldr, double* Rp, int64_t ntiles, int nrb, int ncb, int nmma, int* err) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -103,7 +108,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t sbase = (dev::smem_u32(smem_raw) + 1023u) & ~1023u;
     int* const s_int = reinterpret_cast<int*>(smem_raw + (sbase - dev::smem_u32(smem_raw)) + STAGES * STAGE_BYTES);
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int units = plan.n * plan.nwin;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             dev::mbar_init(&full_bar[s], 1);
@@ -134,9 +138,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {   // ---- TMA producer
             int64_t g = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
-                const int rb = (int)(t / ncb), cb = (int)(t % ncb);
+                const int gr = (int)(t / ((int64_t)nrb * ncb)), rb = (int)(t / ncb % nrb), cb = (int)(t % ncb);
+                const int units = (plan.gbeg[gr + 1] - plan.gbeg[gr]) * plan.nwin;
                 for (int u = 0; u < units && !s_abort; ++u) {
-                    const int p = u / plan.nwin, w = u % plan.nwin;
+                    const int p = plan.gbeg[gr] + u / plan.nwin, w = u % plan.nwin;
                     const int ya = (plan.s[p] - 1) * N + rb * BM, yx = (plan.t[p] - 1) * kpad + cb * nmma;
                     for (int c = 0; c < CPW; ++c, ++g) {
                         const int slot = (int)(g % STAGES);
@@ -160,6 +165,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             bool ok = true;
             const uint32_t idesc = idesc_bf16(nmma);
             for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int gr = (int)(t / ((int64_t)nrb * ncb));
+                const int units = (plan.gbeg[gr + 1] - plan.gbeg[gr]) * plan.nwin;
                 for (int u = 0; u < units && ok; ++u, ++lu) {
                     const uint32_t ab = (uint32_t)(lu & 1), aph = (uint32_t)((lu >> 1) & 1);
                     if (!tc::wait_or_abort(&tempty_bar[ab], aph ^ 1u, &s_abort)) {
@@ -200,7 +207,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         int* const si = s_int + (warp - 2) * 32 + lane;
         int64_t lu = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            const int rb = (int)(t / ncb), cb = (int)(t % ncb);
+            const int gr = (int)(t / ((int64_t)nrb * ncb)), rb = (int)(t / ncb % nrb), cb = (int)(t % ncb);
+            const int units = (plan.gbeg[gr + 1] - plan.gbeg[gr]) * plan.nwin;
             const int row = rb * BM + q * 32 + lane;
             const int c0 = cb * nmma + grp * 64;
             const int cend = min(64, nmma - grp * 64);   // the group's columns inside this tile
@@ -233,10 +241,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                 fence_before();
                 __syncwarp();
                 if (lane == 0) tc::mbar_arrive(&tempty_bar[ab]);
-                const int p = u / plan.nwin, w = u % plan.nwin;
+                const int p = plan.gbeg[gr] + u / plan.nwin, w = u % plan.nwin;
                 if (active && w == plan.nwin - 1 && ((plan.flush >> p) & 1ull)) {   // level sum -> R (FP64)
                     // 32 columns at a time through shared memory, so the (rare) FP64 pass holds few registers
                     const int lev = plan.s[p] + plan.t[p];
+                    // group 0 sums into R, group g > 0 into its own n x k slice of Rp (leading dimension N)
+                    double* const Rg = gr == 0 ? R : Rp + (int64_t)(gr - 1) * N * k;
+                    const int64_t ldg = gr == 0 ? ldr : N;
 #pragma unroll
                     for (int h = 0; h < 64 / SPILL; ++h) {
 #pragma unroll
@@ -249,7 +260,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 const int col = c0 + h * SPILL + j;
                                 const int v = si[j * (EPI_WARPS * 32)];
                                 if (h * SPILL + j < cend && col < k && v != 0) {
-                                    R[row + (int64_t)col * ldr] += sgn * scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
+                                    Rg[row + (int64_t)col * ldg] +=
+                                        sgn * scalbn((double)v, er + __ldg(cexp + col) - beta * lev);
                                 }
                             }
                         }
@@ -272,6 +284,17 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
     if (warp == 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// R += the ng partial sums of the level groups 1.. (n x k slices of P), in group order.
+__global__ void sum_groups_kernel(int64_t n, int64_t k, int ng, const double* __restrict__ P, double* R, int64_t ldr) {
+    for (int64_t j = blockIdx.y; j < k; j += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+             i += (int64_t)gridDim.x * blockDim.x) {
+            double v = R[i + j * ldr];
+            for (int g = 0; g < ng; ++g) v += P[g * n * k + i + j * n];
+            R[i + j * ldr] = v;
+        }
 }
 
 // Digits of the columns of a column-major FP64 matrix: column c (rows j < n)
@@ -493,12 +516,53 @@ void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, con
                                            tcr::BM);
     const CUtensorMap mX = tc::make_map_2d(Xd, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (int64_t)ndx * kpad, ld, ld,
                                            tcr::BK, nmma);
-    const int64_t ntiles = (int64_t)nrb * ncb;
+    // few output tiles (a short side of the product): each tile's digit pairs are split into level-aligned
+    // groups, contiguous runs of levels with about equal pair counts, summed into separate slices and added
+    // in a fixed order afterwards (deterministic)
+    std::vector<int> lbeg;
+    for (int p = 0; p < plan.n; ++p)
+        if (p == 0 || pairs[p].first + pairs[p].second != pairs[p - 1].first + pairs[p - 1].second) lbeg.push_back(p);
+    lbeg.push_back(plan.n);
+    const int nlev = (int)lbeg.size() - 1;
+    const int64_t tiles = (int64_t)nrb * ncb;
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>({n_sm / tiles, (int64_t)tcr::MAXGROUPS, (int64_t)nlev}));
+    {   // contiguous partition of the levels into G groups minimising the largest pair count
+        const int INF = 1 << 30;
+        std::vector<std::vector<int>> best(G + 1, std::vector<int>(nlev + 1, INF)), cut(G + 1, std::vector<int>(nlev + 1, 0));
+        best[0][0] = 0;
+        for (int g = 1; g <= G; ++g)
+            for (int i = g; i <= nlev; ++i)
+                for (int j = g - 1; j < i; ++j) {
+                    if (best[g - 1][j] == INF) continue;
+                    const int c = std::max(best[g - 1][j], lbeg[i] - lbeg[j]);
+                    if (c < best[g][i]) {
+                        best[g][i] = c;
+                        cut[g][i] = j;
+                    }
+                }
+        plan.ngroups = G;
+        int i = nlev;
+        for (int g = G; g >= 1; --g) {
+            plan.gbeg[g] = lbeg[i];
+            i = cut[g][i];
+        }
+        plan.gbeg[0] = 0;
+    }
+    DevBuf parts(G > 1 ? (size_t)(G - 1) * n * k * 8 : 0, s);
+    if (G > 1) OMG_CUDA(cudaMemsetAsync(parts.p, 0, (size_t)(G - 1) * n * k * 8, s));
+    const int64_t ntiles = tiles * G;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
     tcr::residual_slices_kernel<<<grid, tcr::THREADS, tcr::SMEM_BYTES, s>>>(mA, mX, plan, (int)n, (int)k, (int)kpad,
-                                                                            beta, rexp, cexp, sgn, R, ldr, ntiles,
-                                                                            ncb, nmma, err);
+                                                                            beta, rexp, cexp, sgn, R, ldr,
+                                                                            parts.as<double>(), ntiles, nrb, ncb,
+                                                                            nmma, err);
     check_tcr(prof_name);
+    if (G > 1) {
+        tcr::sum_groups_kernel<<<dim3((unsigned)std::min<int64_t>((n + 255) / 256, 1024),
+                                      (unsigned)std::min<int64_t>(k, 32768)), 256, 0, s>>>(
+            n, k, G - 1, parts.as<double>(), R, ldr);
+        check_tcr("digit GEMM groups");
+    }
 }
 
 // R = B - A X, A symmetric n x n (its digit rows are its digit columns).
