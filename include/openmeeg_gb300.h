@@ -207,8 +207,15 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
  * numbering, lower triangle read) -- SymMatrix::solveLin on an existing HM. */
 int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double* hm, int64_t ld,
                                 int32_t precision, omg_solver* out);
-/* In place: B (N x nrhs, leading dimension ldb) <- HeadMat^-1 B. */
+/* In place: B (N x nrhs, leading dimension ldb) <- HeadMat^-1 B.  Mixed
+ * precision: if the refinement stalls above its tolerance, the head matrix is
+ * rebuilt and solved in FP64 (quasi-definite LDL^T, or the pivoted LU), and the
+ * solver stays FP64 from then on. */
 int omg_solver_solve_dev(omg_solver s, double* b, int64_t ldb, int64_t nrhs);
+/* Mixed-precision refinement controls: stop when the predicted relative error
+ * of the solution is below tol (default 1e-6), after at most max_steps
+ * residual steps (default 10). */
+int omg_solver_set_refinement(omg_solver s, double tol, int32_t max_steps);
 int omg_solver_destroy(omg_solver s);
 
 /* ---- gain ------------------------------------------------------------------ *

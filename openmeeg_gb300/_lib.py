@@ -127,6 +127,7 @@ _PROTOS = [
     ("omg_solver_create", c_i32, [c_vp, c_vp, ctypes.POINTER(Integrator), c_i32, ctypes.POINTER(c_vp)]),
     ("omg_solver_from_headmat_dev", c_i32, [c_vp, c_vp, c_vp, c_i64, c_i32, ctypes.POINTER(c_vp)]),
     ("omg_solver_solve_dev", c_i32, [c_vp, c_vp, c_i64, c_i64]),
+    ("omg_solver_set_refinement", c_i32, [c_vp, ctypes.c_double, c_i32]),
     ("omg_solver_destroy", c_i32, [c_vp]),
     ("omg_gain_dev", c_i32, [c_vp, c_vp, c_i32, ctypes.POINTER(Integrator), ctypes.POINTER(Integrator), c_vp, c_i64,
                              c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, ctypes.POINTER(GainStats)]),

@@ -365,6 +365,12 @@ class Solver:
                                                            _prec(precision), ctypes.byref(h)))
         self.handle = h
 
+    def set_refinement(self, tol: float = 1e-6, max_steps: int = 10) -> None:
+        """Mixed precision: stop refining when the predicted relative error is
+        below tol, after at most max_steps residual steps; a refinement that
+        stalls above tol falls back to an FP64 solve of the rebuilt head matrix."""
+        check(self.ctx.lib.omg_solver_set_refinement(self.handle, float(tol), int(max_steps)))
+
     def solve(self, B) -> torch.Tensor:
         """HM^-1 B for B of shape (N,) or (N, k)."""
         b = _as_dev(B, self.ctx)

@@ -51,7 +51,11 @@ void launch_fold_to_reference(int64_t Nref, int64_t nvg, int64_t nP, const int64
 void launch_partial_block(const DevGeom& g, int64_t p0, int64_t npc, const double* pts, const int* pdom,
                           const int64_t* rows, const int32_t* tmesh, const int64_t* tidx_ref, const int* barrier,
                           const int* orient, int maxb, const int* dnb, const int* bmesh, const int* binside,
-                          const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s);
+                          const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s,
+                          int64_t tshift = 0);
+void launch_fold_columns(int64_t nrow, int64_t Nref, int64_t nvg, int64_t nv, const int64_t* gbeg,
+                         const int64_t* gcopy, const double* in, int64_t ldi, double* out, int64_t ldo,
+                         cudaStream_t s);
 void launch_nearest_triangle(const DevGeom& g, const double* pos, int64_t ne, int64_t ncand, const int32_t* cand,
                              int64_t* out_tri, cudaStream_t s);
 void launch_eit_rows(const DevGeom& g, const int64_t* inj, int64_t nk, int64_t t2b, int64_t t2e, int64_t vb,
@@ -1123,6 +1127,33 @@ void solve_mixed_fixed(omg_solver sv, double* B, int64_t ldb, int64_t nrhs, int 
     copy_convert<double, double>(N, nrhs, x, N, B, ldb, false, 1.0, s);
 }
 
+// A stalled mixed refinement: the head matrix rebuilt and factored in FP64 (LDL^T, or the pivoted LU), the
+// right-hand sides solved again from their saved copy.
+static void solve_mixed_or_fp64(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
+    cudaStream_t s = sv->ctx->stream;
+    const int64_t N = sv->N;
+    DevBuf B0(sv->rebuild ? (size_t)N * nrhs * 8 : 0, s);
+    if (sv->rebuild) OMG_CUDA(cudaMemcpy2DAsync(B0.p, N * 8, B, ldb * 8, N * 8, nrhs, cudaMemcpyDeviceToDevice, s));
+    try {
+        solve_mixed(sv, B, ldb, nrhs);
+        return;
+    } catch (const Error& e) {
+        if (e.code != OMG_ERR_NOT_CONVERGED || !sv->rebuild) throw;
+    }
+    sv->A32.release();
+    sv->A32r.release();
+    sv->W.release();
+    sv->Linv32.release();
+    sv->Adig.release();
+    sv->rexp.release();
+    sv->A64.release();
+    sv->w_off.clear();
+    sv->precision = OMG_PREC_FP64;
+    solver_factor_or_pivot(sv, sv->rebuild(), sv->rebuild);
+    OMG_CUDA(cudaMemcpy2DAsync(B, ldb * 8, B0.p, N * 8, N * 8, nrhs, cudaMemcpyDeviceToDevice, s));
+    solver_solve_internal(sv, B, ldb, nrhs);
+}
+
 void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) {
     if (nrhs <= 0) return;
     if (sv->lu) {
@@ -1133,7 +1164,7 @@ void solver_solve_internal(omg_solver sv, double* B, int64_t ldb, int64_t nrhs) 
     } else if (sv->precision == OMG_PREC_FP64)
         solve_ldlt<double>(sv, sv->A64.as<double>(), sv->N, B, ldb, nrhs);
     else
-        solve_mixed(sv, B, ldb, nrhs);
+        solve_mixed_or_fp64(sv, B, ldb, nrhs);
 }
 
 // ---------------------------------------------------------------------------
@@ -1298,7 +1329,7 @@ static void build_source_surface(SourceSurface& u, omg_geometry geo, const doubl
         std::copy(geo->h.T.begin(), geo->h.T.end(), T.begin());
         for (int m = 0; m < geo->h.nmesh; ++m)
             for (int64_t t = geo->h.tbeg[m]; t < geo->h.tbeg[m + 1]; ++t)
-                if (!geo->h.barrier[m]) tpos[t] = (int32_t)(geo->h.tidx[t] - geo->h.nv);
+                if (!geo->h.barrier[m]) tpos[t] = (int32_t)(geo->h.tidx[t] - geo->h.nvg);
     }
     std::copy(verts, verts + 3 * nvs, V.begin() + 3 * nv0);
     for (int64_t i = 0; i < 3 * nts; ++i) T[3 * nt0 + i] = (int32_t)(tris[i] + nv0);
@@ -1614,7 +1645,6 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && ssm, "null argument");
         set_device(ctx);
-        require_distinct_vertices(geo, "SurfSourceMat");
         const omg_integrator it = integ ? *integ : default_hm_integrator();
         check_integrator(it, false);
         cudaStream_t s = ctx->stream;
@@ -1660,7 +1690,11 @@ int omg_surfsourcemat_dev(omg_context ctx, omg_geometry geo, const double* verts
                                 s, true);
             }
         }
-        launch_rows_to_reference(geo->d, n_verts, out.as<double>(), Nint, ssm, geo->d.Nref, s);
+        if (h.shared)   // rows of the vertex copies summed per distinct vertex (a shared vertex gathers both meshes)
+            launch_fold_to_reference(h.N, h.nvg, geo->d.nP, geo->gbeg, geo->gcopy, n_verts, out.as<double>(), Nint,
+                                     ssm, 1, h.N, s);
+        else
+            launch_rows_to_reference(geo->d, n_verts, out.as<double>(), Nint, ssm, geo->d.Nref, s);
         check_err(ctx, "SurfSourceMat");
     });
 }
@@ -1721,7 +1755,6 @@ int omg_surf2volmat_dev(omg_context ctx, omg_geometry geo, const double* points,
                         int64_t* n_kept) {
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && n_kept && (n_points == 0 || (points && out)), "null argument");
-        require_distinct_vertices(geo, "Surf2VolMat");
         OMG_REQUIRE(n_points >= 0, "negative point count");
         set_device(ctx);
         cudaStream_t s = ctx->stream;
@@ -1731,15 +1764,22 @@ int omg_surf2volmat_dev(omg_context ctx, omg_geometry geo, const double* points,
         *n_kept = kp.kept;
         const int64_t ld = kp.kept, Nref = geo->d.Nref;
         if (kp.kept == 0) return;
-        OMG_CUDA(cudaMemsetAsync(out, 0, (size_t)ld * Nref * 8, s));
+        // meshes sharing vertices: the columns of every vertex copy first (nv + triangle unknowns), folded to the
+        // distinct vertices afterwards (a shared vertex's P1 basis spans the triangles of all its meshes)
+        const HostGeometry& h = geo->h;
+        const int64_t ncol_w = h.shared ? h.nv + (Nref - h.nvg) : Nref, tshift = h.shared ? h.nv - h.nvg : 0;
+        DevBuf work(h.shared ? (size_t)ld * ncol_w * 8 : 0, s);
+        double* dst = h.shared ? work.as<double>() : out;
+        OMG_CUDA(cudaMemsetAsync(dst, 0, (size_t)ld * ncol_w * 8, s));
         // chunk the points so the P1 scratch stays near 512 MB
         const int64_t per = std::max<int64_t>(1, std::min<int64_t>(4096, (512ll << 20) / (geo->h.nt * 24)));
         DevBuf p1((size_t)std::min(per, n_points) * geo->h.nt * 24, s);
         for (int64_t p0 = 0; p0 < n_points; p0 += per)
             launch_partial_block(geo->d, p0, std::min(per, n_points - p0), points, kp.dom.as<int>(),
                                  kp.rows.as<int64_t>(), geo->tmesh, geo->tidx_ref, geo->barrier, geo->orient,
-                                 geo->maxb, geo->dnb, geo->bmesh, geo->binside, geo->dsigma, p1.as<double>(), out, ld,
-                                 s);
+                                 geo->maxb, geo->dnb, geo->bmesh, geo->binside, geo->dsigma, p1.as<double>(), dst, ld,
+                                 s, tshift);
+        if (h.shared) launch_fold_columns(ld, Nref, h.nvg, h.nv, geo->gbeg, geo->gcopy, dst, ld, out, ld, s);
         check_err(ctx, "Surf2VolMat");
     });
 }
@@ -2068,7 +2108,8 @@ int omg_solver_create(omg_context ctx, omg_geometry geo, const omg_integrator* i
         const omg_integrator it = integ ? *integ : default_hm_integrator();
         DevBuf hm = assemble_system(geo, it, precision, true);
         check_err(ctx, "HeadMat");
-        solver_factor_or_pivot(sv.get(), std::move(hm), [&] { return assemble_system(geo, it, precision, true); });
+        sv->rebuild = [geo, it, precision] { return assemble_system(geo, it, precision, true); };
+        solver_factor_or_pivot(sv.get(), std::move(hm), sv->rebuild);
         ctx->refs++;
         geo->refs++;
         *out = sv.release();
@@ -2094,6 +2135,7 @@ int omg_solver_from_headmat_dev(omg_context ctx, omg_geometry geo, const double*
             launch_from_reference_dense(geo->dg, hm, ld, A.as<double>(), sv->N, ctx->stream);
             return A;
         };
+        // (the caller's matrix is not kept: a stalled refinement is reported, not re-solved)
         solver_factor_or_pivot(sv.get(), copy_in(), copy_in);
         ctx->refs++;
         geo->refs++;
@@ -2122,6 +2164,15 @@ int omg_solver_solve_dev(omg_solver sv, double* b, int64_t ldb, int64_t nrhs) {
             OMG_CUDA(cudaMemcpyAsync(b + j * ldb, x + j * N + nP, (size_t)nv * 8, cudaMemcpyDeviceToDevice, s));
         }
         OMG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int omg_solver_set_refinement(omg_solver sv, double tol, int32_t max_steps) {
+    return guarded([&] {
+        OMG_REQUIRE(sv, "null argument");
+        OMG_REQUIRE(tol > 0.0 && max_steps >= 0, "bad refinement controls");
+        sv->refine_tol = tol;
+        sv->max_refine = max_steps;
     });
 }
 
@@ -2195,7 +2246,8 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaEventRecord(ev[1], s));
     OMG_CUDA(cudaStreamWaitEvent(s, ev[6], 0));
     OMG_CUDA(cudaEventRecord(ev[2], s));
-    solver_factor_or_pivot(sv.get(), std::move(hm), [&] { return assemble_system(geo, hm_it, precision, false); });
+    sv->rebuild = [geo, hm_it, precision] { return assemble_system(geo, hm_it, precision, false); };
+    solver_factor_or_pivot(sv.get(), std::move(hm), sv->rebuild);
     OMG_CUDA(cudaEventRecord(ev[3], s));
     {   // after the factorization's last work on the second stream (stream order); every stage of the
         // pipeline is throughput-bound, so the sources run where they take the least (under the assembly

@@ -2124,7 +2124,7 @@ __global__ void partial_block_kernel(int64_t p0, int64_t npc, const double* __re
                                      const int* __restrict__ barrier, const int* __restrict__ orient, int maxb,
                                      const int* __restrict__ dnb, const int* __restrict__ bmesh,
                                      const int* __restrict__ binside, const double* __restrict__ dsigma,
-                                     double* __restrict__ p1tmp, double* out, int64_t ldo) {
+                                     double* __restrict__ p1tmp, double* out, int64_t ldo, int64_t tshift) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t il = blockIdx.y;
     if (t >= nt || il >= npc) return;
@@ -2149,7 +2149,7 @@ __global__ void partial_block_kernel(int64_t p0, int64_t npc, const double* __re
     o3[0] = v[0] * -c;
     o3[1] = v[1] * -c;
     o3[2] = v[2] * -c;
-    if (!barrier[m]) out[row + tidx_ref[t] * ldo] = (c / dsigma[d]) * dev::operator_S(srec + t * SREC, x);
+    if (!barrier[m]) out[row + (tidx_ref[t] + tshift) * ldo] = (c / dsigma[d]) * dev::operator_S(srec + t * SREC, x);
 }
 
 __global__ void partial_block_gather_kernel(int64_t p0, int64_t npc, const int64_t* __restrict__ rows, int64_t nv,
@@ -2169,12 +2169,14 @@ __global__ void partial_block_gather_kernel(int64_t p0, int64_t npc, const int64
 void launch_partial_block(const DevGeom& g, int64_t p0, int64_t npc, const double* pts, const int* pdom,
                           const int64_t* rows, const int32_t* tmesh, const int64_t* tidx_ref, const int* barrier,
                           const int* orient, int maxb, const int* dnb, const int* bmesh, const int* binside,
-                          const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s) {
+                          const double* dsigma, double* p1tmp, double* out, int64_t ldo, cudaStream_t s,
+                          int64_t tshift) {
     if (npc == 0) return;
     ProfScope prof_("partial_block", s);
     dim3 grid(nblocks(g.nt, 128), (unsigned)npc);
     partial_block_kernel<<<grid, 128, 0, s>>>(p0, npc, pts, pdom, rows, g.nt, g.srec, g.prec, tmesh, tidx_ref,
-                                              barrier, orient, maxb, dnb, bmesh, binside, dsigma, p1tmp, out, ldo);
+                                              barrier, orient, maxb, dnb, bmesh, binside, dsigma, p1tmp, out, ldo,
+                                              tshift);
     check_launch("partial block");
     dim3 grid2(nblocks(g.nv, 128), (unsigned)npc);
     partial_block_gather_kernel<<<grid2, 128, 0, s>>>(p0, npc, rows, g.nv, g.nt, p1tmp, g.v2t_beg, g.v2t_tri,
@@ -2477,6 +2479,35 @@ __global__ void fold_to_reference_kernel(int64_t Nref, int64_t nvg, int64_t nP, 
         for (int64_t k = a0; k < a1; ++k) acc += in[copy_at(k, nP, gcopy) + c * ldi];
         out[r * rs + c * cs] = acc;
     }
+}
+
+// Columns of a per-copy matrix (nrow x (nv + triangles): vertex copies, then the triangle unknowns) folded to
+// the reference's columns (distinct vertices, then triangles): out(:, r) = sum of the copies of vertex r, in
+// copy order, for r < nvg; the triangle columns moved.
+__global__ void fold_columns_kernel(int64_t nrow, int64_t Nref, int64_t nvg, int64_t nv, const int64_t* __restrict__ gbeg,
+                                    const int64_t* __restrict__ gcopy, const double* __restrict__ in, int64_t ldi,
+                                    double* out, int64_t ldo) {
+    for (int64_t r = blockIdx.y; r < Nref; r += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nrow;
+             i += (int64_t)gridDim.x * blockDim.x) {
+            double acc = 0.0;
+            if (r < nvg) {
+                for (int64_t k = gbeg[r]; k < gbeg[r + 1]; ++k) acc += in[i + gcopy[k] * ldi];
+            } else {
+                acc = in[i + (r - nvg + nv) * ldi];
+            }
+            out[i + r * ldo] = acc;
+        }
+}
+
+void launch_fold_columns(int64_t nrow, int64_t Nref, int64_t nvg, int64_t nv, const int64_t* gbeg,
+                         const int64_t* gcopy, const double* in, int64_t ldi, double* out, int64_t ldo,
+                         cudaStream_t s) {
+    if (nrow <= 0) return;
+    ProfScope prof_("fold", s);
+    dim3 grid(nblocks(nrow, 256), (unsigned)std::min<int64_t>(Nref, 32768));
+    fold_columns_kernel<<<grid, 256, 0, s>>>(nrow, Nref, nvg, nv, gbeg, gcopy, in, ldi, out, ldo);
+    check_launch("fold columns");
 }
 
 void launch_fold_to_reference(int64_t Nref, int64_t nvg, int64_t nP, const int64_t* gbeg, const int64_t* gcopy,

@@ -46,6 +46,8 @@ struct omg_solver_s {
     // Bunch-Kaufman DSPTRF) and perm its row order
     bool lu = false;
     DevBuf perm;
+    // the head matrix again (assembled or copied in), for the FP64 solve a stalled refinement falls back to
+    std::function<DevBuf()> rebuild;
 };
 
 // Near-pair lists of a geometry's mixed-precision assembly, one per mesh pair.

@@ -308,6 +308,44 @@ def save_cortical():
     print("cortical", {k: v.shape for k, v in d.items()})
 
 
+def save_shared_vertex_sources():
+    """om_assemble -SSM and -H2IPM on the reference's HeadNNa1, whose two
+    hemispheres share the vertices of their cut mesh: an ico1 source surface in
+    the north hemisphere and points inside both hemispheres (plus two in the
+    air, dropped).  The head's files are in reference_heads.npz."""
+    import subprocess
+    import shutil
+    import tempfile
+    from openmeeg_gb300 import synthetic as syn
+    R = ref_runner.REFERENCE_DIR
+    if not ref_runner.available():
+        ref_runner.build()
+    wd = tempfile.mkdtemp()
+    base = os.path.join(R, "data", "HeadNNa1")
+    for f in os.listdir(base):
+        shutil.copy(os.path.join(base, f), wd)
+    V, T = syn.icosphere(1, inward=False)
+    V = V * 0.08 + np.array([0.02, -0.01, 0.45])
+    rng = np.random.default_rng(5)
+    P = []
+    while len(P) < 16:   # inside the hemispheres, away from the cut and the cortex
+        x = rng.uniform(-0.7, 0.7, 3)
+        if np.linalg.norm(x) < 0.7 and abs(x[2]) > 0.1:
+            P.append(x)
+    P = np.array(P + [[1.3, 0.0, 0.0], [0.0, -1.3, 0.2]])
+    io.write_tri(os.path.join(wd, "src.tri"), V, T)
+    io.write_matrix_txt(os.path.join(wd, "pts.txt"), P)
+    for args in (["om_assemble", "-SSM", "HeadNNa1.geom", "HeadNNa1.cond", "src.tri", "ssm.bin"],
+                 ["om_assemble", "-H2IPM", "HeadNNa1.geom", "HeadNNa1.cond", "pts.txt", "h2ipm.bin"]):
+        subprocess.check_call([os.path.join(ref_runner.REF_BIN, args[0]), *args[1:]], cwd=wd,
+                              stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    d = {"src_vertices": V, "src_triangles": T, "points": P,
+         "ssm": io.read_bin(os.path.join(wd, "ssm.bin"))[1], "h2ipm": io.read_bin(os.path.join(wd, "h2ipm.bin"))[1]}
+    shutil.rmtree(wd, ignore_errors=True)
+    np.savez_compressed(os.path.join(OUT, "shared_vertex_sources.npz"), **d)
+    print("shared_vertex_sources", {k: v.shape for k, v in d.items()})
+
+
 REFERENCE_HEADS = ("HeadNNb1", "HeadMN1", "HeadMN2", "HeadMN3", "HeadNNa1", "HeadNNc1")
 
 
@@ -354,6 +392,9 @@ def main():
     if "--head1-only" in sys.argv:
         save_head1()
         return
+    if "--shared-only" in sys.argv:
+        save_shared_vertex_sources()
+        return
     save_head3_analytic()
     if "--analytic-only" in sys.argv:
         return
@@ -372,6 +413,7 @@ def main():
     save_direct_gains()
     save_cortical()
     save_head1()
+    save_shared_vertex_sources()
     if not ref_runner.available():
         ref_runner.build()
     big = "--big" in sys.argv

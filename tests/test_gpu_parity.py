@@ -155,6 +155,22 @@ def test_solver_pivots_when_the_matrix_is_not_quasi_definite(cuda, precision):
     assert e.value.code == -9
 
 
+def test_mixed_solver_falls_back_to_fp64_when_refinement_stalls(cuda):
+    """An unreachable refinement tolerance: the mixed refinement stalls, the
+    solver rebuilds its (mixed-assembled) head matrix and solves it in FP64."""
+    api = _api()
+    w = _w("small_ico2_3l_pert")
+    geo = api.Geometry.from_head(w.head)
+    Hm = api.HeadMat(geo, precision="mixed").cpu().numpy()
+    B = np.random.default_rng(2).standard_normal((Hm.shape[0], 4))
+    s = api.Solver(geo, precision="mixed")
+    s.set_refinement(1e-300, 2)
+    X = s.solve(B).cpu().numpy()
+    assert rel(X, np.linalg.solve(Hm, B)) < 1e-11
+    X2 = s.solve(B).cpu().numpy()           # the solver stays FP64 from then on
+    assert rel(X2, X) < 1e-14
+
+
 def test_headmat_config0_matches_oracle(cuda):
     from oracle import oracle
     api = _api()

@@ -76,3 +76,19 @@ def test_reference_head_gains(cuda, ref, name, prec, tmp_path):
     if f"{name}_eeg_analytic" in ref:
         ana = ref[f"{name}_eeg_analytic"]
         assert np.all(analytic.rdm(ge, ana) < 0.10) and np.all(analytic.mag(ge, ana) < 0.10)
+
+
+def test_shared_vertex_surface_sources_match_reference(cuda, ref, tmp_path):
+    """SurfSourceMat and Surf2VolMat on HeadNNa1, whose hemispheres share the
+    vertices of their cut mesh: computed on the per-mesh vertex copies and
+    folded to the distinct vertices (rows for SurfSourceMat, columns for
+    Surf2VolMat); against om_assemble -SSM / -H2IPM
+    (tests/golden/shared_vertex_sources.npz)."""
+    from openmeeg_gb300 import api
+    S = golden("shared_vertex_sources")
+    geom, cond = _files(ref, "HeadNNa1", tmp_path)
+    geo = api.Geometry(geom, cond)
+    ssm = api.SurfSourceMat(geo, S["src_vertices"], S["src_triangles"]).cpu().numpy()
+    assert ssm.shape == S["ssm"].shape and rel(ssm, S["ssm"]) < 1e-12
+    h2ipm = api.Surf2VolMat(geo, S["points"]).cpu().numpy()
+    assert h2ipm.shape == S["h2ipm"].shape and rel(h2ipm, S["h2ipm"]) < 1e-12
