@@ -238,11 +238,23 @@ NCU_TRAFFIC_PER_UNIT = {
     # residual B - A X (double-float): bytes per N^2 element of the float-pair head matrix
     # (ncu at N = 17926: 3.205 GB per launch)
     "residual_df64": 9.97,
-    # residual from digits: DRAM bytes per byte of one digit plane, per digit pair and column
-    # block of right-hand sides (ncu at N = 4486, 96 right-hand sides: 1.105 GB per launch for
-    # 28 pairs of 40.8 MB planes); column blocks are counted as if they shared nothing in L2
-    "residual_tc": 0.968,
+    # residual from digits: DRAM bytes per launch at config1 (N = 17926, 215 right-hand sides, tiles of
+    # 128 x 224, one level group; ncu dram__bytes_read.sum + dram__bytes_write.sum of the first residual
+    # launch: 14.01 GB + 157.5 MB), per byte of the 21 digit-plane reads the kernel structure implies
+    # (21 x N x ld x 2 B = 13.54 GB)
+    "residual_tc": (14.01e9 + 0.1575e9) / (21 * 17926 * 17984 * 2.0),   # 14.17 GB per launch; 1.05
 }
+
+
+def digit_tiles(n, k, n_sm=152):
+    """The digit GEMM's tile width (columns per tile, a multiple of 16) and column-block count for an
+    n x k output, as the library picks them (tc_residual.cu, digit_gemm)."""
+    nrb = (n + 127) // 128
+    ncb = (k + 255) // 256
+    width = lambda nc: ((k + nc - 1) // nc + 15) // 16 * 16
+    while 2 * nrb * ncb < n_sm and width(ncb + 1) >= 64:
+        ncb += 1
+    return width(ncb), ncb
 
 
 def pipe_peaks():
@@ -296,22 +308,25 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_, pipes):
     info = {"kernel": name, "launches_per_step": per_step, "mean_launch_ms": ms / launches}
     if name == "residual_tc":
         # R = B - A X from 6 + 6 bf16 digit planes, 21 digit pairs (levels <= 7): every pair is a full
-        # N x N x k integer GEMM on the tensor cores, padded to 128-column tiles of the k right-hand sides
+        # N x N x k integer GEMM on the tensor cores, k padded to the tiles' width (a multiple of 16)
         pairs = 21
-        kpad = (k + 127) // 128 * 128
-        flops = 2.0 * N * N * kpad * pairs
+        width, ncb = digit_tiles(N, k)
+        kexec = width * ncb
+        flops = 2.0 * N * N * kexec * pairs
         achieved = flops / t_launch / 1e12
         ld = (N + 63) // 64 * 64
-        traffic = NCU_TRAFFIC_PER_UNIT["residual_tc"] * pairs * (N * ld * 2.0) * (kpad // 128)
+        plane_reads = pairs * (N * ld * 2.0) * ncb     # each pair streams one A plane per column block
+        measured = NCU_TRAFFIC_PER_UNIT["residual_tc"]
         info.update({"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": achieved / bf16, "traffic": traffic,
-                     "traffic_note": "DRAM bytes per launch scaled from an ncu capture at N = 4486; "
-                                     "an upper bound when the "
-                                     "column blocks share digit tiles in L2",
+                     "frac": achieved / bf16, "traffic": measured * plane_reads if measured else None,
+                     "digit_plane_reads_per_launch": plane_reads,
+                     "hbm_frac_if_plane_reads": plane_reads / t_launch / 1e9 / hbm,
+                     "traffic_note": "DRAM bytes per launch from an ncu capture of the config1 residual, scaled by "
+                                     "the plane reads (null when not captured)",
                      "algorithmic_fp64_equivalent_flops_per_launch": 2.0 * N * N * k,
                      "executed_bf16_flops_per_launch": flops,
-                     "note": f"executed bf16 tensor flops (21 exact digit-pair GEMMs, k padded to {kpad}) vs "
-                             f"{kind} bf16 burst peak"})
+                     "note": f"executed bf16 tensor flops (21 exact digit-pair GEMMs, {ncb} tile(s) of {width} "
+                             f"columns) vs {kind} bf16 burst peak"})
     elif name == "residual_df64":
         nbytes = 8.0 * N * N + 24.0 * N * k
         achieved = nbytes / t_launch / 1e9
