@@ -1908,7 +1908,6 @@ int omg_eitsourcemat_dev(omg_context ctx, omg_geometry geo, const double* positi
                          int64_t n_electrodes, const omg_integrator* integ, double* out) {
     return guarded([&] {
         OMG_REQUIRE(ctx && geo && (n_electrodes == 0 || (positions && out)), "null argument");
-        require_distinct_vertices(geo, "EITSourceMat");
         OMG_REQUIRE(n_electrodes >= 0, "negative electrode count");
         set_device(ctx);
         const omg_integrator it = integ ? *integ : default_hm_integrator();

@@ -41,6 +41,10 @@ void launch_h2mm(const DevGeom& g, const double* sq, int64_t np, const int32_t* 
                  double mag = kMagFactor);
 void launch_ds2mm(const double* dip, int64_t nd, const double* sq, int64_t np, double* out, int64_t ldo,
                   cudaStream_t s);
+void launch_fold_hm(int64_t Ng, int64_t nP, const int64_t* gbeg, const int64_t* gcopy, const double* hl, int64_t ldl,
+                    double* hg, int64_t ldg, cudaStream_t s);
+void launch_fold_rows(int64_t Ng, int64_t nP, const int64_t* gbeg, const int64_t* gcopy, int64_t ncol, const double* in,
+                      int64_t ldi, double* out, int64_t ldo, cudaStream_t s);
 void profile_enable(bool on);
 bool profiling_enabled();
 }  // namespace omg
@@ -141,7 +145,10 @@ void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
     omg_geometry g = m.geo;
     BindGeometry bind(g, c);
     cudaStream_t s = c->stream;
-    const int64_t N = g->d.N, ne = m.ne, nm = m.nm, nd = m.nd, k = ne + nm;
+    // N: the solver's unknowns (distinct vertices); meshes that share vertices are assembled on their vertex
+    // copies (Nl unknowns) and folded, as the single-model pipeline does
+    const int64_t N = g->dg.N, Nl = g->d.N, ne = m.ne, nm = m.nm, nd = m.nd, k = ne + nm;
+    const bool shared = g->h.shared;
     const bool mixed = b->precision == OMG_PREC_MIXED;
     auto sv = std::make_unique<omg_solver_s>();
     sv->ctx = c;
@@ -152,18 +159,29 @@ void enqueue_model(omg_batch b, BatchModel& m, omg_context c, bool planning) {
     sv->refine_tol = b->refine_tol;
     sv->residual_choice = planning ? -1 : m.tc_residual;
     DevBuf hm((size_t)N * N * 8, s);
-    if (mixed)
-        assemble_headmat_mixed(g, b->hm_it, hm.as<double>(), N, &m.near);
-    else
-        assemble_headmat_internal(g, b->hm_it, hm.as<double>(), N);
+    {
+        DevBuf hl(shared ? (size_t)Nl * Nl * 8 : 0, s);
+        double* dst = shared ? hl.as<double>() : hm.as<double>();
+        if (mixed)
+            assemble_headmat_mixed(g, b->hm_it, dst, Nl, &m.near);
+        else
+            assemble_headmat_internal(g, b->hm_it, dst, Nl);
+        if (shared) launch_fold_hm(N, g->d.nP, g->gbeg, g->gcopy, hl.as<double>(), Nl, hm.as<double>(), N, s);
+    }
     DevBuf B((size_t)N * std::max<int64_t>(k, 1) * 8, s), DSM((size_t)N * std::max<int64_t>(nd, 1) * 8, s);
     OMG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)N * std::max<int64_t>(k, 1) * 8, s));
     if (ne > 0)
         launch_h2em(g->d, m.el.as<double>(), ne, g->n_eeg_seg, g->eeg_seg, g->eeg_cand, 1, B.as<double>(), 1, N, 0,
                     nullptr, nullptr, s);
     DevBuf F((size_t)std::max<int64_t>(nm, 1) * g->h.nt * 8, s);
-    if (nm > 0)
+    if (nm > 0 && shared) {   // on the vertex copies, then summed per distinct vertex
+        DevBuf loc((size_t)Nl * nm * 8, s);
+        OMG_CUDA(cudaMemsetAsync(loc.p, 0, (size_t)Nl * nm * 8, s));
+        launch_h2mm(g->d, m.sq.as<double>(), nm, g->tmesh, g->jump, 1, loc.as<double>(), 1, Nl, 0, F.as<double>(), s);
+        launch_fold_rows(N, g->d.nP, g->gbeg, g->gcopy, nm, loc.as<double>(), Nl, B.as<double>() + ne * N, N, s);
+    } else if (nm > 0) {
         launch_h2mm(g->d, m.sq.as<double>(), nm, g->tmesh, g->jump, 1, B.as<double>(), 1, N, ne, F.as<double>(), s);
+    }
     std::vector<int> src_meshes;
     dsm_internal(g, m.dip.as<double>(), nd, b->dsm_it, -1, 1, DSM.as<double>(), N, b->precision,
                  planning ? &src_meshes : nullptr, planning ? 0 : m.allowed);
@@ -448,8 +466,6 @@ int omg_batch_create(omg_context ctx, int32_t n_models, const omg_batch_model* m
         for (int32_t i = 0; i < n_models; ++i) {
             const omg_batch_model& in = models[i];
             OMG_REQUIRE(in.geometry, "null geometry in batch");
-            if (in.geometry->h.shared)
-                throw Error(OMG_ERR_UNSUPPORTED, "batched forward of geometries whose meshes share vertices");
             OMG_REQUIRE(in.geometry->ctx->device == ctx->device, "batch geometries must live on the context's device");
             OMG_REQUIRE(in.n_dipoles >= 0 && in.n_electrodes >= 0 && in.n_squids >= 0, "negative count");
             OMG_REQUIRE(in.n_dipoles == 0 || in.dipoles, "null dipoles");

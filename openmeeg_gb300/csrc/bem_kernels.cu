@@ -2306,23 +2306,27 @@ __global__ void eit_d_gather_kernel(const int64_t* __restrict__ inj, int64_t nk,
                                     int64_t nvb, double coeffD, int self, const double* __restrict__ tmp,
                                     const int32_t* __restrict__ v2t_beg, const int32_t* __restrict__ v2t_tri,
                                     const int8_t* __restrict__ v2t_loc, const int32_t* __restrict__ T,
-                                    const double* __restrict__ srec, double* R, int64_t Nref) {
+                                    const double* __restrict__ srec, const int64_t* __restrict__ vglob, double* R,
+                                    int64_t Nref) {
     const int64_t iv = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t k = blockIdx.y;
     if (iv >= nvb || k >= nk) return;
     const int64_t v = vb + iv;
+    // the column of the vertex: a copy of a vertex shared by several meshes adds into its distinct vertex
+    // (the copies are in different meshes, so different launches, one after the other)
+    const int64_t col = vglob ? vglob[v] : v;
     double sum = 0.0;
     for (int q = v2t_beg[v]; q < v2t_beg[v + 1]; ++q) {
         const int64_t t2 = v2t_tri[q];
         if (t2 < t2b || t2 >= t2b + nb) continue;
         sum += tmp[(k * nb + (t2 - t2b)) * 3 + v2t_loc[q]];
     }
-    double r = R[k * Nref + v] + coeffD * sum;
+    double r = R[k * Nref + col] + coeffD * sum;
     if (self) {
         const int64_t u = inj[k];
         if (T[3 * u] == v || T[3 * u + 1] == v || T[3 * u + 2] == v) r += -0.5 * (srec[u * SREC + 12] / 3.0);
     }
-    R[k * Nref + v] = r;
+    R[k * Nref + col] = r;
 }
 
 // R[k, tidx(t2)] = coeffS * integral over t2 of OperatorS(inj[k]).
@@ -2351,7 +2355,7 @@ void launch_eit_rows(const DevGeom& g, const int64_t* inj, int64_t nk, int64_t t
     check_launch("EIT D");
     dim3 grid2(nblocks(ve - vb, 128), (unsigned)nk);
     eit_d_gather_kernel<<<grid2, 128, 0, s>>>(inj, nk, t2b, nb, vb, ve - vb, coeffD, self ? 1 : 0, tmp, g.v2t_beg,
-                                              g.v2t_tri, g.v2t_loc, g.T, g.srec, R, g.Nref);
+                                              g.v2t_tri, g.v2t_loc, g.T, g.srec, g.vglob, R, g.Nref);
     check_launch("EIT D gather");
     if (withS) {
         eit_s_kernel<<<grid, 128, 0, s>>>(inj, nk, g.srec, g.qrec, t2b, nb, order, tidx_ref, coeffS, R, g.Nref);

@@ -309,10 +309,11 @@ def save_cortical():
 
 
 def save_shared_vertex_sources():
-    """om_assemble -SSM and -H2IPM on the reference's HeadNNa1, whose two
-    hemispheres share the vertices of their cut mesh: an ico1 source surface in
-    the north hemisphere and points inside both hemispheres (plus two in the
-    air, dropped).  The head's files are in reference_heads.npz."""
+    """om_assemble -SSM, -H2IPM and -EITSM on the reference's HeadNNa1, whose
+    two hemispheres share the vertices of their cut mesh: an ico1 source
+    surface in the north hemisphere, points inside both hemispheres (plus two
+    in the air, dropped) and the head's own EEG patches as point electrodes.
+    The head's files are in reference_heads.npz."""
     import subprocess
     import shutil
     import tempfile
@@ -336,11 +337,14 @@ def save_shared_vertex_sources():
     io.write_tri(os.path.join(wd, "src.tri"), V, T)
     io.write_matrix_txt(os.path.join(wd, "pts.txt"), P)
     for args in (["om_assemble", "-SSM", "HeadNNa1.geom", "HeadNNa1.cond", "src.tri", "ssm.bin"],
-                 ["om_assemble", "-H2IPM", "HeadNNa1.geom", "HeadNNa1.cond", "pts.txt", "h2ipm.bin"]):
+                 ["om_assemble", "-H2IPM", "HeadNNa1.geom", "HeadNNa1.cond", "pts.txt", "h2ipm.bin"],
+                 ["om_assemble", "-EITSM", "HeadNNa1.geom", "HeadNNa1.cond", "HeadNNa1.patches", "eit.bin"]):
         subprocess.check_call([os.path.join(ref_runner.REF_BIN, args[0]), *args[1:]], cwd=wd,
                               stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     d = {"src_vertices": V, "src_triangles": T, "points": P,
-         "ssm": io.read_bin(os.path.join(wd, "ssm.bin"))[1], "h2ipm": io.read_bin(os.path.join(wd, "h2ipm.bin"))[1]}
+         "ssm": io.read_bin(os.path.join(wd, "ssm.bin"))[1], "h2ipm": io.read_bin(os.path.join(wd, "h2ipm.bin"))[1],
+         "eit": io.read_bin(os.path.join(wd, "eit.bin"))[1],
+         "eit_electrodes": io.read_sensors_txt(os.path.join(wd, "HeadNNa1.patches"))[1]}
     shutil.rmtree(wd, ignore_errors=True)
     np.savez_compressed(os.path.join(OUT, "shared_vertex_sources.npz"), **d)
     print("shared_vertex_sources", {k: v.shape for k, v in d.items()})

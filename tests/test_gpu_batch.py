@@ -132,3 +132,27 @@ def test_batch_autotune_and_info(heads, tmp_path, monkeypatch):
         ge, _ = b2.gains(i)
         re, _ = _single(g, w, w.dipoles, "mixed")
         assert _rel(ge, re) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_of_shared_vertex_heads(cuda, tmp_path, prec):
+    """HeadNNa1 (hemispheres sharing the vertices of their cut mesh) in a batch
+    beside a nested head: assembled on the vertex copies and folded, as the
+    single-model path does; each model's gains equal the single-model ones."""
+    from conftest import golden
+    from openmeeg_gb300 import api, workloads
+    R = golden("reference_heads")
+    for fn, tx in zip(R["HeadNNa1_files"], R["HeadNNa1_texts"]):
+        (tmp_path / str(fn)).write_text(str(tx))
+    f = [str(x) for x in R["HeadNNa1_files"]]
+    g1 = api.Geometry(str(tmp_path / f[0]), str(tmp_path / f[1]))
+    w2 = workloads.small(1, layers=3)
+    g2 = api.Geometry.from_head(w2.head)
+    models = [(g1, R["HeadNNa1_dipoles"], R["HeadNNa1_electrodes"], R["HeadNNa1_squids"]),
+              (g2, w2.dipoles, w2.electrodes, w2.squids)]
+    b = api.BatchForward(models, precision=prec, n_branches=2)
+    b.run()
+    for i, (g, dip, el, sq) in enumerate(models):
+        ge, gm = b.gains(i)
+        re, rm, _ = api.forward_gain(g, dip, el, sq, precision=prec)
+        assert _rel(ge, re) <= 1e-12 and _rel(gm, rm) <= 1e-12, i

@@ -79,11 +79,11 @@ def test_reference_head_gains(cuda, ref, name, prec, tmp_path):
 
 
 def test_shared_vertex_surface_sources_match_reference(cuda, ref, tmp_path):
-    """SurfSourceMat and Surf2VolMat on HeadNNa1, whose hemispheres share the
-    vertices of their cut mesh: computed on the per-mesh vertex copies and
-    folded to the distinct vertices (rows for SurfSourceMat, columns for
-    Surf2VolMat); against om_assemble -SSM / -H2IPM
-    (tests/golden/shared_vertex_sources.npz)."""
+    """SurfSourceMat, Surf2VolMat and EITSourceMat on HeadNNa1, whose
+    hemispheres share the vertices of their cut mesh: computed on the per-mesh
+    vertex copies and folded to the distinct vertices (rows for SurfSourceMat,
+    columns for Surf2VolMat and EITSourceMat); against om_assemble -SSM /
+    -H2IPM / -EITSM (tests/golden/shared_vertex_sources.npz)."""
     from openmeeg_gb300 import api
     S = golden("shared_vertex_sources")
     geom, cond = _files(ref, "HeadNNa1", tmp_path)
@@ -92,3 +92,5 @@ def test_shared_vertex_surface_sources_match_reference(cuda, ref, tmp_path):
     assert ssm.shape == S["ssm"].shape and rel(ssm, S["ssm"]) < 1e-12
     h2ipm = api.Surf2VolMat(geo, S["points"]).cpu().numpy()
     assert h2ipm.shape == S["h2ipm"].shape and rel(h2ipm, S["h2ipm"]) < 1e-12
+    eit = api.EITSourceMat(geo, S["eit_electrodes"]).cpu().numpy()
+    assert eit.shape == S["eit"].shape and rel(eit, S["eit"]) < 1e-12
