@@ -124,6 +124,7 @@ void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld,
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
 void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t col_offset, float* Linv, float* Bh,
                float* Bl, cudaStream_t s, bool store_l = true, bool pdl = false);
+void linv_from_split(int64_t nblocks, const float* B, float* Linv, float* LCh, float* LCl, cudaStream_t s);
 void diag_update(float* A, int64_t lda, int n, const float* P0h, const float* P0l, const float* P1h, const float* P1l,
                  cudaStream_t s, bool pdl = false);
 void apply_inv_blocks(int64_t nblocks, int nb, int n_last, int64_t ncol, const float* Li, bool trans, float* B,
@@ -690,8 +691,8 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
             float* Bil = Bih + (size_t)nb * nb;
             // programmatic dependent launches: each starts while its predecessor on the chain drains
             if (fp[0]) diag_update(A + k0 + k0 * ld, ld, (int)nk, fp[0], fp[1], fp[2], fp[3], sc, true);
-            potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0,
-                      sv->Linv32.as<float>() + b * nb * nb, Bih, Bil, sc, false, fp[0] != nullptr);
+            potrf_inv(A + k0 + k0 * ld, ld, (int)nk, sv->ctx->d_err, sv->ctx->d_errcol, k0, nullptr, Bih, Bil, sc,
+                      false, fp[0] != nullptr);
             for (auto& q : fp) q = nullptr;
             if (m == 0) continue;
             // L21 = A21 L11^-T on the tensor cores, written as heads (A) + remainders (A32r); its epilogue
@@ -787,7 +788,7 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     DevBuf LC((size_t)2 * nblocks * nb * nb * sizeof(float), s);   // Linv_b split as stored (column-major)
     float* LCh = LC.as<float>();
     float* LCl = LCh + nblocks * nb * nb;
-    split_cols(nb, (int64_t)nblocks * nb, nb, sv->Linv32.as<float>(), nb, LCh, LCl, s);
+    linv_from_split((int64_t)nblocks, Bi.as<float>(), sv->Linv32.as<float>(), LCh, LCl, s);
     // the panel folds on the main stream, the block-row folds on the second one: disjoint memory, and each
     // product is a few latency-bound waves, so two at a time fill the GPU
     OMG_CUDA(cudaEventRecord(ev_l, s));

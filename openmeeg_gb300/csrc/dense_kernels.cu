@@ -668,8 +668,10 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 // block A11 and the inverse of its factor, in one CTA of 512 threads, blocked
 // by 32 columns (4 block steps J):
 //   1. warp 0 factors the 32 x 32 diagonal block in registers (lane i holds
-//      row i, shifted so the current column is in a fixed register; column j
-//      is broadcast by shuffles), no CTA barrier inside;
+//      row i, shifted so the current column is in a fixed register; the
+//      unscaled column j is broadcast through shared memory while the pivot's
+//      reciprocal square root is formed, so the update a_ik -= a_ij a_kj / a_jj
+//      waits for one multiply after the broadcast), no CTA barrier inside;
 //   2. warp 0 inverts that block (lane c solves column c of X_JJ) while the
 //      threads of warps 1-3 solve one panel row each, L_rJ = A_rJ L_JJ^-T, by
 //      forward substitution (rows below the block);
@@ -682,11 +684,14 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 // memory (row-major, padded); columns past n act as the identity.
 
 // Outputs: L11 over A11 (lower; left out when store_l is false: the
-// factorization's solves use only the inverse), Linv column-major (ldi = 128, zero above the
-// diagonal and beyond n) for the solves, and Linv as TF32 head/remainder
+// factorization's solves use only the inverse), Linv as TF32 head/remainder
 // K-major rows (128 x 128 each, zero padded) for the tensor-core panel solve
-// L21 = A21 Linv^T.  A pivot that is not positive is reported as
-// OMG_ERR_NOT_DEFINITE at its column (and replaced by 1 so the kernel ends).
+// L21 = A21 Linv^T, and, when Linv is not null, Linv column-major (ldi = 128,
+// zero above the diagonal and beyond n).  The factorization leaves Linv null
+// and transposes all the blocks' splits at its end (linv_from_split): the
+// chain of diagonal blocks then stores 128 KB per block instead of 192 KB.
+// A pivot that is not positive is reported as OMG_ERR_NOT_DEFINITE at its
+// column (and replaced by 1 so the kernel ends).
 // ---------------------------------------------------------------------------
 constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512, PI_BS = 32, PI_TLD = 33;
 constexpr size_t PI_SMEM =
@@ -761,48 +766,59 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     asm volatile("griddepcontrol.launch_dependents;");
     asm volatile("griddepcontrol.wait;" ::: "memory");   // the block's last update (no-op without PDL)
-#pragma unroll 16
-    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // 32 iterations: loads batched by the unroll
-        const int r = e % PI_NB, c = e / PI_NB;    // coalesced down the columns of A
-        float v = 0.f;
-        if (r >= c) v = (r < n && c < n) ? A[r + (int64_t)c * lda] : (r == c ? 1.f : 0.f);
-        sA[r * PI_LD + c] = v;
+    // the lower triangle by 4-byte asynchronous copies (all of a thread's 32 in flight at once, no
+    // registers held), coalesced down the columns of A; identity beyond n, zero above the diagonal
+    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
+        const int r = e % PI_NB, c = e / PI_NB;
+        float* dst = sA + r * PI_LD + c;
+        if (r >= c && r < n) {   // c <= r < n
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(A + r + (int64_t)c * lda)
+                         : "memory");
+        } else {
+            *dst = (r == c) ? 1.f : 0.f;
+        }
         sX[r * PI_LD + c] = 0.f;
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     for (int J = 0; J < 4; ++J) {
         const int j0 = J * PI_BS;
         if (warp == 0) {   // ---- 1. Cholesky of the diagonal block
             // lane i holds row i, shifted left by one column per step so that the current column
-            // sits in r[0]; column j of L is broadcast through shared memory at positions relative
-            // to the pivot (l_(j+m)j at cb[m - 1]), read back as 8 aligned float4 (static offsets)
+            // sits in r[0]; the unscaled column j (a_(j+m)j at cb[m], the pivot at cb[0]) is broadcast
+            // through shared memory and read back as 8 aligned float4 (static offsets) while the
+            // pivot comes by shuffle and its reciprocal square root is formed
             float r[PI_BS];
 #pragma unroll
             for (int m = 0; m < PI_BS; ++m) r[m] = (m <= lane) ? sA[(j0 + lane) * PI_LD + j0 + m] : 0.f;
             int bad = -1;
 #pragma unroll 1
             for (int j = 0; j < PI_BS; ++j) {
-                float d = __shfl_sync(FULL, r[0], j);
+                const float u = r[0];   // a_(lane)j after the updates by the columns before j
+                const float ub = lane > j ? u : 0.f;   // rows j and above are final: no update
+                float* cb = sCol + (j & 1) * PI_BS;
+                if (lane >= j) cb[lane - j] = u;
+                float d = __shfl_sync(FULL, u, j);
+                __syncwarp();
                 if (!(d > 0.f)) {
                     if (bad < 0) bad = j;
                     d = 1.f;
                 }
                 const float inv = rsqrtf(d);
-                const float l = (lane == j) ? d * inv : (lane > j ? r[0] * inv : 0.f);
-                float* cb = sCol + (j & 1) * PI_BS;
-                if (lane > j) cb[lane - j - 1] = l;
-                __syncwarp();
-                sA[(j0 + lane) * PI_LD + j0 + j] = l;   // rows above j write their zero upper element
+                const float sc = ub * (inv * inv);   // l_ij / l_jj
+                sA[(j0 + lane) * PI_LD + j0 + j] = (lane == j) ? d * inv : (lane > j ? u * inv : 0.f);
                 if (lane == j) sInv[j0 + j] = inv;
-                // a[i][j + m] -= l_ij l_(j+m)j; slots past the block read stale values and are never pivots
+                // a[i][j + m] -= (a_ij / a_jj) a_(j+m)j; slots past the block read stale values and are
+                // never pivots
 #pragma unroll
                 for (int q = 0; q < PI_BS / 4; ++q) {
                     const float4 c4 = reinterpret_cast<const float4*>(cb)[q];
                     const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {
-                        const int m = 4 * q + t + 1;
-                        if (m < PI_BS) r[m - 1] = fmaf(-l, cv[t], r[m]);
+                        const int m = 4 * q + t;
+                        if (m >= 1) r[m - 1] = fmaf(-sc, cv[t], r[m]);
                     }
                 }
                 r[PI_BS - 1] = 0.f;
@@ -894,24 +910,20 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
             if (r >= c && r < n) A[r + (int64_t)c * lda] = sA[r * PI_LD + c];
         }
     }
-    for (int e = tid; e < PI_NB * PI_NB / 4; e += PI_THREADS) {   // float4 stores (64 KB-aligned blocks)
-        {   // column-major Linv: 4 rows of one column
-            const int r = (e % 32) * 4, c = e / 32;
-            float v[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) v[q] = (r + q < n && c < n) ? sX[(r + q) * PI_LD + c] : 0.f;
-            reinterpret_cast<float4*>(Linv)[e] = make_float4(v[0], v[1], v[2], v[3]);
-        }
-        {   // K-major rows: B[rr][cc] = Linv[rr][cc], 4 columns of one row
-            const int rr = e / 32, cc = (e % 32) * 4;
-            float h[4], w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                w[q] = (rr < n && cc + q < n) ? sX[rr * PI_LD + cc + q] : 0.f;
-                h[q] = __uint_as_float(__float_as_uint(w[q]) & 0xFFFFE000u);
-            }
-            reinterpret_cast<float4*>(Bh)[e] = make_float4(h[0], h[1], h[2], h[3]);
-            reinterpret_cast<float4*>(Bl)[e] = make_float4(w[0] - h[0], w[1] - h[1], w[2] - h[2], w[3] - h[3]);
+    // one element per thread and step, consecutive lanes on consecutive (bank-distinct) words of the
+    // padded rows and columns of X, 128-byte coalesced stores
+#pragma unroll 4
+    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // K-major rows: B[rr][cc] = Linv[rr][cc]
+        const int rr = e / PI_NB, cc = e % PI_NB;
+        const float w = (rr < n && cc < n) ? sX[rr * PI_LD + cc] : 0.f;
+        const float h = __uint_as_float(__float_as_uint(w) & 0xFFFFE000u);
+        Bh[e] = h;
+        Bl[e] = w - h;
+    }
+    if (Linv) {
+        for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // column-major Linv
+            const int r = e % PI_NB, c = e / PI_NB;
+            Linv[e] = (r < n && c < n) ? sX[r * PI_LD + c] : 0.f;
         }
     }
 }
@@ -929,6 +941,40 @@ void potrf_inv(float* A, int64_t lda, int n, int* err, int64_t* err_col, int64_t
     launch_maybe_pdl(pdl, potrf_inv_kernel, 1, PI_THREADS, sm, s, A, lda, n, err, err_col, col_offset, Linv, Bh, Bl,
                      store_l ? 1 : 0);
     check("potrf_inv");
+}
+
+// The diagonal-block inverses from their K-major splits (block b: heads at
+// B + 2 b 128^2, remainders 128^2 further, row-major 128 x 128): Linv
+// column-major (ld 128, block b at b 128^2) and its split as stored, LCh / LCl
+// (the same layout).  head + remainder is exactly the FP32 value, so Linv is
+// bit-identical to the inverse the diagonal-block kernel computed.  One 32 x 32
+// tile per CTA, transposed through shared memory.
+__global__ void linv_from_split_kernel(const float* __restrict__ B, float* __restrict__ Linv, float* __restrict__ LCh,
+                                       float* __restrict__ LCl) {
+    __shared__ float th[32][33], tl[32][33];
+    const int64_t blk = (int64_t)blockIdx.x * PI_NB * PI_NB;
+    const float* Bh = B + 2 * blk;
+    const float* Bl = Bh + PI_NB * PI_NB;
+    const int r0 = 32 * blockIdx.y, c0 = 32 * blockIdx.z, x = threadIdx.x;
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {   // rows r0 + y, columns c0 + x of the inverse
+        th[y][x] = Bh[(r0 + y) * PI_NB + c0 + x];
+        tl[y][x] = Bl[(r0 + y) * PI_NB + c0 + x];
+    }
+    __syncthreads();
+    for (int y = threadIdx.y; y < 32; y += blockDim.y) {   // column c0 + y, rows r0 + x
+        const float h = th[x][y], l = tl[x][y];
+        const int64_t o = blk + (int64_t)(c0 + y) * PI_NB + r0 + x;
+        Linv[o] = h + l;
+        LCh[o] = h;
+        LCl[o] = l;
+    }
+}
+
+void linv_from_split(int64_t nblocks, const float* B, float* Linv, float* LCh, float* LCl, cudaStream_t s) {
+    if (nblocks <= 0) return;
+    ProfScope prof_("linv_from_split", s);
+    linv_from_split_kernel<<<dim3((unsigned)nblocks, PI_NB / 32, PI_NB / 32), dim3(32, 8), 0, s>>>(B, Linv, LCh, LCl);
+    check("linv_from_split");
 }
 
 // Symmetric update of an n x n (n <= 128) diagonal block by up to two panels
