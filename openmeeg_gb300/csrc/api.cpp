@@ -119,6 +119,8 @@ void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float
                       const float* A2l, int64_t lda2, const float* B2h, const float* B2l, int64_t ldb2, float beta,
                       float* C, int64_t ldc, bool lower, int* err, cudaStream_t s, const char* prof_name,
                       int max_ctas, float* Sh, float* Sl, int64_t s_row0, int s_kpad, bool pdl = false);
+void gemm_tf32x3_grouped(const GemmOperand ops[8], const std::vector<GemmProduct>& prods, float alpha, int* err,
+                         cudaStream_t s, const char* prof_name, bool pdl = false);
 void split_panel_kmajor(int64_t m, int nk, int kpad, const float* P, int64_t ld, float* H, float* L,
                         cudaStream_t s);
 void split_cols(int nk, int64_t ncol, int kpad, const float* X, int64_t ldx, float* H, float* L, cudaStream_t s);
@@ -789,8 +791,36 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     float* LCh = LC.as<float>();
     float* LCl = LCh + nblocks * nb * nb;
     linv_from_split((int64_t)nblocks, Bi.as<float>(), sv->Linv32.as<float>(), LCh, LCl, s);
-    // the panel folds on the main stream, the block-row folds on the second one: disjoint memory, and each
-    // product is a few latency-bound waves, so two at a time fill the GPU
+    if (!std::getenv("OMG_FOLD_SEPARATE")) {
+        // all the folds as one grouped persistent launch (each product alone is a few latency-bound waves of
+        // K = 128 tiles): the panel folds read Linv_b's split (LC) and W, the block-row folds Linv_b's K-major
+        // split (Bi) and the columns of the head / remainder matrices at K offset k0
+        const int64_t w_rows = sv->w_off[nblocks] / nb;
+        const GemmOperand ops[8] = {{LCh, (int64_t)nblocks * nb, nb, nb},
+                                    {LCl, (int64_t)nblocks * nb, nb, nb},
+                                    {sv->W.as<float>(), w_rows, nb, nb},
+                                    {sv->W.as<float>(), w_rows, nb, nb},
+                                    {Bi.as<float>(), 2 * (int64_t)nblocks * nb, nb, nb},
+                                    {Bi.as<float>(), 2 * (int64_t)nblocks * nb, nb, nb},
+                                    {A, N, N, ld},
+                                    {Ar, N, N, ld}};
+        std::vector<GemmProduct> prods;
+        prods.reserve(2 * nblocks);
+        for (size_t b = 0; b < nblocks; ++b) {
+            const int64_t k0 = sv->bounds[b], k1 = sv->bounds[b + 1], nk = k1 - k0, m = N - k1;
+            const int64_t wr = sv->w_off[b] / nb;
+            if (m > 0)   // W_b <- L21_b Linv_b
+                prods.push_back(GemmProduct{wh(b), wl(b), nb, nk, m, nk, 0, (int64_t)b * nb, (int64_t)b * nb, wr,
+                                            wr + m, 0, 0});
+            if (k0 > 0)   // block row b <- Linv_b x block row b
+                prods.push_back(GemmProduct{A + k0, Ar + k0, ld, nk, k0, nk, 1, 2 * (int64_t)b * nb,
+                                            (2 * (int64_t)b + 1) * nb, 0, 0, 0, k0});
+        }
+        gemm_tf32x3_grouped(ops, prods, 1.f, sv->ctx->d_err, s, "fold", true);
+        return;
+    }
+    // one launch per product (OMG_FOLD_SEPARATE=1; the grouped launch is tested against it): the panel folds
+    // on the main stream, the block-row folds on the second one
     OMG_CUDA(cudaEventRecord(ev_l, s));
     OMG_CUDA(cudaStreamWaitEvent(s2, ev_l, 0));
     for (size_t b = 0; b < nblocks; ++b) {

@@ -690,8 +690,8 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 // zero above the diagonal and beyond n).  The factorization leaves Linv null
 // and transposes all the blocks' splits at its end (linv_from_split): the
 // chain of diagonal blocks then stores 128 KB per block instead of 192 KB.
-// A pivot that is not positive is reported as OMG_ERR_NOT_DEFINITE at its
-// column (and replaced by 1 so the kernel ends).
+// A pivot that is not a positive normal FP32 number is reported as
+// OMG_ERR_NOT_DEFINITE at its column (and replaced by 1 so the kernel ends).
 // ---------------------------------------------------------------------------
 constexpr int PI_NB = 128, PI_LD = 129, PI_THREADS = 512, PI_BS = 32, PI_TLD = 33;
 constexpr size_t PI_SMEM =
@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
             float r[PI_BS];
 #pragma unroll
             for (int m = 0; m < PI_BS; ++m) r[m] = (m <= lane) ? sA[(j0 + lane) * PI_LD + j0 + m] : 0.f;
-            int bad = -1;
+            unsigned badmask = 0u;   // a bit per pivot that is not a positive normal number
 #pragma unroll 1
             for (int j = 0; j < PI_BS; ++j) {
                 const float u = r[0];   // a_(lane)j after the updates by the columns before j
@@ -801,11 +801,12 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
                 if (lane >= j) cb[lane - j] = u;
                 float d = __shfl_sync(FULL, u, j);
                 __syncwarp();
-                if (!(d > 0.f)) {
-                    if (bad < 0) bad = j;
-                    d = 1.f;
-                }
-                const float inv = rsqrtf(d);
+                // branch-free (a branch here doubled the step's latency); NaN fails the test too
+                const bool ok = d >= 1.17549435e-38f;
+                badmask |= ok ? 0u : (1u << j);
+                d = ok ? d : 1.f;
+                float inv;   // 1 / sqrt(d), the PTX approximation (relative error below 2^-22)
+                asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(d));
                 const float sc = ub * (inv * inv);   // l_ij / l_jj
                 sA[(j0 + lane) * PI_LD + j0 + j] = (lane == j) ? d * inv : (lane > j ? u * inv : 0.f);
                 if (lane == j) sInv[j0 + j] = inv;
@@ -823,8 +824,8 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
                 }
                 r[PI_BS - 1] = 0.f;
             }
-            if (bad >= 0 && lane == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
-                *err_col = col_offset + j0 + bad;
+            if (badmask && lane == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
+                *err_col = col_offset + j0 + (__ffs((int)badmask) - 1);
         } else if (J > 0) {   // ---- 1'. meanwhile T_JK = sum_{M=K}^{J-1} L_JM X_MK for K < J (inverse, block row J)
             for (int t = tid - 32; t < J * 64; t += PI_THREADS - 32) pi_inv_rowblock_t(sA, sX, sT, J, t);
         }

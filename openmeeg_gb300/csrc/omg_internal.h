@@ -197,4 +197,22 @@ struct ProfScope {
     }
 };
 
+// Grouped tensor-core products (tc_gemm.cu, gemm_tf32x3_grouped).  An operand
+// map: K-major FP32 rows (`rows` rows of `kext` elements, row stride `ld`).
+struct GemmOperand {
+    const float* base;
+    int64_t rows, kext, ld;
+};
+// One product C (M x N, column-major, ldc) = alpha A B^T with K-extent K:
+// heads into C, remainders into Cr; A and B read through operand maps
+// 4 set .. 4 set + 3 (Ah, Al, Bh, Bl) at rows ay_h / ay_l / by_h / by_l and
+// K offsets ax / bx (multiples of 4).
+struct GemmProduct {
+    float* C;
+    float* Cr;
+    int64_t ldc, M, N, K;
+    int set;
+    int64_t ay_h, ay_l, by_h, by_l, ax, bx;
+};
+
 }  // namespace omg

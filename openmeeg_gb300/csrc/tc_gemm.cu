@@ -23,7 +23,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <climits>
+#include <memory>
 #include <mutex>
+#include <vector>
 
 #include "device_common.cuh"
 #include "omg_internal.h"
@@ -84,15 +87,86 @@ struct EpiArgs {
     int s_row0, s_kpad, x_row0;
 };
 
+// Grouped launch: independent products C_p (M_p x N_p, ldc_p) = alpha A_p B_p^T,
+// written as TF32 heads (C_p) and remainders (Cr_p), walked as one list of
+// tiles by one persistent launch.  The operand tiles of product p are read
+// through the first (set 0) or second (set 1) group of tensor maps at row
+// coordinates ay_h / ay_l (A heads / remainders, + 128 tm) and by_h / by_l
+// (B, + 128 tn), K coordinates ax / bx (+ 32 per chunk).  Rows past M_p or N_p
+// read whatever the map holds there (zero past its extent); they only feed
+// accumulator rows and columns that are not written.
+constexpr int MAX_GROUP = 320;
+struct GroupEntry {
+    float* C;
+    float* Cr;
+    int ldc, M, N, K, set;
+    int ay_h, ay_l, by_h, by_l, ax, bx;
+    int tile0;   // first tile of this product in the walk
+};
+template <bool G>
+struct GroupParam {   // empty for the single-product kernel
+    int n;
+};
+template <>
+struct GroupParam<true> {
+    int n;
+    GroupEntry g[MAX_GROUP];
+};
+
+// The tile a role works on: position, K chunks, output.
+struct TileJob {
+    int tm, tn, nk, M, N, ldc, p;
+    float* C;
+    float* Cr;
+};
+
+template <bool G>
+__device__ __forceinline__ TileJob tile_job(int64_t t, const GroupParam<G>& gp, int tiles_m, int lower, int M, int N,
+                                            int nk, float* C, int64_t ldc, float* Cr) {
+    TileJob j;
+    if constexpr (G) {
+        int lo = 0, hi = gp.n - 1;   // last product whose first tile is <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (gp.g[mid].tile0 <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const GroupEntry& e = gp.g[lo];
+        const int tmz = (e.M + BM - 1) / BM, loc = (int)(t - e.tile0);
+        j.tm = loc % tmz;
+        j.tn = loc / tmz;
+        j.nk = (e.K + BK - 1) / BK;
+        j.M = e.M;
+        j.N = e.N;
+        j.ldc = e.ldc;
+        j.C = e.C;
+        j.Cr = e.Cr;
+        j.p = lo;
+    } else {
+        tile_of(t, tiles_m, lower, j.tm, j.tn);
+        j.nk = nk;
+        j.M = M;
+        j.N = N;
+        j.ldc = (int)ldc;
+        j.C = C;
+        j.Cr = Cr;
+        j.p = 0;
+    }
+    return j;
+}
+
 // K may come in two segments with their own operand maps (the second set is
 // used for the chunks past K0 when K > K0): an update by two panels at once.
+template <bool G>
 __global__ void __launch_bounds__(THREADS, 1)
     gemm_tf32x3_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
                        const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl,
                        const __grid_constant__ CUtensorMap tAh2, const __grid_constant__ CUtensorMap tAl2,
                        const __grid_constant__ CUtensorMap tBh2, const __grid_constant__ CUtensorMap tBl2, int M,
                        int N, int K, int K0, float alpha, float beta, float* C, int64_t ldc, int lower, int nprod,
-                       int64_t ntiles, int* err, const EpiArgs ep) {
+                       int64_t ntiles, int* err, const EpiArgs ep, const __grid_constant__ GroupParam<G> gp) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
     __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], fin_bar;
@@ -147,23 +221,33 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {   // ---- TMA producer
             int64_t g = 0;
             for (int64_t t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
-                int tm, tn;
-                tile_of(t, tiles_m, lower, tm, tn);
-                for (int c = 0; c < nk; ++c, ++g) {
+                const TileJob tj = tile_job<G>(t, gp, tiles_m, lower, M, N, nk, C, ldc, ep.Cr);
+                const int tm = tj.tm, tn = tj.tn;
+                for (int c = 0; c < tj.nk; ++c, ++g) {
                     const int slot = (int)(g % STAGES);
                     if (!wait_or_abort(&empty_bar[slot], (uint32_t)(((g / STAGES) & 1) ^ 1), &s_abort)) {
                         s_abort = 1;
                         break;
                     }
                     const uint32_t st = sbase + slot * STAGE_BYTES;
-                    const bool seg2 = c >= nk0;
-                    const int x = (seg2 ? c - nk0 : c) * BK;
                     dev::mbar_expect_tx(&full_bar[slot], bytes_per_stage);
-                    tma_load_2d(st, seg2 ? &tAh2 : &tAh, x, tm * BM, &full_bar[slot]);
-                    tma_load_2d(st + 2 * TILE_BYTES, seg2 ? &tBh2 : &tBh, x, tn * BN, &full_bar[slot]);
-                    if (nprod == 3) {
-                        tma_load_2d(st + TILE_BYTES, seg2 ? &tAl2 : &tAl, x, tm * BM, &full_bar[slot]);
-                        tma_load_2d(st + 3 * TILE_BYTES, seg2 ? &tBl2 : &tBl, x, tn * BN, &full_bar[slot]);
+                    if constexpr (G) {
+                        const GroupEntry& e = gp.g[tj.p];
+                        const bool s2 = e.set != 0;
+                        const int xa = e.ax + c * BK, xb = e.bx + c * BK;
+                        tma_load_2d(st, s2 ? &tAh2 : &tAh, xa, e.ay_h + tm * BM, &full_bar[slot]);
+                        tma_load_2d(st + 2 * TILE_BYTES, s2 ? &tBh2 : &tBh, xb, e.by_h + tn * BN, &full_bar[slot]);
+                        tma_load_2d(st + TILE_BYTES, s2 ? &tAl2 : &tAl, xa, e.ay_l + tm * BM, &full_bar[slot]);
+                        tma_load_2d(st + 3 * TILE_BYTES, s2 ? &tBl2 : &tBl, xb, e.by_l + tn * BN, &full_bar[slot]);
+                    } else {
+                        const bool seg2 = c >= nk0;
+                        const int x = (seg2 ? c - nk0 : c) * BK;
+                        tma_load_2d(st, seg2 ? &tAh2 : &tAh, x, tm * BM, &full_bar[slot]);
+                        tma_load_2d(st + 2 * TILE_BYTES, seg2 ? &tBh2 : &tBh, x, tn * BN, &full_bar[slot]);
+                        if (nprod == 3) {
+                            tma_load_2d(st + TILE_BYTES, seg2 ? &tAl2 : &tAl, x, tm * BM, &full_bar[slot]);
+                            tma_load_2d(st + 3 * TILE_BYTES, seg2 ? &tBl2 : &tBl, x, tn * BN, &full_bar[slot]);
+                        }
                     }
                     s_issued = g + 1;
                 }
@@ -181,7 +265,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 fence_after();
                 const uint32_t acc = tmem + ab * BN;
-                for (int c = 0; c < nk; ++c, ++g) {
+                const int tnk = G ? tile_job<G>(t, gp, tiles_m, lower, M, N, nk, C, ldc, ep.Cr).nk : nk;
+                for (int c = 0; c < tnk; ++c, ++g) {
                     const int slot = (int)(g % STAGES);
                     if (!wait_or_abort(&full_bar[slot], (uint32_t)((g / STAGES) & 1), &s_abort)) {
                         ok = false;
@@ -215,16 +300,16 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int half = (warp - 2) / 4;
         int64_t lt = 0;
         for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
-            int tm, tn;
-            tile_of(t, tiles_m, lower, tm, tn);
+            const TileJob tj = tile_job<G>(t, gp, tiles_m, lower, M, N, nk, C, ldc, ep.Cr);
+            const int tm = tj.tm, tn = tj.tn, Mt = tj.M;
             const uint32_t ab = (uint32_t)(lt & 1), aph = (uint32_t)((lt >> 1) & 1);
             const int row = tm * BM + q * 32 + lane;
             const int n0 = tn * BN + half * 64;
             // columns n0 + j, j < jmax, are written by this thread (inside C, lower triangle when asked)
-            int jmax = row < M ? min(64, N - n0) : 0;
+            int jmax = row < Mt ? min(64, tj.N - n0) : 0;
             if (lower) jmax = min(jmax, row - n0 + 1);
-            float* const cp = C + ((int64_t)row + (int64_t)n0 * ldc);
-            const int ld32 = (int)ldc;   // 64 * ldc fits in 32 bits (host-checked)
+            const int ld32 = tj.ldc;   // 64 * ldc fits in 32 bits (host-checked)
+            float* const cp = tj.C + ((int64_t)row + (int64_t)n0 * ld32);
             // C of this tile into registers while its products run (independent loads, all in flight)
             float cv[64];
 #pragma unroll
@@ -239,7 +324,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             // optional K-major TF32 head / remainder copy of rows >= s_row0 (row stride s_kpad, zero past N)
             float* const sh =
                 (ep.Sh && row >= ep.s_row0 && row < M) ? ep.Sh + (int64_t)(row - ep.s_row0) * ep.s_kpad + n0 : nullptr;
-            float* const crp = ep.Cr ? ep.Cr + (cp - C) : nullptr;
+            float* const crp = tj.Cr ? tj.Cr + (cp - tj.C) : nullptr;
             // optional transposed copy of the band [x_row0, x_row0 + 128): column j -> row j
             const bool xband = ep.Xh && row >= ep.x_row0 && row < ep.x_row0 + BM;
             const int xmax = xband ? min(64, N - n0) : 0;
@@ -275,7 +360,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                     for (int j = 0; j < 16; ++j)
                         if (jb + j < xmax) {
-                            const float x = row < M ? v[j] : 0.f;
+                            const float x = row < Mt ? v[j] : 0.f;
                             const float h = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
                             xh[(int64_t)(jb + j) * BM] = h;
                             xl[(int64_t)(jb + j) * BM] = x - h;
@@ -336,10 +421,10 @@ static inline void check_tc(const char* what) {
 // Launch of the kernel; with `pdl` (programmatic dependent launch) it may be
 // scheduled while the previous kernel in the stream finishes: the kernel
 // waits for that kernel's completion before it touches memory.
-template <typename... Args>
+template <bool G = false, typename... Args>
 static void launch_gemm(bool pdl, unsigned grid, cudaStream_t s, Args... args) {
     if (!pdl) {
-        tc::gemm_tf32x3_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(args...);
+        tc::gemm_tf32x3_kernel<G><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(args...);
         return;
     }
     cudaLaunchConfig_t cfg = {};
@@ -352,7 +437,7 @@ static void launch_gemm(bool pdl, unsigned grid, cudaStream_t s, Args... args) {
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, tc::gemm_tf32x3_kernel, args...);
+    cudaLaunchKernelEx(&cfg, tc::gemm_tf32x3_kernel<G>, args...);
 }
 
 // Checks the optional epilogue outputs against the shape and packs them.
@@ -391,7 +476,8 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     static bool attr = false;
     static int n_sm = 0;
     if (!attr) {
-        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::SMEM_BYTES);
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
@@ -405,7 +491,7 @@ void gemm_tf32x3(int64_t M, int64_t N, int64_t K, float alpha, const float* Ah, 
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
     launch_gemm(pdl, grid, s, mAh, mAl, mBh, mBl, mAh, mAl, mBh, mBl, (int)M, (int)N, (int)K, (int)K, alpha, beta, C,
-                ldc, lower ? 1 : 0, nprod, ntiles, err, ep);
+                ldc, lower ? 1 : 0, nprod, ntiles, err, ep, tc::GroupParam<false>{0});
     check_tc("gemm_tf32x3");
 }
 
@@ -428,7 +514,8 @@ void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float
     static bool attr = false;
     static int n_sm = 0;
     if (!attr) {
-        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::SMEM_BYTES);
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
@@ -441,8 +528,63 @@ void gemm_tf32x3_pair(int64_t M, int64_t N, float alpha, int64_t K1, const float
     const int64_t ntiles = lower ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm);
     launch_gemm(pdl, grid, s, m1h, m1l, n1h, n1l, m2h, m2l, n2h, n2l, (int)M, (int)N, (int)(K1 + K2), (int)K1, alpha,
-                beta, C, ldc, lower ? 1 : 0, 3, ntiles, err, ep);
+                beta, C, ldc, lower ? 1 : 0, 3, ntiles, err, ep, tc::GroupParam<false>{0});
     check_tc("gemm_tf32x3");
+}
+
+// Independent products C_p = alpha A_p B_p^T (3xTF32, heads into C_p, remainders into Cr_p), all read through
+// two sets of four operand maps (Ah, Al, Bh, Bl: K-major FP32, `rows` rows of `kext` elements, row stride
+// `ld`) at the products' own coordinates; one persistent launch per MAX_GROUP products instead of one launch
+// per product.  Each product's tiles read only operand rows and write only outputs of their own (the caller
+// guarantees that products do not overlap in what they write nor write what another reads).
+void gemm_tf32x3_grouped(const GemmOperand ops[8], const std::vector<GemmProduct>& prods, float alpha, int* err,
+                         cudaStream_t s, const char* prof_name, bool pdl) {
+    if (prods.empty()) return;
+    ProfScope prof_(prof_name, s);
+    CUtensorMap maps[8];
+    for (int i = 0; i < 8; ++i) {
+        if (!ops[i].base || ops[i].rows <= 0 || ops[i].kext <= 0)
+            throw Error(OMG_ERR_INVALID, "grouped tensor-core GEMM: empty operand map");
+        if (ops[i].rows > INT32_MAX || ops[i].kext > INT32_MAX)
+            throw Error(OMG_ERR_UNSUPPORTED, "grouped tensor-core GEMM: operand too large for 32-bit coordinates");
+        maps[i] = tc::make_map(ops[i].base, ops[i].rows, ops[i].kext, ops[i].ld);
+    }
+    static bool attr = false;
+    static int n_sm = 0;
+    if (!attr) {
+        cudaFuncSetAttribute(tc::gemm_tf32x3_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc::SMEM_BYTES);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        if (n_sm <= 0) n_sm = 1;
+        attr = true;
+    }
+    auto gp = std::make_unique<tc::GroupParam<true>>();
+    for (size_t b0 = 0; b0 < prods.size(); b0 += tc::MAX_GROUP) {
+        const size_t b1 = std::min(prods.size(), b0 + (size_t)tc::MAX_GROUP);
+        int64_t ntiles = 0;
+        gp->n = 0;
+        for (size_t i = b0; i < b1; ++i) {
+            const GemmProduct& q = prods[i];
+            if (q.M <= 0 || q.N <= 0) continue;
+            if (q.K <= 0 || q.set < 0 || q.set > 1 || !q.C || !q.Cr || q.ldc <= 0 || q.ldc > (int64_t)(1 << 24) ||
+                q.ax % 4 || q.bx % 4 || q.ax < 0 || q.bx < 0 || q.ay_h < 0 || q.ay_l < 0 || q.by_h < 0 || q.by_l < 0)
+                throw Error(OMG_ERR_INVALID, "grouped tensor-core GEMM: bad product");
+            const int64_t t = ((q.M + tc::BM - 1) / tc::BM) * ((q.N + tc::BN - 1) / tc::BN);
+            if (ntiles + t > INT32_MAX) throw Error(OMG_ERR_UNSUPPORTED, "grouped tensor-core GEMM: too many tiles");
+            tc::GroupEntry& e = gp->g[gp->n++];
+            e = tc::GroupEntry{q.C,       q.Cr,      (int)q.ldc, (int)q.M,  (int)q.N,  (int)q.K,  q.set,
+                               (int)q.ay_h, (int)q.ay_l, (int)q.by_h, (int)q.by_l, (int)q.ax, (int)q.bx, (int)ntiles};
+            ntiles += t;
+        }
+        if (gp->n == 0) continue;
+        const unsigned grid = (unsigned)std::min<int64_t>(ntiles, n_sm);
+        const tc::EpiArgs ep{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0};
+        launch_gemm<true>(pdl, grid, s, maps[0], maps[1], maps[2], maps[3], maps[4], maps[5], maps[6], maps[7], 0, 0,
+                          0, 0, alpha, 0.f, (float*)nullptr, (int64_t)0, 0, 3, ntiles, err, ep, *gp);
+        check_tc("gemm_tf32x3_grouped");
+    }
 }
 
 // ---------------------------------------------------------------------------

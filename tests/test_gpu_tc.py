@@ -373,3 +373,23 @@ def test_persistent_sweep_solve(cuda, name, nrhs, monkeypatch):
     assert e_sweep <= 1e-6 and e_chain <= 1e-6, (e_sweep, e_chain)
     X2 = sv.solve(B).cpu().numpy()          # flags and counters are reset for every sweep
     assert np.array_equal(X, X2)
+
+
+@pytest.mark.parametrize("name", ["ico2", "config0"])
+def test_grouped_fold_matches_separate_launches(cuda, name, monkeypatch):
+    """The folds of the diagonal-block inverses into the solve operators
+    (W_b <- L21_b Linv_b and block row b <- Linv_b x block row b) run as one
+    grouped persistent launch; one launch per product (OMG_FOLD_SEPARATE=1)
+    computes every tile the same way, so the factors, and the solutions, are
+    bit-identical."""
+    from openmeeg_gb300 import api, workloads
+    w = workloads.small(2, layers=3, perturb=True) if name == "ico2" else workloads.config0()
+    geo = api.Geometry.from_head(w.head)
+    rng = np.random.default_rng(7)
+    B = rng.standard_normal((geo.size, 37))
+    X = api.Solver(geo, precision="mixed").solve(B).cpu().numpy()
+    monkeypatch.setenv("OMG_FOLD_SEPARATE", "1")
+    Xs = api.Solver(geo, precision="mixed").solve(B).cpu().numpy()
+    monkeypatch.delenv("OMG_FOLD_SEPARATE")
+    assert np.isfinite(X).all()
+    assert np.array_equal(X, Xs)
