@@ -386,27 +386,36 @@ __global__ void __launch_bounds__(DG_THREADS) digits_kernel(const double* __rest
     }
     __syncthreads();
     const int k = nd * beta - s_e;
-    // one rounding to the digit grid 2^-(nd beta), then balanced base-2^beta digits
-    // by integer arithmetic (|Y| <= 2^(nd beta) <= 2^62)
-    const long long half = 1ll << (beta - 1), mask = (1ll << beta) - 1;
+    // one rounding to the digit grid 2^-(nd beta), then balanced base-2^beta digits by integer
+    // arithmetic (|Y| <= 2^(nd beta) <= 2^62).  Taken one after the other, r = ((Y + h) & mask) - h,
+    // Y <- (Y - r) >> beta (h = 2^(beta-1)); by induction the i-th remainder is
+    // floor((Y + h sum_{j<i} 2^(beta j)) / 2^(beta i)), so with the bias Bs = h sum_{j<nd-1} 2^(beta j)
+    // (extra terms only add multiples of 2^beta to the shifted value) the digits carry nothing:
+    // digit i < nd-1 is ((Y + Bs) >> (beta i) & mask) - h and the top one (Y + Bs) >> (beta (nd-1)).
+    const long long half = 1ll << (beta - 1);
+    const unsigned mask = (1u << beta) - 1u;
+    long long Bs = 0;
+    for (int j = 0; j + 1 < nd; ++j) Bs += half << (beta * j);
+    const int bf_off = 0x4B400000 - (int)half;   // float bits of 1.5 * 2^23 + (field - h)
     for (int64_t j0 = 4 * threadIdx.x; j0 < ldo; j0 += 4 * DG_THREADS) {
-        long long Y[4];
+        long long Z[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const double x = j0 + u < n ? at(j0 + u) : 0.0;
-            Y[u] = j0 + u < n ? scaled_rn(x, k) : 0;
+            Z[u] = (j0 + u < n ? scaled_rn(x, k) : 0) + Bs;
             if (lower32 && j0 + u >= c && j0 + u < n) lower32[j0 + u + c * ld32] = (float)x;   // lower triangle
         }
         for (int d = nd - 1; d >= 0; --d) {
+            const int sh = beta * (nd - 1 - d);
             unsigned int h[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                long long r = Y[u];
-                if (d > 0) {
-                    r = ((Y[u] + half) & mask) - half;
-                    Y[u] = (Y[u] - r) >> beta;
+                if (d > 0) {   // bf16 of the digit: float(1.5 * 2^23 + digit) - 1.5 * 2^23, exact
+                    const unsigned field = (unsigned)(Z[u] >> sh) & mask;
+                    h[u] = __float_as_uint(__int_as_float(bf_off + (int)field) - 12582912.0f) >> 16;
+                } else {
+                    h[u] = small_int_bf16(Z[u] >> sh);
                 }
-                h[u] = small_int_bf16(r);
             }
             o2[(((int64_t)d * rows_per_plane + c) * ldo + j0) / 4] = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
         }
