@@ -675,13 +675,19 @@ void col_amax(int64_t m, int64_t n, const double* A, int64_t lda, double* out, c
 //   2. warp 0 inverts that block (lane c solves column c of X_JJ) while the
 //      threads of warps 1-3 solve one panel row each, L_rJ = A_rJ L_JJ^-T, by
 //      forward substitution (rows below the block);
-//   3. all threads apply the rank-32 update to the trailing lower triangle
-//      in 4 x 4 register tiles, reading the panel from a k-major copy;
+//   3. the rank-32 update of the trailing lower triangle in 4 x 4 register
+//      tiles, reading the panel from a k-major copy;
 // the off-diagonal blocks of the inverse, X_JK = -X_JJ sum_{M=K}^{J-1} L_JM
-// X_MK, are computed block row by block row inside the same loop: the sums
-// by warps 1-15 while warp 0 factors diagonal block J (step 1), the products
-// with X_JJ beside the trailing update (step 3).  The block lives in shared
-// memory (row-major, padded); columns past n act as the identity.
+// X_MK, are computed block row by block row inside the same loop.  With a
+// look-ahead, warp 0 factors block J+1 as soon as that block alone is
+// updated: warp 1's panel rows (those of block J+1) are handed to warps 4-15,
+// which update block J+1 beside the other panel rows and X_JJ; the rest of the
+// trailing update, block row J of the inverse and the sums of block row J+1
+// then run while warp 0 factors block J+1 (two named barriers), on the 12
+// warps outside warp 0's scheduler partition (sharing it, the factorization's
+// serial steps lost most of their issue slots and nothing was gained).
+// The block lives in shared memory (row-major, padded); columns past n act as
+// the identity.
 
 // Outputs: L11 over A11 (lower; left out when store_l is false: the
 // factorization's solves use only the inverse), Linv as TF32 head/remainder
@@ -752,6 +758,36 @@ __device__ __forceinline__ void pi_inv_rowblock_x(float* sX, const float* sT, in
         for (int j = 0; j < 4; ++j) sX[(r0 + i) * PI_LD + c0 + j] = -acc[i][j];
 }
 
+// One 4 x 4 tile t (lower triangle, row-major tile order) of the rank-32 update of the trailing lower
+// triangle from row and column b by the panel in sP (k-major): A_rc -= sum_k P_rk P_ck, r >= c.
+__device__ __forceinline__ void pi_trailing_tile(float* sA, const float* sP, int b, int t) {
+    int ti = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    while (ti * (ti + 1) / 2 > t) --ti;
+    const int tj = t - ti * (ti + 1) / 2;
+    const int r0 = b + 4 * ti, c0 = b + 4 * tj;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < PI_BS; ++k) {
+        const float4 a = *reinterpret_cast<const float4*>(sP + k * PI_NB + r0);
+        const float4 c = *reinterpret_cast<const float4*>(sP + k * PI_NB + c0);
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (c0 + j <= r0 + i) sA[(r0 + i) * PI_LD + c0 + j] -= acc[i][j];
+}
+
 __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int64_t lda, int n, int* err,
                                                                int64_t* err_col, int64_t col_offset, float* Linv,
                                                                float* Bh, float* Bl, int store_l) {
@@ -766,9 +802,13 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     asm volatile("griddepcontrol.launch_dependents;");
     asm volatile("griddepcontrol.wait;" ::: "memory");   // the block's last update (no-op without PDL)
-    // the lower triangle by 4-byte asynchronous copies (all of a thread's 32 in flight at once, no
-    // registers held), coalesced down the columns of A; identity beyond n, zero above the diagonal
-    for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {
+    // the lower triangle by 4-byte asynchronous copies (a thread's 32 in flight at once, no registers
+    // held), coalesced down the columns of A, in two groups: the first column block (all the first
+    // diagonal block needs) and the rest, which lands while warp 0 factors that block; identity beyond
+    // n, zero above the diagonal
+#pragma unroll 1
+    for (int i = 0; i < PI_NB * PI_NB / PI_THREADS; ++i) {
+        const int e = tid + i * PI_THREADS;
         const int r = e % PI_NB, c = e / PI_NB;
         float* dst = sA + r * PI_LD + c;
         if (r >= c && r < n) {   // c <= r < n
@@ -779,9 +819,18 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
             *dst = (r == c) ? 1.f : 0.f;
         }
         sX[r * PI_LD + c] = 0.f;
+        if (i == PI_BS * PI_NB / PI_THREADS - 1) asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 1;" ::: "memory");   // this thread's copies of the first column block
     __syncthreads();
+    // Look-ahead: each diagonal block is factored as soon as its own update is complete.
+    //   phase 1 (J): warp 0 factors diagonal block J; the warps of the other scheduler partitions apply
+    //                the rest of panel J-1's trailing update (rows past block J), finish block row J-1 of
+    //                the inverse and form the sums T_JK of block row J (named barrier 1 between the two)
+    //   phase 2 (J): warp 0 inverts L_JJ; warps 1-3 solve the panel rows; warp 1's rows (those of block
+    //                J+1) go first to warps 5 and 6, which update diagonal block J+1 by them (named
+    //                barrier 2)
     for (int J = 0; J < 4; ++J) {
         const int j0 = J * PI_BS;
         if (warp == 0) {   // ---- 1. Cholesky of the diagonal block
@@ -826,8 +875,23 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
             }
             if (badmask && lane == 0 && atomicCAS(err, 0, -3 /* OMG_ERR_NOT_DEFINITE */) == 0)
                 *err_col = col_offset + j0 + (__ffs((int)badmask) - 1);
-        } else if (J > 0) {   // ---- 1'. meanwhile T_JK = sum_{M=K}^{J-1} L_JM X_MK for K < J (inverse, block row J)
-            for (int t = tid - 32; t < J * 64; t += PI_THREADS - 32) pi_inv_rowblock_t(sA, sX, sT, J, t);
+            if (J == 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
+        } else if (J == 0) {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");   // the rest of the block
+        } else if (warp & 3) {
+            // helpers: the 12 warps outside warp 0's scheduler partition (warp w issues on partition w % 4),
+            // so the factorization's latency-bound steps keep their issue slots; warps 4, 8, 12 wait
+            const int ht = (warp - 1 - (warp >> 2)) * 32 + lane, nh = 12 * 32;
+            // ---- 3. the rest of panel J-1's trailing update: 4 x 4 tiles of its lower trailing triangle
+            // (from row and column j0) past the first 8 tile rows, which are diagonal block J (updated in
+            // phase 2 of J-1)
+            const int tm = (PI_NB - j0) / 4, ntiles = tm * (tm + 1) / 2;
+            for (int t = 36 + ht; t < ntiles; t += nh) pi_trailing_tile(sA, sP, j0, t);
+            if (J > 1)   // ---- 3'. X_(J-1)K = -X_(J-1)(J-1) T_(J-1)K, K < J-1
+                for (int t = ht; t < (J - 1) * 64; t += nh) pi_inv_rowblock_x(sX, sT, J - 1, t);
+            asm volatile("bar.sync 1, %0;" ::"n"(12 * 32) : "memory");   // the helpers
+            // ---- 1'. T_JK = sum_{M=K}^{J-1} L_JM X_MK for K < J (needs block row J-1 of the inverse)
+            for (int t = ht; t < J * 64; t += nh) pi_inv_rowblock_t(sA, sX, sT, J, t);
         }
         __syncthreads();
         const int below = PI_NB - j0 - PI_BS;
@@ -848,63 +912,43 @@ __global__ void __launch_bounds__(PI_THREADS, 1) potrf_inv_kernel(float* A, int6
             }
 #pragma unroll
             for (int r = 0; r < PI_BS; ++r) sX[(j0 + r) * PI_LD + j0 + lane] = x[r];
-        } else if (tid - 32 < below) {   // ---- 2b. one panel row: L_rJ L_JJ^T = A_rJ
-            const int r = j0 + PI_BS + (tid - 32);
-            float l[PI_BS];
+        } else if (warp < 4) {
+            if (tid - 32 < below) {   // ---- 2b. one panel row: L_rJ L_JJ^T = A_rJ
+                const int r = j0 + PI_BS + (tid - 32);
+                float l[PI_BS];
 #pragma unroll
-            for (int j = 0; j < PI_BS; ++j) {
-                const float* Lj = sA + (j0 + j) * PI_LD + j0;
-                float acc0 = sA[r * PI_LD + j0 + j], acc1 = 0.f;
+                for (int j = 0; j < PI_BS; ++j) {
+                    const float* Lj = sA + (j0 + j) * PI_LD + j0;
+                    float acc0 = sA[r * PI_LD + j0 + j], acc1 = 0.f;
 #pragma unroll
-                for (int k = 0; k < j; ++k) {
-                    if (k & 1)
-                        acc1 = fmaf(-l[k], Lj[k], acc1);
-                    else
-                        acc0 = fmaf(-l[k], Lj[k], acc0);
+                    for (int k = 0; k < j; ++k) {
+                        if (k & 1)
+                            acc1 = fmaf(-l[k], Lj[k], acc1);
+                        else
+                            acc0 = fmaf(-l[k], Lj[k], acc0);
+                    }
+                    l[j] = (acc0 + acc1) * sInv[j0 + j];
                 }
-                l[j] = (acc0 + acc1) * sInv[j0 + j];
-            }
 #pragma unroll
-            for (int j = 0; j < PI_BS; ++j) {
-                sA[r * PI_LD + j0 + j] = l[j];
-                sP[j * PI_NB + r] = l[j];
+                for (int j = 0; j < PI_BS; ++j) {
+                    sA[r * PI_LD + j0 + j] = l[j];
+                    sP[j * PI_NB + r] = l[j];
+                }
             }
+            if (warp == 1 && below > 0) {   // the rows of diagonal block J+1 are in
+                __threadfence_block();
+                asm volatile("bar.arrive 2, %0;" ::"n"(3 * 32) : "memory");   // warps 1, 5, 6
+            }
+        } else if ((warp == 5 || warp == 6) && below > 0) {
+            // ---- 3. diagonal block J+1 by panel J: the first 36 tiles of its trailing triangle (on
+            // partitions 1 and 2, beside warp 0's inverse of L_JJ)
+            asm volatile("bar.sync 2, %0;" ::"n"(3 * 32) : "memory");
+            for (int t = (warp - 5) * 32 + lane; t < 36; t += 64) pi_trailing_tile(sA, sP, j0 + PI_BS, t);
         }
         __syncthreads();
-        if (below > 0) {   // ---- 3. trailing update, lower 4 x 4 tiles
-            const int tm = below / 4, ntiles = tm * (tm + 1) / 2;
-            for (int t = tid; t < ntiles; t += PI_THREADS) {
-                int ti = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
-                while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-                while (ti * (ti + 1) / 2 > t) --ti;
-                const int tj = t - ti * (ti + 1) / 2;
-                const int r0 = j0 + PI_BS + 4 * ti, c0 = j0 + PI_BS + 4 * tj;
-                float acc[4][4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-#pragma unroll 8
-                for (int k = 0; k < PI_BS; ++k) {
-                    const float4 a = *reinterpret_cast<const float4*>(sP + k * PI_NB + r0);
-                    const float4 b = *reinterpret_cast<const float4*>(sP + k * PI_NB + c0);
-                    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-                }
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (c0 + j <= r0 + i) sA[(r0 + i) * PI_LD + c0 + j] -= acc[i][j];
-            }
-        }
-        if (J > 0)   // ---- 3'. X_JK = -X_JJ T_JK, K < J (disjoint from the trailing update)
-            for (int t = tid; t < J * 64; t += PI_THREADS) pi_inv_rowblock_x(sX, sT, J, t);
-        if (below > 0 || J > 0) __syncthreads();
     }
+    for (int t = tid; t < 3 * 64; t += PI_THREADS) pi_inv_rowblock_x(sX, sT, 3, t);   // X_3K = -X_33 T_3K
+    __syncthreads();
     if (store_l) {
         for (int e = tid; e < PI_NB * PI_NB; e += PI_THREADS) {   // no division by the runtime size
             const int r = e % PI_NB, c = e / PI_NB;
