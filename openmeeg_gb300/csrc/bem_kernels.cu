@@ -737,16 +737,18 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
     const float* g1 = grec + (t1b + i) * GREC;
     const double* c1p = reinterpret_cast<const double*>(g1);
     const double c1x = c1p[0], c1y = c1p[1], c1z = c1p[2];
-    // the 16 points of t1 in packed pairs (even p in the low lane, odd p in the high lane): the inner
-    // products run two point pairs per FP32x2 instruction
-    f2 P1x[8], P1y[8], P1z[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        P1x[k] = pk2(g1[6 + 6 * k], g1[9 + 6 * k]);
-        P1y[k] = pk2(g1[7 + 6 * k], g1[10 + 6 * k]);
-        P1z[k] = pk2(g1[8 + 6 * k], g1[11 + 6 * k]);
-    }
     const f2* W = reinterpret_cast<const f2*>(c_w16);   // weight pairs, read from the constant bank
+    // t1's 7 points, packed (0,1) (2,3) (4,5) (6,6) (the last pair's second lane has a zero weight), held
+    // across the loop: most pairs take the 7-point rule
+    f2 Px[4], Py[4], Pz[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float* p7 = g1 + GREC_P7;
+        const int u = 2 * k, v = 2 * k + 1 < 7 ? 2 * k + 1 : 6;
+        Px[k] = pk2(p7[3 * u], p7[3 * v]);
+        Py[k] = pk2(p7[3 * u + 1], p7[3 * v + 1]);
+        Pz[k] = pk2(p7[3 * u + 2], p7[3 * v + 2]);
+    }
     const float n1x = g1[54], n1y = g1[55], n1z = g1[56], h1 = g1[57];
     const double A1 = reinterpret_cast<const double*>(g1 + 58)[0];
     for (int jj = 0; jj < nj; ++jj) {
@@ -772,17 +774,11 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
         const f2 DN2 = pk2(dn2, dn2), N2x = pk2(n2x, n2x), N2y = pk2(n2y, n2y), N2z = pk2(n2z, n2z);
         float s = 0.f, e0 = 0.f, e1 = 0.f, e2 = 0.f, u0 = 0.f, u1 = 0.f, u2 = 0.f;   // u: D21
         if (dist2 >= kFarTier7 * hmax * hmax) {
-            // well separated (>= 6 max edges): the 7 x 7 product rule, within 1e-7 of the 16 x 16 one there;
-            // t1's 7 points from its record (L1), packed (0,1) (2,3) (4,5) (6,6) with a zero weight on the last lane
+            // well separated (>= 6 max edges): the 7 x 7 product rule, within 1e-7 of the 16 x 16 one there
             const f2* W7 = reinterpret_cast<const f2*>(c_w7);
-            const float* p7 = g1 + GREC_P7;
-            f2 Px[4], Py[4], Pz[4], WD7[4], A7[4];
+            f2 WD7[4], A7[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const int u = 2 * k, v = 2 * k + 1 < 7 ? 2 * k + 1 : 6;
-                Px[k] = pk2(p7[3 * u], p7[3 * v]);
-                Py[k] = pk2(p7[3 * u + 1], p7[3 * v + 1]);
-                Pz[k] = pk2(p7[3 * u + 2], p7[3 * v + 2]);
                 WD7[k] = mul2(W7[k], sub2(DN2, fma2(Px[k], N2x, fma2(Py[k], N2y, mul2(Pz[k], N2z)))));
                 A7[k] = pk2(0.f, 0.f);
             }
@@ -821,7 +817,16 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
                 }
             }
         } else {
-            f2 WD[8], A21[8];
+            // the 16 points of t1 in packed pairs (even p in the low lane, odd p in the high lane; the inner
+            // products run two point pairs per FP32x2 instruction), loaded (L1) for the few pairs of this tier
+            // instead of held across the loop: the registers go to more resident warps
+            f2 P1x[8], P1y[8], P1z[8], WD[8], A21[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                P1x[k] = pk2(g1[6 + 6 * k], g1[9 + 6 * k]);
+                P1y[k] = pk2(g1[7 + 6 * k], g1[10 + 6 * k]);
+                P1z[k] = pk2(g1[8 + 6 * k], g1[11 + 6 * k]);
+            }
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 WD[k] = mul2(W[k], sub2(DN2, fma2(P1x[k], N2x, fma2(P1y[k], N2y, mul2(P1z[k], N2z)))));
