@@ -605,8 +605,9 @@ void launch_from_reference_dense(const DevGeom& g, const double* in, int64_t ldi
 // distances are shared.  Near pairs are appended to a list and recomputed
 // with the FP64 analytic kernels.
 // ===========================================================================
-// floats per triangle: centroid (3 doubles), 16-point offsets, normal, h, area (double), 7-point offsets
-constexpr int GREC = kFarRecFloats, GREC_P7 = 64;
+// floats per triangle: centroid (3 doubles), 16-point offsets, normal, h, area (double), 7-point offsets,
+// area (FP32)
+constexpr int GREC = kFarRecFloats, GREC_P7 = 64, GREC_AF = GREC_P7 + 21;
 // The 16-point rule of c_rules[3] rounded to FP32 (weights, barycentric nodes).
 __constant__ __align__(8) float c_w16[16] = {0.144315607677786f, 0.095091634267284f, 0.095091634267284f, 0.095091634267284f, 0.032458497623198f, 0.032458497623198f, 0.032458497623198f, 0.103217370534718f, 0.103217370534718f, 0.103217370534718f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f, 0.027230314174434f};
 __constant__ float c_b16[16][3] = {
@@ -664,7 +665,8 @@ __global__ void prepare_gg_kernel(int64_t nt, const double* __restrict__ V, cons
         const d3 v = bary_point(c_rules[2][k], p0, p1, p2) - c;
         g[GREC_P7 + 3 * k] = (float)v.x; g[GREC_P7 + 3 * k + 1] = (float)v.y; g[GREC_P7 + 3 * k + 2] = (float)v.z;
     }
-    for (int k = GREC_P7 + 21; k < GREC; ++k) g[k] = 0.f;
+    g[GREC_AF] = (float)(0.5 * nrm);
+    for (int k = GREC_AF + 1; k < GREC; ++k) g[k] = 0.f;
 }
 
 void launch_prepare_gg(const DevGeom& g, float* grec, cudaStream_t s) {
@@ -750,21 +752,21 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
         Pz[k] = pk2(p7[3 * u + 2], p7[3 * v + 2]);
     }
     const float n1x = g1[54], n1y = g1[55], n1z = g1[56], h1 = g1[57];
-    const double A1 = reinterpret_cast<const double*>(g1 + 58)[0];
+    const float A1f = g1[GREC_AF], cSf = (float)cS;
     for (int jj = 0; jj < nj; ++jj) {
         const int64_t j = j0 + jj;
         if (same && j < i) continue;
         const float* g2 = sJ + jj * GREC;
         const double* c2p = reinterpret_cast<const double*>(g2);
-        const double dx = c2p[0] - c1x, dy = c2p[1] - c1y, dz = c2p[2] - c1z;
+        // the centroid difference in FP64 (no cancellation), rounded once; the rest of the pair in FP32
+        const float fx = (float)(c2p[0] - c1x), fy = (float)(c2p[1] - c1y), fz = (float)(c2p[2] - c1z);
         const float hmax = fmaxf(h1, g2[57]);
-        const float dist2 = (float)(dx * dx + dy * dy + dz * dz);
+        const float dist2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
         if (dist2 < rho * rho * hmax * hmax) {
             const int slot = atomicAdd(near_count, 1);
             if (slot < near_cap) near[slot] = make_int2((int)i, (int)j);
             continue;
         }
-        const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
         const float n2x = g2[54], n2y = g2[55], n2z = g2[56];
         // r = d + Q_q - P_k (d: centroid difference, P_k / Q_q: the points' offsets in the planes of t1 / t2,
         // so P_k . n1 = Q_q . n2 = 0): r . n2 = d . n2 - P_k . n2 depends on k only and r . n1 = d . n1 + Q_q . n1
@@ -865,22 +867,23 @@ __global__ void __launch_bounds__(FF_TI, 3) ff_block_kernel(const float* __restr
                 }
             }
         }
-        const double AA = A1 * reinterpret_cast<const double*>(g2 + 58)[0];
+        // the sums are FP32: scaled by the area product in FP32, widened once each
+        const float AA = A1f * g2[GREC_AF];
         if (wantS) {
             if (hm)
-                hm[lower_at(tpos[t1b + i], tpos[t2b + j], ld)] = (double)s * AA * cS;
+                hm[lower_at(tpos[t1b + i], tpos[t2b + j], ld)] = (double)(s * (AA * cSf));
             else {
-                stmp[i * n2 + j] = (double)s * AA;
-                if (same) stmp[j * n2 + i] = (double)s * AA;
+                stmp[i * n2 + j] = (double)(s * AA);
+                if (same) stmp[j * n2 + i] = (double)(s * AA);
             }
         }
         if (wantD12) {
             double* o = d12 + (i * n2 + j) * 3;
-            o[0] = (double)e0 * AA; o[1] = (double)e1 * AA; o[2] = (double)e2 * AA;
+            o[0] = (double)(e0 * AA); o[1] = (double)(e1 * AA); o[2] = (double)(e2 * AA);
         }
         if (wantD21 || (same && wantD12)) {
             double* o = same ? d12 + (j * n2 + i) * 3 : d21 + (j * n1 + i) * 3;
-            o[0] = (double)u0 * AA; o[1] = (double)u1 * AA; o[2] = (double)u2 * AA;
+            o[0] = (double)(u0 * AA); o[1] = (double)(u1 * AA); o[2] = (double)(u2 * AA);
         }
     }
 }
