@@ -717,7 +717,7 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
     return d;
 }
 
-constexpr int FF_TI = 128, FF_TJ = 32;
+constexpr int FF_TI = 128, FF_TJ = 16;
 constexpr float kFarTier7 = 36.f;   // squared: pairs at >= 6 max edges take the 7-point rule
 
 // One thread per t1 row, looping over the CTA's FF_TJ staged t2 records.
