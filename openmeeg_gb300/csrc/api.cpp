@@ -146,7 +146,7 @@ void digit_gemm(int64_t n, int64_t k, int64_t kdim, const void* Ad, int nda, con
 size_t sweep_scratch_bytes(int64_t nblocks, int64_t nrhs);
 void solve_sweep_tc(bool backward, int64_t N, int64_t nblocks, const float* W, int64_t w_rows, const float* A,
                     const float* Ar, int64_t ld, float* B, int64_t ldb, int64_t nrhs, void* scratch, int* err,
-                    cudaStream_t s);
+                    cudaStream_t s, int max_ctas = 0);
 void residual_slices(int64_t n, int64_t k, const void* Ad, int nda, const int* rexp, const void* Xd, int ndx,
                      int64_t kpad, const int* cexp, int beta, int lmax, const double* B, int64_t ldb, double* R,
                      int64_t ldr, int* err, cudaStream_t s);
@@ -863,10 +863,11 @@ static void solve_ldlt_tc(omg_solver sv, float* B, int64_t ldb, int64_t nrhs) {
         // tensor-core update per block below (kept as the reference the sweep is tested against)
         DevBuf scratch(sweep_scratch_bytes((int64_t)nblocks, nrhs), s);
         solve_sweep_tc(false, N, (int64_t)nblocks, sv->W.as<float>(), sv->w_off[nblocks] / nb, nullptr, nullptr, 0, B,
-                       ldb, nrhs, scratch.p, sv->ctx->d_err, s);
+                       ldb, nrhs, scratch.p, sv->ctx->d_err, s, sv->sweep_ctas);
         apply_inv_blocks((int64_t)nblocks, nb, n_last, nrhs, sv->Linv32.as<float>(), false, B, ldb, s);
         negate_rows<float>(B, ldb, sv->nP, N, nrhs, s);
-        solve_sweep_tc(true, N, (int64_t)nblocks, nullptr, 0, A, Ar, ld, B, ldb, nrhs, scratch.p, sv->ctx->d_err, s);
+        solve_sweep_tc(true, N, (int64_t)nblocks, nullptr, 0, A, Ar, ld, B, ldb, nrhs, scratch.p, sv->ctx->d_err, s,
+                       sv->sweep_ctas);
         apply_inv_blocks((int64_t)nblocks, nb, n_last, nrhs, sv->Linv32.as<float>(), true, B, ldb, s);
         return;
     }
@@ -2277,6 +2278,9 @@ static void gain_pipeline(omg_context ctx, omg_geometry geo, int precision, cons
     OMG_CUDA(cudaStreamWaitEvent(s, ev[6], 0));
     OMG_CUDA(cudaEventRecord(ev[2], s));
     sv->rebuild = [geo, hm_it, precision] { return assemble_system(geo, hm_it, precision, false); };
+    // the sources run beside the solves: the sweeps take five eighths of the SMs (config1, solves +
+    // sources: 96 CTAs 12.2 ms, 152 CTAs 12.6 ms, 64 CTAs 12.3 ms, 48 CTAs 13.8 ms)
+    sv->sweep_ctas = std::max(1, n_sm() * 5 / 8);
     solver_factor_or_pivot(sv.get(), std::move(hm), sv->rebuild);
     OMG_CUDA(cudaEventRecord(ev[3], s));
     {   // after the factorization's last work on the second stream (stream order); every stage of the

@@ -41,6 +41,7 @@ struct omg_solver_s {
     int last_steps = 0;
     double last_residual = 0.0;
     double last_correction = 0.0;
+    int sweep_ctas = 0;                     // mixed: CTAs of a persistent sweep (0: one per SM)
     // pivoted fallback: the quasi-definite LDL^T met a pivot of the wrong sign, so A64 holds the FP64 LU
     // factors with partial pivoting of the whole matrix (any nonsingular matrix, as the reference's
     // Bunch-Kaufman DSPTRF) and perm its row order

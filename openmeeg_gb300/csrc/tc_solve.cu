@@ -328,7 +328,7 @@ size_t sweep_scratch_bytes(int64_t nblocks, int64_t nrhs) {
 // column-major.  `scratch` holds sweep_scratch_bytes(nblocks, nrhs) bytes.
 void solve_sweep_tc(bool backward, int64_t N, int64_t nblocks, const float* W, int64_t w_rows, const float* A,
                     const float* Ar, int64_t ld, float* B, int64_t ldb, int64_t nrhs, void* scratch, int* err,
-                    cudaStream_t s) {
+                    cudaStream_t s, int max_ctas) {
     if (nrhs <= 0 || N <= 0) return;
     if (N > (int64_t)INT32_MAX / 2 || nblocks * tcs::BM < N || (nblocks - 1) * tcs::BM >= N)
         throw Error(OMG_ERR_INVALID, "solve sweep: blocks do not cover the rows");
@@ -366,7 +366,9 @@ void solve_sweep_tc(bool backward, int64_t N, int64_t nblocks, const float* W, i
     }
     tcs::SweepArgs args{backward ? 1 : 0, (int)nblocks, (int)N, (int)nrhs, (int)ncg, (int)ncolpad, B, ldb, XSh, XSl,
                         flags, counter, err};
-    const unsigned grid = (unsigned)std::min<int64_t>(nblocks * ncg, n_sm);
+    // max_ctas > 0 leaves SMs to work on another stream: most CTAs of a sweep wait on the block chain
+    const int cap = max_ctas > 0 ? std::min(max_ctas, n_sm) : n_sm;
+    const unsigned grid = (unsigned)std::min<int64_t>(nblocks * ncg, cap);
     tcs::sweep_kernel<<<grid, tcs::THREADS, tcs::SMEM_BYTES, s>>>(mAh, mAl, mXh, mXl, args);
     check_tcs("solve sweep");
 }
