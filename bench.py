@@ -557,13 +557,22 @@ def run_gpu(args):
     err_eeg = relerr(gex, ge64)
     err_meg = relerr(gmx, gm64) if gm64 is not None else None
 
-    # end to end through the C ABI with host buffers: geometry from host arrays + gain_host
+    # end to end through the C ABI with host buffers: geometry from host arrays + gain_host, the sources and
+    # the gains in pinned host memory
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        t[...] = a
+        return t
+    dip_h = pinned(np.ascontiguousarray(np.asarray(w.dipoles, np.float64)[:, :6]))
+    el_h = pinned(np.ascontiguousarray(np.asarray(w.electrodes, np.float64)[:, :3]))
+    sq_h = pinned(np.ascontiguousarray(np.asarray(w.squids, np.float64)[:, :6])) if nm else None
+    out_h = (pinned(np.zeros((nd, ne))), pinned(np.zeros((nd, nm))))
     e2e_times = []
     for _ in range(max(1, args.e2e_steps)):
         torch.cuda.synchronize()
         s = time.perf_counter()
         g2 = api.Geometry.from_head(w.head, ctx)
-        api.forward_gain(g2, w.dipoles, w.electrodes, w.squids if nm else None, precision="mixed", host=True)
+        api.forward_gain(g2, dip_h, el_h, sq_h, precision="mixed", host=True, out=out_h)
         e2e_times.append(time.perf_counter() - s)
         del g2
     t_e2e = float(np.median(e2e_times))
@@ -622,7 +631,8 @@ def run_gpu(args):
             "mixed_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stx.items()},
             "fp64_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st64.items()},
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "path": "omg_geometry_create + omg_gain_host (host buffers, mixed)"},
+                    "path": "omg_geometry_create + omg_gain_host (pinned host buffers, mixed; median of "
+                            f"{max(1, args.e2e_steps)} steps)"},
             "gpu_launches": int(launches),
             "kernels_ms_per_step": {k: round(v[1] / args.profile_steps, 3) for k, v in
                                     sorted(prof.items(), key=lambda kv: -kv[1][1])},
@@ -1024,7 +1034,7 @@ def main():
                     help="config2 / next: the head the rows run on (config0: a small profiling case)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--profile-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only-mixed", action="store_true",
                     help="profiling aid: run the mixed-precision steps only (no FP64 reference, e2e or CPU leg)")

@@ -394,10 +394,13 @@ class Solver:
 
 def forward_gain(geom: Geometry, dipoles, electrodes=None, squids=None, precision=FP64,
                  hm_integrator: Optional[Integrator] = None, dsm_integrator: Optional[Integrator] = None,
-                 host: bool = False):
+                 host: bool = False, out=None):
     """Adjoint gain pipeline (gain.h:78-136) in one call.  Returns
     (G_eeg or None, G_meg or None, stats dict).  host=True goes through the
-    host-buffer entry point (copies included)."""
+    host-buffer entry point (copies included); there `out` may give the two
+    C-contiguous float64 host arrays (n_dipoles x n_electrodes,
+    n_dipoles x n_squids) the gains are written to -- pinned memory makes the
+    device-to-host copies direct."""
     ctx = geom.ctx
     dip = np.ascontiguousarray(np.asarray(dipoles, np.float64)[:, :6]) if host else _as_dev(dipoles, ctx, 6)
     nd = dip.shape[0]
@@ -409,8 +412,15 @@ def forward_gain(geom: Geometry, dipoles, electrodes=None, squids=None, precisio
     if host:
         el = np.ascontiguousarray(np.asarray(electrodes, np.float64)[:, :3]) if ne else np.zeros((0, 3))
         sq = np.ascontiguousarray(np.asarray(squids, np.float64)[:, :6]) if nm else np.zeros((0, 6))
-        ge = np.zeros((nd, ne))   # column-major ne x nd
-        gm = np.zeros((nd, nm))
+        if out is not None:
+            ge, gm = out
+            for a, c in ((ge, ne), (gm, nm)):
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.shape == (nd, c)
+                        and a.flags.c_contiguous):
+                    raise ValueError("out: C-contiguous float64 arrays of shape (n_dipoles, n_sensors)")
+        else:
+            ge = np.empty((nd, ne))   # column-major ne x nd, every entry written by the library
+            gm = np.empty((nd, nm))
         P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         check(ctx.lib.omg_gain_host(ctx.handle, geom.handle, _prec(precision), ctypes.byref(hi), ctypes.byref(di),
                                     P(dip), nd, P(el), ne, P(sq), nm, P(ge), P(gm), ctypes.byref(st)))

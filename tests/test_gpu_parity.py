@@ -93,6 +93,15 @@ def test_host_entry_point_equals_device_entry_point(cuda):
     ge, gm, _ = api.forward_gain(geo, w.dipoles, w.electrodes, w.squids)
     he, hm, _ = api.forward_gain(geo, w.dipoles, w.electrodes, w.squids, host=True)
     assert np.array_equal(ge.cpu().numpy(), he) and np.array_equal(gm.cpu().numpy(), hm)
+    # caller-provided outputs in pinned host memory (the copies go straight to them)
+    import torch
+    nd, ne, nm = len(w.dipoles), len(w.electrodes), len(w.squids)
+    oe = torch.full((nd, ne), np.nan, dtype=torch.float64, pin_memory=True).numpy()
+    om = torch.full((nd, nm), np.nan, dtype=torch.float64, pin_memory=True).numpy()
+    pe, pm, _ = api.forward_gain(geo, w.dipoles, w.electrodes, w.squids, host=True, out=(oe, om))
+    assert np.array_equal(pe, he) and np.array_equal(pm, hm) and np.array_equal(oe.T, he)
+    with pytest.raises(ValueError):
+        api.forward_gain(geo, w.dipoles, w.electrodes, w.squids, host=True, out=(oe[:, :-1], om))
 
 
 @pytest.mark.parametrize("name", ["small_ico2_3l_pert", "config0"])
