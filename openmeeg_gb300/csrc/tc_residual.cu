@@ -317,10 +317,13 @@ __device__ __forceinline__ long long scaled_rn(double x, int k) {
     } else if (sh < -63) {
         q = 0;   // below 2^-11
     } else {
-        const int r = -sh;
-        const unsigned long long rem = m & ((1ull << r) - 1), half = 1ull << (r - 1);
-        q = m >> r;
-        if (rem > half || (rem == half && (q & 1))) ++q;
+        // t = m >> (r - 1) keeps the half bit as its lowest bit; the bits below it are the sticky part:
+        // round up when the half bit is set and (anything below it is set, or q is odd)
+        const int r1 = -sh - 1;
+        const unsigned long long t = m >> r1;
+        const unsigned long long sticky = (m & ((1ull << r1) - 1ull)) != 0ull ? 1ull : 0ull;
+        q = t >> 1;
+        q += t & (sticky | q) & 1ull;
     }
     return (b >> 63) ? -(long long)q : (long long)q;
 }
@@ -344,11 +347,15 @@ __device__ __forceinline__ unsigned short small_int_bf16(long long r) {
 // column's entries on and below the diagonal, rounded to FP32, to lower32.
 constexpr int DG_THREADS = 256;
 
+// ND_T / BETA_T > 0: the layout fixed at compile time (the digit shifts become immediates and the
+// digit loop unrolls); 0: taken from nd / beta at run time.
+template <int ND_T, int BETA_T>
 __global__ void __launch_bounds__(DG_THREADS) digits_kernel(const double* __restrict__ M, int64_t n, int64_t ncol,
-                                                            int64_t ldm, int nd, int beta, int64_t rows_per_plane,
+                                                            int64_t ldm, int nd_rt, int beta_rt, int64_t rows_per_plane,
                                                             int64_t ldo, __nv_bfloat16* out, int* ex,
                                                             const __grid_constant__ RowRanges rr, float* lower32,
                                                             int64_t ld32) {
+    const int nd = ND_T > 0 ? ND_T : nd_rt, beta = BETA_T > 0 ? BETA_T : beta_rt;
     __shared__ unsigned long long red[DG_THREADS / 32];
     __shared__ int s_e;
     const int64_t c = blockIdx.x;
@@ -405,19 +412,21 @@ __global__ void __launch_bounds__(DG_THREADS) digits_kernel(const double* __rest
             Z[u] = (j0 + u < n ? scaled_rn(x, k) : 0) + Bs;
             if (lower32 && j0 + u >= c && j0 + u < n) lower32[j0 + u + c * ld32] = (float)x;   // lower triangle
         }
-        for (int d = nd - 1; d >= 0; --d) {
+#pragma unroll
+        for (int d = (ND_T > 0 ? ND_T : nd) - 1; d >= 0; --d) {
             const int sh = beta * (nd - 1 - d);
-            unsigned int h[4];
+            unsigned int f[4];   // FP32 bits of the digits; their high halves are the bf16 values
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                if (d > 0) {   // bf16 of the digit: float(1.5 * 2^23 + digit) - 1.5 * 2^23, exact
+                if (d > 0) {   // float(1.5 * 2^23 + digit) - 1.5 * 2^23, exact
                     const unsigned field = (unsigned)(Z[u] >> sh) & mask;
-                    h[u] = __float_as_uint(__int_as_float(bf_off + (int)field) - 12582912.0f) >> 16;
+                    f[u] = __float_as_uint(__int_as_float(bf_off + (int)field) - 12582912.0f);
                 } else {
-                    h[u] = small_int_bf16(Z[u] >> sh);
+                    f[u] = (unsigned)small_int_bf16(Z[u] >> sh) << 16;
                 }
             }
-            o2[(((int64_t)d * rows_per_plane + c) * ldo + j0) / 4] = make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
+            o2[(((int64_t)d * rows_per_plane + c) * ldo + j0) / 4] =
+                make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
         }
     }
 }
@@ -452,9 +461,12 @@ void digits_columns(const double* M, int64_t n, int64_t ncol, int64_t ldm, int n
         }
         if (tot != n) throw Error(OMG_ERR_INVALID, "digits: row ranges do not add up");
     }
-    tcr::digits_kernel<<<(unsigned)rows_per_plane, tcr::DG_THREADS, 0, s>>>(M, n, ncol, ldm, nd, beta, rows_per_plane,
-                                                                           ldo, static_cast<__nv_bfloat16*>(out), ex,
-                                                                           rr, lower32, ld32);
+    if (nd == 6 && beta == 7)   // the library's layout
+        tcr::digits_kernel<6, 7><<<(unsigned)rows_per_plane, tcr::DG_THREADS, 0, s>>>(
+            M, n, ncol, ldm, nd, beta, rows_per_plane, ldo, static_cast<__nv_bfloat16*>(out), ex, rr, lower32, ld32);
+    else
+        tcr::digits_kernel<0, 0><<<(unsigned)rows_per_plane, tcr::DG_THREADS, 0, s>>>(
+            M, n, ncol, ldm, nd, beta, rows_per_plane, ldo, static_cast<__nv_bfloat16*>(out), ex, rr, lower32, ld32);
     check_tcr("digits");
 }
 

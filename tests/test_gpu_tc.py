@@ -230,17 +230,20 @@ def _digits_ref(col, nd, beta, ldo):
     return planes, e
 
 
-def test_digit_planes_bit_exact(cuda):
+@pytest.mark.parametrize("nd", [7, 6])
+def test_digit_planes_bit_exact(cuda, nd):
     """The digit planes and column exponents of the integer-arithmetic digit
     kernel equal the definition evaluated in exact integers: columns with zero,
     signed zeros, subnormals, exact ties of the rounding and entries over 600
-    binary orders; n not a multiple of 4; padding rows and columns zero."""
+    binary orders; n not a multiple of 4; padding rows and columns zero.  Six
+    digits of base 2^7 (the library's layout) take the kernel compiled for that
+    layout, seven the general one."""
     import torch
     f = _lib_hook("omg_internal_digits", [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                           ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
                                           ctypes.c_void_p, ctypes.c_void_p])
     rng = np.random.default_rng(5)
-    n, ncol, ldm, nd, beta = 301, 9, 305, 7, 7
+    n, ncol, ldm, beta = 301, 9, 305, 7
     ldo, rpp = 320, 12
     M = np.zeros((ncol, ldm))
     M[0, :n] = rng.standard_normal(n)
@@ -250,8 +253,9 @@ def test_digit_planes_bit_exact(cuda):
     M[3, :n] = rng.standard_normal(n) * 1e-310                      # subnormal column
     M[4, :n] = rng.standard_normal(n)
     M[4, 0] = 1.0
-    M[4, 1:20] = (np.arange(19) + 0.5) * np.exp2(-48)                 # exact ties of the digit grid
-    M[4, 20:40] = -(np.arange(20) + 0.5) * np.exp2(-48)
+    tie = np.exp2(-(nd * beta - 1))                                  # the digit grid's step (column max 1)
+    M[4, 1:20] = (np.arange(19) + 0.5) * tie                          # exact ties of the digit grid
+    M[4, 20:40] = -(np.arange(20) + 0.5) * tie
     M[5, :n] = -rng.random(n) * 3e8
     M[6, :n] = rng.standard_normal(n)
     M[6, 7] = -4.0                                                   # the largest magnitude negative
