@@ -13,7 +13,9 @@
 #include <array>
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 #include <fstream>
+#include <future>
 #include <map>
 #include <set>
 #include <sstream>
@@ -44,10 +46,8 @@ double mesh_solid_angle(const HostGeometry& g, int m, const double p[3]) {
         for (int i = 0; i < 3; ++i) d[i] = std::sqrt(r[i][0] * r[i][0] + r[i][1] * r[i][1] + r[i][2] * r[i][2]);
         double e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
         double nn[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-        double nrm = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
-        double area = 0.5 * nrm;
-        double dn = (r[0][0] * nn[0] + r[0][1] * nn[1] + r[0][2] * nn[2]) / nrm;
-        double dd = 2 * area * dn;
+        // twice the area times the signed height of p: r0 . (e1 x e2)
+        const double dd = r[0][0] * nn[0] + r[0][1] * nn[1] + r[0][2] * nn[2];
         auto dot = [&](int i, int j) { return r[i][0] * r[j][0] + r[i][1] * r[j][1] + r[i][2] * r[j][2]; };
         double den = d[0] * d[1] * d[2] + (d[0] * dot(1, 2) + d[1] * dot(2, 0) + d[2] * dot(0, 1));
         total += (std::fabs(dd) < 1e-10) ? 0.0 : 2 * std::atan2(dd, den);
@@ -109,18 +109,47 @@ void HostGeometry::finalize() {
     // distinct vertices: copies with equal coordinates are one unknown (Geometry::add_vertex,
     // geometry.h:100-108), numbered in order of first appearance
     {
-        std::map<std::array<double, 3>, int64_t> seen;
+        // an open-addressing table over the coordinates' bit patterns (-0.0 folded into +0.0, so equal
+        // coordinates hash equally; the coordinates are finite), probed linearly; each slot holds the first
+        // vertex with its coordinates: the numbering of an ordered map in linear time, without allocations
+        auto bits = [this](int64_t v, int c) {
+            const double x = V[3 * v + c] + 0.0;   // -0.0 + 0.0 = +0.0
+            uint64_t b;
+            std::memcpy(&b, &x, sizeof b);
+            return b;
+        };
+        size_t cap = 16;
+        while (cap < 2 * (size_t)nv) cap <<= 1;
+        std::vector<int64_t> slot(cap, -1);
         vglob.assign(nv, 0);
+        int64_t count = 0;
         for (int64_t v = 0; v < nv; ++v) {
-            auto it = seen.emplace(std::array<double, 3>{V[3 * v], V[3 * v + 1], V[3 * v + 2]}, (int64_t)seen.size());
-            vglob[v] = it.first->second;
+            uint64_t h = 0x9E3779B97F4A7C15ull;
+            for (int c = 0; c < 3; ++c) {
+                h ^= bits(v, c) + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+                h *= 0xBF58476D1CE4E5B9ull;
+            }
+            size_t i = (size_t)(h ^ (h >> 31)) & (cap - 1);
+            for (;; i = (i + 1) & (cap - 1)) {
+                const int64_t u = slot[i];
+                if (u < 0) {
+                    slot[i] = v;
+                    vglob[v] = count++;
+                    break;
+                }
+                if (V[3 * u] == V[3 * v] && V[3 * u + 1] == V[3 * v + 1] && V[3 * u + 2] == V[3 * v + 2]) {
+                    vglob[v] = vglob[u];
+                    break;
+                }
+            }
         }
-        nvg = (int64_t)seen.size();
+        nvg = count;
         shared = nvg < nv;
     }
     // Interface orientation (interface.cpp:55-95): the solid angle at the bounding-box centre of the
     // interface, summed over its oriented meshes, must be -4 pi or 0; +4 pi flips the interface.
-    for (size_t i = 0; i < ifaces.size(); ++i) {
+    // the interfaces' sums are independent: one thread each on large geometries (each sum in mesh order)
+    auto iface_angle = [this](size_t i) {
         double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
         for (const auto& om : ifaces[i])
             for (int64_t v = vbeg[om.first]; v < vbeg[om.first + 1]; ++v)
@@ -128,9 +157,22 @@ void HostGeometry::finalize() {
                     lo[k] = std::min(lo[k], V[3 * v + k]);
                     hi[k] = std::max(hi[k], V[3 * v + k]);
                 }
-        double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+        const double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
         double s = 0.0;
         for (const auto& om : ifaces[i]) s += om.second * mesh_solid_angle(*this, om.first, c);
+        return s;
+    };
+    std::vector<double> angle(ifaces.size(), 0.0);
+    if (ifaces.size() > 1 && nt >= 8192) {
+        std::vector<std::future<double>> fut;
+        for (size_t i = 1; i < ifaces.size(); ++i) fut.push_back(std::async(std::launch::async, iface_angle, i));
+        angle[0] = iface_angle(0);
+        for (size_t i = 1; i < ifaces.size(); ++i) angle[i] = fut[i - 1].get();
+    } else {
+        for (size_t i = 0; i < ifaces.size(); ++i) angle[i] = iface_angle(i);
+    }
+    for (size_t i = 0; i < ifaces.size(); ++i) {
+        double s = angle[i];
         if (almost_equal(s, 4 * M_PI)) {
             for (auto& om : ifaces[i]) om.second = -om.second;
             s = -s;
