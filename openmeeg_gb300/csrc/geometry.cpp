@@ -642,3 +642,32 @@ HostGeometry load_geometry_files(const std::string& geom, const std::string& con
 }
 
 }  // namespace omg
+
+// Test hook (not part of the public header; host only, no device needed): the
+// numbering a geometry loaded from .geom / .cond files gets.  sizes receives
+// {meshes, vertex copies, distinct vertices, triangles, unknowns N, triangle
+// unknowns}; when the capacities suffice, V (copies x 3), vglob (copy ->
+// distinct vertex), tidx (triangle -> unknown, reference order), orient and
+// barrier (per mesh) are filled too.  Returns 0, or -1 with nothing written
+// past sizes when the files are refused.
+extern "C" int omg_internal_geometry_numbering(const char* geom, const char* cond, int64_t* sizes, double* V,
+                                               int64_t* vglob, int64_t* tidx, int32_t* orient, int32_t* barrier,
+                                               int64_t cap_v, int64_t cap_t, int32_t cap_m) {
+    try {
+        const omg::HostGeometry h = omg::load_geometry_files(geom, cond);
+        const int64_t s[6] = {h.nmesh, h.nv, h.nvg, h.nt, h.N, h.nP};
+        for (int i = 0; i < 6; ++i) sizes[i] = s[i];
+        if (cap_v >= h.nv && cap_t >= h.nt && cap_m >= h.nmesh) {
+            for (int64_t i = 0; i < 3 * h.nv; ++i) V[i] = h.V[i];
+            for (int64_t i = 0; i < h.nv; ++i) vglob[i] = h.vglob[i];
+            for (int64_t i = 0; i < h.nt; ++i) tidx[i] = h.tidx[i];
+            for (int m = 0; m < h.nmesh; ++m) {
+                orient[m] = h.orient[m];
+                barrier[m] = h.barrier[m];
+            }
+        }
+        return 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
