@@ -631,8 +631,9 @@ static void factor_ldlt_tc(omg_solver sv, float* A, int64_t ld, int nb) {
     OMG_CUDA(cudaEventRecord(ev_l, s));   // the head matrix is ready
     OMG_CUDA(cudaStreamWaitEvent(sc, ev_l, 0));
     bool rest_pending = false;
-    const int reserve = 32;   // SMs the rest update leaves to the chain and the look-ahead (config1 factorization:
-                              // 32: 17.06-17.09 ms, 24: 17.15-17.20, 40: 17.31, 16: 17.76, 48: 17.90, 12: 18.21)
+    const int reserve = 24;   // SMs the rest update leaves to the chain and the look-ahead (config1 factorization:
+                              // 24: 17.15-17.20 ms, 32: 17.06-17.09 (within the run-to-run spread, the trailing
+                              // update on 8 fewer SMs), 40: 17.31, 16: 17.76, 48: 17.90, 12: 18.21)
     bool have_t = false;     // Th/Tl hold this panel's A21 split (written by the look-ahead update on s)
     bool wait_g = false;     // the group's second diagonal block waits for its look-ahead update (ev_g)
     bool g_recorded = false; // ev_g recorded in this call (a wait on an older record would cross a graph capture)
