@@ -243,6 +243,9 @@ NCU_TRAFFIC_PER_UNIT = {
     # launch: 14.01 GB + 157.5 MB), per byte of the 21 digit-plane reads the kernel structure implies
     # (21 x N x ld x 2 B = 13.54 GB)
     "residual_tc": (14.01e9 + 0.1575e9) / (21 * 17926 * 17984 * 2.0),   # 14.17 GB per launch; 1.05
+    # grouped fold of the diagonal-block inverses: DRAM bytes per algorithmic byte (ncu at config1:
+    # 2.72 GB read + 2.49 GB written for 2048 x 140 x 17926 B)
+    "fold": (2.72e9 + 2.49e9) / (2048.0 * 140 * 17926),
 }
 
 
@@ -412,6 +415,19 @@ def roofline_entry(name, launches, ms, steps, N, k, nd, stats, peaks_, pipes):
                      "note": "first-level integrand evaluations (80 points per dipole-triangle pair) per second; "
                              "the launch overlaps the solves on the second stream, so its event time includes "
                              "waiting for SMs"})
+    elif name == "fold":
+        # the folds of the diagonal-block inverses into the solve operators after the factorization, one grouped
+        # launch: every element of the panels below the blocks and of the block rows left of them (N - nk_b rows
+        # or columns of 128 per block b) is read and written as TF32 head + remainder, 16 bytes, so
+        # 2048 (nblocks - 1) N bytes in all; the inverses themselves (64 KB each) stay in L2
+        nblk = (N + 127) // 128
+        nbytes = 2048.0 * (nblk - 1) * N / per_step
+        achieved = nbytes / t_launch / 1e9
+        tr = NCU_TRAFFIC_PER_UNIT.get(name)
+        info.update({"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": tr * nbytes if tr else None, "algorithmic_bytes_per_launch": nbytes,
+                     "note": f"280 3xTF32 products at config1 in one persistent launch; HBM fraction of {kind} copy "
+                             f"bandwidth"})
     elif name in ("potrf_inv", "apply_inv"):
         info.update({"bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
                      "note": "one diagonal block per launch (128 x 128, one CTA), sequential over the blocks: "
@@ -597,7 +613,7 @@ def run_gpu(args):
     roof["dominant_rule"] = "largest profiled kernel on the main streams (DipSourceMat overlaps on the second one)"
     others = {n: roofline_entry(n, v[0], v[1], args.profile_steps, N, ne + nm, nd, stx_r, pk, pipes)
               for n, v in prof.items() if n in ("residual_tc", "residual_df64", "gemm_syrk", "ff_block", "near_pairs",
-                                                 "solve_sweep", "dsm")
+                                                 "solve_sweep", "dsm", "fold")
               and n != dname}
     e_s, e_d = assembly_evaluations(w.head)
     assembly = {"evaluations_per_headmat": {"E_S": e_s, "E_D": e_d},
